@@ -1,0 +1,79 @@
+"""Regenerate the golden fixtures in this folder from the reference's own files.
+
+Run in a checkout that has the reference source tree (default location given by
+``--reference``).  It reads files as text only; nothing of the reference is
+compiled or imported.  Outputs:
+
+* ``godunov_elastic.json``  -- Godunov-state matrices of ``tests/Model/Values.h``
+  (homogeneous and heterogeneous elastic cases) with the two materials.
+* ``global_matrices_pin.json`` -- for every matrix of
+  ``codegen/matrices/matrices_{20,35,56}.xml``: shape, non-zero count, sum,
+  Frobenius norm and a deterministic sample of entries.
+"""
+import argparse
+import json
+import os
+import re
+import xml.etree.ElementTree as ET
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def parse_values_h(path):
+    text = open(path).read()
+    out = {}
+    for name in ("SolutionHomogeneousLocal", "SolutionHomogeneousNeighbor",
+                 "SolutionHeterogeneousLocal", "SolutionHeterogeneousNeighbor"):
+        m = re.search(name + r"\s*=\s*\{(.*?)\};", text, re.S)
+        body = m.group(1)
+        rows = []
+        for row in re.findall(r"\{([^{}]*)\}", body):
+            vals = []
+            for tok in row.split(","):
+                tok = tok.strip()
+                if not tok:
+                    continue
+                vals.append(float(eval(tok, {"__builtins__": {}})))
+            rows.append(vals)
+        assert len(rows) == 9 and all(len(r) == 9 for r in rows), name
+        out[name] = rows
+    m = re.search(r"struct SolutionData<model::ElasticMaterial>.*?MaterialVal1\{([^}]*)\}.*?MaterialVal2\{([^}]*)\}", text, re.S)
+    out["MaterialVal1"] = [float(x) for x in m.group(1).split(",")]
+    out["MaterialVal2"] = [float(x) for x in m.group(2).split(",")]
+    out["_layout"] = "golden[j][i] == QgodView(i, j); materials are (rho, mu, lambda)"
+    return out
+
+
+def parse_xml(path):
+    root = ET.parse(path).getroot()
+    res = {}
+    for m in root:
+        rows, cols = int(m.get("rows")), int(m.get("columns"))
+        ent = [(int(e.get("row")) - 1, int(e.get("column")) - 1, float(e.get("value"))) for e in m]
+        ent.sort()
+        nz = [e for e in ent if e[2] != 0.0]
+        step = max(1, len(nz) // 24)
+        res[m.get("name")] = {
+            "shape": [rows, cols],
+            "nnz": len(nz),
+            "sum": sum(e[2] for e in nz),
+            "fro": sum(e[2] ** 2 for e in nz) ** 0.5,
+            "sample": [[r, c, v] for (r, c, v) in nz[::step]],
+        }
+    return res
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    a = ap.parse_args()
+    g = parse_values_h(os.path.join(a.reference, "tests/Model/Values.h"))
+    json.dump(g, open(os.path.join(HERE, "godunov_elastic.json"), "w"), indent=1)
+    pin = {}
+    for b in (20, 35, 56):
+        pin[str(b)] = parse_xml(os.path.join(a.reference, f"codegen/matrices/matrices_{b}.xml"))
+    json.dump(pin, open(os.path.join(HERE, "global_matrices_pin.json"), "w"))
+
+
+if __name__ == "__main__":
+    main()
