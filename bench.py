@@ -1,0 +1,335 @@
+"""Benchmark of the ADER-DG element update (ADER + local + neighbour) on one GB300.
+
+Workload (the configuration the metric is quoted on): elastic, convergence order 6
+(56 basis functions x 9 quantities), 400,000 tetrahedra = 40 x 40 x 50 cubes of 5 tets,
+periodic, cube edge 100 m, rho/vp/vs = 2700/6000/3464 each perturbed +-10% per cell
+(seeded), DOFs seeded U[-1, 1], CFL time step (cfl 0.5).  Synthetic data throughout.
+
+A bench "step" is one global time step of proxy kernel 'all' over all cells.
+  value : cell-updates/s with DOFs resident in HBM, device time (CUDA events on the
+          library's stream) over exactly K steps, max over ranks.
+  e2e   : the same metric through the public C ABI with host buffers: every step is
+          sei_run_host(all, 1 step) = pinned-host -> device copy of the DOFs, the step,
+          device -> host copy of the result.
+The DOF, time-integrated DOF and operator arrays (about 3 GB) exceed L2 (129 MB), so no
+L2 flush is needed between steps.
+
+--impl reference times the oracle port of the reference's CPU path (FP64 C, all host
+threads) on a bounded sample of the same workload (a smaller periodic cube of the same
+shape parameters), one time step per bench step.
+
+Multiple GPUs (torchrun): the path does not shard; each rank runs an independent replica
+and value = total cell updates of all ranks / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ADER-DG cell-updates/s on 1 GB300: mixed-prec vs plain FP32 at stated L2 err"
+UNIT = "cell-updates/s"
+ORDER = 6
+DIMS = (40, 40, 50)
+PERTURB = 0.1
+SEED = 2024
+CPU_SAMPLE_DIMS = (8, 8, 10)
+FALLBACK_HBM_GBS = 6800.0
+
+
+def bytes_per_cell(order, kernel):
+    """Algorithmic HBM bytes per cell and launch (float32, each array touched once)."""
+    b = order * (order + 1) * (order + 2) // 6
+    dof = 4 * 9 * ((b + 3) // 4 * 4)
+    if kernel == "local":  # read Q, write Q, write I, star non-zeros, A+ x4, face types
+        return 3 * dof + 4 * 72 + 4 * 324 + 4
+    if kernel == "neighbor":  # read Q, write Q, read neighbour I (once per cell), A- x4, relations
+        return 3 * dof + 4 * 324 + 16 + 4 + 4
+    if kernel == "model":  # compulsory traffic of one fused cell update (reference data model)
+        return 4 * dof + 4 * 72 + 4 * 324 + 4 * 324 + 16 + 4
+    raise ValueError(kernel)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample():
+    """The CPU sample of the workload, set up entirely by the oracle (no product code)."""
+    import numpy as np
+
+    from oracle import cube_mesh, dg_setup
+
+    topo, coords = cube_mesh.periodic_cube(*CPU_SAMPLE_DIMS)
+    n = topo.shape[0]
+    rng = np.random.default_rng(SEED)
+    f = rng.uniform(1 - PERTURB, 1 + PERTURB, (n, 3))
+    rho, vp, vs = 2700.0 * f[:, 0], 6000.0 * f[:, 1], 3464.0 * f[:, 2]
+    mu = rho * vs * vs
+    mat = np.stack([rho, mu, rho * vp * vp - 2 * mu], axis=1)
+    nb, side, orient = dg_setup.face_relations(topo)
+    ops = dg_setup.cell_operators(coords, mat, nb)
+    dt = dg_setup.cfl_timestep(coords, vp, ORDER, 0.5).min()
+    q = rng.uniform(-1, 1, (n, 9, dg_setup.nbasis3(ORDER)))
+    args = (ops["star"], ops["AplusT"], ops["AminusT"], nb, side, orient)
+    return n, q, args, dt, np.zeros((n, 4), np.int8)
+
+
+def cpu_baseline(k_steps=None, budget_s=12.0, sample=None):
+    """Oracle port (FP64 C, OpenMP on all host threads) on a bounded sample of the workload."""
+    from oracle import oracle_py
+
+    n, q, args, dt, ft = sample or cpu_sample()
+    o = oracle_py.Oracle(ORDER)
+    t0 = time.perf_counter()
+    q = o.steps(q, *args, dt, 1, ft)
+    one = time.perf_counter() - t0
+    steps = k_steps if k_steps else max(1, min(200, int(budget_s / max(one, 1e-3))))
+    t0 = time.perf_counter()
+    q = o.steps(q, *args, dt, steps, ft)
+    el = time.perf_counter() - t0
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": n * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"order {ORDER} elastic, {n} tets ({CPU_SAMPLE_DIMS[0]}x{CPU_SAMPLE_DIMS[1]}x{CPU_SAMPLE_DIMS[2]} "
+                      f"cubes, same material/seed distribution), {steps} steps of kernel 'all', FP64",
+            "seconds": el, "steps": steps, "cells": n}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier_max(world, value):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    from oracle import oracle_py
+    sample = cpu_sample()
+    base = cpu_baseline(k_steps=1, sample=sample)
+    # warm-up and K timed steps, each one time step of the sample
+    n, q, a, dt, ft = sample
+    o = oracle_py.Oracle(ORDER)
+    for _ in range(args.warmup):
+        q = o.steps(q, *a, dt, 1, ft)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        q = o.steps(q, *a, dt, 1, ft)
+    el = time.perf_counter() - t0
+    value = n * args.steps / el
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": f"elastic order {ORDER}, bounded sample of {n} tets of the 400,000-tet periodic cube "
+                                   "(same material and DOF distributions), kernel all", "cells": n, "order": ORDER},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": base["cores"], "kind": "port",
+                             "sample": base["sample"].replace("1 steps", f"{args.steps} timed steps (one per bench step)")},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    from seissol_gb300 import Context
+
+    hbm, peak_kind = peaks()
+    ctx = Context(ORDER, device=local)
+    n = ctx.build_periodic_cube(*DIMS, perturb=PERTURB, seed=SEED + rank)
+    dt = ctx.cfl_timestep(0.5)
+    ctx.run("all", dt, args.warmup)
+    ctx.sync()
+    torch.cuda.synchronize(local)
+    barrier(world)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize(local)
+        barrier(world)
+        ctx.run("all", dt, args.steps)
+        ctx.sync()
+        torch.cuda.synchronize(local)
+        ms = ctx.last_run_ms()
+        barrier(world)
+    ms = barrier_max(world, ms)
+    value = world * n * args.steps / (ms / 1e3)
+    clocks = clk.summary()
+
+    # per-launch durations of the two kernels inside a profiled run of the same workload
+    ctx.set_profiling(True)
+    ctx.run("all", dt, args.steps)
+    ctx.sync()
+    loc_ms, nb_ms, launches = ctx.kernel_times_ms()
+    ctx.set_profiling(False)
+    kernels = {"local": loc_ms / args.steps, "neighbor": nb_ms / args.steps}
+    dom = max(kernels, key=kernels.get)
+    algo = bytes_per_cell(ORDER, dom) * n
+    achieved = algo / (kernels[dom] / 1e3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "dram_traffic_per_cell.txt")
+    if os.path.exists(tf):
+        for line in open(tf):
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == f"sei_{dom}_o{ORDER}":
+                traffic = float(parts[1]) * n
+    roof = {"bound": "hbm", "kernel": f"sei_{dom}_o{ORDER}", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "peak_source": f"{peak_kind} hbm_gbs", "traffic": traffic,
+            "algorithmic_bytes_per_launch": algo, "launch_ms": kernels[dom],
+            "step_model_frac": value / world * bytes_per_cell(ORDER, "model") / (hbm * 1e9)}
+    try:
+        from seissol_gb300.codegen.gen_kernels import nnz_flops
+        f = nnz_flops(ORDER)
+        flop_cell = f["ader"] + f["local"] + f["neighbor"]
+        roof["nonzero_tflops"] = value / world * flop_cell / 1e12
+    except Exception:
+        pass
+
+    # end to end through the C ABI with pinned host buffers, one step per call
+    e2e = None
+    if args.e2e_steps > 0:
+        B = 56
+        hin = torch.empty((n, 9, B), dtype=torch.float32, pin_memory=True)
+        hout = torch.empty((n, 9, B), dtype=torch.float32, pin_memory=True)
+        hin.copy_(torch.from_numpy(ctx.get_dofs()))
+        import ctypes
+        pin, pout = ctypes.c_void_p(hin.data_ptr()), ctypes.c_void_p(hout.data_ptr())
+        for _ in range(2):
+            ctx._check(ctx.lib.sei_run_host(ctx.h, 0, dt, 1, pin, pout), "sei_run_host")
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            ctx._check(ctx.lib.sei_run_host(ctx.h, 0, dt, 1, pin, pout), "sei_run_host")
+            hin, hout = hout, hin
+            pin, pout = pout, pin
+        el = barrier_max(world, time.perf_counter() - t0)
+        nbytes = n * 9 * B * 4
+        e2e = {"value": world * n * args.e2e_steps / el, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": nbytes, "steps": args.e2e_steps,
+               "call": "sei_run_host(SEI_KERNEL_ALL, dt, 1, dofs_in, dofs_out) with pinned host DOFs"}
+    ctx.close()
+
+    base = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        base = cpu_baseline()
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "elastic order 6 (56x9), 400,000-tet periodic cube 40x40x50 cubes x 5 tets, "
+                                       "material +-10% per cell, kernel all (ADER+local+neighbour), GTS, CFL 0.5",
+                           "cells_per_gpu": n, "order": ORDER, "precision": "FP32 CUDA cores (sparse, non-zero flops)",
+                           "l2": "inputs larger than L2 (~3 GB resident per GPU), no flush",
+                           "parallelism": f"replicas x{world}"},
+                "roofline": roof, "cpu_baseline": base, "e2e": e2e, "clocks": clocks,
+                "gpu_launches": 2 * args.steps, "kernel_ms_per_step": kernels}
+        print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+    return run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,141 @@
+/*
+ * sei_gb300 — C ABI of the GB300 ADER-DG element update.
+ *
+ * One context owns one CUDA device's data for one mesh: DOFs, time-integrated DOFs,
+ * per-cell operators and neighbour relations, all resident in HBM.  Host arrays passed
+ * in are copied and never retained; arrays passed out are owned by the caller.
+ * Every function returns SEI_OK (0) or a negative SEI_ERR_* code and never aborts;
+ * sei_last_error() describes the last failure.  A context is not thread-safe: use one
+ * per host thread.  All device work runs on the context's own CUDA stream.
+ *
+ * Layouts (the reference's yateto column-major convention):
+ *   DOF tensors   [ncells][9][B]   basis index fastest, B = order(order+1)(order+2)/6
+ *   9x9 operators column-major, element (q, p) at q + 9 p
+ *   star          [ncells][3][81]  (src/Initializer/Typedefs.h:187-196 starMatrices)
+ *   aplus/aminus  [ncells][4][81]  (nApNm1 / nAmNm1, src/Initializer/Typedefs.h:187-205)
+ *   neighbor      [ncells][4] int32 cell id or -1, side/orient [ncells][4] int8
+ *                 (CellLocalInformation::faceRelations, src/Initializer/Typedefs.h:221-233)
+ *   face_type     [ncells][4] int8: 0 regular, 1 dynamic rupture, 2 none (boundary)
+ */
+#ifndef SEI_GB300_H_
+#define SEI_GB300_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SEI_OK 0
+#define SEI_ERR_ARG (-1)
+#define SEI_ERR_OOM (-2)
+#define SEI_ERR_CUDA (-3)
+#define SEI_ERR_TIMEOUT (-4)
+#define SEI_ERR_NAN (-5)
+#define SEI_ERR_STATE (-6)
+#define SEI_ERR_UNSUPPORTED (-7)
+
+/* Proxy kernels (src/Proxy/Common.h:18, names in src/Proxy/Common.cpp:22-40). */
+#define SEI_KERNEL_ALL 0
+#define SEI_KERNEL_LOCAL 1
+#define SEI_KERNEL_NEIGHBOR 2
+#define SEI_KERNEL_ADER 3
+#define SEI_KERNEL_LOCAL_WO_ADER 4
+#define SEI_KERNEL_NEIGHBOR_DR 5
+#define SEI_KERNEL_GODUNOV_DR 6
+#define SEI_KERNEL_ALL_DR 7
+
+/* Arithmetic of the global-matrix contractions. */
+#define SEI_PREC_FP32 0 /* CUDA-core FP32, sparse (non-zero flops only) */
+
+typedef struct sei_ctx sei_ctx;
+
+typedef struct sei_config {
+  int order;     /* convergence order: 4, 5 or 6 */
+  int device;    /* CUDA device ordinal */
+  int precision; /* SEI_PREC_* */
+  int store_derivatives; /* keep the CK derivatives of every cell (needed by dynamic rupture) */
+} sei_config;
+
+/* Synthetic periodic cube: nx*ny*nz cubes of edge h, 5 tetrahedra each (even counts >= 4).
+ * Material rho, vp, vs, each multiplied per cell by U[1-perturb, 1+perturb] (seeded). */
+typedef struct sei_cube_params {
+  int nx, ny, nz;
+  double h;
+  double rho, vp, vs;
+  double perturb;
+  uint64_t seed;
+} sei_cube_params;
+
+/* PerformanceEstimate of the reference (src/Monitoring/Metric.h:8-60), per cell and step. */
+typedef struct sei_perf {
+  double nonzero_flop;  /* executed non-zero flops */
+  double hardware_flop; /* flops issued by the kernels */
+  double bytes;         /* algorithmic HBM bytes (compulsory traffic) */
+} sei_perf;
+
+int sei_version(void);
+
+/* Replaces setGlobalData + storage allocation (src/Kernels/Kernel.h:18, src/Proxy/Allocator.cpp:137-144).
+ * cfg->device < 0 makes a host-only context: mesh/operator set-up and the sei_get_* copies of it,
+ * no CUDA calls (used to check the set-up on machines without a GPU). */
+int sei_create(const sei_config* cfg, sei_ctx** out);
+void sei_destroy(sei_ctx* ctx);
+const char* sei_last_error(const sei_ctx* ctx);
+
+/* Builds the synthetic periodic cube on the host (geometry, face relations, materials,
+ * star matrices and flux solvers as src/Initializer/Model/CellLocalMatrices.cpp:66-296),
+ * uploads it and seeds the DOFs U[-1, 1].  Returns the cell count. */
+int sei_build_periodic_cube(sei_ctx* ctx, const sei_cube_params* p, int64_t* ncells);
+
+/* Generic mesh upload (drop-in for the LTS storage of one layer). */
+int sei_set_cells(sei_ctx* ctx, int64_t ncells, const float* star, const float* aplus, const float* aminus,
+                  const int32_t* neighbor, const int8_t* side, const int8_t* orient, const int8_t* face_type);
+int64_t sei_num_cells(const sei_ctx* ctx);
+
+/* Host copies of what sei_build_periodic_cube made (for checking against independent set-ups). */
+int sei_get_cells(sei_ctx* ctx, float* star, float* aplus, float* aminus, int32_t* neighbor, int8_t* side,
+                  int8_t* orient, int8_t* face_type);
+int sei_get_geometry(sei_ctx* ctx, double* vertices /*[n][4][3]*/, double* material /*[n][3] rho, mu, lambda*/,
+                     int64_t* topology /*[n][4] vertex ids*/);
+/* Smallest CFL time step of the mesh (src/Initializer/TimeStepping/GlobalTimestep.cpp:27-47). */
+int sei_cfl_timestep(sei_ctx* ctx, double cfl, double* dt);
+
+int sei_set_dofs(sei_ctx* ctx, const float* dofs);
+int sei_get_dofs(sei_ctx* ctx, float* dofs);
+int sei_get_time_integrated(sei_ctx* ctx, float* tint);
+int sei_get_derivatives(sei_ctx* ctx, float* derivs);
+int sei_derivatives_size(int order);
+
+/* Spacetime::computeBatchedAder (src/Kernels/LinearCK/Time.cpp:142-217) for all cells,
+ * coeffs = MonomialBasis::integrate(0, dt) (src/Numerical/TimeBasis.h:82-93). */
+int sei_compute_ader(sei_ctx* ctx, double dt);
+/* Local::computeBatchedIntegral (src/Kernels/LinearCK/Local.cpp:255-395): volume + local flux. */
+int sei_compute_local_integral(sei_ctx* ctx);
+/* ADER followed by the local integral in one launch (src/Proxy/KernelHost.cpp:108-131). */
+int sei_compute_ader_local(sei_ctx* ctx, double dt);
+/* Neighbor::computeBatchedNeighborsIntegral (src/Kernels/LinearCK/Neighbor.cpp:111-188). */
+int sei_compute_neighbors_integral(sei_ctx* ctx);
+/* Time::evaluateBatched (src/Kernels/LinearCK/Time.cpp:256-292) of the stored derivatives. */
+int sei_evaluate_taylor(sei_ctx* ctx, const double* coeffs, float* out_device);
+
+/* Runs a proxy kernel for nsteps steps (src/Proxy/Runner.cpp:99-111); asynchronous. */
+int sei_run(sei_ctx* ctx, int kernel, double dt, int nsteps);
+/* Same with host buffers: copies dofs_in to the device, runs, copies the result to dofs_out. */
+int sei_run_host(sei_ctx* ctx, int kernel, double dt, int nsteps, const float* dofs_in, float* dofs_out);
+int sei_sync(sei_ctx* ctx);
+/* Device-side duration of the last sei_run, milliseconds (CUDA events on the context stream). */
+int sei_last_run_ms(sei_ctx* ctx, double* ms);
+
+/* Per-launch device timing: when on, every kernel launch of sei_run is bracketed by CUDA events on the
+ * context stream; sei_kernel_times_ms sums the durations of the last sei_run per kernel kind. */
+int sei_set_profiling(sei_ctx* ctx, int on);
+int sei_kernel_times_ms(sei_ctx* ctx, double* local_ms, double* neighbor_ms, int* launches);
+
+/* Per-cell, per-step estimate of a proxy kernel (Local.cpp:462-522, Neighbor.cpp:190-228). */
+int sei_metrics(const sei_ctx* ctx, int kernel, sei_perf* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SEI_GB300_H_ */

@@ -31,7 +31,8 @@ def _tets(parity):
 
 def periodic_cube(nx, ny, nz, h=100.0):
     """Returns (topology [n,4] int64 vertex ids, coords [n,4,3] float64 unwrapped)."""
-    assert nx % 2 == 0 and ny % 2 == 0 and nz % 2 == 0
+    # even counts keep the alternating split conforming; >= 4 keeps periodic faces distinct
+    assert min(nx, ny, nz) >= 4 and nx % 2 == 0 and ny % 2 == 0 and nz % 2 == 0
     cubes = [(i, j, k) for k in range(nz) for j in range(ny) for i in range(nx)]
     topo, coords = [], []
     for parity in (0, 1):

@@ -1,0 +1,327 @@
+"""Generator of the FP32 CUDA-core kernels of the ADER-DG element update.
+
+For each convergence order it writes one header with two kernels:
+
+* ``sei_local_o{N}``    Cauchy-Kovalevskaya predictor (codegen/kernels/aderdg.py:463-537),
+                        volume integral (:337-351) and local flux (:373-386);
+* ``sei_neighbor_o{N}`` neighbour flux rDivM_i fP_h rT_j I_nb AminusT_i (:414-428);
+
+plus ``sei_taylor_o{N}`` (derivativeTaylorExpansion, :531-536) for derivative
+evaluation.  The global matrices enter the code as literals: every non-zero becomes
+one FFMA with an immediate operand, zero entries produce no instruction, so each
+kernel executes exactly the non-zero flops of the reference's sparse kernels.
+
+Thread mapping: a CTA holds 32 cells and 9 warps; warp q owns quantity column q of
+those 32 cells (lane = cell).  Products with a global matrix act on one column and
+are thread-local; the per-cell 9x9 operators (star, A+, A-) mix columns and exchange
+data through shared memory laid out [q][row][lane] (conflict-free).
+"""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+from .basis import global_matrices, nb2, nb3
+
+NQ = 9
+CPB = 32  # cells per block
+
+# Non-zero pattern of the elastic star matrix (codegen/matrices/star.xml): for output
+# column p, the source rows q.  The 24 non-zeros are stored per cell in this order
+# (column-major over (q, p)).
+STAR_NZ = [(6, 0), (7, 0), (8, 0), (6, 1), (7, 1), (8, 1), (6, 2), (7, 2), (8, 2), (6, 3), (7, 3), (7, 4), (8, 4),
+           (6, 5), (8, 5), (0, 6), (3, 6), (5, 6), (1, 7), (3, 7), (4, 7), (2, 8), (4, 8), (5, 8)]
+
+
+def star_sources():
+    src, idx = [], []
+    for p in range(NQ):
+        ent = [(q, i) for i, (q, pp) in enumerate(STAR_NZ) if pp == p]
+        while len(ent) < 3:
+            ent.append((ent[0][0], -1))
+        src.append([e[0] for e in ent])
+        idx.append([e[1] for e in ent])
+    return src, idx
+
+
+def flit(v: float) -> str:
+    """Exact float32 literal (hexadecimal)."""
+    return float(np.float32(v)).hex() + "f"
+
+
+def padded(b: int) -> int:
+    """Column stride of DOF tensors: basis count rounded up to 4 floats (16 bytes)."""
+    return (b + 3) // 4 * 4
+
+
+def _cols(mat, rows=None, cols=None):
+    """Non-zeros grouped by column: {l: [(k, val), ...]}, float32-rounded, zero-skipped."""
+    r = mat.shape[0] if rows is None else rows
+    c = mat.shape[1] if cols is None else cols
+    out = {}
+    for l in range(c):
+        ent = [(k, float(mat[k, l])) for k in range(r) if mat[k, l] != 0.0 and np.float32(mat[k, l]) != 0]
+        if ent:
+            out[l] = ent
+    return out
+
+
+def _matvec(lines, ind, mat, src, dst, rows, cols, init_zero):
+    """dst[k] (+)= sum_l mat[k, l] * src[l] (thread-local, column form)."""
+    bycol = _cols(mat, rows, cols)
+    touched = set()
+    if init_zero:
+        for k in range(rows):
+            lines.append(f"{ind}{dst}[{k}] = 0.f;")
+    for l in sorted(bycol):
+        for k, v in bycol[l]:
+            lines.append(f"{ind}{dst}[{k}] = fmaf({flit(v)}, {src}[{l}], {dst}[{k}]);")
+            touched.add(k)
+    return touched
+
+
+def gen_order(order: int) -> str:
+    B, F = nb3(order), nb2(order)
+    G = global_matrices(order)
+    src, idx = star_sources()
+    L = []
+    a = L.append
+    a(f"// Generated by seissol_gb300/codegen/gen_kernels.py for convergence order {order} (B={B}, F={F}).")
+    a("// Do not edit.")
+    a("#pragma once")
+    a(f"namespace sei_o{order} {{")
+    a(f"constexpr int kOrder = {order}, kB = {B}, kBp = {padded(B)}, kF = {F}, kQ = 9, kCPB = {CPB};")
+    a(f"constexpr int kDerivSize = {sum(nb3(order - i) for i in range(order)) * NQ};")
+    a("__constant__ int c_src[9][3] = {" + ",".join("{" + ",".join(map(str, s)) + "}" for s in src) + "};")
+    a("__constant__ int c_nzi[9][3] = {" + ",".join("{" + ",".join(map(str, s)) + "}" for s in idx) + "};")
+
+    # ---------------- local kernel ----------------
+    a(f"""
+// Q[n][9][B] in/out (in place), I[n][9][B] out, star_nz[n][3][24], aplus[n][4][81] (column-major 9x9),
+// ftype[n][4] (1 = dynamic rupture: no local flux), coeffs[order] Taylor integration coefficients,
+// derivs: optional packed derivative output [n][kDerivSize] (nullptr to skip).
+extern "C" __global__ void __launch_bounds__(288, 1)
+sei_local_o{order}(int n, float* __restrict__ Q, float* __restrict__ Iout, const float* __restrict__ star_nz,
+                   const float* __restrict__ aplus, const unsigned char* __restrict__ ftype,
+                   SeiCoeffs coeffs, float* __restrict__ derivs) {{
+  extern __shared__ float sm[];
+  const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int cell = blockIdx.x * kCPB + lane;
+  const bool valid = cell < n;
+  const int cl = valid ? cell : n - 1;
+  float* X = sm;  // [9][kB][32]
+  const int s0 = c_src[q][0], s1 = c_src[q][1], s2 = c_src[q][2];
+  const float* Xs0 = X + s0 * kB * 32 + lane;
+  const float* Xs1 = X + s1 * kB * 32 + lane;
+  const float* Xs2 = X + s2 * kB * 32 + lane;
+  float* Xq = X + q * kB * 32 + lane;
+  float st[3][3];
+#pragma unroll
+  for (int e = 0; e < 3; ++e)
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {{
+      const int i = c_nzi[q][s];
+      st[e][s] = i >= 0 ? __ldg(star_nz + (size_t)cl * 72 + e * 24 + i) : 0.f;
+    }}
+  const float* qcol = Q + ((size_t)cl * 9 + q) * kBp;
+  float z[kBp];
+  sei_load_col<kBp>(qcol, z);
+  float I[kBp];
+#pragma unroll
+  for (int k = 0; k < kBp; ++k) I[k] = coeffs.c[0] * z[k];
+  float* dcol = derivs ? derivs + (size_t)cl * kDerivSize + q * kB : nullptr;
+  if (dcol && valid) sei_store_col_scalar<kB>(dcol, z);""")
+    off = B * NQ
+    for i in range(1, order):
+        bp, bc = nb3(order - i + 1), nb3(order - i)
+        a(f"  // ---- CK stage {i}: rows {bc} from {bp}")
+        a("  {")
+        a(f"#pragma unroll\n    for (int k = 0; k < {bp}; ++k) Xq[k * 32] = z[k];")
+        a("    __syncthreads();")
+        a(f"    float zn[{bc}];")
+        a(f"#pragma unroll\n    for (int k = 0; k < {bc}; ++k) zn[k] = 0.f;")
+        cols = [_cols(G["kDivMT"][e], bc, bp) for e in range(3)]
+        for l in range(bp):
+            if not any(l in c for c in cols):
+                continue
+            a(f"    {{ const float x0 = Xs0[{l * 32}], x1 = Xs1[{l * 32}], x2 = Xs2[{l * 32}];")
+            for e in range(3):
+                if l in cols[e]:
+                    a(f"      const float y{e} = st[{e}][0] * x0 + st[{e}][1] * x1 + st[{e}][2] * x2;")
+            for e in range(3):
+                for k, v in cols[e].get(l, []):
+                    a(f"      zn[{k}] = fmaf({flit(v)}, y{e}, zn[{k}]);")
+            a("    }")
+        a("    __syncthreads();")
+        a(f"#pragma unroll\n    for (int k = 0; k < {bc}; ++k) {{ I[k] = fmaf(coeffs.c[{i}], zn[k], I[k]); z[k] = zn[k]; }}")
+        a(f"    if (dcol && valid) sei_store_col_scalar<{bc}>(derivs + (size_t)cl * kDerivSize + {off} + q * {bc}, zn);")
+        off += bc * NQ
+        a("  }")
+    # volume
+    a("  // ---- volume: Q += sum_e kDivM_e (I star_e)")
+    a(f"#pragma unroll\n  for (int k = 0; k < kB; ++k) Xq[k * 32] = I[k];")
+    a("  __syncthreads();")
+    a("  float acc[kBp];")
+    a("  sei_load_col<kBp>(qcol, acc);")
+    cols = [_cols(G["kDivM"][e]) for e in range(3)]
+    for l in range(B):
+        if not any(l in c for c in cols):
+            continue
+        a(f"  {{ const float x0 = Xs0[{l * 32}], x1 = Xs1[{l * 32}], x2 = Xs2[{l * 32}];")
+        for e in range(3):
+            if l in cols[e]:
+                a(f"    const float y{e} = st[{e}][0] * x0 + st[{e}][1] * x1 + st[{e}][2] * x2;")
+        for e in range(3):
+            for k, v in cols[e].get(l, []):
+                a(f"    acc[{k}] = fmaf({flit(v)}, y{e}, acc[{k}]);")
+        a("  }")
+    a("  __syncthreads();")
+    # local flux
+    for f in range(4):
+        a(f"  // ---- local flux, face {f}: Q += rDivM_{f} ((fMrT_{f} I) AplusT_{f})")
+        a("  {")
+        a("    float T[kF];")
+        _matvec(L, "    ", G["fMrT"][f], "I", "T", F, B, True)
+        a(f"#pragma unroll\n    for (int m = 0; m < kF; ++m) Xq[m * 32] = T[m];")
+        a("    __syncthreads();")
+        a(f"    const bool on = valid && ftype[(size_t)cl * 4 + {f}] != 1;")
+        a(f"    const float* ap = aplus + ((size_t)cl * 4 + {f}) * 81 + 9 * q;")
+        a("    float av[9];")
+        a("#pragma unroll\n    for (int s = 0; s < 9; ++s) av[s] = on ? __ldg(ap + s) : 0.f;")
+        bycol = _cols(G["rDivM"][f])
+        for m in range(F):
+            if m not in bycol:
+                continue
+            a(f"    {{ float g = 0.f;")
+            a(f"#pragma unroll\n      for (int s = 0; s < 9; ++s) g = fmaf(X[(s * kB + {m}) * 32 + lane], av[s], g);")
+            for k, v in bycol[m]:
+                a(f"      acc[{k}] = fmaf({flit(v)}, g, acc[{k}]);")
+            a("    }")
+        a("    __syncthreads();")
+        a("  }")
+    a("  if (valid) {")
+    a("    sei_store_col<kBp>(Q + ((size_t)cell * 9 + q) * kBp, acc);")
+    a("    sei_store_col<kBp>(Iout + ((size_t)cell * 9 + q) * kBp, I);")
+    a("  }")
+    a("}")
+
+    # ---------------- neighbour kernel ----------------
+    a(f"""
+// Q[n][9][B] updated in place with the neighbour flux of all regular faces.
+// I[n][9][B] time-integrated DOFs of all cells, aminus[n][4][81], nbr[n][4], rel[n][4] = side | orient << 2,
+// ftype[n][4] (0 = regular face).
+extern "C" __global__ void __launch_bounds__(288, 1)
+sei_neighbor_o{order}(int n, float* __restrict__ Q, const float* __restrict__ I, const float* __restrict__ aminus,
+                      const int* __restrict__ nbr, const unsigned char* __restrict__ rel,
+                      const unsigned char* __restrict__ ftype) {{
+  extern __shared__ float sm[];
+  const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int cell = blockIdx.x * kCPB + lane;
+  const bool valid = cell < n;
+  const int cl = valid ? cell : n - 1;
+  float* X = sm;  // [9][kF][32]
+  float* Xq = X + q * kF * 32 + lane;
+  float acc[kBp];
+  sei_load_col<kBp>(Q + ((size_t)cl * 9 + q) * kBp, acc);
+#pragma unroll 1
+  for (int f = 0; f < 4; ++f) {{
+    const int nb = __ldg(nbr + (size_t)cl * 4 + f);
+    const int r = rel[(size_t)cl * 4 + f];
+    const bool on = valid && nb >= 0 && ftype[(size_t)cl * 4 + f] == 0;
+    const int src = on ? nb : cl;
+    float x[kBp];
+    sei_load_col<kBp>(I + ((size_t)src * 9 + q) * kBp, x);
+    float R[kF];
+    switch (r & 3) {{""")
+    for j in range(4):
+        a(f"      case {j}: {{")
+        _matvec(L, "        ", G["rT"][j], "x", "R", F, B, True)
+        a("        break; }")
+    a("    }")
+    a("    float S[kF];")
+    a("    switch (r >> 2) {")
+    for h in range(3):
+        a(f"      {'default' if h == 2 else 'case ' + str(h)}: {{")
+        _matvec(L, "        ", G["fP"][h], "R", "S", F, F, True)
+        a("        break; }")
+    a("    }")
+    a(f"#pragma unroll\n    for (int m = 0; m < kF; ++m) Xq[m * 32] = S[m];")
+    a("    __syncthreads();")
+    a("    const float* am = aminus + ((size_t)cl * 4 + f) * 81 + 9 * q;")
+    a("    float av[9];")
+    a("#pragma unroll\n    for (int s = 0; s < 9; ++s) av[s] = on ? __ldg(am + s) : 0.f;")
+    a("    switch (f) {")
+    for f in range(4):
+        a(f"      case {f}: {{")
+        bycol = _cols(G["rDivM"][f])
+        for m in range(F):
+            if m not in bycol:
+                continue
+            a(f"        {{ float g = 0.f;")
+            a(f"#pragma unroll\n          for (int s = 0; s < 9; ++s) g = fmaf(X[(s * kF + {m}) * 32 + lane], av[s], g);")
+            for k, v in bycol[m]:
+                a(f"          acc[{k}] = fmaf({flit(v)}, g, acc[{k}]);")
+            a("        }")
+        a("        break; }")
+    a("    }")
+    a("    __syncthreads();")
+    a("  }")
+    a("  if (valid) sei_store_col<kBp>(Q + ((size_t)cell * 9 + q) * kBp, acc);")
+    a("}")
+
+    # ---------------- Taylor evaluation ----------------
+    a(f"""
+// out[n][9][B] = sum_i coeffs[i] dQ(i) from packed derivatives [n][kDerivSize]; one thread per (cell, q).
+extern "C" __global__ void sei_taylor_o{order}(int n, const float* __restrict__ derivs, SeiCoeffs coeffs,
+                                               float* __restrict__ out) {{
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)n * 9) return;
+  const long cell = t / 9;
+  const int q = (int)(t % 9);
+  const float* d = derivs + cell * kDerivSize;
+  float o[kBp];
+#pragma unroll
+  for (int k = 0; k < kBp; ++k) o[k] = 0.f;""")
+    off = 0
+    for i in range(order):
+        bi = nb3(order - i)
+        a(f"  {{ const float* s = d + {off} + q * {bi};")
+        a(f"#pragma unroll\n    for (int k = 0; k < {bi}; ++k) o[k] = fmaf(coeffs.c[{i}], s[k], o[k]); }}")
+        off += bi * NQ
+    a("  sei_store_col<kBp>(out + ((size_t)cell * 9 + q) * kBp, o);")
+    a("}")
+    a(f"}}  // namespace sei_o{order}")
+    return "\n".join(L) + "\n"
+
+
+def nnz_flops(order: int) -> dict:
+    """Non-zero flop counts per cell of the generated kernels (ADER, local, neighbour)."""
+    B, F = nb3(order), nb2(order)
+    G = global_matrices(order)
+    nz = lambda m, r=None, c=None: sum(len(v) for v in _cols(m, r, c).values())
+    ader = 0
+    for i in range(1, order):
+        bp, bc = nb3(order - i + 1), nb3(order - i)
+        ader += NQ * 2 * sum(nz(G["kDivMT"][e], bc, bp) for e in range(3)) + 3 * 2 * 24 * bc // NQ * NQ
+        ader += 2 * bc * NQ
+    ader += B * NQ
+    vol = NQ * 2 * sum(nz(G["kDivM"][e]) for e in range(3)) + 3 * 2 * 24 * B
+    lflux = sum(NQ * 2 * (nz(G["fMrT"][f]) + nz(G["rDivM"][f])) + 2 * 81 * F for f in range(4))
+    rt = sum(nz(G["rT"][j]) for j in range(4)) / 4.0
+    fp = sum(nz(G["fP"][h]) for h in range(3)) / 3.0
+    nflux = sum(NQ * 2 * (rt + fp + nz(G["rDivM"][f])) + 2 * 81 * F for f in range(4))
+    return {"ader": ader, "local": vol + lflux, "neighbor": nflux}
+
+
+def write_all(outdir: str, orders=(4, 5, 6)) -> list:
+    os.makedirs(outdir, exist_ok=True)
+    paths = []
+    for o in orders:
+        p = os.path.join(outdir, f"kernels_o{o}.cuh")
+        src = gen_order(o)
+        if not os.path.exists(p) or open(p).read() != src:
+            with open(p, "w") as fh:
+                fh.write(src)
+        paths.append(p)
+    return paths

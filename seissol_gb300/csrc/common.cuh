@@ -1,0 +1,48 @@
+// Device helpers shared by the generated ADER-DG kernels.
+#pragma once
+#include <cstddef>
+
+// Taylor coefficients of one time integration, passed by value (up to order 8).
+struct SeiCoeffs {
+  float c[8];
+};
+
+// Column of N floats starting at a 16-byte aligned address (N % 4 == 0) or any address.
+template <int N>
+__device__ __forceinline__ void sei_load_col(const float* __restrict__ p, float (&v)[N]) {
+  if constexpr (N % 4 == 0) {
+    const float4* p4 = reinterpret_cast<const float4*>(p);
+#pragma unroll
+    for (int i = 0; i < N / 4; ++i) {
+      const float4 t = __ldg(p4 + i);
+      v[4 * i] = t.x;
+      v[4 * i + 1] = t.y;
+      v[4 * i + 2] = t.z;
+      v[4 * i + 3] = t.w;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; ++i) v[i] = __ldg(p + i);
+  }
+}
+
+template <int N, int M>
+__device__ __forceinline__ void sei_store_col(float* __restrict__ p, const float (&v)[M]) {
+  static_assert(N <= M, "store longer than array");
+  if constexpr (N % 4 == 0) {
+    float4* p4 = reinterpret_cast<float4*>(p);
+#pragma unroll
+    for (int i = 0; i < N / 4; ++i) p4[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; ++i) p[i] = v[i];
+  }
+}
+
+// Scalar stores for packed layouts without 16-byte alignment.
+template <int N, int M>
+__device__ __forceinline__ void sei_store_col_scalar(float* __restrict__ p, const float (&v)[M]) {
+  static_assert(N <= M, "store longer than array");
+#pragma unroll
+  for (int i = 0; i < N; ++i) p[i] = v[i];
+}

@@ -1,0 +1,53 @@
+// Launchers of the FP32 CUDA-core kernels for one convergence order.  Included by
+// kernels_o{4,5,6}.cu after the generated kernel bodies (seissol_gb300/codegen/gen_kernels.py)
+// with SEI_ORDER defined.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "internal.h"
+
+#define SEI_CAT2(a, b) a##b
+#define SEI_CAT(a, b) SEI_CAT2(a, b)
+
+namespace {
+namespace K = SEI_CAT(sei_o, SEI_ORDER);
+
+SeiCoeffs toCoeffs(const float* c) {
+  SeiCoeffs s{};
+  for (int i = 0; i < K::kOrder; ++i) s.c[i] = c[i];
+  return s;
+}
+
+int launchLocal(const sei::DeviceArrays& d, const float* coeffs, void* stream) {
+  if (d.n <= 0) return 0;
+  const size_t smem = sizeof(float) * 9 * K::kB * 32;
+  if (cudaFuncSetAttribute(K::SEI_CAT(sei_local_o, SEI_ORDER), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return -1;
+  const int blocks = (d.n + K::kCPB - 1) / K::kCPB;
+  K::SEI_CAT(sei_local_o, SEI_ORDER)<<<blocks, 288, smem, (cudaStream_t)stream>>>(
+      d.n, d.Q, d.I, d.star_nz, d.aplus, d.ftype, toCoeffs(coeffs), d.derivs);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launchNeighbor(const sei::DeviceArrays& d, void* stream) {
+  if (d.n <= 0) return 0;
+  const size_t smem = sizeof(float) * 9 * K::kF * 32;
+  const int blocks = (d.n + K::kCPB - 1) / K::kCPB;
+  K::SEI_CAT(sei_neighbor_o, SEI_ORDER)<<<blocks, 288, smem, (cudaStream_t)stream>>>(
+      d.n, d.Q, d.I, d.aminus, d.nbr, d.rel, d.ftype);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launchTaylor(int n, const float* derivs, const float* coeffs, float* out, void* stream) {
+  if (n <= 0) return 0;
+  const long threads = (long)n * 9;
+  const int blocks = (int)((threads + 255) / 256);
+  K::SEI_CAT(sei_taylor_o, SEI_ORDER)<<<blocks, 256, 0, (cudaStream_t)stream>>>(n, derivs, toCoeffs(coeffs), out);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+}  // namespace
+
+namespace sei {
+OrderKernels SEI_CAT(orderKernels, SEI_ORDER)() { return OrderKernels{launchLocal, launchNeighbor, launchTaylor}; }
+}  // namespace sei

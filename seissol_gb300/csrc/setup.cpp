@@ -1,0 +1,366 @@
+// Host-side set-up of the element update: synthetic periodic cube mesh, face relations,
+// materials, star matrices and flux solvers (float64 arithmetic, stored as float32).
+//
+// Conventions followed:
+//   FACE2NODES, normals, tangents   src/Geometry/MeshTools.cpp:21-69
+//   neighbour side / orientation    src/Geometry/PUMLReader.cpp:151-163, 405-427
+//   Jacobian of the reference map   src/Numerical/Transformation.cpp:66-108
+//   A^T, B^T, C^T, Godunov state    src/Equations/elastic/Model/ElasticSetup.h:27-180
+//   face rotation T, Tinv           src/Numerical/Transformation.cpp:110-290
+//   star matrices, flux solvers     src/Initializer/Model/CellLocalMatrices.cpp:46-296
+//                                   codegen/kernels/aderdg.py:226-246
+//   CFL time step                   src/Initializer/TimeStepping/GlobalTimestep.cpp:27-47
+#include "internal.h"
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <map>
+#include <stdexcept>
+
+namespace sei {
+
+namespace {
+
+const int kFace2Nodes[4][3] = {{0, 2, 1}, {0, 1, 3}, {0, 3, 2}, {1, 2, 3}};
+
+// 5-tetrahedron split of a unit cube (even parity); odd cubes use the mirror image in x.
+const int kEvenTets[5][4][3] = {
+    {{0, 0, 0}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1}},
+    {{1, 0, 0}, {0, 0, 0}, {1, 1, 0}, {1, 0, 1}},
+    {{0, 1, 0}, {0, 0, 0}, {1, 1, 0}, {0, 1, 1}},
+    {{0, 0, 1}, {0, 0, 0}, {1, 0, 1}, {0, 1, 1}},
+    {{1, 1, 1}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1}},
+};
+
+using Vec3 = std::array<double, 3>;
+using Mat9 = std::array<double, 81>;  // row-major [i][j] = view (i, j)
+
+Vec3 sub(const Vec3& a, const Vec3& b) { return {a[0] - b[0], a[1] - b[1], a[2] - b[2]}; }
+Vec3 cross(const Vec3& a, const Vec3& b) {
+  return {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+}
+double dot(const Vec3& a, const Vec3& b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+double norm(const Vec3& a) { return std::sqrt(dot(a, a)); }
+Vec3 scale(const Vec3& a, double s) { return {a[0] * s, a[1] * s, a[2] * s}; }
+
+// splitmix64: portable, seeded uniform numbers.
+struct Rng {
+  uint64_t s;
+  explicit Rng(uint64_t seed) : s(seed) {}
+  uint64_t next() {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  }
+  double uniform(double lo, double hi) { return lo + (hi - lo) * ((next() >> 11) * (1.0 / 9007199254740992.0)); }
+};
+
+void coefficientMatrixT(double rho, double mu, double lam, int dim, Mat9& m) {
+  m.fill(0.0);
+  const double l2m = lam + 2.0 * mu, ri = 1.0 / rho;
+  auto at = [&](int i, int j) -> double& { return m[i * 9 + j]; };
+  if (dim == 0) {
+    at(6, 0) = -l2m; at(6, 1) = -lam; at(6, 2) = -lam; at(7, 3) = -mu; at(8, 5) = -mu;
+    at(0, 6) = -ri; at(3, 7) = -ri; at(5, 8) = -ri;
+  } else if (dim == 1) {
+    at(7, 0) = -lam; at(7, 1) = -l2m; at(7, 2) = -lam; at(6, 3) = -mu; at(8, 4) = -mu;
+    at(1, 7) = -ri; at(3, 6) = -ri; at(4, 8) = -ri;
+  } else {
+    at(8, 0) = -lam; at(8, 1) = -lam; at(8, 2) = -l2m; at(7, 4) = -mu; at(6, 5) = -mu;
+    at(2, 8) = -ri; at(5, 6) = -ri; at(4, 7) = -ri;
+  }
+}
+
+// Solves A X = Bm (9x9, row-major) by LU with partial pivoting; Bm is overwritten with X.
+void solve9(Mat9 a, Mat9& bm) {
+  int piv[9];
+  for (int i = 0; i < 9; ++i) piv[i] = i;
+  for (int c = 0; c < 9; ++c) {
+    int p = c;
+    for (int r = c + 1; r < 9; ++r)
+      if (std::fabs(a[r * 9 + c]) > std::fabs(a[p * 9 + c])) p = r;
+    if (a[p * 9 + c] == 0.0) throw std::runtime_error("singular eigenvector basis in Godunov state");
+    if (p != c) {
+      for (int j = 0; j < 9; ++j) {
+        std::swap(a[c * 9 + j], a[p * 9 + j]);
+        std::swap(bm[c * 9 + j], bm[p * 9 + j]);
+      }
+    }
+    for (int r = c + 1; r < 9; ++r) {
+      const double f = a[r * 9 + c] / a[c * 9 + c];
+      if (f == 0.0) continue;
+      for (int j = c; j < 9; ++j) a[r * 9 + j] -= f * a[c * 9 + j];
+      for (int j = 0; j < 9; ++j) bm[r * 9 + j] -= f * bm[c * 9 + j];
+    }
+  }
+  for (int c = 8; c >= 0; --c) {
+    for (int j = 0; j < 9; ++j) {
+      double s = bm[c * 9 + j];
+      for (int k = c + 1; k < 9; ++k) s -= a[c * 9 + k] * bm[k * 9 + j];
+      bm[c * 9 + j] = s / a[c * 9 + c];
+    }
+  }
+}
+
+// Transposed Godunov states of a regular face; materials (rho, mu, lambda).
+void godunovState(const double* loc, const double* nb, Mat9& local, Mat9& neigh) {
+  const double rl = loc[0], ml = loc[1], ll = loc[2];
+  const double rn = nb[0], mn = nb[1], ln = nb[2];
+  Mat9 r{};
+  auto R = [&](int i, int j) -> double& { return r[i * 9 + j]; };
+  R(0, 0) = ll + 2 * ml; R(1, 0) = ll; R(2, 0) = ll; R(6, 0) = std::sqrt((ll + 2 * ml) / rl);
+  R(3, 1) = ml; R(7, 1) = std::sqrt(ml / rl);
+  R(5, 2) = ml; R(8, 2) = std::sqrt(ml / rl);
+  R(4, 3) = ll + 2 * ml; R(1, 4) = ll + 2 * ml; R(2, 5) = ll + 2 * ml;
+  R(5, 6) = mn; R(8, 6) = -std::sqrt(mn / rn);
+  R(3, 7) = mn; R(7, 7) = -std::sqrt(mn / rn);
+  R(0, 8) = ln + 2 * mn; R(1, 8) = ln; R(2, 8) = ln; R(6, 8) = -std::sqrt((ln + 2 * mn) / rn);
+  Mat9 rt{}, rhs{};
+  for (int i = 0; i < 9; ++i)
+    for (int j = 0; j < 9; ++j) rt[i * 9 + j] = r[j * 9 + i];
+  // rhs = chi R^T with chi = diag(1, 1, 1, 0, ...): the first three rows of R^T.
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 9; ++j) rhs[i * 9 + j] = rt[i * 9 + j];
+  solve9(rt, rhs);
+  for (int i = 0; i < 9; ++i)
+    for (int j = 0; j < 9; ++j) {
+      neigh[i * 9 + j] = rhs[i * 9 + j];
+      local[i * 9 + j] = (i == j ? 1.0 : 0.0) - rhs[i * 9 + j];
+    }
+}
+
+void rotation(const Vec3& n, const Vec3& s, const Vec3& t, Mat9& T, Mat9& Ti) {
+  T.fill(0.0);
+  Ti.fill(0.0);
+  auto at = [](Mat9& m, int i, int j) -> double& { return m[i * 9 + j]; };
+  const double nx = n[0], ny = n[1], nz = n[2], sx = s[0], sy = s[1], sz = s[2], tx = t[0], ty = t[1], tz = t[2];
+  const double tcol[6][6] = {
+      {nx * nx, ny * ny, nz * nz, ny * nx, nz * ny, nz * nx},
+      {sx * sx, sy * sy, sz * sz, sy * sx, sz * sy, sz * sx},
+      {tx * tx, ty * ty, tz * tz, ty * tx, tz * ty, tz * tx},
+      {2 * nx * sx, 2 * ny * sy, 2 * nz * sz, ny * sx + nx * sy, nz * sy + ny * sz, nz * sx + nx * sz},
+      {2 * sx * tx, 2 * sy * ty, 2 * sz * tz, sy * tx + sx * ty, sz * ty + sy * tz, sz * tx + sx * tz},
+      {2 * nx * tx, 2 * ny * ty, 2 * nz * tz, ny * tx + nx * ty, nz * ty + ny * tz, nz * tx + nx * tz}};
+  const double icol[6][6] = {
+      {nx * nx, sx * sx, tx * tx, nx * sx, sx * tx, nx * tx},
+      {ny * ny, sy * sy, ty * ty, ny * sy, sy * ty, ny * ty},
+      {nz * nz, sz * sz, tz * tz, nz * sz, sz * tz, nz * tz},
+      {2 * ny * nx, 2 * sy * sx, 2 * ty * tx, ny * sx + nx * sy, sy * tx + sx * ty, ny * tx + nx * ty},
+      {2 * nz * ny, 2 * sz * sy, 2 * tz * ty, nz * sy + ny * sz, sz * ty + sy * tz, nz * ty + ny * tz},
+      {2 * nz * nx, 2 * sz * sx, 2 * tz * tx, nz * sx + nx * sz, sz * tx + sx * tz, nz * tx + nx * tz}};
+  for (int c = 0; c < 6; ++c)
+    for (int r = 0; r < 6; ++r) {
+      at(T, r, c) = tcol[c][r];
+      at(Ti, r, c) = icol[c][r];
+    }
+  for (int i = 0; i < 3; ++i) {
+    at(T, 6 + i, 6) = n[i];
+    at(T, 6 + i, 7) = s[i];
+    at(T, 6 + i, 8) = t[i];
+    at(Ti, 6, 6 + i) = n[i];
+    at(Ti, 7, 6 + i) = s[i];
+    at(Ti, 8, 6 + i) = t[i];
+  }
+}
+
+// out(i, j) = s * sum_{k, l} Tinv(k, i) (Qgod A~^T)(k, l) T(j, l), written column-major (i + 9 j) as float.
+void fluxSolver(double s, const Mat9& Ti, const Mat9& qgod, const Mat9& at, const Mat9& T, float* out) {
+  Mat9 qa{}, tmp{};
+  for (int k = 0; k < 9; ++k)
+    for (int l = 0; l < 9; ++l) {
+      double v = 0;
+      for (int q = 0; q < 9; ++q) v += qgod[k * 9 + q] * at[q * 9 + l];
+      qa[k * 9 + l] = v;
+    }
+  for (int i = 0; i < 9; ++i)
+    for (int l = 0; l < 9; ++l) {
+      double v = 0;
+      for (int k = 0; k < 9; ++k) v += Ti[k * 9 + i] * qa[k * 9 + l];
+      tmp[i * 9 + l] = v;
+    }
+  for (int i = 0; i < 9; ++i)
+    for (int j = 0; j < 9; ++j) {
+      double v = 0;
+      for (int l = 0; l < 9; ++l) v += tmp[i * 9 + l] * T[j * 9 + l];
+      out[i + 9 * j] = static_cast<float>(s * v);
+    }
+}
+
+}  // namespace
+
+void buildPeriodicCube(const sei_cube_params& p, HostMesh& m) {
+  // Even counts keep the alternating 5-tet split conforming across cubes; at least 4 cubes per
+  // direction keep the periodically identified faces distinct.
+  if (p.nx < 4 || p.ny < 4 || p.nz < 4 || p.nx % 2 || p.ny % 2 || p.nz % 2)
+    throw std::invalid_argument("periodic cube needs even cube counts >= 4 in every direction");
+  if (!(p.h > 0) || !(p.rho > 0) || !(p.vp > 0) || !(p.vs > 0) || p.perturb < 0 || p.perturb >= 0.5)
+    throw std::invalid_argument("invalid cube geometry or material");
+  const int64_t ncubes = (int64_t)p.nx * p.ny * p.nz;
+  m.n = ncubes * 5;
+  m.topo.resize(m.n * 4);
+  m.coords.resize(m.n * 12);
+  m.material.resize(m.n * 3);
+  int tets[2][5][4][3];
+  for (int par = 0; par < 2; ++par)
+    for (int t = 0; t < 5; ++t) {
+      for (int v = 0; v < 4; ++v) {
+        tets[par][t][v][0] = par ? 1 - kEvenTets[t][v][0] : kEvenTets[t][v][0];
+        tets[par][t][v][1] = kEvenTets[t][v][1];
+        tets[par][t][v][2] = kEvenTets[t][v][2];
+      }
+      Vec3 a{}, b{}, c{}, d{};
+      for (int k = 0; k < 3; ++k) {
+        a[k] = tets[par][t][0][k];
+        b[k] = tets[par][t][1][k];
+        c[k] = tets[par][t][2][k];
+        d[k] = tets[par][t][3][k];
+      }
+      if (dot(cross(sub(b, a), sub(c, a)), sub(d, a)) < 0)
+        for (int k = 0; k < 3; ++k) std::swap(tets[par][t][2][k], tets[par][t][3][k]);
+    }
+  // Cells ordered by (parity, tet type, cube): equal face relations are contiguous.
+  int64_t cell = 0;
+  for (int par = 0; par < 2; ++par)
+    for (int t = 0; t < 5; ++t)
+      for (int k = 0; k < p.nz; ++k)
+        for (int j = 0; j < p.ny; ++j)
+          for (int i = 0; i < p.nx; ++i) {
+            if ((i + j + k) % 2 != par) continue;
+            for (int v = 0; v < 4; ++v) {
+              const int gi = i + tets[par][t][v][0], gj = j + tets[par][t][v][1], gk = k + tets[par][t][v][2];
+              m.topo[cell * 4 + v] = (gi % p.nx) + (int64_t)p.nx * ((gj % p.ny) + (int64_t)p.ny * (gk % p.nz));
+              m.coords[cell * 12 + v * 3 + 0] = gi * p.h;
+              m.coords[cell * 12 + v * 3 + 1] = gj * p.h;
+              m.coords[cell * 12 + v * 3 + 2] = gk * p.h;
+            }
+            ++cell;
+          }
+  Rng rng(p.seed);
+  for (int64_t c = 0; c < m.n; ++c) {
+    double rho = p.rho, vp = p.vp, vs = p.vs;
+    if (p.perturb > 0) {
+      rho *= rng.uniform(1 - p.perturb, 1 + p.perturb);
+      vp *= rng.uniform(1 - p.perturb, 1 + p.perturb);
+      vs *= rng.uniform(1 - p.perturb, 1 + p.perturb);
+    }
+    const double mu = rho * vs * vs, lam = rho * vp * vp - 2 * mu;
+    if (!(lam > -2.0 / 3.0 * mu)) throw std::invalid_argument("material perturbation gives a non-physical cell");
+    m.material[c * 3 + 0] = rho;
+    m.material[c * 3 + 1] = mu;
+    m.material[c * 3 + 2] = lam;
+  }
+  computeFaceRelations(m);
+}
+
+void computeFaceRelations(HostMesh& m) {
+  m.nbr.assign(m.n * 4, -1);
+  m.side.assign(m.n * 4, 0);
+  m.orient.assign(m.n * 4, 0);
+  m.ftype.assign(m.n * 4, 2);
+  std::map<std::array<int64_t, 3>, std::array<int64_t, 2>> faces;
+  for (int64_t c = 0; c < m.n; ++c)
+    for (int f = 0; f < 4; ++f) {
+      std::array<int64_t, 3> key{m.topo[c * 4 + kFace2Nodes[f][0]], m.topo[c * 4 + kFace2Nodes[f][1]],
+                                 m.topo[c * 4 + kFace2Nodes[f][2]]};
+      std::sort(key.begin(), key.end());
+      auto it = faces.find(key);
+      if (it == faces.end()) {
+        faces.emplace(key, std::array<int64_t, 2>{c * 4 + f, -1});
+      } else {
+        if (it->second[1] != -1) throw std::runtime_error("non-manifold face in mesh");
+        it->second[1] = c * 4 + f;
+      }
+    }
+  for (const auto& kv : faces) {
+    const int64_t a = kv.second[0], b = kv.second[1];
+    if (b < 0) continue;
+    for (int dir = 0; dir < 2; ++dir) {
+      const int64_t cf = dir ? b : a, df = dir ? a : b;
+      const int64_t c = cf / 4, d = df / 4;
+      const int f = (int)(cf % 4), j = (int)(df % 4);
+      m.nbr[cf] = (int32_t)d;
+      m.side[cf] = (int8_t)j;
+      m.ftype[cf] = 0;
+      const int64_t first = m.topo[c * 4 + kFace2Nodes[f][0]];
+      int h = -1;
+      for (int k = 0; k < 3; ++k)
+        if (m.topo[d * 4 + kFace2Nodes[j][k]] == first) h = k;
+      if (h < 0) throw std::runtime_error("face orientation not found");
+      m.orient[cf] = (int8_t)h;
+    }
+  }
+}
+
+void buildOperators(const HostMesh& m, std::vector<float>& star, std::vector<float>& aplus,
+                    std::vector<float>& aminus) {
+  star.assign(m.n * 3 * 81, 0.f);
+  aplus.assign(m.n * 4 * 81, 0.f);
+  aminus.assign(m.n * 4 * 81, 0.f);
+#pragma omp parallel for schedule(static)
+  for (int64_t c = 0; c < m.n; ++c) {
+    const double* mat = &m.material[c * 3];
+    Mat9 at[3];
+    for (int d = 0; d < 3; ++d) coefficientMatrixT(mat[0], mat[1], mat[2], d, at[d]);
+    Vec3 v[4];
+    for (int k = 0; k < 4; ++k) v[k] = {m.coords[c * 12 + k * 3], m.coords[c * 12 + k * 3 + 1], m.coords[c * 12 + k * 3 + 2]};
+    // Rows of the inverse of J = [v1-v0, v2-v0, v3-v0] (columns) are grad xi, grad eta, grad zeta.
+    const Vec3 e1 = sub(v[1], v[0]), e2 = sub(v[2], v[0]), e3 = sub(v[3], v[0]);
+    const double det = dot(e1, cross(e2, e3));
+    const Vec3 g[3] = {scale(cross(e2, e3), 1.0 / det), scale(cross(e3, e1), 1.0 / det),
+                       scale(cross(e1, e2), 1.0 / det)};
+    for (int e = 0; e < 3; ++e)
+      for (int i = 0; i < 9; ++i)
+        for (int j = 0; j < 9; ++j)
+          star[(c * 3 + e) * 81 + i + 9 * j] =
+              static_cast<float>(g[e][0] * at[0][i * 9 + j] + g[e][1] * at[1][i * 9 + j] + g[e][2] * at[2][i * 9 + j]);
+    const double volume = std::fabs(det) / 6.0;
+    for (int f = 0; f < 4; ++f) {
+      const Vec3 a = v[kFace2Nodes[f][0]], b = v[kFace2Nodes[f][1]], cc = v[kFace2Nodes[f][2]];
+      Vec3 nrm = cross(sub(b, a), sub(cc, a));
+      const double area = 0.5 * norm(nrm);
+      Vec3 t1 = sub(b, a);
+      Vec3 t2 = cross(nrm, t1);
+      nrm = scale(nrm, 1.0 / norm(nrm));
+      t1 = scale(t1, 1.0 / norm(t1));
+      t2 = scale(t2, 1.0 / norm(t2));
+      const int32_t nb = m.nbr[c * 4 + f];
+      const double* nmat = nb >= 0 ? &m.material[(int64_t)nb * 3] : mat;
+      Mat9 qgl, qgn, T, Ti;
+      godunovState(mat, nmat, qgl, qgn);
+      rotation(nrm, t1, t2, T, Ti);
+      const double fs = -2.0 * area / (6.0 * volume);
+      const bool dr = m.ftype[c * 4 + f] == 1;
+      fluxSolver(dr ? 0.0 : fs, Ti, qgl, at[0], T, &aplus[(c * 4 + f) * 81]);
+      fluxSolver(fs, Ti, qgn, at[0], T, &aminus[(c * 4 + f) * 81]);
+    }
+  }
+}
+
+double cflTimestep(const HostMesh& m, int order, double cfl) {
+  double best = 1e300;
+  for (int64_t c = 0; c < m.n; ++c) {
+    Vec3 x[4];
+    for (int k = 0; k < 4; ++k) x[k] = {m.coords[c * 12 + k * 3], m.coords[c * 12 + k * 3 + 1], m.coords[c * 12 + k * 3 + 2]};
+    const double alpha = dot(sub(x[1], x[0]), cross(sub(x[2], x[0]), sub(x[3], x[0])));
+    const double areas = norm(cross(sub(x[1], x[0]), sub(x[2], x[0]))) + norm(cross(sub(x[1], x[0]), sub(x[3], x[0]))) +
+                         norm(cross(sub(x[2], x[0]), sub(x[3], x[0]))) + norm(cross(sub(x[2], x[1]), sub(x[3], x[1])));
+    const double insphere = std::fabs(alpha) / areas;
+    const double rho = m.material[c * 3], mu = m.material[c * 3 + 1], lam = m.material[c * 3 + 2];
+    const double vp = std::sqrt((lam + 2 * mu) / rho);
+    best = std::min(best, cfl * 2.0 * insphere / (vp * (2 * order - 1)));
+  }
+  return best;
+}
+
+void seedDofs(int64_t n, int order, uint64_t seed, std::vector<float>& dofs) {
+  const int b = numBasis(order), bp = paddedBasis(order);
+  dofs.assign(n * 9 * bp, 0.f);
+  Rng rng(seed ^ 0x5DEECE66Dull);
+  for (int64_t c = 0; c < n; ++c)
+    for (int q = 0; q < 9; ++q)
+      for (int k = 0; k < b; ++k) dofs[(c * 9 + q) * bp + k] = static_cast<float>(rng.uniform(-1.0, 1.0));
+}
+
+}  // namespace sei

@@ -1,0 +1,247 @@
+"""ctypes bindings of libsei_gb300.so (C ABI in include/sei_gb300.h).
+
+Numpy conventions used by this front-end: DOF tensors are [ncells, 9, B] (basis index
+fastest, as the reference's column-major Q[k, p]); per-cell 9x9 operators are numpy arrays
+indexed [..., q, p] (row q, column p of the reference's view) and are converted to the
+ABI's column-major storage here.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsei_gb300.so")
+
+SEI_OK = 0
+ERRORS = {-1: "SEI_ERR_ARG", -2: "SEI_ERR_OOM", -3: "SEI_ERR_CUDA", -4: "SEI_ERR_TIMEOUT", -5: "SEI_ERR_NAN",
+          -6: "SEI_ERR_STATE", -7: "SEI_ERR_UNSUPPORTED"}
+# Proxy kernel names (src/Proxy/Common.cpp:22-40) -> SEI_KERNEL_*.
+KERNELS = {"all": 0, "local": 1, "neigh": 2, "ader": 3, "localwoader": 4, "neigh_dr": 5, "godunov_dr": 6, "all_dr": 7}
+
+
+class SeiError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class _Config(C.Structure):
+    _fields_ = [("order", C.c_int), ("device", C.c_int), ("precision", C.c_int), ("store_derivatives", C.c_int)]
+
+
+class _CubeParams(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("h", C.c_double), ("rho", C.c_double),
+                ("vp", C.c_double), ("vs", C.c_double), ("perturb", C.c_double), ("seed", C.c_uint64)]
+
+
+class _Perf(C.Structure):
+    _fields_ = [("nonzero_flop", C.c_double), ("hardware_flop", C.c_double), ("bytes", C.c_double)]
+
+
+_lib = None
+VP = C.c_void_p
+
+
+def _sig(lib, name, res, args):
+    fn = getattr(lib, name)
+    fn.restype = res
+    fn.argtypes = args
+
+
+def load_library(path: str | None = None):
+    """Loads the CUDA library; raises if it has not been built (no fallback exists)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise SeiError(-7, f"{p} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(p)
+    i, i64, d = C.c_int, C.c_int64, C.c_double
+    _sig(lib, "sei_version", i, [])
+    _sig(lib, "sei_create", i, [C.POINTER(_Config), C.POINTER(VP)])
+    _sig(lib, "sei_destroy", None, [VP])
+    _sig(lib, "sei_last_error", C.c_char_p, [VP])
+    _sig(lib, "sei_build_periodic_cube", i, [VP, C.POINTER(_CubeParams), C.POINTER(i64)])
+    _sig(lib, "sei_set_cells", i, [VP, i64, VP, VP, VP, VP, VP, VP, VP])
+    _sig(lib, "sei_num_cells", i64, [VP])
+    _sig(lib, "sei_get_cells", i, [VP, VP, VP, VP, VP, VP, VP, VP])
+    _sig(lib, "sei_get_geometry", i, [VP, VP, VP, VP])
+    _sig(lib, "sei_cfl_timestep", i, [VP, d, C.POINTER(d)])
+    _sig(lib, "sei_set_dofs", i, [VP, VP])
+    _sig(lib, "sei_get_dofs", i, [VP, VP])
+    _sig(lib, "sei_get_time_integrated", i, [VP, VP])
+    _sig(lib, "sei_get_derivatives", i, [VP, VP])
+    _sig(lib, "sei_derivatives_size", i, [i])
+    _sig(lib, "sei_compute_ader", i, [VP, d])
+    _sig(lib, "sei_compute_local_integral", i, [VP])
+    _sig(lib, "sei_compute_ader_local", i, [VP, d])
+    _sig(lib, "sei_compute_neighbors_integral", i, [VP])
+    _sig(lib, "sei_evaluate_taylor", i, [VP, VP, VP])
+    _sig(lib, "sei_run", i, [VP, i, d, i])
+    _sig(lib, "sei_run_host", i, [VP, i, d, i, VP, VP])
+    _sig(lib, "sei_sync", i, [VP])
+    _sig(lib, "sei_last_run_ms", i, [VP, C.POINTER(d)])
+    _sig(lib, "sei_metrics", i, [VP, i, C.POINTER(_Perf)])
+    _sig(lib, "sei_set_profiling", i, [VP, i])
+    _sig(lib, "sei_kernel_times_ms", i, [VP, C.POINTER(d), C.POINTER(d), C.POINTER(i)])
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def nbasis(order):
+    return order * (order + 1) * (order + 2) // 6
+
+
+def padded_basis(order):
+    return (nbasis(order) + 3) // 4 * 4
+
+
+def derivatives_size(order):
+    return sum(nbasis(order - i) for i in range(order)) * 9
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(VP)
+
+
+def _colmajor(a, dtype=np.float32):
+    return np.ascontiguousarray(np.swapaxes(np.asarray(a), -1, -2), dtype=dtype)
+
+
+class Context:
+    """One device-resident mesh and its element-update kernels (sei_ctx)."""
+
+    def __init__(self, order: int, device: int = 0, precision: int = 0, store_derivatives: bool = False):
+        self.lib = load_library()
+        self.order = order
+        self.B = nbasis(order)
+        cfg = _Config(order, device, precision, int(store_derivatives))
+        h = VP()
+        rc = self.lib.sei_create(C.byref(cfg), C.byref(h))
+        if rc != SEI_OK:
+            raise SeiError(rc, f"sei_create(order={order}, device={device}, precision={precision}) failed")
+        self.h = h
+        self.n = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sei_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc, what):
+        if rc != SEI_OK:
+            msg = self.lib.sei_last_error(self.h)
+            raise SeiError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+    # -- set-up ------------------------------------------------------------------------
+    def build_periodic_cube(self, nx, ny, nz, h=100.0, rho=2700.0, vp=6000.0, vs=3464.0, perturb=0.0, seed=1):
+        p = _CubeParams(nx, ny, nz, h, rho, vp, vs, perturb, seed)
+        n = C.c_int64()
+        self._check(self.lib.sei_build_periodic_cube(self.h, C.byref(p), C.byref(n)), "sei_build_periodic_cube")
+        self.n = n.value
+        return self.n
+
+    def set_cells(self, star, aplus, aminus, neighbor, side, orient, face_type):
+        n = star.shape[0]
+        arrs = [_colmajor(star), _colmajor(aplus), _colmajor(aminus), np.ascontiguousarray(neighbor, np.int32),
+                np.ascontiguousarray(side, np.int8), np.ascontiguousarray(orient, np.int8),
+                np.ascontiguousarray(face_type, np.int8)]
+        self._check(self.lib.sei_set_cells(self.h, n, *[_ptr(a) for a in arrs]), "sei_set_cells")
+        self.n = n
+
+    def get_cells(self):
+        n = self.n
+        star = np.empty((n, 3, 9, 9), np.float32)
+        ap = np.empty((n, 4, 9, 9), np.float32)
+        am = np.empty((n, 4, 9, 9), np.float32)
+        nb = np.empty((n, 4), np.int32)
+        side = np.empty((n, 4), np.int8)
+        orient = np.empty((n, 4), np.int8)
+        ft = np.empty((n, 4), np.int8)
+        self._check(self.lib.sei_get_cells(self.h, *[_ptr(a) for a in (star, ap, am, nb, side, orient, ft)]), "sei_get_cells")
+        sw = lambda a: np.swapaxes(a, -1, -2)  # stored column-major -> numpy [q, p]
+        return {"star": sw(star), "AplusT": sw(ap), "AminusT": sw(am), "neighbor": nb, "side": side, "orient": orient,
+                "face_type": ft}
+
+    def get_geometry(self):
+        n = self.n
+        v = np.empty((n, 4, 3), np.float64)
+        m = np.empty((n, 3), np.float64)
+        t = np.empty((n, 4), np.int64)
+        self._check(self.lib.sei_get_geometry(self.h, _ptr(v), _ptr(m), _ptr(t)), "sei_get_geometry")
+        return v, m, t
+
+    def cfl_timestep(self, cfl=0.5):
+        d = C.c_double()
+        self._check(self.lib.sei_cfl_timestep(self.h, cfl, C.byref(d)), "sei_cfl_timestep")
+        return d.value
+
+    # -- data ---------------------------------------------------------------------------
+    def set_dofs(self, dofs):
+        a = np.ascontiguousarray(dofs, np.float32)
+        assert a.shape == (self.n, 9, self.B), a.shape
+        self._check(self.lib.sei_set_dofs(self.h, _ptr(a)), "sei_set_dofs")
+
+    def get_dofs(self):
+        a = np.empty((self.n, 9, self.B), np.float32)
+        self._check(self.lib.sei_get_dofs(self.h, _ptr(a)), "sei_get_dofs")
+        return a
+
+    def get_time_integrated(self):
+        a = np.empty((self.n, 9, self.B), np.float32)
+        self._check(self.lib.sei_get_time_integrated(self.h, _ptr(a)), "sei_get_time_integrated")
+        return a
+
+    def get_derivatives(self):
+        a = np.empty((self.n, derivatives_size(self.order)), np.float32)
+        self._check(self.lib.sei_get_derivatives(self.h, _ptr(a)), "sei_get_derivatives")
+        return a
+
+    # -- kernels ------------------------------------------------------------------------
+    def compute_ader_local(self, dt):
+        self._check(self.lib.sei_compute_ader_local(self.h, dt), "sei_compute_ader_local")
+
+    def compute_neighbors_integral(self):
+        self._check(self.lib.sei_compute_neighbors_integral(self.h), "sei_compute_neighbors_integral")
+
+    def run(self, kernel, dt, nsteps):
+        k = KERNELS[kernel] if isinstance(kernel, str) else kernel
+        self._check(self.lib.sei_run(self.h, k, dt, nsteps), f"sei_run({kernel})")
+
+    def run_host(self, kernel, dt, nsteps, dofs_in, dofs_out):
+        k = KERNELS[kernel] if isinstance(kernel, str) else kernel
+        self._check(self.lib.sei_run_host(self.h, k, dt, nsteps, _ptr(dofs_in), _ptr(dofs_out)), f"sei_run_host({kernel})")
+
+    def sync(self):
+        self._check(self.lib.sei_sync(self.h), "sei_sync")
+
+    def set_profiling(self, on=True):
+        self._check(self.lib.sei_set_profiling(self.h, int(on)), "sei_set_profiling")
+
+    def kernel_times_ms(self):
+        """(local ms, neighbour ms, launches) summed over the last run with profiling on."""
+        a, b, n = C.c_double(), C.c_double(), C.c_int()
+        self._check(self.lib.sei_kernel_times_ms(self.h, C.byref(a), C.byref(b), C.byref(n)), "sei_kernel_times_ms")
+        return a.value, b.value, n.value
+
+    def last_run_ms(self):
+        d = C.c_double()
+        self._check(self.lib.sei_last_run_ms(self.h, C.byref(d)), "sei_last_run_ms")
+        return d.value
