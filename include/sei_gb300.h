@@ -58,14 +58,47 @@ typedef struct sei_config {
 } sei_config;
 
 /* Synthetic periodic cube: nx*ny*nz cubes of edge h, 5 tetrahedra each (even counts >= 4).
- * Material rho, vp, vs, each multiplied per cell by U[1-perturb, 1+perturb] (seeded). */
+ * Material rho, vp, vs, each multiplied per cell by U[1-perturb, 1+perturb] (seeded).
+ * fault_plane in 1..nx-1 turns the faces on the plane x = fault_plane * h into a planar
+ * vertical dynamic-rupture fault (plus side at smaller x); -1 builds no fault. */
 typedef struct sei_cube_params {
   int nx, ny, nz;
   double h;
   double rho, vp, vs;
   double perturb;
   uint64_t seed;
+  int fault_plane;
 } sei_cube_params;
+
+/* Fast-velocity-weakening rate-and-state friction (src/Initializer/Parameters/DRParameters.h:36-73,
+ * names of the reference: rs_f0, rs_b, rs_sr0, rs_sl0, rs_muw, rs_srW) with the seeded initial
+ * state of the synthetic fault: a ~ U[a_min, a_max] per point, normal stress ~ U[sn_min, sn_max]
+ * (negative = compression), shear traction (along tangent 1) ~ U[tau_min, tau_max], slip rate
+ * v_init, state variable at steady state for v_init.  Newton: max_newton updates, tolerance
+ * newton_tol on |g|; fixed point: max_outer passes, tolerance state_tol on the slip-rate change
+ * (reference defaults 60, 1e-8, 10, 1e-8). */
+typedef struct sei_rs_params {
+  double f0, b, v0, l, muw, vw;
+  double a_min, a_max, sn_min, sn_max, tau_min, tau_max, v_init;
+  double newton_tol, state_tol;
+  int max_newton, max_outer;
+  uint64_t seed;
+} sei_rs_params;
+
+/* Friction-state fields for sei_dr_get_state. */
+#define SEI_DR_PSI 0
+#define SEI_DR_SLIP_RATE1 1
+#define SEI_DR_SLIP_RATE2 2
+#define SEI_DR_SLIP1 3
+#define SEI_DR_SLIP2 4
+#define SEI_DR_SLIP 5
+#define SEI_DR_MU 6
+#define SEI_DR_TRACTION1 7
+#define SEI_DR_TRACTION2 8
+#define SEI_DR_A 9
+#define SEI_DR_SN0 10
+#define SEI_DR_TAU1_0 11
+#define SEI_DR_TAU2_0 12
 
 /* PerformanceEstimate of the reference (src/Monitoring/Metric.h:8-60), per cell and step. */
 typedef struct sei_perf {
@@ -104,6 +137,7 @@ int sei_cfl_timestep(sei_ctx* ctx, double cfl, double* dt);
 int sei_set_dofs(sei_ctx* ctx, const float* dofs);
 int sei_get_dofs(sei_ctx* ctx, float* dofs);
 int sei_get_time_integrated(sei_ctx* ctx, float* tint);
+/* Stored CK derivatives: [n][size] with store_derivatives, or [2 nfaces][size] by fault slot after sei_dr_setup. */
 int sei_get_derivatives(sei_ctx* ctx, float* derivs);
 int sei_derivatives_size(int order);
 
@@ -126,6 +160,32 @@ int sei_run_host(sei_ctx* ctx, int kernel, double dt, int nsteps, const float* d
 int sei_sync(sei_ctx* ctx);
 /* Device-side duration of the last sei_run, milliseconds (CUDA events on the context stream). */
 int sei_last_run_ms(sei_ctx* ctx, double* ms);
+
+/* ---- dynamic rupture (built with fault_plane >= 0; order <= 4, i.e. at most 32 face points) ----
+ * Replaces DynamicRupture::spaceTimeInterpolation + FrictionSolver::evaluate + the DR branch of
+ * Neighbor::computeNeighborsIntegral (src/Kernels/DynamicRupture.cpp:57-168,
+ * src/DynamicRupture/FrictionLaws/FrictionSolver.h:38-44, src/Kernels/LinearCK/Neighbor.cpp:91-101).
+ * The step of SEI_KERNEL_ALL_DR is: ADER + local (storing the CK derivatives of fault cells),
+ * the fault kernel (interpolation at the Gauss-Legendre time points, friction, imposed state,
+ * nodal flux into both cells), the neighbour flux of the regular faces. */
+int sei_dr_setup(sei_ctx* ctx, const sei_rs_params* p, int64_t* nfaces);
+int sei_dr_num_points(int order);
+int64_t sei_dr_num_faces(const sei_ctx* ctx);
+/* Per face: cells [nf][2] (plus, minus), sides [nf][3] (plus side, minus side, face relation 1..3),
+ * TinvT / flux solvers [nf][81] column-major, impedances [nf][8] (zp, zs, zp', zs', eta_p, eta_s, 1/eta_s, 0). */
+int sei_dr_get_faces(sei_ctx* ctx, int32_t* cells, int8_t* sides, float* tinvt, float* flux_plus, float* flux_minus,
+                     double* impedance);
+int sei_dr_get_state(sei_ctx* ctx, int field, double* out /*[nf][npts]*/);
+int sei_dr_set_state(sei_ctx* ctx, int field, const double* in /*[nf][npts]*/);
+/* Imposed states of the last step, [nf][9][npts] each (points fastest). */
+int sei_dr_get_imposed(sei_ctx* ctx, float* plus, float* minus);
+/* Accumulated Newton iterations over all points and steps since the last reset. */
+int sei_dr_newton_iterations(sei_ctx* ctx, int64_t* total, int64_t* solves_points);
+int sei_dr_reset_counters(sei_ctx* ctx);
+/* Runs only the fault kernel (after a step that stored the derivatives). */
+int sei_dr_faces_step(sei_ctx* ctx, double dt);
+/* Slot of each fault cell in the derivative buffer ([n], -1 for cells without a fault face). */
+int sei_dr_get_slots(sei_ctx* ctx, int32_t* slots);
 
 /* Per-launch device timing: when on, every kernel launch of sei_run is bracketed by CUDA events on the
  * context stream; sei_kernel_times_ms sums the durations of the last sei_run per kernel kind. */

@@ -371,3 +371,112 @@ def cfl_timestep(coords: np.ndarray, vp: np.ndarray, order: int, cfl: float = 0.
         insphere = abs(alpha) / areas
         out[c] = cfl * 2.0 * insphere / (vp[c] * (2 * order - 1))
     return out
+
+
+# ---------------------------------------------------------------------------
+# Dynamic rupture (codegen/matrices/dr_stroud_matrices_{N}.json, DynamicRuptureMatrices.cpp)
+# ---------------------------------------------------------------------------
+def stroud_points(order):
+    """Stroud conical-product rule with order+1 points per direction on the face triangle.
+
+    First coordinate from Gauss-Jacobi(1, 0) nodes (descending), second from Gauss-Legendre
+    scaled by (1 - first); ordering and weights as codegen/matrices/dr_stroud_matrices_{N}.json.
+    """
+    from scipy.special import roots_jacobi, roots_legendre
+    n = order + 1
+    xj, wj = roots_jacobi(n, 1, 0)
+    xl, wl = roots_legendre(n)
+    pts, ws = [], []
+    for i in reversed(range(n)):
+        u = (1 + xj[i]) / 2
+        for j in range(n):
+            pts.append((u, (1 - u) * (1 - xl[j]) / 2))
+            ws.append(wj[i] / 4 * wl[j] / 2)
+    return np.array(pts), np.array(ws)
+
+
+@lru_cache(maxsize=None)
+def dr_matrices(order):
+    """V3mTo2n[side*4+rel] (npts x B), V3mTo2nTWDivM (B x npts), resample (npts x npts), points, weights.
+
+    rel 0 is the unrotated face (plus side); rel h >= 1 maps the points with orientation h - 1
+    (minus side, faceRelation = sideOrientation + 1, DynamicRuptureMatrices.cpp:159-165).
+    """
+    pts, ws = stroud_points(order)
+    ids = basis_indices3(order)
+    mass = global_matrices(order)["M"]
+    v3m, tw = [], []
+    for side in range(4):
+        for rel in range(4):
+            chi, tau = pts[:, 0], pts[:, 1]
+            if rel > 0:
+                chi, tau = orientation_map(rel - 1, chi, tau)
+            x, y, z = face_point(side, chi, tau)
+            V = np.array([tet_dubiner(*t, x, y, z) for t in ids]).T
+            v3m.append(V)
+            tw.append((V * ws[:, None]).T / mass[:, None])
+    ids2 = basis_indices2(order)
+    V2 = np.array([tri_dubiner(*t, pts[:, 0], pts[:, 1]) for t in ids2]).T
+    fm = (V2 * ws[:, None]).T @ V2
+    res = V2 @ np.linalg.solve(fm, (V2 * ws[:, None]).T)
+    return {"V3mTo2n": v3m, "V3mTo2nTWDivM": tw, "resample": res, "points": pts, "weights": ws}
+
+
+def gauss_legendre_time(order, dt):
+    """ShiftedGaussLegendre(order, 0, dt): points and weights on [0, dt]."""
+    x, w = leggauss(order)
+    return (x + 1) * dt / 2, w * dt / 2
+
+
+def friction_delta_t(points):
+    """FrictionSolver::computeDeltaT (FrictionSolver.cpp:20-37)."""
+    d = np.empty(len(points))
+    d[0] = points[0]
+    d[1:] = np.diff(points)
+    d[-1] += points[0]
+    return d
+
+
+def fault_face_data(coords, material, plus_face):
+    """Per fault face: TinvT, flux solvers and impedances (DynamicRuptureMatrices.cpp:290-476).
+
+    plus_face: [nf, 4] = (plus cell, plus side, minus cell, minus side).  The normal is the
+    outward normal of the plus face, tangent1 its first edge (MeshReader.cpp:160-200).
+    """
+    nf = plus_face.shape[0]
+    tinvt = np.zeros((nf, 9, 9))
+    fsp = np.zeros((nf, 9, 9))
+    fsm = np.zeros((nf, 9, 9))
+    imp = np.zeros((nf, 7))
+    for f in range(nf):
+        pc, ps, mc, ms = plus_face[f]
+        v = coords[pc]
+        a, b, c = (v[k] for k in FACE2NODES[ps])
+        nrm = np.cross(b - a, c - a)
+        nrm /= np.linalg.norm(nrm)
+        t1 = (b - a) / np.linalg.norm(b - a)
+        t2 = np.cross(nrm, t1)
+        T, Ti = rotation_matrices(nrm, t1, t2)
+        tinvt[f] = Ti.T
+
+        def area_vol(cell, side):
+            w = coords[cell]
+            aa, bb, cc = (w[k] for k in FACE2NODES[side])
+            area = 0.5 * np.linalg.norm(np.cross(bb - aa, cc - aa))
+            vol = abs(np.dot(w[3] - w[0], np.cross(w[1] - w[0], w[2] - w[0]))) / 6.0
+            return area, vol
+
+        ap, vp_ = area_vol(pc, ps)
+        am, vm_ = area_vol(mc, ms)
+        rp, mup, lp = material[pc]
+        rm, mum, lm = material[mc]
+        fsp[f] = (-2.0 * ap / (6.0 * vp_)) * coefficient_matrix_T(rp, mup, lp, 0) @ T.T
+        fsm[f] = (2.0 * am / (6.0 * vm_)) * coefficient_matrix_T(rm, mum, lm, 0) @ T.T
+        zp = rp * math.sqrt((lp + 2 * mup) / rp)
+        zs = rp * math.sqrt(mup / rp)
+        zpn = rm * math.sqrt((lm + 2 * mum) / rm)
+        zsn = rm * math.sqrt(mum / rm)
+        etap = 1.0 / (1.0 / zp + 1.0 / zpn)
+        etas = 1.0 / (1.0 / zs + 1.0 / zsn)
+        imp[f] = [zp, zs, zpn, zsn, etap, etas, 1.0 / zs + 1.0 / zsn]
+    return {"TinvT": tinvt, "fluxSolverPlus": fsp, "fluxSolverMinus": fsm, "imp": imp}

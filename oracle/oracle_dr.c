@@ -1,0 +1,449 @@
+/*
+ * CPU oracle, dynamic-rupture half (TEST INFRASTRUCTURE ONLY; compiled into liboracle_*.so
+ * together with oracle.c).  Float64 restatement of
+ *   projectToDR          codegen/kernels/dynamic_rupture.py:126-172 (QDR(s) = V3mTo2n(side, rel) .
+ *                        (sum_p coeffDR(s, p) dQ(p)) . TinvT), time points collocated as
+ *                        src/Solver/TimeStepping/TimeCluster.cpp:236-241
+ *   precompute stress    src/DynamicRupture/FrictionLaws/FrictionSolverCommon.h:146-200
+ *   FVW rate and state   src/DynamicRupture/FrictionLaws/GpuImpl/RateAndState.h:51-270,
+ *                        GpuImpl/FastVelocityWeakeningLaw.h:35-108, RateAndStateCommon.h:22-139
+ *                        (per-point Newton; the outer fixed point stops when every point of the
+ *                        face has converged, as the reference's warp-wide vote over one face)
+ *   state resampling     GpuImpl/FastVelocityWeakeningLaw.h:98-106 with the resample matrix
+ *   imposed state        FrictionSolverCommon.h:333-420
+ *   nodal flux           dynamic_rupture.py:174-190 (Q += V3mTo2nTWDivM(side, rel) . imposed . fluxSolver)
+ *   time sub-steps       src/DynamicRupture/FrictionLaws/FrictionSolver.cpp:20-37
+ *
+ * Layouts: per fault face, QInterpolated[ts][9][npts] (points fastest, as the reference's
+ * QInterpolated view), imposed state [9][npts]; 9x9 matrices column-major (q + 9 p);
+ * V3mTo2n[16][npts][B] (index side * 4 + rel, column-major npts x B), V3mTo2nTWDivM[16][B][npts].
+ * Friction state is float64.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifndef REAL
+#define REAL double
+#endif
+typedef REAL real;
+
+static int dr_nb3(int n) { return n * (n + 1) * (n + 2) / 6; }
+
+/* QInterpolated of one side for all time points from packed derivatives (layout of oracle.c). */
+void oracle_dr_interpolate(int order, int npts, int nts, int64_t nfaces, const real* derivs, const int32_t* cell,
+                           const int8_t* side, const int8_t* rel, const double* tinvt, const double* v3m,
+                           const double* coeff /*[nts][order]*/, real* qi /*[nfaces][nts][9][npts]*/) {
+  const int B = dr_nb3(order);
+  int dsz = 0;
+  for (int i = 0; i < order; ++i) dsz += dr_nb3(order - i) * 9;
+#pragma omp parallel
+  {
+    double* ts = (double*)malloc(sizeof(double) * (size_t)B * 9);
+    double* tr = (double*)malloc(sizeof(double) * (size_t)B * 9);
+#pragma omp for schedule(static)
+    for (int64_t f = 0; f < nfaces; ++f) {
+      const real* d = derivs + (size_t)cell[f] * dsz;
+      const double* V = v3m + (size_t)(side[f] * 4 + rel[f]) * npts * B;
+      const double* R = tinvt + (size_t)f * 81;
+      for (int s = 0; s < nts; ++s) {
+        memset(ts, 0, sizeof(double) * (size_t)B * 9);
+        size_t off = 0;
+        for (int i = 0; i < order; ++i) {
+          const int bi = dr_nb3(order - i);
+          for (int q = 0; q < 9; ++q)
+            for (int l = 0; l < bi; ++l) ts[l + (size_t)B * q] += coeff[s * order + i] * (double)d[off + l + (size_t)bi * q];
+          off += (size_t)bi * 9;
+        }
+        /* tr = ts . TinvT */
+        for (int p = 0; p < 9; ++p)
+          for (int l = 0; l < B; ++l) {
+            double v = 0;
+            for (int q = 0; q < 9; ++q) v += ts[l + (size_t)B * q] * R[q + 9 * p];
+            tr[l + (size_t)B * p] = v;
+          }
+        real* out = qi + ((size_t)f * nts + s) * 9 * npts;
+        for (int p = 0; p < 9; ++p)
+          for (int k = 0; k < npts; ++k) {
+            double v = 0;
+            for (int l = 0; l < B; ++l) v += V[k + (size_t)npts * l] * tr[l + (size_t)B * p];
+            out[k + (size_t)npts * p] = (real)v;
+          }
+      }
+    }
+    free(ts);
+    free(tr);
+  }
+}
+
+/* Friction parameters that are uniform over the fault (DRParameters); a is per point. */
+typedef struct {
+  double f0, b, v0, l, muw, vw;
+  double newton_tol, state_tol;
+  int max_newton, max_outer;
+} oracle_rs_params;
+
+/* Per-face impedances (DynamicRuptureMatrices.cpp:339-357). */
+typedef struct {
+  double zp, zs, zpn, zsn, etap, etas, inv_etas;
+} oracle_imp;
+
+static double sq(double x) { return x * x; }
+
+static double logsinh(double x, double c) {
+  const double sign = c >= 0 ? 1.0 : -1.0;
+  const double ac = fabs(c);
+  return ac + log(x / 2 * -sign * expm1(-2 * ac));
+}
+
+static double compute_cexp(double cexplog) { return cexplog > 0 ? exp(-cexplog) : exp(cexplog); }
+
+static double arsinhexp(double x, double explog, double e) {
+  int xexp = 0;
+  (void)frexp(x, &xexp);
+  const double log2 = 0.69314718055994530943;
+  if (explog + (xexp > 0 ? xexp : 0) * log2 > 10.0 || explog >= 50.0) {
+    if (explog <= 0) e = 1 / e;
+    const double xa = fabs(x);
+    const double xs = x >= 0 ? 1.0 : -1.0;
+    return xs * (explog + log(xa + sqrt(xa * xa + e * e)));
+  }
+  if (explog > 0) e = 1 / e;
+  return asinh(e * x);
+}
+
+static double arsinhexp_deriv(double x, double explog, double e) {
+  int xexp = 0;
+  (void)frexp(x, &xexp);
+  const double log2 = 0.69314718055994530943;
+  if (explog + (xexp > 0 ? xexp : 0) * log2 > 10.0 || explog >= 50.0) {
+    if (explog <= 0) e = 1 / e;
+    return 1 / sqrt(x * x + e * e);
+  }
+  if (explog > 0) e = 1 / e;
+  const double v = e * x;
+  return e / sqrt(1 + v * v);
+}
+
+static double state_update(const oracle_rs_params* P, double a, double psi_ref, double dt, double v) {
+  double lowv = P->f0 - (P->b - a) * log(v / P->v0);
+  if (lowv < 0) lowv = 0;
+  const double vv = v / P->vw;
+  const double v8 = sq(sq(sq(vv)));
+  const double fss = P->muw + (lowv - P->muw) / pow(1.0 + v8, 1.0 / 8.0);
+  const double psiss = a * logsinh(P->v0 / v * 2, fss / a);
+  const double pre = -v * (dt / P->l);
+  return psiss * -expm1(pre) + exp(pre) * psi_ref;
+}
+
+#define ALMOST_ZERO 1e-45
+
+/* Newton solve of g(V) = -(|sn| mu(V, psi) - tau) / eta_s - V = 0 from guess v0; returns the
+ * iteration count (number of updates made) and sets *conv.  With bail, the solve gives up as
+ * soon as |g| does not fall (used for the network's starting value). */
+static int newton(const oracle_rs_params* P, double a, double psi, double sn, double tau, double inv_etas,
+                  double guess, double* vout, double* muout, int* conv, int bail) {
+  const double clin = 0.5 / P->v0;
+  const double cexplog = psi / a;
+  const double cexp = compute_cexp(cexplog);
+  double v = guess;
+  double prev = 1e300;
+  for (int i = 0; i < P->max_newton; ++i) {
+    const double mu = a * arsinhexp(clin * v, cexplog, cexp);
+    const double g = -inv_etas * (fabs(sn) * mu - tau) - v;
+    if (fabs(g) < P->newton_tol) {
+      *vout = v;
+      *muout = mu;
+      *conv = 1;
+      return i;
+    }
+    if (bail && !(fabs(g) < prev)) {
+      *vout = v;
+      *muout = 0.0;
+      *conv = 0;
+      return i;
+    }
+    prev = fabs(g);
+    const double dmu = a * clin * arsinhexp_deriv(clin * v, cexplog, cexp);
+    const double dg = -inv_etas * (fabs(sn) * dmu) - 1.0;
+    v = v - g / dg;
+    if (v < ALMOST_ZERO) v = ALMOST_ZERO;
+  }
+  *vout = v;
+  *muout = 0.0;
+  *conv = 0;
+  return P->max_newton;
+}
+
+/* Warm-start network 5 -> 64 -> 64 -> 1 (tanh), float32: returns log10 of the guessed slip rate.
+ * Parameters W1[64][5], b1[64], W2[64][64], b2[64], W3[64], b3; norm[0..4] input shifts,
+ * norm[5..9] input scales, norm[10..11] output shift and scale. */
+#define MLP_H 64
+double oracle_mlp_forward(const float* w, const float* norm, double sn, double tau, double psi, double a, double b) {
+  const float x[5] = {(float)((sn - norm[0]) * norm[5]), (float)((tau - norm[1]) * norm[6]),
+                      (float)((psi - norm[2]) * norm[7]), (float)((a - norm[3]) * norm[8]),
+                      (float)((b - norm[4]) * norm[9])};
+  const float* W1 = w;
+  const float* b1 = W1 + MLP_H * 5;
+  const float* W2 = b1 + MLP_H;
+  const float* b2 = W2 + MLP_H * MLP_H;
+  const float* W3 = b2 + MLP_H;
+  const float b3 = W3[MLP_H];
+  float h1[MLP_H];
+  for (int j = 0; j < MLP_H; ++j) {
+    float s = b1[j];
+    for (int i = 0; i < 5; ++i) s = fmaf(W1[j * 5 + i], x[i], s);
+    h1[j] = tanhf(s);
+  }
+  float out = b3;
+  for (int j = 0; j < MLP_H; ++j) {
+    float s = b2[j];
+    for (int i = 0; i < MLP_H; ++i) s = fmaf(W2[j * MLP_H + i], h1[i], s);
+    out = fmaf(W3[j], tanhf(s), out);
+  }
+  return (double)out * norm[11] + norm[10];
+}
+
+/* Friction solve of all faces for one time step.  State arrays are [nfaces][npts] float64:
+ * psi, v1, v2, slip1, slip2, slip (accumulated magnitude), mu, traction1, traction2;
+ * init[nfaces][3][npts] holds sn0, tau1_0, tau2_0.  With mlp non-null the first Newton solve
+ * of every time point starts from the network's guess and falls back to the plain start
+ * (previous slip rate) when its residual does not fall.  newton_iters[nfaces][npts]
+ * accumulates the Newton iteration counts. */
+
+void oracle_dr_friction(int npts, int nts, int64_t nfaces, const oracle_rs_params* P, const oracle_imp* imp,
+                        const real* qip, const real* qim, const double* a, const double* init, double* psi,
+                        double* v1, double* v2, double* slip1, double* slip2, double* slip, double* mu,
+                        double* trac1, double* trac2, const double* deltat, const double* tweights,
+                        const double* resample, real* isp, real* ism, int64_t* newton_iters,
+                        const float* mlp, const float* mlp_norm) {
+#pragma omp parallel
+  {
+    double* buf = (double*)malloc(sizeof(double) * (size_t)npts * 12);
+    double* psib = buf;
+    double* vmag = buf + npts;
+    double* lsr = buf + 2 * npts;
+    double* sref = buf + 3 * npts;
+    double* taus = buf + 4 * npts;
+    double* sns = buf + 5 * npts;
+    double* vt = buf + 6 * npts;
+    double* dpsi = buf + 7 * npts;
+    double* isacc = (double*)malloc(sizeof(double) * 18 * (size_t)npts);
+    double* fs = (double*)malloc(sizeof(double) * 3 * (size_t)nts * npts);
+    double* tr = (double*)malloc(sizeof(double) * 2 * (size_t)nts * npts);
+    int* convo = (int*)malloc(sizeof(int) * (size_t)npts);
+#pragma omp for schedule(static)
+    for (int64_t f = 0; f < nfaces; ++f) {
+      const oracle_imp* im = imp + f;
+      const size_t fo = (size_t)f * npts;
+      /* precompute stress (etaPDamp = 1) */
+      for (int s = 0; s < nts; ++s) {
+        const real* P_ = qip + ((size_t)f * nts + s) * 9 * npts;
+        const real* M_ = qim + ((size_t)f * nts + s) * 9 * npts;
+        for (int k = 0; k < npts; ++k) {
+#define QP(q) ((double)P_[k + (size_t)npts * (q)])
+#define QM(q) ((double)M_[k + (size_t)npts * (q)])
+          fs[(0 * nts + s) * npts + k] = im->etap * (QM(6) - QP(6) + QP(0) / im->zp + QM(0) / im->zpn);
+          fs[(1 * nts + s) * npts + k] = im->etas * (QM(7) - QP(7) + QP(3) / im->zs + QM(3) / im->zsn);
+          fs[(2 * nts + s) * npts + k] = im->etas * (QM(8) - QP(8) + QP(5) / im->zs + QM(5) / im->zsn);
+        }
+      }
+      for (int k = 0; k < npts; ++k) psib[k] = psi[fo + k];
+      for (int s = 0; s < nts; ++s) {
+        const double dt = deltat[s];
+        for (int k = 0; k < npts; ++k) {
+          const double sn0 = init[(size_t)f * 3 * npts + k];
+          const double t10 = init[(size_t)f * 3 * npts + npts + k];
+          const double t20 = init[(size_t)f * 3 * npts + 2 * npts + k];
+          double sn = fs[(0 * nts + s) * npts + k] + sn0;
+          sns[k] = sn < 0 ? sn : 0.0;
+          sref[k] = psib[k];
+          const double tt1 = t10 + fs[(1 * nts + s) * npts + k];
+          const double tt2 = t20 + fs[(2 * nts + s) * npts + k];
+          taus[k] = sqrt(tt1 * tt1 + tt2 * tt2);
+          double vm = sqrt(v1[fo + k] * v1[fo + k] + v2[fo + k] * v2[fo + k]);
+          if (vm < ALMOST_ZERO) vm = ALMOST_ZERO;
+          vmag[k] = vm;
+          lsr[k] = vm;
+        }
+        for (int j = 0; j < P->max_outer; ++j) {
+          int all = 1;
+          for (int k = 0; k < npts; ++k) {
+            const double ak = a[fo + k];
+            psib[k] = state_update(P, ak, sref[k], dt, lsr[k]);
+            double vnew = 0, munew = 0;
+            int conv = 0;
+            if (mlp && j == 0) {
+              double lg = oracle_mlp_forward(mlp, mlp_norm, sns[k], taus[k], psib[k], ak, P->b);
+              lg = lg < -40.0 ? -40.0 : (lg > 3.0 ? 3.0 : lg);
+              newton_iters[fo + k] +=
+                  newton(P, ak, psib[k], sns[k], taus[k], im->inv_etas, pow(10.0, lg), &vnew, &munew, &conv, 1);
+            }
+            if (!conv)
+              newton_iters[fo + k] +=
+                  newton(P, ak, psib[k], sns[k], taus[k], im->inv_etas, vmag[k], &vnew, &munew, &conv, 0);
+            lsr[k] = 0.5 * (vmag[k] + vnew);
+            convo[k] = fabs(vmag[k] - vnew) < P->state_tol;
+            vmag[k] = vnew;
+            mu[fo + k] = munew;
+            all &= convo[k];
+          }
+          if (all) break;
+        }
+        for (int k = 0; k < npts; ++k) {
+          const double ak = a[fo + k];
+          psib[k] = state_update(P, ak, sref[k], dt, lsr[k]);
+          const double clin = 0.5 / P->v0;
+          const double cexplog = psib[k] / ak;
+          const double m = ak * arsinhexp(clin * vmag[k], cexplog, compute_cexp(cexplog));
+          mu[fo + k] = m;
+          const double strength = -m * sns[k];
+          const double t10 = init[(size_t)f * 3 * npts + npts + k];
+          const double t20 = init[(size_t)f * 3 * npts + 2 * npts + k];
+          const double st1 = fs[(1 * nts + s) * npts + k], st2 = fs[(2 * nts + s) * npts + k];
+          const double tt1 = t10 + st1, tt2 = t20 + st2;
+          slip[fo + k] += vmag[k] * dt;
+          const double div = strength + im->etas * vmag[k];
+          const double sr1 = vmag[k] * tt1 / div, sr2 = vmag[k] * tt2 / div;
+          const double tr1 = st1 - im->etas * sr1, tr2 = st2 - im->etas * sr2;
+          trac1[fo + k] = tr1;
+          trac2[fo + k] = tr2;
+          slip1[fo + k] += sr1 * dt;
+          slip2[fo + k] += sr2 * dt;
+          tr[(0 * nts + s) * npts + k] = tr1;
+          tr[(1 * nts + s) * npts + k] = tr2;
+          v1[fo + k] = sr1;
+          v2[fo + k] = sr2;
+        }
+      }
+      /* resample the state variable increment (FastVelocityWeakeningLaw.h:98-106) */
+      for (int k = 0; k < npts; ++k) dpsi[k] = psib[k] - psi[fo + k];
+      for (int k = 0; k < npts; ++k) {
+        double v = 0;
+        for (int j = 0; j < npts; ++j) v += resample[k + (size_t)npts * j] * dpsi[j];
+        vt[k] = psi[fo + k] + v;
+      }
+      for (int k = 0; k < npts; ++k) psi[fo + k] = vt[k];
+      /* imposed state */
+      memset(isacc, 0, sizeof(double) * 18 * (size_t)npts);
+      for (int s = 0; s < nts; ++s) {
+        const double w = tweights[s];
+        const real* P_ = qip + ((size_t)f * nts + s) * 9 * npts;
+        const real* M_ = qim + ((size_t)f * nts + s) * 9 * npts;
+        for (int k = 0; k < npts; ++k) {
+          const double sn = fs[(0 * nts + s) * npts + k];
+          const double t1 = tr[(0 * nts + s) * npts + k], t2 = tr[(1 * nts + s) * npts + k];
+          double* m_ = isacc;
+          double* p_ = isacc + 9 * npts;
+          m_[0 * npts + k] += w * sn;
+          m_[3 * npts + k] += w * t1;
+          m_[5 * npts + k] += w * t2;
+          m_[6 * npts + k] += w * (QM(6) - (sn - QM(0)) / im->zpn);
+          m_[7 * npts + k] += w * (QM(7) - (t1 - QM(3)) / im->zsn);
+          m_[8 * npts + k] += w * (QM(8) - (t2 - QM(5)) / im->zsn);
+          p_[0 * npts + k] += w * sn;
+          p_[3 * npts + k] += w * t1;
+          p_[5 * npts + k] += w * t2;
+          p_[6 * npts + k] += w * (QP(6) + (sn - QP(0)) / im->zp);
+          p_[7 * npts + k] += w * (QP(7) + (t1 - QP(3)) / im->zs);
+          p_[8 * npts + k] += w * (QP(8) + (t2 - QP(5)) / im->zs);
+#undef QP
+#undef QM
+        }
+      }
+      for (int i = 0; i < 9 * npts; ++i) {
+        ism[(size_t)f * 9 * npts + i] = (real)isacc[i];
+        isp[(size_t)f * 9 * npts + i] = (real)isacc[9 * npts + i];
+      }
+    }
+    free(buf);
+    free(isacc);
+    free(fs);
+    free(tr);
+    free(convo);
+  }
+}
+
+/* Q(cell) += V3mTo2nTWDivM(side, rel) . imposed . fluxSolver for one side of every face. */
+void oracle_dr_nodal_flux(int order, int npts, int64_t nfaces, const int32_t* cell, const int8_t* side,
+                          const int8_t* rel, const double* twdivm, const real* imposed, const double* fluxsolver,
+                          real* Q) {
+  const int B = dr_nb3(order);
+  for (int64_t f = 0; f < nfaces; ++f) {
+    const double* W = twdivm + (size_t)(side[f] * 4 + rel[f]) * B * npts;
+    const real* is = imposed + (size_t)f * 9 * npts;
+    const double* fsv = fluxsolver + (size_t)f * 81;
+    real* q = Q + (size_t)cell[f] * B * 9;
+    for (int p = 0; p < 9; ++p)
+      for (int l = 0; l < B; ++l) {
+        double v = 0;
+        for (int k = 0; k < npts; ++k) {
+          double g = 0;
+          for (int qq = 0; qq < 9; ++qq) g += (double)is[k + (size_t)npts * qq] * fsv[qq + 9 * p];
+          v += W[l + (size_t)B * k] * g;
+        }
+        q[l + (size_t)B * p] += (real)v;
+      }
+  }
+}
+
+/* Precompute / postcompute known-answer helpers (FrictionSolverCommon.h), exposed for the
+ * restated unit test of tests/DynamicRupture/FrictionLaws/FrictionSolverCommon.t.h. */
+void oracle_dr_precompute(int npts, int nts, const oracle_imp* im, const real* qip, const real* qim, double* out) {
+  for (int s = 0; s < nts; ++s)
+    for (int k = 0; k < npts; ++k) {
+      const real* P_ = qip + (size_t)s * 9 * npts;
+      const real* M_ = qim + (size_t)s * 9 * npts;
+      out[(0 * nts + s) * npts + k] = im->etap * (M_[6 * npts + k] - P_[6 * npts + k] + P_[k] / im->zp + M_[k] / im->zpn);
+      out[(1 * nts + s) * npts + k] =
+          im->etas * (M_[7 * npts + k] - P_[7 * npts + k] + P_[3 * npts + k] / im->zs + M_[3 * npts + k] / im->zsn);
+      out[(2 * nts + s) * npts + k] =
+          im->etas * (M_[8 * npts + k] - P_[8 * npts + k] + P_[5 * npts + k] / im->zs + M_[5 * npts + k] / im->zsn);
+    }
+}
+
+/* Imposed states from the stresses of every time point (FrictionSolverCommon.h:333-420);
+ * normal[nts][npts], t1/t2 are the new tractions [nts][npts]. */
+void oracle_dr_postcompute(int npts, int nts, const oracle_imp* im, const real* qip, const real* qim,
+                           const double* normal, const double* t1, const double* t2, const double* tweights, double* isp,
+                           double* ism) {
+  memset(isp, 0, sizeof(double) * 9 * (size_t)npts);
+  memset(ism, 0, sizeof(double) * 9 * (size_t)npts);
+  for (int s = 0; s < nts; ++s) {
+    const double w = tweights[s];
+    const real* P_ = qip + (size_t)s * 9 * npts;
+    const real* M_ = qim + (size_t)s * 9 * npts;
+    for (int k = 0; k < npts; ++k) {
+      const double sn = normal[s * npts + k], a1 = t1[s * npts + k], a2 = t2[s * npts + k];
+      ism[0 * npts + k] += w * sn;
+      ism[3 * npts + k] += w * a1;
+      ism[5 * npts + k] += w * a2;
+      ism[6 * npts + k] += w * (M_[6 * npts + k] - (sn - M_[0 * npts + k]) / im->zpn);
+      ism[7 * npts + k] += w * (M_[7 * npts + k] - (a1 - M_[3 * npts + k]) / im->zsn);
+      ism[8 * npts + k] += w * (M_[8 * npts + k] - (a2 - M_[5 * npts + k]) / im->zsn);
+      isp[0 * npts + k] += w * sn;
+      isp[3 * npts + k] += w * a1;
+      isp[5 * npts + k] += w * a2;
+      isp[6 * npts + k] += w * (P_[6 * npts + k] + (sn - P_[0 * npts + k]) / im->zp);
+      isp[7 * npts + k] += w * (P_[7 * npts + k] + (a1 - P_[3 * npts + k]) / im->zs);
+      isp[8 * npts + k] += w * (P_[8 * npts + k] + (a2 - P_[5 * npts + k]) / im->zs);
+    }
+  }
+}
+
+/* Newton root of one point for the unit tests (returns iterations; conv set). */
+int oracle_dr_newton_point(double a, double psi, double sn, double tau, double inv_etas, double v_start,
+                           const oracle_rs_params* P, double* v, int* conv) {
+  double mu = 0;
+  return newton(P, a, psi, sn, tau, inv_etas, v_start, v, &mu, conv, 0);
+}
+
+double oracle_dr_state_update(const oracle_rs_params* P, double a, double psi_ref, double dt, double v) {
+  return state_update(P, a, psi_ref, dt, v);
+}
+
+double oracle_dr_mu(const oracle_rs_params* P, double a, double psi, double v) {
+  const double cl = psi / a;
+  return a * arsinhexp(0.5 / P->v0 * v, cl, compute_cexp(cl));
+}

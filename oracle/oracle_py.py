@@ -4,6 +4,7 @@ Arrays follow the layouts documented in oracle/oracle.c.  Per-cell 9x9 operators
 passed as numpy [.., q, p] arrays and converted here to column-major (q + 9 p).
 """
 import ctypes as C
+import math
 import os
 import subprocess
 
@@ -105,3 +106,107 @@ class Oracle:
                             _p(np.ascontiguousarray(orient, dtype=np.int8)), _p(ft) if ft is not None else None,
                             _p(np.ascontiguousarray(coeffs, dtype=np.float64)), C.c_int(nsteps), _p(Iw))
         return Q
+
+
+# ---------------------------------------------------------------------------
+# Dynamic rupture (oracle_dr.c)
+# ---------------------------------------------------------------------------
+class RSParamsC(C.Structure):
+    _fields_ = [("f0", C.c_double), ("b", C.c_double), ("v0", C.c_double), ("l", C.c_double), ("muw", C.c_double),
+                ("vw", C.c_double), ("newton_tol", C.c_double), ("state_tol", C.c_double), ("max_newton", C.c_int),
+                ("max_outer", C.c_int)]
+
+
+
+STATE_FIELDS = ("psi", "v1", "v2", "slip1", "slip2", "slip", "mu", "trac1", "trac2")
+
+
+def dr_collocation(order, dt):
+    """Time points, weights, friction sub-steps and collocation coefficients t_s^p / p!."""
+    tp, tw = dg_setup.gauss_legendre_time(order, dt)
+    coll = np.array([[t ** p / math.factorial(p) for p in range(order)] for t in tp])
+    return tp, tw, dg_setup.friction_delta_t(tp), coll
+
+
+class DROracle:
+    """FP64 dynamic-rupture step of the oracle on a fault described by the product's face list."""
+
+    def __init__(self, order, faces, params, dtype=np.float64):
+        self.order = order
+        self.L = lib(dtype)
+        self.dtype = np.dtype(dtype)
+        m = dg_setup.dr_matrices(order)
+        self.npts = m["points"].shape[0]
+        self.v3m = np.ascontiguousarray(np.stack([np.asfortranarray(v).ravel(order="F") for v in m["V3mTo2n"]]))
+        self.tw = np.ascontiguousarray(np.stack([np.asfortranarray(v).ravel(order="F") for v in m["V3mTo2nTWDivM"]]))
+        self.res = np.ascontiguousarray(np.asfortranarray(m["resample"]).ravel(order="F"))
+        self.f = faces
+        self.P = RSParamsC(params["f0"], params["b"], params["v0"], params["l"], params["muw"], params["vw"],
+                           params["newton_tol"], params["state_tol"], params["max_newton"], params["max_outer"])
+        for fn in ("oracle_dr_interpolate", "oracle_dr_friction", "oracle_dr_nodal_flux", "oracle_dr_precompute"):
+            getattr(self.L, fn).restype = None
+
+    def interpolate(self, derivs_per_face, side, rel, coll):
+        """derivs_per_face: [nf, dsize] derivatives of the cell on this side."""
+        nf = derivs_per_face.shape[0]
+        nts = coll.shape[0]
+        out = np.zeros((nf, nts, 9, self.npts), self.dtype)
+        idx = np.arange(nf, dtype=np.int32)
+        tinvt = np.ascontiguousarray(np.swapaxes(self.f["TinvT"], -1, -2), np.float64)
+        self.L.oracle_dr_interpolate(self.order, self.npts, nts, C.c_int64(nf),
+                                     _p(np.ascontiguousarray(derivs_per_face, self.dtype)), _p(idx),
+                                     _p(np.ascontiguousarray(side, np.int8)), _p(np.ascontiguousarray(rel, np.int8)),
+                                     _p(tinvt), _p(self.v3m), _p(np.ascontiguousarray(coll, np.float64)), _p(out))
+        return out
+
+    def friction(self, qip, qim, state, a, init, deltat, tweights, mlp=None):
+        """Updates state (dict of [nf, npts] float64 arrays) in place; returns imposed states and iterations."""
+        nf = qip.shape[0]
+        nts = qip.shape[1]
+        imp = np.ascontiguousarray(self.f["imp"][:, :7], np.float64)
+        isp = np.zeros((nf, 9, self.npts), self.dtype)
+        ism = np.zeros((nf, 9, self.npts), self.dtype)
+        iters = np.zeros((nf, self.npts), np.int64)
+        for k in STATE_FIELDS:
+            state[k] = np.ascontiguousarray(state[k], np.float64)
+        w = n = None
+        if mlp is not None:
+            w = np.ascontiguousarray(mlp[0], np.float32)
+            n = np.ascontiguousarray(mlp[1], np.float32)
+        self.L.oracle_dr_friction(self.npts, nts, C.c_int64(nf), C.byref(self.P), _p(imp),
+                                  _p(np.ascontiguousarray(qip, self.dtype)), _p(np.ascontiguousarray(qim, self.dtype)),
+                                  _p(np.ascontiguousarray(a, np.float64)), _p(np.ascontiguousarray(init, np.float64)),
+                                  *[_p(state[k]) for k in STATE_FIELDS],
+                                  _p(np.ascontiguousarray(deltat, np.float64)),
+                                  _p(np.ascontiguousarray(tweights, np.float64)), _p(self.res), _p(isp), _p(ism),
+                                  _p(iters), _p(w) if w is not None else None, _p(n) if n is not None else None)
+        return isp, ism, iters
+
+    def nodal_flux(self, Q, cells, side, rel, imposed, flux):
+        Q = np.array(Q, dtype=self.dtype, order="C")
+        fl = np.ascontiguousarray(np.swapaxes(flux, -1, -2), np.float64)
+        self.L.oracle_dr_nodal_flux(self.order, self.npts, C.c_int64(cells.shape[0]),
+                                    _p(np.ascontiguousarray(cells, np.int32)), _p(np.ascontiguousarray(side, np.int8)),
+                                    _p(np.ascontiguousarray(rel, np.int8)), _p(self.tw),
+                                    _p(np.ascontiguousarray(imposed, self.dtype)), _p(fl), _p(Q))
+        return Q
+
+
+def dr_full_step(o, dro, Q, cells, faces, state, a, init, dt, mlp=None):
+    """One step of proxy kernel all_dr in FP64: ADER + local, fault, neighbour (the GPU's order)."""
+    order = o.order
+    ft = cells["face_type"]
+    coeffs = dg_setup.taylor_integrate(order, 0.0, dt)
+    star = cells["star"].astype(np.float64)
+    I, d = o.ader(np.asarray(Q, np.float64), star, coeffs, want_derivs=True)
+    Q = o.local(Q, I, star, cells["AplusT"].astype(np.float64), ft)
+    tp, tw, deltat, coll = dr_collocation(order, dt)
+    pc, mc = faces["cells"][:, 0], faces["cells"][:, 1]
+    ps, ms, rel = faces["sides"][:, 0], faces["sides"][:, 1], faces["sides"][:, 2]
+    qip = dro.interpolate(d[pc], ps, np.zeros_like(ps), coll)
+    qim = dro.interpolate(d[mc], ms, rel, coll)
+    isp, ism, iters = dro.friction(qip, qim, state, a, init, deltat, tw, mlp)
+    Q = dro.nodal_flux(Q, pc, ps, np.zeros_like(ps), isp, faces["fluxSolverPlus"])
+    Q = dro.nodal_flux(Q, mc, ms, rel, ism, faces["fluxSolverMinus"])
+    Q = o.neighbor(Q, I, cells["AminusT"].astype(np.float64), cells["neighbor"], cells["side"], cells["orient"], ft)
+    return Q, isp, ism, iters, (d, qip, qim)

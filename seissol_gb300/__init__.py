@@ -7,6 +7,8 @@ fallback: without the built library every entry point raises.
 """
 from .lib import (  # noqa: F401
     Context,
+    RSParams,
+    DR_FIELDS,
     SeiError,
     KERNELS,
     load_library,

@@ -208,3 +208,85 @@ def global_matrices(order: int) -> dict:
         fP.append(np.array([[float(_int_simplex(psi[m] * psih[n])) for n in range(F)] for m in range(F)]))
     return {"kDivM": kdivm, "kDivMT": kdivmt, "rT": rT, "fMrT": fMrT, "rDivM": rDivM, "fP": fP,
             "M": np.array([float(m) for m in mass]), "fM": np.array([float(m) for m in fmass])}
+
+
+def _poly_eval(p: Poly, pts: np.ndarray) -> np.ndarray:
+    """Evaluates a polynomial at points [n, nv]."""
+    out = np.zeros(pts.shape[0])
+    for k, v in p.t.items():
+        term = np.full(pts.shape[0], float(v))
+        for i, e in enumerate(k):
+            if e:
+                term = term * pts[:, i] ** e
+        out += term
+    return out
+
+
+def _gauss_jacobi(n, alpha, beta):
+    """Nodes and weights of Gauss-Jacobi on [-1, 1] by the Golub-Welsch eigenvalue method."""
+    k = np.arange(n, dtype=float)
+    ab = alpha + beta
+    diag = np.empty(n)
+    diag[0] = (beta - alpha) / (ab + 2)
+    kk = k[1:]
+    diag[1:] = (beta ** 2 - alpha ** 2) / ((2 * kk + ab) * (2 * kk + ab + 2))
+    kk = np.arange(1, n, dtype=float)
+    off = np.sqrt(4 * kk * (kk + alpha) * (kk + beta) * (kk + ab) / ((2 * kk + ab) ** 2 * (2 * kk + ab + 1) * (2 * kk + ab - 1)))
+    J = np.diag(diag) + np.diag(off, 1) + np.diag(off, -1)
+    x, vecs = np.linalg.eigh(J)
+    mu0 = 2 ** (ab + 1) * math.gamma(alpha + 1) * math.gamma(beta + 1) / math.gamma(ab + 2)
+    return x, mu0 * vecs[0] ** 2
+
+
+def stroud_rule(order):
+    """Conical-product points on the face triangle (order+1 per direction), the reference's ordering."""
+    n = order + 1
+    xj, wj = _gauss_jacobi(n, 1.0, 0.0)
+    xl, wl = _gauss_jacobi(n, 0.0, 0.0)
+    pts, ws = [], []
+    for i in reversed(range(n)):
+        u = (1 + xj[i]) / 2
+        for j in range(n):
+            pts.append((u, (1 - u) * (1 - xl[j]) / 2))
+            ws.append(wj[i] / 4 * wl[j] / 2)
+    return np.array(pts), np.array(ws)
+
+
+@lru_cache(maxsize=None)
+def dr_matrices(order: int) -> dict:
+    """Dynamic-rupture face matrices (codegen/matrices/dr_stroud_matrices_{N}.json).
+
+    V3mTo2n[side * 4 + rel]: 3D basis at the face quadrature points (npts x B); rel 0 is the
+    plus side, rel >= 1 the minus side with orientation rel - 1.  V3mTo2nTWDivM = M^-1 V^T W.
+    resample: L2 projection of point values onto the face basis, evaluated at the points.
+    """
+    pts, ws = stroud_rule(order)
+    phi = tet_basis(order)
+    psi = tri_basis(order)
+    mass = np.array([float(_int_simplex(p * p)) for p in phi])
+    v3m, tw = [], []
+    for side in range(4):
+        for rel in range(4):
+            chi, tau = pts[:, 0], pts[:, 1]
+            if rel == 1:
+                chi, tau = tau, chi
+            elif rel == 2:
+                chi, tau = 1 - chi - tau, tau
+            elif rel == 3:
+                chi, tau = chi, 1 - chi - tau
+            xyz = {0: (tau, chi, 0 * chi), 1: (chi, 0 * chi, tau), 2: (0 * chi, tau, chi),
+                   3: (1 - chi - tau, chi, tau)}[side]
+            P = np.stack(xyz, axis=1)
+            V = np.stack([_poly_eval(p, P) for p in phi], axis=1)
+            v3m.append(V)
+            tw.append((V * ws[:, None]).T / mass[:, None])
+    V2 = np.stack([_poly_eval(p, pts) for p in psi], axis=1)
+    fm = (V2 * ws[:, None]).T @ V2
+    res = V2 @ np.linalg.solve(fm, (V2 * ws[:, None]).T)
+    return {"V3mTo2n": v3m, "V3mTo2nTWDivM": tw, "resample": res, "points": pts, "weights": ws}
+
+
+def gauss_legendre01(n):
+    """Gauss-Legendre nodes and weights on [0, 1]."""
+    x, w = _gauss_jacobi(n, 0.0, 0.0)
+    return (x + 1) / 2, w / 2

@@ -100,11 +100,12 @@ def gen_order(order: int) -> str:
     a(f"""
 // Q[n][9][B] in/out (in place), I[n][9][B] out, star_nz[n][3][24], aplus[n][4][81] (column-major 9x9),
 // ftype[n][4] (1 = dynamic rupture: no local flux), coeffs[order] Taylor integration coefficients,
-// derivs: optional packed derivative output [n][kDerivSize] (nullptr to skip).
+// derivs: optional packed derivative output [slots][kDerivSize] (nullptr to skip); the slot of a
+// cell is dslot[cell] (-1: not stored), or the cell itself when dslot is nullptr.
 extern "C" __global__ void __launch_bounds__(288, 1)
 sei_local_o{order}(int n, float* __restrict__ Q, float* __restrict__ Iout, const float* __restrict__ star_nz,
                    const float* __restrict__ aplus, const unsigned char* __restrict__ ftype,
-                   SeiCoeffs coeffs, float* __restrict__ derivs) {{
+                   SeiCoeffs coeffs, float* __restrict__ derivs, const int* __restrict__ dslot) {{
   extern __shared__ float sm[];
   const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int cell = blockIdx.x * kCPB + lane;
@@ -130,8 +131,9 @@ sei_local_o{order}(int n, float* __restrict__ Q, float* __restrict__ Iout, const
   float I[kBp];
 #pragma unroll
   for (int k = 0; k < kBp; ++k) I[k] = coeffs.c[0] * z[k];
-  float* dcol = derivs ? derivs + (size_t)cl * kDerivSize + q * kB : nullptr;
-  if (dcol && valid) sei_store_col_scalar<kB>(dcol, z);""")
+  const int dsl = derivs ? (dslot ? __ldg(dslot + cl) : cl) : -1;
+  float* dbase = (dsl >= 0 && valid) ? derivs + (size_t)dsl * kDerivSize : nullptr;
+  if (dbase) sei_store_col_scalar<kB>(dbase + q * kB, z);""")
     off = B * NQ
     for i in range(1, order):
         bp, bc = nb3(order - i + 1), nb3(order - i)
@@ -155,7 +157,7 @@ sei_local_o{order}(int n, float* __restrict__ Q, float* __restrict__ Iout, const
             a("    }")
         a("    __syncthreads();")
         a(f"#pragma unroll\n    for (int k = 0; k < {bc}; ++k) {{ I[k] = fmaf(coeffs.c[{i}], zn[k], I[k]); z[k] = zn[k]; }}")
-        a(f"    if (dcol && valid) sei_store_col_scalar<{bc}>(derivs + (size_t)cl * kDerivSize + {off} + q * {bc}, zn);")
+        a(f"    if (dbase) sei_store_col_scalar<{bc}>(dbase + {off} + q * {bc}, zn);")
         off += bc * NQ
         a("  }")
     # volume
@@ -320,6 +322,46 @@ def write_all(outdir: str, orders=(4, 5, 6)) -> list:
     for o in orders:
         p = os.path.join(outdir, f"kernels_o{o}.cuh")
         src = gen_order(o)
+        if not os.path.exists(p) or open(p).read() != src:
+            with open(p, "w") as fh:
+                fh.write(src)
+        paths.append(p)
+    return paths
+
+
+def gen_dr_tables(order: int) -> str:
+    """Device tables of the dynamic-rupture face matrices for one order."""
+    from .basis import dr_matrices, gauss_legendre01
+    D = dr_matrices(order)
+    B = nb3(order)
+    npts = D["points"].shape[0]
+    glx, glw = gauss_legendre01(order)
+    L = [f"// Generated by seissol_gb300/codegen/gen_kernels.py: dynamic-rupture tables, order {order}.",
+         "#pragma once", f"namespace sei_dr_o{order} {{",
+         f"constexpr int kOrder = {order}, kB = {B}, kNP = {npts};"]
+
+    def arr(name, ty, vals, fmt):
+        L.append(f"__device__ const {ty} {name}[{len(vals)}] = {{" + ",".join(fmt(v) for v in vals) + "};")
+
+    f32 = lambda v: flit(v)
+    f64 = lambda v: float(v).hex()
+    # V3mTo2n[rel combo][k][l] row-major (point k, basis l)
+    arr("kV3m", "float", np.concatenate([m.ravel() for m in D["V3mTo2n"]]), f32)
+    # V3mTo2nTWDivM[rel combo][l][k] row-major (basis l, point k)
+    arr("kTW", "float", np.concatenate([m.ravel() for m in D["V3mTo2nTWDivM"]]), f32)
+    arr("kResample", "double", D["resample"].ravel(), f64)
+    arr("kGLx", "double", glx, f64)
+    arr("kGLw", "double", glw, f64)
+    L.append(f"}}  // namespace sei_dr_o{order}")
+    return "\n".join(L) + "\n"
+
+
+def write_dr_tables(outdir: str, orders=(4,)) -> list:
+    os.makedirs(outdir, exist_ok=True)
+    paths = []
+    for o in orders:
+        p = os.path.join(outdir, f"dr_tables_o{o}.cuh")
+        src = gen_dr_tables(o)
         if not os.path.exists(p) or open(p).read() != src:
             with open(p, "w") as fh:
                 fh.write(src)

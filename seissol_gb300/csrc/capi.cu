@@ -37,11 +37,24 @@ struct sei_ctx {
   // device arrays
   float *Q = nullptr, *I = nullptr, *derivs = nullptr, *star_nz = nullptr, *aplus = nullptr, *aminus = nullptr;
   int32_t* nbr = nullptr;
+  int32_t* dslot = nullptr;  // derivative slots (dynamic rupture): only fault cells store derivatives
   uint8_t *rel = nullptr, *ftype = nullptr;
   // host copies of what the context built (for sei_get_cells / sei_get_geometry)
   sei::HostMesh mesh;
   std::vector<float> h_star, h_aplus, h_aminus;
   bool has_mesh = false;
+  // dynamic rupture
+  sei::HostFault fault;
+  bool has_fault = false, dr_ready = false;
+  int64_t nslots = 0;  // rows of the derivative buffer
+  sei_rs_params rs{};
+  int npts = 0;
+  int32_t *d_pc = nullptr, *d_mc = nullptr, *d_pslot = nullptr, *d_mslot = nullptr, *d_iters = nullptr;
+  uint8_t *d_ps = nullptr, *d_ms = nullptr, *d_rel = nullptr;
+  float *d_tinvt = nullptr, *d_fsp = nullptr, *d_fsm = nullptr, *d_isp = nullptr, *d_ism = nullptr;
+  double *d_imp = nullptr, *d_state = nullptr;  // state: 13 fields x [nf][npts]
+  float* d_mlp = nullptr;
+  float mlp_norm[12] = {0};
   // per-launch timing (sei_set_profiling): one event before every launch plus one at the end
   bool profiling = false;
   std::vector<cudaEvent_t> prof_events;
@@ -76,6 +89,17 @@ void freeArrays(sei_ctx* c) {
   cudaFree(c->nbr);
   cudaFree(c->rel);
   cudaFree(c->ftype);
+  cudaFree(c->dslot);
+  for (void* p : {(void*)c->d_pc, (void*)c->d_mc, (void*)c->d_pslot, (void*)c->d_mslot, (void*)c->d_iters, (void*)c->d_ps,
+                  (void*)c->d_ms, (void*)c->d_rel, (void*)c->d_tinvt, (void*)c->d_fsp, (void*)c->d_fsm, (void*)c->d_isp,
+                  (void*)c->d_ism, (void*)c->d_imp, (void*)c->d_state, (void*)c->d_mlp})
+    cudaFree(p);
+  c->d_pc = c->d_mc = c->d_pslot = c->d_mslot = c->d_iters = nullptr;
+  c->d_ps = c->d_ms = c->d_rel = nullptr;
+  c->d_tinvt = c->d_fsp = c->d_fsm = c->d_isp = c->d_ism = c->d_mlp = nullptr;
+  c->d_imp = c->d_state = nullptr;
+  c->dslot = nullptr;
+  c->dr_ready = false;
   c->Q = c->I = c->derivs = c->star_nz = c->aplus = c->aminus = nullptr;
   c->nbr = nullptr;
   c->rel = c->ftype = nullptr;
@@ -93,8 +117,10 @@ int allocArrays(sei_ctx* c, int64_t n) {
             alloc((void**)&c->aminus, (size_t)n * 4 * 81 * sizeof(float)) &&
             alloc((void**)&c->nbr, (size_t)n * 4 * sizeof(int32_t)) && alloc((void**)&c->rel, (size_t)n * 4) &&
             alloc((void**)&c->ftype, (size_t)n * 4);
-  if (ok && c->cfg.store_derivatives)
+  if (ok && c->cfg.store_derivatives) {
     ok = alloc((void**)&c->derivs, (size_t)n * sei::derivativesSize(c->cfg.order) * sizeof(float));
+    c->nslots = n;
+  }
   if (!ok) {
     cudaGetLastError();
     freeArrays(c);
@@ -136,7 +162,7 @@ int uploadCells(sei_ctx* c, int64_t n, const float* star, const float* aplus, co
 }
 
 sei::DeviceArrays arrays(sei_ctx* c) {
-  return sei::DeviceArrays{(int)c->n, c->Q, c->I, c->derivs, c->star_nz, c->aplus, c->aminus, c->nbr, c->rel, c->ftype};
+  return sei::DeviceArrays{(int)c->n, c->Q, c->I, c->derivs, c->dslot, c->star_nz, c->aplus, c->aminus, c->nbr, c->rel, c->ftype};
 }
 
 void taylorCoeffs(int order, double dt, float* out) {
@@ -184,6 +210,78 @@ int launchNeighbor(sei_ctx* c, const sei::DeviceArrays& d) {
   return SEI_OK;
 }
 
+sei::DrArgs drArgs(sei_ctx* c, double dt) {
+  sei::DrArgs a{};
+  const int64_t nf = c->fault.nf, np = c->npts;
+  a.nfaces = (int)nf;
+  a.plus_cell = c->d_pc;
+  a.minus_cell = c->d_mc;
+  a.plus_side = c->d_ps;
+  a.minus_side = c->d_ms;
+  a.rel = c->d_rel;
+  a.plus_slot = c->d_pslot;
+  a.minus_slot = c->d_mslot;
+  a.derivs = c->derivs;
+  a.tinvt = c->d_tinvt;
+  a.fsp = c->d_fsp;
+  a.fsm = c->d_fsm;
+  a.imp = c->d_imp;
+  double* st = c->d_state;
+  auto field = [&](int k) { return st + (size_t)k * nf * np; };
+  a.psi = field(SEI_DR_PSI);
+  a.v1 = field(SEI_DR_SLIP_RATE1);
+  a.v2 = field(SEI_DR_SLIP_RATE2);
+  a.slip1 = field(SEI_DR_SLIP1);
+  a.slip2 = field(SEI_DR_SLIP2);
+  a.slip = field(SEI_DR_SLIP);
+  a.mu = field(SEI_DR_MU);
+  a.trac1 = field(SEI_DR_TRACTION1);
+  a.trac2 = field(SEI_DR_TRACTION2);
+  a.a = field(SEI_DR_A);
+  a.init = field(SEI_DR_SN0);  // sn0, tau1_0, tau2_0 are consecutive fields: [3][nf][npts]
+  a.isp = c->d_isp;
+  a.ism = c->d_ism;
+  a.newton_iters = c->d_iters;
+  a.Q = c->Q;
+  const sei_rs_params& r = c->rs;
+  a.f0 = r.f0;
+  a.b = r.b;
+  a.v0 = r.v0;
+  a.l = r.l;
+  a.muw = r.muw;
+  a.vw = r.vw;
+  a.newton_tol = r.newton_tol;
+  a.state_tol = r.state_tol;
+  a.max_newton = r.max_newton;
+  a.max_outer = r.max_outer;
+  // Gauss-Legendre time points on [0, dt] (TimeCluster.cpp:236-241), sub-steps (FrictionSolver.cpp:20-37)
+  const int N = c->cfg.order;
+  double x[8], w[8];
+  sei::gaussLegendre01(N, x, w);
+  for (int s = 0; s < N; ++s) {
+    const double t = x[s] * dt;
+    a.tweights[s] = w[s] * dt;
+    a.deltat[s] = s == 0 ? t : t - x[s - 1] * dt;
+    double v = 1.0;
+    for (int p = 0; p < N; ++p) {
+      a.coll[s][p] = (float)v;  // t^p / p!
+      v *= t / (p + 1);
+    }
+  }
+  a.deltat[N - 1] += x[0] * dt;
+  a.mlp = c->d_mlp;
+  for (int i = 0; i < 12; ++i) a.mlp_norm[i] = c->mlp_norm[i];
+  return a;
+}
+
+int launchDr(sei_ctx* c, double dt) {
+  if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up (sei_dr_setup)");
+  int rc = profMark(c, 2);
+  if (rc) return rc;
+  if (sei::launchDrFaces(c->cfg.order, drArgs(c, dt), c->stream) != 0) return fail(c, SEI_ERR_CUDA, "fault kernel launch failed");
+  return SEI_OK;
+}
+
 int runKernel(sei_ctx* c, int kernel, double dt, int steps) {
   float coeffs[8];
   taylorCoeffs(c->cfg.order, dt, coeffs);
@@ -200,7 +298,16 @@ int runKernel(sei_ctx* c, int kernel, double dt, int steps) {
         rc = launchLocal(c, d, coeffs);
         break;
       case SEI_KERNEL_NEIGHBOR:
+      case SEI_KERNEL_NEIGHBOR_DR:
         rc = launchNeighbor(c, d);
+        break;
+      case SEI_KERNEL_GODUNOV_DR:
+        rc = launchDr(c, dt);
+        break;
+      case SEI_KERNEL_ALL_DR:
+        rc = launchLocal(c, d, coeffs);
+        if (!rc) rc = launchDr(c, dt);
+        if (!rc) rc = launchNeighbor(c, d);
         break;
       default:
         return fail(c, SEI_ERR_UNSUPPORTED, "kernel not supported by this build");
@@ -271,6 +378,14 @@ int sei_build_periodic_cube(sei_ctx* c, const sei_cube_params* p, int64_t* ncell
   try {
     c->mesh = sei::HostMesh();
     sei::buildPeriodicCube(*p, c->mesh);
+    c->has_fault = false;
+    if (p->fault_plane >= 0) {
+      if (p->fault_plane < 1 || p->fault_plane > p->nx - 1)
+        throw std::invalid_argument("fault_plane must lie in 1..nx-1 (or -1 for no fault)");
+      sei::buildPlanarFault(c->mesh, p->fault_plane, p->h, c->fault);
+      sei::faultFaceData(c->mesh, c->fault);
+      c->has_fault = true;
+    }
     sei::buildOperators(c->mesh, c->h_star, c->h_aplus, c->h_aminus);
   } catch (const std::invalid_argument& e) {
     return fail(c, SEI_ERR_ARG, e.what());
@@ -393,7 +508,7 @@ int sei_get_derivatives(sei_ctx* c, float* derivs) {
   int rc = checkReady(c);
   if (rc) return rc;
   if (!c->derivs) return fail(c, SEI_ERR_STATE, "context created without store_derivatives");
-  SEI_CUDA(cudaMemcpyAsync(derivs, c->derivs, (size_t)c->n * sei::derivativesSize(c->cfg.order) * sizeof(float),
+  SEI_CUDA(cudaMemcpyAsync(derivs, c->derivs, (size_t)c->nslots * sei::derivativesSize(c->cfg.order) * sizeof(float),
                            cudaMemcpyDeviceToHost, c->stream));
   SEI_CUDA(cudaStreamSynchronize(c->stream));
   return SEI_OK;
@@ -417,7 +532,7 @@ int sei_compute_local_integral(sei_ctx* c) { return fail(c, SEI_ERR_UNSUPPORTED,
 int sei_evaluate_taylor(sei_ctx* c, const double* coeffs, float* out_device) {
   int rc = checkReady(c);
   if (rc) return rc;
-  if (!c->derivs) return fail(c, SEI_ERR_STATE, "context created without store_derivatives");
+  if (!c->derivs || c->dslot) return fail(c, SEI_ERR_STATE, "derivatives of all cells are not stored (store_derivatives off or fault slots)");
   if (!coeffs || !out_device) return fail(c, SEI_ERR_ARG, "null argument");
   float cf[8];
   for (int i = 0; i < c->cfg.order; ++i) cf[i] = (float)coeffs[i];
@@ -461,6 +576,186 @@ int sei_last_run_ms(sei_ctx* c, double* ms) {
   float f = 0;
   SEI_CUDA(cudaEventElapsedTime(&f, c->ev0, c->ev1));
   *ms = f;
+  return SEI_OK;
+}
+
+int sei_dr_num_points(int order) { return (order >= 2 && order <= 4) ? sei::drNumPoints(order) : 0; }
+
+int64_t sei_dr_num_faces(const sei_ctx* c) { return (c && c->has_fault) ? c->fault.nf : 0; }
+
+int sei_dr_setup(sei_ctx* c, const sei_rs_params* p, int64_t* nfaces) {
+  int rc = checkReady(c);
+  if (rc) return rc;
+  if (!p) return fail(c, SEI_ERR_ARG, "null parameters");
+  if (!c->has_fault) return fail(c, SEI_ERR_STATE, "mesh has no fault (fault_plane < 0)");
+  if (c->cfg.order > 4) return fail(c, SEI_ERR_UNSUPPORTED, "dynamic rupture is built for order <= 4 (<= 32 face points)");
+  if (!(p->a_min > 0) || p->a_max < p->a_min || !(p->v0 > 0) || !(p->l > 0) || !(p->vw > 0) || !(p->v_init > 0) ||
+      p->max_newton <= 0 || p->max_outer <= 0 || !(p->newton_tol > 0) || !(p->state_tol > 0) || p->sn_max > 0)
+    return fail(c, SEI_ERR_ARG, "invalid rate-and-state parameters");
+  c->rs = *p;
+  const int64_t nf = c->fault.nf;
+  const int np = sei::drNumPoints(c->cfg.order);
+  c->npts = np;
+  // host initial state
+  std::vector<double> st((size_t)13 * nf * np, 0.0);
+  auto field = [&](int k) { return st.data() + (size_t)k * nf * np; };
+  uint64_t z = p->seed;
+  auto uni = [&](double lo, double hi) {
+    z += 0x9E3779B97F4A7C15ull;
+    uint64_t x = z;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    x ^= x >> 31;
+    return lo + (hi - lo) * ((x >> 11) * (1.0 / 9007199254740992.0));
+  };
+  for (int64_t i = 0; i < nf * np; ++i) {
+    const double a = uni(p->a_min, p->a_max);
+    field(SEI_DR_A)[i] = a;
+    field(SEI_DR_SN0)[i] = uni(p->sn_min, p->sn_max);
+    field(SEI_DR_TAU1_0)[i] = uni(p->tau_min, p->tau_max);
+    field(SEI_DR_TAU2_0)[i] = 0.0;
+    field(SEI_DR_SLIP_RATE1)[i] = p->v_init;
+    field(SEI_DR_PSI)[i] = sei::fvwSteadyState(p->v_init, a, p->b, p->f0, p->v0, p->muw, p->vw);
+  }
+  // derivative slots: every fault cell stores its derivatives
+  std::vector<int32_t> slot(c->n, -1), ps(nf), ms(nf);
+  for (int64_t f = 0; f < nf; ++f) {
+    ps[f] = (int32_t)(2 * f);
+    ms[f] = (int32_t)(2 * f + 1);
+    slot[c->fault.plus_cell[f]] = ps[f];
+    slot[c->fault.minus_cell[f]] = ms[f];
+  }
+  auto dalloc = [&](void** ptr, size_t bytes) { return cudaMalloc(ptr, bytes) == cudaSuccess; };
+  const size_t dsz = (size_t)sei::derivativesSize(c->cfg.order) * sizeof(float);
+  cudaFree(c->derivs);
+  c->derivs = nullptr;
+  bool ok = dalloc((void**)&c->derivs, 2 * nf * dsz) && dalloc((void**)&c->dslot, c->n * 4) &&
+            dalloc((void**)&c->d_pc, nf * 4) && dalloc((void**)&c->d_mc, nf * 4) && dalloc((void**)&c->d_pslot, nf * 4) &&
+            dalloc((void**)&c->d_mslot, nf * 4) && dalloc((void**)&c->d_iters, nf * np * 4) &&
+            dalloc((void**)&c->d_ps, nf) && dalloc((void**)&c->d_ms, nf) && dalloc((void**)&c->d_rel, nf) &&
+            dalloc((void**)&c->d_tinvt, nf * 81 * 4) && dalloc((void**)&c->d_fsp, nf * 81 * 4) &&
+            dalloc((void**)&c->d_fsm, nf * 81 * 4) && dalloc((void**)&c->d_isp, nf * 9 * np * 4) &&
+            dalloc((void**)&c->d_ism, nf * 9 * np * 4) && dalloc((void**)&c->d_imp, nf * 8 * 8) &&
+            dalloc((void**)&c->d_state, st.size() * 8);
+  if (!ok) {
+    cudaGetLastError();
+    return fail(c, SEI_ERR_OOM, "device allocation for the fault failed");
+  }
+  const sei::HostFault& F = c->fault;
+  SEI_CUDA(cudaMemcpy(c->dslot, slot.data(), c->n * 4, cudaMemcpyHostToDevice));
+  SEI_CUDA(cudaMemcpy(c->d_pc, F.plus_cell.data(), nf * 4, cudaMemcpyHostToDevice));
+  SEI_CUDA(cudaMemcpy(c->d_mc, F.minus_cell.data(), nf * 4, cudaMemcpyHostToDevice));
+  SEI_CUDA(cudaMemcpy(c->d_pslot, ps.data(), nf * 4, cudaMemcpyHostToDevice));
+  SEI_CUDA(cudaMemcpy(c->d_mslot, ms.data(), nf * 4, cudaMemcpyHostToDevice));
+  SEI_CUDA(cudaMemcpy(c->d_ps, F.plus_side.data(), nf, cudaMemcpyHostToDevice));
+  SEI_CUDA(cudaMemcpy(c->d_ms, F.minus_side.data(), nf, cudaMemcpyHostToDevice));
+  SEI_CUDA(cudaMemcpy(c->d_rel, F.rel.data(), nf, cudaMemcpyHostToDevice));
+  SEI_CUDA(cudaMemcpy(c->d_tinvt, F.tinvt.data(), nf * 81 * 4, cudaMemcpyHostToDevice));
+  SEI_CUDA(cudaMemcpy(c->d_fsp, F.fsp.data(), nf * 81 * 4, cudaMemcpyHostToDevice));
+  SEI_CUDA(cudaMemcpy(c->d_fsm, F.fsm.data(), nf * 81 * 4, cudaMemcpyHostToDevice));
+  SEI_CUDA(cudaMemcpy(c->d_imp, F.imp.data(), nf * 8 * 8, cudaMemcpyHostToDevice));
+  SEI_CUDA(cudaMemcpy(c->d_state, st.data(), st.size() * 8, cudaMemcpyHostToDevice));
+  SEI_CUDA(cudaMemset(c->d_iters, 0, nf * np * 4));
+  SEI_CUDA(cudaMemset(c->d_isp, 0, nf * 9 * np * 4));
+  SEI_CUDA(cudaMemset(c->d_ism, 0, nf * 9 * np * 4));
+  SEI_CUDA(cudaMemset(c->derivs, 0, 2 * nf * dsz));
+  c->dr_ready = true;
+  c->nslots = 2 * nf;
+  if (nfaces) *nfaces = nf;
+  return SEI_OK;
+}
+
+int sei_dr_get_faces(sei_ctx* c, int32_t* cells, int8_t* sides, float* tinvt, float* flux_plus, float* flux_minus,
+                     double* impedance) {
+  if (!c) return SEI_ERR_ARG;
+  if (!c->has_fault) return fail(c, SEI_ERR_STATE, "mesh has no fault");
+  const sei::HostFault& F = c->fault;
+  for (int64_t f = 0; f < F.nf; ++f) {
+    if (cells) {
+      cells[2 * f] = F.plus_cell[f];
+      cells[2 * f + 1] = F.minus_cell[f];
+    }
+    if (sides) {
+      sides[3 * f] = (int8_t)F.plus_side[f];
+      sides[3 * f + 1] = (int8_t)F.minus_side[f];
+      sides[3 * f + 2] = (int8_t)F.rel[f];
+    }
+  }
+  if (tinvt) std::memcpy(tinvt, F.tinvt.data(), F.tinvt.size() * 4);
+  if (flux_plus) std::memcpy(flux_plus, F.fsp.data(), F.fsp.size() * 4);
+  if (flux_minus) std::memcpy(flux_minus, F.fsm.data(), F.fsm.size() * 4);
+  if (impedance) std::memcpy(impedance, F.imp.data(), F.imp.size() * 8);
+  return SEI_OK;
+}
+
+static int drField(sei_ctx* c, int field, double*& dev) {
+  if (!c) return SEI_ERR_ARG;
+  if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up");
+  if (field < 0 || field > 12) return fail(c, SEI_ERR_ARG, "unknown friction-state field");
+  dev = c->d_state + (size_t)field * c->fault.nf * c->npts;
+  return SEI_OK;
+}
+
+int sei_dr_get_state(sei_ctx* c, int field, double* out) {
+  double* dev = nullptr;
+  int rc = drField(c, field, dev);
+  if (rc) return rc;
+  if (!out) return fail(c, SEI_ERR_ARG, "null output");
+  SEI_CUDA(cudaMemcpyAsync(out, dev, (size_t)c->fault.nf * c->npts * 8, cudaMemcpyDeviceToHost, c->stream));
+  SEI_CUDA(cudaStreamSynchronize(c->stream));
+  return SEI_OK;
+}
+
+int sei_dr_set_state(sei_ctx* c, int field, const double* in) {
+  double* dev = nullptr;
+  int rc = drField(c, field, dev);
+  if (rc) return rc;
+  if (!in) return fail(c, SEI_ERR_ARG, "null input");
+  SEI_CUDA(cudaMemcpyAsync(dev, in, (size_t)c->fault.nf * c->npts * 8, cudaMemcpyHostToDevice, c->stream));
+  SEI_CUDA(cudaStreamSynchronize(c->stream));
+  return SEI_OK;
+}
+
+int sei_dr_get_imposed(sei_ctx* c, float* plus, float* minus) {
+  if (!c) return SEI_ERR_ARG;
+  if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up");
+  const size_t bytes = (size_t)c->fault.nf * 9 * c->npts * 4;
+  if (plus) SEI_CUDA(cudaMemcpyAsync(plus, c->d_isp, bytes, cudaMemcpyDeviceToHost, c->stream));
+  if (minus) SEI_CUDA(cudaMemcpyAsync(minus, c->d_ism, bytes, cudaMemcpyDeviceToHost, c->stream));
+  SEI_CUDA(cudaStreamSynchronize(c->stream));
+  return SEI_OK;
+}
+
+int sei_dr_newton_iterations(sei_ctx* c, int64_t* total, int64_t* points) {
+  if (!c || !total || !points) return SEI_ERR_ARG;
+  if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up");
+  std::vector<int32_t> it((size_t)c->fault.nf * c->npts);
+  SEI_CUDA(cudaMemcpyAsync(it.data(), c->d_iters, it.size() * 4, cudaMemcpyDeviceToHost, c->stream));
+  SEI_CUDA(cudaStreamSynchronize(c->stream));
+  int64_t s = 0;
+  for (int32_t v : it) s += v;
+  *total = s;
+  *points = (int64_t)it.size();
+  return SEI_OK;
+}
+
+int sei_dr_reset_counters(sei_ctx* c) {
+  if (!c) return SEI_ERR_ARG;
+  if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up");
+  SEI_CUDA(cudaMemsetAsync(c->d_iters, 0, (size_t)c->fault.nf * c->npts * 4, c->stream));
+  return SEI_OK;
+}
+
+int sei_dr_faces_step(sei_ctx* c, double dt) {
+  int rc = checkReady(c);
+  if (rc) return rc;
+  return launchDr(c, dt);
+}
+
+int sei_dr_get_slots(sei_ctx* c, int32_t* slots) {
+  if (!c || !slots) return SEI_ERR_ARG;
+  if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up");
+  SEI_CUDA(cudaMemcpy(slots, c->dslot, (size_t)c->n * 4, cudaMemcpyDeviceToHost));
   return SEI_OK;
 }
 

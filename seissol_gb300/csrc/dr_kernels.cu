@@ -1,0 +1,373 @@
+// Dynamic-rupture face kernel: one warp per fault face.
+//
+// Per face and time step (reference: src/Kernels/DynamicRupture.cpp:57-168 projectToDR,
+// src/DynamicRupture/FrictionLaws/GpuImpl/BaseFrictionSolver.h:133-236 evaluatePoint,
+// GpuImpl/RateAndState.h:51-270, GpuImpl/FastVelocityWeakeningLaw.h:35-108,
+// FrictionSolverCommon.h:146-200 and 333-420, codegen/kernels/dynamic_rupture.py:107-190):
+//   1. QInterpolated of both sides at every Gauss-Legendre time point: Taylor evaluation of
+//      the stored CK derivatives, rotation by TinvT, evaluation at the face quadrature points;
+//   2. fast-velocity-weakening rate-and-state friction per point (lane): Newton on the slip
+//      rate inside a fixed point on the state variable; residual, slip rate, state variable
+//      and slip accumulation in float64; the fixed point stops when all points of the face
+//      converged (warp vote);
+//   3. resampling of the state-variable increment (25x25 face projection);
+//   4. time-weighted imposed states of both sides;
+//   5. nodal flux Q += V3mTo2nTWDivM(side, rel) . imposed . fluxSolver into both cells.
+// An optional small network (5 -> 64 -> 64 -> 1, tanh) proposes the starting slip rate of the
+// first Newton solve of every time point; the plain start (previous slip rate) is used
+// whenever the residual does not fall.
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "internal.h"
+#include "_gen/dr_tables_o4.cuh"
+
+namespace {
+
+constexpr int kFacesPerBlock = 4;
+constexpr int kHidden = 64;
+constexpr int kMlpParams = kHidden * 5 + kHidden + kHidden * kHidden + kHidden + kHidden + 1;
+constexpr double kAlmostZero = 1e-45;
+
+__device__ __forceinline__ double logsinh(double x, double c) {
+  const double sign = c >= 0 ? 1.0 : -1.0;
+  const double ac = fabs(c);
+  return ac + log(x / 2 * -sign * expm1(-2 * ac));
+}
+
+__device__ __forceinline__ double cexpOf(double l) { return l > 0 ? exp(-l) : exp(l); }
+
+__device__ __forceinline__ bool largeBranch(double x, double explog) {
+  int xexp = 0;
+  (void)frexp(x, &xexp);
+  return explog + (xexp > 0 ? xexp : 0) * 0.69314718055994530943 > 10.0 || explog >= 50.0;
+}
+
+// asinh(x * exp(explog)) with the large-argument form of RateAndStateCommon.h:46-74.
+__device__ __forceinline__ double arsinhexp(double x, double explog, double e) {
+  if (largeBranch(x, explog)) {
+    if (explog <= 0) e = 1 / e;
+    const double xa = fabs(x);
+    return (x >= 0 ? 1.0 : -1.0) * (explog + log(xa + sqrt(xa * xa + e * e)));
+  }
+  if (explog > 0) e = 1 / e;
+  return asinh(e * x);
+}
+
+__device__ __forceinline__ double arsinhexpDeriv(double x, double explog, double e) {
+  if (largeBranch(x, explog)) {
+    if (explog <= 0) e = 1 / e;
+    return 1 / sqrt(x * x + e * e);
+  }
+  if (explog > 0) e = 1 / e;
+  const double v = e * x;
+  return e / sqrt(1 + v * v);
+}
+
+__device__ double stateUpdate(const sei::DrArgs& A, double a, double psiRef, double dt, double v) {
+  double lowv = A.f0 - (A.b - a) * log(v / A.v0);
+  lowv = lowv > 0 ? lowv : 0.0;
+  const double r = v / A.vw;
+  const double r2 = r * r, r4 = r2 * r2, r8 = r4 * r4;
+  const double fss = A.muw + (lowv - A.muw) / pow(1.0 + r8, 0.125);
+  const double psiss = a * logsinh(A.v0 / v * 2, fss / a);
+  const double pre = -v * (dt / A.l);
+  return psiss * -expm1(pre) + exp(pre) * psiRef;
+}
+
+struct NewtonOut {
+  double v, mu;
+  int iters;
+  bool conv;
+};
+
+// Newton on g(V) = -(|sn| mu(V) - tau) / eta_s - V from v; stops early when |g| grows if bail.
+__device__ NewtonOut newton(const sei::DrArgs& A, double a, double psi, double sn, double tau, double invEtaS,
+                            double v, bool bail) {
+  const double clin = 0.5 / A.v0;
+  const double cl = psi / a;
+  const double ce = cexpOf(cl);
+  double prev = 1e300;
+  for (int i = 0; i < A.max_newton; ++i) {
+    const double mu = a * arsinhexp(clin * v, cl, ce);
+    const double g = -invEtaS * (fabs(sn) * mu - tau) - v;
+    if (fabs(g) < A.newton_tol) return {v, mu, i, true};
+    if (bail && !(fabs(g) < prev)) return {v, 0.0, i, false};
+    prev = fabs(g);
+    const double dmu = a * clin * arsinhexpDeriv(clin * v, cl, ce);
+    const double dg = -invEtaS * (fabs(sn) * dmu) - 1.0;
+    v = v - g / dg;
+    v = v < kAlmostZero ? kAlmostZero : v;
+  }
+  return {v, 0.0, A.max_newton, false};
+}
+
+// Network guess of log10 of the converged slip rate.
+__device__ double mlpGuess(const float* __restrict__ w, const float* nrm, double sn, double tau, double psi, double a,
+                           double b) {
+  const float x[5] = {(float)((sn - nrm[0]) * nrm[5]), (float)((tau - nrm[1]) * nrm[6]), (float)((psi - nrm[2]) * nrm[7]),
+                      (float)((a - nrm[3]) * nrm[8]), (float)((b - nrm[4]) * nrm[9])};
+  const float* W1 = w;
+  const float* b1 = W1 + kHidden * 5;
+  const float* W2 = b1 + kHidden;
+  const float* b2 = W2 + kHidden * kHidden;
+  const float* W3 = b2 + kHidden;
+  const float b3 = W3[kHidden];
+  float h1[kHidden];
+#pragma unroll 8
+  for (int j = 0; j < kHidden; ++j) {
+    float s = b1[j];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) s = fmaf(W1[j * 5 + i], x[i], s);
+    h1[j] = tanhf(s);
+  }
+  float out = b3;
+#pragma unroll 4
+  for (int j = 0; j < kHidden; ++j) {
+    float s = b2[j];
+#pragma unroll
+    for (int i = 0; i < kHidden; ++i) s = fmaf(W2[j * kHidden + i], h1[i], s);
+    out = fmaf(W3[j], tanhf(s), out);
+  }
+  return (double)out * nrm[11] + nrm[10];
+}
+
+template <int N, int B, int NP>
+__global__ void __launch_bounds__(32 * kFacesPerBlock)
+    sei_dr_faces(sei::DrArgs A, const float* __restrict__ V3m, const float* __restrict__ TW,
+                 const double* __restrict__ R) {
+  constexpr int Bp = (B + 3) / 4 * 4;
+  constexpr int kQsel[6] = {0, 3, 5, 6, 7, 8};
+  int dsz = 0;
+#pragma unroll
+  for (int i = 0; i < N; ++i) dsz += (N - i) * (N - i + 1) * (N - i + 2) / 6 * 9;
+  __shared__ float sI[kFacesPerBlock][B * 9];
+  __shared__ float sJ[kFacesPerBlock][B * 9];
+  __shared__ float sG[kFacesPerBlock][NP * 9];
+  __shared__ double sD[kFacesPerBlock][32];
+  __shared__ float sW[kMlpParams];
+  const bool useMlp = A.mlp != nullptr;
+  if (useMlp)
+    for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) sW[i] = A.mlp[i];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int f = blockIdx.x * kFacesPerBlock + warp;
+  if (f >= A.nfaces) return;
+  const bool pt = lane < NP;
+  const int k = pt ? lane : 0;
+
+  // ---- 1. space-time interpolation of both sides (six quantities needed per point)
+  float qi[2][N][6];
+#pragma unroll
+  for (int sd = 0; sd < 2; ++sd) {
+    const int slot = sd == 0 ? A.plus_slot[f] : A.minus_slot[f];
+    const int combo = sd == 0 ? A.plus_side[f] * 4 : A.minus_side[f] * 4 + A.rel[f];
+    const float* d = A.derivs + (size_t)slot * dsz;
+    const float* T = A.tinvt + (size_t)f * 81;
+    const float* V = V3m + (size_t)combo * NP * B;
+#pragma unroll 1
+    for (int s = 0; s < N; ++s) {
+      for (int e = lane; e < B * 9; e += 32) {
+        const int l = e % B, q = e / B;
+        float v = 0.f;
+        int off = 0;
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          const int bi = (N - i) * (N - i + 1) * (N - i + 2) / 6;
+          if (l < bi) v = fmaf(A.coll[s][i], __ldg(d + off + l + bi * q), v);
+          off += bi * 9;
+        }
+        sI[warp][q * B + l] = v;
+      }
+      __syncwarp();
+      for (int e = lane; e < B * 9; e += 32) {
+        const int l = e % B, p = e / B;
+        float v = 0.f;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) v = fmaf(sI[warp][q * B + l], __ldg(T + q + 9 * p), v);
+        sJ[warp][p * B + l] = v;
+      }
+      __syncwarp();
+#pragma unroll
+      for (int j = 0; j < 6; ++j) {
+        float v = 0.f;
+        for (int l = 0; l < B; ++l) v = fmaf(__ldg(V + k * B + l), sJ[warp][kQsel[j] * B + l], v);
+        qi[sd][s][j] = v;
+      }
+      __syncwarp();
+    }
+  }
+
+  // ---- 2. friction (lanes < NP own one point each)
+  const size_t po = (size_t)f * NP + k;
+  const double* imp = A.imp + (size_t)f * 8;
+  const double zp = imp[0], zs = imp[1], zpn = imp[2], zsn = imp[3], etap = imp[4], etas = imp[5], invEtaS = imp[6];
+  const double a = pt ? A.a[po] : 0.01;
+  const size_t plane = (size_t)A.nfaces * NP;  // init holds sn0, tau1_0, tau2_0 as [3][nf][npts]
+  const double sn0 = pt ? A.init[po] : 0.0;
+  const double t10 = pt ? A.init[plane + po] : 0.0;
+  const double t20 = pt ? A.init[2 * plane + po] : 0.0;
+  double psiStored = pt ? A.psi[po] : 0.0;
+  double psib = psiStored;
+  double v1 = pt ? A.v1[po] : 1.0, v2 = pt ? A.v2[po] : 0.0;
+  double slip1 = pt ? A.slip1[po] : 0.0, slip2 = pt ? A.slip2[po] : 0.0, slip = pt ? A.slip[po] : 0.0;
+  double mu = 0.0, tr1 = 0.0, tr2 = 0.0;
+  int iters = 0;
+  double isP[6] = {0, 0, 0, 0, 0, 0}, isM[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll 1
+  for (int s = 0; s < N; ++s) {
+    const double dt = A.deltat[s];
+    // precompute stress (etaPDamp = 1): qi order N, T1, T2, U, V, W
+    const double fsn = etap * ((double)qi[1][s][3] - qi[0][s][3] + qi[0][s][0] / zp + qi[1][s][0] / zpn);
+    const double ft1 = etas * ((double)qi[1][s][4] - qi[0][s][4] + qi[0][s][1] / zs + qi[1][s][1] / zsn);
+    const double ft2 = etas * ((double)qi[1][s][5] - qi[0][s][5] + qi[0][s][2] / zs + qi[1][s][2] / zsn);
+    double sn = fsn + sn0;
+    sn = sn < 0 ? sn : 0.0;
+    const double sref = psib;
+    const double tt1 = t10 + ft1, tt2 = t20 + ft2;
+    const double tau = sqrt(tt1 * tt1 + tt2 * tt2);
+    double vmag = sqrt(v1 * v1 + v2 * v2);
+    vmag = vmag < kAlmostZero ? kAlmostZero : vmag;
+    double lsr = vmag;
+#pragma unroll 1
+    for (int j = 0; j < A.max_outer; ++j) {
+      bool conv = true;
+      if (pt) {
+        psib = stateUpdate(A, a, sref, dt, lsr);
+        NewtonOut r{};
+        bool done = false;
+        if (useMlp && j == 0) {
+          const double lg = mlpGuess(sW, A.mlp_norm, sn, tau, psib, a, A.b);
+          const double g0 = exp10(fmin(fmax(lg, -40.0), 3.0));
+          r = newton(A, a, psib, sn, tau, invEtaS, g0, true);
+          iters += r.iters;
+          done = r.conv;
+        }
+        if (!done) {
+          r = newton(A, a, psib, sn, tau, invEtaS, vmag, false);
+          iters += r.iters;
+        }
+        lsr = 0.5 * (vmag + r.v);
+        conv = fabs(vmag - r.v) < A.state_tol;
+        vmag = r.v;
+        mu = r.mu;
+      }
+      if (__all_sync(0xffffffffu, conv)) break;
+    }
+    if (pt) {
+      psib = stateUpdate(A, a, sref, dt, lsr);
+      const double clin = 0.5 / A.v0, cl = psib / a;
+      mu = a * arsinhexp(clin * vmag, cl, cexpOf(cl));
+      const double strength = -mu * sn;
+      slip += vmag * dt;
+      const double div = strength + etas * vmag;
+      v1 = vmag * tt1 / div;
+      v2 = vmag * tt2 / div;
+      tr1 = ft1 - etas * v1;
+      tr2 = ft2 - etas * v2;
+      slip1 += v1 * dt;
+      slip2 += v2 * dt;
+      const double w = A.tweights[s];
+      isM[0] += w * fsn;
+      isM[1] += w * tr1;
+      isM[2] += w * tr2;
+      isM[3] += w * (qi[1][s][3] - (fsn - qi[1][s][0]) / zpn);
+      isM[4] += w * (qi[1][s][4] - (tr1 - qi[1][s][1]) / zsn);
+      isM[5] += w * (qi[1][s][5] - (tr2 - qi[1][s][2]) / zsn);
+      isP[0] += w * fsn;
+      isP[1] += w * tr1;
+      isP[2] += w * tr2;
+      isP[3] += w * (qi[0][s][3] + (fsn - qi[0][s][0]) / zp);
+      isP[4] += w * (qi[0][s][4] + (tr1 - qi[0][s][1]) / zs);
+      isP[5] += w * (qi[0][s][5] + (tr2 - qi[0][s][2]) / zs);
+    }
+  }
+
+  // ---- 3. resample the state-variable increment over the face
+  sD[warp][lane] = pt ? psib - psiStored : 0.0;
+  __syncwarp();
+  if (pt) {
+    double v = 0.0;
+    for (int j = 0; j < NP; ++j) v += R[k * NP + j] * sD[warp][j];
+    A.psi[po] = psiStored + v;
+    A.v1[po] = v1;
+    A.v2[po] = v2;
+    A.slip1[po] = slip1;
+    A.slip2[po] = slip2;
+    A.slip[po] = slip;
+    A.mu[po] = mu;
+    A.trac1[po] = tr1;
+    A.trac2[po] = tr2;
+    A.newton_iters[po] += iters;
+  }
+
+  // ---- 4./5. imposed states and nodal flux, plus side then minus side
+#pragma unroll 1
+  for (int sd = 0; sd < 2; ++sd) {
+    const double* is = sd == 0 ? isP : isM;
+    float* isOut = (sd == 0 ? A.isp : A.ism) + (size_t)f * 9 * NP;
+    const float* fs = (sd == 0 ? A.fsp : A.fsm) + (size_t)f * 81;
+    if (pt) {
+      float full[9] = {(float)is[0], 0.f, 0.f, (float)is[1], 0.f, (float)is[2], (float)is[3], (float)is[4], (float)is[5]};
+#pragma unroll
+      for (int q = 0; q < 9; ++q) isOut[q * NP + k] = full[q];
+#pragma unroll
+      for (int p = 0; p < 9; ++p) {
+        float g = 0.f;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) g = fmaf(full[q], __ldg(fs + q + 9 * p), g);
+        sG[warp][k * 9 + p] = g;
+      }
+    }
+    __syncwarp();
+    const int cell = sd == 0 ? A.plus_cell[f] : A.minus_cell[f];
+    const int combo = sd == 0 ? A.plus_side[f] * 4 : A.minus_side[f] * 4 + A.rel[f];
+    const float* W = TW + (size_t)combo * B * NP;
+    float* q = A.Q + (size_t)cell * 9 * Bp;
+    for (int e = lane; e < B * 9; e += 32) {
+      const int l = e % B, p = e / B;
+      float v = 0.f;
+      for (int kk = 0; kk < NP; ++kk) v = fmaf(__ldg(W + l * NP + kk), sG[warp][kk * 9 + p], v);
+      q[p * Bp + l] += v;
+    }
+    __syncwarp();
+  }
+}
+
+template <int N, int B, int NP>
+int launch(const sei::DrArgs& a, const float* v3m, const float* tw, const double* res, void* stream) {
+  if (a.nfaces <= 0) return 0;
+  const int blocks = (a.nfaces + kFacesPerBlock - 1) / kFacesPerBlock;
+  sei_dr_faces<N, B, NP><<<blocks, 32 * kFacesPerBlock, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <typename T>
+const T* symbolAddress(const T& sym) {
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, sym) != cudaSuccess) return nullptr;
+  return static_cast<const T*>(p);
+}
+
+}  // namespace
+
+namespace sei {
+
+int drNumPoints(int order) { return (order + 1) * (order + 1); }
+
+int launchDrFaces(int order, const DrArgs& a, void* stream) {
+  // One lane per face point: built for order 4 (25 points).  Device addresses of the
+  // generated tables are looked up here (host code may not take them directly).
+  void *v = nullptr, *t = nullptr, *r = nullptr;
+  switch (order) {
+    case 4:
+      if (cudaGetSymbolAddress(&v, sei_dr_o4::kV3m) || cudaGetSymbolAddress(&t, sei_dr_o4::kTW) ||
+          cudaGetSymbolAddress(&r, sei_dr_o4::kResample))
+        return -1;
+      return launch<4, 20, 25>(a, (const float*)v, (const float*)t, (const double*)r, stream);
+    default:
+      return -1;
+  }
+}
+
+}  // namespace sei

@@ -42,7 +42,8 @@ struct DeviceArrays {
   int n;
   float* Q;
   float* I;
-  float* derivs;  // nullable
+  float* derivs;        // nullable
+  const int32_t* dslot;  // nullable: derivative slot per cell (-1 none); nullptr = slot is the cell
   const float* star_nz;
   const float* aplus;
   const float* aminus;
@@ -63,4 +64,56 @@ struct OrderKernels {
 
 bool kernelsForOrder(int order, OrderKernels& out);
 
+}  // namespace sei
+
+namespace sei {
+// Device arguments of the dynamic-rupture face kernel (passed by value).
+struct DrArgs {
+  int nfaces;
+  const int32_t* plus_cell;
+  const int32_t* minus_cell;
+  const uint8_t* plus_side;
+  const uint8_t* minus_side;
+  const uint8_t* rel;  // minus-side face relation 1..3 (plus side uses 0)
+  const int32_t* plus_slot;
+  const int32_t* minus_slot;
+  const float* derivs;  // [slots][derivativesSize]
+  const float* tinvt;   // [nf][81] column-major
+  const float* fsp;     // flux solvers [nf][81]
+  const float* fsm;
+  const double* imp;   // [nf][8]: zp, zs, zpn, zsn, etap, etas, inv_etas, unused
+  const double* a;     // [nf][npts]
+  const double* init;  // [3][nf][npts]: sn0, tau1_0, tau2_0
+  double *psi, *v1, *v2, *slip1, *slip2, *slip, *mu, *trac1, *trac2;  // [nf][npts]
+  float* isp;  // imposed states [nf][9][npts]
+  float* ism;
+  int32_t* newton_iters;  // [nf][npts], accumulated
+  float* Q;               // DOFs [n][9][Bp] (nodal flux target)
+  double f0, b, v0, l, muw, vw, newton_tol, state_tol;
+  int max_newton, max_outer;
+  double deltat[8], tweights[8];
+  float coll[8][8];     // collocation coefficients t_s^p / p! of the time points
+  const float* mlp;     // warm-start network parameters (nullptr: plain Newton)
+  float mlp_norm[12];   // input shift/scale and output shift/scale of the network
+};
+int launchDrFaces(int order, const DrArgs& a, void* stream);
+int drNumPoints(int order);
+}  // namespace sei
+
+namespace sei {
+// Planar fault of a periodic cube: faces on the plane x = plane * h.  The plus side is the
+// cell on the -x side (the reference point lies there), so the fault normal is +x
+// (src/Geometry/MeshReader.cpp:160-200).
+struct HostFault {
+  int64_t nf = 0;
+  std::vector<int32_t> plus_cell, minus_cell;
+  std::vector<uint8_t> plus_side, minus_side, rel;  // rel = orientation of the plus side + 1
+  std::vector<float> tinvt, fsp, fsm;               // [nf][81] column-major
+  std::vector<double> imp;                          // [nf][8]
+};
+void buildPlanarFault(HostMesh& m, int plane, double h, HostFault& f);
+void faultFaceData(const HostMesh& m, HostFault& f);
+// Steady-state state variable of the fast-velocity-weakening law at slip rate v.
+double fvwSteadyState(double v, double a, double b, double f0, double v0, double muw, double vw);
+void gaussLegendre01(int n, double* x, double* w);
 }  // namespace sei

@@ -26,7 +26,7 @@ int launchLocal(const sei::DeviceArrays& d, const float* coeffs, void* stream) {
     return -1;
   const int blocks = (d.n + K::kCPB - 1) / K::kCPB;
   K::SEI_CAT(sei_local_o, SEI_ORDER)<<<blocks, 288, smem, (cudaStream_t)stream>>>(
-      d.n, d.Q, d.I, d.star_nz, d.aplus, d.ftype, toCoeffs(coeffs), d.derivs);
+      d.n, d.Q, d.I, d.star_nz, d.aplus, d.ftype, toCoeffs(coeffs), d.derivs, d.dslot);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

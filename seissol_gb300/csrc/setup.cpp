@@ -17,6 +17,7 @@
 #include <cmath>
 #include <map>
 #include <stdexcept>
+#include <vector>
 
 namespace sei {
 
@@ -220,14 +221,22 @@ void buildPeriodicCube(const sei_cube_params& p, HostMesh& m) {
       if (dot(cross(sub(b, a), sub(c, a)), sub(d, a)) < 0)
         for (int k = 0; k < 3; ++k) std::swap(tets[par][t][2][k], tets[par][t][3][k]);
     }
-  // Cells ordered by (parity, tet type, cube): equal face relations are contiguous.
+  // Cell order: the cubes of each parity are listed in (k, j, i) order and cut into chunks of
+  // 32; chunk c emits, for parity 0 then 1 and tet type 0..4, the 32 cells of that type.  A
+  // 32-cell CTA therefore holds one tet type (uniform face relations), and consecutive CTAs
+  // cover neighbouring cubes, so neighbour data is reused from L2.
+  std::vector<std::array<int, 3>> cubes[2];
+  for (int k = 0; k < p.nz; ++k)
+    for (int j = 0; j < p.ny; ++j)
+      for (int i = 0; i < p.nx; ++i) cubes[(i + j + k) % 2].push_back({i, j, k});
+  const size_t chunks = (cubes[0].size() + 31) / 32;
   int64_t cell = 0;
-  for (int par = 0; par < 2; ++par)
-    for (int t = 0; t < 5; ++t)
-      for (int k = 0; k < p.nz; ++k)
-        for (int j = 0; j < p.ny; ++j)
-          for (int i = 0; i < p.nx; ++i) {
-            if ((i + j + k) % 2 != par) continue;
+  for (size_t ch = 0; ch < chunks; ++ch)
+    for (int par = 0; par < 2; ++par)
+      for (int t = 0; t < 5; ++t)
+        for (size_t mi = ch * 32; mi < std::min(cubes[par].size(), ch * 32 + 32); ++mi) {
+          const int i = cubes[par][mi][0], j = cubes[par][mi][1], k = cubes[par][mi][2];
+          {
             for (int v = 0; v < 4; ++v) {
               const int gi = i + tets[par][t][v][0], gj = j + tets[par][t][v][1], gk = k + tets[par][t][v][2];
               m.topo[cell * 4 + v] = (gi % p.nx) + (int64_t)p.nx * ((gj % p.ny) + (int64_t)p.ny * (gk % p.nz));
@@ -237,6 +246,7 @@ void buildPeriodicCube(const sei_cube_params& p, HostMesh& m) {
             }
             ++cell;
           }
+        }
   Rng rng(p.seed);
   for (int64_t c = 0; c < m.n; ++c) {
     double rho = p.rho, vp = p.vp, vs = p.vs;
@@ -361,6 +371,130 @@ void seedDofs(int64_t n, int order, uint64_t seed, std::vector<float>& dofs) {
   for (int64_t c = 0; c < n; ++c)
     for (int q = 0; q < 9; ++q)
       for (int k = 0; k < b; ++k) dofs[(c * 9 + q) * bp + k] = static_cast<float>(rng.uniform(-1.0, 1.0));
+}
+
+}  // namespace sei
+
+namespace sei {
+
+void buildPlanarFault(HostMesh& m, int plane, double h, HostFault& F) {
+  const double xf = plane * h;
+  const int kMissing[4] = {3, 2, 1, 0};  // FACE2MISSINGNODE
+  F = HostFault();
+  std::vector<int> drCount(m.n, 0);
+  for (int64_t c = 0; c < m.n; ++c)
+    for (int f = 0; f < 4; ++f) {
+      bool on = true;
+      for (int k = 0; k < 3; ++k) on = on && std::fabs(m.coords[c * 12 + kFace2Nodes[f][k] * 3] - xf) < 1e-9 * h;
+      if (!on || m.coords[c * 12 + kMissing[f] * 3] >= xf) continue;  // plus side: rest of the cell at x < xf
+      const int32_t d = m.nbr[c * 4 + f];
+      if (d < 0) continue;
+      const int j = m.side[c * 4 + f];
+      F.plus_cell.push_back((int32_t)c);
+      F.plus_side.push_back((uint8_t)f);
+      F.minus_cell.push_back(d);
+      F.minus_side.push_back((uint8_t)j);
+      F.rel.push_back((uint8_t)(m.orient[c * 4 + f] + 1));
+      m.ftype[c * 4 + f] = 1;
+      m.ftype[(int64_t)d * 4 + j] = 1;
+      ++drCount[c];
+      ++drCount[d];
+    }
+  F.nf = (int64_t)F.plus_cell.size();
+  for (int64_t c = 0; c < m.n; ++c)
+    if (drCount[c] > 1) throw std::invalid_argument("a cell with more than one dynamic-rupture face is not supported");
+  if (F.nf == 0) throw std::invalid_argument("fault plane has no faces (plane index outside the mesh?)");
+}
+
+void faultFaceData(const HostMesh& m, HostFault& F) {
+  F.tinvt.assign(F.nf * 81, 0.f);
+  F.fsp.assign(F.nf * 81, 0.f);
+  F.fsm.assign(F.nf * 81, 0.f);
+  F.imp.assign(F.nf * 8, 0.0);
+  auto cellVec = [&](int64_t c, int k) {
+    return Vec3{m.coords[c * 12 + k * 3], m.coords[c * 12 + k * 3 + 1], m.coords[c * 12 + k * 3 + 2]};
+  };
+  auto areaVolume = [&](int64_t c, int side, double& area, double& vol) {
+    const Vec3 a = cellVec(c, kFace2Nodes[side][0]), b = cellVec(c, kFace2Nodes[side][1]), cc = cellVec(c, kFace2Nodes[side][2]);
+    area = 0.5 * norm(cross(sub(b, a), sub(cc, a)));
+    vol = std::fabs(dot(sub(cellVec(c, 3), cellVec(c, 0)), cross(sub(cellVec(c, 1), cellVec(c, 0)), sub(cellVec(c, 2), cellVec(c, 0))))) / 6.0;
+  };
+  for (int64_t f = 0; f < F.nf; ++f) {
+    const int64_t pc = F.plus_cell[f], mc = F.minus_cell[f];
+    const int ps = F.plus_side[f], ms = F.minus_side[f];
+    const Vec3 a = cellVec(pc, kFace2Nodes[ps][0]), b = cellVec(pc, kFace2Nodes[ps][1]), cc = cellVec(pc, kFace2Nodes[ps][2]);
+    Vec3 nrm = cross(sub(b, a), sub(cc, a));
+    nrm = scale(nrm, 1.0 / norm(nrm));
+    Vec3 t1 = sub(b, a);
+    t1 = scale(t1, 1.0 / norm(t1));
+    const Vec3 t2 = cross(nrm, t1);
+    Mat9 T, Ti;
+    rotation(nrm, t1, t2, T, Ti);
+    for (int i = 0; i < 9; ++i)
+      for (int j = 0; j < 9; ++j) F.tinvt[f * 81 + i + 9 * j] = (float)Ti[j * 9 + i];  // TinvT(i, j) = Tinv(j, i)
+    double ap, vp, am, vm;
+    areaVolume(pc, ps, ap, vp);
+    areaVolume(mc, ms, am, vm);
+    const double* mp = &m.material[pc * 3];
+    const double* mm = &m.material[mc * 3];
+    Mat9 atp, atm;
+    coefficientMatrixT(mp[0], mp[1], mp[2], 0, atp);
+    coefficientMatrixT(mm[0], mm[1], mm[2], 0, atm);
+    const double sp = -2.0 * ap / (6.0 * vp), sm = 2.0 * am / (6.0 * vm);
+    // fluxSolver(q, p) = scale * sum_k A^T(q, k) T(p, k)  (dynamic_rupture.py rotateFluxMatrix)
+    for (int q = 0; q < 9; ++q)
+      for (int p = 0; p < 9; ++p) {
+        double vpv = 0, vmv = 0;
+        for (int k = 0; k < 9; ++k) {
+          vpv += atp[q * 9 + k] * T[p * 9 + k];
+          vmv += atm[q * 9 + k] * T[p * 9 + k];
+        }
+        F.fsp[f * 81 + q + 9 * p] = (float)(sp * vpv);
+        F.fsm[f * 81 + q + 9 * p] = (float)(sm * vmv);
+      }
+    const double zp = std::sqrt(mp[0] * (mp[2] + 2 * mp[1])), zs = std::sqrt(mp[0] * mp[1]);
+    const double zpn = std::sqrt(mm[0] * (mm[2] + 2 * mm[1])), zsn = std::sqrt(mm[0] * mm[1]);
+    double* im = &F.imp[f * 8];
+    im[0] = zp;
+    im[1] = zs;
+    im[2] = zpn;
+    im[3] = zsn;
+    im[4] = 1.0 / (1.0 / zp + 1.0 / zpn);
+    im[5] = 1.0 / (1.0 / zs + 1.0 / zsn);
+    im[6] = 1.0 / zs + 1.0 / zsn;
+  }
+}
+
+double fvwSteadyState(double v, double a, double b, double f0, double v0, double muw, double vw) {
+  double lowv = f0 - (b - a) * std::log(v / v0);
+  lowv = lowv > 0 ? lowv : 0.0;
+  const double r = v / vw;
+  const double fss = muw + (lowv - muw) / std::pow(1.0 + std::pow(r, 8.0), 0.125);
+  const double c = fss / a;
+  const double sign = c >= 0 ? 1.0 : -1.0, ac = std::fabs(c);
+  return a * (ac + std::log(v0 / v * 2 / 2 * -sign * std::expm1(-2 * ac)));
+}
+
+void gaussLegendre01(int n, double* x, double* w) {
+  const double pi = 3.14159265358979323846;
+  for (int i = 0; i < n; ++i) {
+    double z = std::cos(pi * (i + 0.75) / (n + 0.5)), dp = 1;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1, p1 = z;
+      for (int k = 2; k <= n; ++k) {
+        const double p2 = ((2 * k - 1) * z * p1 - (k - 1) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      if (n == 1) p1 = z, p0 = 1;
+      dp = n * (z * p1 - p0) / (z * z - 1);
+      const double dz = p1 / dp;
+      z -= dz;
+      if (std::fabs(dz) < 1e-16) break;
+    }
+    x[n - 1 - i] = 0.5 * (z + 1);  // ascending on [0, 1]
+    w[n - 1 - i] = 1.0 / ((1 - z * z) * dp * dp);
+  }
 }
 
 }  // namespace sei

@@ -34,7 +34,28 @@ class _Config(C.Structure):
 
 class _CubeParams(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("h", C.c_double), ("rho", C.c_double),
-                ("vp", C.c_double), ("vs", C.c_double), ("perturb", C.c_double), ("seed", C.c_uint64)]
+                ("vp", C.c_double), ("vs", C.c_double), ("perturb", C.c_double), ("seed", C.c_uint64),
+                ("fault_plane", C.c_int)]
+
+
+class RSParams(C.Structure):
+    """sei_rs_params: fast-velocity-weakening rate-and-state friction and the seeded fault state."""
+    _fields_ = [(n, C.c_double) for n in ("f0", "b", "v0", "l", "muw", "vw", "a_min", "a_max", "sn_min", "sn_max",
+                                          "tau_min", "tau_max", "v_init", "newton_tol", "state_tol")] + \
+               [("max_newton", C.c_int), ("max_outer", C.c_int), ("seed", C.c_uint64)]
+
+    @classmethod
+    def fault_config(cls, seed=7, **kw):
+        """The rate-and-state set-up of the planar-fault workload (MPa as Pa)."""
+        d = dict(f0=0.6, b=0.014, v0=1e-6, l=0.02, muw=0.1, vw=0.1, a_min=0.008, a_max=0.02, sn_min=-120e6,
+                 sn_max=-40e6, tau_min=20e6, tau_max=75e6, v_init=1e-16, newton_tol=1e-8, state_tol=1e-8,
+                 max_newton=60, max_outer=10, seed=seed)
+        d.update(kw)
+        return cls(**d)
+
+
+DR_FIELDS = {"psi": 0, "slip_rate1": 1, "slip_rate2": 2, "slip1": 3, "slip2": 4, "slip": 5, "mu": 6, "traction1": 7,
+             "traction2": 8, "a": 9, "sn0": 10, "tau1_0": 11, "tau2_0": 12}
 
 
 class _Perf(C.Structure):
@@ -87,6 +108,17 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_last_run_ms", i, [VP, C.POINTER(d)])
     _sig(lib, "sei_metrics", i, [VP, i, C.POINTER(_Perf)])
     _sig(lib, "sei_set_profiling", i, [VP, i])
+    _sig(lib, "sei_dr_setup", i, [VP, C.POINTER(RSParams), C.POINTER(i64)])
+    _sig(lib, "sei_dr_num_points", i, [i])
+    _sig(lib, "sei_dr_num_faces", i64, [VP])
+    _sig(lib, "sei_dr_get_faces", i, [VP, VP, VP, VP, VP, VP, VP])
+    _sig(lib, "sei_dr_get_state", i, [VP, i, VP])
+    _sig(lib, "sei_dr_set_state", i, [VP, i, VP])
+    _sig(lib, "sei_dr_get_imposed", i, [VP, VP, VP])
+    _sig(lib, "sei_dr_newton_iterations", i, [VP, C.POINTER(i64), C.POINTER(i64)])
+    _sig(lib, "sei_dr_reset_counters", i, [VP])
+    _sig(lib, "sei_dr_faces_step", i, [VP, d])
+    _sig(lib, "sei_dr_get_slots", i, [VP, VP])
     _sig(lib, "sei_kernel_times_ms", i, [VP, C.POINTER(d), C.POINTER(d), C.POINTER(i)])
     if path is None:
         _lib = lib
@@ -151,8 +183,9 @@ class Context:
             raise SeiError(rc, f"{what}: {msg.decode() if msg else ''}")
 
     # -- set-up ------------------------------------------------------------------------
-    def build_periodic_cube(self, nx, ny, nz, h=100.0, rho=2700.0, vp=6000.0, vs=3464.0, perturb=0.0, seed=1):
-        p = _CubeParams(nx, ny, nz, h, rho, vp, vs, perturb, seed)
+    def build_periodic_cube(self, nx, ny, nz, h=100.0, rho=2700.0, vp=6000.0, vs=3464.0, perturb=0.0, seed=1,
+                            fault_plane=-1):
+        p = _CubeParams(nx, ny, nz, h, rho, vp, vs, perturb, seed, fault_plane)
         n = C.c_int64()
         self._check(self.lib.sei_build_periodic_cube(self.h, C.byref(p), C.byref(n)), "sei_build_periodic_cube")
         self.n = n.value
@@ -231,6 +264,65 @@ class Context:
 
     def sync(self):
         self._check(self.lib.sei_sync(self.h), "sei_sync")
+
+    # -- dynamic rupture ------------------------------------------------------------------
+    def dr_setup(self, params: "RSParams"):
+        nf = C.c_int64()
+        self._check(self.lib.sei_dr_setup(self.h, C.byref(params), C.byref(nf)), "sei_dr_setup")
+        self.nfaces = nf.value
+        self.npts = self.lib.sei_dr_num_points(self.order)
+        return self.nfaces
+
+    def dr_faces(self):
+        nf = self.lib.sei_dr_num_faces(self.h)
+        cells = np.empty((nf, 2), np.int32)
+        sides = np.empty((nf, 3), np.int8)
+        tinvt = np.empty((nf, 9, 9), np.float32)
+        fsp = np.empty((nf, 9, 9), np.float32)
+        fsm = np.empty((nf, 9, 9), np.float32)
+        imp = np.empty((nf, 8), np.float64)
+        self._check(self.lib.sei_dr_get_faces(self.h, *[_ptr(a) for a in (cells, sides, tinvt, fsp, fsm, imp)]),
+                    "sei_dr_get_faces")
+        sw = lambda a: np.swapaxes(a, -1, -2)
+        return {"cells": cells, "sides": sides, "TinvT": sw(tinvt), "fluxSolverPlus": sw(fsp),
+                "fluxSolverMinus": sw(fsm), "imp": imp}
+
+    def dr_state(self, field):
+        out = np.empty((self.nfaces, self.npts), np.float64)
+        self._check(self.lib.sei_dr_get_state(self.h, DR_FIELDS[field], _ptr(out)), "sei_dr_get_state")
+        return out
+
+    def dr_set_state(self, field, values):
+        a = np.ascontiguousarray(values, np.float64)
+        assert a.shape == (self.nfaces, self.npts)
+        self._check(self.lib.sei_dr_set_state(self.h, DR_FIELDS[field], _ptr(a)), "sei_dr_set_state")
+
+    def dr_imposed(self):
+        p = np.empty((self.nfaces, 9, self.npts), np.float32)
+        m = np.empty((self.nfaces, 9, self.npts), np.float32)
+        self._check(self.lib.sei_dr_get_imposed(self.h, _ptr(p), _ptr(m)), "sei_dr_get_imposed")
+        return p, m
+
+    def dr_newton_iterations(self):
+        t, n = C.c_int64(), C.c_int64()
+        self._check(self.lib.sei_dr_newton_iterations(self.h, C.byref(t), C.byref(n)), "sei_dr_newton_iterations")
+        return t.value, n.value
+
+    def dr_reset_counters(self):
+        self._check(self.lib.sei_dr_reset_counters(self.h), "sei_dr_reset_counters")
+
+    def dr_faces_step(self, dt):
+        self._check(self.lib.sei_dr_faces_step(self.h, dt), "sei_dr_faces_step")
+
+    def dr_slots(self):
+        out = np.empty(self.n, np.int32)
+        self._check(self.lib.sei_dr_get_slots(self.h, _ptr(out)), "sei_dr_get_slots")
+        return out
+
+    def get_derivatives_slots(self, nslots):
+        a = np.empty((nslots, derivatives_size(self.order)), np.float32)
+        self._check(self.lib.sei_get_derivatives(self.h, _ptr(a)), "sei_get_derivatives")
+        return a
 
     def set_profiling(self, on=True):
         self._check(self.lib.sei_set_profiling(self.h, int(on)), "sei_set_profiling")

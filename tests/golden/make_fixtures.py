@@ -6,6 +6,9 @@ compiled or imported.  Outputs:
 
 * ``godunov_elastic.json``  -- Godunov-state matrices of ``tests/Model/Values.h``
   (homogeneous and heterogeneous elastic cases) with the two materials.
+* ``dr_matrices_pin.json`` -- for ``codegen/matrices/dr_stroud_matrices_{4,5,6}.json``: the
+  quadrature points and weights in full and the same summary as below for V3mTo2n,
+  V3mTo2nTWDivM and resample.
 * ``global_matrices_pin.json`` -- for every matrix of
   ``codegen/matrices/matrices_{20,35,56}.xml``: shape, non-zero count, sum,
   Frobenius norm and a deterministic sample of entries.
@@ -63,6 +66,21 @@ def parse_xml(path):
     return res
 
 
+def parse_dr_json(path):
+    res = {}
+    for m in json.load(open(path)):
+        rows, cols = int(m["rows"]), int(m["columns"])
+        ent = sorted((int(e[0]) - 1, int(e[1]) - 1, float(e[2])) for e in m["entries"])
+        if m["name"] in ("quadpoints", "quadweights"):
+            res[m["name"]] = {"shape": [rows, cols], "entries": [[r, c, v] for (r, c, v) in ent]}
+            continue
+        nz = [e for e in ent if e[2] != 0.0]
+        step = max(1, len(nz) // 24)
+        res[m["name"]] = {"shape": [rows, cols], "nnz": len(nz), "sum": sum(e[2] for e in nz),
+                          "fro": sum(e[2] ** 2 for e in nz) ** 0.5, "sample": [[r, c, v] for (r, c, v) in nz[::step]]}
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -73,6 +91,9 @@ def main():
     for b in (20, 35, 56):
         pin[str(b)] = parse_xml(os.path.join(a.reference, f"codegen/matrices/matrices_{b}.xml"))
     json.dump(pin, open(os.path.join(HERE, "global_matrices_pin.json"), "w"))
+    dr = {str(o): parse_dr_json(os.path.join(a.reference, f"codegen/matrices/dr_stroud_matrices_{o}.json"))
+          for o in (4, 5, 6)}
+    json.dump(dr, open(os.path.join(HERE, "dr_matrices_pin.json"), "w"))
 
 
 if __name__ == "__main__":
