@@ -225,6 +225,8 @@ def run_ours(args, world, rank, local):
 
     hbm, peak_kind = peaks()
     ctx = Context(ORDER, device=local)
+    if args.fused_local:
+        ctx.set_option(1, 1)  # SEI_OPT_FUSED_LOCAL
     n = ctx.build_periodic_cube(*DIMS, perturb=PERTURB, seed=SEED + rank)
     dt = ctx.cfl_timestep(0.5)
     ctx.run("all", dt, args.warmup)
@@ -309,7 +311,7 @@ def run_ours(args, world, rank, local):
                            "l2": "inputs larger than L2 (~3 GB resident per GPU), no flush",
                            "parallelism": f"replicas x{world}"},
                 "roofline": roof, "cpu_baseline": base, "e2e": e2e, "clocks": clocks,
-                "gpu_launches": 2 * args.steps, "kernel_ms_per_step": kernels}
+                "gpu_launches": launches, "kernel_ms_per_step": kernels}
         print(json.dumps(line))
     return 0
 
@@ -322,6 +324,7 @@ def main():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fused-local", action="store_true", help="ADER and local integral in one launch")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -144,7 +144,8 @@ int sei_derivatives_size(int order);
 /* Spacetime::computeBatchedAder (src/Kernels/LinearCK/Time.cpp:142-217) for all cells,
  * coeffs = MonomialBasis::integrate(0, dt) (src/Numerical/TimeBasis.h:82-93). */
 int sei_compute_ader(sei_ctx* ctx, double dt);
-/* Local::computeBatchedIntegral (src/Kernels/LinearCK/Local.cpp:255-395): volume + local flux. */
+/* Local::computeBatchedIntegral (src/Kernels/LinearCK/Local.cpp:255-395): volume + local flux from the
+ * time-integrated DOFs of the last sei_compute_ader. */
 int sei_compute_local_integral(sei_ctx* ctx);
 /* ADER followed by the local integral in one launch (src/Proxy/KernelHost.cpp:108-131). */
 int sei_compute_ader_local(sei_ctx* ctx, double dt);
@@ -152,6 +153,11 @@ int sei_compute_ader_local(sei_ctx* ctx, double dt);
 int sei_compute_neighbors_integral(sei_ctx* ctx);
 /* Time::evaluateBatched (src/Kernels/LinearCK/Time.cpp:256-292) of the stored derivatives. */
 int sei_evaluate_taylor(sei_ctx* ctx, const double* coeffs, float* out_device);
+
+/* Options. SEI_OPT_FUSED_LOCAL: 1 runs ADER and the local integral as one launch, 0 (default)
+ * as two launches (smaller kernels; I is written and re-read once). */
+#define SEI_OPT_FUSED_LOCAL 1
+int sei_set_option(sei_ctx* ctx, int option, int value);
 
 /* Runs a proxy kernel for nsteps steps (src/Proxy/Runner.cpp:99-111); asynchronous. */
 int sei_run(sei_ctx* ctx, int kernel, double dt, int nsteps);

@@ -96,16 +96,8 @@ def gen_order(order: int) -> str:
     a("__constant__ int c_src[9][3] = {" + ",".join("{" + ",".join(map(str, s)) + "}" for s in src) + "};")
     a("__constant__ int c_nzi[9][3] = {" + ",".join("{" + ",".join(map(str, s)) + "}" for s in idx) + "};")
 
-    # ---------------- local kernel ----------------
-    a(f"""
-// Q[n][9][B] in/out (in place), I[n][9][B] out, star_nz[n][3][24], aplus[n][4][81] (column-major 9x9),
-// ftype[n][4] (1 = dynamic rupture: no local flux), coeffs[order] Taylor integration coefficients,
-// derivs: optional packed derivative output [slots][kDerivSize] (nullptr to skip); the slot of a
-// cell is dslot[cell] (-1: not stored), or the cell itself when dslot is nullptr.
-extern "C" __global__ void __launch_bounds__(288, 1)
-sei_local_o{order}(int n, float* __restrict__ Q, float* __restrict__ Iout, const float* __restrict__ star_nz,
-                   const float* __restrict__ aplus, const unsigned char* __restrict__ ftype,
-                   SeiCoeffs coeffs, float* __restrict__ derivs, const int* __restrict__ dslot) {{
+    # ---------------- ADER + local kernels ----------------
+    prologue = f"""
   extern __shared__ float sm[];
   const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int cell = blockIdx.x * kCPB + lane;
@@ -125,8 +117,10 @@ sei_local_o{order}(int n, float* __restrict__ Q, float* __restrict__ Iout, const
       const int i = c_nzi[q][s];
       st[e][s] = i >= 0 ? __ldg(star_nz + (size_t)cl * 72 + e * 24 + i) : 0.f;
     }}
-  const float* qcol = Q + ((size_t)cl * 9 + q) * kBp;
-  float z[kBp];
+  const float* qcol = Q + ((size_t)cl * 9 + q) * kBp;"""
+
+    def emit_ck():
+        a("""  float z[kBp];
   sei_load_col<kBp>(qcol, z);
   float I[kBp];
 #pragma unroll
@@ -134,78 +128,114 @@ sei_local_o{order}(int n, float* __restrict__ Q, float* __restrict__ Iout, const
   const int dsl = derivs ? (dslot ? __ldg(dslot + cl) : cl) : -1;
   float* dbase = (dsl >= 0 && valid) ? derivs + (size_t)dsl * kDerivSize : nullptr;
   if (dbase) sei_store_col_scalar<kB>(dbase + q * kB, z);""")
-    off = B * NQ
-    for i in range(1, order):
-        bp, bc = nb3(order - i + 1), nb3(order - i)
-        a(f"  // ---- CK stage {i}: rows {bc} from {bp}")
-        a("  {")
-        a(f"#pragma unroll\n    for (int k = 0; k < {bp}; ++k) Xq[k * 32] = z[k];")
-        a("    __syncthreads();")
-        a(f"    float zn[{bc}];")
-        a(f"#pragma unroll\n    for (int k = 0; k < {bc}; ++k) zn[k] = 0.f;")
-        cols = [_cols(G["kDivMT"][e], bc, bp) for e in range(3)]
-        for l in range(bp):
+        off = B * NQ
+        for i in range(1, order):
+            bp, bc = nb3(order - i + 1), nb3(order - i)
+            a(f"  // ---- CK stage {i}: rows {bc} from {bp}")
+            a("  {")
+            a(f"#pragma unroll\n    for (int k = 0; k < {bp}; ++k) Xq[k * 32] = z[k];")
+            a("    __syncthreads();")
+            a(f"    float zn[{bc}];")
+            a(f"#pragma unroll\n    for (int k = 0; k < {bc}; ++k) zn[k] = 0.f;")
+            cols = [_cols(G["kDivMT"][e], bc, bp) for e in range(3)]
+            for l in range(bp):
+                if not any(l in c for c in cols):
+                    continue
+                a(f"    {{ const float x0 = Xs0[{l * 32}], x1 = Xs1[{l * 32}], x2 = Xs2[{l * 32}];")
+                for e in range(3):
+                    if l in cols[e]:
+                        a(f"      const float y{e} = st[{e}][0] * x0 + st[{e}][1] * x1 + st[{e}][2] * x2;")
+                for e in range(3):
+                    for k, v in cols[e].get(l, []):
+                        a(f"      zn[{k}] = fmaf({flit(v)}, y{e}, zn[{k}]);")
+                a("    }")
+            a("    __syncthreads();")
+            a(f"#pragma unroll\n    for (int k = 0; k < {bc}; ++k) {{ I[k] = fmaf(coeffs.c[{i}], zn[k], I[k]); z[k] = zn[k]; }}")
+            a(f"    if (dbase) sei_store_col_scalar<{bc}>(dbase + {off} + q * {bc}, zn);")
+            off += bc * NQ
+            a("  }")
+
+    def emit_volume_flux():
+        a("  // ---- volume: Q += sum_e kDivM_e (I star_e)")
+        a(f"#pragma unroll\n  for (int k = 0; k < kB; ++k) Xq[k * 32] = I[k];")
+        a("  __syncthreads();")
+        a("  float acc[kBp];")
+        a("  sei_load_col<kBp>(qcol, acc);")
+        cols = [_cols(G["kDivM"][e]) for e in range(3)]
+        for l in range(B):
             if not any(l in c for c in cols):
                 continue
-            a(f"    {{ const float x0 = Xs0[{l * 32}], x1 = Xs1[{l * 32}], x2 = Xs2[{l * 32}];")
+            a(f"  {{ const float x0 = Xs0[{l * 32}], x1 = Xs1[{l * 32}], x2 = Xs2[{l * 32}];")
             for e in range(3):
                 if l in cols[e]:
-                    a(f"      const float y{e} = st[{e}][0] * x0 + st[{e}][1] * x1 + st[{e}][2] * x2;")
+                    a(f"    const float y{e} = st[{e}][0] * x0 + st[{e}][1] * x1 + st[{e}][2] * x2;")
             for e in range(3):
                 for k, v in cols[e].get(l, []):
-                    a(f"      zn[{k}] = fmaf({flit(v)}, y{e}, zn[{k}]);")
-            a("    }")
-        a("    __syncthreads();")
-        a(f"#pragma unroll\n    for (int k = 0; k < {bc}; ++k) {{ I[k] = fmaf(coeffs.c[{i}], zn[k], I[k]); z[k] = zn[k]; }}")
-        a(f"    if (dbase) sei_store_col_scalar<{bc}>(dbase + {off} + q * {bc}, zn);")
-        off += bc * NQ
-        a("  }")
-    # volume
-    a("  // ---- volume: Q += sum_e kDivM_e (I star_e)")
-    a(f"#pragma unroll\n  for (int k = 0; k < kB; ++k) Xq[k * 32] = I[k];")
-    a("  __syncthreads();")
-    a("  float acc[kBp];")
-    a("  sei_load_col<kBp>(qcol, acc);")
-    cols = [_cols(G["kDivM"][e]) for e in range(3)]
-    for l in range(B):
-        if not any(l in c for c in cols):
-            continue
-        a(f"  {{ const float x0 = Xs0[{l * 32}], x1 = Xs1[{l * 32}], x2 = Xs2[{l * 32}];")
-        for e in range(3):
-            if l in cols[e]:
-                a(f"    const float y{e} = st[{e}][0] * x0 + st[{e}][1] * x1 + st[{e}][2] * x2;")
-        for e in range(3):
-            for k, v in cols[e].get(l, []):
-                a(f"    acc[{k}] = fmaf({flit(v)}, y{e}, acc[{k}]);")
-        a("  }")
-    a("  __syncthreads();")
-    # local flux
-    for f in range(4):
-        a(f"  // ---- local flux, face {f}: Q += rDivM_{f} ((fMrT_{f} I) AplusT_{f})")
-        a("  {")
-        a("    float T[kF];")
-        _matvec(L, "    ", G["fMrT"][f], "I", "T", F, B, True)
-        a(f"#pragma unroll\n    for (int m = 0; m < kF; ++m) Xq[m * 32] = T[m];")
-        a("    __syncthreads();")
-        a(f"    const bool on = valid && ftype[(size_t)cl * 4 + {f}] != 1;")
-        a(f"    const float* ap = aplus + ((size_t)cl * 4 + {f}) * 81 + 9 * q;")
-        a("    float av[9];")
-        a("#pragma unroll\n    for (int s = 0; s < 9; ++s) av[s] = on ? __ldg(ap + s) : 0.f;")
-        bycol = _cols(G["rDivM"][f])
-        for m in range(F):
-            if m not in bycol:
-                continue
-            a(f"    {{ float g = 0.f;")
-            a(f"#pragma unroll\n      for (int s = 0; s < 9; ++s) g = fmaf(X[(s * kB + {m}) * 32 + lane], av[s], g);")
-            for k, v in bycol[m]:
-                a(f"      acc[{k}] = fmaf({flit(v)}, g, acc[{k}]);")
-            a("    }")
-        a("    __syncthreads();")
-        a("  }")
+                    a(f"    acc[{k}] = fmaf({flit(v)}, y{e}, acc[{k}]);")
+            a("  }")
+        a("  __syncthreads();")
+        for f in range(4):
+            a(f"  // ---- local flux, face {f}: Q += rDivM_{f} ((fMrT_{f} I) AplusT_{f})")
+            a("  {")
+            a("    float T[kF];")
+            _matvec(L, "    ", G["fMrT"][f], "I", "T", F, B, True)
+            a(f"#pragma unroll\n    for (int m = 0; m < kF; ++m) Xq[m * 32] = T[m];")
+            a("    __syncthreads();")
+            a(f"    const bool on = valid && ftype[(size_t)cl * 4 + {f}] != 1;")
+            a(f"    const float* ap = aplus + ((size_t)cl * 4 + {f}) * 81 + 9 * q;")
+            a("    float av[9];")
+            a("#pragma unroll\n    for (int s = 0; s < 9; ++s) av[s] = on ? __ldg(ap + s) : 0.f;")
+            bycol = _cols(G["rDivM"][f])
+            for m in range(F):
+                if m not in bycol:
+                    continue
+                a(f"    {{ float g = 0.f;")
+                a(f"#pragma unroll\n      for (int s = 0; s < 9; ++s) g = fmaf(X[(s * kB + {m}) * 32 + lane], av[s], g);")
+                for k, v in bycol[m]:
+                    a(f"      acc[{k}] = fmaf({flit(v)}, g, acc[{k}]);")
+                a("    }")
+            a("    __syncthreads();")
+            a("  }")
+
+    # fused ADER + local integral
+    a(f"""
+// ADER + local integral in one launch.
+// Q[n][9][Bp] in/out (in place), I[n][9][Bp] out, star_nz[n][3][24], aplus[n][4][81] (column-major 9x9),
+// ftype[n][4] (1 = dynamic rupture: no local flux), coeffs Taylor integration coefficients,
+// derivs: optional packed derivative output [slots][kDerivSize] (nullptr to skip); the slot of a
+// cell is dslot[cell] (-1: not stored), or the cell itself when dslot is nullptr.
+extern "C" __global__ void __launch_bounds__(288, 1)
+sei_local_o{order}(int n, float* __restrict__ Q, float* __restrict__ Iout, const float* __restrict__ star_nz,
+                   const float* __restrict__ aplus, const unsigned char* __restrict__ ftype,
+                   SeiCoeffs coeffs, float* __restrict__ derivs, const int* __restrict__ dslot) {{""" + prologue)
+    emit_ck()
+    emit_volume_flux()
     a("  if (valid) {")
     a("    sei_store_col<kBp>(Q + ((size_t)cell * 9 + q) * kBp, acc);")
     a("    sei_store_col<kBp>(Iout + ((size_t)cell * 9 + q) * kBp, I);")
     a("  }")
+    a("}")
+
+    # ADER alone (Spacetime::computeAder)
+    a(f"""
+// Cauchy-Kovalevskaya predictor alone: I = sum_i coeffs[i] dQ(i) (Q unchanged), optional derivatives.
+extern "C" __global__ void __launch_bounds__(288, 1)
+sei_ader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout, const float* __restrict__ star_nz,
+                  SeiCoeffs coeffs, float* __restrict__ derivs, const int* __restrict__ dslot) {{""" + prologue)
+    emit_ck()
+    a("  if (valid) sei_store_col<kBp>(Iout + ((size_t)cell * 9 + q) * kBp, I);")
+    a("}")
+
+    # local integral alone (Local::computeIntegral)
+    a(f"""
+// Volume + local flux from the time-integrated DOFs: Q += ... (in place).
+extern "C" __global__ void __launch_bounds__(288, 1)
+sei_lint_o{order}(int n, float* __restrict__ Q, const float* __restrict__ Iin, const float* __restrict__ star_nz,
+                  const float* __restrict__ aplus, const unsigned char* __restrict__ ftype) {{""" + prologue)
+    a("  float I[kBp];")
+    a("  sei_load_col<kBp>(Iin + ((size_t)cl * 9 + q) * kBp, I);")
+    emit_volume_flux()
+    a("  if (valid) sei_store_col<kBp>(Q + ((size_t)cell * 9 + q) * kBp, acc);")
     a("}")
 
     # ---------------- neighbour kernel ----------------
@@ -224,6 +254,19 @@ sei_neighbor_o{order}(int n, float* __restrict__ Q, const float* __restrict__ I,
   const int cl = valid ? cell : n - 1;
   float* X = sm;  // [9][kF][32]
   float* Xq = X + q * kF * 32 + lane;
+  // double-buffered prefetch of the neighbour columns: [2][288][kBp + 4] (row padding keeps
+  // the 16-byte reads of the 8 lanes of a phase on distinct banks)
+  constexpr int kPS = kBp + 4;
+  float* P = sm + 9 * kF * 32 + threadIdx.x * kPS;
+  auto prefetch = [&](int f, float* dst) {{
+    const int nb = __ldg(nbr + (size_t)cl * 4 + f);
+    const bool on = valid && nb >= 0 && ftype[(size_t)cl * 4 + f] == 0;
+    const float* src = I + ((size_t)(on ? nb : cl) * 9 + q) * kBp;
+#pragma unroll
+    for (int i = 0; i < kBp / 4; ++i) sei_cp_async16(dst + 4 * i, src + 4 * i);
+    sei_cp_async_commit();
+  }};
+  prefetch(0, P);
   float acc[kBp];
   sei_load_col<kBp>(Q + ((size_t)cl * 9 + q) * kBp, acc);
 #pragma unroll 1
@@ -231,9 +274,22 @@ sei_neighbor_o{order}(int n, float* __restrict__ Q, const float* __restrict__ I,
     const int nb = __ldg(nbr + (size_t)cl * 4 + f);
     const int r = rel[(size_t)cl * 4 + f];
     const bool on = valid && nb >= 0 && ftype[(size_t)cl * 4 + f] == 0;
-    const int src = on ? nb : cl;
+    if (f < 3) {{
+      prefetch(f + 1, P + ((f + 1) & 1) * 288 * kPS);
+      sei_cp_async_wait<1>();
+    }} else {{
+      sei_cp_async_wait<0>();
+    }}
+    const float* buf = P + (f & 1) * 288 * kPS;
     float x[kBp];
-    sei_load_col<kBp>(I + ((size_t)src * 9 + q) * kBp, x);
+#pragma unroll
+    for (int i = 0; i < kBp / 4; ++i) {{
+      const float4 t = reinterpret_cast<const float4*>(buf)[i];
+      x[4 * i] = t.x;
+      x[4 * i + 1] = t.y;
+      x[4 * i + 2] = t.z;
+      x[4 * i + 3] = t.w;
+    }}
     float R[kF];
     switch (r & 3) {{""")
     for j in range(4):

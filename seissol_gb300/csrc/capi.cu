@@ -57,6 +57,7 @@ struct sei_ctx {
   float mlp_norm[12] = {0};
   // per-launch timing (sei_set_profiling): one event before every launch plus one at the end
   bool profiling = false;
+  bool fused_local = false;  // SEI_OPT_FUSED_LOCAL: ADER and local integral in one launch
   std::vector<cudaEvent_t> prof_events;
   std::vector<int> prof_kind;  // kind of the launch that starts at event i (0 local, 1 neighbour)
   size_t prof_used = 0;
@@ -196,7 +197,26 @@ int profMark(sei_ctx* c, int kind) {
   return SEI_OK;
 }
 
+int launchAderOnly(sei_ctx* c, const sei::DeviceArrays& d, const float* coeffs) {
+  int rc = profMark(c, 0);
+  if (rc) return rc;
+  if (c->k.ader(d, coeffs, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "ADER kernel launch failed");
+  return SEI_OK;
+}
+
+int launchLintOnly(sei_ctx* c, const sei::DeviceArrays& d) {
+  int rc = profMark(c, 0);
+  if (rc) return rc;
+  if (c->k.lint(d, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "local-integral kernel launch failed");
+  return SEI_OK;
+}
+
+// ADER followed by the local integral: two launches (default) or one fused launch.
 int launchLocal(sei_ctx* c, const sei::DeviceArrays& d, const float* coeffs) {
+  if (!c->fused_local) {
+    int rc = launchAderOnly(c, d, coeffs);
+    return rc ? rc : launchLintOnly(c, d);
+  }
   int rc = profMark(c, 0);
   if (rc) return rc;
   if (c->k.local(d, coeffs, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "local kernel launch failed");
@@ -296,6 +316,12 @@ int runKernel(sei_ctx* c, int kernel, double dt, int steps) {
         break;
       case SEI_KERNEL_LOCAL:
         rc = launchLocal(c, d, coeffs);
+        break;
+      case SEI_KERNEL_ADER:
+        rc = launchAderOnly(c, d, coeffs);
+        break;
+      case SEI_KERNEL_LOCAL_WO_ADER:
+        rc = launchLintOnly(c, d);
         break;
       case SEI_KERNEL_NEIGHBOR:
       case SEI_KERNEL_NEIGHBOR_DR:
@@ -526,8 +552,28 @@ int sei_compute_neighbors_integral(sei_ctx* c) {
   return runKernel(c, SEI_KERNEL_NEIGHBOR, 0.0, 1);
 }
 
-int sei_compute_ader(sei_ctx* c, double) { return fail(c, SEI_ERR_UNSUPPORTED, "ADER alone is not built yet"); }
-int sei_compute_local_integral(sei_ctx* c) { return fail(c, SEI_ERR_UNSUPPORTED, "local alone is not built yet"); }
+int sei_compute_ader(sei_ctx* c, double dt) {
+  int rc = checkReady(c);
+  if (rc) return rc;
+  return runKernel(c, SEI_KERNEL_ADER, dt, 1);
+}
+
+int sei_compute_local_integral(sei_ctx* c) {
+  int rc = checkReady(c);
+  if (rc) return rc;
+  return runKernel(c, SEI_KERNEL_LOCAL_WO_ADER, 0.0, 1);
+}
+
+int sei_set_option(sei_ctx* c, int option, int value) {
+  if (!c) return SEI_ERR_ARG;
+  switch (option) {
+    case SEI_OPT_FUSED_LOCAL:
+      c->fused_local = value != 0;
+      return SEI_OK;
+    default:
+      return fail(c, SEI_ERR_ARG, "unknown option");
+  }
+}
 
 int sei_evaluate_taylor(sei_ctx* c, const double* coeffs, float* out_device) {
   int rc = checkReady(c);

@@ -46,3 +46,14 @@ __device__ __forceinline__ void sei_store_col_scalar(float* __restrict__ p, cons
 #pragma unroll
   for (int i = 0; i < N; ++i) p[i] = v[i];
 }
+
+// Asynchronous 16-byte global -> shared copies (both addresses 16-byte aligned).
+__device__ __forceinline__ void sei_cp_async16(void* smem, const void* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void sei_cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void sei_cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}

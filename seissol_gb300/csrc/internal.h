@@ -56,10 +56,14 @@ using LaunchLocalFn = int (*)(const DeviceArrays&, const float* coeffs, void* st
 using LaunchNeighborFn = int (*)(const DeviceArrays&, void* stream);
 using LaunchTaylorFn = int (*)(int n, const float* derivs, const float* coeffs, float* out, void* stream);
 
+using LaunchLintFn = int (*)(const DeviceArrays&, void* stream);
+
 struct OrderKernels {
-  LaunchLocalFn local;
-  LaunchNeighborFn neighbor;
-  LaunchTaylorFn taylor;
+  LaunchLocalFn local;        // ADER + local integral, one launch
+  LaunchNeighborFn neighbor;  // neighbour flux
+  LaunchTaylorFn taylor;      // Taylor evaluation of stored derivatives
+  LaunchLocalFn ader;         // ADER alone (writes I, optional derivatives)
+  LaunchLintFn lint;          // volume + local flux from I
 };
 
 bool kernelsForOrder(int order, OrderKernels& out);

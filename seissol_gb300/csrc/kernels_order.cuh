@@ -32,10 +32,37 @@ int launchLocal(const sei::DeviceArrays& d, const float* coeffs, void* stream) {
 
 int launchNeighbor(const sei::DeviceArrays& d, void* stream) {
   if (d.n <= 0) return 0;
-  const size_t smem = sizeof(float) * 9 * K::kF * 32;
+  const size_t smem = sizeof(float) * (9 * K::kF * 32 + 2 * 288 * (K::kBp + 4));
+  if (cudaFuncSetAttribute(K::SEI_CAT(sei_neighbor_o, SEI_ORDER), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return -1;
   const int blocks = (d.n + K::kCPB - 1) / K::kCPB;
   K::SEI_CAT(sei_neighbor_o, SEI_ORDER)<<<blocks, 288, smem, (cudaStream_t)stream>>>(
       d.n, d.Q, d.I, d.aminus, d.nbr, d.rel, d.ftype);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launchAder(const sei::DeviceArrays& d, const float* coeffs, void* stream) {
+  if (d.n <= 0) return 0;
+  const size_t smem = sizeof(float) * 9 * K::kB * 32;
+  if (cudaFuncSetAttribute(K::SEI_CAT(sei_ader_o, SEI_ORDER), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return -1;
+  const int blocks = (d.n + K::kCPB - 1) / K::kCPB;
+  K::SEI_CAT(sei_ader_o, SEI_ORDER)<<<blocks, 288, smem, (cudaStream_t)stream>>>(
+      d.n, d.Q, d.I, d.star_nz, toCoeffs(coeffs), d.derivs, d.dslot);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launchLint(const sei::DeviceArrays& d, void* stream) {
+  if (d.n <= 0) return 0;
+  const size_t smem = sizeof(float) * 9 * K::kB * 32;
+  if (cudaFuncSetAttribute(K::SEI_CAT(sei_lint_o, SEI_ORDER), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return -1;
+  const int blocks = (d.n + K::kCPB - 1) / K::kCPB;
+  K::SEI_CAT(sei_lint_o, SEI_ORDER)<<<blocks, 288, smem, (cudaStream_t)stream>>>(d.n, d.Q, d.I, d.star_nz, d.aplus,
+                                                                                d.ftype);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -49,5 +76,7 @@ int launchTaylor(int n, const float* derivs, const float* coeffs, float* out, vo
 }  // namespace
 
 namespace sei {
-OrderKernels SEI_CAT(orderKernels, SEI_ORDER)() { return OrderKernels{launchLocal, launchNeighbor, launchTaylor}; }
+OrderKernels SEI_CAT(orderKernels, SEI_ORDER)() {
+  return OrderKernels{launchLocal, launchNeighbor, launchTaylor, launchAder, launchLint};
+}
 }  // namespace sei

@@ -108,6 +108,7 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_last_run_ms", i, [VP, C.POINTER(d)])
     _sig(lib, "sei_metrics", i, [VP, i, C.POINTER(_Perf)])
     _sig(lib, "sei_set_profiling", i, [VP, i])
+    _sig(lib, "sei_set_option", i, [VP, i, i])
     _sig(lib, "sei_dr_setup", i, [VP, C.POINTER(RSParams), C.POINTER(i64)])
     _sig(lib, "sei_dr_num_points", i, [i])
     _sig(lib, "sei_dr_num_faces", i64, [VP])
@@ -248,6 +249,15 @@ class Context:
         return a
 
     # -- kernels ------------------------------------------------------------------------
+    def set_option(self, option, value):
+        self._check(self.lib.sei_set_option(self.h, option, int(value)), "sei_set_option")
+
+    def compute_ader(self, dt):
+        self._check(self.lib.sei_compute_ader(self.h, dt), "sei_compute_ader")
+
+    def compute_local_integral(self):
+        self._check(self.lib.sei_compute_local_integral(self.h), "sei_compute_local_integral")
+
     def compute_ader_local(self, dt):
         self._check(self.lib.sei_compute_ader_local(self.h, dt), "sei_compute_ader_local")
 

@@ -138,3 +138,31 @@ def test_bad_relations_rejected(built_lib):
                        cells["face_type"])
     ctx.close()
     ctx2.close()
+
+
+@pytest.mark.parametrize("order", [4, 6])
+def test_ader_and_local_integral_separately(built_lib, order):
+    """sei_compute_ader leaves Q unchanged and matches the oracle; sei_compute_local_integral then
+    matches the oracle's volume + local flux; the fused launch gives the same bits."""
+    ctx, n, cells, q0 = _setup(order, store_derivatives=False)
+    dt = ctx.cfl_timestep(0.5)
+    o = oracle_py.Oracle(order)
+    ops = _ops64(cells)
+    i_ref = o.ader(q0.astype(np.float64), ops["star"], dg_setup.taylor_integrate(order, 0.0, dt))
+    ctx.compute_ader(dt)
+    ctx.sync()
+    assert np.array_equal(ctx.get_dofs(), q0)
+    i_gpu = ctx.get_time_integrated()
+    assert max(rel_l2_per_quantity(i_gpu, i_ref)) < TOL_ONE
+    ctx.compute_local_integral()
+    ctx.sync()
+    q_split = ctx.get_dofs()
+    q_ref = o.local(q0, i_ref, ops["star"], ops["AplusT"], cells["face_type"])
+    assert max(rel_l2_per_quantity(q_split - q0, q_ref - q0)) < TOL_ONE
+    ctx.set_dofs(q0)
+    ctx.set_option(1, 1)  # SEI_OPT_FUSED_LOCAL
+    ctx.compute_ader_local(dt)
+    ctx.sync()
+    assert np.array_equal(ctx.get_dofs(), q_split)
+    assert np.array_equal(ctx.get_time_integrated(), i_gpu)
+    ctx.close()
