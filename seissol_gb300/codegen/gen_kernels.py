@@ -254,19 +254,6 @@ sei_neighbor_o{order}(int n, float* __restrict__ Q, const float* __restrict__ I,
   const int cl = valid ? cell : n - 1;
   float* X = sm;  // [9][kF][32]
   float* Xq = X + q * kF * 32 + lane;
-  // double-buffered prefetch of the neighbour columns: [2][288][kBp + 4] (row padding keeps
-  // the 16-byte reads of the 8 lanes of a phase on distinct banks)
-  constexpr int kPS = kBp + 4;
-  float* P = sm + 9 * kF * 32 + threadIdx.x * kPS;
-  auto prefetch = [&](int f, float* dst) {{
-    const int nb = __ldg(nbr + (size_t)cl * 4 + f);
-    const bool on = valid && nb >= 0 && ftype[(size_t)cl * 4 + f] == 0;
-    const float* src = I + ((size_t)(on ? nb : cl) * 9 + q) * kBp;
-#pragma unroll
-    for (int i = 0; i < kBp / 4; ++i) sei_cp_async16(dst + 4 * i, src + 4 * i);
-    sei_cp_async_commit();
-  }};
-  prefetch(0, P);
   float acc[kBp];
   sei_load_col<kBp>(Q + ((size_t)cl * 9 + q) * kBp, acc);
 #pragma unroll 1
@@ -274,22 +261,8 @@ sei_neighbor_o{order}(int n, float* __restrict__ Q, const float* __restrict__ I,
     const int nb = __ldg(nbr + (size_t)cl * 4 + f);
     const int r = rel[(size_t)cl * 4 + f];
     const bool on = valid && nb >= 0 && ftype[(size_t)cl * 4 + f] == 0;
-    if (f < 3) {{
-      prefetch(f + 1, P + ((f + 1) & 1) * 288 * kPS);
-      sei_cp_async_wait<1>();
-    }} else {{
-      sei_cp_async_wait<0>();
-    }}
-    const float* buf = P + (f & 1) * 288 * kPS;
     float x[kBp];
-#pragma unroll
-    for (int i = 0; i < kBp / 4; ++i) {{
-      const float4 t = reinterpret_cast<const float4*>(buf)[i];
-      x[4 * i] = t.x;
-      x[4 * i + 1] = t.y;
-      x[4 * i + 2] = t.z;
-      x[4 * i + 3] = t.w;
-    }}
+    sei_load_col<kBp>(I + ((size_t)(on ? nb : cl) * 9 + q) * kBp, x);
     float R[kF];
     switch (r & 3) {{""")
     for j in range(4):

@@ -32,7 +32,7 @@ int launchLocal(const sei::DeviceArrays& d, const float* coeffs, void* stream) {
 
 int launchNeighbor(const sei::DeviceArrays& d, void* stream) {
   if (d.n <= 0) return 0;
-  const size_t smem = sizeof(float) * (9 * K::kF * 32 + 2 * 288 * (K::kBp + 4));
+  const size_t smem = sizeof(float) * 9 * K::kF * 32;
   if (cudaFuncSetAttribute(K::SEI_CAT(sei_neighbor_o, SEI_ORDER), cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem) != cudaSuccess)
     return -1;
