@@ -198,6 +198,12 @@ int sei_dr_get_slots(sei_ctx* ctx, int32_t* slots);
 int sei_set_profiling(sei_ctx* ctx, int on);
 int sei_kernel_times_ms(sei_ctx* ctx, double* local_ms, double* neighbor_ms, int* launches);
 
+/* Diagnostic: one 128 x N x K tile D = A B^T on the tensor cores (tcgen05 kind::tf32, TMEM
+ * accumulator), A [128][K] and B [N][K] row-major host arrays, D [128][N]; terms 1 = plain TF32,
+ * 3 = split TF32.  N multiple of 16 in 16..256, K multiple of 8 in 8..64.  Checks the tensor-core
+ * conventions of the library on the current device. */
+int sei_tc_gemm_check(const float* A, const float* B, float* D, int N, int K, int terms);
+
 /* Per-cell, per-step estimate of a proxy kernel (Local.cpp:462-522, Neighbor.cpp:190-228). */
 int sei_metrics(const sei_ctx* ctx, int kernel, sei_perf* out);
 

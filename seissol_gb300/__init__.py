@@ -6,6 +6,7 @@ proxy bindings (app/Proxy/Bindings.cpp:14-60) and kernel interface.  There is no
 fallback: without the built library every entry point raises.
 """
 from .lib import (  # noqa: F401
+    tc_gemm_check,
     Context,
     RSParams,
     DR_FIELDS,

@@ -1,0 +1,114 @@
+// Blackwell (sm_103a) tensor-core primitives: tcgen05 MMA with TMEM accumulators.
+//
+// Operand layout in shared memory: K-major, no swizzle.  The tile is cut into "core matrices"
+// of 8 rows x 16 bytes (8 rows x 4 tf32), each stored as 128 contiguous bytes (row r at r*16).
+// Core matrix (row group g, K chunk j) of a tile with KC chunks along K sits at byte offset
+// (g * KC + j) * 128, i.e. the leading byte offset (next K chunk) is 128 and the stride byte
+// offset (next 8-row group) is KC * 128.  One kind::tf32 MMA consumes K = 8 = 2 chunks, so
+// the descriptor start address advances by 256 bytes per K step.
+#pragma once
+#include <cstdint>
+
+namespace sei_tc {
+
+// Byte offset of element (row, k) in a K-major no-swizzle tile with kc chunks of 4 floats along K.
+__host__ __device__ __forceinline__ uint32_t kmajorOffset(int row, int k, int kc) {
+  return (uint32_t)(((row >> 3) * kc + (k >> 2)) * 128 + (row & 7) * 16 + (k & 3) * 4);
+}
+
+// Shared-memory matrix descriptor (version 1 = sm_100 family), no swizzle.
+__device__ __forceinline__ uint64_t smemDesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
+  return d;                // base offset 0, absolute LBO mode, layout type 0 = no swizzle
+}
+
+// Instruction descriptor of kind::tf32: F32 accumulator, TF32 A and B, both K-major.
+__host__ __device__ constexpr uint32_t idescTf32(int M, int N) {
+  return (1u << 4)                    // D format F32
+         | (2u << 7)                  // A format TF32
+         | (2u << 10)                 // B format TF32
+         | ((uint32_t)(N >> 3) << 17) // N / 8
+         | ((uint32_t)(M >> 4) << 24);// M / 16
+}
+
+__device__ __forceinline__ uint32_t smemAddr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// One full warp allocates ncols TMEM columns; the address is written to *slot (shared).
+__device__ __forceinline__ void tmemAlloc(uint32_t* slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smemAddr(slot)), "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void tmemDealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T, M x N x 8 (tf32).
+__device__ __forceinline__ void mmaSS(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, bool accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"((uint32_t)accum)
+      : "memory");
+}
+
+// Arrives on the mbarrier once all previously issued MMAs of this thread have completed.
+__device__ __forceinline__ void mmaCommit(uint64_t* mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smemAddr(mbar))
+               : "memory");
+}
+
+__device__ __forceinline__ void fenceBeforeSync() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fenceAfterSync() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+// Makes generic-proxy shared-memory writes visible to the tensor-core (async) proxy.
+__device__ __forceinline__ void fenceProxyAsync() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+__device__ __forceinline__ void mbarInit(uint64_t* mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smemAddr(mbar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+
+// Waits for the phase with the given parity; gives up after maxPolls polls and returns false.
+__device__ __forceinline__ bool mbarWait(uint64_t* mbar, uint32_t parity, uint32_t maxPolls) {
+  const uint32_t a = smemAddr(mbar);
+  for (uint32_t i = 0; i < maxPolls; ++i) {
+    uint32_t done = 0;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// 16 consecutive 32-bit TMEM columns of this thread's lane (warp w reads lanes 32 (w % 4) ...).
+__device__ __forceinline__ void tmemLoad16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmemLoadWait() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+
+// Splits x into a TF32-exact high part (low 13 mantissa bits cleared) and the remainder.
+__device__ __forceinline__ void splitTf32(float x, float& hi, float& lo) {
+  hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+  lo = x - hi;
+}
+
+}  // namespace sei_tc

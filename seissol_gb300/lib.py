@@ -109,6 +109,7 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_metrics", i, [VP, i, C.POINTER(_Perf)])
     _sig(lib, "sei_set_profiling", i, [VP, i])
     _sig(lib, "sei_set_option", i, [VP, i, i])
+    _sig(lib, "sei_tc_gemm_check", i, [VP, VP, VP, i, i, i])
     _sig(lib, "sei_dr_setup", i, [VP, C.POINTER(RSParams), C.POINTER(i64)])
     _sig(lib, "sei_dr_num_points", i, [i])
     _sig(lib, "sei_dr_num_faces", i64, [VP])
@@ -144,6 +145,18 @@ def _ptr(a):
 
 def _colmajor(a, dtype=np.float32):
     return np.ascontiguousarray(np.swapaxes(np.asarray(a), -1, -2), dtype=dtype)
+
+
+def tc_gemm_check(A, B, terms=3):
+    """D = A B^T for one 128 x N x K tile on the tensor cores (diagnostic of the TC conventions)."""
+    lib = load_library()
+    A = np.ascontiguousarray(A, np.float32)
+    B = np.ascontiguousarray(B, np.float32)
+    D = np.empty((A.shape[0], B.shape[0]), np.float32)
+    rc = lib.sei_tc_gemm_check(_ptr(A), _ptr(B), _ptr(D), B.shape[0], A.shape[1], terms)
+    if rc != SEI_OK:
+        raise SeiError(rc, "sei_tc_gemm_check")
+    return D
 
 
 class Context:
