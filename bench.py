@@ -224,7 +224,8 @@ def run_ours(args, world, rank, local):
     from seissol_gb300 import Context
 
     hbm, peak_kind = peaks()
-    ctx = Context(ORDER, device=local)
+    prec = {"fp32": 0, "f16x3": 1}[args.precision]
+    ctx = Context(ORDER, device=local, precision=prec)
     if args.fused_local:
         ctx.set_option(1, 1)  # SEI_OPT_FUSED_LOCAL
     n = ctx.build_periodic_cube(*DIMS, perturb=PERTURB, seed=SEED + rank)
@@ -325,6 +326,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fused-local", action="store_true", help="ADER and local integral in one launch")
+    ap.add_argument("--precision", choices=("fp32", "f16x3"), default="fp32")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

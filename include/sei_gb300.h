@@ -47,6 +47,10 @@ extern "C" {
 
 /* Arithmetic of the global-matrix contractions. */
 #define SEI_PREC_FP32 0 /* CUDA-core FP32, sparse (non-zero flops only) */
+/* Mixed precision: the global-matrix contractions of the local integral on the tensor cores
+ * (tcgen05 kind::f16), each product split into three FP16 products (hi*hi + hi*lo + lo*hi) of
+ * power-of-two row-scaled operands with FP32 accumulation; everything else FP32. */
+#define SEI_PREC_F16X3 1
 
 typedef struct sei_ctx sei_ctx;
 

@@ -69,6 +69,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     os.makedirs(OBJ, exist_ok=True)
     gen_kernels.write_all(GEN, ORDERS)
     gen_kernels.write_dr_tables(GEN, (4,))
+    gen_kernels.write_tc_tables(GEN, ORDERS)
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=jobs or min(len(srcs), os.cpu_count() or 4)) as ex:
         results = list(ex.map(lambda s: _compile(s, verbose), srcs))

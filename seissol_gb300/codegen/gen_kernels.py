@@ -396,3 +396,101 @@ def write_dr_tables(outdir: str, orders=(4,)) -> list:
                 fh.write(src)
         paths.append(p)
     return paths
+
+
+# ---------------------------------------------------------------------------
+# Tensor-core tables: stacked global matrices as the B operand (N x K, K-major) of
+# tcgen05 kind::f16 MMAs, split into FP16 hi/lo after scaling every row n by 2^-f_n
+# (max |row| in [0.5, 1)); stored in the core-matrix layout (8 rows x 16 bytes blocks,
+# block (g, j) at (g * KC + j) * 128 bytes, KC = Kpad / 8).
+# ---------------------------------------------------------------------------
+def _pad(x, m):
+    return (x + m - 1) // m * m
+
+
+def _f16_split_rows(Mx):
+    """Returns (hi, lo, exps): float16 parts of Mx * 2^-exps[n] per row n."""
+    import math as _m
+    exps = np.zeros(Mx.shape[0], dtype=np.int64)
+    for n in range(Mx.shape[0]):
+        mx = np.abs(Mx[n]).max()
+        exps[n] = _m.frexp(mx)[1] if mx > 0 else 0
+    S = Mx * np.ldexp(1.0, -exps)[:, None]
+    hi = S.astype(np.float16)
+    lo = (S - hi.astype(np.float64)).astype(np.float16)
+    return hi, lo, exps
+
+
+def _core_layout(A16, kpad):
+    """N x Kpad float16 -> flat uint16 array in the K-major core-matrix layout."""
+    n = A16.shape[0]
+    kc = kpad // 8
+    out = np.zeros(n * kpad, dtype=np.uint16)
+    bits = A16.view(np.uint16)
+    for r in range(n):
+        for k in range(kpad):
+            off = (((r >> 3) * kc + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2) // 2
+            out[off] = bits[r, k]
+    return out
+
+
+def tc_operands(order):
+    """Stacked B operands of the tensor-core kernels for one order (dense float64, padded)."""
+    B, F = nb3(order), nb2(order)
+    G = global_matrices(order)
+    ops = {}
+    # CK stages: rows e * bc + k, columns l < bp: kDivMT_e[k, l]
+    for i in range(1, order):
+        bp, bc = nb3(order - i + 1), nb3(order - i)
+        N, K = _pad(3 * bc, 16), _pad(bp, 16)
+        M = np.zeros((N, K))
+        for e in range(3):
+            M[e * bc:(e + 1) * bc, :bp] = G["kDivMT"][e][:bc, :bp]
+        ops[f"ck{i}"] = M
+    # volume and local-flux traces: rows e * B + k (kDivM_e), 3 B + f F + m (fMrT_f)
+    N1, KB = _pad(3 * B + 4 * F, 16), _pad(B, 16)
+    M = np.zeros((N1, KB))
+    for e in range(3):
+        M[e * B:(e + 1) * B, :B] = G["kDivM"][e]
+    for f in range(4):
+        M[3 * B + f * F:3 * B + (f + 1) * F, :B] = G["fMrT"][f]
+    ops["vol"] = M
+    # face projections back to the volume: rows k < B, columns f F + m: rDivM_f[k, m]
+    M = np.zeros((_pad(B, 16), _pad(4 * F, 16)))
+    for f in range(4):
+        M[:B, f * F:(f + 1) * F] = G["rDivM"][f]
+    ops["rdivm"] = M
+    # neighbour traces of all four sides: rows j F + m: rT_j[m, l]
+    M = np.zeros((_pad(4 * F, 16), KB))
+    for j in range(4):
+        M[j * F:(j + 1) * F, :B] = G["rT"][j]
+    ops["rt"] = M
+    return ops
+
+
+def gen_tc_tables(order: int) -> str:
+    ops = tc_operands(order)
+    L = [f"// Generated by seissol_gb300/codegen/gen_kernels.py: tensor-core operand tables, order {order}.",
+         "#pragma once", "#include <cstdint>", f"namespace sei_tc_o{order} {{"]
+    for name, M in ops.items():
+        hi, lo, ex = _f16_split_rows(M)
+        N, K = M.shape
+        both = np.concatenate([_core_layout(hi, K), _core_layout(lo, K)])
+        L.append(f"constexpr int k{name}_N = {N}, k{name}_K = {K};")
+        L.append(f"__device__ __align__(16) const uint16_t k{name}_op[{both.size}] = {{" + ",".join(str(int(v)) for v in both) + "};")
+        L.append(f"__device__ const float k{name}_scale[{N}] = {{" + ",".join(flit(np.ldexp(1.0, int(e))) for e in ex) + "};")
+    L.append(f"}}  // namespace sei_tc_o{order}")
+    return "\n".join(L) + "\n"
+
+
+def write_tc_tables(outdir: str, orders=(4, 5, 6)) -> list:
+    os.makedirs(outdir, exist_ok=True)
+    paths = []
+    for o in orders:
+        p = os.path.join(outdir, f"tc_tables_o{o}.cuh")
+        src = gen_tc_tables(o)
+        if not os.path.exists(p) or open(p).read() != src:
+            with open(p, "w") as fh:
+                fh.write(src)
+        paths.append(p)
+    return paths

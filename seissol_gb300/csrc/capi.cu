@@ -58,6 +58,8 @@ struct sei_ctx {
   // per-launch timing (sei_set_profiling): one event before every launch plus one at the end
   bool profiling = false;
   bool fused_local = false;  // SEI_OPT_FUSED_LOCAL: ADER and local integral in one launch
+  int sms = 0;               // multiprocessors of the device (persistent tensor-core grids)
+  int* d_status = nullptr;   // device error word: 1 = a bounded wait in a kernel gave up
   std::vector<cudaEvent_t> prof_events;
   std::vector<int> prof_kind;  // kind of the launch that starts at event i (0 local, 1 neighbour)
   size_t prof_used = 0;
@@ -207,13 +209,18 @@ int launchAderOnly(sei_ctx* c, const sei::DeviceArrays& d, const float* coeffs) 
 int launchLintOnly(sei_ctx* c, const sei::DeviceArrays& d) {
   int rc = profMark(c, 0);
   if (rc) return rc;
+  if (c->cfg.precision == SEI_PREC_F16X3) {
+    if (sei::launchLintTensorCore(c->cfg.order, d, c->d_status, c->sms, c->stream) != 0)
+      return fail(c, SEI_ERR_CUDA, "tensor-core local-integral kernel launch failed");
+    return SEI_OK;
+  }
   if (c->k.lint(d, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "local-integral kernel launch failed");
   return SEI_OK;
 }
 
 // ADER followed by the local integral: two launches (default) or one fused launch.
 int launchLocal(sei_ctx* c, const sei::DeviceArrays& d, const float* coeffs) {
-  if (!c->fused_local) {
+  if (!c->fused_local || c->cfg.precision != SEI_PREC_FP32) {
     int rc = launchAderOnly(c, d, coeffs);
     return rc ? rc : launchLintOnly(c, d);
   }
@@ -359,7 +366,7 @@ int sei_create(const sei_config* cfg, sei_ctx** out) {
     delete c;
     return SEI_ERR_UNSUPPORTED;
   }
-  if (cfg->precision != SEI_PREC_FP32) {
+  if (cfg->precision != SEI_PREC_FP32 && cfg->precision != SEI_PREC_F16X3) {
     delete c;
     return SEI_ERR_UNSUPPORTED;
   }
@@ -371,7 +378,9 @@ int sei_create(const sei_config* cfg, sei_ctx** out) {
     return SEI_OK;
   }
   if (cudaSetDevice(cfg->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
+      cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, cfg->device) != cudaSuccess ||
+      cudaMalloc(&c->d_status, sizeof(int)) != cudaSuccess || cudaMemset(c->d_status, 0, sizeof(int)) != cudaSuccess) {
     cudaGetLastError();
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -391,6 +400,7 @@ void sei_destroy(sei_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   freeArrays(c);
   for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
+  cudaFree(c->d_status);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -613,7 +623,14 @@ int sei_run_host(sei_ctx* c, int kernel, double dt, int nsteps, const float* dof
 
 int sei_sync(sei_ctx* c) {
   if (!c) return SEI_ERR_ARG;
+  if (c->cfg.device < 0) return SEI_OK;
   SEI_CUDA(cudaStreamSynchronize(c->stream));
+  int st = 0;
+  SEI_CUDA(cudaMemcpy(&st, c->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (st) {
+    cudaMemset(c->d_status, 0, sizeof(int));
+    return fail(c, SEI_ERR_TIMEOUT, "a bounded wait inside a tensor-core kernel gave up");
+  }
   return SEI_OK;
 }
 

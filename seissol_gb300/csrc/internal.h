@@ -121,3 +121,21 @@ void faultFaceData(const HostMesh& m, HostFault& f);
 double fvwSteadyState(double v, double a, double b, double f0, double v0, double muw, double vw);
 void gaussLegendre01(int n, double* x, double* w);
 }  // namespace sei
+
+namespace sei {
+// Arguments of the tensor-core local-integral kernel.
+struct TcLintArgs {
+  int n;
+  float* Q;
+  const float* I;
+  const float* star_nz;
+  const float* aplus;
+  const uint8_t* ftype;
+  const uint16_t* opVol;  // pre-split FP16 operand tables (hi then lo), core-matrix layout
+  const float* scVol;     // per-row power-of-two scales of the operand tables
+  const uint16_t* opRd;
+  const float* scRd;
+  int* status;  // set to 1 when a wait gave up
+};
+int launchLintTensorCore(int order, const DeviceArrays& d, int* status, int sms, void* stream);
+}  // namespace sei

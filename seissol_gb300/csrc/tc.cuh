@@ -35,8 +35,40 @@ __host__ __device__ constexpr uint32_t idescTf32(int M, int N) {
          | ((uint32_t)(M >> 4) << 24);// M / 16
 }
 
+// Instruction descriptor of kind::f16: F32 accumulator, FP16 A and B, both K-major (K = 16 per MMA).
+__host__ __device__ constexpr uint32_t idescF16(int M, int N) {
+  return (1u << 4)                     // D format F32
+         | ((uint32_t)(N >> 3) << 17)  // N / 8 (A, B format 0 = F16)
+         | ((uint32_t)(M >> 4) << 24); // M / 16
+}
+
+// Byte offset of 16-bit element (row, k) in a K-major no-swizzle tile with kc chunks of 8 along K.
+__host__ __device__ __forceinline__ uint32_t kmajorOffset16(int row, int k, int kc) {
+  return (uint32_t)(((row >> 3) * kc + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
 __device__ __forceinline__ uint32_t smemAddr(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T, M x N x 16 (fp16).
+__device__ __forceinline__ void mmaSSf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, bool accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"((uint32_t)accum)
+      : "memory");
+}
+
+// Bulk (non-tensor) TMA copy global -> shared, completing tx bytes on the mbarrier.
+__device__ __forceinline__ void mbarExpectTx(uint64_t* mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smemAddr(mbar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulkCopyG2S(void* dst, const void* src, uint32_t bytes, uint64_t* mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                   smemAddr(dst)),
+               "l"(src), "r"(bytes), "r"(smemAddr(mbar))
+               : "memory");
 }
 
 // One full warp allocates ncols TMEM columns; the address is written to *slot (shared).

@@ -1,0 +1,74 @@
+"""Mixed-precision path (SEI_PREC_F16X3: local integral on tcgen05 tensor cores, split FP16)
+against the FP64 oracle.
+
+Tolerances: one application of the local integral 2e-5 relative L2 of the update per quantity
+(the FP32 bar); ten time steps of kernel 'all' 1e-5 relative L2 per quantity of the field (the
+accuracy bar of the mixed-precision metric).
+"""
+import numpy as np
+import pytest
+
+from oracle import dg_setup, oracle_py
+from tests.helpers import rel_l2_per_quantity, seeded_dofs
+
+pytestmark = pytest.mark.gpu
+
+PREC_F16X3 = 1
+
+
+def _ctx(order, precision, dims=(4, 4, 4), seed=3):
+    from seissol_gb300 import Context
+    ctx = Context(order, device=0, precision=precision)
+    n = ctx.build_periodic_cube(*dims, perturb=0.1, seed=seed)
+    q0 = seeded_dofs(n, order, seed)
+    ctx.set_dofs(q0)
+    return ctx, n, q0
+
+
+@pytest.mark.parametrize("order", [4, 5, 6])
+def test_local_integral_tensor_cores(built_lib, order):
+    ctx, n, q0 = _ctx(order, PREC_F16X3)
+    cells = ctx.get_cells()
+    dt = ctx.cfl_timestep(0.5)
+    ctx.compute_ader(dt)
+    ctx.sync()
+    i_gpu = ctx.get_time_integrated()
+    ctx.compute_local_integral()
+    ctx.sync()
+    q_gpu = ctx.get_dofs()
+    o = oracle_py.Oracle(order)
+    q_ref = o.local(q0, i_gpu.astype(np.float64), cells["star"].astype(np.float64), cells["AplusT"].astype(np.float64),
+                    cells["face_type"])
+    errs = rel_l2_per_quantity(q_gpu - q0, q_ref - q0)
+    assert max(errs) < 2e-5, errs
+    ctx.close()
+
+
+@pytest.mark.parametrize("order", [4, 6])
+def test_ten_steps_mixed_precision(built_lib, order):
+    ctx, n, q0 = _ctx(order, PREC_F16X3)
+    cells = ctx.get_cells()
+    dt = ctx.cfl_timestep(0.5)
+    q_ref = oracle_py.Oracle(order).steps(q0, cells["star"].astype(np.float64), cells["AplusT"].astype(np.float64),
+                                          cells["AminusT"].astype(np.float64), cells["neighbor"], cells["side"],
+                                          cells["orient"], dt, 10, cells["face_type"])
+    ctx.run("all", dt, 10)
+    ctx.sync()
+    errs = rel_l2_per_quantity(ctx.get_dofs(), q_ref)
+    assert max(errs) < 1e-5, errs
+    ctx.close()
+
+
+def test_mixed_and_fp32_agree_on_larger_mesh(built_lib):
+    """Both precisions on the same 8x8x8-cube mesh for 5 steps stay within 1e-5 of each other."""
+    a, n, q0 = _ctx(6, 0, dims=(8, 8, 8), seed=5)
+    b, _, _ = _ctx(6, PREC_F16X3, dims=(8, 8, 8), seed=5)
+    dt = a.cfl_timestep(0.5)
+    a.run("all", dt, 5)
+    b.run("all", dt, 5)
+    a.sync()
+    b.sync()
+    errs = rel_l2_per_quantity(b.get_dofs(), a.get_dofs())
+    assert max(errs) < 1e-5, errs
+    a.close()
+    b.close()
