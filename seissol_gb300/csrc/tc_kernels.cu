@@ -162,13 +162,16 @@ __global__ void __launch_bounds__(128, 1) sei_lint_tc(sei::TcLintArgs A) {
   const uint16_t* volLo = opVol + D::N1 * D::KB;
   const uint16_t* rdHi = opRd;
   const uint16_t* rdLo = opRd + D::N2 * D::K2;
-  const int r = tid, c = r / 9, q = r % 9;
+  const int r = tid, q = r % 9;
   const bool rowOk = r < 9 * kCellsPerTile;
+  // The padding rows 126 and 127 mix the rows of cell 13: their results are never stored, and
+  // every exchange read 9 c + s then stays inside the 128 rows of the buffer.
+  const int c = rowOk ? r / 9 : kCellsPerTile - 1;
   const int s0 = c_tsrc[q][0], s1 = c_tsrc[q][1], s2 = c_tsrc[q][2];
   const int ntiles = (A.n + kCellsPerTile - 1) / kCellsPerTile;
   for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     const int cell = tile * kCellsPerTile + c;
-    const bool valid = rowOk && cell < A.n;
+    const bool valid = rowOk && cell < A.n;  // padding rows never store
     const int cl = valid ? cell : 0;
     float st[3][3];
 #pragma unroll
