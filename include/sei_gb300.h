@@ -189,13 +189,48 @@ int sei_dr_get_state(sei_ctx* ctx, int field, double* out /*[nf][npts]*/);
 int sei_dr_set_state(sei_ctx* ctx, int field, const double* in /*[nf][npts]*/);
 /* Imposed states of the last step, [nf][9][npts] each (points fastest). */
 int sei_dr_get_imposed(sei_ctx* ctx, float* plus, float* minus);
-/* Accumulated Newton iterations over all points and steps since the last reset. */
-int sei_dr_newton_iterations(sei_ctx* ctx, int64_t* total, int64_t* solves_points);
+/* Accumulated Newton iterations over all points and steps since the last reset: *total over all
+ * solves, *first (may be NULL) over the first solve of each time point (the solve a warm start
+ * replaces); *solves_points = faces x points. */
+int sei_dr_newton_iterations(sei_ctx* ctx, int64_t* total, int64_t* solves_points, int64_t* first);
 int sei_dr_reset_counters(sei_ctx* ctx);
 /* Runs only the fault kernel (after a step that stored the derivatives). */
 int sei_dr_faces_step(sei_ctx* ctx, double dt);
 /* Slot of each fault cell in the derivative buffer ([n], -1 for cells without a fault face). */
 int sei_dr_get_slots(sei_ctx* ctx, int32_t* slots);
+
+/* Learned warm start of the slip-rate Newton solve (no counterpart in the reference, whose solve
+ * starts from the previous slip rate, src/DynamicRupture/FrictionLaws/CpuImpl/RateAndState.h:340-417).
+ * Network 5 -> 64 -> 64 -> 1 with tanh, FP32, on the raw inputs (normal stress sn, absolute shear
+ * traction tau, state variable psi, a, b) through fixed dimensionless features
+ * (tau / (|sn| a), psi / a, ln(|sn| a), a, b), each normalised as (f - norm[i]) * norm[5 + i]; its
+ * output y gives t = y * norm[11] + norm[10] and the guess ln V = norm[12] + tau / (|sn| a) - psi / a - t,
+ * with norm[12] = ln(2 V0) and norm[13..15] = 0.  Parameters, in this order: W1 [64][5], b1 [64],
+ * W2 [64][64], b2 [64], W3 [64], b3 (sei_mlp_num_params() floats).  The fault kernel evaluates it
+ * only for the first Newton solve of each time point and only starts from the guess when the
+ * residual there is smaller than at the previous slip rate; a solve whose residual stops falling
+ * falls back to the plain start, so the converged slip rates are those of the plain solve to
+ * within the Newton tolerance. */
+int sei_mlp_num_params(void);
+/* Records up to `capacity` training samples [6] = (inputs [5], log10 converged slip rate) from the
+ * first, plainly started Newton solve of each point in later fault steps (0 stops recording). */
+int sei_dr_record_samples(sei_ctx* ctx, int64_t capacity);
+/* Copies min(max, recorded) samples to out [.][6]; *count = the recorded number (<= capacity). */
+int sei_dr_get_samples(sei_ctx* ctx, float* out, int64_t max, int64_t* count);
+/* Trains the context's network on the GPU (Adam, full batch, cosine-decayed rate from lr, seeded
+ * Glorot initialisation), `samples` [n][6] from the host or NULL for the recorded samples; the
+ * normalisation is the samples' mean and standard deviation.  Mean-squared losses of the first
+ * and last step are returned in normalised units. */
+int sei_mlp_train(sei_ctx* ctx, const float* samples, int64_t n, int steps, float lr, uint64_t seed, float* loss_first,
+                  float* loss_last);
+int sei_mlp_get(sei_ctx* ctx, float* params, float* norm /*[16]*/);
+int sei_mlp_set(sei_ctx* ctx, const float* params, const float* norm /*[16]*/);
+/* Turns the warm start of the fault kernel on or off (needs a network). */
+int sei_dr_warm_start(sei_ctx* ctx, int on);
+/* Context-free checks on the current device: gradient of the mean-squared loss (normalised target)
+ * over samples [n][6] and the network's log10 slip rate for each sample (target column ignored). */
+int sei_mlp_gradient(const float* params, const float* norm, const float* samples, int64_t n, float* grads, float* loss);
+int sei_mlp_predict(const float* params, const float* norm, const float* samples, int64_t n, float* out);
 
 /* Per-launch device timing: when on, every kernel launch of sei_run is bracketed by CUDA events on the
  * context stream; sei_kernel_times_ms sums the durations of the last sei_run per kernel kind. */

@@ -176,14 +176,33 @@ static int newton(const oracle_rs_params* P, double a, double psi, double sn, do
   return P->max_newton;
 }
 
-/* Warm-start network 5 -> 64 -> 64 -> 1 (tanh), float32: returns log10 of the guessed slip rate.
- * Parameters W1[64][5], b1[64], W2[64][64], b2[64], W3[64], b3; norm[0..4] input shifts,
- * norm[5..9] input scales, norm[10..11] output shift and scale. */
+/* Warm-start network 5 -> 64 -> 64 -> 1 (tanh), float32: returns the natural log of the guessed
+ * slip rate.  Parameters W1[64][5], b1[64], W2[64][64], b2[64], W3[64], b3.  The inputs are the
+ * fixed features (tau / (|sn| a), psi / a, ln(|sn| a), a, b) with |sn| a floored at 1 Pa,
+ * normalised by norm[0..4] (shift) and norm[5..9] (scale); the output y gives
+ * r = y norm[11] + norm[10] and ln V = norm[12] + tau / (|sn| a) - psi / a - softplus(z) - r with
+ * z = tau / (|sn| a) - psi / a - ln(|sn| a). */
 #define MLP_H 64
+/* Points the network applies to: |sn| a > 1 Pa and tau < 500 |sn| a. */
+static int mlp_usable(double sn, double tau, double a) {
+  const double an = fabs(sn) * a;
+  return an > 1.0 && tau < 500.0 * an;
+}
+void oracle_mlp_features(double sn, double tau, double psi, double a, double b, double* f) {
+  double an = fabs(sn) * a;
+  if (!(an > 1.0)) an = 1.0;
+  f[0] = tau / an;
+  f[1] = psi / a;
+  f[2] = log(an);
+  f[3] = a;
+  f[4] = b;
+}
+
 double oracle_mlp_forward(const float* w, const float* norm, double sn, double tau, double psi, double a, double b) {
-  const float x[5] = {(float)((sn - norm[0]) * norm[5]), (float)((tau - norm[1]) * norm[6]),
-                      (float)((psi - norm[2]) * norm[7]), (float)((a - norm[3]) * norm[8]),
-                      (float)((b - norm[4]) * norm[9])};
+  double f[5];
+  oracle_mlp_features(sn, tau, psi, a, b, f);
+  float x[5];
+  for (int i = 0; i < 5; ++i) x[i] = (float)((f[i] - norm[i]) * norm[5 + i]);
   const float* W1 = w;
   const float* b1 = W1 + MLP_H * 5;
   const float* W2 = b1 + MLP_H;
@@ -202,22 +221,28 @@ double oracle_mlp_forward(const float* w, const float* norm, double sn, double t
     for (int i = 0; i < MLP_H; ++i) s = fmaf(W2[j * MLP_H + i], h1[i], s);
     out = fmaf(W3[j], tanhf(s), out);
   }
-  return (double)out * norm[11] + norm[10];
+  const double z = f[0] - f[1] - f[2];
+  const double softplus = z > 30.0 ? z : log1p(exp(z));
+  return norm[12] + f[0] - f[1] - softplus - ((double)out * norm[11] + norm[10]);
 }
 
 /* Friction solve of all faces for one time step.  State arrays are [nfaces][npts] float64:
  * psi, v1, v2, slip1, slip2, slip (accumulated magnitude), mu, traction1, traction2;
  * init[nfaces][3][npts] holds sn0, tau1_0, tau2_0.  With mlp non-null the first Newton solve
- * of every time point starts from the network's guess and falls back to the plain start
- * (previous slip rate) when its residual does not fall.  newton_iters[nfaces][npts]
- * accumulates the Newton iteration counts. */
+ * of every time point starts from the network's guess when its residual is below that of the
+ * plain start (previous slip rate), and falls back to the plain start when the residual from
+ * the guess stops falling.  newton_iters[nfaces][npts] accumulates the Newton iteration counts
+ * and first_iters (optional) those of the first solve of each time point.  With rec non-null the
+ * inputs and log10 of the converged slip rate of every plainly started, converged first solve are
+ * appended as [6] floats at rec[(*rec_count)++] (up to rec_cap). */
 
 void oracle_dr_friction(int npts, int nts, int64_t nfaces, const oracle_rs_params* P, const oracle_imp* imp,
                         const real* qip, const real* qim, const double* a, const double* init, double* psi,
                         double* v1, double* v2, double* slip1, double* slip2, double* slip, double* mu,
                         double* trac1, double* trac2, const double* deltat, const double* tweights,
                         const double* resample, real* isp, real* ism, int64_t* newton_iters,
-                        const float* mlp, const float* mlp_norm) {
+                        const float* mlp, const float* mlp_norm, int64_t* first_iters, float* rec,
+                        int64_t rec_cap, int64_t* rec_count) {
 #pragma omp parallel
   {
     double* buf = (double*)malloc(sizeof(double) * (size_t)npts * 12);
@@ -273,16 +298,35 @@ void oracle_dr_friction(int npts, int nts, int64_t nfaces, const oracle_rs_param
             const double ak = a[fo + k];
             psib[k] = state_update(P, ak, sref[k], dt, lsr[k]);
             double vnew = 0, munew = 0;
-            int conv = 0;
-            if (mlp && j == 0) {
+            int conv = 0, its = 0;
+            if (mlp && j == 0 && mlp_usable(sns[k], taus[k], ak)) {
               double lg = oracle_mlp_forward(mlp, mlp_norm, sns[k], taus[k], psib[k], ak, P->b);
-              lg = lg < -40.0 ? -40.0 : (lg > 3.0 ? 3.0 : lg);
-              newton_iters[fo + k] +=
-                  newton(P, ak, psib[k], sns[k], taus[k], im->inv_etas, pow(10.0, lg), &vnew, &munew, &conv, 1);
+              lg = lg < -103.616329 ? -103.616329 : (lg > 6.907755 ? 6.907755 : lg); /* 1e-45 .. 1e3 m/s */
+              const double g0 = exp(lg);
+              const double cl = psib[k] / ak, ce = compute_cexp(cl), clin = 0.5 / P->v0;
+              const double rg = -im->inv_etas * (fabs(sns[k]) * ak * arsinhexp(clin * g0, cl, ce) - taus[k]) - g0;
+              const double rp = -im->inv_etas * (fabs(sns[k]) * ak * arsinhexp(clin * vmag[k], cl, ce) - taus[k]) - vmag[k];
+              if (fabs(rg) < fabs(rp)) its += newton(P, ak, psib[k], sns[k], taus[k], im->inv_etas, g0, &vnew, &munew, &conv, 1);
             }
-            if (!conv)
-              newton_iters[fo + k] +=
-                  newton(P, ak, psib[k], sns[k], taus[k], im->inv_etas, vmag[k], &vnew, &munew, &conv, 0);
+            if (!conv) {
+              its += newton(P, ak, psib[k], sns[k], taus[k], im->inv_etas, vmag[k], &vnew, &munew, &conv, 0);
+              if (rec && j == 0 && conv && mlp_usable(sns[k], taus[k], ak)) {
+                int64_t idx;
+#pragma omp atomic capture
+                idx = (*rec_count)++;
+                if (idx < rec_cap) {
+                  float* o = rec + idx * 6;
+                  o[0] = (float)sns[k];
+                  o[1] = (float)taus[k];
+                  o[2] = (float)psib[k];
+                  o[3] = (float)ak;
+                  o[4] = (float)P->b;
+                  o[5] = (float)log10(vnew);
+                }
+              }
+            }
+            newton_iters[fo + k] += its;
+            if (first_iters && j == 0) first_iters[fo + k] += its;
             lsr[k] = 0.5 * (vmag[k] + vnew);
             convo[k] = fabs(vmag[k] - vnew) < P->state_tol;
             vmag[k] = vnew;

@@ -159,8 +159,12 @@ class DROracle:
                                      _p(tinvt), _p(self.v3m), _p(np.ascontiguousarray(coll, np.float64)), _p(out))
         return out
 
-    def friction(self, qip, qim, state, a, init, deltat, tweights, mlp=None):
-        """Updates state (dict of [nf, npts] float64 arrays) in place; returns imposed states and iterations."""
+    def friction(self, qip, qim, state, a, init, deltat, tweights, mlp=None, record=None, first_iters=None):
+        """Updates state (dict of [nf, npts] float64 arrays) in place; returns imposed states and iterations.
+
+        record: optional [cap, 6] float32 array with a one-element int64 counter, (rec, count),
+        receiving the samples of plainly started, converged first solves; first_iters: optional
+        [nf, npts] int64 array accumulating the iterations of the first solve of each time point."""
         nf = qip.shape[0]
         nts = qip.shape[1]
         imp = np.ascontiguousarray(self.f["imp"][:, :7], np.float64)
@@ -179,7 +183,11 @@ class DROracle:
                                   *[_p(state[k]) for k in STATE_FIELDS],
                                   _p(np.ascontiguousarray(deltat, np.float64)),
                                   _p(np.ascontiguousarray(tweights, np.float64)), _p(self.res), _p(isp), _p(ism),
-                                  _p(iters), _p(w) if w is not None else None, _p(n) if n is not None else None)
+                                  _p(iters), _p(w) if w is not None else None, _p(n) if n is not None else None,
+                                  _p(first_iters) if first_iters is not None else None,
+                                  _p(record[0]) if record is not None else None,
+                                  C.c_int64(record[0].shape[0] if record is not None else 0),
+                                  _p(record[1]) if record is not None else None)
         return isp, ism, iters
 
     def nodal_flux(self, Q, cells, side, rel, imposed, flux):
@@ -192,7 +200,7 @@ class DROracle:
         return Q
 
 
-def dr_full_step(o, dro, Q, cells, faces, state, a, init, dt, mlp=None):
+def dr_full_step(o, dro, Q, cells, faces, state, a, init, dt, mlp=None, record=None, first_iters=None):
     """One step of proxy kernel all_dr in FP64: ADER + local, fault, neighbour (the GPU's order)."""
     order = o.order
     ft = cells["face_type"]
@@ -205,7 +213,7 @@ def dr_full_step(o, dro, Q, cells, faces, state, a, init, dt, mlp=None):
     ps, ms, rel = faces["sides"][:, 0], faces["sides"][:, 1], faces["sides"][:, 2]
     qip = dro.interpolate(d[pc], ps, np.zeros_like(ps), coll)
     qim = dro.interpolate(d[mc], ms, rel, coll)
-    isp, ism, iters = dro.friction(qip, qim, state, a, init, deltat, tw, mlp)
+    isp, ism, iters = dro.friction(qip, qim, state, a, init, deltat, tw, mlp, record, first_iters)
     Q = dro.nodal_flux(Q, pc, ps, np.zeros_like(ps), isp, faces["fluxSolverPlus"])
     Q = dro.nodal_flux(Q, mc, ms, rel, ism, faces["fluxSolverMinus"])
     Q = o.neighbor(Q, I, cells["AminusT"].astype(np.float64), cells["neighbor"], cells["side"], cells["orient"], ft)

@@ -7,6 +7,9 @@ fallback: without the built library every entry point raises.
 """
 from .lib import (  # noqa: F401
     tc_gemm_check,
+    mlp_gradient,
+    mlp_predict,
+    mlp_num_params,
     Context,
     RSParams,
     DR_FIELDS,

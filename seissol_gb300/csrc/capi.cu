@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "mlp.cuh"
 
 namespace sei {
 OrderKernels orderKernels4();
@@ -53,8 +54,12 @@ struct sei_ctx {
   uint8_t *d_ps = nullptr, *d_ms = nullptr, *d_rel = nullptr;
   float *d_tinvt = nullptr, *d_fsp = nullptr, *d_fsm = nullptr, *d_isp = nullptr, *d_ism = nullptr;
   double *d_imp = nullptr, *d_state = nullptr;  // state: 13 fields x [nf][npts]
-  float* d_mlp = nullptr;
-  float mlp_norm[12] = {0};
+  float* d_mlp = nullptr;  // trained warm-start network (nullptr: none)
+  float mlp_norm[sei_mlp::kNorm] = {0};
+  bool warm_start = false;
+  float* d_rec = nullptr;  // recorded training samples [rec_cap][6]
+  unsigned* d_rec_count = nullptr;
+  unsigned rec_cap = 0;
   // per-launch timing (sei_set_profiling): one event before every launch plus one at the end
   bool profiling = false;
   bool fused_local = false;  // SEI_OPT_FUSED_LOCAL: ADER and local integral in one launch
@@ -95,11 +100,11 @@ void freeArrays(sei_ctx* c) {
   cudaFree(c->dslot);
   for (void* p : {(void*)c->d_pc, (void*)c->d_mc, (void*)c->d_pslot, (void*)c->d_mslot, (void*)c->d_iters, (void*)c->d_ps,
                   (void*)c->d_ms, (void*)c->d_rel, (void*)c->d_tinvt, (void*)c->d_fsp, (void*)c->d_fsm, (void*)c->d_isp,
-                  (void*)c->d_ism, (void*)c->d_imp, (void*)c->d_state, (void*)c->d_mlp})
+                  (void*)c->d_ism, (void*)c->d_imp, (void*)c->d_state})
     cudaFree(p);
   c->d_pc = c->d_mc = c->d_pslot = c->d_mslot = c->d_iters = nullptr;
   c->d_ps = c->d_ms = c->d_rel = nullptr;
-  c->d_tinvt = c->d_fsp = c->d_fsm = c->d_isp = c->d_ism = c->d_mlp = nullptr;
+  c->d_tinvt = c->d_fsp = c->d_fsm = c->d_isp = c->d_ism = nullptr;
   c->d_imp = c->d_state = nullptr;
   c->dslot = nullptr;
   c->dr_ready = false;
@@ -296,8 +301,11 @@ sei::DrArgs drArgs(sei_ctx* c, double dt) {
     }
   }
   a.deltat[N - 1] += x[0] * dt;
-  a.mlp = c->d_mlp;
-  for (int i = 0; i < 12; ++i) a.mlp_norm[i] = c->mlp_norm[i];
+  a.mlp = c->warm_start ? c->d_mlp : nullptr;
+  for (int i = 0; i < sei_mlp::kNorm; ++i) a.mlp_norm[i] = c->mlp_norm[i];
+  a.rec = c->d_rec;
+  a.rec_count = c->d_rec_count;
+  a.rec_cap = c->rec_cap;
   return a;
 }
 
@@ -401,6 +409,9 @@ void sei_destroy(sei_ctx* c) {
   freeArrays(c);
   for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
   cudaFree(c->d_status);
+  cudaFree(c->d_rec);
+  cudaFree(c->d_rec_count);
+  cudaFree(c->d_mlp);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -694,7 +705,7 @@ int sei_dr_setup(sei_ctx* c, const sei_rs_params* p, int64_t* nfaces) {
   c->derivs = nullptr;
   bool ok = dalloc((void**)&c->derivs, 2 * nf * dsz) && dalloc((void**)&c->dslot, c->n * 4) &&
             dalloc((void**)&c->d_pc, nf * 4) && dalloc((void**)&c->d_mc, nf * 4) && dalloc((void**)&c->d_pslot, nf * 4) &&
-            dalloc((void**)&c->d_mslot, nf * 4) && dalloc((void**)&c->d_iters, nf * np * 4) &&
+            dalloc((void**)&c->d_mslot, nf * 4) && dalloc((void**)&c->d_iters, 2 * nf * np * 4) &&
             dalloc((void**)&c->d_ps, nf) && dalloc((void**)&c->d_ms, nf) && dalloc((void**)&c->d_rel, nf) &&
             dalloc((void**)&c->d_tinvt, nf * 81 * 4) && dalloc((void**)&c->d_fsp, nf * 81 * 4) &&
             dalloc((void**)&c->d_fsm, nf * 81 * 4) && dalloc((void**)&c->d_isp, nf * 9 * np * 4) &&
@@ -718,7 +729,7 @@ int sei_dr_setup(sei_ctx* c, const sei_rs_params* p, int64_t* nfaces) {
   SEI_CUDA(cudaMemcpy(c->d_fsm, F.fsm.data(), nf * 81 * 4, cudaMemcpyHostToDevice));
   SEI_CUDA(cudaMemcpy(c->d_imp, F.imp.data(), nf * 8 * 8, cudaMemcpyHostToDevice));
   SEI_CUDA(cudaMemcpy(c->d_state, st.data(), st.size() * 8, cudaMemcpyHostToDevice));
-  SEI_CUDA(cudaMemset(c->d_iters, 0, nf * np * 4));
+  SEI_CUDA(cudaMemset(c->d_iters, 0, 2 * nf * np * 4));
   SEI_CUDA(cudaMemset(c->d_isp, 0, nf * 9 * np * 4));
   SEI_CUDA(cudaMemset(c->d_ism, 0, nf * 9 * np * 4));
   SEI_CUDA(cudaMemset(c->derivs, 0, 2 * nf * dsz));
@@ -789,23 +800,25 @@ int sei_dr_get_imposed(sei_ctx* c, float* plus, float* minus) {
   return SEI_OK;
 }
 
-int sei_dr_newton_iterations(sei_ctx* c, int64_t* total, int64_t* points) {
+int sei_dr_newton_iterations(sei_ctx* c, int64_t* total, int64_t* points, int64_t* first) {
   if (!c || !total || !points) return SEI_ERR_ARG;
   if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up");
-  std::vector<int32_t> it((size_t)c->fault.nf * c->npts);
+  const size_t np = (size_t)c->fault.nf * c->npts;
+  std::vector<int32_t> it(2 * np);
   SEI_CUDA(cudaMemcpyAsync(it.data(), c->d_iters, it.size() * 4, cudaMemcpyDeviceToHost, c->stream));
   SEI_CUDA(cudaStreamSynchronize(c->stream));
-  int64_t s = 0;
-  for (int32_t v : it) s += v;
+  int64_t s = 0, f = 0;
+  for (size_t i = 0; i < np; ++i) s += it[i], f += it[np + i];
   *total = s;
-  *points = (int64_t)it.size();
+  *points = (int64_t)np;
+  if (first) *first = f;
   return SEI_OK;
 }
 
 int sei_dr_reset_counters(sei_ctx* c) {
   if (!c) return SEI_ERR_ARG;
   if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up");
-  SEI_CUDA(cudaMemsetAsync(c->d_iters, 0, (size_t)c->fault.nf * c->npts * 4, c->stream));
+  SEI_CUDA(cudaMemsetAsync(c->d_iters, 0, 2 * (size_t)c->fault.nf * c->npts * 4, c->stream));
   return SEI_OK;
 }
 
@@ -820,6 +833,249 @@ int sei_dr_get_slots(sei_ctx* c, int32_t* slots) {
   if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up");
   SEI_CUDA(cudaMemcpy(slots, c->dslot, (size_t)c->n * 4, cudaMemcpyDeviceToHost));
   return SEI_OK;
+}
+
+int sei_mlp_num_params(void) { return sei::mlpNumParams(); }
+
+int sei_dr_record_samples(sei_ctx* c, int64_t capacity) {
+  if (!c || capacity < 0 || capacity > (int64_t)1 << 31) return SEI_ERR_ARG;
+  if (c->cfg.device < 0) return fail(c, SEI_ERR_STATE, "host-only context");
+  cudaFree(c->d_rec);
+  cudaFree(c->d_rec_count);
+  c->d_rec = nullptr;
+  c->d_rec_count = nullptr;
+  c->rec_cap = 0;
+  if (capacity == 0) return SEI_OK;
+  if (cudaMalloc(&c->d_rec, (size_t)capacity * 6 * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&c->d_rec_count, sizeof(unsigned)) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(c, SEI_ERR_OOM, "sample buffer allocation failed");
+  }
+  SEI_CUDA(cudaMemset(c->d_rec_count, 0, sizeof(unsigned)));
+  c->rec_cap = (unsigned)capacity;
+  return SEI_OK;
+}
+
+int sei_dr_get_samples(sei_ctx* c, float* out, int64_t max, int64_t* count) {
+  if (!c || !count) return SEI_ERR_ARG;
+  if (!c->d_rec) return fail(c, SEI_ERR_STATE, "no sample recording active");
+  unsigned n = 0;
+  SEI_CUDA(cudaStreamSynchronize(c->stream));
+  SEI_CUDA(cudaMemcpy(&n, c->d_rec_count, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  const int64_t avail = n < c->rec_cap ? n : c->rec_cap;
+  *count = avail;
+  if (out && max > 0) {
+    const int64_t k = avail < max ? avail : max;
+    SEI_CUDA(cudaMemcpy(out, c->d_rec, (size_t)k * 6 * sizeof(float), cudaMemcpyDeviceToHost));
+  }
+  return SEI_OK;
+}
+
+namespace {
+constexpr size_t kNormBytes = sizeof(float) * sei_mlp::kNorm;
+
+// Normalisation of a sample set: mean and 1 / standard deviation of the five features, mean and
+// standard deviation of the target (scale 1 for constant columns), ln(2 V0).
+void sampleNorm(const float* smp, int64_t n, double v0, float* norm) {
+  const double ln2v0 = std::log(2.0 * v0);
+  double sum[6] = {0}, sq[6] = {0};
+  for (int64_t i = 0; i < n; ++i) {
+    const float* r = smp + i * 6;
+    double f[6];
+    sei_mlp::features(r[0], r[1], r[2], r[3], r[4], f);
+    f[5] = sei_mlp::target(f, ln2v0, r[5]);
+    for (int k = 0; k < 6; ++k) {
+      sum[k] += f[k];
+      sq[k] += f[k] * f[k];
+    }
+  }
+  for (int k = 0; k < sei_mlp::kNorm; ++k) norm[k] = 0.f;
+  for (int k = 0; k < 6; ++k) {
+    const double m = sum[k] / (double)n;
+    const double var = sq[k] / (double)n - m * m;
+    const double sd = var > 1e-12 * (1.0 + m * m) ? std::sqrt(var) : 0.0;
+    if (k < 5) {
+      norm[k] = (float)m;
+      norm[5 + k] = sd > 0 ? (float)(1.0 / sd) : 1.f;
+    } else {
+      norm[10] = (float)m;
+      norm[11] = sd > 0 ? (float)sd : 1.f;
+    }
+  }
+  norm[12] = (float)ln2v0;
+}
+
+// Keeps the samples the network applies to (sei_mlp::usable).
+std::vector<float> usableSamples(const float* smp, int64_t n) {
+  std::vector<float> out;
+  out.reserve((size_t)n * 6);
+  for (int64_t i = 0; i < n; ++i)
+    if (sei_mlp::usable(smp[i * 6], smp[i * 6 + 1], smp[i * 6 + 3])) out.insert(out.end(), smp + i * 6, smp + i * 6 + 6);
+  return out;
+}
+
+// Splits [n][6] samples into inputs [n][5] and targets [n].
+void splitSamples(const float* smp, int64_t n, std::vector<float>& X, std::vector<float>& T) {
+  X.resize((size_t)n * 5);
+  T.resize((size_t)n);
+  for (int64_t i = 0; i < n; ++i) {
+    for (int k = 0; k < 5; ++k) X[i * 5 + k] = smp[i * 6 + k];
+    T[i] = smp[i * 6 + 5];
+  }
+}
+}  // namespace
+
+int sei_mlp_train(sei_ctx* c, const float* samples, int64_t n, int steps, float lr, uint64_t seed, float* loss_first,
+                  float* loss_last) {
+  if (!c || steps <= 0 || !(lr > 0)) return SEI_ERR_ARG;
+  if (c->cfg.device < 0) return fail(c, SEI_ERR_STATE, "host-only context");
+  std::vector<float> host;
+  if (!samples) {
+    int64_t cnt = 0;
+    int rc = sei_dr_get_samples(c, nullptr, 0, &cnt);
+    if (rc) return rc;
+    host.resize((size_t)cnt * 6);
+    rc = sei_dr_get_samples(c, host.data(), cnt, &cnt);
+    if (rc) return rc;
+    n = cnt;
+    samples = host.data();
+  }
+  const std::vector<float> kept = usableSamples(samples, n);
+  n = (int64_t)kept.size() / 6;
+  samples = kept.data();
+  if (n < 16) return fail(c, SEI_ERR_ARG, "too few training samples");
+  std::vector<float> X, T;
+  splitSamples(samples, n, X, T);
+  if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up (the network needs V0)");
+  float norm[sei_mlp::kNorm];
+  sampleNorm(samples, n, c->rs.v0, norm);
+  const int np = sei::mlpNumParams();
+  std::vector<float> P(np, 0.f);
+  // Glorot-uniform initialisation (seeded), zero biases
+  uint64_t z = seed;
+  auto uni = [&](double lim) {
+    z += 0x9E3779B97F4A7C15ull;
+    uint64_t x = z;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    x ^= x >> 31;
+    return (float)(lim * (2.0 * ((x >> 11) * (1.0 / 9007199254740992.0)) - 1.0));
+  };
+  const int H = 64;
+  for (int i = 0; i < H * 5; ++i) P[i] = uni(std::sqrt(6.0 / (5 + H)));
+  for (int i = 0; i < H * H; ++i) P[H * 5 + H + i] = uni(std::sqrt(6.0 / (2 * H)));
+  for (int i = 0; i < H; ++i) P[H * 5 + H + H * H + H + i] = uni(std::sqrt(6.0 / (H + 1)));
+  float *dP = nullptr, *dG = nullptr, *dM = nullptr, *dV = nullptr, *dL = nullptr, *dX = nullptr, *dT = nullptr, *dN = nullptr;
+  auto cleanup = [&]() {
+    for (float* p : {dG, dM, dV, dL, dX, dT, dN}) cudaFree(p);
+  };
+  if (cudaMalloc(&dP, np * 4) || cudaMalloc(&dG, np * 4) || cudaMalloc(&dM, np * 4) || cudaMalloc(&dV, np * 4) ||
+      cudaMalloc(&dL, 4) || cudaMalloc(&dX, X.size() * 4) || cudaMalloc(&dT, T.size() * 4) || cudaMalloc(&dN, kNormBytes)) {
+    cudaGetLastError();
+    cudaFree(dP);
+    cleanup();
+    return fail(c, SEI_ERR_OOM, "training buffers");
+  }
+  int rc = SEI_OK;
+  if (cudaMemcpy(dP, P.data(), np * 4, cudaMemcpyHostToDevice) || cudaMemset(dM, 0, np * 4) || cudaMemset(dV, 0, np * 4) ||
+      cudaMemcpy(dX, X.data(), X.size() * 4, cudaMemcpyHostToDevice) ||
+      cudaMemcpy(dT, T.data(), T.size() * 4, cudaMemcpyHostToDevice) || cudaMemcpy(dN, norm, kNormBytes, cudaMemcpyHostToDevice))
+    rc = fail(c, SEI_ERR_CUDA, "training upload failed");
+  for (int st = 0; st < steps && rc == SEI_OK; ++st) {
+    const float lrt = lr * (0.05f + 0.95f * 0.5f * (1.f + std::cos(3.14159265f * st / steps)));
+    if (cudaMemsetAsync(dG, 0, np * 4, c->stream) || cudaMemsetAsync(dL, 0, 4, c->stream) ||
+        sei::launchMlpGrad(dP, dN, dX, dT, (int)n, dG, dL, c->sms, c->stream) ||
+        sei::launchMlpAdam(dP, dG, dM, dV, lrt, st + 1, c->stream)) {
+      rc = fail(c, SEI_ERR_CUDA, "training step failed");
+      break;
+    }
+    if (st == 0 || st == steps - 1) {
+      float l = 0;
+      if (cudaMemcpyAsync(&l, dL, 4, cudaMemcpyDeviceToHost, c->stream) || cudaStreamSynchronize(c->stream)) {
+        rc = fail(c, SEI_ERR_CUDA, "loss read failed");
+        break;
+      }
+      if (st == 0 && loss_first) *loss_first = l;
+      if (st == steps - 1 && loss_last) *loss_last = l;
+    }
+  }
+  cleanup();
+  if (rc) {
+    cudaFree(dP);
+    return rc;
+  }
+  cudaFree(c->d_mlp);
+  c->d_mlp = dP;
+  std::memcpy(c->mlp_norm, norm, sizeof(norm));
+  return SEI_OK;
+}
+
+int sei_mlp_get(sei_ctx* c, float* params, float* norm) {
+  if (!c || !params || !norm) return SEI_ERR_ARG;
+  if (!c->d_mlp) return fail(c, SEI_ERR_STATE, "no network");
+  SEI_CUDA(cudaMemcpy(params, c->d_mlp, sei::mlpNumParams() * 4, cudaMemcpyDeviceToHost));
+  std::memcpy(norm, c->mlp_norm, kNormBytes);
+  return SEI_OK;
+}
+
+int sei_mlp_set(sei_ctx* c, const float* params, const float* norm) {
+  if (!c || !params || !norm) return SEI_ERR_ARG;
+  if (c->cfg.device < 0) return fail(c, SEI_ERR_STATE, "host-only context");
+  if (!c->d_mlp && cudaMalloc(&c->d_mlp, sei::mlpNumParams() * 4) != cudaSuccess) return fail(c, SEI_ERR_OOM, "network");
+  SEI_CUDA(cudaMemcpy(c->d_mlp, params, sei::mlpNumParams() * 4, cudaMemcpyHostToDevice));
+  std::memcpy(c->mlp_norm, norm, kNormBytes);
+  return SEI_OK;
+}
+
+int sei_dr_warm_start(sei_ctx* c, int on) {
+  if (!c) return SEI_ERR_ARG;
+  if (on && !c->d_mlp) return fail(c, SEI_ERR_STATE, "no trained network (sei_mlp_train or sei_mlp_set)");
+  c->warm_start = on != 0;
+  return SEI_OK;
+}
+
+int sei_mlp_gradient(const float* params, const float* norm, const float* samples, int64_t n, float* grads, float* loss) {
+  if (!params || !norm || !samples || !grads || !loss || n <= 0 || n > (int64_t)1 << 28) return SEI_ERR_ARG;
+  std::vector<float> X, T;
+  splitSamples(samples, n, X, T);
+  const int np = sei::mlpNumParams();
+  float *dP = nullptr, *dN = nullptr, *dX = nullptr, *dT = nullptr, *dG = nullptr, *dL = nullptr;
+  int sms = 0, dev = 0;
+  int rc = SEI_OK;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaMalloc(&dP, np * 4) || cudaMalloc(&dN, kNormBytes) || cudaMalloc(&dX, X.size() * 4) || cudaMalloc(&dT, T.size() * 4) ||
+      cudaMalloc(&dG, np * 4) || cudaMalloc(&dL, 4))
+    rc = SEI_ERR_OOM;
+  else if (cudaMemcpy(dP, params, np * 4, cudaMemcpyHostToDevice) || cudaMemcpy(dN, norm, kNormBytes, cudaMemcpyHostToDevice) ||
+           cudaMemcpy(dX, X.data(), X.size() * 4, cudaMemcpyHostToDevice) ||
+           cudaMemcpy(dT, T.data(), T.size() * 4, cudaMemcpyHostToDevice) || cudaMemset(dG, 0, np * 4) ||
+           cudaMemset(dL, 0, 4) || sei::launchMlpGrad(dP, dN, dX, dT, (int)n, dG, dL, sms > 0 ? sms : 1, nullptr) ||
+           cudaDeviceSynchronize() || cudaMemcpy(grads, dG, np * 4, cudaMemcpyDeviceToHost) ||
+           cudaMemcpy(loss, dL, 4, cudaMemcpyDeviceToHost))
+    rc = SEI_ERR_CUDA;
+  cudaGetLastError();
+  for (float* p : {dP, dN, dX, dT, dG, dL}) cudaFree(p);
+  return rc;
+}
+
+int sei_mlp_predict(const float* params, const float* norm, const float* samples, int64_t n, float* out) {
+  if (!params || !norm || !samples || !out || n <= 0 || n > (int64_t)1 << 28) return SEI_ERR_ARG;
+  std::vector<float> X, T;
+  splitSamples(samples, n, X, T);
+  const int np = sei::mlpNumParams();
+  float *dP = nullptr, *dN = nullptr, *dX = nullptr, *dO = nullptr;
+  int rc = SEI_OK;
+  if (cudaMalloc(&dP, np * 4) || cudaMalloc(&dN, kNormBytes) || cudaMalloc(&dX, X.size() * 4) || cudaMalloc(&dO, n * 4))
+    rc = SEI_ERR_OOM;
+  else if (cudaMemcpy(dP, params, np * 4, cudaMemcpyHostToDevice) || cudaMemcpy(dN, norm, kNormBytes, cudaMemcpyHostToDevice) ||
+           cudaMemcpy(dX, X.data(), X.size() * 4, cudaMemcpyHostToDevice) ||
+           sei::launchMlpPredict(dP, dN, dX, (int)n, dO, nullptr) || cudaDeviceSynchronize() ||
+           cudaMemcpy(out, dO, n * 4, cudaMemcpyDeviceToHost))
+    rc = SEI_ERR_CUDA;
+  cudaGetLastError();
+  for (float* p : {dP, dN, dX, dO}) cudaFree(p);
+  return rc;
 }
 
 int sei_set_profiling(sei_ctx* c, int on) {

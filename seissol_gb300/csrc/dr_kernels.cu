@@ -14,20 +14,26 @@
 //   4. time-weighted imposed states of both sides;
 //   5. nodal flux Q += V3mTo2nTWDivM(side, rel) . imposed . fluxSolver into both cells.
 // An optional small network (5 -> 64 -> 64 -> 1, tanh) proposes the starting slip rate of the
-// first Newton solve of every time point; the plain start (previous slip rate) is used
-// whenever the residual does not fall.
+// first Newton solve of every time point: it is used when its residual is below that of the
+// plain start (previous slip rate), and the plain solve runs whenever the residual from the
+// network's start stops falling.  Optionally the converged first solves of the plain method
+// are recorded as training samples (normal stress, shear, state, a, b, log10 V).
 #include <cuda_runtime.h>
 
 #include "common.cuh"
 #include "internal.h"
+#include "mlp.cuh"
 #include "_gen/dr_tables_o4.cuh"
 
 namespace {
 
 constexpr int kFacesPerBlock = 4;
-constexpr int kHidden = 64;
+constexpr int kHidden = sei_mlp::kHidden;
 constexpr int kMlpParams = kHidden * 5 + kHidden + kHidden * kHidden + kHidden + kHidden + 1;
 constexpr double kAlmostZero = 1e-45;
+// range of the network's guess, natural log of m/s (1e-45 .. 1e3)
+constexpr double kLnGuessMin = -103.616329;
+constexpr double kLnGuessMax = 6.907755;
 
 __device__ __forceinline__ double logsinh(double x, double c) {
   const double sign = c >= 0 ? 1.0 : -1.0;
@@ -75,6 +81,12 @@ __device__ double stateUpdate(const sei::DrArgs& A, double a, double psiRef, dou
   return psiss * -expm1(pre) + exp(pre) * psiRef;
 }
 
+__device__ __forceinline__ double residual(const sei::DrArgs& A, double a, double psi, double sn, double tau,
+                                           double invEtaS, double v) {
+  const double cl = psi / a;
+  return -invEtaS * (fabs(sn) * a * arsinhexp(0.5 / A.v0 * v, cl, cexpOf(cl)) - tau) - v;
+}
+
 struct NewtonOut {
   double v, mu;
   int iters;
@@ -102,11 +114,14 @@ __device__ NewtonOut newton(const sei::DrArgs& A, double a, double psi, double s
   return {v, 0.0, A.max_newton, false};
 }
 
-// Network guess of log10 of the converged slip rate.
+// Network guess of the natural log of the converged slip rate (feature and output maps of mlp.cuh).
 __device__ double mlpGuess(const float* __restrict__ w, const float* nrm, double sn, double tau, double psi, double a,
                            double b) {
-  const float x[5] = {(float)((sn - nrm[0]) * nrm[5]), (float)((tau - nrm[1]) * nrm[6]), (float)((psi - nrm[2]) * nrm[7]),
-                      (float)((a - nrm[3]) * nrm[8]), (float)((b - nrm[4]) * nrm[9])};
+  double f[5];
+  sei_mlp::features(sn, tau, psi, a, b, f);
+  float x[5];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) x[i] = (float)((f[i] - nrm[i]) * nrm[5 + i]);
   const float* W1 = w;
   const float* b1 = W1 + kHidden * 5;
   const float* W2 = b1 + kHidden;
@@ -129,7 +144,7 @@ __device__ double mlpGuess(const float* __restrict__ w, const float* nrm, double
     for (int i = 0; i < kHidden; ++i) s = fmaf(W2[j * kHidden + i], h1[i], s);
     out = fmaf(W3[j], tanhf(s), out);
   }
-  return (double)out * nrm[11] + nrm[10];
+  return sei_mlp::lnSlipRate(f, nrm[12], (double)out * nrm[11] + nrm[10]);
 }
 
 template <int N, int B, int NP>
@@ -212,7 +227,7 @@ __global__ void __launch_bounds__(32 * kFacesPerBlock)
   double v1 = pt ? A.v1[po] : 1.0, v2 = pt ? A.v2[po] : 0.0;
   double slip1 = pt ? A.slip1[po] : 0.0, slip2 = pt ? A.slip2[po] : 0.0, slip = pt ? A.slip[po] : 0.0;
   double mu = 0.0, tr1 = 0.0, tr2 = 0.0;
-  int iters = 0;
+  int iters = 0, firstIters = 0;
   double isP[6] = {0, 0, 0, 0, 0, 0}, isM[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll 1
   for (int s = 0; s < N; ++s) {
@@ -236,16 +251,31 @@ __global__ void __launch_bounds__(32 * kFacesPerBlock)
         psib = stateUpdate(A, a, sref, dt, lsr);
         NewtonOut r{};
         bool done = false;
-        if (useMlp && j == 0) {
+        if (useMlp && j == 0 && sei_mlp::usable(sn, tau, a)) {
+          // start from the network's guess when its residual is below the plain start's
           const double lg = mlpGuess(sW, A.mlp_norm, sn, tau, psib, a, A.b);
-          const double g0 = exp10(fmin(fmax(lg, -40.0), 3.0));
-          r = newton(A, a, psib, sn, tau, invEtaS, g0, true);
-          iters += r.iters;
-          done = r.conv;
+          const double g0 = exp(fmin(fmax(lg, kLnGuessMin), kLnGuessMax));
+          if (fabs(residual(A, a, psib, sn, tau, invEtaS, g0)) < fabs(residual(A, a, psib, sn, tau, invEtaS, vmag))) {
+            r = newton(A, a, psib, sn, tau, invEtaS, g0, true);
+            firstIters += r.iters;
+            done = r.conv;
+          }
         }
         if (!done) {
           r = newton(A, a, psib, sn, tau, invEtaS, vmag, false);
-          iters += r.iters;
+          (j == 0 ? firstIters : iters) += r.iters;
+          if (A.rec && j == 0 && r.conv && sei_mlp::usable(sn, tau, a)) {
+            const unsigned idx = atomicAdd(A.rec_count, 1u);
+            if (idx < A.rec_cap) {
+              float* o = A.rec + (size_t)idx * 6;
+              o[0] = (float)sn;
+              o[1] = (float)tau;
+              o[2] = (float)psib;
+              o[3] = (float)a;
+              o[4] = (float)A.b;
+              o[5] = (float)log10(r.v);
+            }
+          }
         }
         lsr = 0.5 * (vmag + r.v);
         conv = fabs(vmag - r.v) < A.state_tol;
@@ -298,7 +328,8 @@ __global__ void __launch_bounds__(32 * kFacesPerBlock)
     A.mu[po] = mu;
     A.trac1[po] = tr1;
     A.trac2[po] = tr2;
-    A.newton_iters[po] += iters;
+    A.newton_iters[po] += iters + firstIters;
+    A.newton_iters[(size_t)A.nfaces * NP + po] += firstIters;
   }
 
   // ---- 4./5. imposed states and nodal flux, plus side then minus side

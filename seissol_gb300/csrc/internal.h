@@ -91,14 +91,17 @@ struct DrArgs {
   double *psi, *v1, *v2, *slip1, *slip2, *slip, *mu, *trac1, *trac2;  // [nf][npts]
   float* isp;  // imposed states [nf][9][npts]
   float* ism;
-  int32_t* newton_iters;  // [nf][npts], accumulated
+  int32_t* newton_iters;  // [2][nf][npts], accumulated: all solves, first solve of each time point
   float* Q;               // DOFs [n][9][Bp] (nodal flux target)
   double f0, b, v0, l, muw, vw, newton_tol, state_tol;
   int max_newton, max_outer;
   double deltat[8], tweights[8];
   float coll[8][8];     // collocation coefficients t_s^p / p! of the time points
   const float* mlp;     // warm-start network parameters (nullptr: plain Newton)
-  float mlp_norm[12];   // input shift/scale and output shift/scale of the network
+  float mlp_norm[16];   // normalisation of the network (layout in mlp.cuh)
+  float* rec;           // training samples [rec_cap][6] (nullptr: not recorded)
+  unsigned* rec_count;
+  unsigned rec_cap;
 };
 int launchDrFaces(int order, const DrArgs& a, void* stream);
 int drNumPoints(int order);
@@ -138,4 +141,13 @@ struct TcLintArgs {
   int* status;  // set to 1 when a wait gave up
 };
 int launchLintTensorCore(int order, const DeviceArrays& d, int* status, int sms, void* stream);
+}  // namespace sei
+
+namespace sei {
+// Warm-start network kernels (mlp_kernels.cu).
+int mlpNumParams();
+int launchMlpGrad(const float* P, const float* norm, const float* X, const float* T, int n, float* grads, float* loss,
+                  int sms, void* stream);
+int launchMlpAdam(float* P, const float* grads, float* m, float* v, float lr, int step, void* stream);
+int launchMlpPredict(const float* P, const float* norm, const float* X, int n, float* out, void* stream);
 }  // namespace sei

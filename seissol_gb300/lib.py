@@ -117,11 +117,20 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_dr_get_state", i, [VP, i, VP])
     _sig(lib, "sei_dr_set_state", i, [VP, i, VP])
     _sig(lib, "sei_dr_get_imposed", i, [VP, VP, VP])
-    _sig(lib, "sei_dr_newton_iterations", i, [VP, C.POINTER(i64), C.POINTER(i64)])
+    _sig(lib, "sei_dr_newton_iterations", i, [VP, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)])
     _sig(lib, "sei_dr_reset_counters", i, [VP])
     _sig(lib, "sei_dr_faces_step", i, [VP, d])
     _sig(lib, "sei_dr_get_slots", i, [VP, VP])
     _sig(lib, "sei_kernel_times_ms", i, [VP, C.POINTER(d), C.POINTER(d), C.POINTER(i)])
+    _sig(lib, "sei_mlp_num_params", i, [])
+    _sig(lib, "sei_dr_record_samples", i, [VP, i64])
+    _sig(lib, "sei_dr_get_samples", i, [VP, VP, i64, C.POINTER(i64)])
+    _sig(lib, "sei_mlp_train", i, [VP, VP, i64, i, C.c_float, C.c_uint64, C.POINTER(C.c_float), C.POINTER(C.c_float)])
+    _sig(lib, "sei_mlp_get", i, [VP, VP, VP])
+    _sig(lib, "sei_mlp_set", i, [VP, VP, VP])
+    _sig(lib, "sei_dr_warm_start", i, [VP, i])
+    _sig(lib, "sei_mlp_gradient", i, [VP, VP, VP, i64, VP, C.POINTER(C.c_float)])
+    _sig(lib, "sei_mlp_predict", i, [VP, VP, VP, i64, VP])
     if path is None:
         _lib = lib
     return lib
@@ -157,6 +166,37 @@ def tc_gemm_check(A, B, terms=3):
     if rc != SEI_OK:
         raise SeiError(rc, "sei_tc_gemm_check")
     return D
+
+
+def mlp_num_params():
+    return load_library().sei_mlp_num_params()
+
+
+def mlp_gradient(params, norm, samples):
+    """(gradient, loss) of the warm-start network's mean-squared loss over samples [n][6], on the GPU."""
+    lib = load_library()
+    params = np.ascontiguousarray(params, np.float32)
+    norm = np.ascontiguousarray(norm, np.float32)
+    samples = np.ascontiguousarray(samples, np.float32)
+    g = np.empty(lib.sei_mlp_num_params(), np.float32)
+    loss = C.c_float()
+    rc = lib.sei_mlp_gradient(_ptr(params), _ptr(norm), _ptr(samples), samples.shape[0], _ptr(g), C.byref(loss))
+    if rc != SEI_OK:
+        raise SeiError(rc, "sei_mlp_gradient")
+    return g, loss.value
+
+
+def mlp_predict(params, norm, samples):
+    """log10 slip rate predicted for each sample [n][6] (last column ignored), on the GPU."""
+    lib = load_library()
+    params = np.ascontiguousarray(params, np.float32)
+    norm = np.ascontiguousarray(norm, np.float32)
+    samples = np.ascontiguousarray(samples, np.float32)
+    out = np.empty(samples.shape[0], np.float32)
+    rc = lib.sei_mlp_predict(_ptr(params), _ptr(norm), _ptr(samples), samples.shape[0], _ptr(out))
+    if rc != SEI_OK:
+        raise SeiError(rc, "sei_mlp_predict")
+    return out
 
 
 class Context:
@@ -326,10 +366,12 @@ class Context:
         self._check(self.lib.sei_dr_get_imposed(self.h, _ptr(p), _ptr(m)), "sei_dr_get_imposed")
         return p, m
 
-    def dr_newton_iterations(self):
-        t, n = C.c_int64(), C.c_int64()
-        self._check(self.lib.sei_dr_newton_iterations(self.h, C.byref(t), C.byref(n)), "sei_dr_newton_iterations")
-        return t.value, n.value
+    def dr_newton_iterations(self, first=False):
+        """(total iterations, points); with first=True also the iterations of the first solves."""
+        t, n, f = C.c_int64(), C.c_int64(), C.c_int64()
+        self._check(self.lib.sei_dr_newton_iterations(self.h, C.byref(t), C.byref(n), C.byref(f)),
+                    "sei_dr_newton_iterations")
+        return (t.value, n.value, f.value) if first else (t.value, n.value)
 
     def dr_reset_counters(self):
         self._check(self.lib.sei_dr_reset_counters(self.h), "sei_dr_reset_counters")
@@ -346,6 +388,38 @@ class Context:
         a = np.empty((nslots, derivatives_size(self.order)), np.float32)
         self._check(self.lib.sei_get_derivatives(self.h, _ptr(a)), "sei_get_derivatives")
         return a
+
+    def dr_record_samples(self, capacity):
+        self._check(self.lib.sei_dr_record_samples(self.h, int(capacity)), "sei_dr_record_samples")
+
+    def dr_samples(self):
+        cnt = C.c_int64()
+        self._check(self.lib.sei_dr_get_samples(self.h, None, 0, C.byref(cnt)), "sei_dr_get_samples")
+        out = np.empty((cnt.value, 6), np.float32)
+        self._check(self.lib.sei_dr_get_samples(self.h, _ptr(out), cnt.value, C.byref(cnt)), "sei_dr_get_samples")
+        return out
+
+    def mlp_train(self, samples=None, steps=2000, lr=3e-3, seed=1):
+        """Trains the warm-start network on the GPU; returns (first loss, last loss)."""
+        s = None if samples is None else np.ascontiguousarray(samples, np.float32)
+        a, b = C.c_float(), C.c_float()
+        self._check(self.lib.sei_mlp_train(self.h, _ptr(s), 0 if s is None else s.shape[0], steps, lr, seed, C.byref(a),
+                                           C.byref(b)), "sei_mlp_train")
+        return a.value, b.value
+
+    def mlp_get(self):
+        p = np.empty(self.lib.sei_mlp_num_params(), np.float32)
+        nrm = np.empty(16, np.float32)
+        self._check(self.lib.sei_mlp_get(self.h, _ptr(p), _ptr(nrm)), "sei_mlp_get")
+        return p, nrm
+
+    def mlp_set(self, params, norm):
+        p = np.ascontiguousarray(params, np.float32)
+        nrm = np.ascontiguousarray(norm, np.float32)
+        self._check(self.lib.sei_mlp_set(self.h, _ptr(p), _ptr(nrm)), "sei_mlp_set")
+
+    def dr_warm_start(self, on=True):
+        self._check(self.lib.sei_dr_warm_start(self.h, int(on)), "sei_dr_warm_start")
 
     def set_profiling(self, on=True):
         self._check(self.lib.sei_set_profiling(self.h, int(on)), "sei_set_profiling")
