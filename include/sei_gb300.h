@@ -200,7 +200,7 @@ int sei_dr_faces_step(sei_ctx* ctx, double dt);
 int sei_dr_get_slots(sei_ctx* ctx, int32_t* slots);
 
 /* Learned warm start of the slip-rate Newton solve (no counterpart in the reference, whose solve
- * starts from the previous slip rate, src/DynamicRupture/FrictionLaws/CpuImpl/RateAndState.h:340-417).
+ * starts from the previous slip rate, src/DynamicRupture/FrictionLaws/CpuImpl/RateAndState.h:339-417, first guess :354-356).
  * Network 5 -> 64 -> 64 -> 1 with tanh, FP32, on the raw inputs (normal stress sn, absolute shear
  * traction tau, state variable psi, a, b) through fixed dimensionless features
  * (tau / (|sn| a), psi / a, ln(|sn| a), a, b), each normalised as (f - norm[i]) * norm[5 + i]; its

@@ -2,7 +2,7 @@
 tanh) and of the gradient of its mean-squared training loss, the checker of the GPU training kernels.
 
 The network has no counterpart in the reference: its rate-and-state solve starts every Newton
-sequence from the previous slip rate (src/DynamicRupture/FrictionLaws/CpuImpl/RateAndState.h:340-417).
+sequence from the previous slip rate (src/DynamicRupture/FrictionLaws/CpuImpl/RateAndState.h:339-417, first guess :354-356).
 Parameter order W1 [64][5], b1 [64], W2 [64][64], b2 [64], W3 [64], b3; samples [n][6] = (normal
 stress sn, |shear traction| tau, state variable psi, a, b, log10 slip rate).  The network sees the
 fixed features (tau / (|sn| a), psi / a, ln(|sn| a), a, b) (|sn| a floored at 1 Pa) and predicts
