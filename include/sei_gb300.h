@@ -34,6 +34,7 @@ extern "C" {
 #define SEI_ERR_NAN (-5)
 #define SEI_ERR_STATE (-6)
 #define SEI_ERR_UNSUPPORTED (-7)
+#define SEI_ERR_CAPACITY (-8) /* request larger than a fixed-size buffer of the library */
 
 /* Proxy kernels (src/Proxy/Common.h:18, names in src/Proxy/Common.cpp:22-40). */
 #define SEI_KERNEL_ALL 0
@@ -231,6 +232,16 @@ int sei_dr_warm_start(sei_ctx* ctx, int on);
  * over samples [n][6] and the network's log10 slip rate for each sample (target column ignored). */
 int sei_mlp_gradient(const float* params, const float* norm, const float* samples, int64_t n, float* grads, float* loss);
 int sei_mlp_predict(const float* params, const float* norm, const float* samples, int64_t n, float* out);
+/* sei_mlp_gradient without device allocation (no counterpart in the reference), for callers that
+ * own all device memory through their own pool and keep streams in flight: a cudaMalloc could fail
+ * or take memory outside that pool, and cudaFree synchronises the whole device.  Its scratch is a
+ * fixed static device array of 421 KiB that limits n to SEI_MLP_NOALLOC_MAX_SAMPLES (larger n
+ * returns SEI_ERR_CAPACITY).  The first call on a device (the current one) looks up the array's
+ * address: make it before any stream capture.  All calls on a device share the array; the
+ * accumulators are cleared by every call, and calls that overlap on the GPU race. */
+#define SEI_MLP_NOALLOC_MAX_SAMPLES 16384
+int sei_mlp_gradient_noalloc(const float* params, const float* norm, const float* samples, int64_t n, float* grads,
+                             float* loss);
 
 /* Per-launch device timing: when on, every kernel launch of sei_run is bracketed by CUDA events on the
  * context stream; sei_kernel_times_ms sums the durations of the last sei_run per kernel kind. */

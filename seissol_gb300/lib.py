@@ -17,7 +17,7 @@ LIB_PATH = os.path.join(HERE, "libsei_gb300.so")
 
 SEI_OK = 0
 ERRORS = {-1: "SEI_ERR_ARG", -2: "SEI_ERR_OOM", -3: "SEI_ERR_CUDA", -4: "SEI_ERR_TIMEOUT", -5: "SEI_ERR_NAN",
-          -6: "SEI_ERR_STATE", -7: "SEI_ERR_UNSUPPORTED"}
+          -6: "SEI_ERR_STATE", -7: "SEI_ERR_UNSUPPORTED", -8: "SEI_ERR_CAPACITY"}
 # Proxy kernel names (src/Proxy/Common.cpp:22-40) -> SEI_KERNEL_*.
 KERNELS = {"all": 0, "local": 1, "neigh": 2, "ader": 3, "localwoader": 4, "neigh_dr": 5, "godunov_dr": 6, "all_dr": 7}
 
@@ -131,6 +131,7 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_dr_warm_start", i, [VP, i])
     _sig(lib, "sei_mlp_gradient", i, [VP, VP, VP, i64, VP, C.POINTER(C.c_float)])
     _sig(lib, "sei_mlp_predict", i, [VP, VP, VP, i64, VP])
+    _sig(lib, "sei_mlp_gradient_noalloc", i, [VP, VP, VP, i64, VP, C.POINTER(C.c_float)])
     if path is None:
         _lib = lib
     return lib
