@@ -48,7 +48,11 @@ def bytes_per_cell(order, kernel):
     """Algorithmic HBM bytes per cell and launch (float32, each array touched once)."""
     b = order * (order + 1) * (order + 2) // 6
     dof = 4 * 9 * ((b + 3) // 4 * 4)
-    if kernel == "local":  # read Q, write Q, write I, star non-zeros, A+ x4, face types
+    if kernel == "local":  # fused ADER + local: read Q, write Q, write I, star non-zeros, A+ x4, face types
+        return 3 * dof + 4 * 72 + 4 * 324 + 4
+    if kernel == "ader":  # read Q, write I, star non-zeros
+        return 2 * dof + 4 * 72
+    if kernel == "lint":  # read Q, write Q, read I, star non-zeros, A+ x4, face types
         return 3 * dof + 4 * 72 + 4 * 324 + 4
     if kernel == "neighbor":  # read Q, write Q, read neighbour I (once per cell), A- x4, relations
         return 3 * dof + 4 * 324 + 16 + 4 + 4
@@ -217,6 +221,87 @@ def run_reference(args, world, rank):
     return 0
 
 
+DR_DIMS = (6, 100, 100)  # 60,000 cubes = 300,000 tets; fault plane x = 3 h: 100 x 100 cube faces = 20,000 faces
+DR_SEED = 77
+
+
+def dr_measurement(local, steps):
+    """Dynamic rupture on the fault workload: elastic order 4, 300,000 tets, a planar fault of
+    20,000 faces (25 points each), fast-velocity-weakening friction with a ~ U[0.008, 0.02],
+    sn ~ U[-120, -40] MPa, tau ~ U[20, 75] MPa, V_init = 1e-16 m/s, kernel all_dr.
+
+    A training run (its own seed) records samples of the plain Newton solve for 3 steps and
+    trains the warm-start network on the GPU; then two contexts with the same (other) seed run
+    `steps` steps from the same initial state, plain and warm-started, timed with CUDA events.
+    Reported: cell- and face-updates/s of each, Newton iterations per point and step (all
+    solves and the first solve of each time point), and the largest slip-rate difference."""
+    import numpy as np
+
+    from seissol_gb300 import Context, RSParams
+
+    def make(seed):
+        ctx = Context(4, device=local)
+        n = ctx.build_periodic_cube(*DR_DIMS, perturb=0.0, seed=seed, fault_plane=3)
+        nf = ctx.dr_setup(RSParams.fault_config(seed=seed + 2))
+        rng = np.random.default_rng(seed)
+        ctx.set_dofs(rng.uniform(-1, 1, (n, 9, 20)).astype(np.float32))
+        return ctx, n, nf
+
+    t0 = time.perf_counter()
+    tr, _, _ = make(DR_SEED)
+    dt = tr.cfl_timestep(0.5)
+    tr.dr_record_samples(400000)
+    tr.run("all_dr", dt, 3)
+    tr.sync()
+    nsamp = len(tr.dr_samples())
+    loss0, loss1 = tr.mlp_train(steps=1500, lr=3e-3, seed=1)
+    params, norm = tr.mlp_get()
+    tr.close()
+    train_s = time.perf_counter() - t0
+    out = {}
+    states = {}
+    for mode in ("plain", "warm"):
+        ctx, n, nf = make(DR_SEED + 1)
+        if mode == "warm":
+            ctx.mlp_set(params, norm)
+            ctx.dr_warm_start(True)
+        ctx.dr_reset_counters()
+        ctx.run("all_dr", dt, steps)
+        ctx.sync()
+        ms = ctx.last_run_ms()
+        tot, npts, first = ctx.dr_newton_iterations(first=True)
+        states[mode] = np.hypot(ctx.dr_state("slip_rate1"), ctx.dr_state("slip_rate2"))
+        ctx.set_profiling(True)
+        ctx.run("all_dr", dt, 1)
+        ctx.sync()
+        fault_ms = ctx.kernel_times_by_kind()["fault"][0]
+        ctx.close()
+        out[mode] = {"ms_per_step": ms / steps, "cell_updates_per_s": n * steps / (ms / 1e3),
+                     "face_updates_per_s": nf * steps / (ms / 1e3), "fault_kernel_ms": fault_ms,
+                     "newton_iters_per_point_step": tot / (npts * steps),
+                     "first_solve_iters_per_point_step": first / (npts * steps)}
+    vp, vw = states["plain"], states["warm"]
+    return {"workload": "elastic order 4, 300,000-tet periodic cube 6x100x100 cubes, planar fault of 20,000 faces "
+                        "x 25 points, FVW rate-and-state (a ~ U[0.008,0.02], sn ~ U[-120,-40] MPa, tau ~ U[20,75] MPa, "
+                        f"V_init 1e-16), kernel all_dr, {steps} steps from the initial state",
+            "cells": n, "faces": nf, "steps": steps, "plain": out["plain"], "warm_start": out["warm"],
+            "first_solve_iteration_ratio": out["plain"]["first_solve_iters_per_point_step"]
+            / max(out["warm"]["first_solve_iters_per_point_step"], 1e-30),
+            "total_iteration_ratio": out["plain"]["newton_iters_per_point_step"]
+            / max(out["warm"]["newton_iters_per_point_step"], 1e-30),
+            "max_abs_dV": float(np.abs(vp - vw).max()),
+            "max_rel_dV": float((np.abs(vp - vw) / np.maximum(vp, 1e-30)).max()),
+            "training": {"samples": nsamp, "adam_steps": 1500, "loss_first": loss0, "loss_last": loss1,
+                         "seconds_incl_recording": train_s}}
+
+
+def kname(kind, args):
+    """Name of the CUDA kernel behind a launch kind of the step."""
+    if kind == "lint" and args.precision == "f16x3":
+        return f"sei_lint_tc<{ORDER}>"
+    return f"sei_{kind}_o{ORDER}"
+
+
 def run_ours(args, world, rank, local):
     import numpy as np
     import torch
@@ -250,9 +335,11 @@ def run_ours(args, world, rank, local):
     ctx.set_profiling(True)
     ctx.run("all", dt, args.steps)
     ctx.sync()
-    loc_ms, nb_ms, launches = ctx.kernel_times_ms()
+    by_kind = ctx.kernel_times_by_kind()
     ctx.set_profiling(False)
-    kernels = {"local": loc_ms / args.steps, "neighbor": nb_ms / args.steps}
+    names = {"ader": "local" if args.fused_local else "ader", "lint": "lint", "neighbor": "neighbor"}
+    kernels = {names[k]: v[0] / v[1] for k, v in by_kind.items() if k in names and v[1] > 0}
+    launches = sum(v[1] for v in by_kind.values())
     dom = max(kernels, key=kernels.get)
     algo = bytes_per_cell(ORDER, dom) * n
     achieved = algo / (kernels[dom] / 1e3) / 1e9
@@ -261,9 +348,9 @@ def run_ours(args, world, rank, local):
     if os.path.exists(tf):
         for line in open(tf):
             parts = line.split()
-            if len(parts) >= 2 and parts[0] == f"sei_{dom}_o{ORDER}":
+            if len(parts) >= 2 and parts[0] == kname(dom, args):
                 traffic = float(parts[1]) * n
-    roof = {"bound": "hbm", "kernel": f"sei_{dom}_o{ORDER}", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+    roof = {"bound": "hbm", "kernel": kname(dom, args), "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "peak_source": f"{peak_kind} hbm_gbs", "traffic": traffic,
             "algorithmic_bytes_per_launch": algo, "launch_ms": kernels[dom],
             "step_model_frac": value / world * bytes_per_cell(ORDER, "model") / (hbm * 1e9)}
@@ -299,6 +386,10 @@ def run_ours(args, world, rank, local):
                "call": "sei_run_host(SEI_KERNEL_ALL, dt, 1, dofs_in, dofs_out) with pinned host DOFs"}
     ctx.close()
 
+    dr = None
+    if rank == 0 and args.dr_steps > 0:
+        dr = dr_measurement(local, args.dr_steps)
+
     base = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         base = cpu_baseline()
@@ -312,7 +403,7 @@ def run_ours(args, world, rank, local):
                            "l2": "inputs larger than L2 (~3 GB resident per GPU), no flush",
                            "parallelism": f"replicas x{world}"},
                 "roofline": roof, "cpu_baseline": base, "e2e": e2e, "clocks": clocks,
-                "gpu_launches": launches, "kernel_ms_per_step": kernels}
+                "gpu_launches": launches, "kernel_ms_per_step": kernels, "dynamic_rupture": dr}
         print(json.dumps(line))
     return 0
 
@@ -327,6 +418,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fused-local", action="store_true", help="ADER and local integral in one launch")
     ap.add_argument("--precision", choices=("fp32", "f16x3"), default="fp32")
+    ap.add_argument("--dr-steps", type=int, default=20,
+                    help="steps of the dynamic-rupture measurement (plain and warm-started); 0 skips it")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -247,6 +247,9 @@ int sei_mlp_gradient_noalloc(const float* params, const float* norm, const float
  * context stream; sei_kernel_times_ms sums the durations of the last sei_run per kernel kind. */
 int sei_set_profiling(sei_ctx* ctx, int on);
 int sei_kernel_times_ms(sei_ctx* ctx, double* local_ms, double* neighbor_ms, int* launches);
+/* The same per launch kind: ms[4] and counts[4] for 0 ADER (or fused ADER + local integral),
+ * 1 neighbour flux, 2 fault kernel, 3 local integral. */
+int sei_kernel_times_by_kind(sei_ctx* ctx, double* ms, int* counts);
 
 /* Diagnostic: one 128 x N x K tile D = A B^T on the tensor cores (tcgen05 kind::tf32, TMEM
  * accumulator), A [128][K] and B [N][K] row-major host arrays, D [128][N]; terms 1 = plain TF32,

@@ -66,7 +66,8 @@ struct sei_ctx {
   int sms = 0;               // multiprocessors of the device (persistent tensor-core grids)
   int* d_status = nullptr;   // device error word: 1 = a bounded wait in a kernel gave up
   std::vector<cudaEvent_t> prof_events;
-  std::vector<int> prof_kind;  // kind of the launch that starts at event i (0 local, 1 neighbour)
+  std::vector<int> prof_kind;  // kind of the launch starting at event i: 0 ADER (or fused ADER + local),
+                               // 1 neighbour, 2 fault, 3 local integral, -1 end of run
   size_t prof_used = 0;
 };
 
@@ -212,7 +213,7 @@ int launchAderOnly(sei_ctx* c, const sei::DeviceArrays& d, const float* coeffs) 
 }
 
 int launchLintOnly(sei_ctx* c, const sei::DeviceArrays& d) {
-  int rc = profMark(c, 0);
+  int rc = profMark(c, 3);
   if (rc) return rc;
   if (c->cfg.precision == SEI_PREC_F16X3) {
     if (sei::launchLintTensorCore(c->cfg.order, d, c->d_status, c->sms, c->stream) != 0)
@@ -1094,9 +1095,25 @@ int sei_kernel_times_ms(sei_ctx* c, double* local_ms, double* neighbor_ms, int* 
   for (size_t i = 0; i + 1 < c->prof_used; ++i) {
     float ms = 0;
     SEI_CUDA(cudaEventElapsedTime(&ms, c->prof_events[i], c->prof_events[i + 1]));
-    if (c->prof_kind[i] == 0) *local_ms += ms;
+    if (c->prof_kind[i] == 0 || c->prof_kind[i] == 3) *local_ms += ms;
     if (c->prof_kind[i] == 1) *neighbor_ms += ms;
     ++*launches;
+  }
+  return SEI_OK;
+}
+
+int sei_kernel_times_by_kind(sei_ctx* c, double* ms, int* counts) {
+  if (!c || !ms || !counts) return SEI_ERR_ARG;
+  for (int k = 0; k < 4; ++k) ms[k] = 0.0, counts[k] = 0;
+  if (!c->profiling || c->prof_used < 2) return fail(c, SEI_ERR_STATE, "profiling off or nothing recorded");
+  SEI_CUDA(cudaEventSynchronize(c->prof_events[c->prof_used - 1]));
+  for (size_t i = 0; i + 1 < c->prof_used; ++i) {
+    const int k = c->prof_kind[i];
+    if (k < 0 || k > 3) continue;
+    float t = 0;
+    SEI_CUDA(cudaEventElapsedTime(&t, c->prof_events[i], c->prof_events[i + 1]));
+    ms[k] += t;
+    ++counts[k];
   }
   return SEI_OK;
 }

@@ -221,14 +221,24 @@ void buildPeriodicCube(const sei_cube_params& p, HostMesh& m) {
       if (dot(cross(sub(b, a), sub(c, a)), sub(d, a)) < 0)
         for (int k = 0; k < 3; ++k) std::swap(tets[par][t][2][k], tets[par][t][3][k]);
     }
-  // Cell order: the cubes of each parity are listed in (k, j, i) order and cut into chunks of
-  // 32; chunk c emits, for parity 0 then 1 and tet type 0..4, the 32 cells of that type.  A
-  // 32-cell CTA therefore holds one tet type (uniform face relations), and consecutive CTAs
-  // cover neighbouring cubes, so neighbour data is reused from L2.
+  // Cell order: the cubes of each parity are listed pencil by pencil (pencils of 8 x 8 cubes in
+  // x, y, all of z; pencils in serpentine order over the x-y plane; (k, j, i) order inside a
+  // pencil) and cut into chunks of 32; chunk c emits, for parity 0 then 1 and tet type 0..4, the
+  // 32 cells of that type.  A 32-cell CTA therefore holds one tet type (uniform face relations).
+  // Every cube's neighbours lie within one pencil (<= 64 cubes away in z) or in the adjacent
+  // pencil, so the four reads of each time-integrated block by the neighbour kernel fall within
+  // a few thousand cubes of each other and are served from L2.
+  constexpr int kPencil = 8;
   std::vector<std::array<int, 3>> cubes[2];
-  for (int k = 0; k < p.nz; ++k)
-    for (int j = 0; j < p.ny; ++j)
-      for (int i = 0; i < p.nx; ++i) cubes[(i + j + k) % 2].push_back({i, j, k});
+  const int npx = (p.nx + kPencil - 1) / kPencil, npy = (p.ny + kPencil - 1) / kPencil;
+  for (int pj = 0; pj < npy; ++pj)
+    for (int pq = 0; pq < npx; ++pq) {
+      const int pi = (pj % 2) ? npx - 1 - pq : pq;
+      for (int k = 0; k < p.nz; ++k)
+        for (int j = pj * kPencil; j < std::min(p.ny, (pj + 1) * kPencil); ++j)
+          for (int i = pi * kPencil; i < std::min(p.nx, (pi + 1) * kPencil); ++i)
+            cubes[(i + j + k) % 2].push_back({i, j, k});
+    }
   const size_t chunks = (cubes[0].size() + 31) / 32;
   int64_t cell = 0;
   for (size_t ch = 0; ch < chunks; ++ch)

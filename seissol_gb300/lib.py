@@ -122,6 +122,7 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_dr_faces_step", i, [VP, d])
     _sig(lib, "sei_dr_get_slots", i, [VP, VP])
     _sig(lib, "sei_kernel_times_ms", i, [VP, C.POINTER(d), C.POINTER(d), C.POINTER(i)])
+    _sig(lib, "sei_kernel_times_by_kind", i, [VP, VP, VP])
     _sig(lib, "sei_mlp_num_params", i, [])
     _sig(lib, "sei_dr_record_samples", i, [VP, i64])
     _sig(lib, "sei_dr_get_samples", i, [VP, VP, i64, C.POINTER(i64)])
@@ -430,6 +431,13 @@ class Context:
         a, b, n = C.c_double(), C.c_double(), C.c_int()
         self._check(self.lib.sei_kernel_times_ms(self.h, C.byref(a), C.byref(b), C.byref(n)), "sei_kernel_times_ms")
         return a.value, b.value, n.value
+
+    def kernel_times_by_kind(self):
+        """{kind: (ms, launches)} of the last run with profiling on: ader, neighbor, fault, lint."""
+        ms = np.zeros(4, np.float64)
+        cnt = np.zeros(4, np.int32)
+        self._check(self.lib.sei_kernel_times_by_kind(self.h, _ptr(ms), _ptr(cnt)), "sei_kernel_times_by_kind")
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(("ader", "neighbor", "fault", "lint"))}
 
     def last_run_ms(self):
         d = C.c_double()

@@ -6,6 +6,7 @@ app/Proxy/Bindings.cpp:14-60.  Unlike the reference proxy, the data are a real m
 (synthetic periodic cube) with physical operators, and the time step is the CFL step.
 
 CLI:  python -m seissol_gb300.proxy <cells> <timesteps> <kernel>[,kernel...] [--order N] [--format json]
+      [--precision fp32|f16x3]; the *_dr kernels need --order 4 and run on a planar fault.
 """
 from __future__ import annotations
 
@@ -31,6 +32,7 @@ class ProxyConfig:
     order: int = 6
     verbose: bool = True
     device: int = 0
+    precision: int = 0  # SEI_PREC_FP32 / SEI_PREC_F16X3
 
 
 @dataclasses.dataclass
@@ -68,8 +70,14 @@ def run_proxy(cfg: ProxyConfig) -> ProxyOutput:
         if k not in KERNELS:
             raise ValueError(f"unknown kernel {k}; allowed: {', '.join(KERNELS)}")
     nx, ny, nz = cube_dims(cfg.cells)
-    with Context(cfg.order, cfg.device) as ctx:
-        n = ctx.build_periodic_cube(nx, ny, nz)
+    dr = any(k.endswith("_dr") for k in cfg.kernels)
+    with Context(cfg.order, cfg.device, precision=cfg.precision) as ctx:
+        # the *_dr kernels run on a planar fault through the middle of the cube (x = nx / 2),
+        # fast-velocity-weakening friction with the fault parameters of RSParams.fault_config
+        n = ctx.build_periodic_cube(nx, ny, nz, fault_plane=nx // 2 if dr else -1)
+        if dr:
+            from .lib import RSParams
+            ctx.dr_setup(RSParams.fault_config())
         dt = ctx.cfl_timestep(0.5)
         for k in cfg.kernels:
             ctx.run(k, dt, 1)  # warm-up
@@ -124,9 +132,12 @@ def main(argv=None):
     ap.add_argument("kernel")
     ap.add_argument("--order", type=int, default=6)
     ap.add_argument("--format", choices=("plain", "json"), default="plain")
+    ap.add_argument("--precision", choices=("fp32", "f16x3"), default="fp32",
+                    help="f16x3: local integral on the tensor cores (split FP16)")
     a = ap.parse_args(argv)
     kernels = tuple(a.kernel.split(","))
-    out = run_proxy(ProxyConfig(cells=a.cells, timesteps=a.timesteps, kernels=kernels, order=a.order))
+    out = run_proxy(ProxyConfig(cells=a.cells, timesteps=a.timesteps, kernels=kernels, order=a.order,
+                                precision={"fp32": 0, "f16x3": 1}[a.precision]))
     write_output(out, a.kernel, a.format)
     return 0
 
