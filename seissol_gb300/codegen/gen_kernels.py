@@ -219,7 +219,8 @@ sei_local_o{order}(int n, float* __restrict__ Q, float* __restrict__ Iout, const
     # ADER alone (Spacetime::computeAder)
     a(f"""
 // Cauchy-Kovalevskaya predictor alone: I = sum_i coeffs[i] dQ(i) (Q unchanged), optional derivatives.
-extern "C" __global__ void __launch_bounds__(288, 1)
+// Two CTAs per SM (at order 6: 96 registers, ~0.2 KB spilled to L1; measured 3.6 % faster step).
+extern "C" __global__ void __launch_bounds__(288, 2)
 sei_ader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout, const float* __restrict__ star_nz,
                   SeiCoeffs coeffs, float* __restrict__ derivs, const int* __restrict__ dslot) {{""" + prologue)
     emit_ck()

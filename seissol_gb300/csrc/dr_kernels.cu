@@ -35,12 +35,6 @@ constexpr double kAlmostZero = 1e-45;
 constexpr double kLnGuessMin = -103.616329;
 constexpr double kLnGuessMax = 6.907755;
 
-__device__ __forceinline__ double logsinh(double x, double c) {
-  const double sign = c >= 0 ? 1.0 : -1.0;
-  const double ac = fabs(c);
-  return ac + log(x / 2 * -sign * expm1(-2 * ac));
-}
-
 __device__ __forceinline__ double cexpOf(double l) { return l > 0 ? exp(-l) : exp(l); }
 
 __device__ __forceinline__ bool largeBranch(double x, double explog) {
@@ -60,25 +54,63 @@ __device__ __forceinline__ double arsinhexp(double x, double explog, double e) {
   return asinh(e * x);
 }
 
-__device__ __forceinline__ double arsinhexpDeriv(double x, double explog, double e) {
-  if (largeBranch(x, explog)) {
-    if (explog <= 0) e = 1 / e;
-    return 1 / sqrt(x * x + e * e);
-  }
-  if (explog > 0) e = 1 / e;
-  const double v = e * x;
-  return e / sqrt(1 + v * v);
+// Natural log of a positive normal double, in float precision, without an FP64 transcendental:
+// the binary exponent plus the float log of the mantissa in [1, 2).
+__device__ __forceinline__ float lnPos(double v) {
+  const long long bits = __double_as_longlong(v);
+  const int e = (int)((bits >> 52) & 0x7FF) - 1023;
+  const double m = __longlong_as_double((bits & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL);
+  return (float)e * 0.6931471806f + logf((float)m);
 }
 
-__device__ double stateUpdate(const sei::DrArgs& A, double a, double psiRef, double dt, double v) {
-  double lowv = A.f0 - (A.b - a) * log(v / A.v0);
-  lowv = lowv > 0 ? lowv : 0.0;
-  const double r = v / A.vw;
-  const double r2 = r * r, r4 = r2 * r2, r8 = r4 * r4;
-  const double fss = A.muw + (lowv - A.muw) / pow(1.0 + r8, 0.125);
-  const double psiss = a * logsinh(A.v0 / v * 2, fss / a);
-  const double pre = -v * (dt / A.l);
-  return psiss * -expm1(pre) + exp(pre) * psiRef;
+// State variable after a sub-step of length dt at slip rate v (RateAndState FVW law).  The
+// steady state f_ss, psi_ss and the relaxation weight 1 - exp(-v dt / L) are evaluated in
+// float; the state itself is advanced in float64: psi = psiRef + w (psi_ss - psiRef).
+// psi_ss = a logsinh(2 V0 / v, f_ss / a) = f_ss - a ln(v / V0) + a ln(1 - exp(-2 f_ss / a)).
+// Reciprocals of the law's constants, taken once per thread (float64 divisions are costly).
+struct LawInv {
+  double v0, vw, l;
+};
+
+__device__ double stateUpdate(const sei::DrArgs& A, const LawInv& inv, double a, double psiRef, double dt, double v) {
+  const float af = (float)a;
+  const float lnvv0 = lnPos(v * inv.v0);
+  float lowv = (float)A.f0 - (float)(A.b - a) * lnvv0;
+  lowv = lowv > 0.f ? lowv : 0.f;
+  const float lnr = lnPos(v * inv.vw);
+  const float r8 = expf(fminf(8.f * lnr, 80.f));
+  const float fss = (float)A.muw + (lowv - (float)A.muw) * powf(1.f + r8, -0.125f);
+  const float c = fss / af;
+  const float psiss = fss - af * lnvv0 + af * log1pf(-expf(-2.f * c));
+  const float w = -expm1f((float)(-v * dt * inv.l));
+  return psiRef + (double)w * ((double)psiss - psiRef);
+}
+
+// Newton update delta = -g / g'(V) of the slip rate.  With y = V exp(psi / a) / (2 V0),
+// -g'(V) = |sn| a / eta_s * exp(psi / a) / (2 V0) / sqrt(1 + y^2) + 1 = 1 + exp(z), so
+// delta = g / (1 + exp(z)), z = ln(|sn| a / eta_s) + ln(exp(psi / a) / (2 V0)) - ln(1 + y^2) / 2.
+// z is evaluated in float log space (its terms span hundreds of e-folds, beyond the float
+// range as plain numbers); only the residual g needs float64.
+__device__ __forceinline__ double newtonDelta(double g, double v, float lnScale, float lnSna) {
+  const float ly = lnPos(v) + lnScale;
+  float half;  // ln(1 + y^2) / 2
+  if (ly > 15.f) {
+    half = ly;
+  } else if (ly < -15.f) {
+    half = 0.f;
+  } else {
+    const float y = expf(ly);
+    half = 0.5f * log1pf(y * y);
+  }
+  const float z = lnSna + lnScale - half;
+  if (z < 20.f) return g * (double)(1.f / (1.f + expf(z)));
+  // 1 / (1 + e^z) = e^-z to 2e-9 relative; e^-z = 2^k m with integer k and m in [1, 2)
+  const float w = -z * 1.4426950409f;
+  const float kf = floorf(w);
+  if (kf < -1000.f) return 0.0;
+  const double m = (double)exp2f(w - kf);
+  const double p2 = __longlong_as_double((long long)((int)kf + 1023) << 52);
+  return g * m * p2;
 }
 
 __device__ __forceinline__ double residual(const sei::DrArgs& A, double a, double psi, double sn, double tau,
@@ -99,6 +131,8 @@ __device__ NewtonOut newton(const sei::DrArgs& A, double a, double psi, double s
   const double clin = 0.5 / A.v0;
   const double cl = psi / a;
   const double ce = cexpOf(cl);
+  const float lnScale = (float)cl - lnPos(2.0 * A.v0);
+  const float lnSna = logf((float)(invEtaS * fabs(sn) * a));
   double prev = 1e300;
   for (int i = 0; i < A.max_newton; ++i) {
     const double mu = a * arsinhexp(clin * v, cl, ce);
@@ -106,9 +140,7 @@ __device__ NewtonOut newton(const sei::DrArgs& A, double a, double psi, double s
     if (fabs(g) < A.newton_tol) return {v, mu, i, true};
     if (bail && !(fabs(g) < prev)) return {v, 0.0, i, false};
     prev = fabs(g);
-    const double dmu = a * clin * arsinhexpDeriv(clin * v, cl, ce);
-    const double dg = -invEtaS * (fabs(sn) * dmu) - 1.0;
-    v = v - g / dg;
+    v = v + newtonDelta(g, v, lnScale, lnSna);
     v = v < kAlmostZero ? kAlmostZero : v;
   }
   return {v, 0.0, A.max_newton, false};
@@ -228,6 +260,7 @@ __global__ void __launch_bounds__(32 * kFacesPerBlock)
   double slip1 = pt ? A.slip1[po] : 0.0, slip2 = pt ? A.slip2[po] : 0.0, slip = pt ? A.slip[po] : 0.0;
   double mu = 0.0, tr1 = 0.0, tr2 = 0.0;
   int iters = 0, firstIters = 0;
+  const LawInv inv{1.0 / A.v0, 1.0 / A.vw, 1.0 / A.l};
   double isP[6] = {0, 0, 0, 0, 0, 0}, isM[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll 1
   for (int s = 0; s < N; ++s) {
@@ -248,7 +281,7 @@ __global__ void __launch_bounds__(32 * kFacesPerBlock)
     for (int j = 0; j < A.max_outer; ++j) {
       bool conv = true;
       if (pt) {
-        psib = stateUpdate(A, a, sref, dt, lsr);
+        psib = stateUpdate(A, inv, a, sref, dt, lsr);
         NewtonOut r{};
         bool done = false;
         if (useMlp && j == 0 && sei_mlp::usable(sn, tau, a)) {
@@ -285,7 +318,7 @@ __global__ void __launch_bounds__(32 * kFacesPerBlock)
       if (__all_sync(0xffffffffu, conv)) break;
     }
     if (pt) {
-      psib = stateUpdate(A, a, sref, dt, lsr);
+      psib = stateUpdate(A, inv, a, sref, dt, lsr);
       const double clin = 0.5 / A.v0, cl = psib / a;
       mu = a * arsinhexp(clin * vmag, cl, cexpOf(cl));
       const double strength = -mu * sn;

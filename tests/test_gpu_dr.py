@@ -91,6 +91,58 @@ def test_dr_ten_steps(built_lib):
     ctx.close()
 
 
+def test_dr_larger_fault_twenty_steps(built_lib):
+    """512 faces (8 x 16 x 16 cubes, fault at x = 4 h) along 20 steps of the oracle's trajectory:
+    before every step the GPU takes the oracle's DOFs and fault state, so each step is compared
+    alone (rupture nucleation amplifies the float rounding of free runs).  Per step: slip rate
+    1e-4 relative + 1e-12 m/s, state variable 1e-6, DOFs 1e-5 relative L2, Newton iterations
+    within 1 %, every state finite.  A free 20-step GPU run stays finite."""
+    from seissol_gb300 import Context, RSParams
+    seed = 21
+    ctx = Context(4, device=0)
+    n = ctx.build_periodic_cube(8, 16, 16, perturb=0.0, seed=seed, fault_plane=4)
+    rs = RSParams.fault_config(seed=seed + 2)
+    nf = ctx.dr_setup(rs)
+    assert nf == 512
+    q = seeded_dofs(n, 4, seed)
+    ctx.set_dofs(q)
+    cells = ctx.get_cells()
+    faces = ctx.dr_faces()
+    state = {k: ctx.dr_state(v) for k, v in FIELDS.items()}
+    start = {k: v.copy() for k, v in state.items()}
+    a = ctx.dr_state("a")
+    init = np.stack([ctx.dr_state("sn0"), ctx.dr_state("tau1_0"), ctx.dr_state("tau2_0")], axis=1)
+    params = {k: getattr(rs, k) for k in ("f0", "b", "v0", "l", "muw", "vw", "newton_tol", "state_tol",
+                                          "max_newton", "max_outer")}
+    dt = ctx.cfl_timestep(0.5)
+    o = oracle_py.Oracle(4)
+    dro = oracle_py.DROracle(4, faces, params)
+    for _ in range(20):
+        q, _, _, it, _ = oracle_py.dr_full_step(o, dro, q, cells, faces, state, a, init, dt)
+        ctx.dr_reset_counters()
+        ctx.run("all_dr", dt, 1)
+        ctx.sync()
+        for name in FIELDS.values():
+            assert np.isfinite(ctx.dr_state(name)).all(), name
+        _compare_state(ctx, state, tol_v=1e-4)
+        it_gpu, _ = ctx.dr_newton_iterations()
+        assert abs(it_gpu - int(it.sum())) <= 0.01 * int(it.sum()), (it_gpu, int(it.sum()))
+        assert rel_l2(ctx.get_dofs(), q) < 1e-5
+        for k, v in FIELDS.items():
+            ctx.dr_set_state(v, state[k])
+        ctx.set_dofs(q.astype(np.float32))
+    # free run from the initial state
+    for k, v in FIELDS.items():
+        ctx.dr_set_state(v, start[k])
+    ctx.set_dofs(seeded_dofs(n, 4, seed))
+    ctx.run("all_dr", dt, 20)
+    ctx.sync()
+    for name in FIELDS.values():
+        assert np.isfinite(ctx.dr_state(name)).all(), name
+    assert np.isfinite(ctx.get_dofs()).all()
+    ctx.close()
+
+
 def test_dr_rejects_high_order(built_lib):
     from seissol_gb300 import Context, RSParams, SeiError
     ctx = Context(5, device=0)
