@@ -73,6 +73,9 @@ typedef struct sei_cube_params {
   double perturb;
   uint64_t seed;
   int fault_plane;
+  /* > 1: graded tensor-product cube; along each direction the cube edges are drawn
+   * log-uniformly in [h, grading h] (seeded); <= 1: uniform edge h */
+  double grading;
 } sei_cube_params;
 
 /* Fast-velocity-weakening rate-and-state friction (src/Initializer/Parameters/DRParameters.h:36-73,
@@ -171,6 +174,22 @@ int sei_run_host(sei_ctx* ctx, int kernel, double dt, int nsteps, const float* d
 int sei_sync(sei_ctx* ctx);
 /* Device-side duration of the last sei_run, milliseconds (CUDA events on the context stream). */
 int sei_last_run_ms(sei_ctx* ctx, double* ms);
+
+/* Local time stepping, rate 2 (replaces the clustering of src/Initializer/TimeStepping with the
+ * maximum-difference property of docs/local-timestepping.rst, the predict / correct order of
+ * src/Solver/TimeStepping/TimeCluster.cpp:358-440, 695-717 and TimeCommon::computeIntegrals,
+ * src/Kernels/TimeCommon.cpp:40-87).  sei_lts_setup clusters the cells of the context's mesh by
+ * their CFL time steps (cluster k: steps in [2^k dt0, 2^{k+1} dt0), at most max_clusters,
+ * neighbours at most one cluster apart) and reorders the cells by cluster (stable; the DOFs move
+ * with their cells; sei_lts_permutation gives new -> old).  A face reads its neighbour's
+ * time-integrated DOFs (same cluster), integration buffer (finer neighbour) or the Taylor integral
+ * of its derivatives over the sub-interval (coarser neighbour).  Not built with a fault. */
+int sei_lts_setup(sei_ctx* ctx, double cfl, int max_clusters, int* nclusters);
+/* Advances every cluster by dt0 2^(nclusters-1) per cycle (asynchronous; sei_last_run_ms times it). */
+int sei_lts_run(sei_ctx* ctx, int ncycles);
+/* Cluster k holds cells [start[k], start[k+1]) with time step dt[k] (start: nclusters + 1 entries). */
+int sei_lts_clusters(sei_ctx* ctx, int* nclusters, int64_t* start, double* dt);
+int sei_lts_permutation(sei_ctx* ctx, int64_t* perm /*[n]*/);
 
 /* ---- dynamic rupture (built with fault_plane >= 0; order <= 4, i.e. at most 32 face points) ----
  * Replaces DynamicRupture::spaceTimeInterpolation + FrictionSolver::evaluate + the DR branch of

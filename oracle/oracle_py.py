@@ -218,3 +218,92 @@ def dr_full_step(o, dro, Q, cells, faces, state, a, init, dt, mlp=None, record=N
     Q = dro.nodal_flux(Q, mc, ms, rel, ism, faces["fluxSolverMinus"])
     Q = o.neighbor(Q, I, cells["AminusT"].astype(np.float64), cells["neighbor"], cells["side"], cells["orient"], ft)
     return Q, isp, ism, iters, (d, qip, qim)
+
+
+# ---------------------------------------------------------------------------
+# Local time stepping, rate 2 (test infrastructure: FP64 restatement)
+# ---------------------------------------------------------------------------
+
+def lts_clusters(dt, neighbor, face_type, max_clusters):
+    """Cluster k holds the cell time steps in [2^k dt0, 2^{k+1} dt0), capped at max_clusters - 1,
+    then neighbouring clusters are lowered until they differ by at most one (maximum difference
+    property, docs/local-timestepping.rst)."""
+    dt = np.asarray(dt, np.float64)
+    dt0 = dt.min()
+    cl = np.clip(np.floor(np.log2(dt / dt0) + 1e-12).astype(np.int64), 0, max_clusters - 1)
+    regular = np.asarray(face_type) == 0
+    nb = np.asarray(neighbor)
+    while True:
+        lim = np.where(regular, cl[np.where(regular, nb, 0)] + 1, np.iinfo(np.int64).max).min(axis=1)
+        new = np.minimum(cl, lim)
+        if np.array_equal(new, cl):
+            return cl, dt0
+        cl = new
+
+
+def lts_cycles(o, Q, cells, cluster, dt0, ncycles):
+    """Rate-2 LTS (TimeCluster.cpp:358-440, 695-717; TimeCommon.cpp:40-87) in FP64.
+
+    Every cycle advances all clusters by dt0 2^(C-1).  At sub-step k of the finest cluster the
+    clusters whose step starts there predict (ADER with derivatives, integration buffer of cells
+    with a coarser neighbour -- reset when the coarser step starts --, local integral); then the
+    clusters whose step ends at k + 1 correct: each regular face takes the neighbour's I (same
+    cluster), its buffer (finer) or the Taylor integral of its derivatives over this step's
+    sub-interval of the neighbour's step (coarser)."""
+    order = o.order
+    Q = np.array(Q, dtype=np.float64)
+    n = Q.shape[0]
+    cluster = np.asarray(cluster)
+    ncl = int(cluster.max()) + 1
+    star, aplus, aminus = (cells[k].astype(np.float64) for k in ("star", "AplusT", "AminusT"))
+    nb, side, orient, ft = cells["neighbor"], cells["side"], cells["orient"], cells["face_type"]
+    I = np.zeros_like(Q)
+    buf = np.zeros_like(Q)
+    derivs = None
+    regular = ft == 0
+    ncl_of = np.where(regular, cluster[np.where(regular, nb, 0)], cluster[:, None])
+    has_coarser = (regular & (ncl_of > cluster[:, None])).any(axis=1)
+    steps = 1 << (ncl - 1)
+    for _ in range(ncycles):
+        for k in range(steps):
+            for c in range(ncl):
+                ln = 1 << c
+                if k % ln:
+                    continue
+                idx = np.nonzero(cluster == c)[0]
+                if idx.size == 0:
+                    continue
+                Ic, d = o.ader(Q[idx], star[idx], dg_setup.taylor_integrate(order, 0.0, dt0 * ln), want_derivs=True)
+                I[idx] = Ic
+                if derivs is None:
+                    derivs = np.zeros((n, d.shape[1]))
+                derivs[idx] = d
+                b = idx[has_coarser[idx]]
+                if (k // ln) % 2 == 0:
+                    buf[b] = I[b]
+                else:
+                    buf[b] += I[b]
+                Q[idx] = o.local(Q[idx], I[idx], star[idx], aplus[idx], ft[idx])
+            for c in range(ncl):
+                ln = 1 << c
+                if (k + 1) % ln:
+                    continue
+                idx = np.nonzero(cluster == c)[0]
+                if idx.size == 0:
+                    continue
+                a = ((k + 1 - ln) % (2 * ln)) * dt0
+                sub = dg_setup.taylor_integrate(order, a, a + ln * dt0)
+                faces = np.zeros((idx.size, 4) + Q.shape[1:])
+                for f in range(4):
+                    nbs = nb[idx, f]
+                    reg = regular[idx, f]
+                    ncf = np.where(reg, cluster[np.where(reg, nbs, 0)], c)
+                    same, finer, coarser = reg & (ncf == c), reg & (ncf < c), reg & (ncf > c)
+                    faces[same, f] = I[nbs[same]]
+                    faces[finer, f] = buf[nbs[finer]]
+                    if coarser.any():
+                        faces[coarser, f] = o.taylor(derivs[nbs[coarser]], sub)
+                pool = faces.reshape((-1,) + Q.shape[1:])
+                pidx = np.arange(idx.size * 4, dtype=np.int32).reshape(idx.size, 4)
+                Q[idx] = o.neighbor(Q[idx], pool, aminus[idx], pidx, side[idx], orient[idx], ft[idx])
+    return Q

@@ -325,6 +325,30 @@ extern "C" __global__ void sei_taylor_o{order}(int n, const float* __restrict__ 
         off += bi * NQ
     a("  sei_store_col<kBp>(out + ((size_t)cell * 9 + q) * kBp, o);")
     a("}")
+
+    # Taylor evaluation gathered into a block pool (local time stepping: a coarser neighbour's
+    # derivatives integrated over the sub-interval of the finer cell; TimeCommon.cpp:40-87)
+    a(f"""
+// pool[dst[e]][9][Bp] = sum_i coeffs[i] dQ(i) of derivative slot src[e], e < m; one thread per (e, q).
+extern "C" __global__ void sei_taylor_gather_o{order}(int m, const int* __restrict__ src, const int* __restrict__ dst,
+                                                      const float* __restrict__ derivs, SeiCoeffs coeffs,
+                                                      float* __restrict__ pool) {{
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)m * 9) return;
+  const long e = t / 9;
+  const int q = (int)(t % 9);
+  const float* d = derivs + (size_t)__ldg(src + e) * kDerivSize;
+  float o[kBp];
+#pragma unroll
+  for (int k = 0; k < kBp; ++k) o[k] = 0.f;""")
+    off = 0
+    for i in range(order):
+        bi = nb3(order - i)
+        a(f"  {{ const float* s = d + {off} + q * {bi};")
+        a(f"#pragma unroll\n    for (int k = 0; k < {bi}; ++k) o[k] = fmaf(coeffs.c[{i}], s[k], o[k]); }}")
+        off += bi * NQ
+    a("  sei_store_col<kBp>(pool + ((size_t)__ldg(dst + e) * 9 + q) * kBp, o);")
+    a("}")
     a(f"}}  // namespace sei_o{order}")
     return "\n".join(L) + "\n"
 

@@ -1,6 +1,7 @@
 // C ABI of the GB300 ADER-DG element update (declarations and reference mapping in include/sei_gb300.h).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <exception>
@@ -67,8 +68,19 @@ struct sei_ctx {
   int* d_status = nullptr;   // device error word: 1 = a bounded wait in a kernel gave up
   std::vector<cudaEvent_t> prof_events;
   std::vector<int> prof_kind;  // kind of the launch starting at event i: 0 ADER (or fused ADER + local),
-                               // 1 neighbour, 2 fault, 3 local integral, -1 end of run
+                               // 1 neighbour, 2 fault, 3 local integral, 4 LTS gather / buffer, -1 end of run
   size_t prof_used = 0;
+  // local time stepping (sei_lts_setup): cells sorted by cluster; the time-integrated array I is a
+  // pool of 9 x Bp blocks: [0, n) the cells' own I, then one integration buffer per cell with a
+  // coarser neighbour, then one block per face whose neighbour is coarser (its Taylor integral)
+  bool lts = false;
+  int ncl = 0;
+  double lts_dt0 = 0.0;
+  std::vector<int64_t> cl_start, b_start, g_start;  // [ncl + 1] each
+  std::vector<int64_t> lts_perm;                    // new cell -> cell before sei_lts_setup
+  int32_t* d_src = nullptr;                         // [n][4] pool block read through each face
+  int32_t *d_bcell = nullptr, *d_bdst = nullptr;    // buffer entries, grouped by cluster
+  int32_t *d_gsrc = nullptr, *d_gdst = nullptr;     // gather entries (derivative slot -> pool block)
 };
 
 namespace {
@@ -99,6 +111,10 @@ void freeArrays(sei_ctx* c) {
   cudaFree(c->rel);
   cudaFree(c->ftype);
   cudaFree(c->dslot);
+  for (void* p : {(void*)c->d_src, (void*)c->d_bcell, (void*)c->d_bdst, (void*)c->d_gsrc, (void*)c->d_gdst}) cudaFree(p);
+  c->d_src = c->d_bcell = c->d_bdst = c->d_gsrc = c->d_gdst = nullptr;
+  c->lts = false;
+  c->ncl = 0;
   for (void* p : {(void*)c->d_pc, (void*)c->d_mc, (void*)c->d_pslot, (void*)c->d_mslot, (void*)c->d_iters, (void*)c->d_ps,
                   (void*)c->d_ms, (void*)c->d_rel, (void*)c->d_tinvt, (void*)c->d_fsp, (void*)c->d_fsm, (void*)c->d_isp,
                   (void*)c->d_ism, (void*)c->d_imp, (void*)c->d_state})
@@ -1077,6 +1093,267 @@ int sei_mlp_predict(const float* params, const float* norm, const float* samples
   cudaGetLastError();
   for (float* p : {dP, dN, dX, dO}) cudaFree(p);
   return rc;
+}
+
+namespace {
+// MonomialBasis::integrate(a, b): (b^{i+1} - a^{i+1}) / (i+1)!
+void subCoeffs(int order, double a, double b, float* out) {
+  double pa = a, pb = b, fact = 1.0;
+  for (int i = 0; i < order; ++i) {
+    fact *= (i + 1);
+    out[i] = (float)((pb - pa) / fact);
+    pa *= a;
+    pb *= b;
+  }
+}
+
+int upload(sei_ctx* c, int32_t** dst, const std::vector<int32_t>& src) {
+  cudaFree(*dst);
+  *dst = nullptr;
+  if (src.empty()) return SEI_OK;
+  if (cudaMalloc(dst, src.size() * sizeof(int32_t)) != cudaSuccess) return fail(c, SEI_ERR_OOM, "LTS table allocation");
+  SEI_CUDA(cudaMemcpy(*dst, src.data(), src.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  return SEI_OK;
+}
+}  // namespace
+
+int sei_lts_setup(sei_ctx* c, double cfl, int max_clusters, int* nclusters) {
+  int rc = checkReady(c);
+  if (rc) return rc;
+  if (!c->has_mesh) return fail(c, SEI_ERR_STATE, "local time stepping needs a mesh built by the context");
+  if (c->has_fault) return fail(c, SEI_ERR_UNSUPPORTED, "local time stepping with a fault is not built");
+  if (c->lts) return fail(c, SEI_ERR_STATE, "local time stepping is already set up");
+  if (!(cfl > 0) || max_clusters < 1 || max_clusters > 16) return fail(c, SEI_ERR_ARG, "cfl > 0, 1 <= max_clusters <= 16");
+  const int64_t n = c->n;
+  std::vector<double> dt;
+  sei::cellTimesteps(c->mesh, c->cfg.order, cfl, dt);
+  double dt0 = 1e300;
+  for (double v : dt) dt0 = std::min(dt0, v);
+  // rate-2 clusters: cluster k holds the time steps in [2^k dt0, 2^{k+1} dt0)
+  std::vector<int> cl(n);
+  for (int64_t i = 0; i < n; ++i) {
+    int k = (int)std::floor(std::log2(dt[i] / dt0) + 1e-12);
+    cl[i] = std::max(0, std::min(max_clusters - 1, k));
+  }
+  // maximum difference property: neighbouring clusters differ by at most one
+  for (bool changed = true; changed;) {
+    changed = false;
+    for (int64_t i = 0; i < n; ++i)
+      for (int f = 0; f < 4; ++f) {
+        if (c->mesh.ftype[i * 4 + f] != 0) continue;
+        const int32_t nb = c->mesh.nbr[i * 4 + f];
+        if (cl[i] > cl[nb] + 1) {
+          cl[i] = cl[nb] + 1;
+          changed = true;
+        }
+      }
+  }
+  int ncl = 0;
+  for (int v : cl) ncl = std::max(ncl, v + 1);
+  // stable reorder by cluster
+  std::vector<int64_t> order(n);
+  for (int64_t i = 0; i < n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return cl[a] < cl[b]; });
+  const int blk = 9 * c->Bp;
+  std::vector<float> qold((size_t)n * blk), qnew((size_t)n * blk);
+  SEI_CUDA(cudaStreamSynchronize(c->stream));
+  SEI_CUDA(cudaMemcpy(qold.data(), c->Q, qold.size() * sizeof(float), cudaMemcpyDeviceToHost));
+  for (int64_t i = 0; i < n; ++i)
+    std::memcpy(&qnew[(size_t)i * blk], &qold[(size_t)order[i] * blk], blk * sizeof(float));
+  try {
+    sei::permuteCells(c->mesh, order);
+    sei::buildOperators(c->mesh, c->h_star, c->h_aplus, c->h_aminus);
+  } catch (const std::exception& e) {
+    return fail(c, SEI_ERR_ARG, e.what());
+  }
+  rc = uploadCells(c, n, c->h_star.data(), c->h_aplus.data(), c->h_aminus.data(), c->mesh.nbr.data(),
+                   c->mesh.side.data(), c->mesh.orient.data(), c->mesh.ftype.data());
+  if (rc) return rc;
+  SEI_CUDA(cudaMemcpy(c->Q, qnew.data(), qnew.size() * sizeof(float), cudaMemcpyHostToDevice));
+  std::vector<int> cn(n);
+  for (int64_t i = 0; i < n; ++i) cn[i] = cl[order[i]];
+  std::vector<int64_t> cs(ncl + 1, 0);
+  for (int64_t i = 0; i < n; ++i) ++cs[cn[i] + 1];
+  for (int k = 0; k < ncl; ++k) cs[k + 1] += cs[k];
+  // buffers (cells with a coarser neighbour), derivative slots (cells with a finer neighbour)
+  std::vector<int32_t> bslot(n, -1), dsl(n, -1);
+  int64_t nB = 0, nD = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    bool coarser = false, finer = false;
+    for (int f = 0; f < 4; ++f) {
+      if (c->mesh.ftype[i * 4 + f] != 0) continue;
+      const int d = cn[c->mesh.nbr[i * 4 + f]] - cn[i];
+      coarser |= d > 0;
+      finer |= d < 0;
+    }
+    if (coarser) bslot[i] = (int32_t)nB++;
+    if (finer) dsl[i] = (int32_t)nD++;
+  }
+  // per-face sources; buffer and gather entries grouped by the cluster of the reading cell
+  std::vector<int32_t> src((size_t)n * 4);
+  std::vector<std::vector<int32_t>> bc(ncl), bd(ncl), gs(ncl), gd(ncl);
+  int64_t nS = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    if (bslot[i] >= 0) {
+      bc[cn[i]].push_back((int32_t)i);
+      bd[cn[i]].push_back((int32_t)(n + bslot[i]));
+    }
+    for (int f = 0; f < 4; ++f) {
+      const int32_t nb = c->mesh.nbr[i * 4 + f];
+      if (c->mesh.ftype[i * 4 + f] != 0) {
+        src[i * 4 + f] = nb;
+        continue;
+      }
+      const int d = cn[nb] - cn[i];
+      if (d == 0) {
+        src[i * 4 + f] = nb;
+      } else if (d < 0) {
+        src[i * 4 + f] = (int32_t)(n + bslot[nb]);
+      } else {
+        const int64_t blkIdx = n + nB + nS++;
+        src[i * 4 + f] = (int32_t)blkIdx;
+        gs[cn[i]].push_back(dsl[nb]);
+        gd[cn[i]].push_back((int32_t)blkIdx);
+      }
+    }
+  }
+  if (n + nB + nS > INT32_MAX) return fail(c, SEI_ERR_ARG, "mesh too large for 32-bit pool indices");
+  std::vector<int32_t> fbc, fbd, fgs, fgd;
+  std::vector<int64_t> bs(ncl + 1, 0), gst(ncl + 1, 0);
+  for (int k = 0; k < ncl; ++k) {
+    fbc.insert(fbc.end(), bc[k].begin(), bc[k].end());
+    fbd.insert(fbd.end(), bd[k].begin(), bd[k].end());
+    fgs.insert(fgs.end(), gs[k].begin(), gs[k].end());
+    fgd.insert(fgd.end(), gd[k].begin(), gd[k].end());
+    bs[k + 1] = (int64_t)fbc.size();
+    gst[k + 1] = (int64_t)fgs.size();
+  }
+  // device: the I pool, derivative slots, tables
+  cudaFree(c->I);
+  c->I = nullptr;
+  if (cudaMalloc(&c->I, (size_t)(n + nB + nS) * blk * sizeof(float)) != cudaSuccess)
+    return fail(c, SEI_ERR_OOM, "LTS pool allocation");
+  SEI_CUDA(cudaMemset(c->I, 0, (size_t)(n + nB + nS) * blk * sizeof(float)));
+  cudaFree(c->derivs);
+  c->derivs = nullptr;
+  const int dsz = sei::derivativesSize(c->cfg.order);
+  if (nD > 0 && cudaMalloc(&c->derivs, (size_t)nD * dsz * sizeof(float)) != cudaSuccess)
+    return fail(c, SEI_ERR_OOM, "LTS derivative allocation");
+  c->nslots = nD;
+  if ((rc = upload(c, &c->dslot, dsl)) || (rc = upload(c, &c->d_src, src)) || (rc = upload(c, &c->d_bcell, fbc)) ||
+      (rc = upload(c, &c->d_bdst, fbd)) || (rc = upload(c, &c->d_gsrc, fgs)) || (rc = upload(c, &c->d_gdst, fgd)))
+    return rc;
+  c->lts = true;
+  c->ncl = ncl;
+  c->lts_dt0 = dt0;
+  c->cl_start = cs;
+  c->b_start = bs;
+  c->g_start = gst;
+  c->lts_perm = order;
+  if (nclusters) *nclusters = ncl;
+  return SEI_OK;
+}
+
+namespace {
+// Cells [s, e) of the context as a kernel view; the neighbour view reads the pool through d_src.
+sei::DeviceArrays rangeView(sei_ctx* c, int64_t s, int64_t e, bool neighbour) {
+  const size_t blk = (size_t)9 * c->Bp;
+  sei::DeviceArrays d{};
+  d.n = (int)(e - s);
+  d.Q = c->Q + s * blk;
+  d.I = neighbour ? c->I : c->I + s * blk;
+  d.derivs = c->derivs;
+  d.dslot = c->dslot ? c->dslot + s : nullptr;
+  d.star_nz = c->star_nz + s * 3 * sei::kStarNnz;
+  d.aplus = c->aplus + s * 4 * 81;
+  d.aminus = c->aminus + s * 4 * 81;
+  d.nbr = (neighbour ? c->d_src : c->nbr) + s * 4;
+  d.rel = c->rel + s * 4;
+  d.ftype = c->ftype + s * 4;
+  return d;
+}
+
+// One cycle: every cluster advances by dt0 2^(ncl-1).  Sub-step k of the finest cluster starts
+// with the predictions (ADER, integration buffer, local integral) of the clusters whose step begins
+// at k, then the corrections (coarse-neighbour Taylor integrals, neighbour flux) of the clusters
+// whose step ends at k + 1 (TimeCluster predict / correct, TimeCommon::computeIntegrals).
+int ltsCycle(sei_ctx* c) {
+  const int blk = 9 * c->Bp;
+  const int64_t steps = (int64_t)1 << (c->ncl - 1);
+  float co[8];
+  for (int64_t k = 0; k < steps; ++k) {
+    for (int cl = 0; cl < c->ncl; ++cl) {
+      const int64_t len = (int64_t)1 << cl;
+      if (k % len) continue;
+      const int64_t s = c->cl_start[cl], e = c->cl_start[cl + 1];
+      if (s == e) continue;
+      taylorCoeffs(c->cfg.order, c->lts_dt0 * (double)len, co);
+      sei::DeviceArrays d = rangeView(c, s, e, false);
+      int rc = launchAderOnly(c, d, co);
+      if (rc) return rc;
+      const int64_t bs = c->b_start[cl], be = c->b_start[cl + 1];
+      if (be > bs) {
+        if ((rc = profMark(c, 4))) return rc;
+        // a new step of the next coarser cluster begins when k / len is even
+        if (sei::launchLtsBuffer((int)(be - bs), c->d_bcell + bs, c->d_bdst + bs, c->I, blk, ((k / len) % 2) == 0,
+                                 c->stream))
+          return fail(c, SEI_ERR_CUDA, "LTS buffer kernel launch failed");
+      }
+      if ((rc = launchLintOnly(c, d))) return rc;
+    }
+    for (int cl = 0; cl < c->ncl; ++cl) {
+      const int64_t len = (int64_t)1 << cl;
+      if ((k + 1) % len) continue;
+      const int64_t s = c->cl_start[cl], e = c->cl_start[cl + 1];
+      if (s == e) continue;
+      const int64_t gs = c->g_start[cl], ge = c->g_start[cl + 1];
+      if (ge > gs) {
+        // position of this step inside the step of the next coarser cluster
+        const int64_t s0 = k + 1 - len;
+        const double a = (double)(s0 % (2 * len)) * c->lts_dt0, b = a + (double)len * c->lts_dt0;
+        subCoeffs(c->cfg.order, a, b, co);
+        int rc = profMark(c, 4);
+        if (rc) return rc;
+        if (c->k.taylorGather((int)(ge - gs), c->d_gsrc + gs, c->d_gdst + gs, c->derivs, co, c->I, c->stream))
+          return fail(c, SEI_ERR_CUDA, "LTS gather kernel launch failed");
+      }
+      int rc = launchNeighbor(c, rangeView(c, s, e, true));
+      if (rc) return rc;
+    }
+  }
+  return SEI_OK;
+}
+}  // namespace
+
+int sei_lts_run(sei_ctx* c, int ncycles) {
+  int rc = checkReady(c);
+  if (rc) return rc;
+  if (!c->lts) return fail(c, SEI_ERR_STATE, "local time stepping not set up (sei_lts_setup)");
+  if (ncycles < 0) return fail(c, SEI_ERR_ARG, "ncycles < 0");
+  c->prof_used = 0;
+  SEI_CUDA(cudaEventRecord(c->ev0, c->stream));
+  for (int i = 0; i < ncycles && rc == SEI_OK; ++i) rc = ltsCycle(c);
+  if (!rc) rc = profMark(c, -1);
+  SEI_CUDA(cudaEventRecord(c->ev1, c->stream));
+  return rc;
+}
+
+int sei_lts_clusters(sei_ctx* c, int* nclusters, int64_t* start, double* dt) {
+  if (!c || !nclusters) return SEI_ERR_ARG;
+  if (!c->lts) return fail(c, SEI_ERR_STATE, "local time stepping not set up (sei_lts_setup)");
+  *nclusters = c->ncl;
+  for (int k = 0; k <= c->ncl; ++k)
+    if (start) start[k] = c->cl_start[k];
+  for (int k = 0; k < c->ncl; ++k)
+    if (dt) dt[k] = c->lts_dt0 * (double)((int64_t)1 << k);
+  return SEI_OK;
+}
+
+int sei_lts_permutation(sei_ctx* c, int64_t* perm) {
+  if (!c || !perm) return SEI_ERR_ARG;
+  if (!c->lts) return fail(c, SEI_ERR_STATE, "local time stepping not set up (sei_lts_setup)");
+  std::memcpy(perm, c->lts_perm.data(), c->lts_perm.size() * sizeof(int64_t));
+  return SEI_OK;
 }
 
 int sei_set_profiling(sei_ctx* c, int on) {

@@ -35,6 +35,10 @@ void buildPeriodicCube(const sei_cube_params& p, HostMesh& m);
 void computeFaceRelations(HostMesh& m);
 void buildOperators(const HostMesh& m, std::vector<float>& star, std::vector<float>& aplus, std::vector<float>& aminus);
 double cflTimestep(const HostMesh& m, int order, double cfl);
+// CFL time step of every cell (GlobalTimestep.cpp:27-47 per element).
+void cellTimesteps(const HostMesh& m, int order, double cfl, std::vector<double>& dt);
+// Reorders the cells: new cell i is old cell order[i]; face relations are recomputed.
+void permuteCells(HostMesh& m, const std::vector<int64_t>& order);
 void seedDofs(int64_t n, int order, uint64_t seed, std::vector<float>& dofs);
 
 // Kernel launchers (one translation unit per order).
@@ -57,6 +61,9 @@ using LaunchNeighborFn = int (*)(const DeviceArrays&, void* stream);
 using LaunchTaylorFn = int (*)(int n, const float* derivs, const float* coeffs, float* out, void* stream);
 
 using LaunchLintFn = int (*)(const DeviceArrays&, void* stream);
+// pool[dst[e]] = Taylor sum of derivative slot src[e], e < m (local time stepping)
+using LaunchTaylorGatherFn = int (*)(int m, const int32_t* src, const int32_t* dst, const float* derivs,
+                                     const float* coeffs, float* pool, void* stream);
 
 struct OrderKernels {
   LaunchLocalFn local;        // ADER + local integral, one launch
@@ -64,7 +71,12 @@ struct OrderKernels {
   LaunchTaylorFn taylor;      // Taylor evaluation of stored derivatives
   LaunchLocalFn ader;         // ADER alone (writes I, optional derivatives)
   LaunchLintFn lint;          // volume + local flux from I
+  LaunchTaylorGatherFn taylorGather;
 };
+
+// pool[dst[e]] = (reset ? 0 : pool[dst[e]]) + pool[cell[e]] for e < m, blocks of blk floats
+// (integration buffers of local time stepping).
+int launchLtsBuffer(int m, const int32_t* cell, const int32_t* dst, float* pool, int blk, int reset, void* stream);
 
 bool kernelsForOrder(int order, OrderKernels& out);
 

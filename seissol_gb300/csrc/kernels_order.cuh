@@ -73,10 +73,19 @@ int launchTaylor(int n, const float* derivs, const float* coeffs, float* out, vo
   K::SEI_CAT(sei_taylor_o, SEI_ORDER)<<<blocks, 256, 0, (cudaStream_t)stream>>>(n, derivs, toCoeffs(coeffs), out);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
+int launchTaylorGather(int m, const int32_t* src, const int32_t* dst, const float* derivs, const float* coeffs,
+                       float* pool, void* stream) {
+  if (m <= 0) return 0;
+  const long threads = (long)m * 9;
+  const int blocks = (int)((threads + 255) / 256);
+  K::SEI_CAT(sei_taylor_gather_o, SEI_ORDER)<<<blocks, 256, 0, (cudaStream_t)stream>>>(m, src, dst, derivs,
+                                                                                       toCoeffs(coeffs), pool);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
 }  // namespace
 
 namespace sei {
 OrderKernels SEI_CAT(orderKernels, SEI_ORDER)() {
-  return OrderKernels{launchLocal, launchNeighbor, launchTaylor, launchAder, launchLint};
+  return OrderKernels{launchLocal, launchNeighbor, launchTaylor, launchAder, launchLint, launchTaylorGather};
 }
 }  // namespace sei

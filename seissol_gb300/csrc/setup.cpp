@@ -198,7 +198,23 @@ void buildPeriodicCube(const sei_cube_params& p, HostMesh& m) {
     throw std::invalid_argument("periodic cube needs even cube counts >= 4 in every direction");
   if (!(p.h > 0) || !(p.rho > 0) || !(p.vp > 0) || !(p.vs > 0) || p.perturb < 0 || p.perturb >= 0.5)
     throw std::invalid_argument("invalid cube geometry or material");
+  if (p.grading > 1.0 && p.fault_plane >= 0)
+    throw std::invalid_argument("a graded cube cannot carry the planar fault");
   const int64_t ncubes = (int64_t)p.nx * p.ny * p.nz;
+  // vertex positions along each direction: cumulative cube edges (uniform h, or log-uniform in
+  // [h, grading h] from the seed); index nx (ny, nz) is the periodic image of 0
+  std::vector<double> pos[3];
+  {
+    Rng grng(p.seed ^ 0x9E3779B97F4A7C15ull);
+    const int cnt[3] = {p.nx, p.ny, p.nz};
+    for (int d = 0; d < 3; ++d) {
+      pos[d].assign(cnt[d] + 1, 0.0);
+      for (int i = 0; i < cnt[d]; ++i) {
+        const double w = p.grading > 1.0 ? p.h * std::exp(grng.uniform(0.0, std::log(p.grading))) : p.h;
+        pos[d][i + 1] = pos[d][i] + w;
+      }
+    }
+  }
   m.n = ncubes * 5;
   m.topo.resize(m.n * 4);
   m.coords.resize(m.n * 12);
@@ -250,9 +266,9 @@ void buildPeriodicCube(const sei_cube_params& p, HostMesh& m) {
             for (int v = 0; v < 4; ++v) {
               const int gi = i + tets[par][t][v][0], gj = j + tets[par][t][v][1], gk = k + tets[par][t][v][2];
               m.topo[cell * 4 + v] = (gi % p.nx) + (int64_t)p.nx * ((gj % p.ny) + (int64_t)p.ny * (gk % p.nz));
-              m.coords[cell * 12 + v * 3 + 0] = gi * p.h;
-              m.coords[cell * 12 + v * 3 + 1] = gj * p.h;
-              m.coords[cell * 12 + v * 3 + 2] = gk * p.h;
+              m.coords[cell * 12 + v * 3 + 0] = pos[0][gi];
+              m.coords[cell * 12 + v * 3 + 1] = pos[1][gj];
+              m.coords[cell * 12 + v * 3 + 2] = pos[2][gk];
             }
             ++cell;
           }
@@ -359,7 +375,15 @@ void buildOperators(const HostMesh& m, std::vector<float>& star, std::vector<flo
 }
 
 double cflTimestep(const HostMesh& m, int order, double cfl) {
+  std::vector<double> dt;
+  cellTimesteps(m, order, cfl, dt);
   double best = 1e300;
+  for (double v : dt) best = std::min(best, v);
+  return best;
+}
+
+void cellTimesteps(const HostMesh& m, int order, double cfl, std::vector<double>& dt) {
+  dt.assign(m.n, 0.0);
   for (int64_t c = 0; c < m.n; ++c) {
     Vec3 x[4];
     for (int k = 0; k < 4; ++k) x[k] = {m.coords[c * 12 + k * 3], m.coords[c * 12 + k * 3 + 1], m.coords[c * 12 + k * 3 + 2]};
@@ -369,9 +393,25 @@ double cflTimestep(const HostMesh& m, int order, double cfl) {
     const double insphere = std::fabs(alpha) / areas;
     const double rho = m.material[c * 3], mu = m.material[c * 3 + 1], lam = m.material[c * 3 + 2];
     const double vp = std::sqrt((lam + 2 * mu) / rho);
-    best = std::min(best, cfl * 2.0 * insphere / (vp * (2 * order - 1)));
+    dt[c] = cfl * 2.0 * insphere / (vp * (2 * order - 1));
   }
-  return best;
+}
+
+void permuteCells(HostMesh& m, const std::vector<int64_t>& order) {
+  const int64_t n = m.n;
+  if ((int64_t)order.size() != n) throw std::invalid_argument("permutation size");
+  std::vector<int64_t> topo(n * 4);
+  std::vector<double> coords(n * 12), material(n * 3);
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t o = order[i];
+    for (int k = 0; k < 4; ++k) topo[i * 4 + k] = m.topo[o * 4 + k];
+    for (int k = 0; k < 12; ++k) coords[i * 12 + k] = m.coords[o * 12 + k];
+    for (int k = 0; k < 3; ++k) material[i * 3 + k] = m.material[o * 3 + k];
+  }
+  m.topo.swap(topo);
+  m.coords.swap(coords);
+  m.material.swap(material);
+  computeFaceRelations(m);
 }
 
 void seedDofs(int64_t n, int order, uint64_t seed, std::vector<float>& dofs) {

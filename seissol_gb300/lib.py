@@ -35,7 +35,7 @@ class _Config(C.Structure):
 class _CubeParams(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("h", C.c_double), ("rho", C.c_double),
                 ("vp", C.c_double), ("vs", C.c_double), ("perturb", C.c_double), ("seed", C.c_uint64),
-                ("fault_plane", C.c_int)]
+                ("fault_plane", C.c_int), ("grading", C.c_double)]
 
 
 class RSParams(C.Structure):
@@ -123,6 +123,10 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_dr_get_slots", i, [VP, VP])
     _sig(lib, "sei_kernel_times_ms", i, [VP, C.POINTER(d), C.POINTER(d), C.POINTER(i)])
     _sig(lib, "sei_kernel_times_by_kind", i, [VP, VP, VP])
+    _sig(lib, "sei_lts_setup", i, [VP, d, i, C.POINTER(i)])
+    _sig(lib, "sei_lts_run", i, [VP, i])
+    _sig(lib, "sei_lts_clusters", i, [VP, C.POINTER(i), VP, VP])
+    _sig(lib, "sei_lts_permutation", i, [VP, VP])
     _sig(lib, "sei_mlp_num_params", i, [])
     _sig(lib, "sei_dr_record_samples", i, [VP, i64])
     _sig(lib, "sei_dr_get_samples", i, [VP, VP, i64, C.POINTER(i64)])
@@ -240,8 +244,8 @@ class Context:
 
     # -- set-up ------------------------------------------------------------------------
     def build_periodic_cube(self, nx, ny, nz, h=100.0, rho=2700.0, vp=6000.0, vs=3464.0, perturb=0.0, seed=1,
-                            fault_plane=-1):
-        p = _CubeParams(nx, ny, nz, h, rho, vp, vs, perturb, seed, fault_plane)
+                            fault_plane=-1, grading=1.0):
+        p = _CubeParams(nx, ny, nz, h, rho, vp, vs, perturb, seed, fault_plane, grading)
         n = C.c_int64()
         self._check(self.lib.sei_build_periodic_cube(self.h, C.byref(p), C.byref(n)), "sei_build_periodic_cube")
         self.n = n.value
@@ -422,6 +426,29 @@ class Context:
 
     def dr_warm_start(self, on=True):
         self._check(self.lib.sei_dr_warm_start(self.h, int(on)), "sei_dr_warm_start")
+
+    def lts_setup(self, cfl=0.5, max_clusters=8):
+        """Rate-2 local time stepping; reorders the cells by cluster.  Returns the cluster count."""
+        k = C.c_int()
+        self._check(self.lib.sei_lts_setup(self.h, cfl, max_clusters, C.byref(k)), "sei_lts_setup")
+        return k.value
+
+    def lts_run(self, ncycles=1):
+        self._check(self.lib.sei_lts_run(self.h, ncycles), "sei_lts_run")
+
+    def lts_clusters(self):
+        """(start [ncl + 1], dt [ncl]) of the clusters."""
+        k = C.c_int()
+        self._check(self.lib.sei_lts_clusters(self.h, C.byref(k), None, None), "sei_lts_clusters")
+        start = np.zeros(k.value + 1, np.int64)
+        dt = np.zeros(k.value, np.float64)
+        self._check(self.lib.sei_lts_clusters(self.h, C.byref(k), _ptr(start), _ptr(dt)), "sei_lts_clusters")
+        return start, dt
+
+    def lts_permutation(self):
+        out = np.zeros(self.n, np.int64)
+        self._check(self.lib.sei_lts_permutation(self.h, _ptr(out)), "sei_lts_permutation")
+        return out
 
     def set_profiling(self, on=True):
         self._check(self.lib.sei_set_profiling(self.h, int(on)), "sei_set_profiling")
