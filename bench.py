@@ -225,6 +225,58 @@ DR_DIMS = (6, 100, 100)  # 60,000 cubes = 300,000 tets; fault plane x = 3 h: 100
 DR_SEED = 77
 
 
+LTS_DIMS = (34, 34, 34)  # 39,304 cubes = 196,520 tets
+
+
+def lts_measurement(local, cycles):
+    """Rate-2 local time stepping on a graded cube: elastic order 5 (35 x 9), 196,520 tets, cube
+    edges log-uniform in [50, 400] m per direction, material +-10 %, CFL 0.5; four clusters.
+    One cycle advances every cluster by the coarsest step.  Reported: cell updates per second
+    (a cell update = one step of one cell in its own cluster), the simulated time per wall second
+    against global time stepping at the finest step (same kernels, same simulated time), with the
+    cycles launched directly and replayed from one recorded CUDA graph."""
+    import numpy as np
+
+    from seissol_gb300 import Context
+
+    out = {}
+    for mode in ("direct", "graph"):
+        ctx = Context(5, device=local)
+        n = ctx.build_periodic_cube(*LTS_DIMS, h=50.0, perturb=PERTURB, seed=SEED, grading=8.0)
+        ncl = ctx.lts_setup(0.5, 8)
+        start, dts = ctx.lts_clusters()
+        counts = np.diff(start)
+        ctx.set_option(2, 1 if mode == "graph" else 0)  # SEI_OPT_LTS_GRAPH
+        ctx.lts_run(2)
+        ctx.sync()
+        ctx.lts_run(cycles)
+        ctx.sync()
+        ms = ctx.last_run_ms()
+        updates = float((counts * (2.0 ** (ncl - 1 - np.arange(ncl)))).sum()) * cycles
+        sim = cycles * dts[-1]
+        out[mode] = {"ms_per_cycle": ms / cycles, "cell_updates_per_s": updates / (ms / 1e3),
+                     "simulated_s_per_wall_s": sim / (ms / 1e3)}
+        if mode == "direct":
+            steps = cycles << (ncl - 1)
+            ctx.run("all", dts[0], 2)
+            ctx.sync()
+            ctx.run("all", dts[0], steps)
+            ctx.sync()
+            gms = ctx.last_run_ms()
+            out["global_stepping"] = {"dt": dts[0], "steps": steps, "ms": gms,
+                                      "cell_updates_per_s": n * steps / (gms / 1e3),
+                                      "simulated_s_per_wall_s": steps * dts[0] / (gms / 1e3)}
+        ctx.close()
+    return {"workload": "elastic order 5 (35x9), 196,520-tet graded periodic cube 34^3 cubes x 5 tets, cube edges "
+                        "log-uniform in [50, 400] m, material +-10%, CFL 0.5, rate-2 clusters (stand-in for the "
+                        "viscoelastic configuration, whose 27-quantity kernels are not built)",
+            "cells": n, "clusters": int(ncl), "cells_per_cluster": [int(x) for x in counts],
+            "cluster_dt": [float(x) for x in dts], "cycles": cycles, "direct": out["direct"], "graph": out["graph"],
+            "global_stepping": out["global_stepping"],
+            "lts_speedup_simulated_time": out["graph"]["simulated_s_per_wall_s"]
+            / out["global_stepping"]["simulated_s_per_wall_s"]}
+
+
 def dr_measurement(local, steps):
     """Dynamic rupture on the fault workload: elastic order 4, 300,000 tets, a planar fault of
     20,000 faces (25 points each), fast-velocity-weakening friction with a ~ U[0.008, 0.02],
@@ -389,6 +441,9 @@ def run_ours(args, world, rank, local):
     dr = None
     if rank == 0 and args.dr_steps > 0:
         dr = dr_measurement(local, args.dr_steps)
+    lts = None
+    if rank == 0 and args.lts_cycles > 0:
+        lts = lts_measurement(local, args.lts_cycles)
 
     base = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -403,7 +458,8 @@ def run_ours(args, world, rank, local):
                            "l2": "inputs larger than L2 (~3 GB resident per GPU), no flush",
                            "parallelism": f"replicas x{world}"},
                 "roofline": roof, "cpu_baseline": base, "e2e": e2e, "clocks": clocks,
-                "gpu_launches": launches, "kernel_ms_per_step": kernels, "dynamic_rupture": dr}
+                "gpu_launches": launches, "kernel_ms_per_step": kernels, "dynamic_rupture": dr,
+                "local_time_stepping": lts}
         print(json.dumps(line))
     return 0
 
@@ -420,6 +476,8 @@ def main():
     ap.add_argument("--precision", choices=("fp32", "f16x3"), default="fp32")
     ap.add_argument("--dr-steps", type=int, default=20,
                     help="steps of the dynamic-rupture measurement (plain and warm-started); 0 skips it")
+    ap.add_argument("--lts-cycles", type=int, default=10,
+                    help="cycles of the local-time-stepping measurement; 0 skips it")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -165,6 +165,10 @@ int sei_evaluate_taylor(sei_ctx* ctx, const double* coeffs, float* out_device);
 /* Options. SEI_OPT_FUSED_LOCAL: 1 runs ADER and the local integral as one launch, 0 (default)
  * as two launches (smaller kernels; I is written and re-read once). */
 #define SEI_OPT_FUSED_LOCAL 1
+/* SEI_OPT_LTS_GRAPH: 1 records one local-time-stepping cycle as a CUDA graph on the first
+ * sei_lts_run and replays it for every cycle (one graph launch per cycle); 0 (default) launches
+ * the kernels of every cycle directly.  Per-launch profiling is not recorded inside the graph. */
+#define SEI_OPT_LTS_GRAPH 2
 int sei_set_option(sei_ctx* ctx, int option, int value);
 
 /* Runs a proxy kernel for nsteps steps (src/Proxy/Runner.cpp:99-111); asynchronous. */

@@ -81,6 +81,9 @@ struct sei_ctx {
   int32_t* d_src = nullptr;                         // [n][4] pool block read through each face
   int32_t *d_bcell = nullptr, *d_bdst = nullptr;    // buffer entries, grouped by cluster
   int32_t *d_gsrc = nullptr, *d_gdst = nullptr;     // gather entries (derivative slot -> pool block)
+  bool lts_graph = false;                           // SEI_OPT_LTS_GRAPH
+  bool capturing = false;                           // recording the cycle graph: no profiling events
+  cudaGraphExec_t lts_exec = nullptr;               // one recorded cycle
 };
 
 namespace {
@@ -113,6 +116,8 @@ void freeArrays(sei_ctx* c) {
   cudaFree(c->dslot);
   for (void* p : {(void*)c->d_src, (void*)c->d_bcell, (void*)c->d_bdst, (void*)c->d_gsrc, (void*)c->d_gdst}) cudaFree(p);
   c->d_src = c->d_bcell = c->d_bdst = c->d_gsrc = c->d_gdst = nullptr;
+  if (c->lts_exec) cudaGraphExecDestroy(c->lts_exec);
+  c->lts_exec = nullptr;
   c->lts = false;
   c->ncl = 0;
   for (void* p : {(void*)c->d_pc, (void*)c->d_mc, (void*)c->d_pslot, (void*)c->d_mslot, (void*)c->d_iters, (void*)c->d_ps,
@@ -207,7 +212,7 @@ int checkReady(sei_ctx* c) {
 }
 
 int profMark(sei_ctx* c, int kind) {
-  if (!c->profiling) return SEI_OK;
+  if (!c->profiling || c->capturing) return SEI_OK;
   if (c->prof_used == c->prof_events.size()) {
     cudaEvent_t e;
     if (cudaEventCreate(&e) != cudaSuccess) return fail(c, SEI_ERR_CUDA, "event creation failed");
@@ -607,6 +612,9 @@ int sei_set_option(sei_ctx* c, int option, int value) {
   switch (option) {
     case SEI_OPT_FUSED_LOCAL:
       c->fused_local = value != 0;
+      return SEI_OK;
+    case SEI_OPT_LTS_GRAPH:
+      c->lts_graph = value != 0;
       return SEI_OK;
     default:
       return fail(c, SEI_ERR_ARG, "unknown option");
@@ -1331,8 +1339,29 @@ int sei_lts_run(sei_ctx* c, int ncycles) {
   if (!c->lts) return fail(c, SEI_ERR_STATE, "local time stepping not set up (sei_lts_setup)");
   if (ncycles < 0) return fail(c, SEI_ERR_ARG, "ncycles < 0");
   c->prof_used = 0;
+  if (c->lts_graph && !c->lts_exec && ncycles > 0) {
+    // record one cycle (relaxed mode: the launchers set kernel attributes while recording)
+    SEI_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+    c->capturing = true;
+    rc = ltsCycle(c);
+    c->capturing = false;
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (rc == SEI_OK && e != cudaSuccess) rc = cudaFail(c, e, "cudaStreamEndCapture");
+    if (rc == SEI_OK && cudaGraphInstantiate(&c->lts_exec, g, 0) != cudaSuccess)
+      rc = fail(c, SEI_ERR_CUDA, "cudaGraphInstantiate of the LTS cycle failed");
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (rc) return rc;
+  }
   SEI_CUDA(cudaEventRecord(c->ev0, c->stream));
-  for (int i = 0; i < ncycles && rc == SEI_OK; ++i) rc = ltsCycle(c);
+  for (int i = 0; i < ncycles && rc == SEI_OK; ++i) {
+    if (c->lts_graph) {
+      if (cudaGraphLaunch(c->lts_exec, c->stream) != cudaSuccess) rc = fail(c, SEI_ERR_CUDA, "cudaGraphLaunch failed");
+    } else {
+      rc = ltsCycle(c);
+    }
+  }
   if (!rc) rc = profMark(c, -1);
   SEI_CUDA(cudaEventRecord(c->ev1, c->stream));
   return rc;

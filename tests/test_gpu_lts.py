@@ -76,3 +76,21 @@ def test_lts_rejects_fault_and_repeat(built_lib):
     with pytest.raises(SeiError, match="SEI_ERR_STATE"):
         ctx.lts_setup(0.5, 4)
     ctx.close()
+
+
+def test_lts_graph_replay_matches_direct_launches(built_lib):
+    """SEI_OPT_LTS_GRAPH: a recorded cycle replayed three times gives the DOFs of three directly
+    launched cycles, bit for bit."""
+    SEI_OPT_LTS_GRAPH = 2
+    out = []
+    for graph in (0, 1):
+        ctx, n = _graded_ctx(5)
+        ctx.lts_setup(0.5, 8)
+        ctx.set_option(SEI_OPT_LTS_GRAPH, graph)
+        ctx.set_dofs(seeded_dofs(n, 5, 11))
+        ctx.lts_run(2)
+        ctx.lts_run(1)
+        ctx.sync()
+        out.append(ctx.get_dofs())
+        ctx.close()
+    assert np.array_equal(out[0], out[1])
