@@ -179,6 +179,27 @@ int sei_sync(sei_ctx* ctx);
 /* Device-side duration of the last sei_run, milliseconds (CUDA events on the context stream). */
 int sei_last_run_ms(sei_ctx* ctx, double* ms);
 
+/* Viscoelastic equations with 3 attenuation mechanisms (the reference's `viscoelastic`
+ * equations, codegen/kernels/equations/viscoelastic.py: 9 elastic quantities + 6 memory
+ * variables per mechanism = 27; set-up of src/Equations/viscoelastic/Model/ViscoelasticSetup.h
+ * and src/Physics/Attenuation.h).  Turns the context's mesh viscoelastic: the cells' moduli
+ * (relaxed, from the mesh) are fitted to quality factors qp, qs over the band around
+ * freq_central with freq_ratio (unrelaxed moduli, relaxation frequencies, theta); Q and I
+ * become [n][27][Bp] (elastic DOFs kept, memory variables zero); sei_run then runs the
+ * viscoelastic ADER (with the source term), local and neighbour kernels for SEI_KERNEL_ALL,
+ * LOCAL, ADER, LOCAL_WO_ADER and NEIGHBOR.  Orders 4 and 5, FP32, no fault, no LTS. */
+int sei_visco_setup(sei_ctx* ctx, double qp, double qs, double freq_central, double freq_ratio);
+/* Quantities per cell of the DOF arrays (9, or 27 after sei_visco_setup). */
+int sei_num_quantities(const sei_ctx* ctx);
+/* Operators of the viscoelastic set-up (also on a host-only context): grad [n][3][3] (d xi_e / d x),
+ * theta [n][3][3], the memory-variable flux blocks wplus / wminus [n][4][9 x 6 column-major] per
+ * unit omega (the flux solvers' memory columns of mechanism l are omega_l w), omega [3]. */
+int sei_visco_operators(sei_ctx* ctx, float* grad, float* theta, float* wplus, float* wminus, double* omega);
+/* The attenuation fit of one material (src/Physics/Attenuation.h:24-104): mu, lam relaxed in,
+ * unrelaxed out; omega [3], theta [3][3] (mechanism-major). */
+int sei_fit_attenuation(double qp, double qs, double freq_central, double freq_ratio, double* mu, double* lam,
+                        double* omega, double* theta);
+
 /* Local time stepping, rate 2 (replaces the clustering of src/Initializer/TimeStepping with the
  * maximum-difference property of docs/local-timestepping.rst, the predict / correct order of
  * src/Solver/TimeStepping/TimeCluster.cpp:358-440, 695-717 and TimeCommon::computeIntegrals,

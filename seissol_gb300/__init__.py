@@ -8,6 +8,7 @@ fallback: without the built library every entry point raises.
 from .lib import (  # noqa: F401
     tc_gemm_check,
     mlp_gradient,
+    fit_attenuation,
     mlp_predict,
     mlp_num_params,
     Context,

@@ -41,7 +41,7 @@ def _deps(src):
     deps = [src] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     deps.append(os.path.join(ROOT, "include", "sei_gb300.h"))
     base = os.path.basename(src)
-    if base.startswith("kernels_o"):
+    if base.startswith("kernels_"):
         deps.append(os.path.join(GEN, base.replace(".cu", ".cuh")))
     return deps
 
@@ -64,10 +64,11 @@ def _compile(src, verbose=False):
 
 def build(verbose: bool = False, jobs: int | None = None) -> str:
     sys.path.insert(0, ROOT)
-    from seissol_gb300.codegen import gen_kernels
+    from seissol_gb300.codegen import gen_kernels, gen_visco
 
     os.makedirs(OBJ, exist_ok=True)
     gen_kernels.write_all(GEN, ORDERS)
+    gen_visco.write_all(GEN)
     gen_kernels.write_dr_tables(GEN, (4,))
     gen_kernels.write_tc_tables(GEN, ORDERS)
     srcs = _sources()

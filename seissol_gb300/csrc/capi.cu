@@ -17,6 +17,15 @@ namespace sei {
 OrderKernels orderKernels4();
 OrderKernels orderKernels5();
 OrderKernels orderKernels6();
+ViscoKernels viscoKernels4();
+ViscoKernels viscoKernels5();
+bool viscoKernelsForOrder(int order, ViscoKernels& out) {
+  switch (order) {
+    case 4: out = viscoKernels4(); return true;
+    case 5: out = viscoKernels5(); return true;
+    default: return false;
+  }
+}
 
 bool kernelsForOrder(int order, OrderKernels& out) {
   switch (order) {
@@ -81,6 +90,13 @@ struct sei_ctx {
   int32_t* d_src = nullptr;                         // [n][4] pool block read through each face
   int32_t *d_bcell = nullptr, *d_bdst = nullptr;    // buffer entries, grouped by cluster
   int32_t *d_gsrc = nullptr, *d_gdst = nullptr;     // gather entries (derivative slot -> pool block)
+  // viscoelastic (sei_visco_setup): 27 quantities per cell in Q and I
+  int nq = 9;
+  bool visco = false;
+  sei::ViscoKernels vk{};
+  float omega[3] = {0, 0, 0};
+  float *d_grad = nullptr, *d_theta = nullptr, *d_wplus = nullptr, *d_wminus = nullptr;
+  std::vector<float> h_grad, h_theta, h_wplus, h_wminus;  // host copies (sei_visco_operators)
   bool lts_graph = false;                           // SEI_OPT_LTS_GRAPH
   bool capturing = false;                           // recording the cycle graph: no profiling events
   cudaGraphExec_t lts_exec = nullptr;               // one recorded cycle
@@ -114,7 +130,12 @@ void freeArrays(sei_ctx* c) {
   cudaFree(c->rel);
   cudaFree(c->ftype);
   cudaFree(c->dslot);
-  for (void* p : {(void*)c->d_src, (void*)c->d_bcell, (void*)c->d_bdst, (void*)c->d_gsrc, (void*)c->d_gdst}) cudaFree(p);
+  for (void* p : {(void*)c->d_src, (void*)c->d_bcell, (void*)c->d_bdst, (void*)c->d_gsrc, (void*)c->d_gdst,
+                  (void*)c->d_grad, (void*)c->d_theta, (void*)c->d_wplus, (void*)c->d_wminus})
+    cudaFree(p);
+  c->d_grad = c->d_theta = c->d_wplus = c->d_wminus = nullptr;
+  c->visco = false;
+  c->nq = 9;
   c->d_src = c->d_bcell = c->d_bdst = c->d_gsrc = c->d_gdst = nullptr;
   if (c->lts_exec) cudaGraphExecDestroy(c->lts_exec);
   c->lts_exec = nullptr;
@@ -339,7 +360,49 @@ int launchDr(sei_ctx* c, double dt) {
   return SEI_OK;
 }
 
+sei::ViscoArrays viscoArrays(sei_ctx* c) {
+  sei::ViscoArrays v{};
+  v.n = (int)c->n;
+  v.Q = c->Q;
+  v.I = c->I;
+  v.star_nz = c->star_nz;
+  v.grad = c->d_grad;
+  v.theta = c->d_theta;
+  v.aplus = c->aplus;
+  v.wplus = c->d_wplus;
+  v.aminus = c->aminus;
+  v.wminus = c->d_wminus;
+  v.nbr = c->nbr;
+  v.rel = c->rel;
+  v.ftype = c->ftype;
+  for (int i = 0; i < 3; ++i) v.omega[i] = c->omega[i];
+  return v;
+}
+
+// Viscoelastic steps: ADER, volume + local flux, neighbour flux (kernel kinds 0, 3, 1).
+int runVisco(sei_ctx* c, int kernel, double dt, int steps) {
+  float coeffs[8];
+  taylorCoeffs(c->cfg.order, dt, coeffs);
+  const sei::ViscoArrays v = viscoArrays(c);
+  const bool ader = kernel == SEI_KERNEL_ALL || kernel == SEI_KERNEL_LOCAL || kernel == SEI_KERNEL_ADER;
+  const bool lint = kernel == SEI_KERNEL_ALL || kernel == SEI_KERNEL_LOCAL || kernel == SEI_KERNEL_LOCAL_WO_ADER;
+  const bool nbr = kernel == SEI_KERNEL_ALL || kernel == SEI_KERNEL_NEIGHBOR;
+  if (!ader && !lint && !nbr) return fail(c, SEI_ERR_UNSUPPORTED, "kernel not built for the viscoelastic equations");
+  c->prof_used = 0;
+  int rc = SEI_OK;
+  for (int s = 0; s < steps && rc == SEI_OK; ++s) {
+    if (ader && !(rc = profMark(c, 0)) && c->vk.ader(v, coeffs, c->stream)) rc = fail(c, SEI_ERR_CUDA, "viscoelastic ADER launch failed");
+    if (!rc && lint && !(rc = profMark(c, 3)) && c->vk.lint(v, c->stream))
+      rc = fail(c, SEI_ERR_CUDA, "viscoelastic local-integral launch failed");
+    if (!rc && nbr && !(rc = profMark(c, 1)) && c->vk.neighbor(v, c->stream))
+      rc = fail(c, SEI_ERR_CUDA, "viscoelastic neighbour launch failed");
+  }
+  if (!rc) rc = profMark(c, -1);
+  return rc;
+}
+
 int runKernel(sei_ctx* c, int kernel, double dt, int steps) {
+  if (c->visco) return runVisco(c, kernel, dt, steps);
   float coeffs[8];
   taylorCoeffs(c->cfg.order, dt, coeffs);
   sei::DeviceArrays d = arrays(c);
@@ -529,15 +592,15 @@ int sei_cfl_timestep(sei_ctx* c, double cfl, double* dt) {
 int sei_derivatives_size(int order) { return (order >= 2 && order <= 8) ? sei::derivativesSize(order) : 0; }
 
 static int copyDofs(sei_ctx* c, float* dst_dev_or_host, const float* src, bool to_device) {
-  // Host arrays are unpadded [n][9][B]; device arrays have column stride Bp.
+  // Host arrays are unpadded [n][nq][B]; device arrays have column stride Bp.
   const size_t n = (size_t)c->n;
   if (c->B == c->Bp) {
-    const size_t bytes = n * 9 * c->B * sizeof(float);
+    const size_t bytes = n * c->nq * c->B * sizeof(float);
     SEI_CUDA(cudaMemcpyAsync(dst_dev_or_host, src, bytes, to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost,
                              c->stream));
   } else {
     SEI_CUDA(cudaMemcpy2DAsync(dst_dev_or_host, (to_device ? c->Bp : c->B) * sizeof(float), src,
-                               (to_device ? c->B : c->Bp) * sizeof(float), c->B * sizeof(float), n * 9,
+                               (to_device ? c->B : c->Bp) * sizeof(float), c->B * sizeof(float), n * c->nq,
                                to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, c->stream));
   }
   return SEI_OK;
@@ -1125,9 +1188,112 @@ int upload(sei_ctx* c, int32_t** dst, const std::vector<int32_t>& src) {
 }
 }  // namespace
 
+int sei_visco_setup(sei_ctx* c, double qp, double qs, double freq_central, double freq_ratio) {
+  if (!c) return SEI_ERR_ARG;
+  const bool host = c->cfg.device < 0;
+  int rc = host ? SEI_OK : checkReady(c);
+  if (rc) return rc;
+  if (!c->has_mesh) return fail(c, SEI_ERR_STATE, "the viscoelastic set-up needs a mesh built by the context");
+  if (c->has_fault || c->lts || c->visco)
+    return fail(c, SEI_ERR_UNSUPPORTED, "viscoelastic set-up: not built with a fault or local time stepping, or twice");
+  if (c->cfg.precision != SEI_PREC_FP32) return fail(c, SEI_ERR_UNSUPPORTED, "viscoelastic kernels are FP32 only");
+  sei::ViscoKernels vk{};
+  if (!sei::viscoKernelsForOrder(c->cfg.order, vk))
+    return fail(c, SEI_ERR_UNSUPPORTED, "viscoelastic kernels are built for orders 4 and 5");
+  if (!(qp > 0) || !(qs > 0) || !(freq_central > 0) || !(freq_ratio > 1)) return fail(c, SEI_ERR_ARG, "Qp, Qs, fc > 0, ratio > 1");
+  const int64_t n = c->mesh.n;
+  sei::HostMesh um = c->mesh;  // unrelaxed moduli
+  std::vector<float> theta((size_t)n * 9);
+  double om[3] = {0, 0, 0};
+  for (int64_t i = 0; i < n; ++i) {
+    double mu = um.material[i * 3 + 1], lam = um.material[i * 3 + 2], th[3][3];
+    sei::fitAttenuation(qp, qs, freq_central, freq_ratio, mu, lam, om, th);
+    um.material[i * 3 + 1] = mu;
+    um.material[i * 3 + 2] = lam;
+    for (int m = 0; m < 3; ++m)
+      for (int k = 0; k < 3; ++k) theta[i * 9 + m * 3 + k] = (float)th[m][k];
+  }
+  std::vector<float> grad, wp, wm;
+  try {
+    sei::buildOperators(um, c->h_star, c->h_aplus, c->h_aminus);
+    sei::buildViscoOperators(um, grad, wp, wm);
+  } catch (const std::exception& e) {
+    return fail(c, SEI_ERR_ARG, e.what());
+  }
+  c->h_grad = grad;
+  c->h_theta = theta;
+  c->h_wplus = wp;
+  c->h_wminus = wm;
+  for (int m = 0; m < 3; ++m) c->omega[m] = (float)om[m];
+  if (host) {  // host-only context: the operators only
+    c->nq = 27;
+    c->visco = true;
+    return SEI_OK;
+  }
+  rc = uploadCells(c, n, c->h_star.data(), c->h_aplus.data(), c->h_aminus.data(), c->mesh.nbr.data(),
+                   c->mesh.side.data(), c->mesh.orient.data(), c->mesh.ftype.data());
+  if (rc) return rc;
+  auto up = [&](float** d, const std::vector<float>& h) -> int {
+    if (cudaMalloc(d, h.size() * sizeof(float)) != cudaSuccess) return fail(c, SEI_ERR_OOM, "viscoelastic arrays");
+    SEI_CUDA(cudaMemcpy(*d, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+    return SEI_OK;
+  };
+  if ((rc = up(&c->d_grad, grad)) || (rc = up(&c->d_theta, theta)) || (rc = up(&c->d_wplus, wp)) ||
+      (rc = up(&c->d_wminus, wm)))
+    return rc;
+  // Q and I with 27 quantities: the elastic DOFs move over, the memory variables start at zero
+  const size_t blk9 = (size_t)9 * c->Bp, blk27 = (size_t)27 * c->Bp;
+  std::vector<float> q9((size_t)n * blk9), q27((size_t)n * blk27, 0.f);
+  SEI_CUDA(cudaStreamSynchronize(c->stream));
+  SEI_CUDA(cudaMemcpy(q9.data(), c->Q, q9.size() * sizeof(float), cudaMemcpyDeviceToHost));
+  for (int64_t i = 0; i < n; ++i) std::memcpy(&q27[i * blk27], &q9[i * blk9], blk9 * sizeof(float));
+  cudaFree(c->Q);
+  cudaFree(c->I);
+  c->Q = c->I = nullptr;
+  if (cudaMalloc(&c->Q, q27.size() * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&c->I, q27.size() * sizeof(float)) != cudaSuccess)
+    return fail(c, SEI_ERR_OOM, "viscoelastic DOF arrays");
+  SEI_CUDA(cudaMemcpy(c->Q, q27.data(), q27.size() * sizeof(float), cudaMemcpyHostToDevice));
+  SEI_CUDA(cudaMemset(c->I, 0, q27.size() * sizeof(float)));
+  for (int m = 0; m < 3; ++m) c->omega[m] = (float)om[m];
+  c->vk = vk;
+  c->nq = 27;
+  c->visco = true;
+  return SEI_OK;
+}
+
+int sei_num_quantities(const sei_ctx* c) { return c ? c->nq : 0; }
+
+int sei_visco_operators(sei_ctx* c, float* grad, float* theta, float* wplus, float* wminus, double* omega) {
+  if (!c) return SEI_ERR_ARG;
+  if (!c->visco) return fail(c, SEI_ERR_STATE, "viscoelastic set-up not done");
+  auto cp = [](float* dst, const std::vector<float>& src) {
+    if (dst) std::memcpy(dst, src.data(), src.size() * sizeof(float));
+  };
+  cp(grad, c->h_grad);
+  cp(theta, c->h_theta);
+  cp(wplus, c->h_wplus);
+  cp(wminus, c->h_wminus);
+  if (omega)
+    for (int m = 0; m < 3; ++m) omega[m] = c->omega[m];
+  return SEI_OK;
+}
+
+int sei_fit_attenuation(double qp, double qs, double freq_central, double freq_ratio, double* mu, double* lam,
+                        double* omega, double* theta) {
+  if (!mu || !lam || !omega || !theta || !(qp > 0) || !(qs > 0) || !(freq_central > 0) || !(freq_ratio > 1))
+    return SEI_ERR_ARG;
+  double th[3][3];
+  sei::fitAttenuation(qp, qs, freq_central, freq_ratio, *mu, *lam, omega, th);
+  for (int m = 0; m < 3; ++m)
+    for (int k = 0; k < 3; ++k) theta[m * 3 + k] = th[m][k];
+  return SEI_OK;
+}
+
 int sei_lts_setup(sei_ctx* c, double cfl, int max_clusters, int* nclusters) {
   int rc = checkReady(c);
   if (rc) return rc;
+  if (c->visco) return fail(c, SEI_ERR_UNSUPPORTED, "local time stepping of the viscoelastic equations is not built");
   if (!c->has_mesh) return fail(c, SEI_ERR_STATE, "local time stepping needs a mesh built by the context");
   if (c->has_fault) return fail(c, SEI_ERR_UNSUPPORTED, "local time stepping with a fault is not built");
   if (c->lts) return fail(c, SEI_ERR_STATE, "local time stepping is already set up");

@@ -7,6 +7,11 @@ struct SeiCoeffs {
   float c[8];
 };
 
+// Relaxation frequencies of the viscoelastic mechanisms (kernel argument).
+struct SeiOmega {
+  float w[3];
+};
+
 // Column of N floats starting at a 16-byte aligned address (N % 4 == 0) or any address.
 template <int N>
 __device__ __forceinline__ void sei_load_col(const float* __restrict__ p, float (&v)[N]) {

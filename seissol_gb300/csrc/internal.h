@@ -39,6 +39,15 @@ double cflTimestep(const HostMesh& m, int order, double cfl);
 void cellTimesteps(const HostMesh& m, int order, double cfl, std::vector<double>& dt);
 // Reorders the cells: new cell i is old cell order[i]; face relations are recomputed.
 void permuteCells(HostMesh& m, const std::vector<int64_t>& order);
+
+// Viscoelastic attenuation (3 mechanisms): relaxed mu, lambda in, unrelaxed out (Attenuation.h).
+constexpr int kMechanisms = 3;
+void fitAttenuation(double qp, double qs, double freqCentral, double freqRatio, double& mu, double& lam,
+                    double omega[kMechanisms], double theta[kMechanisms][3]);
+// Per cell: grad [n][3][3] (d xi_e / d x), and the 9 x 6 memory-variable flux blocks W+, W-
+// [n][4][9 + 9 j] (memory variable j of mechanism l receives omega_l W).
+void buildViscoOperators(const HostMesh& m, std::vector<float>& grad, std::vector<float>& wplus,
+                         std::vector<float>& wminus);
 void seedDofs(int64_t n, int order, uint64_t seed, std::vector<float>& dofs);
 
 // Kernel launchers (one translation unit per order).
@@ -79,6 +88,30 @@ struct OrderKernels {
 int launchLtsBuffer(int m, const int32_t* cell, const int32_t* dst, float* pool, int blk, int reset, void* stream);
 
 bool kernelsForOrder(int order, OrderKernels& out);
+
+// Viscoelastic (27 quantities) device arrays; Q, I [n][27][Bp].
+struct ViscoArrays {
+  int n;
+  float* Q;
+  float* I;
+  const float* star_nz;  // [n][3][24] elastic star non-zeros with the unrelaxed moduli
+  const float* grad;     // [n][3][3]
+  const float* theta;    // [n][3][3]
+  const float* aplus;    // [n][4][81] elastic block
+  const float* wplus;    // [n][4][54] memory block per unit omega
+  const float* aminus;
+  const float* wminus;
+  const int32_t* nbr;
+  const uint8_t* rel;
+  const uint8_t* ftype;
+  float omega[3];
+};
+struct ViscoKernels {
+  int (*ader)(const ViscoArrays&, const float* coeffs, void* stream);
+  int (*lint)(const ViscoArrays&, void* stream);
+  int (*neighbor)(const ViscoArrays&, void* stream);
+};
+bool viscoKernelsForOrder(int order, ViscoKernels& out);
 
 }  // namespace sei
 

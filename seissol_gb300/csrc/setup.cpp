@@ -374,6 +374,137 @@ void buildOperators(const HostMesh& m, std::vector<float>& star, std::vector<flo
   }
 }
 
+void fitAttenuation(double qp, double qs, double freqCentral, double freqRatio, double& mu, double& lam,
+                    double omega[kMechanisms], double theta[kMechanisms][3]) {
+  // Attenuation.h:24-104: kMax = 2 L - 1 frequencies log-spaced over the band; least-squares
+  // weights alpha (P) and beta (S); unrelaxed moduli from the phase at the central frequency.
+  constexpr int L = kMechanisms, K = 2 * kMechanisms - 1;
+  const double pi = 3.14159265358979323846;
+  const double w0 = 2 * pi * freqCentral, wmin = w0 / std::sqrt(freqRatio);
+  double w[K];
+  for (int i = 0; i < K; ++i) w[i] = std::exp(std::log(wmin) + (double)i / (K - 1) * std::log(freqRatio));
+  for (int i = 0; i < L; ++i) omega[i] = w[2 * i];
+  auto lsq = [&](double q, double* x) {
+    // columns a_j(i) = (w_2j w_i + w_2j^2 / q) / (w_2j^2 + w_i^2); solve min |A x - 1/q| by Gram-Schmidt QR
+    double a[L][K], r[L][L] = {}, b[K];
+    for (int i = 0; i < K; ++i) b[i] = 1.0 / q;
+    for (int j = 0; j < L; ++j)
+      for (int i = 0; i < K; ++i) {
+        const double wj = w[2 * j];
+        a[j][i] = (wj * w[i] + wj * wj / q) / (wj * wj + w[i] * w[i]);
+      }
+    for (int j = 0; j < L; ++j) {
+      for (int p = 0; p < j; ++p) {
+        double d = 0;
+        for (int i = 0; i < K; ++i) d += a[p][i] * a[j][i];
+        r[p][j] = d;
+        for (int i = 0; i < K; ++i) a[j][i] -= d * a[p][i];
+      }
+      double nrm = 0;
+      for (int i = 0; i < K; ++i) nrm += a[j][i] * a[j][i];
+      nrm = std::sqrt(nrm);
+      r[j][j] = nrm;
+      for (int i = 0; i < K; ++i) a[j][i] /= nrm;
+    }
+    double y[L];
+    for (int j = 0; j < L; ++j) {
+      double d = 0;
+      for (int i = 0; i < K; ++i) d += a[j][i] * b[i];
+      y[j] = d;
+    }
+    for (int j = L - 1; j >= 0; --j) {
+      double s = y[j];
+      for (int p = j + 1; p < L; ++p) s -= r[j][p] * x[p];
+      x[j] = s / r[j][j];
+    }
+  };
+  double alpha[L], beta[L];
+  lsq(qp, alpha);
+  lsq(qs, beta);
+  double p1 = 1, p2 = 0, s1 = 1, s2 = 0;
+  for (int i = 0; i < L; ++i) {
+    const double r = w0 / w[2 * i], d = 1 + r * r;
+    p1 -= alpha[i] / d;
+    p2 += alpha[i] * r / d;
+    s1 -= beta[i] / d;
+    s2 += beta[i] * r / d;
+  }
+  const double rp = std::sqrt(p1 * p1 + p2 * p2), rs = std::sqrt(s1 * s1 + s2 * s2);
+  const double varP = (lam + 2 * mu) * (rp + p1) / (2 * rp * rp);
+  const double varMu = mu * (rs + s1) / (2 * rs * rs);
+  for (int i = 0; i < L; ++i) {
+    const double t1 = -varP * alpha[i], t2 = -2.0 * varMu * beta[i];
+    theta[i][0] = t1;
+    theta[i][1] = t1 - t2;
+    theta[i][2] = t2;
+  }
+  mu = varMu;
+  lam = varP - 2 * varMu;
+}
+
+void buildViscoOperators(const HostMesh& m, std::vector<float>& grad, std::vector<float>& wplus,
+                         std::vector<float>& wminus) {
+  // The memory variables of mechanism l couple to the velocities through -omega_l C_x
+  // (ViscoelasticSetup.h:26-48 with omega = 1) and receive the flux omega_l W, with
+  // W[i][j] = s sum_k Tinv(k, i) sum_l (Qgod C_0)(k, l) T6(j, l) (aderdg.py:226-246; T6 the
+  // stress block of T, which also rotates every mechanism's memory variables).
+  grad.assign(m.n * 9, 0.f);
+  wplus.assign(m.n * 4 * 54, 0.f);
+  wminus.assign(m.n * 4 * 54, 0.f);
+#pragma omp parallel for schedule(static)
+  for (int64_t c = 0; c < m.n; ++c) {
+    const double* mat = &m.material[c * 3];
+    Vec3 v[4];
+    for (int k = 0; k < 4; ++k) v[k] = {m.coords[c * 12 + k * 3], m.coords[c * 12 + k * 3 + 1], m.coords[c * 12 + k * 3 + 2]};
+    const Vec3 e1 = sub(v[1], v[0]), e2 = sub(v[2], v[0]), e3 = sub(v[3], v[0]);
+    const double det = dot(e1, cross(e2, e3));
+    const Vec3 g[3] = {scale(cross(e2, e3), 1.0 / det), scale(cross(e3, e1), 1.0 / det),
+                       scale(cross(e1, e2), 1.0 / det)};
+    for (int e = 0; e < 3; ++e)
+      for (int x = 0; x < 3; ++x) grad[c * 9 + e * 3 + x] = (float)g[e][x];
+    const double volume = std::fabs(det) / 6.0;
+    for (int f = 0; f < 4; ++f) {
+      const Vec3 a = v[kFace2Nodes[f][0]], b = v[kFace2Nodes[f][1]], cc = v[kFace2Nodes[f][2]];
+      Vec3 nrm = cross(sub(b, a), sub(cc, a));
+      const double area = 0.5 * norm(nrm);
+      Vec3 t1 = sub(b, a);
+      Vec3 t2 = cross(nrm, t1);
+      nrm = scale(nrm, 1.0 / norm(nrm));
+      t1 = scale(t1, 1.0 / norm(t1));
+      t2 = scale(t2, 1.0 / norm(t2));
+      const int32_t nb = m.nbr[c * 4 + f];
+      const double* nmat = nb >= 0 ? &m.material[(int64_t)nb * 3] : mat;
+      Mat9 qgl, qgn, T, Ti;
+      godunovState(mat, nmat, qgl, qgn);
+      rotation(nrm, t1, t2, T, Ti);
+      const double fs = -2.0 * area / (6.0 * volume);
+      const bool dr = m.ftype[c * 4 + f] == 1;
+      for (int side = 0; side < 2; ++side) {
+        const Mat9& qg = side == 0 ? qgl : qgn;
+        const double s = side == 0 && dr ? 0.0 : fs;
+        float* out = (side == 0 ? wplus : wminus).data() + (c * 4 + f) * 54;
+        // G(k, l) = sum_q Qgod(k, q) C_0(q, l): C_0(6, 0) = -1, C_0(7, 3) = C_0(8, 5) = -1/2
+        double G[9][6] = {};
+        for (int k = 0; k < 9; ++k) {
+          G[k][0] = -qg[k * 9 + 6];
+          G[k][3] = -0.5 * qg[k * 9 + 7];
+          G[k][5] = -0.5 * qg[k * 9 + 8];
+        }
+        for (int i = 0; i < 9; ++i)
+          for (int j = 0; j < 6; ++j) {
+            double acc = 0;
+            for (int k = 0; k < 9; ++k) {
+              double t = 0;
+              for (int l = 0; l < 6; ++l) t += G[k][l] * T[j * 9 + l];
+              acc += Ti[k * 9 + i] * t;
+            }
+            out[i + 9 * j] = (float)(s * acc);
+          }
+      }
+    }
+  }
+}
+
 double cflTimestep(const HostMesh& m, int order, double cfl) {
   std::vector<double> dt;
   cellTimesteps(m, order, cfl, dt);

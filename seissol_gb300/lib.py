@@ -123,6 +123,10 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_dr_get_slots", i, [VP, VP])
     _sig(lib, "sei_kernel_times_ms", i, [VP, C.POINTER(d), C.POINTER(d), C.POINTER(i)])
     _sig(lib, "sei_kernel_times_by_kind", i, [VP, VP, VP])
+    _sig(lib, "sei_visco_setup", i, [VP, d, d, d, d])
+    _sig(lib, "sei_num_quantities", i, [VP])
+    _sig(lib, "sei_visco_operators", i, [VP, VP, VP, VP, VP, VP])
+    _sig(lib, "sei_fit_attenuation", i, [d, d, d, d, C.POINTER(d), C.POINTER(d), VP, VP])
     _sig(lib, "sei_lts_setup", i, [VP, d, i, C.POINTER(i)])
     _sig(lib, "sei_lts_run", i, [VP, i])
     _sig(lib, "sei_lts_clusters", i, [VP, C.POINTER(i), VP, VP])
@@ -174,6 +178,17 @@ def tc_gemm_check(A, B, terms=3):
     return D
 
 
+def fit_attenuation(mu, lam, qp, qs, freq_central, freq_ratio):
+    """(unrelaxed mu, lambda, omega [3], theta [3][3]) of the library's attenuation fit."""
+    lib = load_library()
+    m, l = C.c_double(mu), C.c_double(lam)
+    om, th = np.empty(3), np.empty(9)
+    rc = lib.sei_fit_attenuation(qp, qs, freq_central, freq_ratio, C.byref(m), C.byref(l), _ptr(om), _ptr(th))
+    if rc != SEI_OK:
+        raise SeiError(rc, "sei_fit_attenuation")
+    return m.value, l.value, om, th.reshape(3, 3)
+
+
 def mlp_num_params():
     return load_library().sei_mlp_num_params()
 
@@ -212,6 +227,7 @@ class Context:
         self.lib = load_library()
         self.order = order
         self.B = nbasis(order)
+        self.nq = 9
         cfg = _Config(order, device, precision, int(store_derivatives))
         h = VP()
         rc = self.lib.sei_create(C.byref(cfg), C.byref(h))
@@ -289,16 +305,16 @@ class Context:
     # -- data ---------------------------------------------------------------------------
     def set_dofs(self, dofs):
         a = np.ascontiguousarray(dofs, np.float32)
-        assert a.shape == (self.n, 9, self.B), a.shape
+        assert a.shape == (self.n, self.nq, self.B), a.shape
         self._check(self.lib.sei_set_dofs(self.h, _ptr(a)), "sei_set_dofs")
 
     def get_dofs(self):
-        a = np.empty((self.n, 9, self.B), np.float32)
+        a = np.empty((self.n, self.nq, self.B), np.float32)
         self._check(self.lib.sei_get_dofs(self.h, _ptr(a)), "sei_get_dofs")
         return a
 
     def get_time_integrated(self):
-        a = np.empty((self.n, 9, self.B), np.float32)
+        a = np.empty((self.n, self.nq, self.B), np.float32)
         self._check(self.lib.sei_get_time_integrated(self.h, _ptr(a)), "sei_get_time_integrated")
         return a
 
@@ -426,6 +442,21 @@ class Context:
 
     def dr_warm_start(self, on=True):
         self._check(self.lib.sei_dr_warm_start(self.h, int(on)), "sei_dr_warm_start")
+
+    def visco_setup(self, qp=100.0, qs=50.0, freq_central=0.5, freq_ratio=100.0):
+        """Viscoelastic equations, 3 mechanisms: the DOFs become [n][27][B]."""
+        self._check(self.lib.sei_visco_setup(self.h, qp, qs, freq_central, freq_ratio), "sei_visco_setup")
+        self.nq = self.lib.sei_num_quantities(self.h)
+
+    def visco_operators(self):
+        """grad [n][3][3], theta [n][3][3], W+ and W- [n][4][9][6], omega [3]."""
+        n = self.n
+        g, t = np.empty((n, 3, 3), np.float32), np.empty((n, 3, 3), np.float32)
+        wp, wm = np.empty((n, 4, 6, 9), np.float32), np.empty((n, 4, 6, 9), np.float32)
+        om = np.empty(3, np.float64)
+        self._check(self.lib.sei_visco_operators(self.h, _ptr(g), _ptr(t), _ptr(wp), _ptr(wm), _ptr(om)),
+                    "sei_visco_operators")
+        return g, t, np.swapaxes(wp, -1, -2), np.swapaxes(wm, -1, -2), om
 
     def lts_setup(self, cfl=0.5, max_clusters=8):
         """Rate-2 local time stepping; reorders the cells by cluster.  Returns the cluster count."""

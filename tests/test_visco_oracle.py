@@ -91,3 +91,38 @@ def test_without_coupling_elastic_part_is_elastic_oracle(built_lib):
                                         cells["orient"], dt, 2, cells["face_type"])
     assert np.abs(out[:, :9] - ref).max() <= 1e-12 * np.abs(ref).max()
     assert np.abs(out[:, 9:]).max() == 0.0
+
+
+def test_library_attenuation_fit_known_answer(built_lib):
+    from seissol_gb300 import fit_attenuation
+    a = ATT_IN
+    mu, lam, omega, theta = fit_attenuation(a["mu"], a["lam"], a["qp"], a["qs"], a["fc"], a["ratio"])
+    assert mu == pytest.approx(ATT_OUT["mu"], rel=1e-12)
+    assert lam == pytest.approx(ATT_OUT["lam"], rel=1e-12)
+    assert np.allclose(omega, ATT_OUT["omega"], rtol=1e-12)
+    assert np.allclose(theta, ATT_OUT["theta"], rtol=1e-11)
+
+
+def test_library_visco_operators_match_oracle(built_lib):
+    """The product's host set-up (host-only context) against the dense oracle operators: the
+    unrelaxed elastic blocks, the memory-variable flux blocks W (= oracle flux column / omega),
+    the gradients and theta; float32 storage, relative 1e-6."""
+    from seissol_gb300 import Context
+    with Context(4, device=-1) as ctx:
+        ctx.build_periodic_cube(4, 4, 4, perturb=0.1, seed=7)
+        coords, material, _ = ctx.get_geometry()
+        ctx.visco_setup(100.0, 50.0, 0.5, 100.0)
+        cells = ctx.get_cells()
+        grad, theta, wp, wm, omega = ctx.visco_operators()
+    mats, om, thetas = _visco_material(material)
+    assert np.allclose(omega, om, rtol=1e-7)  # stored as float (kernel argument)
+    assert np.allclose(theta, thetas, rtol=1e-6)
+    ops = visco.cell_operators(coords, mats, om, thetas, cells["neighbor"])
+    close = lambda a, b: np.abs(a - b).max() <= 1e-6 * np.abs(b).max()
+    assert close(cells["star"], ops["star"][:, :, :9, :9])
+    assert close(cells["AplusT"], ops["AplusT"][:, :, :9, :9])
+    assert close(cells["AminusT"], ops["AminusT"][:, :, :9, :9])
+    assert close(wp, ops["AplusT"][:, :, :9, 9:15] / om[0])
+    assert close(wm, ops["AminusT"][:, :, :9, 9:15] / om[0])
+    ref_grad = np.stack([np.array(dg_setup.reference_jacobian(*coords[c].T)) for c in range(coords.shape[0])])
+    assert close(grad, ref_grad)
