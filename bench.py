@@ -277,6 +277,53 @@ def lts_measurement(local, cycles):
             / out["global_stepping"]["simulated_s_per_wall_s"]}
 
 
+def visco_bytes_per_cell(kind):
+    """Algorithmic bytes per cell of the viscoelastic O5 launches (float32, 27 x 36 per DOF block)."""
+    dof = 4 * 27 * 36
+    el = 4 * 9 * 36
+    small = 4 * (72 + 9 + 9)  # star non-zeros, gradients, theta
+    if kind == "ader":  # read Q, write I
+        return 2 * dof + small
+    if kind == "lint":  # read Q, write Q, read I, A+ and W+ of 4 faces, face types
+        return 3 * dof + small + 4 * 4 * (81 + 54) + 4
+    if kind == "neighbor":  # read Q, write Q, elastic columns of the neighbours' I, A- and W-
+        return 2 * dof + el + 4 * 4 * (81 + 54) + 16 + 4 + 4
+    raise ValueError(kind)
+
+
+def visco_measurement(local, steps):
+    """Viscoelastic equations (3 mechanisms, 27 quantities), order 5, 196,520 tets (34^3 cubes of 5
+    tets, edge 100 m, material +-10 %), Qp 100, Qs 50, central frequency 0.5 Hz, ratio 100, kernel
+    all, CFL 0.5 (the equations and order of the viscoelastic configuration, on global time steps)."""
+    from seissol_gb300 import Context
+
+    hbm, _ = peaks()
+    ctx = Context(5, device=local)
+    n = ctx.build_periodic_cube(34, 34, 34, perturb=PERTURB, seed=SEED)
+    ctx.visco_setup(100.0, 50.0, 0.5, 100.0)
+    dt = ctx.cfl_timestep(0.5)
+    ctx.run("all", dt, 3)
+    ctx.sync()
+    ctx.run("all", dt, steps)
+    ctx.sync()
+    ms = ctx.last_run_ms()
+    ctx.set_profiling(True)
+    ctx.run("all", dt, steps)
+    ctx.sync()
+    by_kind = ctx.kernel_times_by_kind()
+    ctx.set_profiling(False)
+    ctx.close()
+    kern = {k: v[0] / v[1] for k, v in by_kind.items() if k in ("ader", "lint", "neighbor") and v[1] > 0}
+    roof = {k: {"ms": t, "algorithmic_gbs": visco_bytes_per_cell(k) * n / (t / 1e3) / 1e9,
+                "frac_of_measured_hbm": visco_bytes_per_cell(k) * n / (t / 1e3) / 1e9 / hbm} for k, t in kern.items()}
+    return {"workload": "viscoelastic order 5 (35x27, 3 mechanisms), 196,520-tet periodic cube 34^3 cubes x 5 tets, "
+                        "material +-10%, Qp 100, Qs 50, fc 0.5 Hz, ratio 100, kernel all, GTS, CFL 0.5",
+            "cells": n, "steps": steps, "ms_per_step": ms / steps, "cell_updates_per_s": n * steps / (ms / 1e3),
+            "kernels": roof,
+            "step_model_bytes_per_cell": 23744,
+            "step_model_frac": n * steps / (ms / 1e3) * 23744 / (hbm * 1e9)}
+
+
 def dr_measurement(local, steps):
     """Dynamic rupture on the fault workload: elastic order 4, 300,000 tets, a planar fault of
     20,000 faces (25 points each), fast-velocity-weakening friction with a ~ U[0.008, 0.02],
@@ -444,6 +491,9 @@ def run_ours(args, world, rank, local):
     lts = None
     if rank == 0 and args.lts_cycles > 0:
         lts = lts_measurement(local, args.lts_cycles)
+    vis = None
+    if rank == 0 and args.visco_steps > 0:
+        vis = visco_measurement(local, args.visco_steps)
 
     base = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -459,7 +509,7 @@ def run_ours(args, world, rank, local):
                            "parallelism": f"replicas x{world}"},
                 "roofline": roof, "cpu_baseline": base, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": launches, "kernel_ms_per_step": kernels, "dynamic_rupture": dr,
-                "local_time_stepping": lts}
+                "local_time_stepping": lts, "viscoelastic": vis}
         print(json.dumps(line))
     return 0
 
@@ -476,6 +526,8 @@ def main():
     ap.add_argument("--precision", choices=("fp32", "f16x3"), default="fp32")
     ap.add_argument("--dr-steps", type=int, default=20,
                     help="steps of the dynamic-rupture measurement (plain and warm-started); 0 skips it")
+    ap.add_argument("--visco-steps", type=int, default=20,
+                    help="steps of the viscoelastic measurement; 0 skips it")
     ap.add_argument("--lts-cycles", type=int, default=10,
                     help="cycles of the local-time-stepping measurement; 0 skips it")
     args = ap.parse_args()
