@@ -301,7 +301,9 @@ int sei_kernel_times_by_kind(sei_ctx* ctx, double* ms, int* counts);
  * conventions of the library on the current device. */
 int sei_tc_gemm_check(const float* A, const float* B, float* D, int N, int K, int terms);
 
-/* Per-cell, per-step estimate of a proxy kernel (Local.cpp:462-522, Neighbor.cpp:190-228). */
+/* Per-cell, per-step estimate of a proxy kernel (Local.cpp:462-522, Neighbor.cpp:190-228), elastic:
+ * SEI_KERNEL_ALL, LOCAL, ADER, LOCAL_WO_ADER, NEIGHBOR (others SEI_ERR_UNSUPPORTED).  Works on a
+ * host-only context. */
 int sei_metrics(const sei_ctx* ctx, int kernel, sei_perf* out);
 
 #ifdef __cplusplus

@@ -93,6 +93,9 @@ def gen_order(order: int) -> str:
     a(f"namespace sei_o{order} {{")
     a(f"constexpr int kOrder = {order}, kB = {B}, kBp = {padded(B)}, kF = {F}, kQ = 9, kCPB = {CPB};")
     a(f"constexpr int kDerivSize = {sum(nb3(order - i) for i in range(order)) * NQ};")
+    fl = nnz_flops(order)
+    a(f"// Non-zero flops per cell of the ADER, local-integral and neighbour kernels (literal FFMAs and premixes).")
+    a(f"constexpr double kFlopAder = {fl['ader']:.1f}, kFlopLocal = {fl['local']:.1f}, kFlopNeighbor = {fl['neighbor']:.1f};")
     a("__constant__ int c_src[9][3] = {" + ",".join("{" + ",".join(map(str, s)) + "}" for s in src) + "};")
     a("__constant__ int c_nzi[9][3] = {" + ",".join("{" + ",".join(map(str, s)) + "}" for s in idx) + "};")
 

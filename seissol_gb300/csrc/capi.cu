@@ -1592,9 +1592,25 @@ int sei_kernel_times_by_kind(sei_ctx* c, double* ms, int* counts) {
 
 int sei_metrics(const sei_ctx* c, int kernel, sei_perf* out) {
   if (!c || !out) return SEI_ERR_ARG;
-  (void)kernel;
   std::memset(out, 0, sizeof(*out));
-  return SEI_ERR_UNSUPPORTED;
+  if (c->visco) return SEI_ERR_UNSUPPORTED;
+  // per cell: the generated kernels execute exactly their non-zero flops (hardware = non-zero);
+  // bytes: compulsory float32 traffic, every array touched once (DOF blocks 9 x Bp)
+  const double dof = 4.0 * 9 * c->Bp, star = 4.0 * 72, flux = 4.0 * 4 * 81, rel = 4.0 * 4 + 4 + 4;
+  const double fa = c->k.flopAder, fl = c->k.flopLocal, fn = c->k.flopNeighbor;
+  double flop = 0, bytes = 0;
+  switch (kernel) {
+    case SEI_KERNEL_ALL: flop = fa + fl + fn; bytes = 4 * dof + star + 2 * flux + 4.0 * 4 + 4; break;
+    case SEI_KERNEL_LOCAL: flop = fa + fl; bytes = 3 * dof + star + flux + 4; break;
+    case SEI_KERNEL_ADER: flop = fa; bytes = 2 * dof + star; break;
+    case SEI_KERNEL_LOCAL_WO_ADER: flop = fl; bytes = 3 * dof + star + flux + 4; break;
+    case SEI_KERNEL_NEIGHBOR: flop = fn; bytes = 3 * dof + flux + rel; break;
+    default: return SEI_ERR_UNSUPPORTED;
+  }
+  out->nonzero_flop = flop;
+  out->hardware_flop = flop;
+  out->bytes = bytes;
+  return SEI_OK;
 }
 
 }  // extern "C"

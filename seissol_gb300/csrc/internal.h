@@ -81,6 +81,7 @@ struct OrderKernels {
   LaunchLocalFn ader;         // ADER alone (writes I, optional derivatives)
   LaunchLintFn lint;          // volume + local flux from I
   LaunchTaylorGatherFn taylorGather;
+  double flopAder, flopLocal, flopNeighbor;  // non-zero flops per cell
 };
 
 // pool[dst[e]] = (reset ? 0 : pool[dst[e]]) + pool[cell[e]] for e < m, blocks of blk floats

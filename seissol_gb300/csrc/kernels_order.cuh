@@ -86,6 +86,7 @@ int launchTaylorGather(int m, const int32_t* src, const int32_t* dst, const floa
 
 namespace sei {
 OrderKernels SEI_CAT(orderKernels, SEI_ORDER)() {
-  return OrderKernels{launchLocal, launchNeighbor, launchTaylor, launchAder, launchLint, launchTaylorGather};
+  return OrderKernels{launchLocal, launchNeighbor, launchTaylor, launchAder, launchLint, launchTaylorGather,
+                      K::kFlopAder, K::kFlopLocal, K::kFlopNeighbor};
 }
 }  // namespace sei

@@ -86,3 +86,26 @@ def test_invalid_arguments_are_errors(built_lib):
     with pytest.raises(SeiError, match="SEI_ERR_UNSUPPORTED"):
         from seissol_gb300 import Context
         Context(3, device=-1)
+
+
+def test_metrics_per_kernel(built_lib):
+    """sei_metrics: non-zero flops of the generated kernels and compulsory bytes per cell and step
+    (order 6: 10,964 B for kernel all, the step model of the elastic configuration)."""
+    import ctypes as C
+    from seissol_gb300 import Context, KERNELS
+    from seissol_gb300.lib import _Perf
+    from seissol_gb300.codegen.gen_kernels import nnz_flops
+    f = nnz_flops(6)
+    with Context(6, device=-1) as ctx:
+        out = {}
+        for name in ("all", "local", "ader", "localwoader", "neigh"):
+            p = _Perf()
+            assert ctx.lib.sei_metrics(ctx.h, KERNELS[name], C.byref(p)) == 0
+            out[name] = (p.nonzero_flop, p.hardware_flop, p.bytes)
+        p = _Perf()
+        assert ctx.lib.sei_metrics(ctx.h, KERNELS["all_dr"], C.byref(p)) != 0
+    assert out["all"][0] == pytest.approx(f["ader"] + f["local"] + f["neighbor"])
+    assert out["local"][0] == pytest.approx(f["ader"] + f["local"])
+    assert out["neigh"][0] == pytest.approx(f["neighbor"])
+    assert out["all"][2] == 10964
+    assert out["ader"][2] == 2 * 2016 + 288
