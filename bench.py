@@ -398,6 +398,8 @@ def kname(kind, args):
     """Name of the CUDA kernel behind a launch kind of the step."""
     if kind == "lint" and args.precision == "f16x3":
         return f"sei_lint_tc<{ORDER}>"
+    if kind == "neighbor" and args.precision == "f16x3":
+        return f"sei_nb_tc<{ORDER}>"
     return f"sei_{kind}_o{ORDER}"
 
 

@@ -43,6 +43,8 @@ def _deps(src):
     base = os.path.basename(src)
     if base.startswith("kernels_"):
         deps.append(os.path.join(GEN, base.replace(".cu", ".cuh")))
+    if base.startswith("tc_"):
+        deps += [os.path.join(GEN, f"{n}_o{o}.cuh") for n in ("tc_tables", "tc_nb") for o in ORDERS]
     return deps
 
 

@@ -513,14 +513,43 @@ def gen_tc_tables(order: int) -> str:
     return "\n".join(L) + "\n"
 
 
+def gen_tc_nb(order: int) -> str:
+    """Face-trace map of the tensor-core neighbour kernel: S = fP_h diag(fM)^-1 T.
+
+    The local integral stores the traces T_j = fMrT_j I = diag(fM) rT_j I of every face
+    (fM, the face mass matrix, is diagonal), so the neighbour chain fP_h rT_j I_nb
+    (codegen/kernels/aderdg.py:414-428) becomes fP_h diag(fM)^-1 T_j(nb).
+    """
+    F = nb2(order)
+    G = global_matrices(order)
+    fm = np.asarray(G["fM"], dtype=float)
+    L = [f"// Generated by seissol_gb300/codegen/gen_kernels.py: neighbour face-trace map, order {order}.",
+         "// Do not edit.", "#pragma once", f"namespace sei_tcnb_o{order} {{",
+         f"constexpr int kF = {F}, kFP = {padded(F)};",
+         "// s = fP_h diag(fM)^-1 t (orientation h; t: one quantity row of a stored face trace).",
+         "__device__ __forceinline__ void applyFp(int h, const float (&t)[kFP], float (&s)[kF]) {",
+         "  switch (h) {"]
+    for h in range(3):
+        M = np.asarray(G["fP"][h], dtype=float) / fm[None, :]
+        L.append(f"    {'default' if h == 2 else 'case ' + str(h)}: {{")
+        _matvec(L, "      ", M, "t", "s", F, F, True)
+        L.append("      break;")
+        L.append("    }")
+    L.append("  }")
+    L.append("}")
+    L.append(f"}}  // namespace sei_tcnb_o{order}")
+    return "\n".join(L) + "\n"
+
+
 def write_tc_tables(outdir: str, orders=(4, 5, 6)) -> list:
     os.makedirs(outdir, exist_ok=True)
     paths = []
     for o in orders:
-        p = os.path.join(outdir, f"tc_tables_o{o}.cuh")
-        src = gen_tc_tables(o)
-        if not os.path.exists(p) or open(p).read() != src:
-            with open(p, "w") as fh:
-                fh.write(src)
-        paths.append(p)
+        for name, gen in (("tc_tables", gen_tc_tables), ("tc_nb", gen_tc_nb)):
+            p = os.path.join(outdir, f"{name}_o{o}.cuh")
+            src = gen(o)
+            if not os.path.exists(p) or open(p).read() != src:
+                with open(p, "w") as fh:
+                    fh.write(src)
+            paths.append(p)
     return paths

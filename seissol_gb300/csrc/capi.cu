@@ -75,6 +75,10 @@ struct sei_ctx {
   bool fused_local = false;  // SEI_OPT_FUSED_LOCAL: ADER and local integral in one launch
   int sms = 0;               // multiprocessors of the device (persistent tensor-core grids)
   int* d_status = nullptr;   // device error word: 1 = a bounded wait in a kernel gave up
+  // tensor-core path (SEI_PREC_F16X3): face traces fMrT_f I of every cell, written by the local
+  // integral and read by the neighbour kernel; valid while I has not changed since
+  float* d_trace = nullptr;
+  bool trace_valid = false;
   std::vector<cudaEvent_t> prof_events;
   std::vector<int> prof_kind;  // kind of the launch starting at event i: 0 ADER (or fused ADER + local),
                                // 1 neighbour, 2 fault, 3 local integral, 4 LTS gather / buffer, -1 end of run
@@ -130,6 +134,9 @@ void freeArrays(sei_ctx* c) {
   cudaFree(c->rel);
   cudaFree(c->ftype);
   cudaFree(c->dslot);
+  cudaFree(c->d_trace);
+  c->d_trace = nullptr;
+  c->trace_valid = false;
   for (void* p : {(void*)c->d_src, (void*)c->d_bcell, (void*)c->d_bdst, (void*)c->d_gsrc, (void*)c->d_gdst,
                   (void*)c->d_grad, (void*)c->d_theta, (void*)c->d_wplus, (void*)c->d_wminus})
     cudaFree(p);
@@ -172,13 +179,16 @@ int allocArrays(sei_ctx* c, int64_t n) {
     ok = alloc((void**)&c->derivs, (size_t)n * sei::derivativesSize(c->cfg.order) * sizeof(float));
     c->nslots = n;
   }
+  const size_t trace_bytes = (size_t)n * sei::traceFloatsPerCell(c->cfg.order) * sizeof(float);
+  if (ok && c->cfg.precision == SEI_PREC_F16X3) ok = alloc((void**)&c->d_trace, trace_bytes);
   if (!ok) {
     cudaGetLastError();
     freeArrays(c);
     return fail(c, SEI_ERR_OOM, "device allocation failed");
   }
   c->n = n;
-  if (cudaMemsetAsync(c->Q, 0, dof, c->stream) != cudaSuccess || cudaMemsetAsync(c->I, 0, dof, c->stream) != cudaSuccess)
+  if (cudaMemsetAsync(c->Q, 0, dof, c->stream) != cudaSuccess || cudaMemsetAsync(c->I, 0, dof, c->stream) != cudaSuccess ||
+      (c->d_trace && cudaMemsetAsync(c->d_trace, 0, trace_bytes, c->stream) != cudaSuccess))
     return fail(c, SEI_ERR_CUDA, "memset failed");
   return SEI_OK;
 }
@@ -250,6 +260,7 @@ int profMark(sei_ctx* c, int kind) {
 int launchAderOnly(sei_ctx* c, const sei::DeviceArrays& d, const float* coeffs) {
   int rc = profMark(c, 0);
   if (rc) return rc;
+  c->trace_valid = false;
   if (c->k.ader(d, coeffs, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "ADER kernel launch failed");
   return SEI_OK;
 }
@@ -258,8 +269,11 @@ int launchLintOnly(sei_ctx* c, const sei::DeviceArrays& d) {
   int rc = profMark(c, 3);
   if (rc) return rc;
   if (c->cfg.precision == SEI_PREC_F16X3) {
-    if (sei::launchLintTensorCore(c->cfg.order, d, c->d_status, c->sms, c->stream) != 0)
+    // the traces cover every cell only outside local time stepping (whose kernels run per cluster)
+    float* trace = c->lts ? nullptr : c->d_trace;
+    if (sei::launchLintTensorCore(c->cfg.order, d, trace, 0, c->d_status, c->sms, c->stream) != 0)
       return fail(c, SEI_ERR_CUDA, "tensor-core local-integral kernel launch failed");
+    c->trace_valid = trace != nullptr;
     return SEI_OK;
   }
   if (c->k.lint(d, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "local-integral kernel launch failed");
@@ -281,6 +295,18 @@ int launchLocal(sei_ctx* c, const sei::DeviceArrays& d, const float* coeffs) {
 int launchNeighbor(sei_ctx* c, const sei::DeviceArrays& d) {
   int rc = profMark(c, 1);
   if (rc) return rc;
+  if (c->cfg.precision == SEI_PREC_F16X3 && !c->lts && c->d_trace) {
+    // tensor-core path: the neighbour flux reads the stored face traces of I; they are
+    // recomputed first when I changed after the last local integral
+    if (!c->trace_valid) {
+      if (sei::launchLintTensorCore(c->cfg.order, d, c->d_trace, 1, c->d_status, c->sms, c->stream) != 0)
+        return fail(c, SEI_ERR_CUDA, "tensor-core trace kernel launch failed");
+      c->trace_valid = true;
+    }
+    if (sei::launchNeighborTensorCore(c->cfg.order, d, c->d_trace, c->d_status, c->sms, c->stream) != 0)
+      return fail(c, SEI_ERR_CUDA, "tensor-core neighbour kernel launch failed");
+    return SEI_OK;
+  }
   if (c->k.neighbor(d, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "neighbour kernel launch failed");
   return SEI_OK;
 }
@@ -1405,6 +1431,7 @@ int sei_lts_setup(sei_ctx* c, double cfl, int max_clusters, int* nclusters) {
   // device: the I pool, derivative slots, tables
   cudaFree(c->I);
   c->I = nullptr;
+  c->trace_valid = false;
   if (cudaMalloc(&c->I, (size_t)(n + nB + nS) * blk * sizeof(float)) != cudaSuccess)
     return fail(c, SEI_ERR_OOM, "LTS pool allocation");
   SEI_CUDA(cudaMemset(c->I, 0, (size_t)(n + nB + nS) * blk * sizeof(float)));

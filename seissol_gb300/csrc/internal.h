@@ -184,9 +184,30 @@ struct TcLintArgs {
   const float* scVol;     // per-row power-of-two scales of the operand tables
   const uint16_t* opRd;
   const float* scRd;
-  int* status;  // set to 1 when a wait gave up
+  float* trace;   // nullable: face traces fMrT_f I out, [n][4][9][FP] (FP = F rounded up to 4)
+  int traceOnly;  // 1: write the traces only (Q unchanged)
+  int* status;    // set to 1 when a wait gave up
 };
-int launchLintTensorCore(int order, const DeviceArrays& d, int* status, int sms, void* stream);
+int launchLintTensorCore(int order, const DeviceArrays& d, float* trace, int traceOnly, int* status, int sms,
+                         void* stream);
+
+// Arguments of the tensor-core neighbour kernel (face traces in, Q updated in place).
+struct TcNbArgs {
+  int n;
+  float* Q;
+  const float* trace;  // [n][4][9][FP] traces fMrT_f I of every cell and face
+  const float* aminus;
+  const int32_t* nbr;
+  const uint8_t* rel;
+  const uint8_t* ftype;
+  const uint16_t* opRd;  // pre-split rDivM stack (B operand), core-matrix layout
+  const float* scRd;
+  int* status;
+};
+int launchNeighborTensorCore(int order, const DeviceArrays& d, const float* trace, int* status, int sms,
+                             void* stream);
+// Floats per cell of the face-trace array of the tensor-core path: 4 faces x 9 quantities x FP.
+inline int traceFloatsPerCell(int order) { return 4 * 9 * ((numFaceBasis(order) + 3) / 4 * 4); }
 }  // namespace sei
 
 namespace sei {

@@ -20,6 +20,9 @@
 #include "_gen/tc_tables_o4.cuh"
 #include "_gen/tc_tables_o5.cuh"
 #include "_gen/tc_tables_o6.cuh"
+#include "_gen/tc_nb_o4.cuh"
+#include "_gen/tc_nb_o5.cuh"
+#include "_gen/tc_nb_o6.cuh"
 
 namespace {
 
@@ -197,7 +200,7 @@ __global__ void __launch_bounds__(128, 1) sei_lint_tc(sei::TcLintArgs A) {
     const float sI = ldexpf(1.f, eI);
     // volume, one star matrix at a time
 #pragma unroll
-    for (int e = 0; e < 3; ++e) {
+    for (int e = 0; e < 3 && !A.traceOnly; ++e) {
       forColumns(tbase, e * B, B, [&](int k, float v) { X[k * 128 + r] = v * sI * __ldg(A.scVol + e * B + k); });
       __syncthreads();
       const float* x0 = X + 9 * c + s0;
@@ -208,8 +211,21 @@ __global__ void __launch_bounds__(128, 1) sei_lint_tc(sei::TcLintArgs A) {
         acc[k] += st[e][0] * x0[k * 128] + st[e][1] * x1[k * 128] + st[e][2] * x2[k * 128];
       __syncthreads();
     }
-    // face traces -> G = traces . AplusT (per face), the A operand of MMA 2
-    forColumns(tbase, 3 * B, 4 * F, [&](int t, float v) { X[t * 128 + r] = v * sI * __ldg(A.scVol + 3 * B + t); });
+    // face traces -> G = traces . AplusT (per face), the A operand of MMA 2; the traces of
+    // every face are also stored for the neighbour kernel of this path
+    constexpr int FP = (F + 3) / 4 * 4;
+    float* trow = (A.trace && valid) ? A.trace + ((size_t)cell * 4 * 9 + q) * FP : nullptr;
+    forColumns(tbase, 3 * B, 4 * F, [&](int t, float v) {
+      const float x = v * sI * __ldg(A.scVol + 3 * B + t);
+      X[t * 128 + r] = x;
+      if (trow) trow[(t / F) * 9 * FP + t % F] = x;
+    });
+    if (A.traceOnly) {
+      sei_tc::fenceBeforeSync();
+      __syncthreads();
+      sei_tc::fenceAfterSync();
+      continue;
+    }
     __syncthreads();
     float G[4 * F];
 #pragma unroll
@@ -250,10 +266,12 @@ __global__ void __launch_bounds__(128, 1) sei_lint_tc(sei::TcLintArgs A) {
 }
 
 template <int ORD>
-int launchLintTc(const sei::DeviceArrays& d, int* status, int sms, void* stream, const void* opVolSym,
-                 const void* scVolSym, const void* opRdSym, const void* scRdSym) {
+int launchLintTc(const sei::DeviceArrays& d, float* trace, int traceOnly, int* status, int sms, void* stream,
+                 const void* opVolSym, const void* scVolSym, const void* opRdSym, const void* scRdSym) {
   using Dm = Dims<ORD>;
   sei::TcLintArgs a{};
+  a.trace = trace;
+  a.traceOnly = traceOnly;
   a.n = d.n;
   a.Q = d.Q;
   a.I = d.I;
@@ -279,21 +297,207 @@ int launchLintTc(const sei::DeviceArrays& d, int* status, int sms, void* stream,
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
+// Face-trace map s = fP_h diag(fM)^-1 t of the given order (generated).
+template <int ORD, int FP, int F>
+__device__ __forceinline__ void applyTraceMap(int h, const float (&t)[FP], float (&s)[F]) {
+  if constexpr (ORD == 4) sei_tcnb_o4::applyFp(h, t, s);
+  if constexpr (ORD == 5) sei_tcnb_o5::applyFp(h, t, s);
+  if constexpr (ORD == 6) sei_tcnb_o6::applyFp(h, t, s);
+}
+
+template <int ORD>
+struct NbDims {
+  static constexpr int B = Dims<ORD>::B, Bp = Dims<ORD>::Bp, F = Dims<ORD>::F;
+  static constexpr int FP = (F + 3) / 4 * 4;
+  static constexpr int K2 = Dims<ORD>::K2, N2 = Dims<ORD>::N2;
+  static constexpr uint32_t kCols = N2 <= 32 ? 32 : (N2 <= 64 ? 64 : 128);
+  static constexpr size_t kOp = (size_t)N2 * K2 * 4;       // rDivM stack, hi + lo
+  static constexpr size_t kX = (size_t)4 * 128 * FP * 4;   // mapped traces, FP32 [face][row][FP]
+  static constexpr size_t kAop = (size_t)128 * K2 * 4;     // A operand, hi + lo (aliases X)
+  static constexpr size_t kSmem = kOp + (kX > kAop ? kX : kAop);
+};
+
+// Neighbour flux (Neighbor::computeNeighborsIntegral, codegen/kernels/aderdg.py:414-428) of a
+// tile of 14 cells from the stored face traces T_f = fMrT_f I of all cells.  Rows of the tile
+// are (cell, quantity) = 9 c + q.  For each regular face i with neighbour nb, side j and
+// orientation h:
+//   thread (c, q):  S_i[q, :] = fP_h diag(fM)^-1 T_j(nb)[q, :]                (CUDA cores, FP32)
+//   thread (c, p):  E[(c,p), i F + m] = sum_q AminusT_i[q, p] S_i[q, m]      (CUDA cores, FP32)
+//   MMA:            D[(c,p), k] = sum_{i,m} E[(c,p), i F + m] rDivM_i[k, m]  (split FP16 x3)
+//   Q += D.
+// Three 128-thread CTAs per SM (74 KB of shared memory each at order 6) overlap one another's
+// waits; the E operand aliases the exchange buffer of the mapped traces.
+template <int ORD>
+__global__ void __launch_bounds__(128, 3) sei_nb_tc(sei::TcNbArgs A) {
+  using D = NbDims<ORD>;
+  constexpr int B = D::B, Bp = D::Bp, F = D::F, FP = D::FP, K2 = D::K2, N2 = D::N2;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t tslot;
+  uint16_t* opRd = reinterpret_cast<uint16_t*>(sm);
+  float* X = reinterpret_cast<float*>(sm + D::kOp);
+  __half* aHi = reinterpret_cast<__half*>(sm + D::kOp);
+  __half* aLo = aHi + 128 * K2;
+  const int tid = threadIdx.x;
+  if (tid < 32) sei_tc::tmemAlloc(&tslot, D::kCols);
+  if (tid == 0) {
+    sei_tc::mbarInit(&mbar, 1);
+    sei_tc::mbarExpectTx(&mbar, (uint32_t)D::kOp);
+    sei_tc::bulkCopyG2S(opRd, A.opRd, (uint32_t)D::kOp, &mbar);
+  }
+  sei_tc::fenceBeforeSync();
+  __syncthreads();
+  sei_tc::fenceAfterSync();
+  const uint32_t taddr = tslot;
+  const uint32_t tbase = taddr + ((uint32_t)((tid >> 5) * 32) << 16);
+  uint32_t phase = 0;
+  bool ok = sei_tc::mbarWait(&mbar, phase, kMaxPolls);
+  phase ^= 1;
+  const uint16_t* rdHi = opRd;
+  const uint16_t* rdLo = opRd + N2 * K2;
+  const int r = tid, q = r % 9;
+  const bool rowOk = r < 9 * kCellsPerTile;
+  // Padding rows 126, 127 compute with cell 13 and never store.
+  const int c = rowOk ? r / 9 : kCellsPerTile - 1;
+  const int ntiles = (A.n + kCellsPerTile - 1) / kCellsPerTile;
+  for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    const int cell = tile * kCellsPerTile + c;
+    const bool valid = rowOk && cell < A.n;
+    const int cl = cell < A.n ? cell : A.n - 1;
+    bool on[4];
+    // (1) thread (c, q): the mapped trace row of every face
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int nb = __ldg(A.nbr + (size_t)cl * 4 + i);
+      const int rl = A.rel[(size_t)cl * 4 + i];
+      on[i] = cell < A.n && nb >= 0 && nb < A.n && A.ftype[(size_t)cl * 4 + i] == 0;
+      float s[F];
+      if (on[i]) {
+        float t[FP];
+        sei_load_col<FP>(A.trace + ((size_t)(nb * 4 + (rl & 3)) * 9 + q) * FP, t);
+        applyTraceMap<ORD>(rl >> 2, t, s);
+      } else {
+#pragma unroll
+        for (int m = 0; m < F; ++m) s[m] = 0.f;
+      }
+      float4* xr = reinterpret_cast<float4*>(X + ((size_t)i * 128 + r) * FP);
+#pragma unroll
+      for (int m4 = 0; m4 < FP / 4; ++m4)
+        xr[m4] = make_float4(4 * m4 < F ? s[4 * m4 < F ? 4 * m4 : 0] : 0.f,
+                             4 * m4 + 1 < F ? s[4 * m4 + 1 < F ? 4 * m4 + 1 : 0] : 0.f,
+                             4 * m4 + 2 < F ? s[4 * m4 + 2 < F ? 4 * m4 + 2 : 0] : 0.f,
+                             4 * m4 + 3 < F ? s[4 * m4 + 3 < F ? 4 * m4 + 3 : 0] : 0.f);
+    }
+    __syncthreads();
+    // (2) thread (c, p = q): E row = sum_q AminusT_i[q, p] S_i[q, :] over the faces
+    float E[4 * F];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      float av[9];
+      const float* am = A.aminus + ((size_t)cl * 4 + i) * 81 + 9 * q;
+#pragma unroll
+      for (int s2 = 0; s2 < 9; ++s2) av[s2] = on[i] ? __ldg(am + s2) : 0.f;
+#pragma unroll
+      for (int m = 0; m < F; ++m) E[i * F + m] = 0.f;
+#pragma unroll
+      for (int s2 = 0; s2 < 9; ++s2) {
+        const float4* xs = reinterpret_cast<const float4*>(X + ((size_t)i * 128 + 9 * c + s2) * FP);
+#pragma unroll
+        for (int m4 = 0; m4 < FP / 4; ++m4) {
+          const float4 x = xs[m4];
+          const float xv[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (4 * m4 + u < F) E[i * F + 4 * m4 + u] = fmaf(xv[u], av[s2], E[i * F + 4 * m4 + u]);
+        }
+      }
+    }
+    __syncthreads();  // every read of X precedes the A operand that overwrites it
+    const int eE = rowExp(E, 4 * F);
+    writeRow<K2>(aHi, aLo, r, E, eE, 4 * F, K2);
+    sei_tc::fenceProxyAsync();
+    sei_tc::fenceBeforeSync();
+    __syncthreads();
+    sei_tc::fenceAfterSync();
+    if (tid == 0) issueSplit(taddr, aHi, aLo, K2, rdHi, rdLo, K2, K2 / 16, sei_tc::idescF16(128, N2), &mbar);
+    float acc[Bp];
+    sei_load_col<Bp>(A.Q + ((size_t)cl * 9 + q) * Bp, acc);
+    ok = sei_tc::mbarWait(&mbar, phase, kMaxPolls) && ok;
+    phase ^= 1;
+    sei_tc::fenceAfterSync();
+    accumulateColumns<B>(tbase, acc, ldexpf(1.f, eE), A.scRd);
+    if (valid) sei_store_col<Bp>(A.Q + ((size_t)cell * 9 + q) * Bp, acc);
+    sei_tc::fenceBeforeSync();
+    __syncthreads();
+    sei_tc::fenceAfterSync();
+  }
+  if (!ok && tid == 0) atomicExch(A.status, 1);
+  sei_tc::fenceBeforeSync();
+  __syncthreads();
+  if (tid < 32) sei_tc::tmemDealloc(taddr, D::kCols);
+}
+
+template <int ORD>
+int launchNbTc(const sei::DeviceArrays& d, const float* trace, int* status, int sms, void* stream, const void* opRdSym,
+               const void* scRdSym) {
+  using Dm = NbDims<ORD>;
+  sei::TcNbArgs a{};
+  a.n = d.n;
+  a.Q = d.Q;
+  a.trace = trace;
+  a.aminus = d.aminus;
+  a.nbr = d.nbr;
+  a.rel = d.rel;
+  a.ftype = d.ftype;
+  a.status = status;
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, opRdSym) != cudaSuccess) return -1;
+  a.opRd = (const uint16_t*)p;
+  if (cudaGetSymbolAddress(&p, scRdSym) != cudaSuccess) return -1;
+  a.scRd = (const float*)p;
+  if (cudaFuncSetAttribute(sei_nb_tc<ORD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Dm::kSmem) != cudaSuccess)
+    return -1;
+  const int ntiles = (d.n + kCellsPerTile - 1) / kCellsPerTile;
+  const int grid = ntiles < 3 * sms ? ntiles : 3 * sms;
+  if (grid <= 0) return 0;
+  sei_nb_tc<ORD><<<grid, 128, Dm::kSmem, (cudaStream_t)stream>>>(a);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
 }  // namespace
 
 namespace sei {
 
-int launchLintTensorCore(int order, const DeviceArrays& d, int* status, int sms, void* stream) {
+int launchLintTensorCore(int order, const DeviceArrays& d, float* trace, int traceOnly, int* status, int sms,
+                         void* stream) {
   switch (order) {
     case 4:
-      return launchLintTc<4>(d, status, sms, stream, (const void*)&sei_tc_o4::kvol_op, (const void*)&sei_tc_o4::kvol_scale,
+      return launchLintTc<4>(d, trace, traceOnly, status, sms, stream, (const void*)&sei_tc_o4::kvol_op, (const void*)&sei_tc_o4::kvol_scale,
                                    (const void*)&sei_tc_o4::krdivm_op, (const void*)&sei_tc_o4::krdivm_scale);
     case 5:
-      return launchLintTc<5>(d, status, sms, stream, (const void*)&sei_tc_o5::kvol_op, (const void*)&sei_tc_o5::kvol_scale,
+      return launchLintTc<5>(d, trace, traceOnly, status, sms, stream, (const void*)&sei_tc_o5::kvol_op, (const void*)&sei_tc_o5::kvol_scale,
                                    (const void*)&sei_tc_o5::krdivm_op, (const void*)&sei_tc_o5::krdivm_scale);
     case 6:
-      return launchLintTc<6>(d, status, sms, stream, (const void*)&sei_tc_o6::kvol_op, (const void*)&sei_tc_o6::kvol_scale,
+      return launchLintTc<6>(d, trace, traceOnly, status, sms, stream, (const void*)&sei_tc_o6::kvol_op, (const void*)&sei_tc_o6::kvol_scale,
                                    (const void*)&sei_tc_o6::krdivm_op, (const void*)&sei_tc_o6::krdivm_scale);
+    default:
+      return -1;
+  }
+}
+
+
+int launchNeighborTensorCore(int order, const DeviceArrays& d, const float* trace, int* status, int sms,
+                             void* stream) {
+  switch (order) {
+    case 4:
+      return launchNbTc<4>(d, trace, status, sms, stream, (const void*)&sei_tc_o4::krdivm_op,
+                           (const void*)&sei_tc_o4::krdivm_scale);
+    case 5:
+      return launchNbTc<5>(d, trace, status, sms, stream, (const void*)&sei_tc_o5::krdivm_op,
+                           (const void*)&sei_tc_o5::krdivm_scale);
+    case 6:
+      return launchNbTc<6>(d, trace, status, sms, stream, (const void*)&sei_tc_o6::krdivm_op,
+                           (const void*)&sei_tc_o6::krdivm_scale);
     default:
       return -1;
   }

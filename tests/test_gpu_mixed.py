@@ -1,9 +1,9 @@
-"""Mixed-precision path (SEI_PREC_F16X3: local integral on tcgen05 tensor cores, split FP16)
-against the FP64 oracle.
+"""Mixed-precision path (SEI_PREC_F16X3: local integral and neighbour flux on tcgen05 tensor
+cores, split FP16) against the FP64 oracle.
 
-Tolerances: one application of the local integral 2e-5 relative L2 of the update per quantity
-(the FP32 bar); ten time steps of kernel 'all' 1e-5 relative L2 per quantity of the field (the
-accuracy bar of the mixed-precision metric).
+Tolerances: one application of the local integral or of the neighbour flux 2e-5 relative L2 of
+the update per quantity (the FP32 bar); ten time steps of kernel 'all' 1e-5 relative L2 per
+quantity of the field (the accuracy bar of the mixed-precision metric).
 """
 import numpy as np
 import pytest
@@ -41,6 +41,31 @@ def test_local_integral_tensor_cores(built_lib, order):
                     cells["face_type"])
     errs = rel_l2_per_quantity(q_gpu - q0, q_ref - q0)
     assert max(errs) < 2e-5, errs
+    ctx.close()
+
+
+@pytest.mark.parametrize("order", [4, 5, 6])
+def test_neighbor_tensor_cores(built_lib, order):
+    """The neighbour flux from the stored face traces; after ADER alone the traces are stale and
+    the neighbour call recomputes them from the new time-integrated DOFs first."""
+    ctx, n, q0 = _ctx(order, PREC_F16X3)
+    cells = ctx.get_cells()
+    dt = ctx.cfl_timestep(0.5)
+    o = oracle_py.Oracle(order)
+    aminus = cells["AminusT"].astype(np.float64)
+    q_prev = q0
+    for rep in range(2):
+        ctx.compute_ader(dt * (1.0 + 0.5 * rep))
+        ctx.sync()
+        i_gpu = ctx.get_time_integrated()
+        ctx.compute_neighbors_integral()
+        ctx.sync()
+        q_gpu = ctx.get_dofs()
+        q_ref = o.neighbor(q_prev.astype(np.float64), i_gpu.astype(np.float64), aminus, cells["neighbor"], cells["side"],
+                           cells["orient"], cells["face_type"])
+        errs = rel_l2_per_quantity(q_gpu - q_prev, q_ref - q_prev)
+        assert max(errs) < 2e-5, (rep, errs)
+        q_prev = q_gpu
     ctx.close()
 
 
