@@ -56,6 +56,12 @@ def bytes_per_cell(order, kernel):
         return 3 * dof + 4 * 72 + 4 * 324 + 4
     if kernel == "neighbor":  # read Q, write Q, read neighbour I (once per cell), A- x4, relations
         return 3 * dof + 4 * 324 + 16 + 4 + 4
+    f = order * (order + 1) // 2
+    trace = 4 * 4 * 9 * ((f + 3) // 4 * 4)  # face traces of one cell, [4][9][FP] float32
+    if kernel in ("lint_trace", "lint_tc"):  # local integral that also writes the face traces
+        return 3 * dof + 4 * 72 + 4 * 324 + 4 + trace
+    if kernel == "neighbor_tc":  # read Q, write Q, read the four neighbour traces, A- x4, relations
+        return 2 * dof + trace + 4 * 324 + 16 + 4 + 4
     if kernel == "model":  # compulsory traffic of one fused cell update (reference data model)
         return 4 * dof + 4 * 72 + 4 * 324 + 4 * 324 + 16 + 4
     raise ValueError(kernel)
@@ -159,6 +165,40 @@ def cpu_baseline(k_steps=None, budget_s=12.0, sample=None):
             "sample": f"order {ORDER} elastic, {n} tets ({CPU_SAMPLE_DIMS[0]}x{CPU_SAMPLE_DIMS[1]}x{CPU_SAMPLE_DIMS[2]} "
                       f"cubes, same material/seed distribution), {steps} steps of kernel 'all', FP64",
             "seconds": el, "steps": steps, "cells": n}
+
+
+ACC_STEPS = 50
+
+
+def accuracy_vs_oracle(local, paths, sample):
+    """Relative L2 error per quantity of each arithmetic path after ACC_STEPS steps of kernel 'all'
+    against the FP64 oracle, on the CPU sample's seeded inputs (mesh, operators, DOFs, dt); part
+    of the CPU leg, the oracle being the checker."""
+    import numpy as np
+
+    from oracle import oracle_py
+    from seissol_gb300 import Context
+
+    n, q, args, dt, ft = sample
+    ref = oracle_py.Oracle(ORDER).steps(q, *args, dt, ACC_STEPS, ft)
+    star, aplus, aminus, nb, side, orient = args
+    out = {}
+    for path in paths:
+        prec, tc_local = PATHS[path]
+        ctx = Context(ORDER, device=local, precision=prec)
+        if tc_local:
+            ctx.set_option(3, 1)
+        ctx.set_cells(star, aplus, aminus, nb, side, orient, ft)
+        ctx.set_dofs(q.astype(np.float32))
+        ctx.run("all", dt, ACC_STEPS)
+        ctx.sync()
+        got = ctx.get_dofs().astype(np.float64)
+        ctx.close()
+        errs = [float(np.linalg.norm(got[:, k] - ref[:, k]) / np.linalg.norm(ref[:, k])) for k in range(9)]
+        out[path] = {"rel_l2_max": max(errs), "rel_l2_per_quantity": errs}
+    return {"vs": "FP64 oracle (CPU)", "steps": ACC_STEPS, "cells": n,
+            "sample": f"{CPU_SAMPLE_DIMS[0]}x{CPU_SAMPLE_DIMS[1]}x{CPU_SAMPLE_DIMS[2]} cubes x 5 tets, same material "
+                      "and DOF distributions as the workload", "paths": out}
 
 
 def dist_setup():
@@ -329,8 +369,8 @@ def dr_measurement(local, steps):
     20,000 faces (25 points each), fast-velocity-weakening friction with a ~ U[0.008, 0.02],
     sn ~ U[-120, -40] MPa, tau ~ U[20, 75] MPa, V_init = 1e-16 m/s, kernel all_dr.
 
-    A training run (its own seed) records samples of the plain Newton solve for 3 steps and
-    trains the warm-start network on the GPU; then two contexts with the same (other) seed run
+    A training run (its own seed) records samples of the plain Newton solve at ten points of a
+    run of the same length and trains the warm-start network on the GPU; then two contexts with the same (other) seed run
     `steps` steps from the same initial state, plain and warm-started, timed with CUDA events.
     Reported: cell- and face-updates/s of each, Newton iterations per point and step (all
     solves and the first solve of each time point), and the largest slip-rate difference."""
@@ -346,28 +386,42 @@ def dr_measurement(local, steps):
         ctx.set_dofs(rng.uniform(-1, 1, (n, 9, 20)).astype(np.float32))
         return ctx, n, nf
 
+    # training samples from the plain solve along a whole run of the training fault: 40,000
+    # samples at the start of each tenth of the run
     t0 = time.perf_counter()
     tr, _, _ = make(DR_SEED)
     dt = tr.cfl_timestep(0.5)
-    tr.dr_record_samples(400000)
-    tr.run("all_dr", dt, 3)
-    tr.sync()
-    nsamp = len(tr.dr_samples())
-    loss0, loss1 = tr.mlp_train(steps=1500, lr=3e-3, seed=1)
+    chunks, nchunk = [], 10
+    for k in range(nchunk):
+        tr.dr_record_samples(400000 // nchunk)
+        tr.run("all_dr", dt, 1)
+        tr.sync()
+        chunks.append(tr.dr_samples())
+        tr.dr_record_samples(0)
+        tr.run("all_dr", dt, max(steps // nchunk - 1, 0))
+    samples = np.concatenate(chunks)
+    nsamp = len(samples)
+    loss0, loss1 = tr.mlp_train(samples=samples, steps=1500, lr=3e-3, seed=1)
     params, norm = tr.mlp_get()
     tr.close()
     train_s = time.perf_counter() - t0
     out = {}
-    states = {}
+    states, early = {}, {}
+    k_early = min(20, steps)
     for mode in ("plain", "warm"):
         ctx, n, nf = make(DR_SEED + 1)
         if mode == "warm":
             ctx.mlp_set(params, norm)
             ctx.dr_warm_start(True)
         ctx.dr_reset_counters()
-        ctx.run("all_dr", dt, steps)
+        ctx.run("all_dr", dt, k_early)
         ctx.sync()
         ms = ctx.last_run_ms()
+        early[mode] = np.hypot(ctx.dr_state("slip_rate1"), ctx.dr_state("slip_rate2"))
+        if steps > k_early:
+            ctx.run("all_dr", dt, steps - k_early)
+            ctx.sync()
+            ms += ctx.last_run_ms()
         tot, npts, first = ctx.dr_newton_iterations(first=True)
         states[mode] = np.hypot(ctx.dr_state("slip_rate1"), ctx.dr_state("slip_rate2"))
         ctx.set_profiling(True)
@@ -390,30 +444,46 @@ def dr_measurement(local, steps):
             / max(out["warm"]["newton_iters_per_point_step"], 1e-30),
             "max_abs_dV": float(np.abs(vp - vw).max()),
             "max_rel_dV": float((np.abs(vp - vw) / np.maximum(vp, 1e-30)).max()),
+            f"max_rel_dV_after_{k_early}_steps": float((np.abs(early["plain"] - early["warm"])
+                                                         / np.maximum(early["plain"], 1e-30)).max()),
+            "dV_note": "plain and warm-started runs are separate trajectories: every solve converges to the "
+                       "Newton tolerance, and the tolerance-level differences feed back through the wave field "
+                       "over the run",
             "training": {"samples": nsamp, "adam_steps": 1500, "loss_first": loss0, "loss_last": loss1,
                          "seconds_incl_recording": train_s}}
 
 
-def kname(kind, args):
+PATHS = {"fp32": (0, False), "f16x3": (1, False), "f16x3_tc_local": (1, True)}
+PATH_DESC = {"fp32": "FP32 CUDA cores (sparse, non-zero flops)",
+             "f16x3": "mixed: neighbour flux on tcgen05 tensor cores (split FP16 x3) from stored face traces, "
+                      "ADER and local integral FP32 CUDA cores",
+             "f16x3_tc_local": "mixed: local integral and neighbour flux on tcgen05 tensor cores (split FP16 x3), "
+                               "ADER FP32 CUDA cores"}
+
+
+def kname(kind, path):
     """Name of the CUDA kernel behind a launch kind of the step."""
-    if kind == "lint" and args.precision == "f16x3":
+    if kind == "lint" and path == "f16x3_tc_local":
         return f"sei_lint_tc<{ORDER}>"
-    if kind == "neighbor" and args.precision == "f16x3":
+    if kind == "neighbor" and path != "fp32":
         return f"sei_nb_tc<{ORDER}>"
     return f"sei_{kind}_o{ORDER}"
 
 
-def run_ours(args, world, rank, local):
-    import numpy as np
+def measure_path(args, world, local, path, hbm, peak_kind, e2e_steps=0):
+    """Kernel 'all' on the workload in one arithmetic path: throughput, per-kernel launch times,
+    roofline of the dominant launch and (optionally) the end-to-end host-buffer figure."""
     import torch
 
     from seissol_gb300 import Context
 
-    hbm, peak_kind = peaks()
-    prec = {"fp32": 0, "f16x3": 1}[args.precision]
+    prec, tc_local = PATHS[path]
+    rank = int(os.environ.get("RANK", "0"))
     ctx = Context(ORDER, device=local, precision=prec)
     if args.fused_local:
         ctx.set_option(1, 1)  # SEI_OPT_FUSED_LOCAL
+    if tc_local:
+        ctx.set_option(3, 1)  # SEI_OPT_TC_LOCAL
     n = ctx.build_periodic_cube(*DIMS, perturb=PERTURB, seed=SEED + rank)
     dt = ctx.cfl_timestep(0.5)
     ctx.run("all", dt, args.warmup)
@@ -430,9 +500,8 @@ def run_ours(args, world, rank, local):
         barrier(world)
     ms = barrier_max(world, ms)
     value = world * n * args.steps / (ms / 1e3)
-    clocks = clk.summary()
 
-    # per-launch durations of the two kernels inside a profiled run of the same workload
+    # per-launch durations inside a profiled run of the same workload
     ctx.set_profiling(True)
     ctx.run("all", dt, args.steps)
     ctx.sync()
@@ -442,30 +511,30 @@ def run_ours(args, world, rank, local):
     kernels = {names[k]: v[0] / v[1] for k, v in by_kind.items() if k in names and v[1] > 0}
     launches = sum(v[1] for v in by_kind.values())
     dom = max(kernels, key=kernels.get)
-    algo = bytes_per_cell(ORDER, dom) * n
+    bkind = dom if path == "fp32" or dom == "ader" else f"{dom}_{'tc' if (dom == 'neighbor' or tc_local) else 'trace'}"
+    algo = bytes_per_cell(ORDER, bkind) * n
     achieved = algo / (kernels[dom] / 1e3) / 1e9
     traffic = None
     tf = os.path.join(ROOT, "profiles", "dram_traffic_per_cell.txt")
     if os.path.exists(tf):
         for line in open(tf):
             parts = line.split()
-            if len(parts) >= 2 and parts[0] == kname(dom, args):
+            if len(parts) >= 2 and parts[0] == kname(dom, path):
                 traffic = float(parts[1]) * n
-    roof = {"bound": "hbm", "kernel": kname(dom, args), "achieved": achieved, "peak": hbm, "unit": "GB/s",
+    roof = {"bound": "hbm", "kernel": kname(dom, path), "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "peak_source": f"{peak_kind} hbm_gbs", "traffic": traffic,
             "algorithmic_bytes_per_launch": algo, "launch_ms": kernels[dom],
             "step_model_frac": value / world * bytes_per_cell(ORDER, "model") / (hbm * 1e9)}
     try:
         from seissol_gb300.codegen.gen_kernels import nnz_flops
         f = nnz_flops(ORDER)
-        flop_cell = f["ader"] + f["local"] + f["neighbor"]
-        roof["nonzero_tflops"] = value / world * flop_cell / 1e12
+        roof["nonzero_tflops"] = value / world * (f["ader"] + f["local"] + f["neighbor"]) / 1e12
     except Exception:
         pass
 
     # end to end through the C ABI with pinned host buffers, one step per call
     e2e = None
-    if args.e2e_steps > 0:
+    if e2e_steps > 0:
         B = 56
         hin = torch.empty((n, 9, B), dtype=torch.float32, pin_memory=True)
         hout = torch.empty((n, 9, B), dtype=torch.float32, pin_memory=True)
@@ -476,16 +545,37 @@ def run_ours(args, world, rank, local):
             ctx._check(ctx.lib.sei_run_host(ctx.h, 0, dt, 1, pin, pout), "sei_run_host")
         barrier(world)
         t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
+        for _ in range(e2e_steps):
             ctx._check(ctx.lib.sei_run_host(ctx.h, 0, dt, 1, pin, pout), "sei_run_host")
             hin, hout = hout, hin
             pin, pout = pout, pin
         el = barrier_max(world, time.perf_counter() - t0)
         nbytes = n * 9 * B * 4
-        e2e = {"value": world * n * args.e2e_steps / el, "unit": UNIT, "h2d_bytes_per_step": nbytes,
-               "d2h_bytes_per_step": nbytes, "steps": args.e2e_steps,
+        e2e = {"value": world * n * e2e_steps / el, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": nbytes, "steps": e2e_steps, "path": path,
                "call": "sei_run_host(SEI_KERNEL_ALL, dt, 1, dofs_in, dofs_out) with pinned host DOFs"}
     ctx.close()
+    return {"value": value, "ms": ms, "n": n, "kernels": kernels, "launches": launches, "roofline": roof,
+            "clocks": clk.summary(), "e2e": e2e, "description": PATH_DESC[path]}
+
+
+def run_ours(args, world, rank, local):
+    hbm, peak_kind = peaks()
+    paths = ["fp32", "f16x3"] if args.precision == "both" else [args.precision]
+    if args.tc_local and "f16x3" in paths:
+        paths[paths.index("f16x3")] = "f16x3_tc_local"
+    res = {p: measure_path(args, world, local, p, hbm, peak_kind) for p in paths}
+    best = max(res, key=lambda p: res[p]["value"])
+    if args.e2e_steps > 0:
+        res[best]["e2e"] = measure_path(args, world, local, best, hbm, peak_kind, args.e2e_steps)["e2e"]
+    head = res[best]
+    n, ms, value = head["n"], head["ms"], head["value"]
+    roof, clocks, kernels, launches, e2e = head["roofline"], head["clocks"], head["kernels"], head["launches"], head["e2e"]
+    paths_out = {p: {"value": r["value"], "ms_per_step": r["ms"] / args.steps, "kernel_ms_per_step": r["kernels"],
+                     "roofline_kernel": r["roofline"]["kernel"], "roofline_frac": r["roofline"]["frac"],
+                     "description": r["description"]} for p, r in res.items()}
+    mixed = [p for p in res if p != "fp32"]
+    ratio = res[mixed[0]]["value"] / res["fp32"]["value"] if mixed and "fp32" in res else None
 
     dr = None
     if rank == 0 and args.dr_steps > 0:
@@ -497,20 +587,25 @@ def run_ours(args, world, rank, local):
     if rank == 0 and args.visco_steps > 0:
         vis = visco_measurement(local, args.visco_steps)
 
-    base = None
+    base = acc = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        base = cpu_baseline()
+        sample = cpu_sample()
+        base = cpu_baseline(sample=sample)
+        acc = accuracy_vs_oracle(local, list(res), sample)
+        for p, a in acc["paths"].items():
+            paths_out[p]["rel_l2_vs_fp64"] = a["rel_l2_max"]
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": "elastic order 6 (56x9), 400,000-tet periodic cube 40x40x50 cubes x 5 tets, "
                                        "material +-10% per cell, kernel all (ADER+local+neighbour), GTS, CFL 0.5",
-                           "cells_per_gpu": n, "order": ORDER, "precision": "FP32 CUDA cores (sparse, non-zero flops)",
+                           "cells_per_gpu": n, "order": ORDER, "path": best, "precision": PATH_DESC[best],
                            "l2": "inputs larger than L2 (~3 GB resident per GPU), no flush",
                            "parallelism": f"replicas x{world}"},
                 "roofline": roof, "cpu_baseline": base, "e2e": e2e, "clocks": clocks,
-                "gpu_launches": launches, "kernel_ms_per_step": kernels, "dynamic_rupture": dr,
+                "gpu_launches": launches, "kernel_ms_per_step": kernels, "paths": paths_out,
+                "mixed_vs_fp32": ratio, "accuracy": acc, "dynamic_rupture": dr,
                 "local_time_stepping": lts, "viscoelastic": vis}
         print(json.dumps(line))
     return 0
@@ -525,8 +620,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fused-local", action="store_true", help="ADER and local integral in one launch")
-    ap.add_argument("--precision", choices=("fp32", "f16x3"), default="fp32")
-    ap.add_argument("--dr-steps", type=int, default=20,
+    ap.add_argument("--precision", choices=("both", "fp32", "f16x3"), default="both",
+                    help="arithmetic path(s) timed; 'both' reports the faster as value and the other beside it")
+    ap.add_argument("--tc-local", action="store_true", help="f16x3: local integral on the tensor cores too")
+    ap.add_argument("--dr-steps", type=int, default=200,
                     help="steps of the dynamic-rupture measurement (plain and warm-started); 0 skips it")
     ap.add_argument("--visco-steps", type=int, default=20,
                     help="steps of the viscoelastic measurement; 0 skips it")

@@ -48,9 +48,11 @@ extern "C" {
 
 /* Arithmetic of the global-matrix contractions. */
 #define SEI_PREC_FP32 0 /* CUDA-core FP32, sparse (non-zero flops only) */
-/* Mixed precision: the global-matrix contractions of the local integral on the tensor cores
- * (tcgen05 kind::f16), each product split into three FP16 products (hi*hi + hi*lo + lo*hi) of
- * power-of-two row-scaled operands with FP32 accumulation; everything else FP32. */
+/* Mixed precision: global-matrix contractions on the tensor cores (tcgen05 kind::f16), each
+ * product split into three FP16 products (hi*hi + hi*lo + lo*hi) of power-of-two row-scaled
+ * operands with FP32 accumulation; everything else FP32.  The neighbour flux always runs on the
+ * tensor cores, from the face traces of I that the local integral stores; the local integral
+ * runs on the tensor cores when SEI_OPT_TC_LOCAL is 1, else on the FP32 CUDA cores. */
 #define SEI_PREC_F16X3 1
 
 typedef struct sei_ctx sei_ctx;
@@ -169,6 +171,9 @@ int sei_evaluate_taylor(sei_ctx* ctx, const double* coeffs, float* out_device);
  * sei_lts_run and replays it for every cycle (one graph launch per cycle); 0 (default) launches
  * the kernels of every cycle directly.  Per-launch profiling is not recorded inside the graph. */
 #define SEI_OPT_LTS_GRAPH 2
+/* SEI_OPT_TC_LOCAL (SEI_PREC_F16X3 only): 1 runs the local integral on the tensor cores as
+ * well; 0 (default) runs it on the FP32 CUDA cores, which is faster at orders 4-6. */
+#define SEI_OPT_TC_LOCAL 3
 int sei_set_option(sei_ctx* ctx, int option, int value);
 
 /* Runs a proxy kernel for nsteps steps (src/Proxy/Runner.cpp:99-111); asynchronous. */

@@ -91,7 +91,7 @@ def gen_order(order: int) -> str:
     a("// Do not edit.")
     a("#pragma once")
     a(f"namespace sei_o{order} {{")
-    a(f"constexpr int kOrder = {order}, kB = {B}, kBp = {padded(B)}, kF = {F}, kQ = 9, kCPB = {CPB};")
+    a(f"constexpr int kOrder = {order}, kB = {B}, kBp = {padded(B)}, kF = {F}, kFP = {padded(F)}, kQ = 9, kCPB = {CPB};")
     a(f"constexpr int kDerivSize = {sum(nb3(order - i) for i in range(order)) * NQ};")
     fl = nnz_flops(order)
     a(f"// Non-zero flops per cell of the ADER, local-integral and neighbour kernels (literal FFMAs and premixes).")
@@ -158,7 +158,7 @@ def gen_order(order: int) -> str:
             off += bc * NQ
             a("  }")
 
-    def emit_volume_flux():
+    def emit_volume_flux(with_trace=False):
         a("  // ---- volume: Q += sum_e kDivM_e (I star_e)")
         a(f"#pragma unroll\n  for (int k = 0; k < kB; ++k) Xq[k * 32] = I[k];")
         a("  __syncthreads();")
@@ -182,8 +182,12 @@ def gen_order(order: int) -> str:
             a("  {")
             a("    float T[kF];")
             _matvec(L, "    ", G["fMrT"][f], "I", "T", F, B, True)
+            if with_trace:
+                a("    sei_stage_trace<kB, kF, kFP>(sm, lane, q, T);")
             a(f"#pragma unroll\n    for (int m = 0; m < kF; ++m) Xq[m * 32] = T[m];")
             a("    __syncthreads();")
+            if with_trace:
+                a(f"    sei_store_traces<kB, kF, kFP, kCPB>(n, sm, trace, {f});")
             a(f"    const bool on = valid && ftype[(size_t)cl * 4 + {f}] != 1;")
             a(f"    const float* ap = aplus + ((size_t)cl * 4 + {f}) * 81 + 9 * q;")
             a("    float av[9];")
@@ -239,6 +243,18 @@ sei_lint_o{order}(int n, float* __restrict__ Q, const float* __restrict__ Iin, c
     a("  float I[kBp];")
     a("  sei_load_col<kBp>(Iin + ((size_t)cl * 9 + q) * kBp, I);")
     emit_volume_flux()
+    a("  if (valid) sei_store_col<kBp>(Q + ((size_t)cell * 9 + q) * kBp, acc);")
+    a("}")
+    a(f"""
+// The same local integral, which also stores the face traces fMrT_f I of every cell,
+// trace[4][n][9][kFP], for the neighbour kernel of the tensor-core path.
+extern "C" __global__ void __launch_bounds__(288, 1)
+sei_lint_trace_o{order}(int n, float* __restrict__ Q, const float* __restrict__ Iin, const float* __restrict__ star_nz,
+                        const float* __restrict__ aplus, const unsigned char* __restrict__ ftype,
+                        float* __restrict__ trace) {{""" + prologue)
+    a("  float I[kBp];")
+    a("  sei_load_col<kBp>(Iin + ((size_t)cl * 9 + q) * kBp, I);")
+    emit_volume_flux(with_trace=True)
     a("  if (valid) sei_store_col<kBp>(Q + ((size_t)cell * 9 + q) * kBp, acc);")
     a("}")
 

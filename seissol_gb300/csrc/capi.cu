@@ -79,6 +79,7 @@ struct sei_ctx {
   // integral and read by the neighbour kernel; valid while I has not changed since
   float* d_trace = nullptr;
   bool trace_valid = false;
+  bool tc_local = false;  // SEI_OPT_TC_LOCAL
   std::vector<cudaEvent_t> prof_events;
   std::vector<int> prof_kind;  // kind of the launch starting at event i: 0 ADER (or fused ADER + local),
                                // 1 neighbour, 2 fault, 3 local integral, 4 LTS gather / buffer, -1 end of run
@@ -268,15 +269,17 @@ int launchAderOnly(sei_ctx* c, const sei::DeviceArrays& d, const float* coeffs) 
 int launchLintOnly(sei_ctx* c, const sei::DeviceArrays& d) {
   int rc = profMark(c, 3);
   if (rc) return rc;
-  if (c->cfg.precision == SEI_PREC_F16X3) {
-    // the traces cover every cell only outside local time stepping (whose kernels run per cluster)
-    float* trace = c->lts ? nullptr : c->d_trace;
+  // the traces cover every cell only outside local time stepping (whose kernels run per cluster)
+  float* trace = (c->cfg.precision == SEI_PREC_F16X3 && !c->lts) ? c->d_trace : nullptr;
+  if (c->cfg.precision == SEI_PREC_F16X3 && c->tc_local) {
     if (sei::launchLintTensorCore(c->cfg.order, d, trace, 0, c->d_status, c->sms, c->stream) != 0)
       return fail(c, SEI_ERR_CUDA, "tensor-core local-integral kernel launch failed");
-    c->trace_valid = trace != nullptr;
-    return SEI_OK;
+  } else {
+    sei::DeviceArrays dt = d;
+    dt.trace = trace;
+    if (c->k.lint(dt, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "local-integral kernel launch failed");
   }
-  if (c->k.lint(d, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "local-integral kernel launch failed");
+  c->trace_valid = trace != nullptr;
   return SEI_OK;
 }
 
@@ -704,6 +707,10 @@ int sei_set_option(sei_ctx* c, int option, int value) {
       return SEI_OK;
     case SEI_OPT_LTS_GRAPH:
       c->lts_graph = value != 0;
+      return SEI_OK;
+    case SEI_OPT_TC_LOCAL:
+      c->tc_local = value != 0;
+      c->trace_valid = false;
       return SEI_OK;
     default:
       return fail(c, SEI_ERR_ARG, "unknown option");

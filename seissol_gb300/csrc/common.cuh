@@ -62,3 +62,37 @@ template <int N>
 __device__ __forceinline__ void sei_cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
+
+// Face traces of the local-integral kernel, staged in shared memory after the exchange buffer:
+// the row of (cell lane, quantity q) holds FP floats (zero padded); a cell's 9 rows are followed
+// by 4 floats of padding, so 16-byte writes of a quarter warp (8 cells) hit distinct banks.
+template <int FP>
+constexpr int seiTraceStageStride() { return 9 * FP + 4; }
+
+template <int B, int F, int FP>
+__device__ __forceinline__ void sei_stage_trace(float* sm, int lane, int q, const float (&T)[F]) {
+  float4* st = reinterpret_cast<float4*>(sm + 9 * B * 32 + lane * seiTraceStageStride<FP>() + q * FP);
+#pragma unroll
+  for (int m4 = 0; m4 < FP / 4; ++m4) {
+    float v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = 4 * m4 + u < F ? T[4 * m4 + u < F ? 4 * m4 + u : 0] : 0.f;
+    st[m4] = make_float4(v[0], v[1], v[2], v[3]);
+  }
+}
+
+// Coalesced 16-byte store of the staged face-f traces of a CPB-cell block to trace[4][n][9][FP].
+// Out of line and not unrolled: the generated kernels are large and their instruction cache is
+// the limit.
+template <int B, int F, int FP, int CPB>
+__device__ __noinline__ void sei_store_traces(int n, const float* sm, float* trace, int f) {
+  constexpr int R4 = 9 * FP / 4;  // float4 per cell
+  const float* st = sm + 9 * B * 32;
+  const int cell0 = blockIdx.x * CPB;
+  float4* dst = reinterpret_cast<float4*>(trace + ((size_t)f * n + cell0) * 9 * FP);
+#pragma unroll 1
+  for (int idx = threadIdx.x; idx < CPB * R4; idx += blockDim.x) {
+    const int L = idx / R4, rem = idx - L * R4;
+    if (cell0 + L < n) dst[idx] = *reinterpret_cast<const float4*>(st + L * seiTraceStageStride<FP>() + 4 * rem);
+  }
+}

@@ -63,6 +63,7 @@ struct DeviceArrays {
   const int32_t* nbr;
   const uint8_t* rel;    // side | orient << 2
   const uint8_t* ftype;  // 0 regular, 1 dynamic rupture, 2 none
+  float* trace = nullptr;  // nullable: face traces fMrT_f I out of the local integral, [4][n][9][FP]
 };
 
 using LaunchLocalFn = int (*)(const DeviceArrays&, const float* coeffs, void* stream);
@@ -184,7 +185,7 @@ struct TcLintArgs {
   const float* scVol;     // per-row power-of-two scales of the operand tables
   const uint16_t* opRd;
   const float* scRd;
-  float* trace;   // nullable: face traces fMrT_f I out, [n][4][9][FP] (FP = F rounded up to 4)
+  float* trace;   // nullable: face traces fMrT_f I out, [4][n][9][FP] (FP = F rounded up to 4)
   int traceOnly;  // 1: write the traces only (Q unchanged)
   int* status;    // set to 1 when a wait gave up
 };
@@ -195,7 +196,7 @@ int launchLintTensorCore(int order, const DeviceArrays& d, float* trace, int tra
 struct TcNbArgs {
   int n;
   float* Q;
-  const float* trace;  // [n][4][9][FP] traces fMrT_f I of every cell and face
+  const float* trace;  // [4][n][9][FP] traces fMrT_f I of every cell and face
   const float* aminus;
   const int32_t* nbr;
   const uint8_t* rel;

@@ -56,11 +56,21 @@ int launchAder(const sei::DeviceArrays& d, const float* coeffs, void* stream) {
 
 int launchLint(const sei::DeviceArrays& d, void* stream) {
   if (d.n <= 0) return 0;
+  const int blocks = (d.n + K::kCPB - 1) / K::kCPB;
+  if (d.trace) {
+    // exchange buffer plus the staging rows of the stored face traces
+    const size_t smem = sizeof(float) * (9 * K::kB * 32 + 32 * seiTraceStageStride<K::kFP>());
+    if (cudaFuncSetAttribute(K::SEI_CAT(sei_lint_trace_o, SEI_ORDER), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
+      return -1;
+    K::SEI_CAT(sei_lint_trace_o, SEI_ORDER)<<<blocks, 288, smem, (cudaStream_t)stream>>>(
+        d.n, d.Q, d.I, d.star_nz, d.aplus, d.ftype, d.trace);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+  }
   const size_t smem = sizeof(float) * 9 * K::kB * 32;
   if (cudaFuncSetAttribute(K::SEI_CAT(sei_lint_o, SEI_ORDER), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return -1;
-  const int blocks = (d.n + K::kCPB - 1) / K::kCPB;
   K::SEI_CAT(sei_lint_o, SEI_ORDER)<<<blocks, 288, smem, (cudaStream_t)stream>>>(d.n, d.Q, d.I, d.star_nz, d.aplus,
                                                                                 d.ftype);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;

@@ -71,6 +71,11 @@ __device__ __forceinline__ void bulkCopyG2S(void* dst, const void* src, uint32_t
                : "memory");
 }
 
+// Bulk prefetch of [p, p + bytes) into L2 (p 16-byte aligned, bytes a multiple of 16).
+__device__ __forceinline__ void prefetchL2(const void* p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(p), "r"(bytes) : "memory");
+}
+
 // One full warp allocates ncols TMEM columns; the address is written to *slot (shared).
 __device__ __forceinline__ void tmemAlloc(uint32_t* slot, uint32_t ncols) {
   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smemAddr(slot)), "r"(ncols)

@@ -214,11 +214,11 @@ __global__ void __launch_bounds__(128, 1) sei_lint_tc(sei::TcLintArgs A) {
     // face traces -> G = traces . AplusT (per face), the A operand of MMA 2; the traces of
     // every face are also stored for the neighbour kernel of this path
     constexpr int FP = (F + 3) / 4 * 4;
-    float* trow = (A.trace && valid) ? A.trace + ((size_t)cell * 4 * 9 + q) * FP : nullptr;
+    float* trow = (A.trace && valid) ? A.trace + ((size_t)cell * 9 + q) * FP : nullptr;
     forColumns(tbase, 3 * B, 4 * F, [&](int t, float v) {
       const float x = v * sI * __ldg(A.scVol + 3 * B + t);
       X[t * 128 + r] = x;
-      if (trow) trow[(t / F) * 9 * FP + t % F] = x;
+      if (trow) trow[(size_t)(t / F) * A.n * 9 * FP + t % F] = x;
     });
     if (A.traceOnly) {
       sei_tc::fenceBeforeSync();
@@ -318,7 +318,7 @@ struct NbDims {
 };
 
 // Neighbour flux (Neighbor::computeNeighborsIntegral, codegen/kernels/aderdg.py:414-428) of a
-// tile of 14 cells from the stored face traces T_f = fMrT_f I of all cells.  Rows of the tile
+// tile of 14 cells from the stored face traces T_f = fMrT_f I of all cells ([face][cell][9][FP]).  Rows of the tile
 // are (cell, quantity) = 9 c + q.  For each regular face i with neighbour nb, side j and
 // orientation h:
 //   thread (c, q):  S_i[q, :] = fP_h diag(fM)^-1 T_j(nb)[q, :]                (CUDA cores, FP32)
@@ -364,23 +364,69 @@ __global__ void __launch_bounds__(128, 3) sei_nb_tc(sei::TcNbArgs A) {
     const int cell = tile * kCellsPerTile + c;
     const bool valid = rowOk && cell < A.n;
     const int cl = cell < A.n ? cell : A.n - 1;
+    // L2 prefetch of the next tile of this CTA: its DOFs and AminusT (contiguous), then, once
+    // the neighbour indices have arrived, the trace rows its faces read
+    const int nt = tile + (int)gridDim.x;
+    int pfNb = -1, pfRl = 0;
+    if (nt < ntiles) {
+      const int c0 = nt * kCellsPerTile;
+      const int cnt = A.n - c0 < kCellsPerTile ? A.n - c0 : kCellsPerTile;
+      if (tid == 0) {
+        sei_tc::prefetchL2(A.Q + (size_t)c0 * 9 * Bp, (uint32_t)(cnt * 9 * Bp * 4));
+        sei_tc::prefetchL2(A.aminus + (size_t)c0 * 4 * 81, (uint32_t)(cnt * 4 * 81 * 4));
+      }
+      if (tid < 4 * cnt) {
+        const size_t f = (size_t)c0 * 4 + tid;
+        pfNb = A.ftype[f] == 0 ? __ldg(A.nbr + f) : -1;
+        pfRl = A.rel[f];
+      }
+    }
     bool on[4];
-    // (1) thread (c, q): the mapped trace row of every face
+    // (1) thread (c, q): the raw trace rows of the four faces arrive together by cp.async into
+    // this thread's rows of X, AminusT into registers meanwhile; then the map fP_h diag(fM)^-1
+    // in place (each thread touches only its own rows until the barrier)
+    int hs[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int nb = __ldg(A.nbr + (size_t)cl * 4 + i);
       const int rl = A.rel[(size_t)cl * 4 + i];
       on[i] = cell < A.n && nb >= 0 && nb < A.n && A.ftype[(size_t)cl * 4 + i] == 0;
+      hs[i] = rl >> 2;
+      float* xr = X + ((size_t)i * 128 + r) * FP;
+      if (on[i]) {
+        const float* src = A.trace + (((size_t)(rl & 3) * A.n + nb) * 9 + q) * FP;
+#pragma unroll
+        for (int m4 = 0; m4 < FP / 4; ++m4) sei_cp_async16(xr + 4 * m4, src + 4 * m4);
+      }
+    }
+    sei_cp_async_commit();
+    float av[4][9];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float* am = A.aminus + ((size_t)cl * 4 + i) * 81 + 9 * q;
+#pragma unroll
+      for (int s2 = 0; s2 < 9; ++s2) av[i][s2] = on[i] ? __ldg(am + s2) : 0.f;
+    }
+    sei_cp_async_wait<0>();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      float4* xr = reinterpret_cast<float4*>(X + ((size_t)i * 128 + r) * FP);
       float s[F];
       if (on[i]) {
         float t[FP];
-        sei_load_col<FP>(A.trace + ((size_t)(nb * 4 + (rl & 3)) * 9 + q) * FP, t);
-        applyTraceMap<ORD>(rl >> 2, t, s);
+#pragma unroll
+        for (int m4 = 0; m4 < FP / 4; ++m4) {
+          const float4 v = xr[m4];
+          t[4 * m4] = v.x;
+          t[4 * m4 + 1] = v.y;
+          t[4 * m4 + 2] = v.z;
+          t[4 * m4 + 3] = v.w;
+        }
+        applyTraceMap<ORD>(hs[i], t, s);
       } else {
 #pragma unroll
         for (int m = 0; m < F; ++m) s[m] = 0.f;
       }
-      float4* xr = reinterpret_cast<float4*>(X + ((size_t)i * 128 + r) * FP);
 #pragma unroll
       for (int m4 = 0; m4 < FP / 4; ++m4)
         xr[m4] = make_float4(4 * m4 < F ? s[4 * m4 < F ? 4 * m4 : 0] : 0.f,
@@ -393,10 +439,6 @@ __global__ void __launch_bounds__(128, 3) sei_nb_tc(sei::TcNbArgs A) {
     float E[4 * F];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      float av[9];
-      const float* am = A.aminus + ((size_t)cl * 4 + i) * 81 + 9 * q;
-#pragma unroll
-      for (int s2 = 0; s2 < 9; ++s2) av[s2] = on[i] ? __ldg(am + s2) : 0.f;
 #pragma unroll
       for (int m = 0; m < F; ++m) E[i * F + m] = 0.f;
 #pragma unroll
@@ -408,7 +450,7 @@ __global__ void __launch_bounds__(128, 3) sei_nb_tc(sei::TcNbArgs A) {
           const float xv[4] = {x.x, x.y, x.z, x.w};
 #pragma unroll
           for (int u = 0; u < 4; ++u)
-            if (4 * m4 + u < F) E[i * F + 4 * m4 + u] = fmaf(xv[u], av[s2], E[i * F + 4 * m4 + u]);
+            if (4 * m4 + u < F) E[i * F + 4 * m4 + u] = fmaf(xv[u], av[i][s2], E[i * F + 4 * m4 + u]);
         }
       }
     }
@@ -420,6 +462,8 @@ __global__ void __launch_bounds__(128, 3) sei_nb_tc(sei::TcNbArgs A) {
     __syncthreads();
     sei_tc::fenceAfterSync();
     if (tid == 0) issueSplit(taddr, aHi, aLo, K2, rdHi, rdLo, K2, K2 / 16, sei_tc::idescF16(128, N2), &mbar);
+    if (pfNb >= 0 && pfNb < A.n)
+      sei_tc::prefetchL2(A.trace + ((size_t)(pfRl & 3) * A.n + pfNb) * 9 * FP, (uint32_t)(9 * FP * 4));
     float acc[Bp];
     sei_load_col<Bp>(A.Q + ((size_t)cl * 9 + q) * Bp, acc);
     ok = sei_tc::mbarWait(&mbar, phase, kMaxPolls) && ok;

@@ -14,11 +14,14 @@ from tests.helpers import rel_l2_per_quantity, seeded_dofs
 pytestmark = pytest.mark.gpu
 
 PREC_F16X3 = 1
+OPT_TC_LOCAL = 3
 
 
-def _ctx(order, precision, dims=(4, 4, 4), seed=3):
+def _ctx(order, precision, dims=(4, 4, 4), seed=3, tc_local=False):
     from seissol_gb300 import Context
     ctx = Context(order, device=0, precision=precision)
+    if tc_local:
+        ctx.set_option(OPT_TC_LOCAL, 1)
     n = ctx.build_periodic_cube(*dims, perturb=0.1, seed=seed)
     q0 = seeded_dofs(n, order, seed)
     ctx.set_dofs(q0)
@@ -27,7 +30,7 @@ def _ctx(order, precision, dims=(4, 4, 4), seed=3):
 
 @pytest.mark.parametrize("order", [4, 5, 6])
 def test_local_integral_tensor_cores(built_lib, order):
-    ctx, n, q0 = _ctx(order, PREC_F16X3)
+    ctx, n, q0 = _ctx(order, PREC_F16X3, tc_local=True)
     cells = ctx.get_cells()
     dt = ctx.cfl_timestep(0.5)
     ctx.compute_ader(dt)
@@ -69,9 +72,9 @@ def test_neighbor_tensor_cores(built_lib, order):
     ctx.close()
 
 
-@pytest.mark.parametrize("order", [4, 6])
-def test_ten_steps_mixed_precision(built_lib, order):
-    ctx, n, q0 = _ctx(order, PREC_F16X3)
+@pytest.mark.parametrize("order,tc_local", [(4, False), (6, False), (4, True), (6, True)])
+def test_ten_steps_mixed_precision(built_lib, order, tc_local):
+    ctx, n, q0 = _ctx(order, PREC_F16X3, tc_local=tc_local)
     cells = ctx.get_cells()
     dt = ctx.cfl_timestep(0.5)
     q_ref = oracle_py.Oracle(order).steps(q0, cells["star"].astype(np.float64), cells["AplusT"].astype(np.float64),
