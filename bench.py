@@ -467,6 +467,8 @@ def kname(kind, path):
         return f"sei_lint_tc<{ORDER}>"
     if kind == "neighbor" and path != "fp32":
         return f"sei_nb_tc<{ORDER}>"
+    if kind == "lint" and path == "f16x3":
+        return f"sei_lint_trace_o{ORDER}"
     return f"sei_{kind}_o{ORDER}"
 
 

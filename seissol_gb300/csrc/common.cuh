@@ -82,10 +82,9 @@ __device__ __forceinline__ void sei_stage_trace(float* sm, int lane, int q, cons
 }
 
 // Coalesced 16-byte store of the staged face-f traces of a CPB-cell block to trace[4][n][9][FP].
-// Out of line and not unrolled: the generated kernels are large and their instruction cache is
-// the limit.
+// Not unrolled: the generated kernels are large and their instruction cache is the limit.
 template <int B, int F, int FP, int CPB>
-__device__ __noinline__ void sei_store_traces(int n, const float* sm, float* trace, int f) {
+__device__ __forceinline__ void sei_store_traces(int n, const float* sm, float* trace, int f) {
   constexpr int R4 = 9 * FP / 4;  // float4 per cell
   const float* st = sm + 9 * B * 32;
   const int cell0 = blockIdx.x * CPB;
