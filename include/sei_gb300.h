@@ -221,7 +221,7 @@ int sei_lts_run(sei_ctx* ctx, int ncycles);
 int sei_lts_clusters(sei_ctx* ctx, int* nclusters, int64_t* start, double* dt);
 int sei_lts_permutation(sei_ctx* ctx, int64_t* perm /*[n]*/);
 
-/* ---- dynamic rupture (built with fault_plane >= 0; order <= 4, i.e. at most 32 face points) ----
+/* ---- dynamic rupture (built with fault_plane >= 0; orders 4-6: (order + 1)^2 = 25, 36, 49 face points) ----
  * Replaces DynamicRupture::spaceTimeInterpolation + FrictionSolver::evaluate + the DR branch of
  * Neighbor::computeNeighborsIntegral (src/Kernels/DynamicRupture.cpp:57-168,
  * src/DynamicRupture/FrictionLaws/FrictionSolver.h:38-44, src/Kernels/LinearCK/Neighbor.cpp:91-101).

@@ -43,6 +43,8 @@ def _deps(src):
     base = os.path.basename(src)
     if base.startswith("kernels_"):
         deps.append(os.path.join(GEN, base.replace(".cu", ".cuh")))
+    if base.startswith("dr_"):
+        deps += [os.path.join(GEN, f"dr_tables_o{o}.cuh") for o in ORDERS]
     if base.startswith("tc_"):
         deps += [os.path.join(GEN, f"{n}_o{o}.cuh") for n in ("tc_tables", "tc_nb") for o in ORDERS]
     return deps
@@ -71,7 +73,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     os.makedirs(OBJ, exist_ok=True)
     gen_kernels.write_all(GEN, ORDERS)
     gen_visco.write_all(GEN)
-    gen_kernels.write_dr_tables(GEN, (4,))
+    gen_kernels.write_dr_tables(GEN, ORDERS)
     gen_kernels.write_tc_tables(GEN, ORDERS)
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=jobs or min(len(srcs), os.cpu_count() or 4)) as ex:

@@ -774,7 +774,7 @@ int sei_last_run_ms(sei_ctx* c, double* ms) {
   return SEI_OK;
 }
 
-int sei_dr_num_points(int order) { return (order >= 2 && order <= 4) ? sei::drNumPoints(order) : 0; }
+int sei_dr_num_points(int order) { return (order >= 2 && order <= 6) ? sei::drNumPoints(order) : 0; }
 
 int64_t sei_dr_num_faces(const sei_ctx* c) { return (c && c->has_fault) ? c->fault.nf : 0; }
 
@@ -783,7 +783,6 @@ int sei_dr_setup(sei_ctx* c, const sei_rs_params* p, int64_t* nfaces) {
   if (rc) return rc;
   if (!p) return fail(c, SEI_ERR_ARG, "null parameters");
   if (!c->has_fault) return fail(c, SEI_ERR_STATE, "mesh has no fault (fault_plane < 0)");
-  if (c->cfg.order > 4) return fail(c, SEI_ERR_UNSUPPORTED, "dynamic rupture is built for order <= 4 (<= 32 face points)");
   if (!(p->a_min > 0) || p->a_max < p->a_min || !(p->v0 > 0) || !(p->l > 0) || !(p->vw > 0) || !(p->v_init > 0) ||
       p->max_newton <= 0 || p->max_outer <= 0 || !(p->newton_tol > 0) || !(p->state_tol > 0) || p->sn_max > 0)
     return fail(c, SEI_ERR_ARG, "invalid rate-and-state parameters");

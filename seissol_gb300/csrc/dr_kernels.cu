@@ -1,4 +1,5 @@
-// Dynamic-rupture face kernel: one warp per fault face.
+// Dynamic-rupture face kernel: one warp per fault face up to 32 face points (order 4), two warps
+// per face up to 64 points (orders 5 and 6: 36 and 49 points); one thread per point.
 //
 // Per face and time step (reference: src/Kernels/DynamicRupture.cpp:57-168 projectToDR,
 // src/DynamicRupture/FrictionLaws/GpuImpl/BaseFrictionSolver.h:133-236 evaluatePoint,
@@ -24,10 +25,11 @@
 #include "internal.h"
 #include "mlp.cuh"
 #include "_gen/dr_tables_o4.cuh"
+#include "_gen/dr_tables_o5.cuh"
+#include "_gen/dr_tables_o6.cuh"
 
 namespace {
 
-constexpr int kFacesPerBlock = 4;
 constexpr int kHidden = sei_mlp::kHidden;
 constexpr int kMlpParams = kHidden * 5 + kHidden + kHidden * kHidden + kHidden + kHidden + 1;
 constexpr double kAlmostZero = 1e-45;
@@ -179,29 +181,65 @@ __device__ double mlpGuess(const float* __restrict__ w, const float* nrm, double
   return sei_mlp::lnSlipRate(f, nrm[12], (double)out * nrm[11] + nrm[10]);
 }
 
+// Threads of one face (a multiple of the warp size covering the face points), faces per block.
+template <int NP>
+struct FaceGroup {
+  static constexpr int kThreads = NP <= 32 ? 32 : 64;
+  static constexpr int kFaces = 128 / kThreads;
+  static_assert(NP <= 64, "at most 64 points per face");
+};
+
+// Barrier of the threads of face slot fs: the warp itself, or named barrier 1 + fs of two warps.
+template <int TPF>
+__device__ __forceinline__ void faceSync(int fs) {
+  if constexpr (TPF == 32) {
+    __syncwarp();
+  } else {
+    asm volatile("bar.sync %0, %1;\n" ::"r"(1 + fs), "n"(TPF) : "memory");
+  }
+}
+
+// True when c holds on every thread of the face.  Two-warp faces vote through shared memory;
+// the flags alternate with the parity of the call so that one barrier per vote suffices.
+template <int TPF>
+__device__ __forceinline__ bool faceAll(bool c, int fs, int t, int parity, int (*flags)[2][2]) {
+  const bool w = __all_sync(0xffffffffu, c);
+  if constexpr (TPF == 32) {
+    return w;
+  } else {
+    if ((t & 31) == 0) flags[fs][parity][t >> 5] = w;
+    faceSync<TPF>(fs);
+    return flags[fs][parity][0] && flags[fs][parity][1];
+  }
+}
+
 template <int N, int B, int NP>
-__global__ void __launch_bounds__(32 * kFacesPerBlock)
+__global__ void __launch_bounds__(128)
     sei_dr_faces(sei::DrArgs A, const float* __restrict__ V3m, const float* __restrict__ TW,
                  const double* __restrict__ R) {
+  constexpr int TPF = FaceGroup<NP>::kThreads, FPB = FaceGroup<NP>::kFaces;
   constexpr int Bp = (B + 3) / 4 * 4;
   constexpr int kQsel[6] = {0, 3, 5, 6, 7, 8};
   int dsz = 0;
 #pragma unroll
   for (int i = 0; i < N; ++i) dsz += (N - i) * (N - i + 1) * (N - i + 2) / 6 * 9;
-  __shared__ float sI[kFacesPerBlock][B * 9];
-  __shared__ float sJ[kFacesPerBlock][B * 9];
-  __shared__ float sG[kFacesPerBlock][NP * 9];
-  __shared__ double sD[kFacesPerBlock][32];
+  __shared__ float sI[FPB][B * 9];
+  __shared__ float sJ[FPB][B * 9];
+  __shared__ float sG[FPB][NP * 9];
+  __shared__ double sD[FPB][TPF];
+  __shared__ int sVote[FPB][2][2];
   __shared__ float sW[kMlpParams];
   const bool useMlp = A.mlp != nullptr;
   if (useMlp)
     for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) sW[i] = A.mlp[i];
   __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int f = blockIdx.x * kFacesPerBlock + warp;
+  // face slot and thread of the face (every thread of a face leaves or stays together)
+  const int warp = threadIdx.x / TPF, lane = threadIdx.x % TPF;
+  const int f = blockIdx.x * FPB + warp;
   if (f >= A.nfaces) return;
   const bool pt = lane < NP;
   const int k = pt ? lane : 0;
+  int votes = 0;
 
   // ---- 1. space-time interpolation of both sides (six quantities needed per point)
   float qi[2][N][6];
@@ -214,7 +252,7 @@ __global__ void __launch_bounds__(32 * kFacesPerBlock)
     const float* V = V3m + (size_t)combo * NP * B;
 #pragma unroll 1
     for (int s = 0; s < N; ++s) {
-      for (int e = lane; e < B * 9; e += 32) {
+      for (int e = lane; e < B * 9; e += TPF) {
         const int l = e % B, q = e / B;
         float v = 0.f;
         int off = 0;
@@ -226,22 +264,22 @@ __global__ void __launch_bounds__(32 * kFacesPerBlock)
         }
         sI[warp][q * B + l] = v;
       }
-      __syncwarp();
-      for (int e = lane; e < B * 9; e += 32) {
+      faceSync<TPF>(warp);
+      for (int e = lane; e < B * 9; e += TPF) {
         const int l = e % B, p = e / B;
         float v = 0.f;
 #pragma unroll
         for (int q = 0; q < 9; ++q) v = fmaf(sI[warp][q * B + l], __ldg(T + q + 9 * p), v);
         sJ[warp][p * B + l] = v;
       }
-      __syncwarp();
+      faceSync<TPF>(warp);
 #pragma unroll
       for (int j = 0; j < 6; ++j) {
         float v = 0.f;
         for (int l = 0; l < B; ++l) v = fmaf(__ldg(V + k * B + l), sJ[warp][kQsel[j] * B + l], v);
         qi[sd][s][j] = v;
       }
-      __syncwarp();
+      faceSync<TPF>(warp);
     }
   }
 
@@ -315,7 +353,7 @@ __global__ void __launch_bounds__(32 * kFacesPerBlock)
         vmag = r.v;
         mu = r.mu;
       }
-      if (__all_sync(0xffffffffu, conv)) break;
+      if (faceAll<TPF>(conv, warp, lane, votes++ & 1, sVote)) break;
     }
     if (pt) {
       psib = stateUpdate(A, inv, a, sref, dt, lsr);
@@ -348,7 +386,7 @@ __global__ void __launch_bounds__(32 * kFacesPerBlock)
 
   // ---- 3. resample the state-variable increment over the face
   sD[warp][lane] = pt ? psib - psiStored : 0.0;
-  __syncwarp();
+  faceSync<TPF>(warp);
   if (pt) {
     double v = 0.0;
     for (int j = 0; j < NP; ++j) v += R[k * NP + j] * sD[warp][j];
@@ -383,26 +421,27 @@ __global__ void __launch_bounds__(32 * kFacesPerBlock)
         sG[warp][k * 9 + p] = g;
       }
     }
-    __syncwarp();
+    faceSync<TPF>(warp);
     const int cell = sd == 0 ? A.plus_cell[f] : A.minus_cell[f];
     const int combo = sd == 0 ? A.plus_side[f] * 4 : A.minus_side[f] * 4 + A.rel[f];
     const float* W = TW + (size_t)combo * B * NP;
     float* q = A.Q + (size_t)cell * 9 * Bp;
-    for (int e = lane; e < B * 9; e += 32) {
+    for (int e = lane; e < B * 9; e += TPF) {
       const int l = e % B, p = e / B;
       float v = 0.f;
       for (int kk = 0; kk < NP; ++kk) v = fmaf(__ldg(W + l * NP + kk), sG[warp][kk * 9 + p], v);
       q[p * Bp + l] += v;
     }
-    __syncwarp();
+    faceSync<TPF>(warp);
   }
 }
 
 template <int N, int B, int NP>
 int launch(const sei::DrArgs& a, const float* v3m, const float* tw, const double* res, void* stream) {
   if (a.nfaces <= 0) return 0;
-  const int blocks = (a.nfaces + kFacesPerBlock - 1) / kFacesPerBlock;
-  sei_dr_faces<N, B, NP><<<blocks, 32 * kFacesPerBlock, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
+  constexpr int FPB = FaceGroup<NP>::kFaces;
+  const int blocks = (a.nfaces + FPB - 1) / FPB;
+  sei_dr_faces<N, B, NP><<<blocks, 128, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -420,8 +459,8 @@ namespace sei {
 int drNumPoints(int order) { return (order + 1) * (order + 1); }
 
 int launchDrFaces(int order, const DrArgs& a, void* stream) {
-  // One lane per face point: built for order 4 (25 points).  Device addresses of the
-  // generated tables are looked up here (host code may not take them directly).
+  // One thread per face point: orders 4 (25 points), 5 (36) and 6 (49).  Device addresses of
+  // the generated tables are looked up here (host code may not take them directly).
   void *v = nullptr, *t = nullptr, *r = nullptr;
   switch (order) {
     case 4:
@@ -429,6 +468,16 @@ int launchDrFaces(int order, const DrArgs& a, void* stream) {
           cudaGetSymbolAddress(&r, sei_dr_o4::kResample))
         return -1;
       return launch<4, 20, 25>(a, (const float*)v, (const float*)t, (const double*)r, stream);
+    case 5:
+      if (cudaGetSymbolAddress(&v, sei_dr_o5::kV3m) || cudaGetSymbolAddress(&t, sei_dr_o5::kTW) ||
+          cudaGetSymbolAddress(&r, sei_dr_o5::kResample))
+        return -1;
+      return launch<5, 35, 36>(a, (const float*)v, (const float*)t, (const double*)r, stream);
+    case 6:
+      if (cudaGetSymbolAddress(&v, sei_dr_o6::kV3m) || cudaGetSymbolAddress(&t, sei_dr_o6::kTW) ||
+          cudaGetSymbolAddress(&r, sei_dr_o6::kResample))
+        return -1;
+      return launch<6, 56, 49>(a, (const float*)v, (const float*)t, (const double*)r, stream);
     default:
       return -1;
   }
