@@ -364,7 +364,7 @@ def visco_measurement(local, steps):
             "step_model_frac": n * steps / (ms / 1e3) * 23744 / (hbm * 1e9)}
 
 
-def dr_measurement(local, steps):
+def dr_measurement(local, steps, order=4, dims=None, plane=3, warm_precision=0, perturb=0.0):
     """Dynamic rupture on the fault workload: elastic order 4, 300,000 tets, a planar fault of
     20,000 faces (25 points each), fast-velocity-weakening friction with a ~ U[0.008, 0.02],
     sn ~ U[-120, -40] MPa, tau ~ U[20, 75] MPa, V_init = 1e-16 m/s, kernel all_dr.
@@ -378,12 +378,15 @@ def dr_measurement(local, steps):
 
     from seissol_gb300 import Context, RSParams
 
-    def make(seed):
-        ctx = Context(4, device=local)
-        n = ctx.build_periodic_cube(*DR_DIMS, perturb=0.0, seed=seed, fault_plane=3)
+    dims = dims or DR_DIMS
+    nb3 = order * (order + 1) * (order + 2) // 6
+
+    def make(seed, precision=0):
+        ctx = Context(order, device=local, precision=precision)
+        n = ctx.build_periodic_cube(*dims, perturb=perturb, seed=seed, fault_plane=plane)
         nf = ctx.dr_setup(RSParams.fault_config(seed=seed + 2))
         rng = np.random.default_rng(seed)
-        ctx.set_dofs(rng.uniform(-1, 1, (n, 9, 20)).astype(np.float32))
+        ctx.set_dofs(rng.uniform(-1, 1, (n, 9, nb3)).astype(np.float32))
         return ctx, n, nf
 
     # training samples from the plain solve along a whole run of the training fault: 40,000
@@ -408,9 +411,12 @@ def dr_measurement(local, steps):
     out = {}
     states, early = {}, {}
     k_early = min(20, steps)
-    for mode in ("plain", "warm"):
-        ctx, n, nf = make(DR_SEED + 1)
-        if mode == "warm":
+    # with a mixed-precision warm arm, an FP32 warm arm isolates the warm start's effect on the
+    # converged slip rates from that of the arithmetic
+    modes = ("plain", "warm") + (("warm_fp32",) if warm_precision else ())
+    for mode in modes:
+        ctx, n, nf = make(DR_SEED + 1, warm_precision if mode == "warm" else 0)
+        if mode != "plain":
             ctx.mlp_set(params, norm)
             ctx.dr_warm_start(True)
         ctx.dr_reset_counters()
@@ -427,16 +433,26 @@ def dr_measurement(local, steps):
         ctx.set_profiling(True)
         ctx.run("all_dr", dt, 1)
         ctx.sync()
-        fault_ms = ctx.kernel_times_by_kind()["fault"][0]
+        by_kind = ctx.kernel_times_by_kind()
+        fault_ms = by_kind["fault"][0]
+        step_kernels = {k: v[0] for k, v in by_kind.items() if v[1] > 0}
         ctx.close()
         out[mode] = {"ms_per_step": ms / steps, "cell_updates_per_s": n * steps / (ms / 1e3),
                      "face_updates_per_s": nf * steps / (ms / 1e3), "fault_kernel_ms": fault_ms,
+                     "kernel_ms_one_step": step_kernels,
                      "newton_iters_per_point_step": tot / (npts * steps),
                      "first_solve_iters_per_point_step": first / (npts * steps)}
-    vp, vw = states["plain"], states["warm"]
-    return {"workload": "elastic order 4, 300,000-tet periodic cube 6x100x100 cubes, planar fault of 20,000 faces "
-                        "x 25 points, FVW rate-and-state (a ~ U[0.008,0.02], sn ~ U[-120,-40] MPa, tau ~ U[20,75] MPa, "
+    same = "warm_fp32" if warm_precision else "warm"
+    vp, vw = states["plain"], states[same]
+    return {"workload": f"elastic order {order}, {n:,}-tet periodic cube {dims[0]}x{dims[1]}x{dims[2]} cubes "
+                        f"(material +-{round(100 * perturb)}%), planar fault of {nf:,} faces x {(order + 1) ** 2} "
+                        "points, FVW rate-and-state (a ~ U[0.008,0.02], sn ~ U[-120,-40] MPa, tau ~ U[20,75] MPa, "
                         f"V_init 1e-16), kernel all_dr, {steps} steps from the initial state",
+            "plain_path": "fp32", "warm_path": "f16x3" if warm_precision else "fp32",
+            **({"warm_start_fp32": out["warm_fp32"],
+                "mixed_warm_vs_plain_speedup": out["plain"]["ms_per_step"] / out["warm"]["ms_per_step"],
+                "max_rel_dV_mixed_warm_vs_plain": float((np.abs(vp - states["warm"]) / np.maximum(vp, 1e-30)).max())}
+               if warm_precision else {}),
             "cells": n, "faces": nf, "steps": steps, "plain": out["plain"], "warm_start": out["warm"],
             "first_solve_iteration_ratio": out["plain"]["first_solve_iters_per_point_step"]
             / max(out["warm"]["first_solve_iters_per_point_step"], 1e-30),
@@ -444,8 +460,9 @@ def dr_measurement(local, steps):
             / max(out["warm"]["newton_iters_per_point_step"], 1e-30),
             "max_abs_dV": float(np.abs(vp - vw).max()),
             "max_rel_dV": float((np.abs(vp - vw) / np.maximum(vp, 1e-30)).max()),
-            f"max_rel_dV_after_{k_early}_steps": float((np.abs(early["plain"] - early["warm"])
+            f"max_rel_dV_after_{k_early}_steps": float((np.abs(early["plain"] - early[same])
                                                          / np.maximum(early["plain"], 1e-30)).max()),
+            "dV_between": f"plain and {same} (same arithmetic)",
             "dV_note": "plain and warm-started runs are separate trajectories: every solve converges to the "
                        "Newton tolerance, and the tolerance-level differences feed back through the wave field "
                        "over the run",
@@ -588,6 +605,12 @@ def run_ours(args, world, rank, local):
     vis = None
     if rank == 0 and args.visco_steps > 0:
         vis = visco_measurement(local, args.visco_steps)
+    comb = None
+    if rank == 0 and args.combined_steps > 0:
+        # order 6, 1,000,000 tets, 50,000-face fault: plain = FP32 + plain Newton, warm = mixed
+        # path + learned Newton start; global time stepping (LTS with a fault is not built)
+        comb = dr_measurement(local, args.combined_steps, order=6, dims=(8, 100, 250), plane=4, warm_precision=1,
+                              perturb=PERTURB)
 
     base = acc = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -607,7 +630,7 @@ def run_ours(args, world, rank, local):
                            "parallelism": f"replicas x{world}"},
                 "roofline": roof, "cpu_baseline": base, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": launches, "kernel_ms_per_step": kernels, "paths": paths_out,
-                "mixed_vs_fp32": ratio, "accuracy": acc, "dynamic_rupture": dr,
+                "mixed_vs_fp32": ratio, "accuracy": acc, "dynamic_rupture": dr, "combined_o6_fault": comb,
                 "local_time_stepping": lts, "viscoelastic": vis}
         print(json.dumps(line))
     return 0
@@ -627,6 +650,8 @@ def main():
     ap.add_argument("--tc-local", action="store_true", help="f16x3: local integral on the tensor cores too")
     ap.add_argument("--dr-steps", type=int, default=200,
                     help="steps of the dynamic-rupture measurement (plain and warm-started); 0 skips it")
+    ap.add_argument("--combined-steps", type=int, default=10,
+                    help="steps of the combined order-6 measurement (1M tets, 50,000-face fault); 0 skips it")
     ap.add_argument("--visco-steps", type=int, default=20,
                     help="steps of the viscoelastic measurement; 0 skips it")
     ap.add_argument("--lts-cycles", type=int, default=10,

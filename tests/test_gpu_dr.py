@@ -18,9 +18,9 @@ FIELDS = dict(psi="psi", v1="slip_rate1", v2="slip_rate2", slip1="slip1", slip2=
               trac1="traction1", trac2="traction2")
 
 
-def _setup(seed=3, order=4):
+def _setup(seed=3, order=4, precision=0):
     from seissol_gb300 import Context, RSParams
-    ctx = Context(order, device=0)
+    ctx = Context(order, device=0, precision=precision)
     n = ctx.build_periodic_cube(8, 4, 4, perturb=0.0, seed=seed, fault_plane=4)
     rs = RSParams.fault_config(seed=seed + 2)
     ctx.dr_setup(rs)
@@ -44,9 +44,10 @@ def _compare_state(ctx, state, tol_v=1e-4):
     assert rel_l2(ctx.dr_state("slip"), state["slip"]) < tol_v
 
 
-@pytest.mark.parametrize("order", [4, 5, 6])
-def test_dr_one_step(built_lib, order):
-    ctx, n, q0, cells, faces, state, a, init, params = _setup(order=order)
+@pytest.mark.parametrize("order,precision", [(4, 0), (5, 0), (6, 0), (6, 1)])
+def test_dr_one_step(built_lib, order, precision):
+    """precision 1: the mixed path (tensor-core neighbour flux beside the fault kernel)."""
+    ctx, n, q0, cells, faces, state, a, init, params = _setup(order=order, precision=precision)
     dt = ctx.cfl_timestep(0.5)
     o = oracle_py.Oracle(order)
     dro = oracle_py.DROracle(order, faces, params)
