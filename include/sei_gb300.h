@@ -76,7 +76,8 @@ typedef struct sei_cube_params {
   uint64_t seed;
   int fault_plane;
   /* > 1: graded tensor-product cube; along each direction the cube edges are drawn
-   * log-uniformly in [h, grading h] (seeded); <= 1: uniform edge h */
+   * log-uniformly in [h, grading h] (seeded), except along x when the cube carries the fault
+   * (fault_plane >= 0), whose x edges stay h; <= 1: uniform edge h */
   double grading;
 } sei_cube_params;
 
@@ -213,7 +214,10 @@ int sei_fit_attenuation(double qp, double qs, double freq_central, double freq_r
  * neighbours at most one cluster apart) and reorders the cells by cluster (stable; the DOFs move
  * with their cells; sei_lts_permutation gives new -> old).  A face reads its neighbour's
  * time-integrated DOFs (same cluster), integration buffer (finer neighbour) or the Taylor integral
- * of its derivatives over the sub-interval (coarser neighbour).  Not built with a fault. */
+ * of its derivatives over the sub-interval (coarser neighbour).  With a fault (sei_dr_setup
+ * first; a fault cannot be set up after this call) both cells of every fault face share one
+ * cluster, the lower, and each cluster's correction runs the fault step of its faces over its own
+ * time step before its neighbour flux (TimeCluster.cpp:804-823). */
 int sei_lts_setup(sei_ctx* ctx, double cfl, int max_clusters, int* nclusters);
 /* Advances every cluster by dt0 2^(nclusters-1) per cycle (asynchronous; sei_last_run_ms times it). */
 int sei_lts_run(sei_ctx* ctx, int ncycles);

@@ -224,10 +224,11 @@ def dr_full_step(o, dro, Q, cells, faces, state, a, init, dt, mlp=None, record=N
 # Local time stepping, rate 2 (test infrastructure: FP64 restatement)
 # ---------------------------------------------------------------------------
 
-def lts_clusters(dt, neighbor, face_type, max_clusters):
+def lts_clusters(dt, neighbor, face_type, max_clusters, fault_cells=None):
     """Cluster k holds the cell time steps in [2^k dt0, 2^{k+1} dt0), capped at max_clusters - 1,
-    then neighbouring clusters are lowered until they differ by at most one (maximum difference
-    property, docs/local-timestepping.rst)."""
+    then neighbouring clusters are lowered until they differ by at most one, and the two cells of
+    every dynamic-rupture face (fault_cells [nf, 2]) share the lower cluster (maximum difference
+    property, docs/local-timestepping.rst:91-96)."""
     dt = np.asarray(dt, np.float64)
     dt0 = dt.min()
     cl = np.clip(np.floor(np.log2(dt / dt0) + 1e-12).astype(np.int64), 0, max_clusters - 1)
@@ -236,13 +237,41 @@ def lts_clusters(dt, neighbor, face_type, max_clusters):
     while True:
         lim = np.where(regular, cl[np.where(regular, nb, 0)] + 1, np.iinfo(np.int64).max).min(axis=1)
         new = np.minimum(cl, lim)
+        if fault_cells is not None:
+            pa, pb = fault_cells[:, 0], fault_cells[:, 1]
+            m = np.minimum(new[pa], new[pb])
+            new[pa] = m
+            new[pb] = m
         if np.array_equal(new, cl):
             return cl, dt0
         cl = new
 
 
-def lts_cycles(o, Q, cells, cluster, dt0, ncycles):
+def _dr_cluster_step(o, dr, Q, derivs, fsel, dt):
+    """The fault step of the faces fsel over one step dt of their cluster, from the derivatives
+    stored at the start of that step; updates dr["state"] in place and returns Q."""
+    faces, params = dr["faces"], dr["params"]
+    sub = {k: np.asarray(v)[fsel] for k, v in faces.items()}
+    dro = DROracle(o.order, sub, params)
+    state = {k: np.ascontiguousarray(v[fsel]) for k, v in dr["state"].items()}
+    tp, tw, deltat, coll = dr_collocation(o.order, dt)
+    pc, mc = sub["cells"][:, 0], sub["cells"][:, 1]
+    ps, ms, rel = sub["sides"][:, 0], sub["sides"][:, 1], sub["sides"][:, 2]
+    qip = dro.interpolate(derivs[pc], ps, np.zeros_like(ps), coll)
+    qim = dro.interpolate(derivs[mc], ms, rel, coll)
+    isp, ism, _ = dro.friction(qip, qim, state, dr["a"][fsel], dr["init"][fsel], deltat, tw)
+    for k, v in state.items():
+        dr["state"][k][fsel] = v
+    Q = dro.nodal_flux(Q, pc, ps, np.zeros_like(ps), isp, sub["fluxSolverPlus"])
+    return dro.nodal_flux(Q, mc, ms, rel, ism, sub["fluxSolverMinus"])
+
+
+def lts_cycles(o, Q, cells, cluster, dt0, ncycles, dr=None):
     """Rate-2 LTS (TimeCluster.cpp:358-440, 695-717; TimeCommon.cpp:40-87) in FP64.
+
+    dr (optional): {"faces", "params", "state", "a", "init"} of a fault whose faces join their
+    cells' cluster: each cluster's correction runs the fault step of its faces over its own time
+    step before the neighbour flux (TimeCluster.cpp:804-823); dr["state"] is updated in place.
 
     Every cycle advances all clusters by dt0 2^(C-1).  At sub-step k of the finest cluster the
     clusters whose step starts there predict (ADER with derivatives, integration buffer of cells
@@ -305,5 +334,9 @@ def lts_cycles(o, Q, cells, cluster, dt0, ncycles):
                         faces[coarser, f] = o.taylor(derivs[nbs[coarser]], sub)
                 pool = faces.reshape((-1,) + Q.shape[1:])
                 pidx = np.arange(idx.size * 4, dtype=np.int32).reshape(idx.size, 4)
+                if dr is not None:
+                    fsel = np.nonzero(cluster[dr["faces"]["cells"][:, 0]] == c)[0]
+                    if fsel.size:
+                        Q = _dr_cluster_step(o, dr, Q, derivs, fsel, dt0 * ln)
                 Q[idx] = o.neighbor(Q[idx], pool, aminus[idx], pidx, side[idx], orient[idx], ft[idx])
     return Q

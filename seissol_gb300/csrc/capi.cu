@@ -95,6 +95,8 @@ struct sei_ctx {
   int32_t* d_src = nullptr;                         // [n][4] pool block read through each face
   int32_t *d_bcell = nullptr, *d_bdst = nullptr;    // buffer entries, grouped by cluster
   int32_t *d_gsrc = nullptr, *d_gdst = nullptr;     // gather entries (derivative slot -> pool block)
+  int32_t* d_fidx = nullptr;                        // fault faces grouped by cluster
+  std::vector<int64_t> f_start;                     // [ncl + 1] ranges of d_fidx
   // viscoelastic (sei_visco_setup): 27 quantities per cell in Q and I
   int nq = 9;
   bool visco = false;
@@ -118,6 +120,13 @@ int cudaFail(sei_ctx* c, cudaError_t e, const char* what) {
   return fail(c, SEI_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// A recorded LTS cycle graph holds the fault kernel's arguments (network, sample buffer); calls
+// that change them drop the graph, which the next sei_lts_run records again.
+void dropLtsGraph(sei_ctx* c) {
+  if (c->lts_exec) cudaGraphExecDestroy(c->lts_exec);
+  c->lts_exec = nullptr;
+}
+
 #define SEI_CUDA(call)                                   \
   do {                                                   \
     cudaError_t e_ = (call);                             \
@@ -138,13 +147,13 @@ void freeArrays(sei_ctx* c) {
   cudaFree(c->d_trace);
   c->d_trace = nullptr;
   c->trace_valid = false;
-  for (void* p : {(void*)c->d_src, (void*)c->d_bcell, (void*)c->d_bdst, (void*)c->d_gsrc, (void*)c->d_gdst,
+  for (void* p : {(void*)c->d_src, (void*)c->d_bcell, (void*)c->d_bdst, (void*)c->d_gsrc, (void*)c->d_gdst, (void*)c->d_fidx,
                   (void*)c->d_grad, (void*)c->d_theta, (void*)c->d_wplus, (void*)c->d_wminus})
     cudaFree(p);
   c->d_grad = c->d_theta = c->d_wplus = c->d_wminus = nullptr;
   c->visco = false;
   c->nq = 9;
-  c->d_src = c->d_bcell = c->d_bdst = c->d_gsrc = c->d_gdst = nullptr;
+  c->d_src = c->d_bcell = c->d_bdst = c->d_gsrc = c->d_gdst = c->d_fidx = nullptr;
   if (c->lts_exec) cudaGraphExecDestroy(c->lts_exec);
   c->lts_exec = nullptr;
   c->lts = false;
@@ -318,6 +327,9 @@ sei::DrArgs drArgs(sei_ctx* c, double dt) {
   sei::DrArgs a{};
   const int64_t nf = c->fault.nf, np = c->npts;
   a.nfaces = (int)nf;
+  a.fidx = nullptr;
+  a.face_begin = 0;
+  a.face_count = (int)nf;
   a.plus_cell = c->d_pc;
   a.minus_cell = c->d_mc;
   a.plus_side = c->d_ps;
@@ -783,6 +795,7 @@ int sei_dr_setup(sei_ctx* c, const sei_rs_params* p, int64_t* nfaces) {
   if (rc) return rc;
   if (!p) return fail(c, SEI_ERR_ARG, "null parameters");
   if (!c->has_fault) return fail(c, SEI_ERR_STATE, "mesh has no fault (fault_plane < 0)");
+  if (c->lts) return fail(c, SEI_ERR_STATE, "set up dynamic rupture before local time stepping");
   if (!(p->a_min > 0) || p->a_max < p->a_min || !(p->v0 > 0) || !(p->l > 0) || !(p->vw > 0) || !(p->v_init > 0) ||
       p->max_newton <= 0 || p->max_outer <= 0 || !(p->newton_tol > 0) || !(p->state_tol > 0) || p->sn_max > 0)
     return fail(c, SEI_ERR_ARG, "invalid rate-and-state parameters");
@@ -959,6 +972,7 @@ int sei_mlp_num_params(void) { return sei::mlpNumParams(); }
 
 int sei_dr_record_samples(sei_ctx* c, int64_t capacity) {
   if (!c || capacity < 0 || capacity > (int64_t)1 << 31) return SEI_ERR_ARG;
+  dropLtsGraph(c);
   if (c->cfg.device < 0) return fail(c, SEI_ERR_STATE, "host-only context");
   cudaFree(c->d_rec);
   cudaFree(c->d_rec_count);
@@ -1127,6 +1141,7 @@ int sei_mlp_train(sei_ctx* c, const float* samples, int64_t n, int steps, float 
   cudaFree(c->d_mlp);
   c->d_mlp = dP;
   std::memcpy(c->mlp_norm, norm, sizeof(norm));
+  dropLtsGraph(c);
   return SEI_OK;
 }
 
@@ -1139,6 +1154,7 @@ int sei_mlp_get(sei_ctx* c, float* params, float* norm) {
 }
 
 int sei_mlp_set(sei_ctx* c, const float* params, const float* norm) {
+  if (c) dropLtsGraph(c);
   if (!c || !params || !norm) return SEI_ERR_ARG;
   if (c->cfg.device < 0) return fail(c, SEI_ERR_STATE, "host-only context");
   if (!c->d_mlp && cudaMalloc(&c->d_mlp, sei::mlpNumParams() * 4) != cudaSuccess) return fail(c, SEI_ERR_OOM, "network");
@@ -1151,6 +1167,7 @@ int sei_dr_warm_start(sei_ctx* c, int on) {
   if (!c) return SEI_ERR_ARG;
   if (on && !c->d_mlp) return fail(c, SEI_ERR_STATE, "no trained network (sei_mlp_train or sei_mlp_set)");
   c->warm_start = on != 0;
+  dropLtsGraph(c);
   return SEI_OK;
 }
 
@@ -1327,7 +1344,8 @@ int sei_lts_setup(sei_ctx* c, double cfl, int max_clusters, int* nclusters) {
   if (rc) return rc;
   if (c->visco) return fail(c, SEI_ERR_UNSUPPORTED, "local time stepping of the viscoelastic equations is not built");
   if (!c->has_mesh) return fail(c, SEI_ERR_STATE, "local time stepping needs a mesh built by the context");
-  if (c->has_fault) return fail(c, SEI_ERR_UNSUPPORTED, "local time stepping with a fault is not built");
+  if (c->has_fault && !c->dr_ready)
+    return fail(c, SEI_ERR_STATE, "set up dynamic rupture (sei_dr_setup) before local time stepping");
   if (c->lts) return fail(c, SEI_ERR_STATE, "local time stepping is already set up");
   if (!(cfl > 0) || max_clusters < 1 || max_clusters > 16) return fail(c, SEI_ERR_ARG, "cfl > 0, 1 <= max_clusters <= 16");
   const int64_t n = c->n;
@@ -1341,9 +1359,19 @@ int sei_lts_setup(sei_ctx* c, double cfl, int max_clusters, int* nclusters) {
     int k = (int)std::floor(std::log2(dt[i] / dt0) + 1e-12);
     cl[i] = std::max(0, std::min(max_clusters - 1, k));
   }
-  // maximum difference property: neighbouring clusters differ by at most one
+  // maximum difference property: neighbouring clusters differ by at most one; both cells of a
+  // dynamic-rupture face share one cluster, the lower (docs/local-timestepping.rst:91-96)
+  const int64_t nf = c->dr_ready ? c->fault.nf : 0;
   for (bool changed = true; changed;) {
     changed = false;
+    for (int64_t f = 0; f < nf; ++f) {
+      const int32_t pa = c->fault.plus_cell[f], pb = c->fault.minus_cell[f];
+      const int m = std::min(cl[pa], cl[pb]);
+      if (cl[pa] != m || cl[pb] != m) {
+        cl[pa] = cl[pb] = m;
+        changed = true;
+      }
+    }
     for (int64_t i = 0; i < n; ++i)
       for (int f = 0; f < 4; ++f) {
         if (c->mesh.ftype[i * 4 + f] != 0) continue;
@@ -1366,8 +1394,18 @@ int sei_lts_setup(sei_ctx* c, double cfl, int max_clusters, int* nclusters) {
   SEI_CUDA(cudaMemcpy(qold.data(), c->Q, qold.size() * sizeof(float), cudaMemcpyDeviceToHost));
   for (int64_t i = 0; i < n; ++i)
     std::memcpy(&qnew[(size_t)i * blk], &qold[(size_t)order[i] * blk], blk * sizeof(float));
+  std::vector<int64_t> inv(n);
+  for (int64_t i = 0; i < n; ++i) inv[order[i]] = i;
   try {
     sei::permuteCells(c->mesh, order);
+    // the fault faces follow their cells; the recomputed face relations are regular, so the
+    // dynamic-rupture faces are marked again before the operators are built
+    for (int64_t f = 0; f < nf; ++f) {
+      c->fault.plus_cell[f] = (int32_t)inv[c->fault.plus_cell[f]];
+      c->fault.minus_cell[f] = (int32_t)inv[c->fault.minus_cell[f]];
+      c->mesh.ftype[(int64_t)c->fault.plus_cell[f] * 4 + c->fault.plus_side[f]] = 1;
+      c->mesh.ftype[(int64_t)c->fault.minus_cell[f] * 4 + c->fault.minus_side[f]] = 1;
+    }
     sei::buildOperators(c->mesh, c->h_star, c->h_aplus, c->h_aminus);
   } catch (const std::exception& e) {
     return fail(c, SEI_ERR_ARG, e.what());
@@ -1394,6 +1432,21 @@ int sei_lts_setup(sei_ctx* c, double cfl, int max_clusters, int* nclusters) {
     }
     if (coarser) bslot[i] = (int32_t)nB++;
     if (finer) dsl[i] = (int32_t)nD++;
+  }
+  // fault cells store their derivatives too (the fault kernel interpolates them in time), and
+  // the faces are listed by the cluster of their cells
+  std::vector<int32_t> pslot(nf), mslot(nf), fidx;
+  std::vector<int64_t> fst(ncl + 1, 0);
+  for (int64_t f = 0; f < nf; ++f)
+    for (int sd = 0; sd < 2; ++sd) {
+      const int32_t cc = sd ? c->fault.minus_cell[f] : c->fault.plus_cell[f];
+      if (dsl[cc] < 0) dsl[cc] = (int32_t)nD++;
+      (sd ? mslot : pslot)[f] = dsl[cc];
+    }
+  for (int k = 0; k < ncl; ++k) {
+    for (int64_t f = 0; f < nf; ++f)
+      if (cn[c->fault.plus_cell[f]] == k) fidx.push_back((int32_t)f);
+    fst[k + 1] = (int64_t)fidx.size();
   }
   // per-face sources; buffer and gather entries grouped by the cluster of the reading cell
   std::vector<int32_t> src((size_t)n * 4);
@@ -1450,6 +1503,12 @@ int sei_lts_setup(sei_ctx* c, double cfl, int max_clusters, int* nclusters) {
   if ((rc = upload(c, &c->dslot, dsl)) || (rc = upload(c, &c->d_src, src)) || (rc = upload(c, &c->d_bcell, fbc)) ||
       (rc = upload(c, &c->d_bdst, fbd)) || (rc = upload(c, &c->d_gsrc, fgs)) || (rc = upload(c, &c->d_gdst, fgd)))
     return rc;
+  if (nf > 0) {
+    if ((rc = upload(c, &c->d_fidx, fidx)) || (rc = upload(c, &c->d_pslot, pslot)) || (rc = upload(c, &c->d_mslot, mslot)) ||
+        (rc = upload(c, &c->d_pc, c->fault.plus_cell)) || (rc = upload(c, &c->d_mc, c->fault.minus_cell)))
+      return rc;
+  }
+  c->f_start = fst;
   c->lts = true;
   c->ncl = ncl;
   c->lts_dt0 = dt0;
@@ -1482,8 +1541,9 @@ sei::DeviceArrays rangeView(sei_ctx* c, int64_t s, int64_t e, bool neighbour) {
 
 // One cycle: every cluster advances by dt0 2^(ncl-1).  Sub-step k of the finest cluster starts
 // with the predictions (ADER, integration buffer, local integral) of the clusters whose step begins
-// at k, then the corrections (coarse-neighbour Taylor integrals, neighbour flux) of the clusters
-// whose step ends at k + 1 (TimeCluster predict / correct, TimeCommon::computeIntegrals).
+// at k, then the corrections (coarse-neighbour Taylor integrals, the fault faces of the cluster,
+// neighbour flux) of the clusters whose step ends at k + 1 (TimeCluster predict / correct,
+// TimeCommon::computeIntegrals).
 int ltsCycle(sei_ctx* c) {
   const int blk = 9 * c->Bp;
   const int64_t steps = (int64_t)1 << (c->ncl - 1);
@@ -1523,6 +1583,16 @@ int ltsCycle(sei_ctx* c) {
         if (rc) return rc;
         if (c->k.taylorGather((int)(ge - gs), c->d_gsrc + gs, c->d_gdst + gs, c->derivs, co, c->I, c->stream))
           return fail(c, SEI_ERR_CUDA, "LTS gather kernel launch failed");
+      }
+      // the fault faces of this cluster first (TimeCluster.cpp:804-823), over its own step
+      if (!c->f_start.empty() && c->f_start[cl + 1] > c->f_start[cl]) {
+        int rc = profMark(c, 2);
+        if (rc) return rc;
+        sei::DrArgs a = drArgs(c, c->lts_dt0 * (double)len);
+        a.fidx = c->d_fidx;
+        a.face_begin = (int)c->f_start[cl];
+        a.face_count = (int)(c->f_start[cl + 1] - c->f_start[cl]);
+        if (sei::launchDrFaces(c->cfg.order, a, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "fault kernel launch failed");
       }
       int rc = launchNeighbor(c, rangeView(c, s, e, true));
       if (rc) return rc;

@@ -235,8 +235,10 @@ __global__ void __launch_bounds__(128)
   __syncthreads();
   // face slot and thread of the face (every thread of a face leaves or stays together)
   const int warp = threadIdx.x / TPF, lane = threadIdx.x % TPF;
-  const int f = blockIdx.x * FPB + warp;
-  if (f >= A.nfaces) return;
+  const int fi = blockIdx.x * FPB + warp;
+  if (fi >= A.face_count) return;
+  const int f = A.fidx ? A.fidx[A.face_begin + fi] : A.face_begin + fi;
+  if (f < 0 || f >= A.nfaces) return;
   const bool pt = lane < NP;
   const int k = pt ? lane : 0;
   int votes = 0;
@@ -438,9 +440,9 @@ __global__ void __launch_bounds__(128)
 
 template <int N, int B, int NP>
 int launch(const sei::DrArgs& a, const float* v3m, const float* tw, const double* res, void* stream) {
-  if (a.nfaces <= 0) return 0;
+  if (a.face_count <= 0) return 0;
   constexpr int FPB = FaceGroup<NP>::kFaces;
-  const int blocks = (a.nfaces + FPB - 1) / FPB;
+  const int blocks = (a.face_count + FPB - 1) / FPB;
   sei_dr_faces<N, B, NP><<<blocks, 128, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }

@@ -120,7 +120,9 @@ bool viscoKernelsForOrder(int order, ViscoKernels& out);
 namespace sei {
 // Device arguments of the dynamic-rupture face kernel (passed by value).
 struct DrArgs {
-  int nfaces;
+  int nfaces;             // all faces (plane stride of the [field][nf][npts] arrays)
+  const int32_t* fidx;    // nullable: faces processed are fidx[face_begin + i], else face_begin + i
+  int face_begin, face_count;  // i < face_count
   const int32_t* plus_cell;
   const int32_t* minus_cell;
   const uint8_t* plus_side;

@@ -198,11 +198,11 @@ void buildPeriodicCube(const sei_cube_params& p, HostMesh& m) {
     throw std::invalid_argument("periodic cube needs even cube counts >= 4 in every direction");
   if (!(p.h > 0) || !(p.rho > 0) || !(p.vp > 0) || !(p.vs > 0) || p.perturb < 0 || p.perturb >= 0.5)
     throw std::invalid_argument("invalid cube geometry or material");
-  if (p.grading > 1.0 && p.fault_plane >= 0)
-    throw std::invalid_argument("a graded cube cannot carry the planar fault");
   const int64_t ncubes = (int64_t)p.nx * p.ny * p.nz;
   // vertex positions along each direction: cumulative cube edges (uniform h, or log-uniform in
-  // [h, grading h] from the seed); index nx (ny, nz) is the periodic image of 0
+  // [h, grading h] from the seed); index nx (ny, nz) is the periodic image of 0.  A cube that
+  // carries the planar fault x = plane h keeps uniform edges along x (its draws are discarded,
+  // so y and z are graded as without the fault).
   std::vector<double> pos[3];
   {
     Rng grng(p.seed ^ 0x9E3779B97F4A7C15ull);
@@ -210,7 +210,8 @@ void buildPeriodicCube(const sei_cube_params& p, HostMesh& m) {
     for (int d = 0; d < 3; ++d) {
       pos[d].assign(cnt[d] + 1, 0.0);
       for (int i = 0; i < cnt[d]; ++i) {
-        const double w = p.grading > 1.0 ? p.h * std::exp(grng.uniform(0.0, std::log(p.grading))) : p.h;
+        double w = p.grading > 1.0 ? p.h * std::exp(grng.uniform(0.0, std::log(p.grading))) : p.h;
+        if (d == 0 && p.fault_plane >= 0) w = p.h;
         pos[d][i + 1] = pos[d][i] + w;
       }
     }
