@@ -470,6 +470,86 @@ def dr_measurement(local, steps, order=4, dims=None, plane=3, warm_precision=0, 
                          "seconds_incl_recording": train_s}}
 
 
+def lts_fault_measurement(local, cycles):
+    """The combined configuration with local time stepping: elastic order 6, 1,000,000 tets of a
+    graded periodic cube (8 x 100 x 250 cubes, edges log-uniform in [50, 400] m, material +-10%),
+    a planar fault of 50,000 faces x 49 points (FVW, the fault configuration's distributions), at
+    most 4 rate-2 clusters; both cells of a fault face share a cluster and the fault step runs in
+    its cluster's correction.  Arms over `cycles` LTS cycles: plain Newton, and the learned Newton
+    start (trained on samples of a plain run of another fault seed).  LTS runs the FP32 kernels
+    (its neighbour data are per-face pool blocks), so both arms share the arithmetic and the
+    slip-rate difference measures the warm start alone."""
+    import numpy as np
+
+    from seissol_gb300 import Context, RSParams
+
+    def make(seed):
+        ctx = Context(6, device=local)
+        n = ctx.build_periodic_cube(8, 100, 250, h=50.0, perturb=PERTURB, seed=SEED, fault_plane=4, grading=8.0)
+        nf = ctx.dr_setup(RSParams.fault_config(seed=seed + 2))
+        rng = np.random.default_rng(seed)
+        ctx.set_dofs(rng.uniform(-1, 1, (n, 9, 56)).astype(np.float32))
+        ncl = ctx.lts_setup(0.5, 4)
+        ctx.set_option(2, 1)  # SEI_OPT_LTS_GRAPH
+        return ctx, n, nf, ncl
+
+    t0 = time.perf_counter()
+    tr, _, _, _ = make(DR_SEED)
+    chunks = []
+    for _ in range(max(cycles, 1)):
+        tr.dr_record_samples(400000 // max(cycles, 1))
+        tr.lts_run(1)
+        tr.sync()
+        chunks.append(tr.dr_samples())
+    tr.dr_record_samples(0)
+    samples = np.concatenate(chunks)
+    loss0, loss1 = tr.mlp_train(samples=samples, steps=1500, lr=3e-3, seed=1)
+    params, norm = tr.mlp_get()
+    tr.close()
+    train_s = time.perf_counter() - t0
+    out, states = {}, {}
+    for mode in ("plain", "warm"):
+        ctx, n, nf, ncl = make(DR_SEED + 1)
+        if mode == "warm":
+            ctx.mlp_set(params, norm)
+            ctx.dr_warm_start(True)
+        start, dts = ctx.lts_clusters()
+        sizes = np.diff(start)
+        faces = ctx.dr_faces()
+        cl_of = np.repeat(np.arange(ncl), sizes)
+        fcl = np.bincount(cl_of[faces["cells"][:, 0]], minlength=ncl)
+        ctx.lts_run(1)  # records the cycle graph
+        ctx.sync()
+        ctx.dr_reset_counters()
+        ctx.lts_run(cycles)
+        ctx.sync()
+        ms = ctx.last_run_ms()
+        tot, npts, first = ctx.dr_newton_iterations(first=True)
+        states[mode] = np.hypot(ctx.dr_state("slip_rate1"), ctx.dr_state("slip_rate2"))
+        ctx.close()
+        upd = int(sum(int(sz) * (1 << (ncl - 1 - k)) for k, sz in enumerate(sizes)))  # cell updates per cycle
+        dr_steps = int(sum(int(f) * (1 << (ncl - 1 - k)) for k, f in enumerate(fcl)))  # face steps per cycle
+        out[mode] = {"ms_per_cycle": ms / cycles, "cell_updates_per_s": upd * cycles / (ms / 1e3),
+                     "face_updates_per_s": dr_steps * cycles / (ms / 1e3),
+                     "simulated_s_per_wall_s": float(dts[-1]) * cycles / (ms / 1e3),
+                     "newton_iters_per_point_face_step": tot / max(npts / nf * dr_steps * cycles, 1),
+                     "first_solve_iters_per_point_face_step": first / max(npts / nf * dr_steps * cycles, 1)}
+    vp, vw = states["plain"], states["warm"]
+    return {"workload": f"elastic order 6, {n:,}-tet graded periodic cube 8x100x250 cubes (edges log-uniform in "
+                        f"[50, 400] m, material +-10%), planar fault of {nf:,} faces x 49 points (FVW), "
+                        f"{ncl} rate-2 clusters, {cycles} LTS cycles, FP32 kernels (LTS), graph replay",
+            "cells": n, "faces": nf, "clusters": ncl, "cells_per_cluster": [int(v) for v in sizes],
+            "faces_per_cluster": [int(v) for v in fcl], "cluster_dt": [float(v) for v in dts], "cycles": cycles,
+            "plain": out["plain"], "warm_start": out["warm"],
+            "first_solve_iteration_ratio": out["plain"]["first_solve_iters_per_point_face_step"]
+            / max(out["warm"]["first_solve_iters_per_point_face_step"], 1e-30),
+            "total_iteration_ratio": out["plain"]["newton_iters_per_point_face_step"]
+            / max(out["warm"]["newton_iters_per_point_face_step"], 1e-30),
+            "max_rel_dV": float((np.abs(vp - vw) / np.maximum(vp, 1e-30)).max()),
+            "training": {"samples": int(len(samples)), "loss_first": loss0, "loss_last": loss1,
+                         "seconds_incl_recording": train_s}}
+
+
 PATHS = {"fp32": (0, False), "f16x3": (1, False), "f16x3_tc_local": (1, True)}
 PATH_DESC = {"fp32": "FP32 CUDA cores (sparse, non-zero flops)",
              "f16x3": "mixed: neighbour flux on tcgen05 tensor cores (split FP16 x3) from stored face traces, "
@@ -611,6 +691,9 @@ def run_ours(args, world, rank, local):
         # path + learned Newton start; global time stepping (LTS with a fault is not built)
         comb = dr_measurement(local, args.combined_steps, order=6, dims=(8, 100, 250), plane=4, warm_precision=1,
                               perturb=PERTURB)
+    comb_lts = None
+    if rank == 0 and args.combined_lts_cycles > 0:
+        comb_lts = lts_fault_measurement(local, args.combined_lts_cycles)
 
     base = acc = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -631,6 +714,7 @@ def run_ours(args, world, rank, local):
                 "roofline": roof, "cpu_baseline": base, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": launches, "kernel_ms_per_step": kernels, "paths": paths_out,
                 "mixed_vs_fp32": ratio, "accuracy": acc, "dynamic_rupture": dr, "combined_o6_fault": comb,
+                "combined_o6_fault_lts": comb_lts,
                 "local_time_stepping": lts, "viscoelastic": vis}
         print(json.dumps(line))
     return 0
@@ -652,6 +736,8 @@ def main():
                     help="steps of the dynamic-rupture measurement (plain and warm-started); 0 skips it")
     ap.add_argument("--combined-steps", type=int, default=10,
                     help="steps of the combined order-6 measurement (1M tets, 50,000-face fault); 0 skips it")
+    ap.add_argument("--combined-lts-cycles", type=int, default=3,
+                    help="LTS cycles of the combined order-6 measurement with 4 clusters; 0 skips it")
     ap.add_argument("--visco-steps", type=int, default=20,
                     help="steps of the viscoelastic measurement; 0 skips it")
     ap.add_argument("--lts-cycles", type=int, default=10,

@@ -66,8 +66,9 @@ typedef struct sei_config {
 
 /* Synthetic periodic cube: nx*ny*nz cubes of edge h, 5 tetrahedra each (even counts >= 4).
  * Material rho, vp, vs, each multiplied per cell by U[1-perturb, 1+perturb] (seeded).
- * fault_plane in 1..nx-1 turns the faces on the plane x = fault_plane * h into a planar
- * vertical dynamic-rupture fault (plus side at smaller x); -1 builds no fault. */
+ * fault_plane in 1..nx-1 turns the faces on cube-vertex plane fault_plane along x (x =
+ * fault_plane * h on a uniform cube) into a planar vertical dynamic-rupture fault (plus side at
+ * smaller x); -1 builds no fault. */
 typedef struct sei_cube_params {
   int nx, ny, nz;
   double h;
@@ -76,8 +77,8 @@ typedef struct sei_cube_params {
   uint64_t seed;
   int fault_plane;
   /* > 1: graded tensor-product cube; along each direction the cube edges are drawn
-   * log-uniformly in [h, grading h] (seeded), except along x when the cube carries the fault
-   * (fault_plane >= 0), whose x edges stay h; <= 1: uniform edge h */
+   * log-uniformly in [h, grading h] (seeded); <= 1: uniform edge h.  The fault lies on the
+   * cube-vertex plane fault_plane along x (x = fault_plane h when uniform). */
   double grading;
 } sei_cube_params;
 

@@ -555,7 +555,7 @@ int sei_build_periodic_cube(sei_ctx* c, const sei_cube_params* p, int64_t* ncell
     if (p->fault_plane >= 0) {
       if (p->fault_plane < 1 || p->fault_plane > p->nx - 1)
         throw std::invalid_argument("fault_plane must lie in 1..nx-1 (or -1 for no fault)");
-      sei::buildPlanarFault(c->mesh, p->fault_plane, p->h, c->fault);
+      sei::buildPlanarFault(c->mesh, c->mesh.fault_x, p->h, c->fault);
       sei::faultFaceData(c->mesh, c->fault);
       c->has_fault = true;
     }

@@ -29,6 +29,7 @@ struct HostMesh {
   std::vector<double> material;  // [n][3] rho, mu, lambda
   std::vector<int32_t> nbr;      // [n][4]
   std::vector<int8_t> side, orient, ftype;
+  double fault_x = 0.0;  // x of the cube's fault plane (cube vertex plane fault_plane), when built
 };
 
 void buildPeriodicCube(const sei_cube_params& p, HostMesh& m);
@@ -167,7 +168,9 @@ struct HostFault {
   std::vector<float> tinvt, fsp, fsm;               // [nf][81] column-major
   std::vector<double> imp;                          // [nf][8]
 };
-void buildPlanarFault(HostMesh& m, int plane, double h, HostFault& f);
+// Fault faces on the plane x = xf (one cube-vertex plane of the mesh; h is the length scale of
+// the coordinate comparison).
+void buildPlanarFault(HostMesh& m, double xf, double h, HostFault& f);
 void faultFaceData(const HostMesh& m, HostFault& f);
 // Steady-state state variable of the fast-velocity-weakening law at slip rate v.
 double fvwSteadyState(double v, double a, double b, double f0, double v0, double muw, double vw);

@@ -200,9 +200,7 @@ void buildPeriodicCube(const sei_cube_params& p, HostMesh& m) {
     throw std::invalid_argument("invalid cube geometry or material");
   const int64_t ncubes = (int64_t)p.nx * p.ny * p.nz;
   // vertex positions along each direction: cumulative cube edges (uniform h, or log-uniform in
-  // [h, grading h] from the seed); index nx (ny, nz) is the periodic image of 0.  A cube that
-  // carries the planar fault x = plane h keeps uniform edges along x (its draws are discarded,
-  // so y and z are graded as without the fault).
+  // [h, grading h] from the seed); index nx (ny, nz) is the periodic image of 0
   std::vector<double> pos[3];
   {
     Rng grng(p.seed ^ 0x9E3779B97F4A7C15ull);
@@ -210,12 +208,12 @@ void buildPeriodicCube(const sei_cube_params& p, HostMesh& m) {
     for (int d = 0; d < 3; ++d) {
       pos[d].assign(cnt[d] + 1, 0.0);
       for (int i = 0; i < cnt[d]; ++i) {
-        double w = p.grading > 1.0 ? p.h * std::exp(grng.uniform(0.0, std::log(p.grading))) : p.h;
-        if (d == 0 && p.fault_plane >= 0) w = p.h;
+        const double w = p.grading > 1.0 ? p.h * std::exp(grng.uniform(0.0, std::log(p.grading))) : p.h;
         pos[d][i + 1] = pos[d][i] + w;
       }
     }
   }
+  m.fault_x = (p.fault_plane >= 0 && p.fault_plane <= p.nx) ? pos[0][p.fault_plane] : 0.0;
   m.n = ncubes * 5;
   m.topo.resize(m.n * 4);
   m.coords.resize(m.n * 12);
@@ -559,8 +557,7 @@ void seedDofs(int64_t n, int order, uint64_t seed, std::vector<float>& dofs) {
 
 namespace sei {
 
-void buildPlanarFault(HostMesh& m, int plane, double h, HostFault& F) {
-  const double xf = plane * h;
+void buildPlanarFault(HostMesh& m, double xf, double h, HostFault& F) {
   const int kMissing[4] = {3, 2, 1, 0};  // FACE2MISSINGNODE
   F = HostFault();
   std::vector<int> drCount(m.n, 0);

@@ -136,8 +136,7 @@ def test_lts_with_fault_single_cluster_is_global_stepping(built_lib):
 
 
 def test_lts_with_fault_matches_oracle(built_lib):
-    """A graded cube (uniform along x, graded along y and z) with the fault x = 4 h in several
-    clusters: the two cells of each fault face share a cluster, and one LTS cycle with the fault
+    """A graded cube with the fault on its fifth cube-vertex plane along x, in several clusters: the two cells of each fault face share a cluster, and one LTS cycle with the fault
     step in each cluster's correction matches the FP64 restatement (DOFs 1e-4 relative L2 per
     quantity, slip rate 1e-4 relative per point + 1e-12 m/s, state variable 1e-6)."""
     order = 4
