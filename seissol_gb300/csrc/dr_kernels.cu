@@ -214,7 +214,7 @@ __device__ __forceinline__ bool faceAll(bool c, int fs, int t, int parity, int (
 }
 
 template <int N, int B, int NP>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 3)
     sei_dr_faces(sei::DrArgs A, const float* __restrict__ V3m, const float* __restrict__ TW,
                  const double* __restrict__ R) {
   constexpr int TPF = FaceGroup<NP>::kThreads, FPB = FaceGroup<NP>::kFaces;
@@ -243,17 +243,16 @@ __global__ void __launch_bounds__(128)
   const int k = pt ? lane : 0;
   int votes = 0;
 
-  // ---- 1. space-time interpolation of both sides (six quantities needed per point)
-  float qi[2][N][6];
-#pragma unroll
-  for (int sd = 0; sd < 2; ++sd) {
-    const int slot = sd == 0 ? A.plus_slot[f] : A.minus_slot[f];
-    const int combo = sd == 0 ? A.plus_side[f] * 4 : A.minus_side[f] * 4 + A.rel[f];
-    const float* d = A.derivs + (size_t)slot * dsz;
-    const float* T = A.tinvt + (size_t)f * 81;
-    const float* V = V3m + (size_t)combo * NP * B;
+  // ---- 1. space-time interpolation of both sides at time point s (six quantities per point),
+  // evaluated inside the friction loop so that only one time point is live at a time
+  const float* Tf = A.tinvt + (size_t)f * 81;
+  auto interpolate = [&](int s, float (&qs)[2][6]) {
 #pragma unroll 1
-    for (int s = 0; s < N; ++s) {
+    for (int sd = 0; sd < 2; ++sd) {
+      const int slot = sd == 0 ? A.plus_slot[f] : A.minus_slot[f];
+      const int combo = sd == 0 ? A.plus_side[f] * 4 : A.minus_side[f] * 4 + A.rel[f];
+      const float* d = A.derivs + (size_t)slot * dsz;
+      const float* V = V3m + (size_t)combo * NP * B;
       for (int e = lane; e < B * 9; e += TPF) {
         const int l = e % B, q = e / B;
         float v = 0.f;
@@ -271,7 +270,7 @@ __global__ void __launch_bounds__(128)
         const int l = e % B, p = e / B;
         float v = 0.f;
 #pragma unroll
-        for (int q = 0; q < 9; ++q) v = fmaf(sI[warp][q * B + l], __ldg(T + q + 9 * p), v);
+        for (int q = 0; q < 9; ++q) v = fmaf(sI[warp][q * B + l], __ldg(Tf + q + 9 * p), v);
         sJ[warp][p * B + l] = v;
       }
       faceSync<TPF>(warp);
@@ -279,11 +278,11 @@ __global__ void __launch_bounds__(128)
       for (int j = 0; j < 6; ++j) {
         float v = 0.f;
         for (int l = 0; l < B; ++l) v = fmaf(__ldg(V + k * B + l), sJ[warp][kQsel[j] * B + l], v);
-        qi[sd][s][j] = v;
+        qs[sd][j] = v;
       }
       faceSync<TPF>(warp);
     }
-  }
+  };
 
   // ---- 2. friction (lanes < NP own one point each)
   const size_t po = (size_t)f * NP + k;
@@ -304,11 +303,13 @@ __global__ void __launch_bounds__(128)
   double isP[6] = {0, 0, 0, 0, 0, 0}, isM[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll 1
   for (int s = 0; s < N; ++s) {
+    float qc[2][6];
+    interpolate(s, qc);
     const double dt = A.deltat[s];
     // precompute stress (etaPDamp = 1): qi order N, T1, T2, U, V, W
-    const double fsn = etap * ((double)qi[1][s][3] - qi[0][s][3] + qi[0][s][0] / zp + qi[1][s][0] / zpn);
-    const double ft1 = etas * ((double)qi[1][s][4] - qi[0][s][4] + qi[0][s][1] / zs + qi[1][s][1] / zsn);
-    const double ft2 = etas * ((double)qi[1][s][5] - qi[0][s][5] + qi[0][s][2] / zs + qi[1][s][2] / zsn);
+    const double fsn = etap * ((double)qc[1][3] - qc[0][3] + qc[0][0] / zp + qc[1][0] / zpn);
+    const double ft1 = etas * ((double)qc[1][4] - qc[0][4] + qc[0][1] / zs + qc[1][1] / zsn);
+    const double ft2 = etas * ((double)qc[1][5] - qc[0][5] + qc[0][2] / zs + qc[1][2] / zsn);
     double sn = fsn + sn0;
     sn = sn < 0 ? sn : 0.0;
     const double sref = psib;
@@ -374,15 +375,15 @@ __global__ void __launch_bounds__(128)
       isM[0] += w * fsn;
       isM[1] += w * tr1;
       isM[2] += w * tr2;
-      isM[3] += w * (qi[1][s][3] - (fsn - qi[1][s][0]) / zpn);
-      isM[4] += w * (qi[1][s][4] - (tr1 - qi[1][s][1]) / zsn);
-      isM[5] += w * (qi[1][s][5] - (tr2 - qi[1][s][2]) / zsn);
+      isM[3] += w * (qc[1][3] - (fsn - qc[1][0]) / zpn);
+      isM[4] += w * (qc[1][4] - (tr1 - qc[1][1]) / zsn);
+      isM[5] += w * (qc[1][5] - (tr2 - qc[1][2]) / zsn);
       isP[0] += w * fsn;
       isP[1] += w * tr1;
       isP[2] += w * tr2;
-      isP[3] += w * (qi[0][s][3] + (fsn - qi[0][s][0]) / zp);
-      isP[4] += w * (qi[0][s][4] + (tr1 - qi[0][s][1]) / zs);
-      isP[5] += w * (qi[0][s][5] + (tr2 - qi[0][s][2]) / zs);
+      isP[3] += w * (qc[0][3] + (fsn - qc[0][0]) / zp);
+      isP[4] += w * (qc[0][4] + (tr1 - qc[0][1]) / zs);
+      isP[5] += w * (qc[0][5] + (tr2 - qc[0][2]) / zs);
     }
   }
 
