@@ -183,3 +183,39 @@ class Visco:
             Q = self.local(Q, I, ops["star"], ops["ET"], ops["AplusT"], face_type)
             Q = self.neighbor(Q, I, ops["AminusT"], nb, side, orient, face_type)
         return Q
+
+
+class ViscoLts:
+    """The dense viscoelastic update behind the interface of the elastic oracle that
+    oracle_py.lts_cycles drives: ader with Taylor coefficients and derivatives, local, neighbour and
+    taylor.  Its star argument carries the three star matrices and the source matrix ET as
+    star[:, 0:3] and star[:, 3] ([n, 4, 27, 27]); derivatives are [n, order * 27 * B], stage-major,
+    with all basis rows at every stage (the source term keeps them, aderdg.py:507-517)."""
+
+    def __init__(self, order):
+        self.order = order
+        self.v = Visco(order)
+
+    def ader(self, Q, star, coeffs, want_derivs=False):
+        dq = np.array(Q, dtype=np.float64)
+        I = coeffs[0] * dq
+        ds = [dq]
+        for i in range(1, self.order):
+            t = np.einsum("dkl,nql->ndqk", self.v.kdmt, dq)
+            dq = np.einsum("ndqk,ndqp->npk", t, star[:, :3]) + np.einsum("nqk,nqp->npk", dq, star[:, 3])
+            I = I + coeffs[i] * dq
+            ds.append(dq)
+        if not want_derivs:
+            return I
+        return I, np.stack(ds, axis=1).reshape(dq.shape[0], -1)
+
+    def taylor(self, derivs, coeffs):
+        n = derivs.shape[0]
+        d = derivs.reshape(n, self.order, NQ, -1)
+        return np.einsum("i,niqk->nqk", np.asarray(coeffs[:self.order], np.float64), d)
+
+    def local(self, Q, I, star, aplus, face_type=None):
+        return self.v.local(Q, I, star[:, :3], star[:, 3], aplus, face_type)
+
+    def neighbor(self, Q, I, aminus, nb, side, orient, face_type=None):
+        return self.v.neighbor(Q, I, aminus, nb, side, orient, face_type)

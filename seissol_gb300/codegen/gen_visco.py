@@ -134,6 +134,8 @@ def gen_visco(order: int) -> str:
     a("#pragma once")
     a(f"namespace sei_v{order} {{")
     a(f"constexpr int kOrder = {order}, kB = {B}, kBp = {padded(B)}, kF = {F}, kNQ = {NQ}, kCPB = {CPB};")
+    a("// Stored derivatives of one cell: [stage][27][kB] (the source term keeps all basis rows).")
+    a(f"constexpr int kDerivSize = {order} * {NQ} * {B};")
     _tables(L)
 
     # ---------------- ADER ----------------
@@ -141,18 +143,23 @@ def gen_visco(order: int) -> str:
 // Cauchy-Kovalevskaya predictor with the viscoelastic source term: I = sum_i coeffs[i] dQ(i).
 // Q, I [n][27][Bp]; star_nz [n][3][24] (elastic, unrelaxed moduli); grad [n][3][3]; theta [n][3][3];
 // omega: relaxation frequencies.  Shared memory: X [9][B][32], M and IM [18][B][32].
+// derivs (nullable): derivative output [slots][kDerivSize]; the slot of a cell is dslot[cell]
+// (-1: not stored), or the cell itself when dslot is nullptr.
 extern "C" __global__ void __launch_bounds__(480, 1)
 sei_vader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout, const float* __restrict__ star_nz,
                    const float* __restrict__ grad, const float* __restrict__ theta, SeiOmega omega,
-                   SeiCoeffs coeffs) {{""" + PROLOGUE)
+                   SeiCoeffs coeffs, float* __restrict__ derivs, const int* __restrict__ dslot) {{""" + PROLOGUE)
     a("""  float* M = X + 9 * kB * 32;    // memory variables of the current stage [l * 6 + j][kB][32]
   float* IM = M + 18 * kB * 32;   // their time integral
   float z[kBp];
   float I[kBp];
+  const int dsl = derivs ? (dslot ? __ldg(dslot + cl) : cl) : -1;
+  float* dbase = (dsl >= 0 && valid) ? derivs + (size_t)dsl * kDerivSize : nullptr;
   if (el) {
     sei_load_col<kBp>(Q + ((size_t)cl * kNQ + q) * kBp, z);
 #pragma unroll
     for (int k = 0; k < kBp; ++k) I[k] = coeffs.c[0] * z[k];
+    if (dbase) sei_store_col_scalar<kB>(dbase + q * kB, z);
   } else {
 #pragma unroll 1
     for (int m = 0; m < 3; ++m) {
@@ -164,6 +171,7 @@ sei_vader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout,
         Mm[k * 32] = z[k];
         IMm[k * 32] = coeffs.c[0] * z[k];
       }
+      if (dbase) sei_store_col_scalar<kB>(dbase + (9 + 6 * m + jv) * kB, z);
     }
   }""")
     for i in range(1, order):
@@ -180,6 +188,7 @@ sei_vader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout,
         a("    __syncthreads();")
         a("    if (el) {")
         a(f"#pragma unroll\n      for (int k = 0; k < kB; ++k) {{ I[k] = fmaf(coeffs.c[{i}], zn[k], I[k]); z[k] = zn[k]; }}")
+        a(f"      if (dbase) sei_store_col_scalar<kB>(dbase + {i} * kNQ * kB + q * kB, zn);")
         a("    } else {")
         a("#pragma unroll 1")
         a("      for (int m = 0; m < 3; ++m) {")
@@ -191,6 +200,7 @@ sei_vader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout,
         a("          const float nw = w * (zn[k] + Mm[k * 32]);")
         a("          Mm[k * 32] = nw;")
         a(f"          IMm[k * 32] = fmaf(coeffs.c[{i}], nw, IMm[k * 32]);")
+        a(f"          if (dbase) dbase[{i} * kNQ * kB + (9 + 6 * m + jv) * kB + k] = nw;")
         a("        }")
         a("      }")
         a("    }")

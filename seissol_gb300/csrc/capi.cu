@@ -102,6 +102,7 @@ struct sei_ctx {
   bool visco = false;
   sei::ViscoKernels vk{};
   float omega[3] = {0, 0, 0};
+  double visco_params[4] = {0, 0, 0, 0};  // Qp, Qs, central frequency, frequency ratio
   float *d_grad = nullptr, *d_theta = nullptr, *d_wplus = nullptr, *d_wminus = nullptr;
   std::vector<float> h_grad, h_theta, h_wplus, h_wminus;  // host copies (sei_visco_operators)
   bool lts_graph = false;                           // SEI_OPT_LTS_GRAPH
@@ -1237,26 +1238,17 @@ int upload(sei_ctx* c, int32_t** dst, const std::vector<int32_t>& src) {
 }
 }  // namespace
 
-int sei_visco_setup(sei_ctx* c, double qp, double qs, double freq_central, double freq_ratio) {
-  if (!c) return SEI_ERR_ARG;
-  const bool host = c->cfg.device < 0;
-  int rc = host ? SEI_OK : checkReady(c);
-  if (rc) return rc;
-  if (!c->has_mesh) return fail(c, SEI_ERR_STATE, "the viscoelastic set-up needs a mesh built by the context");
-  if (c->has_fault || c->lts || c->visco)
-    return fail(c, SEI_ERR_UNSUPPORTED, "viscoelastic set-up: not built with a fault or local time stepping, or twice");
-  if (c->cfg.precision != SEI_PREC_FP32) return fail(c, SEI_ERR_UNSUPPORTED, "viscoelastic kernels are FP32 only");
-  sei::ViscoKernels vk{};
-  if (!sei::viscoKernelsForOrder(c->cfg.order, vk))
-    return fail(c, SEI_ERR_UNSUPPORTED, "viscoelastic kernels are built for orders 4 and 5");
-  if (!(qp > 0) || !(qs > 0) || !(freq_central > 0) || !(freq_ratio > 1)) return fail(c, SEI_ERR_ARG, "Qp, Qs, fc > 0, ratio > 1");
+// Host operators of the viscoelastic equations for the context's mesh: elastic blocks with the
+// unrelaxed moduli (h_star, h_aplus, h_aminus), gradients, theta, W+/- and omega.
+static int buildViscoHost(sei_ctx* c) {
+  const double qp = c->visco_params[0], qs = c->visco_params[1], fc = c->visco_params[2], fr = c->visco_params[3];
   const int64_t n = c->mesh.n;
   sei::HostMesh um = c->mesh;  // unrelaxed moduli
   std::vector<float> theta((size_t)n * 9);
   double om[3] = {0, 0, 0};
   for (int64_t i = 0; i < n; ++i) {
     double mu = um.material[i * 3 + 1], lam = um.material[i * 3 + 2], th[3][3];
-    sei::fitAttenuation(qp, qs, freq_central, freq_ratio, mu, lam, om, th);
+    sei::fitAttenuation(qp, qs, fc, fr, mu, lam, om, th);
     um.material[i * 3 + 1] = mu;
     um.material[i * 3 + 2] = lam;
     for (int m = 0; m < 3; ++m)
@@ -1274,6 +1266,29 @@ int sei_visco_setup(sei_ctx* c, double qp, double qs, double freq_central, doubl
   c->h_wplus = wp;
   c->h_wminus = wm;
   for (int m = 0; m < 3; ++m) c->omega[m] = (float)om[m];
+  return SEI_OK;
+}
+
+int sei_visco_setup(sei_ctx* c, double qp, double qs, double freq_central, double freq_ratio) {
+  if (!c) return SEI_ERR_ARG;
+  const bool host = c->cfg.device < 0;
+  int rc = host ? SEI_OK : checkReady(c);
+  if (rc) return rc;
+  if (!c->has_mesh) return fail(c, SEI_ERR_STATE, "the viscoelastic set-up needs a mesh built by the context");
+  if (c->has_fault || c->lts || c->visco)
+    return fail(c, SEI_ERR_UNSUPPORTED, "viscoelastic set-up: not built with a fault or local time stepping, or twice");
+  if (c->cfg.precision != SEI_PREC_FP32) return fail(c, SEI_ERR_UNSUPPORTED, "viscoelastic kernels are FP32 only");
+  sei::ViscoKernels vk{};
+  if (!sei::viscoKernelsForOrder(c->cfg.order, vk))
+    return fail(c, SEI_ERR_UNSUPPORTED, "viscoelastic kernels are built for orders 4 and 5");
+  if (!(qp > 0) || !(qs > 0) || !(freq_central > 0) || !(freq_ratio > 1)) return fail(c, SEI_ERR_ARG, "Qp, Qs, fc > 0, ratio > 1");
+  const int64_t n = c->mesh.n;
+  c->visco_params[0] = qp;
+  c->visco_params[1] = qs;
+  c->visco_params[2] = freq_central;
+  c->visco_params[3] = freq_ratio;
+  if ((rc = buildViscoHost(c))) return rc;
+  const std::vector<float>&grad = c->h_grad, &theta = c->h_theta, &wp = c->h_wplus, &wm = c->h_wminus;
   if (host) {  // host-only context: the operators only
     c->nq = 27;
     c->visco = true;
@@ -1304,7 +1319,6 @@ int sei_visco_setup(sei_ctx* c, double qp, double qs, double freq_central, doubl
     return fail(c, SEI_ERR_OOM, "viscoelastic DOF arrays");
   SEI_CUDA(cudaMemcpy(c->Q, q27.data(), q27.size() * sizeof(float), cudaMemcpyHostToDevice));
   SEI_CUDA(cudaMemset(c->I, 0, q27.size() * sizeof(float)));
-  for (int m = 0; m < 3; ++m) c->omega[m] = (float)om[m];
   c->vk = vk;
   c->nq = 27;
   c->visco = true;
@@ -1342,7 +1356,6 @@ int sei_fit_attenuation(double qp, double qs, double freq_central, double freq_r
 int sei_lts_setup(sei_ctx* c, double cfl, int max_clusters, int* nclusters) {
   int rc = checkReady(c);
   if (rc) return rc;
-  if (c->visco) return fail(c, SEI_ERR_UNSUPPORTED, "local time stepping of the viscoelastic equations is not built");
   if (!c->has_mesh) return fail(c, SEI_ERR_STATE, "local time stepping needs a mesh built by the context");
   if (c->has_fault && !c->dr_ready)
     return fail(c, SEI_ERR_STATE, "set up dynamic rupture (sei_dr_setup) before local time stepping");
@@ -1388,7 +1401,7 @@ int sei_lts_setup(sei_ctx* c, double cfl, int max_clusters, int* nclusters) {
   std::vector<int64_t> order(n);
   for (int64_t i = 0; i < n; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return cl[a] < cl[b]; });
-  const int blk = 9 * c->Bp;
+  const int blk = c->nq * c->Bp;
   std::vector<float> qold((size_t)n * blk), qnew((size_t)n * blk);
   SEI_CUDA(cudaStreamSynchronize(c->stream));
   SEI_CUDA(cudaMemcpy(qold.data(), c->Q, qold.size() * sizeof(float), cudaMemcpyDeviceToHost));
@@ -1406,9 +1419,15 @@ int sei_lts_setup(sei_ctx* c, double cfl, int max_clusters, int* nclusters) {
       c->mesh.ftype[(int64_t)c->fault.plus_cell[f] * 4 + c->fault.plus_side[f]] = 1;
       c->mesh.ftype[(int64_t)c->fault.minus_cell[f] * 4 + c->fault.minus_side[f]] = 1;
     }
-    sei::buildOperators(c->mesh, c->h_star, c->h_aplus, c->h_aminus);
+    if (!c->visco) sei::buildOperators(c->mesh, c->h_star, c->h_aplus, c->h_aminus);
   } catch (const std::exception& e) {
     return fail(c, SEI_ERR_ARG, e.what());
+  }
+  if (c->visco) {  // the viscoelastic operators of the reordered cells
+    if ((rc = buildViscoHost(c))) return rc;
+    for (auto [d, h] : {std::pair<float*, const std::vector<float>*>{c->d_grad, &c->h_grad}, {c->d_theta, &c->h_theta},
+                        {c->d_wplus, &c->h_wplus}, {c->d_wminus, &c->h_wminus}})
+      SEI_CUDA(cudaMemcpy(d, h->data(), h->size() * sizeof(float), cudaMemcpyHostToDevice));
   }
   rc = uploadCells(c, n, c->h_star.data(), c->h_aplus.data(), c->h_aminus.data(), c->mesh.nbr.data(),
                    c->mesh.side.data(), c->mesh.orient.data(), c->mesh.ftype.data());
@@ -1496,7 +1515,7 @@ int sei_lts_setup(sei_ctx* c, double cfl, int max_clusters, int* nclusters) {
   SEI_CUDA(cudaMemset(c->I, 0, (size_t)(n + nB + nS) * blk * sizeof(float)));
   cudaFree(c->derivs);
   c->derivs = nullptr;
-  const int dsz = sei::derivativesSize(c->cfg.order);
+  const int dsz = c->visco ? c->vk.derivSize : sei::derivativesSize(c->cfg.order);
   if (nD > 0 && cudaMalloc(&c->derivs, (size_t)nD * dsz * sizeof(float)) != cudaSuccess)
     return fail(c, SEI_ERR_OOM, "LTS derivative allocation");
   c->nslots = nD;
@@ -1539,13 +1558,34 @@ sei::DeviceArrays rangeView(sei_ctx* c, int64_t s, int64_t e, bool neighbour) {
   return d;
 }
 
+sei::ViscoArrays viscoRangeView(sei_ctx* c, int64_t s, int64_t e, bool neighbour) {
+  const size_t blk = (size_t)c->nq * c->Bp;
+  sei::ViscoArrays v = viscoArrays(c);
+  v.n = (int)(e - s);
+  v.Q = c->Q + s * blk;
+  v.I = neighbour ? c->I : c->I + s * blk;
+  v.star_nz = c->star_nz + s * 3 * sei::kStarNnz;
+  v.grad = c->d_grad + s * 9;
+  v.theta = c->d_theta + s * 9;
+  v.aplus = c->aplus + s * 4 * 81;
+  v.wplus = c->d_wplus + s * 4 * 54;
+  v.aminus = c->aminus + s * 4 * 81;
+  v.wminus = c->d_wminus + s * 4 * 54;
+  v.nbr = (neighbour ? c->d_src : c->nbr) + s * 4;
+  v.rel = c->rel + s * 4;
+  v.ftype = c->ftype + s * 4;
+  v.derivs = c->derivs;
+  v.dslot = c->dslot ? c->dslot + s : nullptr;
+  return v;
+}
+
 // One cycle: every cluster advances by dt0 2^(ncl-1).  Sub-step k of the finest cluster starts
 // with the predictions (ADER, integration buffer, local integral) of the clusters whose step begins
 // at k, then the corrections (coarse-neighbour Taylor integrals, the fault faces of the cluster,
 // neighbour flux) of the clusters whose step ends at k + 1 (TimeCluster predict / correct,
 // TimeCommon::computeIntegrals).
 int ltsCycle(sei_ctx* c) {
-  const int blk = 9 * c->Bp;
+  const int blk = c->nq * c->Bp;
   const int64_t steps = (int64_t)1 << (c->ncl - 1);
   float co[8];
   for (int64_t k = 0; k < steps; ++k) {
@@ -1556,8 +1596,14 @@ int ltsCycle(sei_ctx* c) {
       if (s == e) continue;
       taylorCoeffs(c->cfg.order, c->lts_dt0 * (double)len, co);
       sei::DeviceArrays d = rangeView(c, s, e, false);
-      int rc = launchAderOnly(c, d, co);
-      if (rc) return rc;
+      const sei::ViscoArrays v = c->visco ? viscoRangeView(c, s, e, false) : sei::ViscoArrays{};
+      int rc;
+      if (c->visco) {
+        if ((rc = profMark(c, 0))) return rc;
+        if (c->vk.ader(v, co, c->stream)) return fail(c, SEI_ERR_CUDA, "viscoelastic ADER launch failed");
+      } else if ((rc = launchAderOnly(c, d, co))) {
+        return rc;
+      }
       const int64_t bs = c->b_start[cl], be = c->b_start[cl + 1];
       if (be > bs) {
         if ((rc = profMark(c, 4))) return rc;
@@ -1566,7 +1612,12 @@ int ltsCycle(sei_ctx* c) {
                                  c->stream))
           return fail(c, SEI_ERR_CUDA, "LTS buffer kernel launch failed");
       }
-      if ((rc = launchLintOnly(c, d))) return rc;
+      if (c->visco) {
+        if ((rc = profMark(c, 3))) return rc;
+        if (c->vk.lint(v, c->stream)) return fail(c, SEI_ERR_CUDA, "viscoelastic local-integral launch failed");
+      } else if ((rc = launchLintOnly(c, d))) {
+        return rc;
+      }
     }
     for (int cl = 0; cl < c->ncl; ++cl) {
       const int64_t len = (int64_t)1 << cl;
@@ -1581,7 +1632,10 @@ int ltsCycle(sei_ctx* c) {
         subCoeffs(c->cfg.order, a, b, co);
         int rc = profMark(c, 4);
         if (rc) return rc;
-        if (c->k.taylorGather((int)(ge - gs), c->d_gsrc + gs, c->d_gdst + gs, c->derivs, co, c->I, c->stream))
+        const int m = (int)(ge - gs);
+        if (c->visco ? sei::launchTaylorGatherFull(m, c->d_gsrc + gs, c->d_gdst + gs, c->derivs, c->cfg.order, c->nq,
+                                                   sei::numBasis(c->cfg.order), c->Bp, co, c->I, c->stream)
+                     : c->k.taylorGather(m, c->d_gsrc + gs, c->d_gdst + gs, c->derivs, co, c->I, c->stream))
           return fail(c, SEI_ERR_CUDA, "LTS gather kernel launch failed");
       }
       // the fault faces of this cluster first (TimeCluster.cpp:804-823), over its own step
@@ -1593,6 +1647,13 @@ int ltsCycle(sei_ctx* c) {
         a.face_begin = (int)c->f_start[cl];
         a.face_count = (int)(c->f_start[cl + 1] - c->f_start[cl]);
         if (sei::launchDrFaces(c->cfg.order, a, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "fault kernel launch failed");
+      }
+      if (c->visco) {
+        int rc = profMark(c, 1);
+        if (rc) return rc;
+        if (c->vk.neighbor(viscoRangeView(c, s, e, true), c->stream))
+          return fail(c, SEI_ERR_CUDA, "viscoelastic neighbour launch failed");
+        continue;
       }
       int rc = launchNeighbor(c, rangeView(c, s, e, true));
       if (rc) return rc;

@@ -108,12 +108,19 @@ struct ViscoArrays {
   const uint8_t* rel;
   const uint8_t* ftype;
   float omega[3];
+  float* derivs = nullptr;         // nullable: ADER derivative output [slots][derivSize]
+  const int32_t* dslot = nullptr;  // nullable: slot per cell (-1 none); nullptr = slot is the cell
 };
 struct ViscoKernels {
   int (*ader)(const ViscoArrays&, const float* coeffs, void* stream);
   int (*lint)(const ViscoArrays&, void* stream);
   int (*neighbor)(const ViscoArrays&, void* stream);
+  int derivSize;  // floats of one cell's stored derivatives: order x 27 x B
 };
+// pool[dst[e]][nq][Bp] = sum_i coeffs[i] dQ(i) of derivative slot src[e] stored as [order][nq][B]
+// (all basis rows at every stage), e < m; local time stepping of the viscoelastic equations.
+int launchTaylorGatherFull(int m, const int32_t* src, const int32_t* dst, const float* derivs, int order, int nq, int b,
+                           int bp, const float* coeffs, float* pool, void* stream);
 bool viscoKernelsForOrder(int order, ViscoKernels& out);
 
 }  // namespace sei

@@ -30,7 +30,7 @@ int launchVAder(const sei::ViscoArrays& d, const float* coeffs, void* stream) {
   for (int i = 0; i < KV::kOrder; ++i) c.c[i] = coeffs[i];
   const int blocks = (d.n + KV::kCPB - 1) / KV::kCPB;
   KV::SEI_VCAT(sei_vader_o, SEI_VORDER)<<<blocks, kThreads, smem, (cudaStream_t)stream>>>(
-      d.n, d.Q, d.I, d.star_nz, d.grad, d.theta, toOmega(d), c);
+      d.n, d.Q, d.I, d.star_nz, d.grad, d.theta, toOmega(d), c, d.derivs, d.dslot);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -57,5 +57,7 @@ int launchVNeighbor(const sei::ViscoArrays& d, void* stream) {
 }  // namespace
 
 namespace sei {
-ViscoKernels SEI_VCAT(viscoKernels, SEI_VORDER)() { return ViscoKernels{launchVAder, launchVLint, launchVNeighbor}; }
+ViscoKernels SEI_VCAT(viscoKernels, SEI_VORDER)() {
+  return ViscoKernels{launchVAder, launchVLint, launchVNeighbor, KV::kDerivSize};
+}
 }  // namespace sei

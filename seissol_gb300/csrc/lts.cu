@@ -8,6 +8,10 @@
 
 namespace {
 
+struct SeiCoeffsGather {
+  float c[8];
+};
+
 __global__ void sei_lts_buffer(int m, const int32_t* __restrict__ cell, const int32_t* __restrict__ dst,
                                float* __restrict__ pool, int blk4, int reset) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -28,9 +32,40 @@ __global__ void sei_lts_buffer(int m, const int32_t* __restrict__ cell, const in
   }
 }
 
+// One thread per (entry e, quantity q): pool[dst[e]][q][k] = sum_i coeffs[i] d[src[e]][i][q][k] for
+// k < b, zero for b <= k < bp (Taylor integral of stored full-row derivatives).
+__global__ void sei_taylor_gather_full(int m, const int32_t* __restrict__ src, const int32_t* __restrict__ dst,
+                                       const float* __restrict__ derivs, int order, int nq, int b, int bp,
+                                       SeiCoeffsGather coeffs, float* __restrict__ pool) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)m * nq) return;
+  const long e = t / nq;
+  const int q = (int)(t % nq);
+  const float* d = derivs + (size_t)__ldg(src + e) * order * nq * b + (size_t)q * b;
+  float* o = pool + ((size_t)__ldg(dst + e) * nq + q) * bp;
+  for (int k = 0; k < bp; ++k) {
+    float v = 0.f;
+    if (k < b)
+      for (int i = 0; i < order; ++i) v = fmaf(coeffs.c[i], __ldg(d + (size_t)i * nq * b + k), v);
+    o[k] = v;
+  }
+}
+
 }  // namespace
 
 namespace sei {
+
+int launchTaylorGatherFull(int m, const int32_t* src, const int32_t* dst, const float* derivs, int order, int nq, int b,
+                           int bp, const float* coeffs, float* pool, void* stream) {
+  if (m <= 0) return 0;
+  if (order < 1 || order > 8) return -1;
+  SeiCoeffsGather c{};
+  for (int i = 0; i < order; ++i) c.c[i] = coeffs[i];
+  const long threads = (long)m * nq;
+  sei_taylor_gather_full<<<(int)((threads + 255) / 256), 256, 0, (cudaStream_t)stream>>>(m, src, dst, derivs, order, nq,
+                                                                                           b, bp, c, pool);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
 
 int launchLtsBuffer(int m, const int32_t* cell, const int32_t* dst, float* pool, int blk, int reset, void* stream) {
   if (m <= 0) return 0;

@@ -99,6 +99,69 @@ def test_visco_rejects_unbuilt(built_lib):
     ctx, *_ = _setup(4)
     with pytest.raises(SeiError, match="SEI_ERR_UNSUPPORTED"):
         ctx.run("all_dr", 1e-4, 1)
-    with pytest.raises(SeiError):
-        ctx.lts_setup(0.5, 4)
+    ctx.close()
+
+
+def _graded_visco(order, grading, max_clusters, seed=31):
+    from seissol_gb300 import Context
+    ctx = Context(order, device=0)
+    n = ctx.build_periodic_cube(8, 8, 8, perturb=0.05, seed=seed, grading=grading)
+    ctx.visco_setup(QP, QS, FC, RATIO)
+    ncl = ctx.lts_setup(0.5, max_clusters)
+    return ctx, n, ncl
+
+
+def test_visco_lts_single_cluster_is_global_stepping(built_lib):
+    """One cluster: the LTS cycle of the viscoelastic kernels is global stepping bit for bit."""
+    from seissol_gb300 import Context
+    a, n, ncl = _graded_visco(4, 6.0, 1)
+    assert ncl == 1
+    _, dts = a.lts_clusters()
+    b = Context(4, device=0)
+    b.build_periodic_cube(8, 8, 8, perturb=0.05, seed=31, grading=6.0)
+    b.visco_setup(QP, QS, FC, RATIO)
+    q0 = np.random.default_rng(3).uniform(-1, 1, (n, 27, a.B)).astype(np.float32)
+    a.set_dofs(q0)
+    b.set_dofs(q0)
+    a.lts_run(3)
+    b.run("all", dts[0], 3)
+    a.sync()
+    b.sync()
+    assert np.array_equal(a.get_dofs(), b.get_dofs())
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("order", [4, 5])
+def test_visco_lts_matches_oracle(built_lib, order):
+    """Rate-2 LTS of the viscoelastic equations on a graded cube (several clusters), one cycle,
+    against the FP64 restatement driving the dense viscoelastic oracle: 1e-4 relative L2 per
+    quantity."""
+    from oracle import dg_setup, oracle_py
+    ctx, n, ncl = _graded_visco(order, 6.0, 8)
+    assert ncl >= 2
+    start, _ = ctx.lts_clusters()
+    cl_gpu = np.repeat(np.arange(ncl), np.diff(start))
+    coords, material, _ = ctx.get_geometry()
+    cells = ctx.get_cells()
+    vp = np.sqrt((material[:, 2] + 2 * material[:, 1]) / material[:, 0])
+    cl, dt0 = oracle_py.lts_clusters(dg_setup.cfl_timestep(coords, vp, order, 0.5), cells["neighbor"],
+                                     cells["face_type"], 8)
+    assert np.array_equal(cl, cl_gpu)
+    mats, thetas = [], []
+    for rho, mu, lam in material:
+        mu_u, lam_u, omega, theta = visco.fit_attenuation(rho, mu, lam, QP, QS, FC, RATIO)
+        mats.append([rho, mu_u, lam_u])
+        thetas.append(theta)
+    ops = visco.cell_operators(coords, np.array(mats), omega, np.array(thetas), cells["neighbor"])
+    vcells = {"star": np.concatenate([ops["star"], ops["ET"][:, None]], axis=1), "AplusT": ops["AplusT"],
+              "AminusT": ops["AminusT"], "neighbor": cells["neighbor"], "side": cells["side"],
+              "orient": cells["orient"], "face_type": cells["face_type"]}
+    q0 = np.random.default_rng(5).uniform(-1, 1, (n, 27, ctx.B)).astype(np.float32)
+    ctx.set_dofs(q0)
+    ctx.lts_run(1)
+    ctx.sync()
+    ref = oracle_py.lts_cycles(visco.ViscoLts(order), q0.astype(np.float64), vcells, cl, dt0, 1)
+    errs = rel_l2_per_quantity(ctx.get_dofs(), ref)
+    assert max(errs) < 1e-4, errs
     ctx.close()
