@@ -268,9 +268,10 @@ DR_SEED = 77
 LTS_DIMS = (34, 34, 34)  # 39,304 cubes = 196,520 tets
 
 
-def lts_measurement(local, cycles):
-    """Rate-2 local time stepping on a graded cube: elastic order 5 (35 x 9), 196,520 tets, cube
-    edges log-uniform in [50, 400] m per direction, material +-10 %, CFL 0.5; four clusters.
+def lts_measurement(local, cycles, visco=True):
+    """Rate-2 local time stepping on a graded cube: order 5, viscoelastic with 3 mechanisms (35 x 27;
+    Qp 100, Qs 50, fc 0.5 Hz, ratio 100) or elastic (35 x 9), 196,520 tets, cube edges log-uniform
+    in [50, 400] m per direction, material +-10 %, CFL 0.5; at most four clusters.
     One cycle advances every cluster by the coarsest step.  Reported: cell updates per second
     (a cell update = one step of one cell in its own cluster), the simulated time per wall second
     against global time stepping at the finest step (same kernels, same simulated time), with the
@@ -283,7 +284,9 @@ def lts_measurement(local, cycles):
     for mode in ("direct", "graph"):
         ctx = Context(5, device=local)
         n = ctx.build_periodic_cube(*LTS_DIMS, h=50.0, perturb=PERTURB, seed=SEED, grading=8.0)
-        ncl = ctx.lts_setup(0.5, 8)
+        if visco:
+            ctx.visco_setup(100.0, 50.0, 0.5, 100.0)
+        ncl = ctx.lts_setup(0.5, 4)
         start, dts = ctx.lts_clusters()
         counts = np.diff(start)
         ctx.set_option(2, 1 if mode == "graph" else 0)  # SEI_OPT_LTS_GRAPH
@@ -307,9 +310,10 @@ def lts_measurement(local, cycles):
                                       "cell_updates_per_s": n * steps / (gms / 1e3),
                                       "simulated_s_per_wall_s": steps * dts[0] / (gms / 1e3)}
         ctx.close()
-    return {"workload": "elastic order 5 (35x9), 196,520-tet graded periodic cube 34^3 cubes x 5 tets, cube edges "
-                        "log-uniform in [50, 400] m, material +-10%, CFL 0.5, rate-2 clusters (stand-in for the "
-                        "viscoelastic configuration, whose 27-quantity kernels are not built)",
+    eq = ("viscoelastic order 5 (35x27, 3 mechanisms, Qp 100, Qs 50, fc 0.5 Hz, ratio 100)" if visco
+          else "elastic order 5 (35x9)")
+    return {"workload": f"{eq}, 196,520-tet graded periodic cube 34^3 cubes x 5 tets, cube edges log-uniform in "
+                        "[50, 400] m per direction, material +-10%, CFL 0.5, at most 4 rate-2 clusters",
             "cells": n, "clusters": int(ncl), "cells_per_cluster": [int(x) for x in counts],
             "cluster_dt": [float(x) for x in dts], "cycles": cycles, "direct": out["direct"], "graph": out["graph"],
             "global_stepping": out["global_stepping"],
@@ -585,6 +589,15 @@ def measure_path(args, world, local, path, hbm, peak_kind, e2e_steps=0):
         ctx.set_option(3, 1)  # SEI_OPT_TC_LOCAL
     n = ctx.build_periodic_cube(*DIMS, perturb=PERTURB, seed=SEED + rank)
     dt = ctx.cfl_timestep(0.5)
+    tune = None
+    fused = bool(args.fused_local)
+    if args.autotune:
+        # the variants of this path timed on this mesh; the fastest stays set (DOFs unchanged)
+        tune = ctx.autotune(dt, 3)
+        fused = bool(tune["fused_local"])
+        tc_local = bool(tune["tc_local"])
+        if path != "fp32":
+            path = "f16x3_tc_local" if tc_local else "f16x3"
     ctx.run("all", dt, args.warmup)
     ctx.sync()
     torch.cuda.synchronize(local)
@@ -606,7 +619,7 @@ def measure_path(args, world, local, path, hbm, peak_kind, e2e_steps=0):
     ctx.sync()
     by_kind = ctx.kernel_times_by_kind()
     ctx.set_profiling(False)
-    names = {"ader": "local" if args.fused_local else "ader", "lint": "lint", "neighbor": "neighbor"}
+    names = {"ader": "local" if fused else "ader", "lint": "lint", "neighbor": "neighbor"}
     kernels = {names[k]: v[0] / v[1] for k, v in by_kind.items() if k in names and v[1] > 0}
     launches = sum(v[1] for v in by_kind.values())
     dom = max(kernels, key=kernels.get)
@@ -655,7 +668,7 @@ def measure_path(args, world, local, path, hbm, peak_kind, e2e_steps=0):
                "call": "sei_run_host(SEI_KERNEL_ALL, dt, 1, dofs_in, dofs_out) with pinned host DOFs"}
     ctx.close()
     return {"value": value, "ms": ms, "n": n, "kernels": kernels, "launches": launches, "roofline": roof,
-            "clocks": clk.summary(), "e2e": e2e, "description": PATH_DESC[path]}
+            "clocks": clk.summary(), "e2e": e2e, "description": PATH_DESC[path], "autotune": tune}
 
 
 def run_ours(args, world, rank, local):
@@ -672,7 +685,7 @@ def run_ours(args, world, rank, local):
     roof, clocks, kernels, launches, e2e = head["roofline"], head["clocks"], head["kernels"], head["launches"], head["e2e"]
     paths_out = {p: {"value": r["value"], "ms_per_step": r["ms"] / args.steps, "kernel_ms_per_step": r["kernels"],
                      "roofline_kernel": r["roofline"]["kernel"], "roofline_frac": r["roofline"]["frac"],
-                     "description": r["description"]} for p, r in res.items()}
+                     "description": r["description"], "autotune": r["autotune"]} for p, r in res.items()}
     mixed = [p for p in res if p != "fp32"]
     ratio = res[mixed[0]]["value"] / res["fp32"]["value"] if mixed and "fp32" in res else None
 
@@ -732,6 +745,8 @@ def main():
     ap.add_argument("--precision", choices=("both", "fp32", "f16x3"), default="both",
                     help="arithmetic path(s) timed; 'both' reports the faster as value and the other beside it")
     ap.add_argument("--tc-local", action="store_true", help="f16x3: local integral on the tensor cores too")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="time the default variant of each path instead of the autotuned one")
     ap.add_argument("--dr-steps", type=int, default=200,
                     help="steps of the dynamic-rupture measurement (plain and warm-started); 0 skips it")
     ap.add_argument("--combined-steps", type=int, default=10,

@@ -176,7 +176,24 @@ int sei_evaluate_taylor(sei_ctx* ctx, const double* coeffs, float* out_device);
 /* SEI_OPT_TC_LOCAL (SEI_PREC_F16X3 only): 1 runs the local integral on the tensor cores as
  * well; 0 (default) runs it on the FP32 CUDA cores, which is faster at orders 4-6. */
 #define SEI_OPT_TC_LOCAL 3
+/* SEI_OPT_NB_CTAS (SEI_PREC_F16X3 only): persistent CTAs per SM of the tensor-core neighbour
+ * kernel, 1..3 (default 3). */
+#define SEI_OPT_NB_CTAS 4
 int sei_set_option(sei_ctx* ctx, int option, int value);
+
+/* Autotuner (no counterpart in the reference, whose kernel shapes are fixed when its code is
+ * generated): times `steps` steps of kernel 'all' on the context's own mesh for every variant of
+ * the step this library has: SEI_OPT_FUSED_LOCAL 0/1 at SEI_PREC_FP32; SEI_OPT_TC_LOCAL 0/1 x
+ * SEI_OPT_NB_CTAS 1..3 at SEI_PREC_F16X3.  It keeps the fastest variant as the context's options.
+ * The DOFs are restored after every variant, so the call leaves the state unchanged.  Global
+ * stepping of the elastic kernels only (SEI_ERR_UNSUPPORTED after sei_visco_setup or
+ * sei_lts_setup).  Synchronous. */
+typedef struct sei_tune_result {
+  int fused_local, tc_local, nb_ctas; /* chosen options */
+  int candidates;                     /* variants timed */
+  double best_ms, worst_ms;           /* per step, fastest and slowest variant */
+} sei_tune_result;
+int sei_autotune(sei_ctx* ctx, double dt, int steps, sei_tune_result* out);
 
 /* Runs a proxy kernel for nsteps steps (src/Proxy/Runner.cpp:99-111); asynchronous. */
 int sei_run(sei_ctx* ctx, int kernel, double dt, int nsteps);

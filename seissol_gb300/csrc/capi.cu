@@ -80,6 +80,7 @@ struct sei_ctx {
   float* d_trace = nullptr;
   bool trace_valid = false;
   bool tc_local = false;  // SEI_OPT_TC_LOCAL
+  int nb_ctas = 3;        // SEI_OPT_NB_CTAS: persistent CTAs per SM of the tensor-core neighbour kernel
   std::vector<cudaEvent_t> prof_events;
   std::vector<int> prof_kind;  // kind of the launch starting at event i: 0 ADER (or fused ADER + local),
                                // 1 neighbour, 2 fault, 3 local integral, 4 LTS gather / buffer, -1 end of run
@@ -92,9 +93,11 @@ struct sei_ctx {
   double lts_dt0 = 0.0;
   std::vector<int64_t> cl_start, b_start, g_start;  // [ncl + 1] each
   std::vector<int64_t> lts_perm;                    // new cell -> cell before sei_lts_setup
-  int32_t* d_src = nullptr;                         // [n][4] pool block read through each face
+  int32_t* d_src = nullptr;                         // [n][4] pool block read through each face (even sub-step)
+  int32_t* d_src1 = nullptr;                        // the same for the odd sub-step of a coarser neighbour's step
   int32_t *d_bcell = nullptr, *d_bdst = nullptr;    // buffer entries, grouped by cluster
-  int32_t *d_gsrc = nullptr, *d_gdst = nullptr;     // gather entries (derivative slot -> pool block)
+  int32_t *d_gsrc = nullptr, *d_gdst = nullptr;     // half-step entries: derivative slot -> first-half block
+  int32_t* d_gdst1 = nullptr;                       // second-half block
   int32_t* d_fidx = nullptr;                        // fault faces grouped by cluster
   std::vector<int64_t> f_start;                     // [ncl + 1] ranges of d_fidx
   // viscoelastic (sei_visco_setup): 27 quantities per cell in Q and I
@@ -148,13 +151,14 @@ void freeArrays(sei_ctx* c) {
   cudaFree(c->d_trace);
   c->d_trace = nullptr;
   c->trace_valid = false;
-  for (void* p : {(void*)c->d_src, (void*)c->d_bcell, (void*)c->d_bdst, (void*)c->d_gsrc, (void*)c->d_gdst, (void*)c->d_fidx,
+  for (void* p : {(void*)c->d_src, (void*)c->d_src1, (void*)c->d_bcell, (void*)c->d_bdst, (void*)c->d_gsrc,
+                  (void*)c->d_gdst, (void*)c->d_gdst1, (void*)c->d_fidx,
                   (void*)c->d_grad, (void*)c->d_theta, (void*)c->d_wplus, (void*)c->d_wminus})
     cudaFree(p);
   c->d_grad = c->d_theta = c->d_wplus = c->d_wminus = nullptr;
   c->visco = false;
   c->nq = 9;
-  c->d_src = c->d_bcell = c->d_bdst = c->d_gsrc = c->d_gdst = c->d_fidx = nullptr;
+  c->d_src = c->d_src1 = c->d_bcell = c->d_bdst = c->d_gsrc = c->d_gdst = c->d_gdst1 = c->d_fidx = nullptr;
   if (c->lts_exec) cudaGraphExecDestroy(c->lts_exec);
   c->lts_exec = nullptr;
   c->lts = false;
@@ -316,7 +320,7 @@ int launchNeighbor(sei_ctx* c, const sei::DeviceArrays& d) {
         return fail(c, SEI_ERR_CUDA, "tensor-core trace kernel launch failed");
       c->trace_valid = true;
     }
-    if (sei::launchNeighborTensorCore(c->cfg.order, d, c->d_trace, c->d_status, c->sms, c->stream) != 0)
+    if (sei::launchNeighborTensorCore(c->cfg.order, d, c->d_trace, c->d_status, c->sms, c->nb_ctas, c->stream) != 0)
       return fail(c, SEI_ERR_CUDA, "tensor-core neighbour kernel launch failed");
     return SEI_OK;
   }
@@ -724,6 +728,10 @@ int sei_set_option(sei_ctx* c, int option, int value) {
     case SEI_OPT_TC_LOCAL:
       c->tc_local = value != 0;
       c->trace_valid = false;
+      return SEI_OK;
+    case SEI_OPT_NB_CTAS:
+      if (value < 1 || value > 3) return fail(c, SEI_ERR_ARG, "SEI_OPT_NB_CTAS takes 1, 2 or 3");
+      c->nb_ctas = value;
       return SEI_OK;
     default:
       return fail(c, SEI_ERR_ARG, "unknown option");
@@ -1467,36 +1475,49 @@ int sei_lts_setup(sei_ctx* c, double cfl, int max_clusters, int* nclusters) {
       if (cn[c->fault.plus_cell[f]] == k) fidx.push_back((int32_t)f);
     fst[k + 1] = (int64_t)fidx.size();
   }
-  // per-face sources; buffer and gather entries grouped by the cluster of the reading cell
-  std::vector<int32_t> src((size_t)n * 4);
+  // every cell with a finer neighbour gets two half-step blocks, the Taylor integrals of its step's
+  // first and second half (computed once after its ADER); a finer cell's face reads the one of its
+  // sub-step, through the source table of that parity
+  std::vector<int32_t> hslot(n, -1);
+  int64_t nH = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    bool finer = false;
+    for (int f = 0; f < 4; ++f)
+      if (c->mesh.ftype[i * 4 + f] == 0) finer |= cn[c->mesh.nbr[i * 4 + f]] < cn[i];
+    if (finer) hslot[i] = (int32_t)nH++;
+  }
+  // per-face sources (two parities); buffer entries grouped by the cluster of the reading cell,
+  // half-step entries by the cluster of the coarse cell
+  std::vector<int32_t> src((size_t)n * 4), src1((size_t)n * 4);
   std::vector<std::vector<int32_t>> bc(ncl), bd(ncl), gs(ncl), gd(ncl);
-  int64_t nS = 0;
   for (int64_t i = 0; i < n; ++i) {
     if (bslot[i] >= 0) {
       bc[cn[i]].push_back((int32_t)i);
       bd[cn[i]].push_back((int32_t)(n + bslot[i]));
     }
+    if (hslot[i] >= 0) {
+      gs[cn[i]].push_back(dsl[i]);
+      gd[cn[i]].push_back((int32_t)(n + nB + 2 * hslot[i]));
+    }
     for (int f = 0; f < 4; ++f) {
       const int32_t nb = c->mesh.nbr[i * 4 + f];
-      if (c->mesh.ftype[i * 4 + f] != 0) {
-        src[i * 4 + f] = nb;
-        continue;
+      int32_t a = nb, b = nb;
+      if (c->mesh.ftype[i * 4 + f] == 0) {
+        const int d = cn[nb] - cn[i];
+        if (d < 0) {
+          a = b = (int32_t)(n + bslot[nb]);
+        } else if (d > 0) {
+          a = (int32_t)(n + nB + 2 * hslot[nb]);
+          b = a + 1;
+        }
       }
-      const int d = cn[nb] - cn[i];
-      if (d == 0) {
-        src[i * 4 + f] = nb;
-      } else if (d < 0) {
-        src[i * 4 + f] = (int32_t)(n + bslot[nb]);
-      } else {
-        const int64_t blkIdx = n + nB + nS++;
-        src[i * 4 + f] = (int32_t)blkIdx;
-        gs[cn[i]].push_back(dsl[nb]);
-        gd[cn[i]].push_back((int32_t)blkIdx);
-      }
+      src[i * 4 + f] = a;
+      src1[i * 4 + f] = b;
     }
   }
+  const int64_t nS = 2 * nH;
   if (n + nB + nS > INT32_MAX) return fail(c, SEI_ERR_ARG, "mesh too large for 32-bit pool indices");
-  std::vector<int32_t> fbc, fbd, fgs, fgd;
+  std::vector<int32_t> fbc, fbd, fgs, fgd, fgd1;
   std::vector<int64_t> bs(ncl + 1, 0), gst(ncl + 1, 0);
   for (int k = 0; k < ncl; ++k) {
     fbc.insert(fbc.end(), bc[k].begin(), bc[k].end());
@@ -1506,6 +1527,7 @@ int sei_lts_setup(sei_ctx* c, double cfl, int max_clusters, int* nclusters) {
     bs[k + 1] = (int64_t)fbc.size();
     gst[k + 1] = (int64_t)fgs.size();
   }
+  for (int32_t v : fgd) fgd1.push_back(v + 1);
   // device: the I pool, derivative slots, tables
   cudaFree(c->I);
   c->I = nullptr;
@@ -1519,8 +1541,9 @@ int sei_lts_setup(sei_ctx* c, double cfl, int max_clusters, int* nclusters) {
   if (nD > 0 && cudaMalloc(&c->derivs, (size_t)nD * dsz * sizeof(float)) != cudaSuccess)
     return fail(c, SEI_ERR_OOM, "LTS derivative allocation");
   c->nslots = nD;
-  if ((rc = upload(c, &c->dslot, dsl)) || (rc = upload(c, &c->d_src, src)) || (rc = upload(c, &c->d_bcell, fbc)) ||
-      (rc = upload(c, &c->d_bdst, fbd)) || (rc = upload(c, &c->d_gsrc, fgs)) || (rc = upload(c, &c->d_gdst, fgd)))
+  if ((rc = upload(c, &c->dslot, dsl)) || (rc = upload(c, &c->d_src, src)) || (rc = upload(c, &c->d_src1, src1)) ||
+      (rc = upload(c, &c->d_bcell, fbc)) || (rc = upload(c, &c->d_bdst, fbd)) || (rc = upload(c, &c->d_gsrc, fgs)) ||
+      (rc = upload(c, &c->d_gdst, fgd)) || (rc = upload(c, &c->d_gdst1, fgd1)))
     return rc;
   if (nf > 0) {
     if ((rc = upload(c, &c->d_fidx, fidx)) || (rc = upload(c, &c->d_pslot, pslot)) || (rc = upload(c, &c->d_mslot, mslot)) ||
@@ -1541,7 +1564,7 @@ int sei_lts_setup(sei_ctx* c, double cfl, int max_clusters, int* nclusters) {
 
 namespace {
 // Cells [s, e) of the context as a kernel view; the neighbour view reads the pool through d_src.
-sei::DeviceArrays rangeView(sei_ctx* c, int64_t s, int64_t e, bool neighbour) {
+sei::DeviceArrays rangeView(sei_ctx* c, int64_t s, int64_t e, bool neighbour, int parity = 0) {
   const size_t blk = (size_t)9 * c->Bp;
   sei::DeviceArrays d{};
   d.n = (int)(e - s);
@@ -1552,13 +1575,13 @@ sei::DeviceArrays rangeView(sei_ctx* c, int64_t s, int64_t e, bool neighbour) {
   d.star_nz = c->star_nz + s * 3 * sei::kStarNnz;
   d.aplus = c->aplus + s * 4 * 81;
   d.aminus = c->aminus + s * 4 * 81;
-  d.nbr = (neighbour ? c->d_src : c->nbr) + s * 4;
+  d.nbr = (neighbour ? (parity ? c->d_src1 : c->d_src) : c->nbr) + s * 4;
   d.rel = c->rel + s * 4;
   d.ftype = c->ftype + s * 4;
   return d;
 }
 
-sei::ViscoArrays viscoRangeView(sei_ctx* c, int64_t s, int64_t e, bool neighbour) {
+sei::ViscoArrays viscoRangeView(sei_ctx* c, int64_t s, int64_t e, bool neighbour, int parity = 0) {
   const size_t blk = (size_t)c->nq * c->Bp;
   sei::ViscoArrays v = viscoArrays(c);
   v.n = (int)(e - s);
@@ -1571,7 +1594,7 @@ sei::ViscoArrays viscoRangeView(sei_ctx* c, int64_t s, int64_t e, bool neighbour
   v.wplus = c->d_wplus + s * 4 * 54;
   v.aminus = c->aminus + s * 4 * 81;
   v.wminus = c->d_wminus + s * 4 * 54;
-  v.nbr = (neighbour ? c->d_src : c->nbr) + s * 4;
+  v.nbr = (neighbour ? (parity ? c->d_src1 : c->d_src) : c->nbr) + s * 4;
   v.rel = c->rel + s * 4;
   v.ftype = c->ftype + s * 4;
   v.derivs = c->derivs;
@@ -1580,10 +1603,10 @@ sei::ViscoArrays viscoRangeView(sei_ctx* c, int64_t s, int64_t e, bool neighbour
 }
 
 // One cycle: every cluster advances by dt0 2^(ncl-1).  Sub-step k of the finest cluster starts
-// with the predictions (ADER, integration buffer, local integral) of the clusters whose step begins
-// at k, then the corrections (coarse-neighbour Taylor integrals, the fault faces of the cluster,
-// neighbour flux) of the clusters whose step ends at k + 1 (TimeCluster predict / correct,
-// TimeCommon::computeIntegrals).
+// with the predictions (ADER, the half-step integrals of cells with a finer neighbour, integration
+// buffer, local integral) of the clusters whose step begins at k, then the corrections (the fault
+// faces of the cluster, neighbour flux) of the clusters whose step ends at k + 1 (TimeCluster
+// predict / correct, TimeCommon::computeIntegrals).
 int ltsCycle(sei_ctx* c) {
   const int blk = c->nq * c->Bp;
   const int64_t steps = (int64_t)1 << (c->ncl - 1);
@@ -1594,7 +1617,8 @@ int ltsCycle(sei_ctx* c) {
       if (k % len) continue;
       const int64_t s = c->cl_start[cl], e = c->cl_start[cl + 1];
       if (s == e) continue;
-      taylorCoeffs(c->cfg.order, c->lts_dt0 * (double)len, co);
+      const double dtc = c->lts_dt0 * (double)len;
+      taylorCoeffs(c->cfg.order, dtc, co);
       sei::DeviceArrays d = rangeView(c, s, e, false);
       const sei::ViscoArrays v = c->visco ? viscoRangeView(c, s, e, false) : sei::ViscoArrays{};
       int rc;
@@ -1603,6 +1627,21 @@ int ltsCycle(sei_ctx* c) {
         if (c->vk.ader(v, co, c->stream)) return fail(c, SEI_ERR_CUDA, "viscoelastic ADER launch failed");
       } else if ((rc = launchAderOnly(c, d, co))) {
         return rc;
+      }
+      // the two half-step integrals of the cells with a finer neighbour (TimeCommon.cpp:40-87,
+      // evaluated once per coarse step instead of once per reading face)
+      const int64_t gs = c->g_start[cl], ge = c->g_start[cl + 1];
+      if (ge > gs) {
+        if ((rc = profMark(c, 4))) return rc;
+        const int m = (int)(ge - gs);
+        for (int half = 0; half < 2; ++half) {
+          subCoeffs(c->cfg.order, 0.5 * dtc * half, 0.5 * dtc * (half + 1), co);
+          const int32_t* dst = (half ? c->d_gdst1 : c->d_gdst) + gs;
+          if (c->visco ? sei::launchTaylorGatherFull(m, c->d_gsrc + gs, dst, c->derivs, c->cfg.order, c->nq,
+                                                     sei::numBasis(c->cfg.order), c->Bp, co, c->I, c->stream)
+                       : c->k.taylorGather(m, c->d_gsrc + gs, dst, c->derivs, co, c->I, c->stream))
+            return fail(c, SEI_ERR_CUDA, "LTS half-step kernel launch failed");
+        }
       }
       const int64_t bs = c->b_start[cl], be = c->b_start[cl + 1];
       if (be > bs) {
@@ -1624,20 +1663,8 @@ int ltsCycle(sei_ctx* c) {
       if ((k + 1) % len) continue;
       const int64_t s = c->cl_start[cl], e = c->cl_start[cl + 1];
       if (s == e) continue;
-      const int64_t gs = c->g_start[cl], ge = c->g_start[cl + 1];
-      if (ge > gs) {
-        // position of this step inside the step of the next coarser cluster
-        const int64_t s0 = k + 1 - len;
-        const double a = (double)(s0 % (2 * len)) * c->lts_dt0, b = a + (double)len * c->lts_dt0;
-        subCoeffs(c->cfg.order, a, b, co);
-        int rc = profMark(c, 4);
-        if (rc) return rc;
-        const int m = (int)(ge - gs);
-        if (c->visco ? sei::launchTaylorGatherFull(m, c->d_gsrc + gs, c->d_gdst + gs, c->derivs, c->cfg.order, c->nq,
-                                                   sei::numBasis(c->cfg.order), c->Bp, co, c->I, c->stream)
-                     : c->k.taylorGather(m, c->d_gsrc + gs, c->d_gdst + gs, c->derivs, co, c->I, c->stream))
-          return fail(c, SEI_ERR_CUDA, "LTS gather kernel launch failed");
-      }
+      // which half of the next coarser cluster's step this step is
+      const int parity = (int)(((k + 1 - len) / len) % 2);
       // the fault faces of this cluster first (TimeCluster.cpp:804-823), over its own step
       if (!c->f_start.empty() && c->f_start[cl + 1] > c->f_start[cl]) {
         int rc = profMark(c, 2);
@@ -1651,11 +1678,11 @@ int ltsCycle(sei_ctx* c) {
       if (c->visco) {
         int rc = profMark(c, 1);
         if (rc) return rc;
-        if (c->vk.neighbor(viscoRangeView(c, s, e, true), c->stream))
+        if (c->vk.neighbor(viscoRangeView(c, s, e, true, parity), c->stream))
           return fail(c, SEI_ERR_CUDA, "viscoelastic neighbour launch failed");
         continue;
       }
-      int rc = launchNeighbor(c, rangeView(c, s, e, true));
+      int rc = launchNeighbor(c, rangeView(c, s, e, true, parity));
       if (rc) return rc;
     }
   }
@@ -1752,6 +1779,77 @@ int sei_kernel_times_by_kind(sei_ctx* c, double* ms, int* counts) {
     ++counts[k];
   }
   return SEI_OK;
+}
+
+int sei_autotune(sei_ctx* c, double dt, int steps, sei_tune_result* out) {
+  int rc = checkReady(c);
+  if (rc) return rc;
+  if (c->visco || c->lts) return fail(c, SEI_ERR_UNSUPPORTED, "the autotuner covers global stepping of the elastic kernels");
+  if (!(dt > 0) || steps < 1 || steps > 1000) return fail(c, SEI_ERR_ARG, "dt > 0, 1 <= steps <= 1000");
+  struct Cand {
+    int fused, tcLocal, nbCtas;
+  };
+  std::vector<Cand> cands;
+  if (c->cfg.precision == SEI_PREC_FP32) {
+    cands = {{0, 0, 3}, {1, 0, 3}};
+  } else {
+    for (int t = 0; t < 2; ++t)
+      for (int k = 1; k <= 3; ++k) cands.push_back({0, t, k});
+  }
+  // the DOFs are restored after every candidate: tuning leaves the state unchanged
+  const size_t bytes = (size_t)c->n * 9 * c->Bp * sizeof(float);
+  float* save = nullptr;
+  if (cudaMalloc(&save, bytes) != cudaSuccess) return fail(c, SEI_ERR_OOM, "autotuner DOF copy");
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  const bool prof = c->profiling;
+  c->profiling = false;
+  auto done = [&](int code) {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(save);
+    c->profiling = prof;
+    return code;
+  };
+  if (cudaMemcpyAsync(save, c->Q, bytes, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    return done(fail(c, SEI_ERR_CUDA, "autotuner set-up"));
+  double best = 1e300, worst = 0.0;
+  Cand pick = cands[0];
+  for (const Cand& k : cands) {
+    c->fused_local = k.fused != 0;
+    c->tc_local = k.tcLocal != 0;
+    c->nb_ctas = k.nbCtas;
+    c->trace_valid = false;
+    if ((rc = runKernel(c, SEI_KERNEL_ALL, dt, 1))) return done(rc);  // warm-up
+    if (cudaEventRecord(e0, c->stream) != cudaSuccess) return done(fail(c, SEI_ERR_CUDA, "event record"));
+    if ((rc = runKernel(c, SEI_KERNEL_ALL, dt, steps))) return done(rc);
+    float ms = 0.f;
+    if (cudaEventRecord(e1, c->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+      return done(fail(c, SEI_ERR_CUDA, "autotuner timing"));
+    const double per = (double)ms / steps;
+    if (per < best) {
+      best = per;
+      pick = k;
+    }
+    worst = per > worst ? per : worst;
+    if (cudaMemcpyAsync(c->Q, save, bytes, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess)
+      return done(fail(c, SEI_ERR_CUDA, "autotuner DOF restore"));
+  }
+  c->fused_local = pick.fused != 0;
+  c->tc_local = pick.tcLocal != 0;
+  c->nb_ctas = pick.nbCtas;
+  c->trace_valid = false;
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return done(fail(c, SEI_ERR_CUDA, "autotuner sync"));
+  if (out) {
+    out->fused_local = pick.fused;
+    out->tc_local = pick.tcLocal;
+    out->nb_ctas = pick.nbCtas;
+    out->candidates = (int)cands.size();
+    out->best_ms = best;
+    out->worst_ms = worst;
+  }
+  return done(SEI_OK);
 }
 
 int sei_metrics(const sei_ctx* c, int kernel, sei_perf* out) {

@@ -217,7 +217,8 @@ struct TcNbArgs {
   const float* scRd;
   int* status;
 };
-int launchNeighborTensorCore(int order, const DeviceArrays& d, const float* trace, int* status, int sms,
+// ctasPerSm: persistent CTAs per SM (1..3; 3 fit the shared memory at order 6)
+int launchNeighborTensorCore(int order, const DeviceArrays& d, const float* trace, int* status, int sms, int ctasPerSm,
                              void* stream);
 // Floats per cell of the face-trace array of the tensor-core path: 4 faces x 9 quantities x FP.
 inline int traceFloatsPerCell(int order) { return 4 * 9 * ((numFaceBasis(order) + 3) / 4 * 4); }

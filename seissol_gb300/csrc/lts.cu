@@ -32,23 +32,24 @@ __global__ void sei_lts_buffer(int m, const int32_t* __restrict__ cell, const in
   }
 }
 
-// One thread per (entry e, quantity q): pool[dst[e]][q][k] = sum_i coeffs[i] d[src[e]][i][q][k] for
-// k < b, zero for b <= k < bp (Taylor integral of stored full-row derivatives).
+// One thread per (entry e, quantity q, basis k < bp), consecutive threads along k (coalesced):
+// pool[dst[e]][q][k] = sum_i coeffs[i] d[src[e]][i][q][k] for k < b, zero for b <= k < bp
+// (Taylor integral of stored full-row derivatives).
 __global__ void sei_taylor_gather_full(int m, const int32_t* __restrict__ src, const int32_t* __restrict__ dst,
                                        const float* __restrict__ derivs, int order, int nq, int b, int bp,
                                        SeiCoeffsGather coeffs, float* __restrict__ pool) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long)m * nq) return;
-  const long e = t / nq;
-  const int q = (int)(t % nq);
-  const float* d = derivs + (size_t)__ldg(src + e) * order * nq * b + (size_t)q * b;
-  float* o = pool + ((size_t)__ldg(dst + e) * nq + q) * bp;
-  for (int k = 0; k < bp; ++k) {
-    float v = 0.f;
-    if (k < b)
-      for (int i = 0; i < order; ++i) v = fmaf(coeffs.c[i], __ldg(d + (size_t)i * nq * b + k), v);
-    o[k] = v;
+  const long per = (long)nq * bp;
+  if (t >= (long)m * per) return;
+  const long e = t / per;
+  const int r = (int)(t - e * per);
+  const int q = r / bp, k = r - q * bp;
+  float v = 0.f;
+  if (k < b) {
+    const float* d = derivs + (size_t)__ldg(src + e) * order * nq * b + (size_t)q * b + k;
+    for (int i = 0; i < order; ++i) v = fmaf(coeffs.c[i], __ldg(d + (size_t)i * nq * b), v);
   }
+  pool[(size_t)__ldg(dst + e) * per + r] = v;
 }
 
 }  // namespace
@@ -61,7 +62,7 @@ int launchTaylorGatherFull(int m, const int32_t* src, const int32_t* dst, const 
   if (order < 1 || order > 8) return -1;
   SeiCoeffsGather c{};
   for (int i = 0; i < order; ++i) c.c[i] = coeffs[i];
-  const long threads = (long)m * nq;
+  const long threads = (long)m * nq * bp;
   sei_taylor_gather_full<<<(int)((threads + 255) / 256), 256, 0, (cudaStream_t)stream>>>(m, src, dst, derivs, order, nq,
                                                                                            b, bp, c, pool);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;

@@ -482,8 +482,8 @@ __global__ void __launch_bounds__(128, 3) sei_nb_tc(sei::TcNbArgs A) {
 }
 
 template <int ORD>
-int launchNbTc(const sei::DeviceArrays& d, const float* trace, int* status, int sms, void* stream, const void* opRdSym,
-               const void* scRdSym) {
+int launchNbTc(const sei::DeviceArrays& d, const float* trace, int* status, int sms, int ctasPerSm, void* stream,
+               const void* opRdSym, const void* scRdSym) {
   using Dm = NbDims<ORD>;
   sei::TcNbArgs a{};
   a.n = d.n;
@@ -502,7 +502,8 @@ int launchNbTc(const sei::DeviceArrays& d, const float* trace, int* status, int 
   if (cudaFuncSetAttribute(sei_nb_tc<ORD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Dm::kSmem) != cudaSuccess)
     return -1;
   const int ntiles = (d.n + kCellsPerTile - 1) / kCellsPerTile;
-  const int grid = ntiles < 3 * sms ? ntiles : 3 * sms;
+  const int perSm = ctasPerSm < 1 ? 1 : (ctasPerSm > 3 ? 3 : ctasPerSm);
+  const int grid = ntiles < perSm * sms ? ntiles : perSm * sms;
   if (grid <= 0) return 0;
   sei_nb_tc<ORD><<<grid, 128, Dm::kSmem, (cudaStream_t)stream>>>(a);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
@@ -530,17 +531,17 @@ int launchLintTensorCore(int order, const DeviceArrays& d, float* trace, int tra
 }
 
 
-int launchNeighborTensorCore(int order, const DeviceArrays& d, const float* trace, int* status, int sms,
+int launchNeighborTensorCore(int order, const DeviceArrays& d, const float* trace, int* status, int sms, int ctasPerSm,
                              void* stream) {
   switch (order) {
     case 4:
-      return launchNbTc<4>(d, trace, status, sms, stream, (const void*)&sei_tc_o4::krdivm_op,
+      return launchNbTc<4>(d, trace, status, sms, ctasPerSm, stream, (const void*)&sei_tc_o4::krdivm_op,
                            (const void*)&sei_tc_o4::krdivm_scale);
     case 5:
-      return launchNbTc<5>(d, trace, status, sms, stream, (const void*)&sei_tc_o5::krdivm_op,
+      return launchNbTc<5>(d, trace, status, sms, ctasPerSm, stream, (const void*)&sei_tc_o5::krdivm_op,
                            (const void*)&sei_tc_o5::krdivm_scale);
     case 6:
-      return launchNbTc<6>(d, trace, status, sms, stream, (const void*)&sei_tc_o6::krdivm_op,
+      return launchNbTc<6>(d, trace, status, sms, ctasPerSm, stream, (const void*)&sei_tc_o6::krdivm_op,
                            (const void*)&sei_tc_o6::krdivm_scale);
     default:
       return -1;

@@ -62,6 +62,11 @@ class _Perf(C.Structure):
     _fields_ = [("nonzero_flop", C.c_double), ("hardware_flop", C.c_double), ("bytes", C.c_double)]
 
 
+class _Tune(C.Structure):
+    _fields_ = [("fused_local", C.c_int), ("tc_local", C.c_int), ("nb_ctas", C.c_int), ("candidates", C.c_int),
+                ("best_ms", C.c_double), ("worst_ms", C.c_double)]
+
+
 _lib = None
 VP = C.c_void_p
 
@@ -107,6 +112,7 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_sync", i, [VP])
     _sig(lib, "sei_last_run_ms", i, [VP, C.POINTER(d)])
     _sig(lib, "sei_metrics", i, [VP, i, C.POINTER(_Perf)])
+    _sig(lib, "sei_autotune", i, [VP, d, i, C.POINTER(_Tune)])
     _sig(lib, "sei_set_profiling", i, [VP, i])
     _sig(lib, "sei_set_option", i, [VP, i, i])
     _sig(lib, "sei_tc_gemm_check", i, [VP, VP, VP, i, i, i])
@@ -501,3 +507,9 @@ class Context:
         d = C.c_double()
         self._check(self.lib.sei_last_run_ms(self.h, C.byref(d)), "sei_last_run_ms")
         return d.value
+
+    def autotune(self, dt, steps=5):
+        """Times every variant of the step on this mesh, keeps the fastest (sei_autotune)."""
+        r = _Tune()
+        self._check(self.lib.sei_autotune(self.h, dt, int(steps), C.byref(r)), "sei_autotune")
+        return {k: getattr(r, k) for k, _ in _Tune._fields_}

@@ -100,3 +100,25 @@ def test_mixed_and_fp32_agree_on_larger_mesh(built_lib):
     assert max(errs) < 1e-5, errs
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("precision,ncand", [(0, 2), (PREC_F16X3, 6)])
+def test_autotune_keeps_state_and_results(built_lib, precision, ncand):
+    """sei_autotune times every variant of the step, restores the DOFs, keeps the fastest variant;
+    five steps with the chosen options then agree with the FP32 path within 1e-5."""
+    a, n, q0 = _ctx(6, precision, dims=(8, 8, 8), seed=5)
+    ref, _, _ = _ctx(6, 0, dims=(8, 8, 8), seed=5)
+    dt = a.cfl_timestep(0.5)
+    r = a.autotune(dt, 2)
+    assert r["candidates"] == ncand
+    assert 0 < r["best_ms"] <= r["worst_ms"]
+    assert r["nb_ctas"] in (1, 2, 3) and r["fused_local"] in (0, 1) and r["tc_local"] in (0, 1)
+    assert np.array_equal(a.get_dofs(), q0)
+    a.run("all", dt, 5)
+    ref.run("all", dt, 5)
+    a.sync()
+    ref.sync()
+    errs = rel_l2_per_quantity(a.get_dofs(), ref.get_dofs())
+    assert max(errs) < 1e-5, errs
+    a.close()
+    ref.close()
