@@ -7,8 +7,10 @@
  *   precompute stress    src/DynamicRupture/FrictionLaws/FrictionSolverCommon.h:146-200
  *   FVW rate and state   src/DynamicRupture/FrictionLaws/GpuImpl/RateAndState.h:51-270,
  *                        GpuImpl/FastVelocityWeakeningLaw.h:35-108, RateAndStateCommon.h:22-139
- *                        (per-point Newton; the outer fixed point stops when every point of the
- *                        face has converged, as the reference's warp-wide vote over one face)
+ *                        (per-point Newton; the outer fixed point stops when every point of a
+ *                        group of 32 consecutive face points has converged, as the reference's
+ *                        GPU warp vote deviceWarpAll, GpuImpl/RateAndState.h:138-142: one group
+ *                        per face up to 32 points, two at orders 5 and 6)
  *   state resampling     GpuImpl/FastVelocityWeakeningLaw.h:98-106 with the resample matrix
  *   imposed state        FrictionSolverCommon.h:333-420
  *   nodal flux           dynamic_rupture.py:174-190 (Q += V3mTo2nTWDivM(side, rel) . imposed . fluxSolver)
@@ -292,9 +294,11 @@ void oracle_dr_friction(int npts, int nts, int64_t nfaces, const oracle_rs_param
           vmag[k] = vm;
           lsr[k] = vm;
         }
+        for (int g0 = 0; g0 < npts; g0 += 32) {  /* one vote per group of 32 points */
+        const int g1 = g0 + 32 < npts ? g0 + 32 : npts;
         for (int j = 0; j < P->max_outer; ++j) {
           int all = 1;
-          for (int k = 0; k < npts; ++k) {
+          for (int k = g0; k < g1; ++k) {
             const double ak = a[fo + k];
             psib[k] = state_update(P, ak, sref[k], dt, lsr[k]);
             double vnew = 0, munew = 0;
@@ -334,6 +338,7 @@ void oracle_dr_friction(int npts, int nts, int64_t nfaces, const oracle_rs_param
             all &= convo[k];
           }
           if (all) break;
+        }
         }
         for (int k = 0; k < npts; ++k) {
           const double ak = a[fo + k];

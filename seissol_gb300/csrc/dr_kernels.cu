@@ -1,5 +1,6 @@
 // Dynamic-rupture face kernel: one warp per fault face up to 32 face points (order 4), two warps
-// per face up to 64 points (orders 5 and 6: 36 and 49 points); one thread per point.
+// per face up to 64 points (orders 5 and 6: 36 and 49 points); one thread per point; the outer
+// fixed point stops per warp, as the reference's GPU solver.
 //
 // Per face and time step (reference: src/Kernels/DynamicRupture.cpp:57-168 projectToDR,
 // src/DynamicRupture/FrictionLaws/GpuImpl/BaseFrictionSolver.h:133-236 evaluatePoint,
@@ -9,7 +10,7 @@
 //      the stored CK derivatives, rotation by TinvT, evaluation at the face quadrature points;
 //   2. fast-velocity-weakening rate-and-state friction per point (lane): Newton on the slip
 //      rate inside a fixed point on the state variable; residual, slip rate, state variable
-//      and slip accumulation in float64; the fixed point stops when all points of the face
+//      and slip accumulation in float64; the fixed point stops when all points of the warp
 //      converged (warp vote);
 //   3. resampling of the state-variable increment (25x25 face projection);
 //   4. time-weighted imposed states of both sides;
@@ -199,19 +200,10 @@ __device__ __forceinline__ void faceSync(int fs) {
   }
 }
 
-// True when c holds on every thread of the face.  Two-warp faces vote through shared memory;
-// the flags alternate with the parity of the call so that one barrier per vote suffices.
-template <int TPF>
-__device__ __forceinline__ bool faceAll(bool c, int fs, int t, int parity, int (*flags)[2][2]) {
-  const bool w = __all_sync(0xffffffffu, c);
-  if constexpr (TPF == 32) {
-    return w;
-  } else {
-    if ((t & 31) == 0) flags[fs][parity][t >> 5] = w;
-    faceSync<TPF>(fs);
-    return flags[fs][parity][0] && flags[fs][parity][1];
-  }
-}
+// Convergence vote of the outer fixed point: over the warp, i.e. a group of 32 consecutive face
+// points, as the reference's GPU friction solver (deviceWarpAll, GpuImpl/RateAndState.h:138-142);
+// the two warps of a face at orders 5 and 6 leave the loop independently.
+__device__ __forceinline__ bool warpAll(bool c) { return __all_sync(0xffffffffu, c); }
 
 template <int N, int B, int NP>
 __global__ void __launch_bounds__(128, 3)
@@ -227,7 +219,6 @@ __global__ void __launch_bounds__(128, 3)
   __shared__ float sJ[FPB][B * 9];
   __shared__ float sG[FPB][NP * 9];
   __shared__ double sD[FPB][TPF];
-  __shared__ int sVote[FPB][2][2];
   __shared__ float sW[kMlpParams];
   const bool useMlp = A.mlp != nullptr;
   if (useMlp)
@@ -241,7 +232,6 @@ __global__ void __launch_bounds__(128, 3)
   if (f < 0 || f >= A.nfaces) return;
   const bool pt = lane < NP;
   const int k = pt ? lane : 0;
-  int votes = 0;
 
   // ---- 1. space-time interpolation of both sides at time point s (six quantities per point),
   // evaluated inside the friction loop so that only one time point is live at a time
@@ -356,7 +346,7 @@ __global__ void __launch_bounds__(128, 3)
         vmag = r.v;
         mu = r.mu;
       }
-      if (faceAll<TPF>(conv, warp, lane, votes++ & 1, sVote)) break;
+      if (warpAll(conv)) break;
     }
     if (pt) {
       psib = stateUpdate(A, inv, a, sref, dt, lsr);
