@@ -277,7 +277,9 @@ __global__ void __launch_bounds__(128, 3)
   // ---- 2. friction (lanes < NP own one point each)
   const size_t po = (size_t)f * NP + k;
   const double* imp = A.imp + (size_t)f * 8;
-  const double zp = imp[0], zs = imp[1], zpn = imp[2], zsn = imp[3], etap = imp[4], etas = imp[5], invEtaS = imp[6];
+  const double etap = imp[4], etas = imp[5], invEtaS = imp[6];
+  // reciprocal impedances, once per thread: FP64 divisions are costly on this part
+  const double rzp = 1.0 / imp[0], rzs = 1.0 / imp[1], rzpn = 1.0 / imp[2], rzsn = 1.0 / imp[3];
   const double a = pt ? A.a[po] : 0.01;
   const size_t plane = (size_t)A.nfaces * NP;  // init holds sn0, tau1_0, tau2_0 as [3][nf][npts]
   const double sn0 = pt ? A.init[po] : 0.0;
@@ -297,9 +299,9 @@ __global__ void __launch_bounds__(128, 3)
     interpolate(s, qc);
     const double dt = A.deltat[s];
     // precompute stress (etaPDamp = 1): qi order N, T1, T2, U, V, W
-    const double fsn = etap * ((double)qc[1][3] - qc[0][3] + qc[0][0] / zp + qc[1][0] / zpn);
-    const double ft1 = etas * ((double)qc[1][4] - qc[0][4] + qc[0][1] / zs + qc[1][1] / zsn);
-    const double ft2 = etas * ((double)qc[1][5] - qc[0][5] + qc[0][2] / zs + qc[1][2] / zsn);
+    const double fsn = etap * ((double)qc[1][3] - qc[0][3] + qc[0][0] * rzp + qc[1][0] * rzpn);
+    const double ft1 = etas * ((double)qc[1][4] - qc[0][4] + qc[0][1] * rzs + qc[1][1] * rzsn);
+    const double ft2 = etas * ((double)qc[1][5] - qc[0][5] + qc[0][2] * rzs + qc[1][2] * rzsn);
     double sn = fsn + sn0;
     sn = sn < 0 ? sn : 0.0;
     const double sref = psib;
@@ -355,8 +357,9 @@ __global__ void __launch_bounds__(128, 3)
       const double strength = -mu * sn;
       slip += vmag * dt;
       const double div = strength + etas * vmag;
-      v1 = vmag * tt1 / div;
-      v2 = vmag * tt2 / div;
+      const double vd = vmag / div;
+      v1 = vd * tt1;
+      v2 = vd * tt2;
       tr1 = ft1 - etas * v1;
       tr2 = ft2 - etas * v2;
       slip1 += v1 * dt;
@@ -365,15 +368,15 @@ __global__ void __launch_bounds__(128, 3)
       isM[0] += w * fsn;
       isM[1] += w * tr1;
       isM[2] += w * tr2;
-      isM[3] += w * (qc[1][3] - (fsn - qc[1][0]) / zpn);
-      isM[4] += w * (qc[1][4] - (tr1 - qc[1][1]) / zsn);
-      isM[5] += w * (qc[1][5] - (tr2 - qc[1][2]) / zsn);
+      isM[3] += w * (qc[1][3] - (fsn - qc[1][0]) * rzpn);
+      isM[4] += w * (qc[1][4] - (tr1 - qc[1][1]) * rzsn);
+      isM[5] += w * (qc[1][5] - (tr2 - qc[1][2]) * rzsn);
       isP[0] += w * fsn;
       isP[1] += w * tr1;
       isP[2] += w * tr2;
-      isP[3] += w * (qc[0][3] + (fsn - qc[0][0]) / zp);
-      isP[4] += w * (qc[0][4] + (tr1 - qc[0][1]) / zs);
-      isP[5] += w * (qc[0][5] + (tr2 - qc[0][2]) / zs);
+      isP[3] += w * (qc[0][3] + (fsn - qc[0][0]) * rzp);
+      isP[4] += w * (qc[0][4] + (tr1 - qc[0][1]) * rzs);
+      isP[5] += w * (qc[0][5] + (tr2 - qc[0][2]) * rzs);
     }
   }
 
