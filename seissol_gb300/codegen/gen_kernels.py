@@ -183,11 +183,11 @@ def gen_order(order: int) -> str:
             a("    float T[kF];")
             _matvec(L, "    ", G["fMrT"][f], "I", "T", F, B, True)
             if with_trace:
-                a("    sei_stage_trace<kB, kF, kFP>(sm, lane, q, T);")
-            a(f"#pragma unroll\n    for (int m = 0; m < kF; ++m) Xq[m * 32] = T[m];")
+                a("    sei_stage_trace<kF, kF, kFP>(sm, lane, q, T);")
+            a(f"#pragma unroll\n    for (int m = 0; m < kF; ++m) X[(q * kF + m) * 32 + lane] = T[m];")
             a("    __syncthreads();")
             if with_trace:
-                a(f"    sei_store_traces<kB, kF, kFP, kCPB>(n, sm, trace, {f});")
+                a(f"    sei_store_traces<kF, kF, kFP, kCPB>(n, sm, trace, {f});")
             a(f"    const bool on = valid && ftype[(size_t)cl * 4 + {f}] != 1;")
             a(f"    const float* ap = aplus + ((size_t)cl * 4 + {f}) * 81 + 9 * q;")
             a("    float av[9];")
@@ -197,7 +197,7 @@ def gen_order(order: int) -> str:
                 if m not in bycol:
                     continue
                 a(f"    {{ float g = 0.f;")
-                a(f"#pragma unroll\n      for (int s = 0; s < 9; ++s) g = fmaf(X[(s * kB + {m}) * 32 + lane], av[s], g);")
+                a(f"#pragma unroll\n      for (int s = 0; s < 9; ++s) g = fmaf(X[(s * kF + {m}) * 32 + lane], av[s], g);")
                 for k, v in bycol[m]:
                     a(f"      acc[{k}] = fmaf({flit(v)}, g, acc[{k}]);")
                 a("    }")

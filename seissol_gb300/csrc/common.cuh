@@ -63,7 +63,8 @@ __device__ __forceinline__ void sei_cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// Face traces of the local-integral kernel, staged in shared memory after the exchange buffer:
+// Face traces of the local-integral kernel, staged in shared memory after the trace exchange
+// buffer of the flux stage ([9][R][32] floats, R = the template argument B):
 // the row of (cell lane, quantity q) holds FP floats (zero padded); a cell's 9 rows are followed
 // by 4 floats of padding, so 16-byte writes of a quarter warp (8 cells) hit distinct banks.
 template <int FP>

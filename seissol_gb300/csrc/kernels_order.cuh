@@ -58,8 +58,10 @@ int launchLint(const sei::DeviceArrays& d, void* stream) {
   if (d.n <= 0) return 0;
   const int blocks = (d.n + K::kCPB - 1) / K::kCPB;
   if (d.trace) {
-    // exchange buffer plus the staging rows of the stored face traces
-    const size_t smem = sizeof(float) * (9 * K::kB * 32 + 32 * seiTraceStageStride<K::kFP>());
+    // the volume stage's exchange buffer, which the flux stage reuses for its trace exchange
+    // ([9][kF][32]) followed by the staging rows of the stored face traces
+    const size_t vol = 9 * K::kB * 32, flux = 9 * K::kF * 32 + 32 * seiTraceStageStride<K::kFP>();
+    const size_t smem = sizeof(float) * (vol > flux ? vol : flux);
     if (cudaFuncSetAttribute(K::SEI_CAT(sei_lint_trace_o, SEI_ORDER), cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess)
       return -1;
