@@ -187,7 +187,7 @@ def gen_order(order: int) -> str:
             a(f"#pragma unroll\n    for (int m = 0; m < kF; ++m) X[(q * kF + m) * 32 + lane] = T[m];")
             a("    __syncthreads();")
             if with_trace:
-                a(f"    sei_store_traces<kF, kF, kFP, kCPB>(n, sm, trace, {f});")
+                a(f"    sei_store_traces<kF, kF, kFP, kCPB>(n, sm, trace, {f}, tplane);")
             a(f"    const bool on = valid && ftype[(size_t)cl * 4 + {f}] != 1;")
             a(f"    const float* ap = aplus + ((size_t)cl * 4 + {f}) * 81 + 9 * q;")
             a("    float av[9];")
@@ -247,11 +247,12 @@ sei_lint_o{order}(int n, float* __restrict__ Q, const float* __restrict__ Iin, c
     a("}")
     a(f"""
 // The same local integral, which also stores the face traces fMrT_f I of every cell,
-// trace[4][n][9][kFP], for the neighbour kernel of the tensor-core path.
+// trace[4][tplane][9][kFP] (tplane cells per face plane; trace points at the first cell of this
+// launch), for the neighbour kernel of the tensor-core path.
 extern "C" __global__ void __launch_bounds__(288, 1)
 sei_lint_trace_o{order}(int n, float* __restrict__ Q, const float* __restrict__ Iin, const float* __restrict__ star_nz,
                         const float* __restrict__ aplus, const unsigned char* __restrict__ ftype,
-                        float* __restrict__ trace) {{""" + prologue)
+                        float* __restrict__ trace, int tplane) {{""" + prologue)
     a("  float I[kBp];")
     a("  sei_load_col<kBp>(Iin + ((size_t)cl * 9 + q) * kBp, I);")
     emit_volume_flux(with_trace=True)

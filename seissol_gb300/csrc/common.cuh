@@ -82,14 +82,15 @@ __device__ __forceinline__ void sei_stage_trace(float* sm, int lane, int q, cons
   }
 }
 
-// Coalesced 16-byte store of the staged face-f traces of a CPB-cell block to trace[4][n][9][FP].
+// Coalesced 16-byte store of the staged face-f traces of a CPB-cell block to
+// trace[4][plane][9][FP] (n cells in this launch, plane cells per face plane).
 // Not unrolled: the generated kernels are large and their instruction cache is the limit.
 template <int B, int F, int FP, int CPB>
-__device__ __forceinline__ void sei_store_traces(int n, const float* sm, float* trace, int f) {
+__device__ __forceinline__ void sei_store_traces(int n, const float* sm, float* trace, int f, int plane) {
   constexpr int R4 = 9 * FP / 4;  // float4 per cell
   const float* st = sm + 9 * B * 32;
   const int cell0 = blockIdx.x * CPB;
-  float4* dst = reinterpret_cast<float4*>(trace + ((size_t)f * n + cell0) * 9 * FP);
+  float4* dst = reinterpret_cast<float4*>(trace + ((size_t)f * plane + cell0) * 9 * FP);
 #pragma unroll 1
   for (int idx = threadIdx.x; idx < CPB * R4; idx += blockDim.x) {
     const int L = idx / R4, rem = idx - L * R4;

@@ -64,7 +64,9 @@ struct DeviceArrays {
   const int32_t* nbr;
   const uint8_t* rel;    // side | orient << 2
   const uint8_t* ftype;  // 0 regular, 1 dynamic rupture, 2 none
-  float* trace = nullptr;  // nullable: face traces fMrT_f I out of the local integral, [4][n][9][FP]
+  float* trace = nullptr;  // nullable: face traces fMrT_f I out of the local integral, [4][ntotal][9][FP]
+  int ntotal = 0;          // cells of the whole mesh when this view covers a range of them (0: n)
+  int first = 0;           // first cell of the range
 };
 
 using LaunchLocalFn = int (*)(const DeviceArrays&, const float* coeffs, void* stream);
@@ -197,7 +199,8 @@ struct TcLintArgs {
   const float* scVol;     // per-row power-of-two scales of the operand tables
   const uint16_t* opRd;
   const float* scRd;
-  float* trace;   // nullable: face traces fMrT_f I out, [4][n][9][FP] (FP = F rounded up to 4)
+  float* trace;   // nullable: face traces fMrT_f I out, [4][tplane][9][FP] (FP = F rounded up to 4)
+  int tplane;     // cells per face plane of the traces (trace points at this launch's first cell)
   int traceOnly;  // 1: write the traces only (Q unchanged)
   int* status;    // set to 1 when a wait gave up
 };
@@ -206,7 +209,8 @@ int launchLintTensorCore(int order, const DeviceArrays& d, float* trace, int tra
 
 // Arguments of the tensor-core neighbour kernel (face traces in, Q updated in place).
 struct TcNbArgs {
-  int n;
+  int n;       // cells of this launch (Q, aminus, nbr, rel, ftype point at its first cell)
+  int ntotal;  // cells of the mesh: face-plane stride of the traces, range of neighbour indices
   float* Q;
   const float* trace;  // [4][n][9][FP] traces fMrT_f I of every cell and face
   const float* aminus;

@@ -66,7 +66,7 @@ int launchLint(const sei::DeviceArrays& d, void* stream) {
                              (int)smem) != cudaSuccess)
       return -1;
     K::SEI_CAT(sei_lint_trace_o, SEI_ORDER)<<<blocks, 288, smem, (cudaStream_t)stream>>>(
-        d.n, d.Q, d.I, d.star_nz, d.aplus, d.ftype, d.trace);
+        d.n, d.Q, d.I, d.star_nz, d.aplus, d.ftype, d.trace, d.ntotal > 0 ? d.ntotal : d.n);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
   }
   const size_t smem = sizeof(float) * 9 * K::kB * 32;

@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(128, 1) sei_lint_tc(sei::TcLintArgs A) {
     forColumns(tbase, 3 * B, 4 * F, [&](int t, float v) {
       const float x = v * sI * __ldg(A.scVol + 3 * B + t);
       X[t * 128 + r] = x;
-      if (trow) trow[(size_t)(t / F) * A.n * 9 * FP + t % F] = x;
+      if (trow) trow[(size_t)(t / F) * A.tplane * 9 * FP + t % F] = x;
     });
     if (A.traceOnly) {
       sei_tc::fenceBeforeSync();
@@ -271,6 +271,7 @@ int launchLintTc(const sei::DeviceArrays& d, float* trace, int traceOnly, int* s
   using Dm = Dims<ORD>;
   sei::TcLintArgs a{};
   a.trace = trace;
+  a.tplane = d.ntotal > 0 ? d.ntotal : d.n;
   a.traceOnly = traceOnly;
   a.n = d.n;
   a.Q = d.Q;
@@ -390,11 +391,11 @@ __global__ void __launch_bounds__(128, 3) sei_nb_tc(sei::TcNbArgs A) {
     for (int i = 0; i < 4; ++i) {
       const int nb = __ldg(A.nbr + (size_t)cl * 4 + i);
       const int rl = A.rel[(size_t)cl * 4 + i];
-      on[i] = cell < A.n && nb >= 0 && nb < A.n && A.ftype[(size_t)cl * 4 + i] == 0;
+      on[i] = cell < A.n && nb >= 0 && nb < A.ntotal && A.ftype[(size_t)cl * 4 + i] == 0;
       hs[i] = rl >> 2;
       float* xr = X + ((size_t)i * 128 + r) * FP;
       if (on[i]) {
-        const float* src = A.trace + (((size_t)(rl & 3) * A.n + nb) * 9 + q) * FP;
+        const float* src = A.trace + (((size_t)(rl & 3) * A.ntotal + nb) * 9 + q) * FP;
 #pragma unroll
         for (int m4 = 0; m4 < FP / 4; ++m4) sei_cp_async16(xr + 4 * m4, src + 4 * m4);
       }
@@ -462,8 +463,8 @@ __global__ void __launch_bounds__(128, 3) sei_nb_tc(sei::TcNbArgs A) {
     __syncthreads();
     sei_tc::fenceAfterSync();
     if (tid == 0) issueSplit(taddr, aHi, aLo, K2, rdHi, rdLo, K2, K2 / 16, sei_tc::idescF16(128, N2), &mbar);
-    if (pfNb >= 0 && pfNb < A.n)
-      sei_tc::prefetchL2(A.trace + ((size_t)(pfRl & 3) * A.n + pfNb) * 9 * FP, (uint32_t)(9 * FP * 4));
+    if (pfNb >= 0 && pfNb < A.ntotal)
+      sei_tc::prefetchL2(A.trace + ((size_t)(pfRl & 3) * A.ntotal + pfNb) * 9 * FP, (uint32_t)(9 * FP * 4));
     float acc[Bp];
     sei_load_col<Bp>(A.Q + ((size_t)cl * 9 + q) * Bp, acc);
     ok = sei_tc::mbarWait(&mbar, phase, kMaxPolls) && ok;
@@ -487,6 +488,7 @@ int launchNbTc(const sei::DeviceArrays& d, const float* trace, int* status, int 
   using Dm = NbDims<ORD>;
   sei::TcNbArgs a{};
   a.n = d.n;
+  a.ntotal = d.ntotal > 0 ? d.ntotal : d.n;
   a.Q = d.Q;
   a.trace = trace;
   a.aminus = d.aminus;

@@ -148,3 +148,18 @@ def test_mixed_outflow_faces(built_lib, order):
     errs = rel_l2_per_quantity(ctx.get_dofs(), ref)
     assert max(errs) < 1e-5, errs
     ctx.close()
+
+
+@pytest.mark.parametrize("precision,nsteps", [(0, 1), (0, 3), (PREC_F16X3, 1), (PREC_F16X3, 3)])
+def test_run_host_pipelined_matches_device_run(built_lib, precision, nsteps):
+    """sei_run_host pipelines the host copies with the step in chunks of cells; its result equals
+    sei_set_dofs + sei_run + sei_get_dofs bit for bit."""
+    a, n, q0 = _ctx(6, precision, dims=(8, 8, 8), seed=12)
+    dt = a.cfl_timestep(0.5)
+    out = np.empty_like(q0)
+    a.run_host("all", dt, nsteps, q0, out)
+    a.set_dofs(q0)
+    a.run("all", dt, nsteps)
+    a.sync()
+    assert np.array_equal(out, a.get_dofs())
+    a.close()
