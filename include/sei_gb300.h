@@ -197,7 +197,9 @@ int sei_autotune(sei_ctx* ctx, double dt, int steps, sei_tune_result* out);
 
 /* Runs a proxy kernel for nsteps steps (src/Proxy/Runner.cpp:99-111); asynchronous. */
 int sei_run(sei_ctx* ctx, int kernel, double dt, int nsteps);
-/* Same with host buffers: copies dofs_in to the device, runs, copies the result to dofs_out. */
+/* Same with host buffers: copies dofs_in to the device, runs, copies the result to dofs_out;
+ * synchronous.  Kernel 'all' on global steps is pipelined in chunks of cells: the copies in
+ * overlap ADER and the local integral, the copies out overlap the last neighbour flux. */
 int sei_run_host(sei_ctx* ctx, int kernel, double dt, int nsteps, const float* dofs_in, float* dofs_out);
 int sei_sync(sei_ctx* ctx);
 /* Device-side duration of the last sei_run, milliseconds (CUDA events on the context stream). */
