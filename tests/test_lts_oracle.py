@@ -4,7 +4,9 @@
 * on a graded cube (cube edges log-uniform in [h, 4 h]) the clustering gives several clusters,
   neighbours at most one cluster apart, and every cell's cluster step within its CFL step;
 * a plane wave advanced by LTS over two or more clusters has the accuracy of global stepping at
-  the finest step (its error against the exact solution within 10 % of that of global stepping).
+  the finest step (its error against the exact solution within 10 % of that of global stepping);
+* with a planar fault the two cells of every fault face share a cluster;
+* the viscoelastic adapter reproduces the dense viscoelastic oracle with one cluster (exactly).
 """
 import numpy as np
 import pytest
@@ -92,3 +94,55 @@ def test_lts_plane_wave_matches_global_stepping(built_lib, order):
     err = lambda q: np.sqrt((((q - qe) ** 2) * Md).sum() / ((qe ** 2) * Md).sum())
     e_lts, e_gts = err(q_lts), err(q_gts)
     assert e_lts < 1.1 * e_gts + 1e-9, (e_lts, e_gts)
+
+
+def test_clustering_keeps_fault_pairs_together(built_lib):
+    """A graded cube with a planar fault: both cells of every dynamic-rupture face share one
+    cluster, regular neighbours stay at most one cluster apart, and no cell is above the cluster
+    of its own CFL step."""
+    from seissol_gb300 import Context
+    order = 4
+    with Context(order, device=-1) as ctx:
+        ctx.build_periodic_cube(8, 6, 6, perturb=0.05, seed=9, grading=4.0, fault_plane=4)
+        cells = ctx.get_cells()
+        coords, material, _ = ctx.get_geometry()
+    vp = np.sqrt((material[:, 2] + 2 * material[:, 1]) / material[:, 0])
+    dt = dg_setup.cfl_timestep(coords, vp, order, 0.5)
+    ft, nb = cells["face_type"], cells["neighbor"]
+    cell_i, face_i = np.nonzero(ft == 1)
+    assert cell_i.size > 0
+    pairs = np.unique(np.sort(np.stack([cell_i, nb[cell_i, face_i]], axis=1), axis=1), axis=0)
+    cl, dt0 = oracle_py.lts_clusters(dt, nb, ft, 8, pairs)
+    assert cl.max() >= 1
+    assert np.array_equal(cl[pairs[:, 0]], cl[pairs[:, 1]])
+    reg = ft == 0
+    assert (np.abs(cl[:, None] - cl[np.where(reg, nb, 0)])[reg] <= 1).all()
+    own = np.clip(np.floor(np.log2(dt / dt0) + 1e-12).astype(np.int64), 0, 7)
+    assert (cl <= own).all()
+
+
+def test_visco_adapter_one_cluster_is_dense_global_stepping(built_lib):
+    """The viscoelastic adapter behind lts_cycles: with one cluster, two LTS cycles equal two steps
+    of the dense viscoelastic oracle exactly."""
+    from oracle import cube_mesh, visco
+    order = 4
+    topo, coords = cube_mesh.periodic_cube(4, 4, 4)
+    n = topo.shape[0]
+    nb, side, orient = dg_setup.face_relations(topo)
+    rho, vs, vp = 2700.0, 3464.0, 6000.0
+    mu = rho * vs * vs
+    lam = rho * vp * vp - 2 * mu
+    mats, thetas = [], []
+    for _ in range(n):
+        mu_u, lam_u, omega, theta = visco.fit_attenuation(rho, mu, lam, 100.0, 50.0, 0.5, 100.0)
+        mats.append([rho, mu_u, lam_u])
+        thetas.append(theta)
+    ops = visco.cell_operators(coords, np.array(mats), omega, np.array(thetas), nb)
+    ft = np.zeros((n, 4), np.int8)
+    vcells = {"star": np.concatenate([ops["star"], ops["ET"][:, None]], axis=1), "AplusT": ops["AplusT"],
+              "AminusT": ops["AminusT"], "neighbor": nb, "side": side, "orient": orient, "face_type": ft}
+    q0 = np.random.default_rng(1).uniform(-1, 1, (n, visco.NQ, dg_setup.nbasis3(order)))
+    dt = 1e-3
+    a = oracle_py.lts_cycles(visco.ViscoLts(order), q0, vcells, np.zeros(n, np.int64), dt, 2)
+    b = visco.Visco(order).steps(q0, ops, nb, side, orient, ft, dt, 2)
+    assert np.array_equal(a, b)
