@@ -1896,15 +1896,22 @@ int sei_autotune(sei_ctx* c, double dt, int steps, sei_tune_result* out) {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   const bool prof = c->profiling;
   c->profiling = false;
+  bool saved = false;
   auto done = [&](int code) {
+    if (code != SEI_OK && saved) {  // a variant failed: put the DOFs back before giving up
+      cudaMemcpyAsync(c->Q, save, bytes, cudaMemcpyDeviceToDevice, c->stream);
+      cudaStreamSynchronize(c->stream);
+    }
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     cudaFree(save);
     c->profiling = prof;
     return code;
   };
-  if (cudaMemcpyAsync(save, c->Q, bytes, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess ||
-      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+  if (cudaMemcpyAsync(save, c->Q, bytes, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess)
+    return done(fail(c, SEI_ERR_CUDA, "autotuner DOF copy"));
+  saved = true;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
     return done(fail(c, SEI_ERR_CUDA, "autotuner set-up"));
   double best = 1e300, worst = 0.0;
   Cand pick = cands[0];
