@@ -701,7 +701,7 @@ def run_ours(args, world, rank, local):
     comb = None
     if rank == 0 and args.combined_steps > 0:
         # order 6, 1,000,000 tets, 50,000-face fault: plain = FP32 + plain Newton, warm = mixed
-        # path + learned Newton start; global time stepping (LTS with a fault is not built)
+        # path + learned Newton start; global time stepping (the LTS form is the next measurement)
         comb = dr_measurement(local, args.combined_steps, order=6, dims=(8, 100, 250), plane=4, warm_precision=1,
                               perturb=PERTURB)
     comb_lts = None

@@ -153,9 +153,14 @@ int sei_get_time_integrated(sei_ctx* ctx, float* tint);
 int sei_get_derivatives(sei_ctx* ctx, float* derivs);
 int sei_derivatives_size(int order);
 
-/* Spacetime::computeBatchedAder (src/Kernels/LinearCK/Time.cpp:142-217) for all cells,
- * coeffs = MonomialBasis::integrate(0, dt) (src/Numerical/TimeBasis.h:82-93). */
-int sei_compute_ader(sei_ctx* ctx, double dt);
+/* Spacetime::computeAder / computeBatchedAder (src/Kernels/Spacetime.h:52-67,
+ * src/Kernels/LinearCK/Time.cpp:142-217) for all cells: I = sum_i coeffs[i] dQ_i, with coeffs[order]
+ * the time-basis coefficients of the integration interval, as the reference's caller passes them
+ * (a TimeCluster passes MonomialBasis::integrate(0, dt), or the sub-interval of a local time step);
+ * coeffs = NULL takes MonomialBasis::integrate(0, dt) (src/Numerical/TimeBasis.h:82-93).  The
+ * global matrices (the reference's setGlobalData, src/Kernels/Kernel.h:18) are compiled into the
+ * kernels, so no global-data call exists. */
+int sei_compute_ader(sei_ctx* ctx, const double* coeffs, double dt);
 /* Local::computeBatchedIntegral (src/Kernels/LinearCK/Local.cpp:255-395): volume + local flux from the
  * time-integrated DOFs of the last sei_compute_ader. */
 int sei_compute_local_integral(sei_ctx* ctx);
@@ -173,23 +178,30 @@ int sei_evaluate_taylor(sei_ctx* ctx, const double* coeffs, float* out_device);
  * sei_lts_run and replays it for every cycle (one graph launch per cycle); 0 (default) launches
  * the kernels of every cycle directly.  Per-launch profiling is not recorded inside the graph. */
 #define SEI_OPT_LTS_GRAPH 2
-/* SEI_OPT_TC_LOCAL (SEI_PREC_F16X3 only): 1 runs the local integral on the tensor cores as
- * well; 0 (default) runs it on the FP32 CUDA cores, which is faster at orders 4-6. */
+/* SEI_OPT_TC_LOCAL (SEI_PREC_F16X3 only): where the local integral (volume + local flux, which also
+ * stores the face traces) runs: 0 (default) FP32 CUDA cores; 1 tensor cores, transposed (the basis
+ * index on the TMEM lanes, a tile's (cell, quantity) pairs on the MMA columns, the per-cell 9 x 9
+ * mixing in registers); 2 tensor cores, rows form (a tile's rows (cell, quantity) on the lanes). */
 #define SEI_OPT_TC_LOCAL 3
-/* SEI_OPT_NB_CTAS (SEI_PREC_F16X3 only): persistent CTAs per SM of the tensor-core neighbour
- * kernel, 1..3 (default 3). */
+/* SEI_OPT_NB_CTAS (SEI_PREC_F16X3 only): persistent CTAs per SM of the rows-form tensor-core
+ * neighbour kernel, 1..3 (default 3). */
 #define SEI_OPT_NB_CTAS 4
+/* SEI_OPT_NB_FORM (SEI_PREC_F16X3 only): layout of the tensor-core neighbour flux.  1 (default),
+ * transposed: the basis index on the TMEM lanes and a tile's (quantity, cell) pairs on the MMA
+ * columns, so the per-cell 9 x 9 mixing stays in registers; 0, rows: a tile's (cell, quantity)
+ * rows on the lanes, the mixing through shared memory. */
+#define SEI_OPT_NB_FORM 5
 int sei_set_option(sei_ctx* ctx, int option, int value);
 
 /* Autotuner (no counterpart in the reference, whose kernel shapes are fixed when its code is
  * generated): times `steps` steps of kernel 'all' on the context's own mesh for every variant of
- * the step this library has: SEI_OPT_FUSED_LOCAL 0/1 at SEI_PREC_FP32; SEI_OPT_TC_LOCAL 0/1 x
- * SEI_OPT_NB_CTAS 1..3 at SEI_PREC_F16X3.  It keeps the fastest variant as the context's options.
+ * the step this library has: SEI_OPT_FUSED_LOCAL 0/1 at SEI_PREC_FP32; SEI_OPT_TC_LOCAL 0/1/2 x
+ * (SEI_OPT_NB_FORM 1, or SEI_OPT_NB_FORM 0 with SEI_OPT_NB_CTAS 1..3) at SEI_PREC_F16X3.  It keeps the fastest variant as the context's options.
  * The DOFs are restored after every variant, so the call leaves the state unchanged.  Global
  * stepping of the elastic kernels only (SEI_ERR_UNSUPPORTED after sei_visco_setup or
  * sei_lts_setup).  Synchronous. */
 typedef struct sei_tune_result {
-  int fused_local, tc_local, nb_ctas; /* chosen options */
+  int fused_local, tc_local, nb_ctas, nb_form; /* chosen options */
   int candidates;                     /* variants timed */
   double best_ms, worst_ms;           /* per step, fastest and slowest variant */
 } sei_tune_result;
@@ -213,7 +225,8 @@ int sei_last_run_ms(sei_ctx* ctx, double* ms);
  * freq_central with freq_ratio (unrelaxed moduli, relaxation frequencies, theta); Q and I
  * become [n][27][Bp] (elastic DOFs kept, memory variables zero); sei_run then runs the
  * viscoelastic ADER (with the source term), local and neighbour kernels for SEI_KERNEL_ALL,
- * LOCAL, ADER, LOCAL_WO_ADER and NEIGHBOR.  Orders 4 and 5, FP32, no fault, no LTS. */
+ * LOCAL, ADER, LOCAL_WO_ADER and NEIGHBOR, on global time steps or, after sei_lts_setup, with
+ * rate-2 local time stepping.  Orders 4 and 5, FP32, no fault. */
 int sei_visco_setup(sei_ctx* ctx, double qp, double qs, double freq_central, double freq_ratio);
 /* Quantities per cell of the DOF arrays (9, or 27 after sei_visco_setup). */
 int sei_num_quantities(const sei_ctx* ctx);
@@ -310,8 +323,13 @@ int sei_mlp_predict(const float* params, const float* norm, const float* samples
  * or take memory outside that pool, and cudaFree synchronises the whole device.  Its scratch is a
  * fixed static device array of 421 KiB that limits n to SEI_MLP_NOALLOC_MAX_SAMPLES (larger n
  * returns SEI_ERR_CAPACITY).  The first call on a device (the current one) looks up the array's
- * address: make it before any stream capture.  All calls on a device share the array; the
- * accumulators are cleared by every call, and calls that overlap on the GPU race. */
+ * address: make it before any stream capture.  Under lazy module loading (the CUDA default) that
+ * first call also loads the module, which allocates the array and may synchronise the device, so
+ * make it at start-up (or set CUDA_MODULE_LOADING=EAGER).  The work runs on the calling thread's
+ * per-thread default stream (cudaStreamPerThread) and the call waits for that stream only, so it
+ * does not wait for the caller's other streams (it does order with the legacy stream 0).  All
+ * calls on a device share the array; the accumulators are cleared by every call, and calls that
+ * overlap on the GPU race. */
 #define SEI_MLP_NOALLOC_MAX_SAMPLES 16384
 int sei_mlp_gradient_noalloc(const float* params, const float* norm, const float* samples, int64_t n, float* grads,
                              float* loss);
@@ -329,6 +347,15 @@ int sei_kernel_times_by_kind(sei_ctx* ctx, double* ms, int* counts);
  * 3 = split TF32.  N multiple of 16 in 16..256, K multiple of 8 in 8..64.  Checks the tensor-core
  * conventions of the library on the current device. */
 int sei_tc_gemm_check(const float* A, const float* B, float* D, int N, int K, int terms);
+
+/* Diagnostic: one M x N x K tile D = A B^T on tcgen05 kind::f16 (operands rounded to FP16, FP32
+ * accumulator) with A K-major and B K-major (bMN = 0) or MN-major (bMN = 1; lboIsK: the
+ * descriptor's leading offset carries the K stride), A K-major (aMN = 0) or MN-major (aMN = 1,
+ * the leading offset carrying the K stride).  A [M][K], B [N][K] row-major host arrays;
+ * D [128][ceil16(N)] receives all 128 TMEM lanes (zeroed before the MMA), so the lane placement of
+ * M = 64 results can be checked.  M 64 or 128; N multiple of 8 (M = 64) or 16 (M = 128) in 8..128;
+ * K multiple of 16 in 16..96. */
+int sei_tc_layout_check(const float* A, const float* B, float* D, int M, int N, int K, int bMN, int lboIsK, int aMN);
 
 /* Per-cell, per-step estimate of a proxy kernel (Local.cpp:462-522, Neighbor.cpp:190-228), elastic:
  * SEI_KERNEL_ALL, LOCAL, ADER, LOCAL_WO_ADER, NEIGHBOR (others SEI_ERR_UNSUPPORTED).  Works on a

@@ -93,6 +93,8 @@ def gen_order(order: int) -> str:
     a(f"namespace sei_o{order} {{")
     a(f"constexpr int kOrder = {order}, kB = {B}, kBp = {padded(B)}, kF = {F}, kFP = {padded(F)}, kQ = 9, kCPB = {CPB};")
     a(f"constexpr int kDerivSize = {sum(nb3(order - i) for i in range(order)) * NQ};")
+    a("// Cell stride (floats) of a DOF block staged in shared memory: 16 bytes of padding per cell.")
+    a("constexpr int kSt = 9 * kBp + 4;")
     fl = nnz_flops(order)
     a(f"// Non-zero flops per cell of the ADER, local-integral and neighbour kernels (literal FFMAs and premixes).")
     a(f"constexpr double kFlopAder = {fl['ader']:.1f}, kFlopLocal = {fl['local']:.1f}, kFlopNeighbor = {fl['neighbor']:.1f};")
@@ -122,10 +124,42 @@ def gen_order(order: int) -> str:
     }}
   const float* qcol = Q + ((size_t)cl * 9 + q) * kBp;"""
 
-    def emit_ck():
-        a("""  float z[kBp];
-  sei_load_col<kBp>(qcol, z);
-  float I[kBp];
+    def emit_ck(staged=False):
+        if staged:
+            # the block's DOFs arrive by one bulk copy per cell into X (cell stride kSt floats,
+            # 16 bytes of padding per cell spread the column reads over the banks); each thread
+            # then reads its column from there instead of 14 strided float4 loads from HBM
+            a("""  __shared__ uint64_t sei_mbar;
+  const int cell0 = blockIdx.x * kCPB;
+  const int cnt = n - cell0 < kCPB ? n - cell0 : kCPB;
+  if (threadIdx.x == 0) sei_tc::mbarInit(&sei_mbar, 1);
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    if (lane == 0) sei_tc::mbarExpectTx(&sei_mbar, (unsigned)(cnt * 9 * kBp * 4));
+    __syncwarp();
+    if (lane < cnt) sei_tc::bulkCopyG2S(X + lane * kSt, Q + (size_t)(cell0 + lane) * 9 * kBp, 9 * kBp * 4, &sei_mbar);
+  }
+  if (!sei_tc::mbarWait(&sei_mbar, 0, 1u << 26)) {
+    if (threadIdx.x == 0 && status) atomicExch(status, 1);
+    (void)sei_tc::mbarWait(&sei_mbar, 0, 1u << 26);  // the copies in flight land before X is reused
+  }
+  float z[kBp];
+  {
+    const float4* src = reinterpret_cast<const float4*>(X + lane * kSt + q * kBp);
+#pragma unroll
+    for (int k4 = 0; k4 < kBp / 4; ++k4) {
+      const float4 t = src[k4];
+      z[4 * k4] = t.x;
+      z[4 * k4 + 1] = t.y;
+      z[4 * k4 + 2] = t.z;
+      z[4 * k4 + 3] = t.w;
+    }
+  }
+  __syncthreads();""")
+        else:
+            a("""  float z[kBp];
+  sei_load_col<kBp>(qcol, z);""")
+        a("""  float I[kBp];
 #pragma unroll
   for (int k = 0; k < kBp; ++k) I[k] = coeffs.c[0] * z[k];
   const int dsl = derivs ? (dslot ? __ldg(dslot + cl) : cl) : -1;
@@ -226,12 +260,26 @@ sei_local_o{order}(int n, float* __restrict__ Q, float* __restrict__ Iout, const
     # ADER alone (Spacetime::computeAder)
     a(f"""
 // Cauchy-Kovalevskaya predictor alone: I = sum_i coeffs[i] dQ(i) (Q unchanged), optional derivatives.
-// Two CTAs per SM (at order 6: 96 registers, ~0.2 KB spilled to L1; measured 3.6 % faster step).
+// Two CTAs per SM.  The block's 32 cells of Q arrive in shared memory by bulk copies and I leaves
+// the same way (one 16-byte-aligned copy per cell each way), so HBM sees whole contiguous rows
+// instead of every thread's strided column loads; status is set when a copy wait gives up.
 extern "C" __global__ void __launch_bounds__(288, 2)
 sei_ader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout, const float* __restrict__ star_nz,
-                  SeiCoeffs coeffs, float* __restrict__ derivs, const int* __restrict__ dslot) {{""" + prologue)
-    emit_ck()
-    a("  if (valid) sei_store_col<kBp>(Iout + ((size_t)cell * 9 + q) * kBp, I);")
+                  SeiCoeffs coeffs, float* __restrict__ derivs, const int* __restrict__ dslot, int* __restrict__ status) {{""" + prologue)
+    emit_ck(staged=True)
+    a("""  // I of the block through X (its last reads ended with the stage barrier), then out by bulk copies
+  {
+    float4* dst = reinterpret_cast<float4*>(X + lane * kSt + q * kBp);
+#pragma unroll
+    for (int k4 = 0; k4 < kBp / 4; ++k4) dst[k4] = make_float4(I[4 * k4], I[4 * k4 + 1], I[4 * k4 + 2], I[4 * k4 + 3]);
+  }
+  sei_tc::fenceProxyAsync();
+  __syncthreads();
+  if (threadIdx.x < 32 && lane < cnt) {
+    sei_tc::bulkCopyS2G(Iout + (size_t)(cell0 + lane) * 9 * kBp, X + lane * kSt, 9 * kBp * 4);
+    sei_tc::bulkCommit();
+    sei_tc::bulkWaitRead();
+  }""")
     a("}")
 
     # local integral alone (Local::computeIntegral)
@@ -512,6 +560,25 @@ def tc_operands(order):
     for j in range(4):
         M[j * F:(j + 1) * F, :B] = G["rT"][j]
     ops["rt"] = M
+    # lift of the face-space flux back to the volume, as the A operand (M = 64 rows k) of the
+    # transposed neighbour kernel: K = (face i, face basis m) with every face padded to KF = F
+    # rounded up to 4 and then to 8 (whole core-matrix chunks per face)
+    KF = _pad(_pad(F, 4), 8)
+    M = np.zeros((64, 4 * KF))
+    for f in range(4):
+        M[:B, f * KF:f * KF + F] = G["rDivM"][f]
+    ops["nbt"] = M
+    # transposed local integral: volume stiffness blocks kDivM_d (rows 64 d + k, K = basis l, 64
+    # wide) and the face-trace stack rT (rows KF i + m, 128 rows, K = basis l, 64 wide; read
+    # K-major for the traces and MN-major, as rT^T, for the lift rDivM_i = diag(1/M) rT_i^T)
+    M = np.zeros((192, 64))
+    for e in range(3):
+        M[64 * e:64 * e + B, :B] = G["kDivM"][e]
+    ops["volt"] = M
+    M = np.zeros((128, 64))
+    for f in range(4):
+        M[f * KF:f * KF + F, :B] = G["rT"][f]
+    ops["rtt"] = M
     return ops
 
 
@@ -526,6 +593,22 @@ def gen_tc_tables(order: int) -> str:
         L.append(f"constexpr int k{name}_N = {N}, k{name}_K = {K};")
         L.append(f"__device__ __align__(16) const uint16_t k{name}_op[{both.size}] = {{" + ",".join(str(int(v)) for v in both) + "};")
         L.append(f"__device__ const float k{name}_scale[{N}] = {{" + ",".join(flit(np.ldexp(1.0, int(e))) for e in ex) + "};")
+    # constants of the transposed local integral: fM_m of every trace row (times the row's
+    # power-of-two scale) and 1/M_k of every basis function
+    B, F = nb3(order), nb2(order)
+    G = global_matrices(order)
+    KF = _pad(_pad(F, 4), 8)
+    _, _, ex = _f16_split_rows(ops["rtt"])
+    fm = np.asarray(G["fM"], dtype=float)
+    tsc = np.zeros(128)
+    for f in range(4):
+        for m in range(F):
+            tsc[f * KF + m] = np.ldexp(1.0, int(ex[f * KF + m])) * fm[m]
+    mass = np.asarray(G["M"], dtype=float)
+    invm = np.zeros(64)
+    invm[:B] = 1.0 / mass
+    L.append("__device__ const float krtt_tsc[128] = {" + ",".join(flit(v) for v in tsc) + "};")
+    L.append("__device__ const float kinvm[64] = {" + ",".join(flit(v) for v in invm) + "};")
     L.append(f"}}  // namespace sei_tc_o{order}")
     return "\n".join(L) + "\n"
 

@@ -79,10 +79,11 @@ struct sei_ctx {
   // integral and read by the neighbour kernel; valid while I has not changed since
   float* d_trace = nullptr;
   bool trace_valid = false;
-  bool tc_local = false;  // SEI_OPT_TC_LOCAL
+  int tc_local = 0;       // SEI_OPT_TC_LOCAL: 0 FP32 CUDA cores, 1 transposed tensor-core kernel, 2 rows form
   cudaStream_t copy_stream = nullptr;      // host <-> device copies of sei_run_host, beside the compute stream
   std::vector<cudaEvent_t> pipe_events;    // chunk events of the pipelined sei_run_host
-  int nb_ctas = 3;        // SEI_OPT_NB_CTAS: persistent CTAs per SM of the tensor-core neighbour kernel
+  int nb_ctas = 3;        // SEI_OPT_NB_CTAS: persistent CTAs per SM of the rows-form tensor-core neighbour kernel
+  int nb_form = 1;        // SEI_OPT_NB_FORM: 1 transposed tensor-core neighbour kernel, 0 rows form
   std::vector<cudaEvent_t> prof_events;
   std::vector<int> prof_kind;  // kind of the launch starting at event i: 0 ADER (or fused ADER + local),
                                // 1 neighbour, 2 fault, 3 local integral, 4 LTS gather / buffer, -1 end of run
@@ -240,7 +241,9 @@ int uploadCells(sei_ctx* c, int64_t n, const float* star, const float* aplus, co
 }
 
 sei::DeviceArrays arrays(sei_ctx* c) {
-  return sei::DeviceArrays{(int)c->n, c->Q, c->I, c->derivs, c->dslot, c->star_nz, c->aplus, c->aminus, c->nbr, c->rel, c->ftype};
+  sei::DeviceArrays d{(int)c->n, c->Q, c->I, c->derivs, c->dslot, c->star_nz, c->aplus, c->aminus, c->nbr, c->rel, c->ftype};
+  d.status = c->d_status;
+  return d;
 }
 
 void taylorCoeffs(int order, double dt, float* out) {
@@ -291,8 +294,9 @@ int launchLintOnly(sei_ctx* c, const sei::DeviceArrays& d) {
                      ? c->d_trace + (size_t)d.first * 9 * ((sei::numFaceBasis(c->cfg.order) + 3) / 4 * 4)
                      : nullptr;
   if (c->cfg.precision == SEI_PREC_F16X3 && c->tc_local) {
-    if (sei::launchLintTensorCore(c->cfg.order, d, trace, 0, c->d_status, c->sms, c->stream) != 0)
-      return fail(c, SEI_ERR_CUDA, "tensor-core local-integral kernel launch failed");
+    const int lrc = c->tc_local == 1 ? sei::launchLintTransposed(c->cfg.order, d, trace, 0, c->d_status, c->sms, c->stream)
+                                     : sei::launchLintTensorCore(c->cfg.order, d, trace, 0, c->d_status, c->sms, c->stream);
+    if (lrc != 0) return fail(c, SEI_ERR_CUDA, "tensor-core local-integral kernel launch failed");
   } else {
     sei::DeviceArrays dt = d;
     dt.trace = trace;
@@ -321,12 +325,14 @@ int launchNeighbor(sei_ctx* c, const sei::DeviceArrays& d) {
     // tensor-core path: the neighbour flux reads the stored face traces of I; they are
     // recomputed first when I changed after the last local integral
     if (!c->trace_valid) {
-      if (sei::launchLintTensorCore(c->cfg.order, d, c->d_trace, 1, c->d_status, c->sms, c->stream) != 0)
+      if (sei::launchLintTransposed(c->cfg.order, d, c->d_trace, 1, c->d_status, c->sms, c->stream) != 0)
         return fail(c, SEI_ERR_CUDA, "tensor-core trace kernel launch failed");
       c->trace_valid = true;
     }
-    if (sei::launchNeighborTensorCore(c->cfg.order, d, c->d_trace, c->d_status, c->sms, c->nb_ctas, c->stream) != 0)
-      return fail(c, SEI_ERR_CUDA, "tensor-core neighbour kernel launch failed");
+    const int lrc = c->nb_form ? sei::launchNeighborTransposed(c->cfg.order, d, c->d_trace, c->d_status, c->sms, c->stream)
+                               : sei::launchNeighborTensorCore(c->cfg.order, d, c->d_trace, c->d_status, c->sms,
+                                                               c->nb_ctas, c->stream);
+    if (lrc != 0) return fail(c, SEI_ERR_CUDA, "tensor-core neighbour kernel launch failed");
     return SEI_OK;
   }
   if (c->k.neighbor(d, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "neighbour kernel launch failed");
@@ -431,9 +437,11 @@ sei::ViscoArrays viscoArrays(sei_ctx* c) {
 }
 
 // Viscoelastic steps: ADER, volume + local flux, neighbour flux (kernel kinds 0, 3, 1).
-int runVisco(sei_ctx* c, int kernel, double dt, int steps) {
+int runVisco(sei_ctx* c, int kernel, double dt, int steps, const double* given = nullptr) {
   float coeffs[8];
   taylorCoeffs(c->cfg.order, dt, coeffs);
+  if (given)
+    for (int i = 0; i < c->cfg.order; ++i) coeffs[i] = (float)given[i];
   const sei::ViscoArrays v = viscoArrays(c);
   const bool ader = kernel == SEI_KERNEL_ALL || kernel == SEI_KERNEL_LOCAL || kernel == SEI_KERNEL_ADER;
   const bool lint = kernel == SEI_KERNEL_ALL || kernel == SEI_KERNEL_LOCAL || kernel == SEI_KERNEL_LOCAL_WO_ADER;
@@ -452,10 +460,13 @@ int runVisco(sei_ctx* c, int kernel, double dt, int steps) {
   return rc;
 }
 
-int runKernel(sei_ctx* c, int kernel, double dt, int steps) {
-  if (c->visco) return runVisco(c, kernel, dt, steps);
+// given: time-basis coefficients of the predictor's time integral (nullptr: MonomialBasis::integrate(0, dt))
+int runKernel(sei_ctx* c, int kernel, double dt, int steps, const double* given = nullptr) {
+  if (c->visco) return runVisco(c, kernel, dt, steps, given);
   float coeffs[8];
   taylorCoeffs(c->cfg.order, dt, coeffs);
+  if (given)
+    for (int i = 0; i < c->cfg.order; ++i) coeffs[i] = (float)given[i];
   sei::DeviceArrays d = arrays(c);
   c->prof_used = 0;
   int rc = SEI_OK;
@@ -711,10 +722,14 @@ int sei_compute_neighbors_integral(sei_ctx* c) {
   return runKernel(c, SEI_KERNEL_NEIGHBOR, 0.0, 1);
 }
 
-int sei_compute_ader(sei_ctx* c, double dt) {
+int sei_compute_ader(sei_ctx* c, const double* coeffs, double dt) {
   int rc = checkReady(c);
   if (rc) return rc;
-  return runKernel(c, SEI_KERNEL_ADER, dt, 1);
+  if (coeffs)
+    for (int i = 0; i < c->cfg.order; ++i)
+      if (!std::isfinite(coeffs[i])) return fail(c, SEI_ERR_ARG, "non-finite time-basis coefficient");
+  if (!coeffs && !(dt > 0)) return fail(c, SEI_ERR_ARG, "dt > 0 needed when no coefficients are given");
+  return runKernel(c, SEI_KERNEL_ADER, dt, 1, coeffs);
 }
 
 int sei_compute_local_integral(sei_ctx* c) {
@@ -733,12 +748,17 @@ int sei_set_option(sei_ctx* c, int option, int value) {
       c->lts_graph = value != 0;
       return SEI_OK;
     case SEI_OPT_TC_LOCAL:
-      c->tc_local = value != 0;
+      if (value < 0 || value > 2) return fail(c, SEI_ERR_ARG, "SEI_OPT_TC_LOCAL takes 0, 1 or 2");
+      c->tc_local = value;
       c->trace_valid = false;
       return SEI_OK;
     case SEI_OPT_NB_CTAS:
       if (value < 1 || value > 3) return fail(c, SEI_ERR_ARG, "SEI_OPT_NB_CTAS takes 1, 2 or 3");
       c->nb_ctas = value;
+      return SEI_OK;
+    case SEI_OPT_NB_FORM:
+      if (value != 0 && value != 1) return fail(c, SEI_ERR_ARG, "SEI_OPT_NB_FORM takes 0 or 1");
+      c->nb_form = value;
       return SEI_OK;
     default:
       return fail(c, SEI_ERR_ARG, "unknown option");
@@ -1880,14 +1900,18 @@ int sei_autotune(sei_ctx* c, double dt, int steps, sei_tune_result* out) {
   if (c->visco || c->lts) return fail(c, SEI_ERR_UNSUPPORTED, "the autotuner covers global stepping of the elastic kernels");
   if (!(dt > 0) || steps < 1 || steps > 1000) return fail(c, SEI_ERR_ARG, "dt > 0, 1 <= steps <= 1000");
   struct Cand {
-    int fused, tcLocal, nbCtas;
+    int fused, tcLocal, nbCtas, nbForm;
   };
   std::vector<Cand> cands;
   if (c->cfg.precision == SEI_PREC_FP32) {
-    cands = {{0, 0, 3}, {1, 0, 3}};
+    cands = {{0, 0, 3, 1}, {1, 0, 3, 1}};
   } else {
-    for (int t = 0; t < 2; ++t)
-      for (int k = 1; k <= 3; ++k) cands.push_back({0, t, k});
+    // local integral on the CUDA cores, transposed or rows-form tensor cores; neighbour
+    // transposed, or rows form with 1..3 CTAs per SM
+    for (int t = 0; t < 3; ++t) {
+      cands.push_back({0, t, 3, 1});
+      for (int k = 1; k <= 3; ++k) cands.push_back({0, t, k, 0});
+    }
   }
   // the DOFs are restored after every candidate: tuning leaves the state unchanged
   const size_t bytes = (size_t)c->n * 9 * c->Bp * sizeof(float);
@@ -1896,8 +1920,19 @@ int sei_autotune(sei_ctx* c, double dt, int steps, sei_tune_result* out) {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   const bool prof = c->profiling;
   c->profiling = false;
+  // the knobs the context had on entry: a failed tune gives them back instead of the failed variant
+  const bool fused0 = c->fused_local;
+  const int tc0 = c->tc_local;
+  const int nbCtas0 = c->nb_ctas, nbForm0 = c->nb_form;
   bool saved = false;
   auto done = [&](int code) {
+    if (code != SEI_OK) {
+      c->fused_local = fused0;
+      c->tc_local = tc0;
+      c->nb_ctas = nbCtas0;
+      c->nb_form = nbForm0;
+      c->trace_valid = false;  // the DOFs are put back below; traces of a variant are stale
+    }
     if (code != SEI_OK && saved) {  // a variant failed: put the DOFs back before giving up
       cudaMemcpyAsync(c->Q, save, bytes, cudaMemcpyDeviceToDevice, c->stream);
       cudaStreamSynchronize(c->stream);
@@ -1917,8 +1952,9 @@ int sei_autotune(sei_ctx* c, double dt, int steps, sei_tune_result* out) {
   Cand pick = cands[0];
   for (const Cand& k : cands) {
     c->fused_local = k.fused != 0;
-    c->tc_local = k.tcLocal != 0;
+    c->tc_local = k.tcLocal;
     c->nb_ctas = k.nbCtas;
+    c->nb_form = k.nbForm;
     c->trace_valid = false;
     if ((rc = runKernel(c, SEI_KERNEL_ALL, dt, 1))) return done(rc);  // warm-up
     if (cudaEventRecord(e0, c->stream) != cudaSuccess) return done(fail(c, SEI_ERR_CUDA, "event record"));
@@ -1937,14 +1973,16 @@ int sei_autotune(sei_ctx* c, double dt, int steps, sei_tune_result* out) {
       return done(fail(c, SEI_ERR_CUDA, "autotuner DOF restore"));
   }
   c->fused_local = pick.fused != 0;
-  c->tc_local = pick.tcLocal != 0;
+  c->tc_local = pick.tcLocal;
   c->nb_ctas = pick.nbCtas;
+  c->nb_form = pick.nbForm;
   c->trace_valid = false;
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return done(fail(c, SEI_ERR_CUDA, "autotuner sync"));
   if (out) {
     out->fused_local = pick.fused;
     out->tc_local = pick.tcLocal;
     out->nb_ctas = pick.nbCtas;
+    out->nb_form = pick.nbForm;
     out->candidates = (int)cands.size();
     out->best_ms = best;
     out->worst_ms = worst;

@@ -67,6 +67,7 @@ struct DeviceArrays {
   float* trace = nullptr;  // nullable: face traces fMrT_f I out of the local integral, [4][ntotal][9][FP]
   int ntotal = 0;          // cells of the whole mesh when this view covers a range of them (0: n)
   int first = 0;           // first cell of the range
+  int* status = nullptr;   // nullable: device status word (set when a bounded wait gives up)
 };
 
 using LaunchLocalFn = int (*)(const DeviceArrays&, const float* coeffs, void* stream);
@@ -224,6 +225,14 @@ struct TcNbArgs {
 // ctasPerSm: persistent CTAs per SM (1..3; 3 fit the shared memory at order 6)
 int launchNeighborTensorCore(int order, const DeviceArrays& d, const float* trace, int* status, int sms, int ctasPerSm,
                              void* stream);
+// Transposed tensor-core neighbour kernel (tc_nbt.cu): the same inputs and result as
+// launchNeighborTensorCore, with the basis index on the TMEM lanes and the per-cell mixing in
+// registers; two persistent CTAs per SM.
+int launchNeighborTransposed(int order, const DeviceArrays& d, const float* trace, int* status, int sms, void* stream);
+// Transposed tensor-core local integral (tc_lintt.cu): volume + local flux of launchLintTensorCore
+// with the basis index on the TMEM lanes; writes the face traces (traceOnly: only them).
+int launchLintTransposed(int order, const DeviceArrays& d, float* trace, int traceOnly, int* status, int sms,
+                         void* stream);
 // Floats per cell of the face-trace array of the tensor-core path: 4 faces x 9 quantities x FP.
 inline int traceFloatsPerCell(int order) { return 4 * 9 * ((numFaceBasis(order) + 3) / 4 * 4); }
 }  // namespace sei

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "internal.h"
+#include "tc.cuh"
 
 #define SEI_CAT2(a, b) a##b
 #define SEI_CAT(a, b) SEI_CAT2(a, b)
@@ -44,13 +45,15 @@ int launchNeighbor(const sei::DeviceArrays& d, void* stream) {
 
 int launchAder(const sei::DeviceArrays& d, const float* coeffs, void* stream) {
   if (d.n <= 0) return 0;
-  const size_t smem = sizeof(float) * 9 * K::kB * 32;
+  // the stage exchange buffer [9][kB][32], also the staging area of the block's DOFs [32][kSt]
+  const size_t xs = 9 * K::kB * 32, st = 32 * K::kSt;
+  const size_t smem = sizeof(float) * (xs > st ? xs : st);
   if (cudaFuncSetAttribute(K::SEI_CAT(sei_ader_o, SEI_ORDER), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return -1;
   const int blocks = (d.n + K::kCPB - 1) / K::kCPB;
   K::SEI_CAT(sei_ader_o, SEI_ORDER)<<<blocks, 288, smem, (cudaStream_t)stream>>>(
-      d.n, d.Q, d.I, d.star_nz, toCoeffs(coeffs), d.derivs, d.dslot);
+      d.n, d.Q, d.I, d.star_nz, toCoeffs(coeffs), d.derivs, d.dslot, d.status);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

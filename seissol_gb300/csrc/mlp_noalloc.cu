@@ -12,7 +12,15 @@
 //
 // Set-up: the first call on a device (the device current at the call) looks up the array's device
 // address with cudaGetSymbolAddress and keeps it for later calls on that device.  Make that first
-// call before any stream capture on the device.
+// call before any stream capture on the device.  With lazy module loading (the CUDA default) that
+// first look-up also loads this module, which is when the driver allocates the 421 KiB array, and a
+// module load may synchronise the device: make the first call at start-up, before the pool takes
+// the device and before streams are in flight (or load eagerly, CUDA_MODULE_LOADING=EAGER).
+//
+// Streams: the copies, the clears and the kernel run on the calling host thread's per-thread
+// default stream (cudaStreamPerThread), which does not wait for the caller's other streams, and
+// the call returns after that stream alone has finished.  It still orders with the legacy default
+// stream (stream 0) if the caller uses that one.
 //
 // Sharing: every call on a device uses the same array.  The gradient and loss accumulators are
 // cleared at the start of every call and the inputs overwritten, so consecutive calls are
@@ -83,18 +91,20 @@ extern "C" int sei_mlp_gradient_noalloc(const float* params, const float* norm, 
   float* T = s + kOffT;
   float* X = s + kOffX;
   const size_t rows = (size_t)n;
-  // samples [n][6] -> inputs [n][5] and targets [n] by strided copies (legacy default stream)
-  if (cudaMemcpy(P, params, sizeof(float) * kParams, cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(N, norm, sizeof(float) * sei_mlp::kNorm, cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy2D(X, 5 * sizeof(float), samples, 6 * sizeof(float), 5 * sizeof(float), rows,
-                   cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy2D(T, sizeof(float), samples + 5, 6 * sizeof(float), sizeof(float), rows, cudaMemcpyHostToDevice) !=
-          cudaSuccess ||
-      cudaMemsetAsync(G, 0, sizeof(float) * kParams, nullptr) != cudaSuccess ||
-      cudaMemsetAsync(L, 0, sizeof(float), nullptr) != cudaSuccess ||
-      sei::launchMlpGrad(P, N, X, T, (int)n, G, L, sms > 0 ? sms : 1, nullptr) != 0 ||
-      cudaMemcpy(grads, G, sizeof(float) * kParams, cudaMemcpyDeviceToHost) != cudaSuccess ||
-      cudaMemcpy(loss, L, sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
+  // samples [n][6] -> inputs [n][5] and targets [n] by strided copies, all on the per-thread stream
+  const cudaStream_t st = cudaStreamPerThread;
+  if (cudaMemcpyAsync(P, params, sizeof(float) * kParams, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(N, norm, sizeof(float) * sei_mlp::kNorm, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpy2DAsync(X, 5 * sizeof(float), samples, 6 * sizeof(float), 5 * sizeof(float), rows,
+                        cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpy2DAsync(T, sizeof(float), samples + 5, 6 * sizeof(float), sizeof(float), rows, cudaMemcpyHostToDevice,
+                        st) != cudaSuccess ||
+      cudaMemsetAsync(G, 0, sizeof(float) * kParams, st) != cudaSuccess ||
+      cudaMemsetAsync(L, 0, sizeof(float), st) != cudaSuccess ||
+      sei::launchMlpGrad(P, N, X, T, (int)n, G, L, sms > 0 ? sms : 1, (void*)st) != 0 ||
+      cudaMemcpyAsync(grads, G, sizeof(float) * kParams, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(loss, L, sizeof(float), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
     rc = SEI_ERR_CUDA;
   cudaGetLastError();
   return rc;

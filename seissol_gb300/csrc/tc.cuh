@@ -42,6 +42,12 @@ __host__ __device__ constexpr uint32_t idescF16(int M, int N) {
          | ((uint32_t)(M >> 4) << 24); // M / 16
 }
 
+// kind::f16 with the operand majors given: bMN = 1 reads B MN-major (N contiguous in 16-byte
+// rows of a core matrix) instead of K-major.
+__host__ __device__ constexpr uint32_t idescF16Major(int M, int N, int aMN, int bMN) {
+  return idescF16(M, N) | ((uint32_t)(aMN & 1) << 15) | ((uint32_t)(bMN & 1) << 16);
+}
+
 // Byte offset of 16-bit element (row, k) in a K-major no-swizzle tile with kc chunks of 8 along K.
 __host__ __device__ __forceinline__ uint32_t kmajorOffset16(int row, int k, int kc) {
   return (uint32_t)(((row >> 3) * kc + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2);
@@ -70,6 +76,15 @@ __device__ __forceinline__ void bulkCopyG2S(void* dst, const void* src, uint32_t
                "l"(src), "r"(bytes), "r"(smemAddr(mbar))
                : "memory");
 }
+
+// Bulk (non-tensor) TMA copy shared -> global in the calling thread's bulk group; then
+// bulkCommit() and bulkWaitRead() before the shared source is overwritten or the CTA exits.
+__device__ __forceinline__ void bulkCopyS2G(void* dst, const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;\n" ::"l"(dst), "r"(smemAddr(src)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulkCommit() { asm volatile("cp.async.bulk.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void bulkWaitRead() { asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory"); }
 
 // Bulk prefetch of [p, p + bytes) into L2 (p 16-byte aligned, bytes a multiple of 16).
 __device__ __forceinline__ void prefetchL2(const void* p, uint32_t bytes) {
@@ -141,6 +156,29 @@ __device__ __forceinline__ void tmemLoad16(uint32_t taddr, float (&v)[16]) {
 }
 
 __device__ __forceinline__ void tmemLoadWait() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+
+// 8 consecutive 32-bit TMEM columns of this thread's lane.
+__device__ __forceinline__ void tmemLoad8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr)
+               : "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Writes 16 consecutive 32-bit TMEM columns of this thread's lane.
+__device__ __forceinline__ void tmemStore16(uint32_t taddr, const float (&v)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};\n" ::"r"(taddr),
+      "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
+      "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
+      "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+      "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15]))
+      : "memory");
+}
+__device__ __forceinline__ void tmemStoreWait() { asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory"); }
 
 // Splits x into a TF32-exact high part (low 13 mantissa bits cleared) and the remainder.
 __device__ __forceinline__ void splitTf32(float x, float& hi, float& lo) {

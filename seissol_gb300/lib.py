@@ -63,7 +63,8 @@ class _Perf(C.Structure):
 
 
 class _Tune(C.Structure):
-    _fields_ = [("fused_local", C.c_int), ("tc_local", C.c_int), ("nb_ctas", C.c_int), ("candidates", C.c_int),
+    _fields_ = [("fused_local", C.c_int), ("tc_local", C.c_int), ("nb_ctas", C.c_int), ("nb_form", C.c_int),
+                ("candidates", C.c_int),
                 ("best_ms", C.c_double), ("worst_ms", C.c_double)]
 
 
@@ -102,7 +103,7 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_get_time_integrated", i, [VP, VP])
     _sig(lib, "sei_get_derivatives", i, [VP, VP])
     _sig(lib, "sei_derivatives_size", i, [i])
-    _sig(lib, "sei_compute_ader", i, [VP, d])
+    _sig(lib, "sei_compute_ader", i, [VP, VP, d])
     _sig(lib, "sei_compute_local_integral", i, [VP])
     _sig(lib, "sei_compute_ader_local", i, [VP, d])
     _sig(lib, "sei_compute_neighbors_integral", i, [VP])
@@ -116,6 +117,7 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_set_profiling", i, [VP, i])
     _sig(lib, "sei_set_option", i, [VP, i, i])
     _sig(lib, "sei_tc_gemm_check", i, [VP, VP, VP, i, i, i])
+    _sig(lib, "sei_tc_layout_check", i, [VP, VP, VP, i, i, i, i, i, i])
     _sig(lib, "sei_dr_setup", i, [VP, C.POINTER(RSParams), C.POINTER(i64)])
     _sig(lib, "sei_dr_num_points", i, [i])
     _sig(lib, "sei_dr_num_faces", i64, [VP])
@@ -181,6 +183,20 @@ def tc_gemm_check(A, B, terms=3):
     rc = lib.sei_tc_gemm_check(_ptr(A), _ptr(B), _ptr(D), B.shape[0], A.shape[1], terms)
     if rc != SEI_OK:
         raise SeiError(rc, "sei_tc_gemm_check")
+    return D
+
+
+def tc_layout_check(A, B, b_mn=0, lbo_is_k=0, a_mn=0):
+    """All 128 TMEM lanes after one M x N x K FP16 tile D = A B^T (A: M x K, B: N x K)."""
+    lib = load_library()
+    A = np.ascontiguousarray(A, np.float32)
+    B = np.ascontiguousarray(B, np.float32)
+    nc = (B.shape[0] + 15) // 16 * 16
+    D = np.empty((128, nc), np.float32)
+    rc = lib.sei_tc_layout_check(_ptr(A), _ptr(B), _ptr(D), A.shape[0], B.shape[0], A.shape[1], int(b_mn), int(lbo_is_k),
+                                 int(a_mn))
+    if rc != SEI_OK:
+        raise SeiError(rc, "sei_tc_layout_check")
     return D
 
 
@@ -333,8 +349,14 @@ class Context:
     def set_option(self, option, value):
         self._check(self.lib.sei_set_option(self.h, option, int(value)), "sei_set_option")
 
-    def compute_ader(self, dt):
-        self._check(self.lib.sei_compute_ader(self.h, dt), "sei_compute_ader")
+    def compute_ader(self, dt, coeffs=None):
+        """Spacetime::computeAder: I = sum_i coeffs[i] dQ_i (coeffs default: integrate(0, dt))."""
+        cp = None
+        if coeffs is not None:
+            cp = np.ascontiguousarray(coeffs, np.float64)
+            if cp.shape != (self.order,):
+                raise ValueError(f"coeffs must have {self.order} entries")
+        self._check(self.lib.sei_compute_ader(self.h, _ptr(cp), dt), "sei_compute_ader")
 
     def compute_local_integral(self):
         self._check(self.lib.sei_compute_local_integral(self.h), "sei_compute_local_integral")

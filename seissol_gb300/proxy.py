@@ -6,7 +6,7 @@ app/Proxy/Bindings.cpp:14-60.  Unlike the reference proxy, the data are a real m
 (synthetic periodic cube) with physical operators, and the time step is the CFL step.
 
 CLI:  python -m seissol_gb300.proxy <cells> <timesteps> <kernel>[,kernel...] [--order N] [--format json]
-      [--precision fp32|f16x3]; the *_dr kernels need --order 4 and run on a planar fault.
+      [--precision fp32|f16x3]; the *_dr kernels run on a planar fault at orders 4-6.
 """
 from __future__ import annotations
 
@@ -133,7 +133,7 @@ def main(argv=None):
     ap.add_argument("--order", type=int, default=6)
     ap.add_argument("--format", choices=("plain", "json"), default="plain")
     ap.add_argument("--precision", choices=("fp32", "f16x3"), default="fp32",
-                    help="f16x3: local integral on the tensor cores (split FP16)")
+                    help="f16x3: the tensor-core path (split FP16 x3 contractions, FP32 accumulation)")
     a = ap.parse_args(argv)
     kernels = tuple(a.kernel.split(","))
     out = run_proxy(ProxyConfig(cells=a.cells, timesteps=a.timesteps, kernels=kernels, order=a.order,

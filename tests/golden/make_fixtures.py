@@ -83,8 +83,11 @@ def parse_dr_json(path):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("SEI_REFERENCE_ROOT"),
+                    help="root of the reference source tree (default: $SEI_REFERENCE_ROOT)")
     a = ap.parse_args()
+    if not a.reference:
+        ap.error("name the reference tree with --reference or SEI_REFERENCE_ROOT")
     g = parse_values_h(os.path.join(a.reference, "tests/Model/Values.h"))
     json.dump(g, open(os.path.join(HERE, "godunov_elastic.json"), "w"), indent=1)
     pin = {}

@@ -166,3 +166,26 @@ def test_ader_and_local_integral_separately(built_lib, order):
     assert np.array_equal(ctx.get_dofs(), q_split)
     assert np.array_equal(ctx.get_time_integrated(), i_gpu)
     ctx.close()
+
+
+def test_ader_with_caller_coefficients(built_lib):
+    """sei_compute_ader(ctx, coeffs, dt) integrates over the interval the caller's coefficients name
+    (Spacetime::computeAder takes them from its TimeCluster): the sub-interval [dt/2, dt] of a local
+    time step matches the oracle with integrate(dt/2, dt), and coeffs = NULL gives integrate(0, dt)."""
+    order = 5
+    ctx, n, cells, q0 = _setup(order, store_derivatives=False)
+    dt = ctx.cfl_timestep(0.5)
+    o = oracle_py.Oracle(order)
+    ops = _ops64(cells)
+    sub = dg_setup.taylor_integrate(order, 0.5 * dt, dt)
+    ctx.compute_ader(dt, coeffs=sub)
+    ctx.sync()
+    i_ref = o.ader(q0.astype(np.float64), ops["star"], sub)
+    assert max(rel_l2_per_quantity(ctx.get_time_integrated(), i_ref)) < TOL_ONE
+    ctx.compute_ader(dt)
+    ctx.sync()
+    i_full = ctx.get_time_integrated()
+    ctx.compute_ader(dt, coeffs=dg_setup.taylor_integrate(order, 0.0, dt))
+    ctx.sync()
+    assert rel_l2(ctx.get_time_integrated(), i_full) < 1e-6  # the same coefficients up to FP32 rounding
+    ctx.close()

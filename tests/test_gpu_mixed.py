@@ -15,22 +15,27 @@ pytestmark = pytest.mark.gpu
 
 PREC_F16X3 = 1
 OPT_TC_LOCAL = 3
+OPT_NB_FORM = 5
 
 
-def _ctx(order, precision, dims=(4, 4, 4), seed=3, tc_local=False):
+def _ctx(order, precision, dims=(4, 4, 4), seed=3, tc_local=0):
+    """tc_local: 0 local integral on the CUDA cores, 1 transposed tensor-core kernel, 2 rows form."""
     from seissol_gb300 import Context
     ctx = Context(order, device=0, precision=precision)
     if tc_local:
-        ctx.set_option(OPT_TC_LOCAL, 1)
+        ctx.set_option(OPT_TC_LOCAL, int(tc_local))
     n = ctx.build_periodic_cube(*dims, perturb=0.1, seed=seed)
     q0 = seeded_dofs(n, order, seed)
     ctx.set_dofs(q0)
     return ctx, n, q0
 
 
-@pytest.mark.parametrize("order", [4, 5, 6])
-def test_local_integral_tensor_cores(built_lib, order):
-    ctx, n, q0 = _ctx(order, PREC_F16X3, tc_local=True)
+@pytest.mark.parametrize("order,form", [(4, 1), (5, 1), (6, 1), (4, 2), (6, 2)])
+def test_local_integral_tensor_cores(built_lib, order, form):
+    """The local integral on the tensor cores, transposed (1) and rows form (2), against the FP64
+    oracle applied to the same time-integrated DOFs (the face traces these kernels store are
+    checked through the neighbour flux that reads them, in the step tests)."""
+    ctx, n, q0 = _ctx(order, PREC_F16X3, tc_local=form)
     cells = ctx.get_cells()
     dt = ctx.cfl_timestep(0.5)
     ctx.compute_ader(dt)
@@ -47,11 +52,13 @@ def test_local_integral_tensor_cores(built_lib, order):
     ctx.close()
 
 
-@pytest.mark.parametrize("order", [4, 5, 6])
-def test_neighbor_tensor_cores(built_lib, order):
-    """The neighbour flux from the stored face traces; after ADER alone the traces are stale and
-    the neighbour call recomputes them from the new time-integrated DOFs first."""
+@pytest.mark.parametrize("order,form", [(4, 1), (5, 1), (6, 1), (4, 0), (6, 0)])
+def test_neighbor_tensor_cores(built_lib, order, form):
+    """The neighbour flux from the stored face traces, transposed (form 1) and rows (form 0)
+    kernels; after ADER alone the traces are stale and the neighbour call recomputes them from
+    the new time-integrated DOFs first."""
     ctx, n, q0 = _ctx(order, PREC_F16X3)
+    ctx.set_option(OPT_NB_FORM, form)
     cells = ctx.get_cells()
     dt = ctx.cfl_timestep(0.5)
     o = oracle_py.Oracle(order)
@@ -72,7 +79,7 @@ def test_neighbor_tensor_cores(built_lib, order):
     ctx.close()
 
 
-@pytest.mark.parametrize("order,tc_local", [(4, False), (6, False), (4, True), (6, True)])
+@pytest.mark.parametrize("order,tc_local", [(4, 0), (6, 0), (4, 1), (5, 1), (6, 1), (6, 2)])
 def test_ten_steps_mixed_precision(built_lib, order, tc_local):
     ctx, n, q0 = _ctx(order, PREC_F16X3, tc_local=tc_local)
     cells = ctx.get_cells()
@@ -102,7 +109,7 @@ def test_mixed_and_fp32_agree_on_larger_mesh(built_lib):
     b.close()
 
 
-@pytest.mark.parametrize("precision,ncand", [(0, 2), (PREC_F16X3, 6)])
+@pytest.mark.parametrize("precision,ncand", [(0, 2), (PREC_F16X3, 12)])
 def test_autotune_keeps_state_and_results(built_lib, precision, ncand):
     """sei_autotune times every variant of the step, restores the DOFs, keeps the fastest variant;
     five steps with the chosen options then agree with the FP32 path within 1e-5."""
@@ -112,7 +119,8 @@ def test_autotune_keeps_state_and_results(built_lib, precision, ncand):
     r = a.autotune(dt, 2)
     assert r["candidates"] == ncand
     assert 0 < r["best_ms"] <= r["worst_ms"]
-    assert r["nb_ctas"] in (1, 2, 3) and r["fused_local"] in (0, 1) and r["tc_local"] in (0, 1)
+    assert r["nb_ctas"] in (1, 2, 3) and r["fused_local"] in (0, 1) and r["tc_local"] in (0, 1, 2)
+    assert r["nb_form"] in (0, 1)
     assert np.array_equal(a.get_dofs(), q0)
     a.run("all", dt, 5)
     ref.run("all", dt, 5)
@@ -163,3 +171,41 @@ def test_run_host_pipelined_matches_device_run(built_lib, precision, nsteps):
     a.sync()
     assert np.array_equal(out, a.get_dofs())
     a.close()
+
+
+@pytest.mark.parametrize("order", [4, 6])
+def test_neighbor_forms_agree_with_partial_tile(built_lib, order):
+    """The transposed and rows forms of the tensor-core neighbour flux on a 317-cell mesh (the first
+    317 cells of a periodic cube, faces towards the dropped cells made outflow), so the last 8-cell
+    tile of the transposed kernel is partial: each within 2e-5 of the FP64 oracle, and within 2e-6
+    of each other."""
+    from seissol_gb300 import Context
+    base, _, _ = _ctx(order, 0, seed=21)
+    cells = base.get_cells()
+    base.close()
+    keep = 317
+    cut = {k: np.ascontiguousarray(v[:keep]) for k, v in cells.items()}
+    ft = np.array(cut["face_type"], dtype=np.int8)
+    nb = np.array(cut["neighbor"])
+    ft[nb >= keep] = 2
+    nb[nb >= keep] = 0
+    q0 = seeded_dofs(keep, order, 21)
+    outs = []
+    for form in (1, 0):
+        ctx = Context(order, device=0, precision=PREC_F16X3)
+        ctx.set_cells(cut["star"], cut["AplusT"], cut["AminusT"], nb, cut["side"], cut["orient"], ft)
+        ctx.set_option(OPT_NB_FORM, form)
+        ctx.set_dofs(q0)
+        ctx.compute_ader(1e-4)
+        ctx.sync()
+        i_gpu = ctx.get_time_integrated()
+        ctx.compute_neighbors_integral()
+        ctx.sync()
+        q_gpu = ctx.get_dofs()
+        q_ref = oracle_py.Oracle(order).neighbor(q0.astype(np.float64), i_gpu.astype(np.float64),
+                                                 cut["AminusT"].astype(np.float64), nb, cut["side"], cut["orient"], ft)
+        errs = rel_l2_per_quantity(q_gpu - q0, q_ref - q0)
+        assert max(errs) < 2e-5, (form, errs)
+        outs.append(q_gpu - q0)
+        ctx.close()
+    assert max(rel_l2_per_quantity(outs[0], outs[1])) < 2e-6
