@@ -554,7 +554,7 @@ def lts_fault_measurement(local, cycles):
                          "seconds_incl_recording": train_s}}
 
 
-PATHS = {"fp32": (0, False), "f16x3": (1, False), "f16x3_tc_local": (1, True)}
+PATHS = {"fp32": (0, 0), "f16x3": (1, 0), "f16x3_tc_local": (1, 1)}
 PATH_DESC = {"fp32": "FP32 CUDA cores (sparse, non-zero flops)",
              "f16x3": "mixed: neighbour flux on tcgen05 tensor cores (split FP16 x3) from stored face traces, "
                       "ADER and local integral FP32 CUDA cores",
@@ -562,13 +562,15 @@ PATH_DESC = {"fp32": "FP32 CUDA cores (sparse, non-zero flops)",
                                "ADER FP32 CUDA cores"}
 
 
-def kname(kind, path):
-    """Name of the CUDA kernel behind a launch kind of the step."""
-    if kind == "lint" and path == "f16x3_tc_local":
-        return f"sei_lint_tc<{ORDER}>"
+def kname(kind, path, tune=None):
+    """Name of the CUDA kernel behind a launch kind of the step (tune: the autotuner's choice)."""
+    tc_local = (tune or {}).get("tc_local", PATHS.get(path, (0, 0))[1])
+    nb_form = (tune or {}).get("nb_form", 1)
+    if kind == "lint" and path != "fp32" and tc_local:
+        return f"sei_lintt<{ORDER}>" if tc_local == 1 else f"sei_lint_tc<{ORDER}>"
     if kind == "neighbor" and path != "fp32":
-        return f"sei_nb_tc<{ORDER}>"
-    if kind == "lint" and path == "f16x3":
+        return f"sei_nbt<{ORDER}>" if nb_form == 1 else f"sei_nb_tc<{ORDER}>"
+    if kind == "lint" and path != "fp32":
         return f"sei_lint_trace_o{ORDER}"
     return f"sei_{kind}_o{ORDER}"
 
@@ -586,7 +588,7 @@ def measure_path(args, world, local, path, hbm, peak_kind, e2e_steps=0):
     if args.fused_local:
         ctx.set_option(1, 1)  # SEI_OPT_FUSED_LOCAL
     if tc_local:
-        ctx.set_option(3, 1)  # SEI_OPT_TC_LOCAL
+        ctx.set_option(3, int(tc_local))  # SEI_OPT_TC_LOCAL: 1 transposed tensor-core kernel
     n = ctx.build_periodic_cube(*DIMS, perturb=PERTURB, seed=SEED + rank)
     dt = ctx.cfl_timestep(0.5)
     tune = None
@@ -595,7 +597,7 @@ def measure_path(args, world, local, path, hbm, peak_kind, e2e_steps=0):
         # the variants of this path timed on this mesh; the fastest stays set (DOFs unchanged)
         tune = ctx.autotune(dt, 3)
         fused = bool(tune["fused_local"])
-        tc_local = bool(tune["tc_local"])
+        tc_local = int(tune["tc_local"])
         if path != "fp32":
             path = "f16x3_tc_local" if tc_local else "f16x3"
     ctx.run("all", dt, args.warmup)
@@ -631,9 +633,9 @@ def measure_path(args, world, local, path, hbm, peak_kind, e2e_steps=0):
     if os.path.exists(tf):
         for line in open(tf):
             parts = line.split()
-            if len(parts) >= 2 and parts[0] == kname(dom, path):
+            if len(parts) >= 2 and parts[0] == kname(dom, path, tune):
                 traffic = float(parts[1]) * n
-    roof = {"bound": "hbm", "kernel": kname(dom, path), "achieved": achieved, "peak": hbm, "unit": "GB/s",
+    roof = {"bound": "hbm", "kernel": kname(dom, path, tune), "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "peak_source": f"{peak_kind} hbm_gbs", "traffic": traffic,
             "algorithmic_bytes_per_launch": algo, "launch_ms": kernels[dom],
             "step_model_frac": value / world * bytes_per_cell(ORDER, "model") / (hbm * 1e9)}

@@ -80,6 +80,12 @@ typedef struct sei_cube_params {
    * log-uniformly in [h, grading h] (seeded); <= 1: uniform edge h.  The fault lies on the
    * cube-vertex plane fault_plane along x (x = fault_plane h when uniform). */
   double grading;
+  /* 1 (with grading >= 8): the local-time-stepping profile of the graded mesh instead: only the
+   * x edges vary, in four octave bands [h, 2h), [2h, 4h), [4h, 8h) and 8h (the y and z edges are
+   * grading h) on 60 / 25 / 10 / 5 % of the x intervals, the bands rising and falling once along
+   * x so that neighbouring cells lie in the same or adjacent bands; rate-2 clustering then gives
+   * four clusters of about those shares.  0: as described for grading. */
+  int lts_profile;
 } sei_cube_params;
 
 /* Fast-velocity-weakening rate-and-state friction (src/Initializer/Parameters/DRParameters.h:36-73,
@@ -341,6 +347,17 @@ int sei_kernel_times_ms(sei_ctx* ctx, double* local_ms, double* neighbor_ms, int
 /* The same per launch kind: ms[4] and counts[4] for 0 ADER (or fused ADER + local integral),
  * 1 neighbour flux, 2 fault kernel, 3 local integral. */
 int sei_kernel_times_by_kind(sei_ctx* ctx, double* ms, int* counts);
+
+/* Diagnostic of the kernels' failure path (no counterpart in the reference): enqueues on the
+ * context stream one warp that waits on an mbarrier with a limit of `polls` polls.  arrive = 0:
+ * nothing arrives and nothing asynchronous is in flight, so the wait gives up, sets the context's
+ * status word and returns, and the next sei_sync reports SEI_ERR_TIMEOUT (and clears the word);
+ * arrive = 1: the wait completes and sei_sync reports SEI_OK.  The context stays usable either way.
+ * 1 <= polls <= 2^20. */
+int sei_check_wait_timeout(sei_ctx* ctx, int polls, int arrive);
+/* Maximum SM clock of a device in kHz; the proxy derives its cycle count from it (the reference
+ * proxy counts host cycles, src/Proxy/Runner.cpp:87-129). */
+int sei_device_clock_khz(int device, int* khz);
 
 /* Diagnostic: one 128 x N x K tile D = A B^T on the tensor cores (tcgen05 kind::tf32, TMEM
  * accumulator), A [128][K] and B [N][K] row-major host arrays, D [128][N]; terms 1 = plain TF32,

@@ -900,6 +900,27 @@ int sei_sync(sei_ctx* c) {
   return SEI_OK;
 }
 
+int sei_device_clock_khz(int device, int* khz) {
+  if (!khz || device < 0) return SEI_ERR_ARG;
+  int v = 0;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrClockRate, device) != cudaSuccess) {
+    cudaGetLastError();
+    return SEI_ERR_CUDA;
+  }
+  *khz = v;
+  return SEI_OK;
+}
+
+int sei_check_wait_timeout(sei_ctx* c, int polls, int arrive) {
+  int rc = checkReady(c);
+  if (rc) return rc;
+  if (polls < 1 || polls > (1 << 20) || (arrive != 0 && arrive != 1))
+    return fail(c, SEI_ERR_ARG, "1 <= polls <= 2^20, arrive 0 or 1");
+  if (sei::launchWaitProbe((uint32_t)polls, arrive, c->d_status, c->stream) != 0)
+    return fail(c, SEI_ERR_CUDA, "wait probe launch failed");
+  return SEI_OK;
+}
+
 int sei_last_run_ms(sei_ctx* c, double* ms) {
   if (!c || !ms) return SEI_ERR_ARG;
   float f = 0;

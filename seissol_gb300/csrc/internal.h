@@ -233,6 +233,8 @@ int launchNeighborTransposed(int order, const DeviceArrays& d, const float* trac
 // with the basis index on the TMEM lanes; writes the face traces (traceOnly: only them).
 int launchLintTransposed(int order, const DeviceArrays& d, float* trace, int traceOnly, int* status, int sms,
                          void* stream);
+// Diagnostic: one warp's bounded mbarrier wait that gives up (arrive = 0) or completes (arrive = 1).
+int launchWaitProbe(uint32_t polls, int arrive, int* status, void* stream);
 // Floats per cell of the face-trace array of the tensor-core path: 4 faces x 9 quantities x FP.
 inline int traceFloatsPerCell(int order) { return 4 * 9 * ((numFaceBasis(order) + 3) / 4 * 4); }
 }  // namespace sei

@@ -191,6 +191,9 @@ void fluxSolver(double s, const Mat9& Ti, const Mat9& qgod, const Mat9& at, cons
 
 }  // namespace
 
+// Shares of the x (y, z) intervals in the octave bands of the local-time-stepping profile.
+constexpr double kLtsBandShare[4] = {0.47, 0.15, 0.05, 0.33};
+
 void buildPeriodicCube(const sei_cube_params& p, HostMesh& m) {
   // Even counts keep the alternating 5-tet split conforming across cubes; at least 4 cubes per
   // direction keep the periodically identified faces distinct.
@@ -207,6 +210,32 @@ void buildPeriodicCube(const sei_cube_params& p, HostMesh& m) {
     const int cnt[3] = {p.nx, p.ny, p.nz};
     for (int d = 0; d < 3; ++d) {
       pos[d].assign(cnt[d] + 1, 0.0);
+      if (p.lts_profile == 1 && p.grading >= 8.0) {
+        // every direction: octave bands b = 0..3 of the edge on fixed shares of the intervals,
+        // rising then falling once (band sequence 0 .. 3 .. 0, each band split between the two
+        // slopes), so neighbouring cubes lie in the same or adjacent bands; the shares are set
+        // so that the smallest edge of a cube, which bounds its time step, falls in band b for
+        // about 60 / 25 / 10 / 5 % of the cubes
+        const double share[4] = {kLtsBandShare[0], kLtsBandShare[1], kLtsBandShare[2], kLtsBandShare[3]};
+        int count[4], used = 0;
+        for (int b = 3; b >= 1; --b) {
+          count[b] = std::max(1, (int)std::lround(share[b] * cnt[d]));
+          used += count[b];
+        }
+        count[0] = std::max(1, cnt[d] - used);
+        std::vector<int> band;
+        for (int b = 0; b < 4; ++b)
+          for (int k = 0; k < (count[b] + 1) / 2; ++k) band.push_back(b);
+        for (int b = 3; b >= 0; --b)
+          for (int k = 0; k < count[b] / 2; ++k) band.push_back(b);
+        band.resize(cnt[d], 0);
+        for (int i = 0; i < cnt[d]; ++i) {
+          const int b = band[i];
+          const double w = p.h * std::ldexp(1.0, b);  // h, 2h, 4h, 8h
+          pos[d][i + 1] = pos[d][i] + w;
+        }
+        continue;
+      }
       for (int i = 0; i < cnt[d]; ++i) {
         const double w = p.grading > 1.0 ? p.h * std::exp(grng.uniform(0.0, std::log(p.grading))) : p.h;
         pos[d][i + 1] = pos[d][i] + w;

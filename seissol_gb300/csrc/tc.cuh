@@ -180,6 +180,15 @@ __device__ __forceinline__ void tmemStore16(uint32_t taddr, const float (&v)[16]
 }
 __device__ __forceinline__ void tmemStoreWait() { asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory"); }
 
+// Power-of-two scaling without ldexpf/frexpf: the binary exponent e of m > 0 in the frexp
+// convention (m = f 2^e, f in [0.5, 1)) from its bits, clamped to [-125, 126] (a zero or
+// subnormal m gives -125), and 2^e as a float built from the exponent field.
+__device__ __forceinline__ int pow2Exp(float m) {
+  const int e = (int)((__float_as_uint(m) >> 23) & 0xFF) - 126;
+  return e < -125 ? -125 : (e > 126 ? 126 : e);
+}
+__device__ __forceinline__ float pow2(int e) { return __uint_as_float((uint32_t)(e + 127) << 23); }
+
 // Splits x into a TF32-exact high part (low 13 mantissa bits cleared) and the remainder.
 __device__ __forceinline__ void splitTf32(float x, float& hi, float& lo) {
   hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);

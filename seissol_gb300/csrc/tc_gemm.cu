@@ -234,3 +234,29 @@ extern "C" int sei_tc_layout_check(const float* A, const float* B, float* D, int
   cudaFree(dS);
   return rc;
 }
+
+namespace {
+
+// One warp waits on an mbarrier of its own.  arrive = 0: nothing ever arrives on it and nothing
+// asynchronous is issued, so the bounded wait gives up after `polls` polls, sets *status and
+// returns; arrive = 1: thread 0 arrives first and the wait completes.  The kernels' give-up path,
+// exercised without a GPU fault.
+__global__ void sei_wait_probe_kernel(uint32_t polls, int arrive, int* __restrict__ status) {
+  __shared__ uint64_t mbar;
+  if (threadIdx.x == 0) sei_tc::mbarInit(&mbar, 1);
+  __syncwarp();
+  if (arrive && threadIdx.x == 0)
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(sei_tc::smemAddr(&mbar)) : "memory");
+  __syncwarp();
+  const bool ok = sei_tc::mbarWait(&mbar, 0, polls);
+  if (!ok && threadIdx.x == 0) atomicExch(status, 1);
+}
+
+}  // namespace
+
+namespace sei {
+int launchWaitProbe(uint32_t polls, int arrive, int* status, void* stream) {
+  sei_wait_probe_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(polls, arrive, status);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+}  // namespace sei

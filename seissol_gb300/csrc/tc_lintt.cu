@@ -115,19 +115,16 @@ __device__ __forceinline__ bool wgSyncAnd(int wg, bool v) {
   return r != 0;
 }
 
-__device__ __forceinline__ int expOf(float m) {
-  int e = 0;
-  if (m > 0.f) (void)frexpf(m, &e);
-  return e;
-}
+__device__ __forceinline__ int expOf(float m) { return sei_tc::pow2Exp(m); }
 
 // Splits 8 values (times 2^-e) into FP16 hi and lo and stores them as one 16-byte row chunk each.
 __device__ __forceinline__ void storeSplit8(uint16_t* hiBase, uint16_t* loBase, uint32_t offBytes, const float (&x)[8],
                                             int e) {
   uint32_t hw[4], lw[4];
+  const float sc = sei_tc::pow2(-e);
 #pragma unroll
   for (int u = 0; u < 4; ++u) {
-    const float x0 = ldexpf(x[2 * u], -e), x1 = ldexpf(x[2 * u + 1], -e);
+    const float x0 = x[2 * u] * sc, x1 = x[2 * u + 1] * sc;
     const __half2 h2 = __floats2half2_rn(x0, x1);
     const float2 b2 = __half22float2(h2);
     const __half2 l2 = __floats2half2_rn(x0 - b2.x, x1 - b2.y);
@@ -287,7 +284,7 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_lintt(LtArgs A) {
         if (pc < kNC) {
           const int n = 9 * pc + q;
           storeSplit8(bHi, biLo, (uint32_t)(((n >> 3) * 8 + po) * 128 + (n & 7) * 16), v, e);
-          if (po == 0) escI[n] = ldexpf(1.f, e);
+          if (po == 0) escI[n] = sei_tc::pow2(e);
         } else if (q < kN - kUsed) {
           const float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
           const int n = kUsed + q;  // unused columns 27..31
@@ -446,7 +443,7 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_lintt(LtArgs A) {
 #pragma unroll
               for (int u = 0; u < 8; ++u) x[u] = S[u][p];
               storeSplit8(bHi, bsLo, (uint32_t)(((n >> 3) * KTC + j) * 128 + (n & 7) * 16), x, e);
-              if (g == 0) escS[n] = ldexpf(1.f, e);
+              if (g == 0) escS[n] = sei_tc::pow2(e);
             }
           } else {
             const float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};

@@ -265,22 +265,15 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const u
       }
     }
     wgSync(wg);  // the maxima are complete and every read of the trace tile is done
-    if (wt < kCols) {
-      int e = 0;
-      const float m = __uint_as_float(smax[wt]);
-      if (m > 0.f) (void)frexpf(m, &e);
-      csc[wt] = ldexpf(1.f, e);
-    }
+    if (wt < kCols) csc[wt] = sei_tc::pow2(sei_tc::pow2Exp(__uint_as_float(smax[wt])));
     if (wt < D::ITEMS) {
 #pragma unroll
       for (int p = 0; p < 9; ++p) {
-        int e = 0;
-        const float m = __uint_as_float(smax[8 * p + c]);
-        if (m > 0.f) (void)frexpf(m, &e);
+        const float sc = sei_tc::pow2(-sei_tc::pow2Exp(__uint_as_float(smax[8 * p + c])));
         uint32_t hw[4], lw[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-          const float x0 = ldexpf(S[2 * u][p], -e), x1 = ldexpf(S[2 * u + 1][p], -e);
+          const float x0 = S[2 * u][p] * sc, x1 = S[2 * u + 1][p] * sc;
           const __half2 h2 = __floats2half2_rn(x0, x1);
           const float2 b2 = __half22float2(h2);
           const __half2 l2 = __floats2half2_rn(x0 - b2.x, x1 - b2.y);

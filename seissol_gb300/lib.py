@@ -35,7 +35,7 @@ class _Config(C.Structure):
 class _CubeParams(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("h", C.c_double), ("rho", C.c_double),
                 ("vp", C.c_double), ("vs", C.c_double), ("perturb", C.c_double), ("seed", C.c_uint64),
-                ("fault_plane", C.c_int), ("grading", C.c_double)]
+                ("fault_plane", C.c_int), ("grading", C.c_double), ("lts_profile", C.c_int)]
 
 
 class RSParams(C.Structure):
@@ -118,6 +118,8 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_set_option", i, [VP, i, i])
     _sig(lib, "sei_tc_gemm_check", i, [VP, VP, VP, i, i, i])
     _sig(lib, "sei_tc_layout_check", i, [VP, VP, VP, i, i, i, i, i, i])
+    _sig(lib, "sei_check_wait_timeout", i, [VP, i, i])
+    _sig(lib, "sei_device_clock_khz", i, [i, C.POINTER(C.c_int)])
     _sig(lib, "sei_dr_setup", i, [VP, C.POINTER(RSParams), C.POINTER(i64)])
     _sig(lib, "sei_dr_num_points", i, [i])
     _sig(lib, "sei_dr_num_faces", i64, [VP])
@@ -184,6 +186,16 @@ def tc_gemm_check(A, B, terms=3):
     if rc != SEI_OK:
         raise SeiError(rc, "sei_tc_gemm_check")
     return D
+
+
+def device_clock_khz(device=0):
+    """Maximum SM clock of a device in kHz (the proxy's cycle count is time x this clock)."""
+    lib = load_library()
+    k = C.c_int()
+    rc = lib.sei_device_clock_khz(int(device), C.byref(k))
+    if rc != SEI_OK:
+        raise SeiError(rc, "sei_device_clock_khz")
+    return k.value
 
 
 def tc_layout_check(A, B, b_mn=0, lbo_is_k=0, a_mn=0):
@@ -282,8 +294,8 @@ class Context:
 
     # -- set-up ------------------------------------------------------------------------
     def build_periodic_cube(self, nx, ny, nz, h=100.0, rho=2700.0, vp=6000.0, vs=3464.0, perturb=0.0, seed=1,
-                            fault_plane=-1, grading=1.0):
-        p = _CubeParams(nx, ny, nz, h, rho, vp, vs, perturb, seed, fault_plane, grading)
+                            fault_plane=-1, grading=1.0, lts_profile=0):
+        p = _CubeParams(nx, ny, nz, h, rho, vp, vs, perturb, seed, fault_plane, grading, int(lts_profile))
         n = C.c_int64()
         self._check(self.lib.sei_build_periodic_cube(self.h, C.byref(p), C.byref(n)), "sei_build_periodic_cube")
         self.n = n.value
@@ -524,6 +536,13 @@ class Context:
         cnt = np.zeros(4, np.int32)
         self._check(self.lib.sei_kernel_times_by_kind(self.h, _ptr(ms), _ptr(cnt)), "sei_kernel_times_by_kind")
         return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(("ader", "neighbor", "fault", "lint"))}
+
+    def metrics(self, kernel):
+        """Per-cell estimate of one step of a proxy kernel (sei_metrics): non-zero flops, hardware
+        flops and compulsory bytes."""
+        out = _Perf()
+        self._check(self.lib.sei_metrics(self.h, KERNELS[kernel], C.byref(out)), "sei_metrics")
+        return {"nonzero_flop": out.nonzero_flop, "hardware_flop": out.hardware_flop, "bytes": out.bytes}
 
     def last_run_ms(self):
         d = C.c_double()

@@ -37,15 +37,73 @@ class ProxyConfig:
 
 @dataclasses.dataclass
 class ProxyOutput:
+    """The fields of src/Proxy/Common.h:30-48.  The LIBXSMM and PSpaMM counts stay 0: no code of
+    those generators runs here.  cycles = time x the device's maximum SM clock (the reference
+    counts host cycles, src/Proxy/Runner.cpp:87-129); gib is the compulsory-traffic estimate of the
+    step, kernelGib the sum over the launched kernels' own compulsory bytes."""
     time: float = 0.0
     cycles: float = 0.0
+    libxsmmNumTotalGFlop: float = 0.0
+    pspammNumTotalGFlop: float = 0.0
+    libxsmmAndpspammNumTotalGFlop: float = 0.0
     actualNonZeroGFlop: float = 0.0
     actualHardwareGFlop: float = 0.0
     gib: float = 0.0
+    kernelGib: float = 0.0
+    nonZeroFlopPerCycle: float = 0.0
+    hardwareFlopPerCycle: float = 0.0
+    bytesPerCycle: float = 0.0
+    kernelBytesPerCycle: float = 0.0
     nonZeroGFlops: float = 0.0
     hardwareGFlops: float = 0.0
     gibPerSecond: float = 0.0
+    kernelGibPerSecond: float = 0.0
     cellUpdatesPerSecond: float = 0.0
+
+    # the snake_case names of the reference's Python module (app/Proxy/Bindings.cpp:33-51)
+    libxsmm_num_total_gflop = property(lambda self: self.libxsmmNumTotalGFlop)
+    pspamm_num_total_gflop = property(lambda self: self.pspammNumTotalGFlop)
+    libxsmm_and_pspamm_num_total_gflop = property(lambda self: self.libxsmmAndpspammNumTotalGFlop)
+    actual_non_zero_gflop = property(lambda self: self.actualNonZeroGFlop)
+    actual_hardware_gflop = property(lambda self: self.actualHardwareGFlop)
+    non_zero_flop_per_cycle = property(lambda self: self.nonZeroFlopPerCycle)
+    hardware_flop_per_cycle = property(lambda self: self.hardwareFlopPerCycle)
+    bytes_per_cycle = property(lambda self: self.bytesPerCycle)
+    non_zero_gflops = property(lambda self: self.nonZeroGFlops)
+    hardware_gflops = property(lambda self: self.hardwareGFlops)
+    gib_per_second = property(lambda self: self.gibPerSecond)
+
+
+class Aux:
+    """Kernel-name helpers and output of the proxy (src/Proxy/Common.h:50-62, Common.cpp)."""
+
+    @staticmethod
+    def str_to_kernel(kernel_str: str) -> list:
+        """'all,neigh' -> ['all', 'neigh']; an unknown name raises ValueError (the reference throws)."""
+        parts = [p.strip() for p in kernel_str.split(",")]
+        for p in parts:
+            if p not in KERNELS:
+                raise ValueError(f"Unknown kernel string: {p}")
+        return parts
+
+    @staticmethod
+    def kernel_to_string(kernels) -> str:
+        for k in kernels:
+            if k not in KERNELS:
+                raise ValueError("Unknown kernel type")
+        return ",".join(kernels)
+
+    @staticmethod
+    def get_allowed_kernels() -> list:
+        return list(KERNELS)
+
+    @staticmethod
+    def write_output(stream, out: "ProxyOutput", kernel_str: str, fmt: str = "plain"):
+        write_output(out, kernel_str, fmt, stream)
+
+    @staticmethod
+    def display_output(out: "ProxyOutput", kernel_str: str):
+        write_output(out, kernel_str, "plain", sys.stdout)
 
 
 def cube_dims(cells: int):
@@ -89,39 +147,75 @@ def run_proxy(cfg: ProxyConfig) -> ProxyOutput:
             ctx.sync()
             total_ms += ctx.last_run_ms()
         wall = time.perf_counter() - t0
-    try:
-        from .codegen.gen_kernels import nnz_flops
-        f = nnz_flops(cfg.order)
-        per = {"all": f["ader"] + f["local"] + f["neighbor"], "local": f["ader"] + f["local"], "neigh": f["neighbor"],
-               "ader": f["ader"], "localwoader": f["local"]}
-        flop = sum(per.get(k, 0.0) for k in cfg.kernels) * n * cfg.timesteps
-    except Exception:
-        flop = 0.0
+        perf = {}
+        for k in ("ader", "localwoader", "neigh", "all", "local"):
+            try:
+                perf[k] = ctx.metrics(k)
+            except Exception:
+                perf[k] = None
+    # per-cell flops and bytes of each proxy kernel: the estimate of the whole step and the
+    # kernels that one step of it launches (ADER, local integral, neighbour flux)
+    launched = {"all": ("ader", "localwoader", "neigh"), "local": ("ader", "localwoader"), "neigh": ("neigh",),
+                "ader": ("ader",), "localwoader": ("localwoader",)}
+    flop = kbytes = ebytes = 0.0
+    for k in cfg.kernels:
+        if perf.get(k):
+            flop += perf[k]["nonzero_flop"]
+            ebytes += perf[k]["bytes"]
+        for part in launched.get(k, ()):
+            if perf.get(part):
+                kbytes += perf[part]["bytes"]
+    if ebytes == 0.0:  # fault kernels: the step model of the elastic update
+        ebytes = bytes_per_cell(cfg.order) * len(cfg.kernels)
+    work = n * cfg.timesteps
     secs = total_ms / 1e3 if total_ms > 0 else wall
-    gib = bytes_per_cell(cfg.order) * n * cfg.timesteps * len(cfg.kernels) / 2 ** 30
-    out = ProxyOutput(time=secs, actualNonZeroGFlop=flop / 1e9, actualHardwareGFlop=flop / 1e9, gib=gib,
-                      nonZeroGFlops=flop / 1e9 / secs, hardwareGFlops=flop / 1e9 / secs, gibPerSecond=gib / secs,
-                      cellUpdatesPerSecond=n * cfg.timesteps / secs)
-    return out
+    try:
+        from .lib import device_clock_khz
+        cycles = secs * device_clock_khz(cfg.device) * 1e3
+    except Exception:
+        cycles = 0.0
+    gflop = flop * work / 1e9
+    gib, kgib = ebytes * work / 2 ** 30, kbytes * work / 2 ** 30
+    per_cycle = (lambda v: v / cycles) if cycles > 0 else (lambda v: 0.0)
+    return ProxyOutput(time=secs, cycles=cycles, actualNonZeroGFlop=gflop, actualHardwareGFlop=gflop, gib=gib,
+                       kernelGib=kgib, nonZeroFlopPerCycle=per_cycle(gflop * 1e9),
+                       hardwareFlopPerCycle=per_cycle(gflop * 1e9), bytesPerCycle=per_cycle(ebytes * work),
+                       kernelBytesPerCycle=per_cycle(kbytes * work), nonZeroGFlops=gflop / secs,
+                       hardwareGFlops=gflop / secs, gibPerSecond=gib / secs, kernelGibPerSecond=kgib / secs,
+                       cellUpdatesPerSecond=work / secs)
 
 
 def write_output(out: ProxyOutput, name: str, fmt: str = "plain", stream=sys.stdout):
+    """Plain or JSON summary with the fields and keys of src/Proxy/Common.cpp:87-154, plus the
+    cell-update rate of this project's metric."""
     if fmt == "json":
-        stream.write(json.dumps({"name": name, "time": out.time, "gflop-nz": out.actualNonZeroGFlop,
-                                 "gflop-hw": out.actualHardwareGFlop, "gib": out.gib, "gflops-nz": out.nonZeroGFlops,
-                                 "gflops-hw": out.hardwareGFlops, "gibs": out.gibPerSecond,
+        stream.write(json.dumps({"name": name, "time": out.time, "cycles": out.cycles,
+                                 "gflop-libxsmm": out.libxsmmNumTotalGFlop, "gflop-pspamm": out.pspammNumTotalGFlop,
+                                 "gflop-nz": out.actualNonZeroGFlop, "gflop-hw": out.actualHardwareGFlop,
+                                 "gib": out.gib, "gib-kernel": out.kernelGib,
+                                 "gflopcycle-nz": out.nonZeroFlopPerCycle, "gflopcycle-hw": out.hardwareFlopPerCycle,
+                                 "gibcycle": out.bytesPerCycle, "gibcycle-kernel": out.kernelBytesPerCycle,
+                                 "gflops-nz": out.nonZeroGFlops, "gflops-hw": out.hardwareGFlops,
+                                 "gibs": out.gibPerSecond, "gibs-kernel": out.kernelGibPerSecond,
                                  "cell-updates-per-s": out.cellUpdatesPerSecond}) + "\n")
         return
+    rows = (("seissol proxy mode", name), ("time for seissol proxy", out.time), ("cycles", out.cycles), None,
+            ("GFLOP (libxsmm)", out.libxsmmNumTotalGFlop), ("GFLOP (pspamm)", out.pspammNumTotalGFlop),
+            ("GFLOP (libxsmm + pspamm)", out.libxsmmAndpspammNumTotalGFlop),
+            ("GFLOP (non-zero) for seissol proxy", out.actualNonZeroGFlop),
+            ("GFLOP (hardware) for seissol proxy", out.actualHardwareGFlop),
+            ("GiB (estimate) for seissol proxy", out.gib), ("GiB (kernels) for seissol proxy", out.kernelGib), None,
+            ("FLOPS/cycle (non-zero)", out.nonZeroFlopPerCycle), ("FLOPS/cycle (hardware)", out.hardwareFlopPerCycle),
+            ("Bytes/cycle (estimate)", out.bytesPerCycle), ("Bytes/cycle (kernel)", out.kernelBytesPerCycle), None,
+            ("GFLOPS (non-zero) for seissol proxy", out.nonZeroGFlops),
+            ("GFLOPS (hardware) for seissol proxy", out.hardwareGFlops),
+            ("GiB/s (estimate) for seissol proxy", out.gibPerSecond),
+            ("GiB/s (kernel) for seissol proxy", out.kernelGibPerSecond), ("cell updates/s", out.cellUpdatesPerSecond))
     stream.write("=================================================\n")
     stream.write("===            PERFORMANCE SUMMARY            ===\n")
     stream.write("=================================================\n")
-    for label, val in (("seissol proxy mode", name), ("time for seissol proxy", out.time),
-                       ("GFLOP (non-zero) for seissol proxy", out.actualNonZeroGFlop),
-                       ("GiB (estimate) for seissol proxy", out.gib),
-                       ("GFLOPS (non-zero) for seissol proxy", out.nonZeroGFlops),
-                       ("GiB/s (estimate) for seissol proxy", out.gibPerSecond),
-                       ("cell updates/s", out.cellUpdatesPerSecond)):
-        stream.write(f"{label:<36}: {val}\n")
+    for row in rows:
+        stream.write("\n" if row is None else f"{row[0]:<36}: {row[1]}\n")
     stream.write("=================================================\n")
 
 
@@ -135,7 +229,7 @@ def main(argv=None):
     ap.add_argument("--precision", choices=("fp32", "f16x3"), default="fp32",
                     help="f16x3: the tensor-core path (split FP16 x3 contractions, FP32 accumulation)")
     a = ap.parse_args(argv)
-    kernels = tuple(a.kernel.split(","))
+    kernels = tuple(Aux.str_to_kernel(a.kernel))
     out = run_proxy(ProxyConfig(cells=a.cells, timesteps=a.timesteps, kernels=kernels, order=a.order,
                                 precision={"fp32": 0, "f16x3": 1}[a.precision]))
     write_output(out, a.kernel, a.format)

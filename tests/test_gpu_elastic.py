@@ -189,3 +189,51 @@ def test_ader_with_caller_coefficients(built_lib):
     ctx.sync()
     assert rel_l2(ctx.get_time_integrated(), i_full) < 1e-6  # the same coefficients up to FP32 rounding
     ctx.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_graded_mesh_global_steps(built_lib, precision):
+    """Five global steps of kernel 'all' (at the smallest CFL step) on a graded cube, whose cells
+    span a factor of about six in edge length, against the FP64 oracle, FP32 and mixed paths."""
+    from seissol_gb300 import Context
+    order = 5
+    ctx = Context(order, device=0, precision=precision)
+    n = ctx.build_periodic_cube(8, 8, 8, perturb=0.05, seed=11, grading=6.0)
+    cells = ctx.get_cells()
+    q0 = seeded_dofs(n, order, 11)
+    ctx.set_dofs(q0)
+    dt = ctx.cfl_timestep(0.5)
+    ctx.run("all", dt, 5)
+    ctx.sync()
+    ops = _ops64(cells)
+    ref = oracle_py.Oracle(order).steps(q0, ops["star"], ops["AplusT"], ops["AminusT"], cells["neighbor"], cells["side"],
+                                        cells["orient"], dt, 5, cells["face_type"])
+    errs = rel_l2_per_quantity(ctx.get_dofs(), ref)
+    assert max(errs) < 1e-5, errs
+    ctx.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_hundred_thousand_cells_one_step(built_lib, precision):
+    """One step of kernel 'all' at order 6 on a 100,000-tet cube (20 x 20 x 50 cubes), FP32 and
+    mixed paths, against the OpenMP FP64 oracle: 1e-5 relative L2 per quantity of the field."""
+    from seissol_gb300 import Context
+    order = 6
+    ctx = Context(order, device=0, precision=precision)
+    n = ctx.build_periodic_cube(20, 20, 50, perturb=0.1, seed=13)
+    assert n == 100000
+    cells = ctx.get_cells()
+    q0 = seeded_dofs(n, order, 13)
+    ctx.set_dofs(q0)
+    dt = ctx.cfl_timestep(0.5)
+    ctx.run("all", dt, 1)
+    ctx.sync()
+    got = ctx.get_dofs()
+    ctx.close()
+    ops = _ops64(cells)
+    ref = oracle_py.Oracle(order).steps(q0, ops["star"], ops["AplusT"], ops["AminusT"], cells["neighbor"], cells["side"],
+                                        cells["orient"], dt, 1, cells["face_type"])
+    errs = rel_l2_per_quantity(got, ref)
+    assert max(errs) < 1e-5, errs
+    upd = rel_l2_per_quantity(got - q0, ref - q0)
+    assert max(upd) < 2e-5, upd  # the update itself, the single-application bar

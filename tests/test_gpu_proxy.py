@@ -10,9 +10,11 @@ pytestmark = pytest.mark.gpu
 def test_proxy_kernels(built_lib, kernels, order, precision):
     from seissol_gb300.proxy import ProxyConfig, run_proxy
     out = run_proxy(ProxyConfig(cells=4000, timesteps=2, kernels=kernels, order=order, precision=precision))
-    assert out.time > 0 and out.cellUpdatesPerSecond > 0
+    assert out.time > 0 and out.cellUpdatesPerSecond > 0 and out.cycles > 0
     if "all" in kernels or "local" in kernels:
-        assert out.nonZeroGFlops > 0
+        assert out.nonZeroGFlops > 0 and out.nonZeroFlopPerCycle > 0
+        # the launched kernels move more than the step's compulsory estimate (I is written and re-read)
+        assert out.kernelGib > out.gib > 0
 
 
 def test_proxy_rejects_unknown_kernel(built_lib):
