@@ -195,7 +195,10 @@ int sei_evaluate_taylor(sei_ctx* ctx, const double* coeffs, float* out_device);
 /* SEI_OPT_NB_FORM (SEI_PREC_F16X3 only): layout of the tensor-core neighbour flux.  1 (default),
  * transposed: the basis index on the TMEM lanes and a tile's (quantity, cell) pairs on the MMA
  * columns, so the per-cell 9 x 9 mixing stays in registers; 0, rows: a tile's (cell, quantity)
- * rows on the lanes, the mixing through shared memory. */
+ * rows on the lanes, the mixing through shared memory; 2: transposed, and in a step of kernel
+ * 'all' (or 'all_dr') the local flux of every face joins the neighbour flux before their common
+ * lift rDivM_i (the local integral then computes the volume term and the face traces only;
+ * SEI_OPT_TC_LOCAL 0).  The separate local-integral and neighbour calls keep their full meaning. */
 #define SEI_OPT_NB_FORM 5
 int sei_set_option(sei_ctx* ctx, int option, int value);
 
@@ -373,6 +376,10 @@ int sei_tc_gemm_check(const float* A, const float* B, float* D, int N, int K, in
  * M = 64 results can be checked.  M 64 or 128; N multiple of 8 (M = 64) or 16 (M = 128) in 8..128;
  * K multiple of 16 in 16..96. */
 int sei_tc_layout_check(const float* A, const float* B, float* D, int M, int N, int K, int bMN, int lboIsK, int aMN);
+/* Diagnostic: the values each thread of one warp receives from a tcgen05.ld of shape 16x64b.x32
+ * (shape 0: lanes 0..15 of the warp's quarter) after every lane wrote 1000 * lane + column into
+ * columns 0..63; out [32 threads][32 registers]. */
+int sei_tc_ld_probe(int shape, float* out);
 
 /* Per-cell, per-step estimate of a proxy kernel (Local.cpp:462-522, Neighbor.cpp:190-228), elastic:
  * SEI_KERNEL_ALL, LOCAL, ADER, LOCAL_WO_ADER, NEIGHBOR (others SEI_ERR_UNSUPPORTED).  Works on a

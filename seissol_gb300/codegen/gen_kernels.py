@@ -95,6 +95,8 @@ def gen_order(order: int) -> str:
     a(f"constexpr int kDerivSize = {sum(nb3(order - i) for i in range(order)) * NQ};")
     a("// Cell stride (floats) of a DOF block staged in shared memory: 16 bytes of padding per cell.")
     a("constexpr int kSt = 9 * kBp + 4;")
+    a("// Cell stride (floats) of the staged face traces of the volume-and-traces kernel.")
+    a("constexpr int kTs = 9 * kFP + 4;")
     fl = nnz_flops(order)
     a(f"// Non-zero flops per cell of the ADER, local-integral and neighbour kernels (literal FFMAs and premixes).")
     a(f"constexpr double kFlopAder = {fl['ader']:.1f}, kFlopLocal = {fl['local']:.1f}, kFlopNeighbor = {fl['neighbor']:.1f};")
@@ -193,11 +195,18 @@ def gen_order(order: int) -> str:
             a("  }")
 
     def emit_volume_flux(with_trace=False):
+        emit_volume_part()
+        emit_flux_part(with_trace)
+
+    def emit_volume_part(acc_zero=False):
         a("  // ---- volume: Q += sum_e kDivM_e (I star_e)")
         a(f"#pragma unroll\n  for (int k = 0; k < kB; ++k) Xq[k * 32] = I[k];")
         a("  __syncthreads();")
         a("  float acc[kBp];")
-        a("  sei_load_col<kBp>(qcol, acc);")
+        if acc_zero:
+            a("#pragma unroll\n  for (int k = 0; k < kBp; ++k) acc[k] = 0.f;")
+        else:
+            a("  sei_load_col<kBp>(qcol, acc);")
         cols = [_cols(G["kDivM"][e]) for e in range(3)]
         for l in range(B):
             if not any(l in c for c in cols):
@@ -211,6 +220,8 @@ def gen_order(order: int) -> str:
                     a(f"    acc[{k}] = fmaf({flit(v)}, y{e}, acc[{k}]);")
             a("  }")
         a("  __syncthreads();")
+
+    def emit_flux_part(with_trace):
         for f in range(4):
             a(f"  // ---- local flux, face {f}: Q += rDivM_{f} ((fMrT_{f} I) AplusT_{f})")
             a("  {")
@@ -237,6 +248,21 @@ def gen_order(order: int) -> str:
                 a("    }")
             a("    __syncthreads();")
             a("  }")
+
+    def emit_volume_traces():
+        """Volume integral into acc (from zero), then the four face traces staged for one coalesced store."""
+        emit_volume_part(acc_zero=True)
+        a("  // ---- face traces fMrT_f I of all four faces, staged [f][lane][q][kFP] (row stride kTs)")
+        for f in range(4):
+            a("  {")
+            a("    float T[kF];")
+            _matvec(L, "    ", G["fMrT"][f], "I", "T", F, B, True)
+            a(f"    float4* st = reinterpret_cast<float4*>(sm + ({f} * 32 + lane) * kTs + q * kFP);")
+            a(f"#pragma unroll\n    for (int m4 = 0; m4 < kFP / 4; ++m4)")
+            a("      st[m4] = make_float4(4 * m4 < kF ? T[4 * m4 < kF ? 4 * m4 : 0] : 0.f, 4 * m4 + 1 < kF ? T[4 * m4 + 1 < kF ? 4 * m4 + 1 : 0] : 0.f,")
+            a("                           4 * m4 + 2 < kF ? T[4 * m4 + 2 < kF ? 4 * m4 + 2 : 0] : 0.f, 4 * m4 + 3 < kF ? T[4 * m4 + 3 < kF ? 4 * m4 + 3 : 0] : 0.f);")
+            a("  }")
+        a("  __syncthreads();")
 
     # fused ADER + local integral
     a(f"""
@@ -305,6 +331,88 @@ sei_lint_trace_o{order}(int n, float* __restrict__ Q, const float* __restrict__ 
     a("  sei_load_col<kBp>(Iin + ((size_t)cl * 9 + q) * kBp, I);")
     emit_volume_flux(with_trace=True)
     a("  if (valid) sei_store_col<kBp>(Q + ((size_t)cell * 9 + q) * kBp, acc);")
+    a("}")
+    a(f"""
+// Volume integral alone (no local flux) plus the face traces fMrT_f I of every cell and face,
+// trace[4][tplane][9][kFP]: the local integral of the path whose tensor-core neighbour kernel also
+// applies the local flux (from these traces).  The block's I and Q arrive by bulk copies (one per
+// cell, cell stride kSt floats in shared memory), Q while the volume and the traces are computed;
+// the traces of all four faces are staged ([face][cell][q][kFP], cell stride kTs) and leave in one
+// coalesced store per face; Q + volume leaves by bulk copies.  status is set when a copy wait
+// gives up.  Shared memory: the larger of the exchange, I and trace areas, then the Q area.
+extern "C" __global__ void __launch_bounds__(288, 1)
+sei_lintv_o{order}(int n, float* __restrict__ Q, const float* __restrict__ Iin, const float* __restrict__ star_nz,
+                   float* __restrict__ trace, int tplane, int* __restrict__ status) {{""" + prologue)
+    a("""  __shared__ uint64_t sei_mbar[2];
+  constexpr int kAreaA = (9 * kB * 32 > 32 * kSt ? (9 * kB * 32 > 4 * 32 * kTs ? 9 * kB * 32 : 4 * 32 * kTs)
+                                                 : (32 * kSt > 4 * 32 * kTs ? 32 * kSt : 4 * 32 * kTs));
+  float* QS = sm + kAreaA;  // the block's Q rows [32][kSt]
+  const int cell0 = blockIdx.x * kCPB;
+  const int cnt = n - cell0 < kCPB ? n - cell0 : kCPB;
+  if (threadIdx.x == 0) {
+    sei_tc::mbarInit(&sei_mbar[0], 1);
+    sei_tc::mbarInit(&sei_mbar[1], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    if (lane == 0) {
+      sei_tc::mbarExpectTx(&sei_mbar[0], (unsigned)(cnt * 9 * kBp * 4));
+      sei_tc::mbarExpectTx(&sei_mbar[1], (unsigned)(cnt * 9 * kBp * 4));
+    }
+    __syncwarp();
+    if (lane < cnt) {
+      sei_tc::bulkCopyG2S(X + lane * kSt, Iin + (size_t)(cell0 + lane) * 9 * kBp, 9 * kBp * 4, &sei_mbar[0]);
+      sei_tc::bulkCopyG2S(QS + lane * kSt, Q + (size_t)(cell0 + lane) * 9 * kBp, 9 * kBp * 4, &sei_mbar[1]);
+    }
+  }
+  bool ok = sei_tc::mbarWait(&sei_mbar[0], 0, 1u << 26);
+  float I[kBp];
+  {
+    const float4* src = reinterpret_cast<const float4*>(X + lane * kSt + q * kBp);
+#pragma unroll
+    for (int k4 = 0; k4 < kBp / 4; ++k4) {
+      const float4 t = src[k4];
+      I[4 * k4] = t.x;
+      I[4 * k4 + 1] = t.y;
+      I[4 * k4 + 2] = t.z;
+      I[4 * k4 + 3] = t.w;
+    }
+  }
+  __syncthreads();""")
+    emit_volume_traces()
+    a("""  {
+    constexpr int R4 = 9 * kFP / 4;  // float4 per cell and face
+#pragma unroll 1
+    for (int f = 0; f < 4; ++f) {
+      float4* dst = reinterpret_cast<float4*>(trace + ((size_t)f * tplane + cell0) * 9 * kFP);
+#pragma unroll 1
+      for (int idx = threadIdx.x; idx < kCPB * R4; idx += blockDim.x) {
+        const int Lc = idx / R4, rem = idx - Lc * R4;
+        if (cell0 + Lc < n) dst[idx] = *reinterpret_cast<const float4*>(sm + (f * 32 + Lc) * kTs + 4 * rem);
+      }
+    }
+  }
+  ok = sei_tc::mbarWait(&sei_mbar[1], 0, 1u << 26) && ok;
+  if (!ok) {
+    if (threadIdx.x == 0 && status) atomicExch(status, 1);
+    (void)sei_tc::mbarWait(&sei_mbar[0], 0, 1u << 26);  // copies in flight land before the block exits
+    (void)sei_tc::mbarWait(&sei_mbar[1], 0, 1u << 26);
+  }
+  {
+    float4* qs = reinterpret_cast<float4*>(QS + lane * kSt + q * kBp);
+#pragma unroll
+    for (int k4 = 0; k4 < kBp / 4; ++k4) {
+      const float4 t = qs[k4];
+      qs[k4] = make_float4(t.x + acc[4 * k4], t.y + acc[4 * k4 + 1], t.z + acc[4 * k4 + 2], t.w + acc[4 * k4 + 3]);
+    }
+  }
+  sei_tc::fenceProxyAsync();
+  __syncthreads();
+  if (threadIdx.x < 32 && lane < cnt) {
+    sei_tc::bulkCopyS2G(Q + (size_t)(cell0 + lane) * 9 * kBp, QS + lane * kSt, 9 * kBp * 4);
+    sei_tc::bulkCommit();
+    sei_tc::bulkWaitRead();
+  }""")
     a("}")
 
     # ---------------- neighbour kernel ----------------

@@ -285,7 +285,13 @@ int launchAderOnly(sei_ctx* c, const sei::DeviceArrays& d, const float* coeffs) 
   return SEI_OK;
 }
 
-int launchLintOnly(sei_ctx* c, const sei::DeviceArrays& d) {
+// True when a step of kernel 'all' runs the local flux inside the tensor-core neighbour kernel
+// (SEI_OPT_NB_FORM 2): the local integral then computes the volume term and the traces only.
+bool fusedFlux(const sei_ctx* c) {
+  return c->cfg.precision == SEI_PREC_F16X3 && c->nb_form == 2 && c->tc_local == 0 && !c->lts && c->d_trace;
+}
+
+int launchLintOnly(sei_ctx* c, const sei::DeviceArrays& d, bool volumeOnly = false) {
   int rc = profMark(c, 3);
   if (rc) return rc;
   // the traces cover every cell only outside local time stepping (whose kernels run per cluster);
@@ -300,17 +306,19 @@ int launchLintOnly(sei_ctx* c, const sei::DeviceArrays& d) {
   } else {
     sei::DeviceArrays dt = d;
     dt.trace = trace;
-    if (c->k.lint(dt, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "local-integral kernel launch failed");
+    const bool vol = volumeOnly && trace != nullptr;
+    if ((vol ? c->k.lintVol(dt, c->stream) : c->k.lint(dt, c->stream)) != 0)
+      return fail(c, SEI_ERR_CUDA, "local-integral kernel launch failed");
   }
   c->trace_valid = trace != nullptr && d.n == c->n;
   return SEI_OK;
 }
 
 // ADER followed by the local integral: two launches (default) or one fused launch.
-int launchLocal(sei_ctx* c, const sei::DeviceArrays& d, const float* coeffs) {
+int launchLocal(sei_ctx* c, const sei::DeviceArrays& d, const float* coeffs, bool volumeOnly = false) {
   if (!c->fused_local || c->cfg.precision != SEI_PREC_FP32) {
     int rc = launchAderOnly(c, d, coeffs);
-    return rc ? rc : launchLintOnly(c, d);
+    return rc ? rc : launchLintOnly(c, d, volumeOnly);
   }
   int rc = profMark(c, 0);
   if (rc) return rc;
@@ -318,7 +326,7 @@ int launchLocal(sei_ctx* c, const sei::DeviceArrays& d, const float* coeffs) {
   return SEI_OK;
 }
 
-int launchNeighbor(sei_ctx* c, const sei::DeviceArrays& d) {
+int launchNeighbor(sei_ctx* c, const sei::DeviceArrays& d, bool withLocal = false) {
   int rc = profMark(c, 1);
   if (rc) return rc;
   if (c->cfg.precision == SEI_PREC_F16X3 && !c->lts && c->d_trace) {
@@ -329,7 +337,8 @@ int launchNeighbor(sei_ctx* c, const sei::DeviceArrays& d) {
         return fail(c, SEI_ERR_CUDA, "tensor-core trace kernel launch failed");
       c->trace_valid = true;
     }
-    const int lrc = c->nb_form ? sei::launchNeighborTransposed(c->cfg.order, d, c->d_trace, c->d_status, c->sms, c->stream)
+    const int lrc = c->nb_form ? sei::launchNeighborTransposed(c->cfg.order, d, c->d_trace, c->d_status, c->sms,
+                                                               c->stream, withLocal && c->nb_form == 2)
                                : sei::launchNeighborTensorCore(c->cfg.order, d, c->d_trace, c->d_status, c->sms,
                                                                c->nb_ctas, c->stream);
     if (lrc != 0) return fail(c, SEI_ERR_CUDA, "tensor-core neighbour kernel launch failed");
@@ -473,8 +482,8 @@ int runKernel(sei_ctx* c, int kernel, double dt, int steps, const double* given 
   for (int s = 0; s < steps && rc == SEI_OK; ++s) {
     switch (kernel) {
       case SEI_KERNEL_ALL:
-        rc = launchLocal(c, d, coeffs);
-        if (!rc) rc = launchNeighbor(c, d);
+        rc = launchLocal(c, d, coeffs, fusedFlux(c));
+        if (!rc) rc = launchNeighbor(c, d, fusedFlux(c));
         break;
       case SEI_KERNEL_LOCAL:
         rc = launchLocal(c, d, coeffs);
@@ -493,9 +502,9 @@ int runKernel(sei_ctx* c, int kernel, double dt, int steps, const double* given 
         rc = launchDr(c, dt);
         break;
       case SEI_KERNEL_ALL_DR:
-        rc = launchLocal(c, d, coeffs);
+        rc = launchLocal(c, d, coeffs, fusedFlux(c));
         if (!rc) rc = launchDr(c, dt);
-        if (!rc) rc = launchNeighbor(c, d);
+        if (!rc) rc = launchNeighbor(c, d, fusedFlux(c));
         break;
       default:
         return fail(c, SEI_ERR_UNSUPPORTED, "kernel not supported by this build");
@@ -757,7 +766,7 @@ int sei_set_option(sei_ctx* c, int option, int value) {
       c->nb_ctas = value;
       return SEI_OK;
     case SEI_OPT_NB_FORM:
-      if (value != 0 && value != 1) return fail(c, SEI_ERR_ARG, "SEI_OPT_NB_FORM takes 0 or 1");
+      if (value < 0 || value > 2) return fail(c, SEI_ERR_ARG, "SEI_OPT_NB_FORM takes 0, 1 or 2");
       c->nb_form = value;
       return SEI_OK;
     default:
@@ -842,18 +851,18 @@ static int runHostPipelined(sei_ctx* c, double dt, int nsteps, const float* in, 
     SEI_CUDA(cudaStreamWaitEvent(c->stream, ev[k], 0));
     const sei::DeviceArrays d = gtsRange(c, b[k], b[k + 1], false);
     rc = launchAderOnly(c, d, co);
-    if (!rc) rc = launchLintOnly(c, d);
+    if (!rc) rc = launchLintOnly(c, d, fusedFlux(c));
   }
   if (rc) return rc;
   c->trace_valid = c->cfg.precision == SEI_PREC_F16X3 && c->d_trace;
   if (nsteps > 1) {
     const sei::DeviceArrays all = arrays(c);
-    if ((rc = launchNeighbor(c, all))) return rc;
+    if ((rc = launchNeighbor(c, all, fusedFlux(c)))) return rc;
     if (nsteps > 2 && (rc = runKernel(c, SEI_KERNEL_ALL, dt, nsteps - 2))) return rc;
-    if ((rc = launchAderOnly(c, all, co)) || (rc = launchLintOnly(c, all))) return rc;
+    if ((rc = launchAderOnly(c, all, co)) || (rc = launchLintOnly(c, all, fusedFlux(c)))) return rc;
   }
   for (int k = 0; k < nch && !rc; ++k) {
-    rc = launchNeighbor(c, gtsRange(c, b[k], b[k + 1], true));
+    rc = launchNeighbor(c, gtsRange(c, b[k], b[k + 1], true), fusedFlux(c));
     if (rc) return rc;
     SEI_CUDA(cudaEventRecord(ev[kChunks + k], c->stream));
     SEI_CUDA(cudaStreamWaitEvent(c->copy_stream, ev[kChunks + k], 0));
@@ -1933,6 +1942,7 @@ int sei_autotune(sei_ctx* c, double dt, int steps, sei_tune_result* out) {
       cands.push_back({0, t, 3, 1});
       for (int k = 1; k <= 3; ++k) cands.push_back({0, t, k, 0});
     }
+    cands.push_back({0, 0, 3, 2});  // local flux inside the transposed neighbour kernel
   }
   // the DOFs are restored after every candidate: tuning leaves the state unchanged
   const size_t bytes = (size_t)c->n * 9 * c->Bp * sizeof(float);

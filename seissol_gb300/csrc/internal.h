@@ -87,6 +87,7 @@ struct OrderKernels {
   LaunchLintFn lint;          // volume + local flux from I
   LaunchTaylorGatherFn taylorGather;
   double flopAder, flopLocal, flopNeighbor;  // non-zero flops per cell
+  LaunchLintFn lintVol;       // volume + face traces, no local flux (the neighbour kernel applies it)
 };
 
 // pool[dst[e]] = (reset ? 0 : pool[dst[e]]) + pool[cell[e]] for e < m, blocks of blk floats
@@ -212,6 +213,8 @@ int launchLintTensorCore(int order, const DeviceArrays& d, float* trace, int tra
 struct TcNbArgs {
   int n;       // cells of this launch (Q, aminus, nbr, rel, ftype point at its first cell)
   int ntotal;  // cells of the mesh: face-plane stride of the traces, range of neighbour indices
+  int first = 0;                  // mesh index of this launch's first cell (its own traces)
+  const float* aplus = nullptr;   // non-null: also the local flux from the cell's own traces
   float* Q;
   const float* trace;  // [4][n][9][FP] traces fMrT_f I of every cell and face
   const float* aminus;
@@ -228,7 +231,10 @@ int launchNeighborTensorCore(int order, const DeviceArrays& d, const float* trac
 // Transposed tensor-core neighbour kernel (tc_nbt.cu): the same inputs and result as
 // launchNeighborTensorCore, with the basis index on the TMEM lanes and the per-cell mixing in
 // registers; two persistent CTAs per SM.
-int launchNeighborTransposed(int order, const DeviceArrays& d, const float* trace, int* status, int sms, void* stream);
+// withLocalFlux: also the local flux rDivM_i T_i A+_i from the cell's own stored traces (one lift
+// for both fluxes; the local integral then ran as volume + traces, OrderKernels::lintVol).
+int launchNeighborTransposed(int order, const DeviceArrays& d, const float* trace, int* status, int sms, void* stream,
+                             bool withLocalFlux = false);
 // Transposed tensor-core local integral (tc_lintt.cu): volume + local flux of launchLintTensorCore
 // with the basis index on the TMEM lanes; writes the face traces (traceOnly: only them).
 int launchLintTransposed(int order, const DeviceArrays& d, float* trace, int traceOnly, int* status, int sms,

@@ -81,6 +81,23 @@ int launchLint(const sei::DeviceArrays& d, void* stream) {
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
+// Volume integral and face traces, no local flux (d.trace required).
+int launchLintVol(const sei::DeviceArrays& d, void* stream) {
+  if (d.n <= 0) return 0;
+  if (!d.trace) return -1;
+  // the exchange, I-staging and trace-staging area, then the block's Q rows
+  const size_t xs = 9 * K::kB * 32, is = 32 * K::kSt, ts = 4 * 32 * K::kTs;
+  const size_t area = xs > is ? (xs > ts ? xs : ts) : (is > ts ? is : ts);
+  const size_t smem = sizeof(float) * (area + 32 * K::kSt);
+  if (cudaFuncSetAttribute(K::SEI_CAT(sei_lintv_o, SEI_ORDER), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return -1;
+  const int blocks = (d.n + K::kCPB - 1) / K::kCPB;
+  K::SEI_CAT(sei_lintv_o, SEI_ORDER)<<<blocks, 288, smem, (cudaStream_t)stream>>>(
+      d.n, d.Q, d.I, d.star_nz, d.trace, d.ntotal > 0 ? d.ntotal : d.n, d.status);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
 int launchTaylor(int n, const float* derivs, const float* coeffs, float* out, void* stream) {
   if (n <= 0) return 0;
   const long threads = (long)n * 9;
@@ -102,6 +119,6 @@ int launchTaylorGather(int m, const int32_t* src, const int32_t* dst, const floa
 namespace sei {
 OrderKernels SEI_CAT(orderKernels, SEI_ORDER)() {
   return OrderKernels{launchLocal, launchNeighbor, launchTaylor, launchAder, launchLint, launchTaylorGather,
-                      K::kFlopAder, K::kFlopLocal, K::kFlopNeighbor};
+                      K::kFlopAder, K::kFlopLocal, K::kFlopNeighbor, launchLintVol};
 }
 }  // namespace sei

@@ -260,3 +260,59 @@ int launchWaitProbe(uint32_t polls, int arrive, int* status, void* stream) {
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 }  // namespace sei
+
+namespace {
+
+// TMEM load-shape check: every thread of a warp writes value = 1000 * lane + column into its own
+// lane (columns 0..63, .32x32b stores), then the warp reads the same region back with the shape
+// under test and records what each thread received: out[thread][reg] (64 registers at most).
+// shape 0: .16x64b.x32 (16 lanes from the warp's quarter base, 32 registers per thread).
+__global__ void sei_tc_ld_probe_kernel(int shape, float* __restrict__ out) {
+  __shared__ uint32_t tslot;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x < 32) sei_tc::tmemAlloc(&tslot, 64);
+  sei_tc::fenceBeforeSync();
+  __syncthreads();
+  sei_tc::fenceAfterSync();
+  const uint32_t base = tslot;  // warp 0: lanes 0..31
+  for (int c0 = 0; c0 < 64; c0 += 16) {
+    float v[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = (float)(1000 * lane + c0 + i);
+    sei_tc::tmemStore16(base + (uint32_t)c0, v);
+  }
+  sei_tc::tmemStoreWait();
+  __syncwarp();
+  uint32_t r[32];
+  const uint32_t a = base + (uint32_t)shape;  // shape 0 only (checked by the caller)
+  asm volatile(
+      "tcgen05.ld.sync.aligned.16x64b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
+      "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(a)
+      : "memory");
+  sei_tc::tmemLoadWait();
+  if (threadIdx.x < 32)
+    for (int i = 0; i < 32; ++i) out[lane * 32 + i] = __uint_as_float(r[i]);
+  sei_tc::fenceBeforeSync();
+  __syncthreads();
+  if (threadIdx.x < 32) sei_tc::tmemDealloc(tslot, 64);
+}
+
+}  // namespace
+
+extern "C" int sei_tc_ld_probe(int shape, float* out) {
+  if (!out || shape != 0) return SEI_ERR_ARG;
+  float* d = nullptr;
+  int rc = SEI_OK;
+  if (cudaMalloc(&d, 32 * 32 * sizeof(float)) != cudaSuccess) return SEI_ERR_OOM;
+  sei_tc_ld_probe_kernel<<<1, 32>>>(shape, d);
+  if (cudaDeviceSynchronize() != cudaSuccess || cudaMemcpy(out, d, 32 * 32 * sizeof(float), cudaMemcpyDeviceToHost))
+    rc = SEI_ERR_CUDA;
+  cudaGetLastError();
+  cudaFree(d);
+  return rc;
+}

@@ -6,6 +6,8 @@
 // tile's (quantity p, cell c) pairs on the 72 columns (n = 8 p + c):
 //   D[k, n] = sum_{i, m} rDivM_i[k, m] S_i[m, n],    A = [rDivM_0 | .. | rDivM_3] (64 x 4 KF),
 //   S_i[m, (p, c)] = sum_q (fP_h diag(fM)^-1 T_j(nb))[m, q] AminusT_i[q, p]   (FP32, CUDA cores),
+// and, when the local flux is fused in (Local.cpp:150-155 shares the lift rDivM_i), also
+//   S_i[m, (p, c)] += sum_q T_i(c)[m, q] AplusT_i[q, p]   (the cell's own stored trace),
 // so every per-cell 9 x 9 mixing stays inside one thread's registers, and the result lands on
 // the lane of the basis function it belongs to: the epilogue adds it to Q with loads and stores
 // that are contiguous along the basis index.
@@ -234,6 +236,30 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const u
 #pragma unroll
       for (int p = 0; p < 9; ++p) S[u][p] = 0.f;
     if (wt < D::ITEMS) {
+      if (A.aplus && c < cnt) {
+        // local flux of face fi from the cell's own trace: S += T_fi AplusT_fi (zero on DR faces)
+        const float* tr = A.trace + (((size_t)fi * A.ntotal + A.first + cell0 + c) * 9) * FP + 8 * oc;
+        const float* ap = A.aplus + ((size_t)(cell0 + c) * 4 + fi) * 81;
+#pragma unroll 3
+        for (int q = 0; q < 9; ++q) {
+          float r[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+          for (int h = 0; h < 2; ++h)
+            if (8 * oc + 4 * h < FP) {
+              const float4 y = __ldg(reinterpret_cast<const float4*>(tr + q * FP) + h);
+              r[4 * h] = y.x;
+              r[4 * h + 1] = y.y;
+              r[4 * h + 2] = y.z;
+              r[4 * h + 3] = y.w;
+            }
+#pragma unroll
+          for (int p = 0; p < 9; ++p) {
+            const float a = __ldg(ap + q + 9 * p);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) S[u][p] = fmaf(r[u], a, S[u][p]);
+          }
+        }
+      }
       if (meta.reg[4 * c + fi]) {
         const float* xr = X + c * CS + fi * 9 * FP + 8 * oc;
         const float* am = A.aminus + ((size_t)(cell0 + c) * 4 + fi) * 81;
@@ -352,11 +378,13 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const u
 
 template <int ORD>
 int launchNbt(const sei::DeviceArrays& d, const float* trace, int* status, int sms, void* stream, const void* opSym,
-              const void* scSym) {
+              const void* scSym, bool withLocalFlux) {
   using Dm = NbtDims<ORD>;
   sei::TcNbArgs a{};
   a.n = d.n;
   a.ntotal = d.ntotal > 0 ? d.ntotal : d.n;
+  a.first = d.first;
+  a.aplus = withLocalFlux ? d.aplus : nullptr;
   a.Q = d.Q;
   a.trace = trace;
   a.aminus = d.aminus;
@@ -381,14 +409,18 @@ int launchNbt(const sei::DeviceArrays& d, const float* trace, int* status, int s
 
 namespace sei {
 
-int launchNeighborTransposed(int order, const DeviceArrays& d, const float* trace, int* status, int sms, void* stream) {
+int launchNeighborTransposed(int order, const DeviceArrays& d, const float* trace, int* status, int sms, void* stream,
+                             bool withLocalFlux) {
   switch (order) {
     case 4:
-      return launchNbt<4>(d, trace, status, sms, stream, (const void*)&sei_tc_o4::knbt_op, (const void*)&sei_tc_o4::knbt_scale);
+      return launchNbt<4>(d, trace, status, sms, stream, (const void*)&sei_tc_o4::knbt_op, (const void*)&sei_tc_o4::knbt_scale,
+                          withLocalFlux);
     case 5:
-      return launchNbt<5>(d, trace, status, sms, stream, (const void*)&sei_tc_o5::knbt_op, (const void*)&sei_tc_o5::knbt_scale);
+      return launchNbt<5>(d, trace, status, sms, stream, (const void*)&sei_tc_o5::knbt_op, (const void*)&sei_tc_o5::knbt_scale,
+                          withLocalFlux);
     case 6:
-      return launchNbt<6>(d, trace, status, sms, stream, (const void*)&sei_tc_o6::knbt_op, (const void*)&sei_tc_o6::knbt_scale);
+      return launchNbt<6>(d, trace, status, sms, stream, (const void*)&sei_tc_o6::knbt_op, (const void*)&sei_tc_o6::knbt_scale,
+                          withLocalFlux);
     default:
       return -1;
   }

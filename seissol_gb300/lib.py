@@ -119,6 +119,7 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_tc_gemm_check", i, [VP, VP, VP, i, i, i])
     _sig(lib, "sei_tc_layout_check", i, [VP, VP, VP, i, i, i, i, i, i])
     _sig(lib, "sei_check_wait_timeout", i, [VP, i, i])
+    _sig(lib, "sei_tc_ld_probe", i, [i, VP])
     _sig(lib, "sei_device_clock_khz", i, [i, C.POINTER(C.c_int)])
     _sig(lib, "sei_dr_setup", i, [VP, C.POINTER(RSParams), C.POINTER(i64)])
     _sig(lib, "sei_dr_num_points", i, [i])

@@ -52,7 +52,7 @@ def test_local_integral_tensor_cores(built_lib, order, form):
     ctx.close()
 
 
-@pytest.mark.parametrize("order,form", [(4, 1), (5, 1), (6, 1), (4, 0), (6, 0)])
+@pytest.mark.parametrize("order,form", [(4, 1), (5, 1), (6, 1), (4, 0), (6, 0), (6, 2)])
 def test_neighbor_tensor_cores(built_lib, order, form):
     """The neighbour flux from the stored face traces, transposed (form 1) and rows (form 0)
     kernels; after ADER alone the traces are stale and the neighbour call recomputes them from
@@ -109,7 +109,7 @@ def test_mixed_and_fp32_agree_on_larger_mesh(built_lib):
     b.close()
 
 
-@pytest.mark.parametrize("precision,ncand", [(0, 2), (PREC_F16X3, 12)])
+@pytest.mark.parametrize("precision,ncand", [(0, 2), (PREC_F16X3, 13)])
 def test_autotune_keeps_state_and_results(built_lib, precision, ncand):
     """sei_autotune times every variant of the step, restores the DOFs, keeps the fastest variant;
     five steps with the chosen options then agree with the FP32 path within 1e-5."""
@@ -120,7 +120,7 @@ def test_autotune_keeps_state_and_results(built_lib, precision, ncand):
     assert r["candidates"] == ncand
     assert 0 < r["best_ms"] <= r["worst_ms"]
     assert r["nb_ctas"] in (1, 2, 3) and r["fused_local"] in (0, 1) and r["tc_local"] in (0, 1, 2)
-    assert r["nb_form"] in (0, 1)
+    assert r["nb_form"] in (0, 1, 2)
     assert np.array_equal(a.get_dofs(), q0)
     a.run("all", dt, 5)
     ref.run("all", dt, 5)
@@ -209,3 +209,28 @@ def test_neighbor_forms_agree_with_partial_tile(built_lib, order):
         outs.append(q_gpu - q0)
         ctx.close()
     assert max(rel_l2_per_quantity(outs[0], outs[1])) < 2e-6
+
+
+@pytest.mark.parametrize("order", [4, 5, 6])
+def test_ten_steps_local_flux_in_neighbour_kernel(built_lib, order):
+    """SEI_OPT_NB_FORM 2: in kernel 'all' the local flux joins the neighbour flux in the transposed
+    tensor-core kernel (the local integral computes the volume and the traces); ten steps within
+    1e-5 of the FP64 oracle, and the pipelined host-buffer run equals the device run bit for bit."""
+    ctx, n, q0 = _ctx(order, PREC_F16X3)
+    ctx.set_option(OPT_NB_FORM, 2)
+    cells = ctx.get_cells()
+    dt = ctx.cfl_timestep(0.5)
+    q_ref = oracle_py.Oracle(order).steps(q0, cells["star"].astype(np.float64), cells["AplusT"].astype(np.float64),
+                                          cells["AminusT"].astype(np.float64), cells["neighbor"], cells["side"],
+                                          cells["orient"], dt, 10, cells["face_type"])
+    ctx.run("all", dt, 10)
+    ctx.sync()
+    errs = rel_l2_per_quantity(ctx.get_dofs(), q_ref)
+    assert max(errs) < 1e-5, errs
+    out = np.empty_like(q0)
+    ctx.run_host("all", dt, 3, q0, out)
+    ctx.set_dofs(q0)
+    ctx.run("all", dt, 3)
+    ctx.sync()
+    assert np.array_equal(out, ctx.get_dofs())
+    ctx.close()
