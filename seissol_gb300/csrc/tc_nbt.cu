@@ -18,14 +18,17 @@
 // one another's copy and MMA waits.  Per tile and warpgroup:
 //   gather  one warp: a bulk copy (cp.async.bulk, mbarrier transaction count) per regular face
 //           of the neighbour's trace rows (9 FP floats); L2 prefetch of the tile's DOFs;
+//   flux    one thread, on its own mbarrier: the tile's AminusT (and AplusT) rows, one contiguous
+//           bulk copy each, issued as soon as the previous tile's mixing has read them;
 //   map     thread (face, q), faces ordered by orientation h so a warp mostly runs one branch:
 //           the trace row through fP_h diag(fM)^-1 in place (generated literal code);
-//   mix     thread (cell c, face i, octet of m): S for 8 m x 9 p in registers (AminusT read from
-//           global); per column (p, c) the maximum over all faces and m (warp shuffles, then
-//           shared atomics) gives a power-of-two scale; S * 2^-e split into FP16 hi + lo, the B
-//           operand (K-major), written over the trace buffer;
+//   mix     thread (cell c, face i, octet of m): S for 8 m x 9 p in registers (flux matrices
+//           from shared memory); per column (p, c) the maximum over all faces and m (warp
+//           shuffles, then shared atomics) gives a power-of-two scale; S * 2^-e split into FP16
+//           hi + lo, the B operand (K-major), written over the trace buffer;
 //   MMA     one thread: D = A_hi S_hi + A_hi S_lo + A_lo S_hi (FP32 accumulation in TMEM);
-//   epilogue  the next tile's gather is issued, then lane k: Q[c][p][k] += D[k, (p, c)] 2^{f_k} 2^{e_(p,c)}.
+//   epilogue  the tile's DOFs are loaded while the MMA runs; the next tile's gather is issued,
+//           then (.16x64b TMEM loads, all 32 threads of a warp) Q[c][p][k] += D[k, (p, c)] 2^{f_k} 2^{e_(p,c)}.
 //
 // Failure handling: every mbarrier wait is bounded and its outcome made uniform over the
 // warpgroup (barrier reduction).  A wait that gives up sets the status word, waits once more
@@ -68,10 +71,11 @@ struct NbtDims {
   static constexpr size_t kX = (size_t)kNC * CS * 4;
   static constexpr size_t kBS = (size_t)kCols * K * 2 * 2;
   static constexpr size_t kWgBuf = ((kX > kBS ? kX : kBS) + 1023) / 1024 * 1024;  // trace tile, then B operand
-  static constexpr size_t kSmem = kOpA + kWG * kWgBuf;
+  static constexpr size_t kAT = (size_t)kNC * 4 * 81 * 4;  // the tile's AminusT (or AplusT) rows
+  static constexpr size_t kSmem = kOpA + kWG * (kWgBuf + 2 * kAT);
   static_assert(B <= 64, "M = 64 holds the basis");
   static_assert(K % 16 == 0 && ITEMS % 32 == 0 && ITEMS <= 128, "whole MMA K steps and whole warps");
-  static_assert(kX % 16 == 0 && kOpA % 1024 == 0, "16-byte regions");
+  static_assert(kX % 16 == 0 && kOpA % 1024 == 0 && kAT % 16 == 0, "16-byte regions");
 };
 
 template <int ORD, int FP, int F>
@@ -141,13 +145,26 @@ __device__ __forceinline__ void issueGather(const sei::TcNbArgs& A, int tile, fl
   if (lane == 0) sei_tc::prefetchL2(A.Q + (size_t)cell0 * 9 * D::Bp, (uint32_t)(cnt * 9 * D::Bp * 4));
 }
 
+// One thread: the bulk copies of tile `tile`'s flux matrices, AminusT (and AplusT with the local
+// flux) of its cells, [cell][face][81] each, into the warpgroup's staging region.
+template <int ORD>
+__device__ __forceinline__ void issueFlux(const sei::TcNbArgs& A, int tile, float* Am, uint64_t* mbar) {
+  using D = NbtDims<ORD>;
+  const int cell0 = tile * kNC;
+  const int cnt = A.n - cell0 < kNC ? A.n - cell0 : kNC;
+  const uint32_t bytes = (uint32_t)cnt * 4 * 81 * 4;
+  sei_tc::mbarExpectTx(mbar, A.aplus ? 2 * bytes : bytes);
+  sei_tc::bulkCopyG2S(Am, A.aminus + (size_t)cell0 * 4 * 81, bytes, mbar);
+  if (A.aplus) sei_tc::bulkCopyG2S(Am + D::kAT / 4, A.aplus + (size_t)cell0 * 4 * 81, bytes, mbar);
+}
+
 template <int ORD>
 __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const uint16_t* __restrict__ opA,
                                                         const float* __restrict__ scA) {
   using D = NbtDims<ORD>;
   constexpr int B = D::B, Bp = D::Bp, F = D::F, FP = D::FP, KC = D::KC, OCT = D::OCT, CS = D::CS;
   extern __shared__ __align__(1024) unsigned char sm[];
-  __shared__ uint64_t mbarTab, mbarLdAll[kWG], mbarMmaAll[kWG];
+  __shared__ uint64_t mbarTab, mbarLdAll[kWG], mbarMmaAll[kWG], mbarAAll[kWG];
   __shared__ uint32_t tslot;
   __shared__ TileMeta metaAll[kWG];
   __shared__ unsigned smaxAll[kWG][kCols];
@@ -162,6 +179,8 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const u
   uint16_t* bLo = bHi + kCols * D::K;
   uint64_t* mbarLd = &mbarLdAll[wg];
   uint64_t* mbarMma = &mbarMmaAll[wg];
+  uint64_t* mbarA = &mbarAAll[wg];
+  float* Am = reinterpret_cast<float*>(sm + D::kOpA + kWG * D::kWgBuf + (size_t)wg * 2 * D::kAT);  // AminusT, AplusT
   TileMeta& meta = metaAll[wg];
   unsigned* smax = smaxAll[wg];
   float* csc = cscAll[wg];
@@ -171,6 +190,7 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const u
     for (int g = 0; g < kWG; ++g) {
       sei_tc::mbarInit(&mbarLdAll[g], 1);
       sei_tc::mbarInit(&mbarMmaAll[g], 1);
+      sei_tc::mbarInit(&mbarAAll[g], 1);
     }
     sei_tc::mbarExpectTx(&mbarTab, (uint32_t)D::kOpA);
     sei_tc::bulkCopyG2S(aHi, opA, (uint32_t)D::kOpA, &mbarTab);
@@ -183,18 +203,21 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const u
   // through its barriers and the warp-collective TMEM loads
   bool ok = wgSyncAnd(wg, sei_tc::mbarWait(&mbarTab, 0, kMaxPolls));
   const bool tabPending = !ok;
-  uint32_t ldPhase = 0, mmaPhase = 0;
-  bool ldPending = false, mmaPending = false;
+  uint32_t ldPhase = 0, mmaPhase = 0, aPhase = 0;
+  bool ldPending = false, mmaPending = false, aPending = false;
   const int ntiles = (A.n + kNC - 1) / kNC;
   const int stride = (int)gridDim.x * kWG;
   int tile = (int)blockIdx.x * kWG + wg;
   if (ok && tile < ntiles) {
     if (ww == 0) issueGather<ORD>(A, tile, X, meta, mbarLd);
-    ldPending = true;
+    if (wt == 32) issueFlux<ORD>(A, tile, Am, mbarA);
+    ldPending = aPending = true;
   }
-  // epilogue row of this thread (M = 64: rows 16 w + t on lanes 32 w + t, t < 16)
-  const int kq = lane < 16 ? 16 * ww + lane : -1;
-  const bool erow = kq >= 0 && kq < B;
+  // epilogue row and column parity of this thread (M = 64: row 16 w + r on lane 32 w + r, r < 16;
+  // the .16x64b load gives thread t row r = (t >> 2) + 8 (t & 1) and the columns of parity (t >> 1) & 1)
+  const int kq = 16 * ww + (lane >> 2) + 8 * (lane & 1);
+  const int es = (lane >> 1) & 1;
+  const bool erow = kq < B;
   const float fsc = erow ? __ldg(scA + kq) : 0.f;
   for (; ok && tile < ntiles; tile += stride) {
     ok = wgSyncAnd(wg, sei_tc::mbarWait(mbarLd, ldPhase, kMaxPolls));  // also: metadata visible
@@ -229,6 +252,10 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const u
     }
     wgSync(wg);
     // ---- mix: S[m, (p, c)] for the 8 m of this thread's octet
+    ok = wgSyncAnd(wg, sei_tc::mbarWait(mbarA, aPhase, kMaxPolls));
+    if (!ok) break;
+    aPhase ^= 1;
+    aPending = false;
     const int c = wt & 7, g = wt >> 3, fi = g / OCT, oc = g % OCT;
     float S[8][9];
 #pragma unroll
@@ -239,7 +266,7 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const u
       if (A.aplus && c < cnt) {
         // local flux of face fi from the cell's own trace: S += T_fi AplusT_fi (zero on DR faces)
         const float* tr = A.trace + (((size_t)fi * A.ntotal + A.first + cell0 + c) * 9) * FP + 8 * oc;
-        const float* ap = A.aplus + ((size_t)(cell0 + c) * 4 + fi) * 81;
+        const float* ap = Am + D::kAT / 4 + (c * 4 + fi) * 81;
 #pragma unroll 3
         for (int q = 0; q < 9; ++q) {
           float r[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -254,7 +281,7 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const u
             }
 #pragma unroll
           for (int p = 0; p < 9; ++p) {
-            const float a = __ldg(ap + q + 9 * p);
+            const float a = ap[q + 9 * p];
 #pragma unroll
             for (int u = 0; u < 8; ++u) S[u][p] = fmaf(r[u], a, S[u][p]);
           }
@@ -262,7 +289,7 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const u
       }
       if (meta.reg[4 * c + fi]) {
         const float* xr = X + c * CS + fi * 9 * FP + 8 * oc;
-        const float* am = A.aminus + ((size_t)(cell0 + c) * 4 + fi) * 81;
+        const float* am = Am + (c * 4 + fi) * 81;
 #pragma unroll 3
         for (int q = 0; q < 9; ++q) {
           const float4 r0 = reinterpret_cast<const float4*>(xr + q * FP)[0];
@@ -273,7 +300,7 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const u
             if (8 * oc + u >= F) r[u] = 0.f;  // past the face basis (the next row at orders 4 and 5)
 #pragma unroll
           for (int p = 0; p < 9; ++p) {
-            const float a = __ldg(am + q + 9 * p);
+            const float a = am[q + 9 * p];
 #pragma unroll
             for (int u = 0; u < 8; ++u) S[u][p] = fmaf(r[u], a, S[u][p]);
           }
@@ -290,7 +317,12 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const u
         if (lane < 8) atomicMax(&smax[8 * p + c], __float_as_uint(mx));
       }
     }
-    wgSync(wg);  // the maxima are complete and every read of the trace tile is done
+    wgSync(wg);  // the maxima are complete and every read of the trace tile and flux matrices is done
+    // the flux matrices of the warpgroup's next tile overlap the split, MMA and epilogue
+    if (tile + stride < ntiles) {
+      if (wt == 32) issueFlux<ORD>(A, tile + stride, Am, mbarA);
+      aPending = true;
+    }
     if (wt < kCols) csc[wt] = sei_tc::pow2(sei_tc::pow2Exp(__uint_as_float(smax[wt])));
     if (wt < D::ITEMS) {
 #pragma unroll
@@ -329,13 +361,15 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const u
       sei_tc::mmaCommit(mbarMma);
     }
     mmaPending = true;
-    // ---- epilogue: lane k adds D[k, (p, c)] to Q[c][p][k]
-    float qv[9][kNC];
+    // ---- epilogue: row k adds D[k, (p, c)] to Q[c][p][k]; register j holds column n = 2 j + es,
+    // i.e. p = j / 4 and c = 2 (j % 4) + es
+    float* Qr = A.Q + ((size_t)cell0 * 9 + (size_t)es * 9) * Bp + kq;
+    float qv[36];
 #pragma unroll
-    for (int p = 0; p < 9; ++p)
-#pragma unroll
-      for (int cc = 0; cc < kNC; ++cc)
-        qv[p][cc] = (erow && cc < cnt) ? A.Q[((size_t)(cell0 + cc) * 9 + p) * Bp + kq] : 0.f;
+    for (int j = 0; j < 36; ++j) {
+      const int cc = 2 * (j & 3) + es;
+      qv[j] = (erow && cc < cnt) ? Qr[(size_t)(18 * (j & 3) + (j >> 2)) * Bp] : 0.f;
+    }
     ok = wgSyncAnd(wg, sei_tc::mbarWait(mbarMma, mmaPhase, kMaxPolls));
     if (!ok) break;
     mmaPhase ^= 1;
@@ -349,14 +383,14 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const u
     }
     {
       const uint32_t tb = taddr + ((uint32_t)(32 * ww) << 16);
+      float v[36];
+      sei_tc::tmemLoad16x64b32(tb, v);
+      sei_tc::tmemLoad16x64b4(tb + 64u, v + 32);
+      sei_tc::tmemLoadWait();
 #pragma unroll
-      for (int p = 0; p < 9; ++p) {
-        float v[8];
-        sei_tc::tmemLoad8(tb + (uint32_t)(8 * p), v);
-        sei_tc::tmemLoadWait();
-#pragma unroll
-        for (int cc = 0; cc < kNC; ++cc)
-          if (erow && cc < cnt) A.Q[((size_t)(cell0 + cc) * 9 + p) * Bp + kq] = qv[p][cc] + v[cc] * fsc * csc[8 * p + cc];
+      for (int j = 0; j < 36; ++j) {
+        const int cc = 2 * (j & 3) + es;
+        if (erow && cc < cnt) Qr[(size_t)(18 * (j & 3) + (j >> 2)) * Bp] = qv[j] + v[j] * fsc * csc[2 * j + es];
       }
     }
     sei_tc::fenceBeforeSync();
@@ -369,6 +403,7 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const u
     // second bounded wait before the tensor memory is freed and the shared memory released
     if (tabPending) (void)sei_tc::mbarWait(&mbarTab, 0, kMaxPolls);
     if (ldPending) (void)sei_tc::mbarWait(mbarLd, ldPhase, kMaxPolls);
+    if (aPending) (void)sei_tc::mbarWait(mbarA, aPhase, kMaxPolls);
     if (mmaPending) (void)sei_tc::mbarWait(mbarMma, mmaPhase, kMaxPolls);
   }
   sei_tc::fenceBeforeSync();
