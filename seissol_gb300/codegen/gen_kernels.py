@@ -249,20 +249,44 @@ def gen_order(order: int) -> str:
             a("    __syncthreads();")
             a("  }")
 
-    def emit_volume_traces():
-        """Volume integral into acc (from zero), then the four face traces staged for one coalesced store."""
-        emit_volume_part(acc_zero=True)
-        a("  // ---- face traces fMrT_f I of all four faces, staged [f][lane][q][kFP] (row stride kTs)")
+    def emit_traces_volume_reduce():
+        """From I in registers: the four face traces through the shared area (one face at a time,
+        one bulk copy per cell out), then the volume integral, added to Q by bulk reduce-adds."""
+        a("  // ---- face traces fMrT_f I, one face at a time through the shared area")
         for f in range(4):
             a("  {")
             a("    float T[kF];")
             _matvec(L, "    ", G["fMrT"][f], "I", "T", F, B, True)
-            a(f"    float4* st = reinterpret_cast<float4*>(sm + ({f} * 32 + lane) * kTs + q * kFP);")
-            a(f"#pragma unroll\n    for (int m4 = 0; m4 < kFP / 4; ++m4)")
-            a("      st[m4] = make_float4(4 * m4 < kF ? T[4 * m4 < kF ? 4 * m4 : 0] : 0.f, 4 * m4 + 1 < kF ? T[4 * m4 + 1 < kF ? 4 * m4 + 1 : 0] : 0.f,")
-            a("                           4 * m4 + 2 < kF ? T[4 * m4 + 2 < kF ? 4 * m4 + 2 : 0] : 0.f, 4 * m4 + 3 < kF ? T[4 * m4 + 3 < kF ? 4 * m4 + 3 : 0] : 0.f);")
+            if f > 0:
+                a("    if (threadIdx.x < 32) sei_tc::bulkWaitRead();  // the previous face's copies have read the area")
+                a("    __syncthreads();")
+            a("    float4* stg = reinterpret_cast<float4*>(X + lane * kTs + q * kFP);")
+            a("#pragma unroll\n    for (int m4 = 0; m4 < kFP / 4; ++m4)")
+            a("      stg[m4] = make_float4(4 * m4 < kF ? T[4 * m4 < kF ? 4 * m4 : 0] : 0.f, 4 * m4 + 1 < kF ? T[4 * m4 + 1 < kF ? 4 * m4 + 1 : 0] : 0.f,")
+            a("                            4 * m4 + 2 < kF ? T[4 * m4 + 2 < kF ? 4 * m4 + 2 : 0] : 0.f, 4 * m4 + 3 < kF ? T[4 * m4 + 3 < kF ? 4 * m4 + 3 : 0] : 0.f);")
+            a("    sei_tc::fenceProxyAsync();")
+            a("    __syncthreads();")
+            a("    if (threadIdx.x < 32 && lane < cnt) {")
+            a(f"      sei_tc::bulkCopyS2G(trace + ((size_t){f} * tplane + cell0 + lane) * 9 * kFP, X + lane * kTs, 9 * kFP * 4);")
+            a("      sei_tc::bulkCommit();")
+            a("    }")
             a("  }")
+        a("  if (threadIdx.x < 32) sei_tc::bulkWaitRead();")
         a("  __syncthreads();")
+        emit_volume_part(acc_zero=True)
+        a("""  // ---- Q += volume: staged, then one bulk reduce-add per cell
+  {
+    float4* dst = reinterpret_cast<float4*>(X + lane * kSt + q * kBp);
+#pragma unroll
+    for (int k4 = 0; k4 < kBp / 4; ++k4) dst[k4] = make_float4(acc[4 * k4], acc[4 * k4 + 1], acc[4 * k4 + 2], acc[4 * k4 + 3]);
+  }
+  sei_tc::fenceProxyAsync();
+  __syncthreads();
+  if (threadIdx.x < 32 && lane < cnt) {
+    sei_tc::bulkReduceAddS2G(Q + (size_t)(cell0 + lane) * 9 * kBp, X + lane * kSt, 9 * kBp * 4);
+    sei_tc::bulkCommit();
+    sei_tc::bulkWaitRead();
+  }""")
 
     # fused ADER + local integral
     a(f"""
@@ -335,37 +359,31 @@ sei_lint_trace_o{order}(int n, float* __restrict__ Q, const float* __restrict__ 
     a(f"""
 // Volume integral alone (no local flux) plus the face traces fMrT_f I of every cell and face,
 // trace[4][tplane][9][kFP]: the local integral of the path whose tensor-core neighbour kernel also
-// applies the local flux (from these traces).  The block's I and Q arrive by bulk copies (one per
-// cell, cell stride kSt floats in shared memory), Q while the volume and the traces are computed;
-// the traces of all four faces are staged ([face][cell][q][kFP], cell stride kTs) and leave in one
-// coalesced store per face; Q + volume leaves by bulk copies.  status is set when a copy wait
-// gives up.  Shared memory: the larger of the exchange, I and trace areas, then the Q area.
-extern "C" __global__ void __launch_bounds__(288, 1)
+// applies the local flux (from these traces).  Shared memory is one area of max(exchange, DOF
+// staging) floats: the block's I rows arrive in it by one bulk copy per cell (cell stride kSt);
+// the traces go first, from I in registers, one face at a time staged in it ([cell][q][kFP],
+// cell stride kTs) and out by one bulk copy per cell; then the volume integral uses it as its
+// exchange, and its contribution, staged there ([cell][q][kBp]), is added to Q in L2 by one
+// bulk f32 reduce-add per cell, so the kernel never reads Q.  The traces before the volume keep
+// either I or the volume accumulator live, not both: two CTAs per SM.  status is set when the
+// copy wait gives up.
+extern "C" __global__ void __launch_bounds__(288, 2)
 sei_lintv_o{order}(int n, float* __restrict__ Q, const float* __restrict__ Iin, const float* __restrict__ star_nz,
                    float* __restrict__ trace, int tplane, int* __restrict__ status) {{""" + prologue)
-    a("""  __shared__ uint64_t sei_mbar[2];
-  constexpr int kAreaA = (9 * kB * 32 > 32 * kSt ? (9 * kB * 32 > 4 * 32 * kTs ? 9 * kB * 32 : 4 * 32 * kTs)
-                                                 : (32 * kSt > 4 * 32 * kTs ? 32 * kSt : 4 * 32 * kTs));
-  float* QS = sm + kAreaA;  // the block's Q rows [32][kSt]
+    a("""  __shared__ uint64_t sei_mbar;
   const int cell0 = blockIdx.x * kCPB;
   const int cnt = n - cell0 < kCPB ? n - cell0 : kCPB;
-  if (threadIdx.x == 0) {
-    sei_tc::mbarInit(&sei_mbar[0], 1);
-    sei_tc::mbarInit(&sei_mbar[1], 1);
-  }
+  if (threadIdx.x == 0) sei_tc::mbarInit(&sei_mbar, 1);
   __syncthreads();
   if (threadIdx.x < 32) {
-    if (lane == 0) {
-      sei_tc::mbarExpectTx(&sei_mbar[0], (unsigned)(cnt * 9 * kBp * 4));
-      sei_tc::mbarExpectTx(&sei_mbar[1], (unsigned)(cnt * 9 * kBp * 4));
-    }
+    if (lane == 0) sei_tc::mbarExpectTx(&sei_mbar, (unsigned)(cnt * 9 * kBp * 4));
     __syncwarp();
-    if (lane < cnt) {
-      sei_tc::bulkCopyG2S(X + lane * kSt, Iin + (size_t)(cell0 + lane) * 9 * kBp, 9 * kBp * 4, &sei_mbar[0]);
-      sei_tc::bulkCopyG2S(QS + lane * kSt, Q + (size_t)(cell0 + lane) * 9 * kBp, 9 * kBp * 4, &sei_mbar[1]);
-    }
+    if (lane < cnt) sei_tc::bulkCopyG2S(X + lane * kSt, Iin + (size_t)(cell0 + lane) * 9 * kBp, 9 * kBp * 4, &sei_mbar);
   }
-  bool ok = sei_tc::mbarWait(&sei_mbar[0], 0, 1u << 26);
+  if (!sei_tc::mbarWait(&sei_mbar, 0, 1u << 26)) {
+    if (threadIdx.x == 0 && status) atomicExch(status, 1);
+    (void)sei_tc::mbarWait(&sei_mbar, 0, 1u << 26);  // the copies in flight land before X is reused
+  }
   float I[kBp];
   {
     const float4* src = reinterpret_cast<const float4*>(X + lane * kSt + q * kBp);
@@ -379,40 +397,29 @@ sei_lintv_o{order}(int n, float* __restrict__ Q, const float* __restrict__ Iin, 
     }
   }
   __syncthreads();""")
-    emit_volume_traces()
-    a("""  {
-    constexpr int R4 = 9 * kFP / 4;  // float4 per cell and face
-#pragma unroll 1
-    for (int f = 0; f < 4; ++f) {
-      float4* dst = reinterpret_cast<float4*>(trace + ((size_t)f * tplane + cell0) * 9 * kFP);
-#pragma unroll 1
-      for (int idx = threadIdx.x; idx < kCPB * R4; idx += blockDim.x) {
-        const int Lc = idx / R4, rem = idx - Lc * R4;
-        if (cell0 + Lc < n) dst[idx] = *reinterpret_cast<const float4*>(sm + (f * 32 + Lc) * kTs + 4 * rem);
-      }
-    }
-  }
-  ok = sei_tc::mbarWait(&sei_mbar[1], 0, 1u << 26) && ok;
-  if (!ok) {
-    if (threadIdx.x == 0 && status) atomicExch(status, 1);
-    (void)sei_tc::mbarWait(&sei_mbar[0], 0, 1u << 26);  // copies in flight land before the block exits
-    (void)sei_tc::mbarWait(&sei_mbar[1], 0, 1u << 26);
-  }
-  {
-    float4* qs = reinterpret_cast<float4*>(QS + lane * kSt + q * kBp);
-#pragma unroll
-    for (int k4 = 0; k4 < kBp / 4; ++k4) {
-      const float4 t = qs[k4];
-      qs[k4] = make_float4(t.x + acc[4 * k4], t.y + acc[4 * k4 + 1], t.z + acc[4 * k4 + 2], t.w + acc[4 * k4 + 3]);
-    }
-  }
-  sei_tc::fenceProxyAsync();
-  __syncthreads();
-  if (threadIdx.x < 32 && lane < cnt) {
-    sei_tc::bulkCopyS2G(Q + (size_t)(cell0 + lane) * 9 * kBp, QS + lane * kSt, 9 * kBp * 4);
-    sei_tc::bulkCommit();
-    sei_tc::bulkWaitRead();
-  }""")
+    emit_traces_volume_reduce()
+    a("}")
+
+    # ADER + volume + traces (the predictor of the fused-flux path); at order 6 the 96 registers of
+    # two CTAs per SM spill, one CTA keeps everything in registers
+    lv_ctas = 1 if order >= 6 else 2
+    a(f"""
+// ADER, volume integral and face traces in one launch: the cell-local part of the step whose
+// tensor-core neighbour kernel applies both the local and the neighbour flux (from these traces).
+// I never leaves the chip.  Shared memory is one area of max(exchange, DOF staging) floats:
+// the block's Q rows arrive in it by bulk copies; the CK stages use it as their exchange; the
+// traces of one face at a time are staged in it ([cell][q][kFP], cell stride kTs) and leave by
+// one bulk copy per cell; the volume integral uses it as its exchange; finally the volume
+// contribution is staged in it ([cell][q][kBp], cell stride kSt) and added to Q in L2 by one
+// bulk f32 reduce-add per cell, so Q is read from HBM once and written once.  {lv_ctas} CTA(s) per SM.
+// derivs / dslot: optional packed derivative output as in sei_local.  status is set when the
+// DOF copy wait gives up.
+extern "C" __global__ void __launch_bounds__(288, {lv_ctas})
+sei_localv_o{order}(int n, float* __restrict__ Q, const float* __restrict__ star_nz, SeiCoeffs coeffs,
+                    float* __restrict__ derivs, const int* __restrict__ dslot, float* __restrict__ trace, int tplane,
+                    int* __restrict__ status) {{""" + prologue)
+    emit_ck(staged=True)
+    emit_traces_volume_reduce()
     a("}")
 
     # ---------------- neighbour kernel ----------------

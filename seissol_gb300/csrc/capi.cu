@@ -316,6 +316,16 @@ int launchLintOnly(sei_ctx* c, const sei::DeviceArrays& d, bool volumeOnly = fal
 
 // ADER followed by the local integral: two launches (default) or one fused launch.
 int launchLocal(sei_ctx* c, const sei::DeviceArrays& d, const float* coeffs, bool volumeOnly = false) {
+  if (volumeOnly && c->fused_local) {
+    // fused-flux path: ADER, volume and face traces in one launch, I stays on chip
+    int rc = profMark(c, 0);
+    if (rc) return rc;
+    sei::DeviceArrays dt = d;
+    dt.trace = c->d_trace + (size_t)d.first * 9 * ((sei::numFaceBasis(c->cfg.order) + 3) / 4 * 4);
+    if (c->k.localVol(dt, coeffs, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "ADER-volume-trace kernel launch failed");
+    c->trace_valid = d.n == c->n;
+    return SEI_OK;
+  }
   if (!c->fused_local || c->cfg.precision != SEI_PREC_FP32) {
     int rc = launchAderOnly(c, d, coeffs);
     return rc ? rc : launchLintOnly(c, d, volumeOnly);
@@ -850,8 +860,7 @@ static int runHostPipelined(sei_ctx* c, double dt, int nsteps, const float* in, 
     SEI_CUDA(cudaEventRecord(ev[k], c->copy_stream));
     SEI_CUDA(cudaStreamWaitEvent(c->stream, ev[k], 0));
     const sei::DeviceArrays d = gtsRange(c, b[k], b[k + 1], false);
-    rc = launchAderOnly(c, d, co);
-    if (!rc) rc = launchLintOnly(c, d, fusedFlux(c));
+    rc = launchLocal(c, d, co, fusedFlux(c));
   }
   if (rc) return rc;
   c->trace_valid = c->cfg.precision == SEI_PREC_F16X3 && c->d_trace;
@@ -859,7 +868,7 @@ static int runHostPipelined(sei_ctx* c, double dt, int nsteps, const float* in, 
     const sei::DeviceArrays all = arrays(c);
     if ((rc = launchNeighbor(c, all, fusedFlux(c)))) return rc;
     if (nsteps > 2 && (rc = runKernel(c, SEI_KERNEL_ALL, dt, nsteps - 2))) return rc;
-    if ((rc = launchAderOnly(c, all, co)) || (rc = launchLintOnly(c, all, fusedFlux(c)))) return rc;
+    if ((rc = launchLocal(c, all, co, fusedFlux(c)))) return rc;
   }
   for (int k = 0; k < nch && !rc; ++k) {
     rc = launchNeighbor(c, gtsRange(c, b[k], b[k + 1], true), fusedFlux(c));
@@ -1943,6 +1952,7 @@ int sei_autotune(sei_ctx* c, double dt, int steps, sei_tune_result* out) {
       for (int k = 1; k <= 3; ++k) cands.push_back({0, t, k, 0});
     }
     cands.push_back({0, 0, 3, 2});  // local flux inside the transposed neighbour kernel
+    cands.push_back({1, 0, 3, 2});  // the same after one ADER + volume + trace launch
   }
   // the DOFs are restored after every candidate: tuning leaves the state unchanged
   const size_t bytes = (size_t)c->n * 9 * c->Bp * sizeof(float);

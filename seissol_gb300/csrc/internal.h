@@ -88,6 +88,7 @@ struct OrderKernels {
   LaunchTaylorGatherFn taylorGather;
   double flopAder, flopLocal, flopNeighbor;  // non-zero flops per cell
   LaunchLintFn lintVol;       // volume + face traces, no local flux (the neighbour kernel applies it)
+  LaunchLocalFn localVol;     // ADER + volume + face traces, one launch (I stays on chip)
 };
 
 // pool[dst[e]] = (reset ? 0 : pool[dst[e]]) + pool[cell[e]] for e < m, blocks of blk floats

@@ -85,16 +85,31 @@ int launchLint(const sei::DeviceArrays& d, void* stream) {
 int launchLintVol(const sei::DeviceArrays& d, void* stream) {
   if (d.n <= 0) return 0;
   if (!d.trace) return -1;
-  // the exchange, I-staging and trace-staging area, then the block's Q rows
-  const size_t xs = 9 * K::kB * 32, is = 32 * K::kSt, ts = 4 * 32 * K::kTs;
-  const size_t area = xs > is ? (xs > ts ? xs : ts) : (is > ts ? is : ts);
-  const size_t smem = sizeof(float) * (area + 32 * K::kSt);
+  // one area: the exchange [9][kB][32], the I staging [32][kSt] and one face's traces [32][kTs]
+  const size_t xs = 9 * K::kB * 32, is = 32 * K::kSt, ts = 32 * K::kTs;
+  const size_t smem = sizeof(float) * (xs > is ? (xs > ts ? xs : ts) : (is > ts ? is : ts));
   if (cudaFuncSetAttribute(K::SEI_CAT(sei_lintv_o, SEI_ORDER), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return -1;
   const int blocks = (d.n + K::kCPB - 1) / K::kCPB;
   K::SEI_CAT(sei_lintv_o, SEI_ORDER)<<<blocks, 288, smem, (cudaStream_t)stream>>>(
       d.n, d.Q, d.I, d.star_nz, d.trace, d.ntotal > 0 ? d.ntotal : d.n, d.status);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+// ADER + volume + face traces (d.trace required); Q += volume by bulk reduce-adds.
+int launchLocalVol(const sei::DeviceArrays& d, const float* coeffs, void* stream) {
+  if (d.n <= 0) return 0;
+  if (!d.trace) return -1;
+  // one area: the exchange [9][kB][32], the DOF staging [32][kSt] and one face's traces [32][kTs]
+  const size_t xs = 9 * K::kB * 32, is = 32 * K::kSt, ts = 32 * K::kTs;
+  const size_t smem = sizeof(float) * (xs > is ? (xs > ts ? xs : ts) : (is > ts ? is : ts));
+  if (cudaFuncSetAttribute(K::SEI_CAT(sei_localv_o, SEI_ORDER), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return -1;
+  const int blocks = (d.n + K::kCPB - 1) / K::kCPB;
+  K::SEI_CAT(sei_localv_o, SEI_ORDER)<<<blocks, 288, smem, (cudaStream_t)stream>>>(
+      d.n, d.Q, d.star_nz, toCoeffs(coeffs), d.derivs, d.dslot, d.trace, d.ntotal > 0 ? d.ntotal : d.n, d.status);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -119,6 +134,6 @@ int launchTaylorGather(int m, const int32_t* src, const int32_t* dst, const floa
 namespace sei {
 OrderKernels SEI_CAT(orderKernels, SEI_ORDER)() {
   return OrderKernels{launchLocal, launchNeighbor, launchTaylor, launchAder, launchLint, launchTaylorGather,
-                      K::kFlopAder, K::kFlopLocal, K::kFlopNeighbor, launchLintVol};
+                      K::kFlopAder, K::kFlopLocal, K::kFlopNeighbor, launchLintVol, launchLocalVol};
 }
 }  // namespace sei

@@ -83,6 +83,12 @@ __device__ __forceinline__ void bulkCopyS2G(void* dst, const void* src, uint32_t
   asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;\n" ::"l"(dst), "r"(smemAddr(src)), "r"(bytes)
                : "memory");
 }
+// The same with an element-wise f32 add into global memory (dst[i] += src[i], performed in L2).
+__device__ __forceinline__ void bulkReduceAddS2G(float* dst, const float* src, uint32_t bytes) {
+  asm volatile("cp.reduce.async.bulk.global.shared::cta.bulk_group.add.f32 [%0], [%1], %2;\n" ::"l"(dst),
+               "r"(smemAddr(src)), "r"(bytes)
+               : "memory");
+}
 __device__ __forceinline__ void bulkCommit() { asm volatile("cp.async.bulk.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void bulkWaitRead() { asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory"); }
 

@@ -27,8 +27,9 @@
 //           shuffles, then shared atomics) gives a power-of-two scale; S * 2^-e split into FP16
 //           hi + lo, the B operand (K-major), written over the trace buffer;
 //   MMA     one thread: D = A_hi S_hi + A_hi S_lo + A_lo S_hi (FP32 accumulation in TMEM);
-//   epilogue  the tile's DOFs are loaded while the MMA runs; the next tile's gather is issued,
-//           then (.16x64b TMEM loads, all 32 threads of a warp) Q[c][p][k] += D[k, (p, c)] 2^{f_k} 2^{e_(p,c)}.
+//   epilogue  the next tile's gather is issued, then (.16x64b TMEM loads, all 32 threads of a
+//           warp) Q[c][p][k] += D[k, (p, c)] 2^{f_k} 2^{e_(p,c)} as f32 reductions performed in L2
+//           (one add per element: the result does not depend on their order).
 //
 // Failure handling: every mbarrier wait is bounded and its outcome made uniform over the
 // warpgroup (barrier reduction).  A wait that gives up sets the status word, waits once more
@@ -361,15 +362,10 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const u
       sei_tc::mmaCommit(mbarMma);
     }
     mmaPending = true;
-    // ---- epilogue: row k adds D[k, (p, c)] to Q[c][p][k]; register j holds column n = 2 j + es,
-    // i.e. p = j / 4 and c = 2 (j % 4) + es
+    // ---- epilogue: row k adds D[k, (p, c)] to Q[c][p][k] by reductions in L2 (the tile's DOFs
+    // were prefetched there by the gather); register j holds column n = 2 j + es, i.e. p = j / 4
+    // and c = 2 (j % 4) + es
     float* Qr = A.Q + ((size_t)cell0 * 9 + (size_t)es * 9) * Bp + kq;
-    float qv[36];
-#pragma unroll
-    for (int j = 0; j < 36; ++j) {
-      const int cc = 2 * (j & 3) + es;
-      qv[j] = (erow && cc < cnt) ? Qr[(size_t)(18 * (j & 3) + (j >> 2)) * Bp] : 0.f;
-    }
     ok = wgSyncAnd(wg, sei_tc::mbarWait(mbarMma, mmaPhase, kMaxPolls));
     if (!ok) break;
     mmaPhase ^= 1;
@@ -390,7 +386,7 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const u
 #pragma unroll
       for (int j = 0; j < 36; ++j) {
         const int cc = 2 * (j & 3) + es;
-        if (erow && cc < cnt) Qr[(size_t)(18 * (j & 3) + (j >> 2)) * Bp] = qv[j] + v[j] * fsc * csc[2 * j + es];
+        if (erow && cc < cnt) atomicAdd(Qr + (size_t)(18 * (j & 3) + (j >> 2)) * Bp, v[j] * fsc * csc[2 * j + es]);
       }
     }
     sei_tc::fenceBeforeSync();

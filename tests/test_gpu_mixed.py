@@ -109,7 +109,7 @@ def test_mixed_and_fp32_agree_on_larger_mesh(built_lib):
     b.close()
 
 
-@pytest.mark.parametrize("precision,ncand", [(0, 2), (PREC_F16X3, 13)])
+@pytest.mark.parametrize("precision,ncand", [(0, 2), (PREC_F16X3, 14)])
 def test_autotune_keeps_state_and_results(built_lib, precision, ncand):
     """sei_autotune times every variant of the step, restores the DOFs, keeps the fastest variant;
     five steps with the chosen options then agree with the FP32 path within 1e-5."""
@@ -211,13 +211,16 @@ def test_neighbor_forms_agree_with_partial_tile(built_lib, order):
     assert max(rel_l2_per_quantity(outs[0], outs[1])) < 2e-6
 
 
+@pytest.mark.parametrize("fused", [0, 1])
 @pytest.mark.parametrize("order", [4, 5, 6])
-def test_ten_steps_local_flux_in_neighbour_kernel(built_lib, order):
+def test_ten_steps_local_flux_in_neighbour_kernel(built_lib, order, fused):
     """SEI_OPT_NB_FORM 2: in kernel 'all' the local flux joins the neighbour flux in the transposed
-    tensor-core kernel (the local integral computes the volume and the traces); ten steps within
-    1e-5 of the FP64 oracle, and the pipelined host-buffer run equals the device run bit for bit."""
+    tensor-core kernel (the local integral computes the volume and the traces; with
+    SEI_OPT_FUSED_LOCAL 1 one launch computes ADER, volume and traces); ten steps within 1e-5 of
+    the FP64 oracle, and the pipelined host-buffer run equals the device run bit for bit."""
     ctx, n, q0 = _ctx(order, PREC_F16X3)
     ctx.set_option(OPT_NB_FORM, 2)
+    ctx.set_option(1, fused)  # SEI_OPT_FUSED_LOCAL
     cells = ctx.get_cells()
     dt = ctx.cfl_timestep(0.5)
     q_ref = oracle_py.Oracle(order).steps(q0, cells["star"].astype(np.float64), cells["AplusT"].astype(np.float64),
@@ -234,3 +237,37 @@ def test_ten_steps_local_flux_in_neighbour_kernel(built_lib, order):
     ctx.sync()
     assert np.array_equal(out, ctx.get_dofs())
     ctx.close()
+
+
+@pytest.mark.parametrize("fused", [0, 1])
+@pytest.mark.parametrize("order", [4, 6])
+def test_local_flux_in_neighbour_kernel_partial_blocks(built_lib, order, fused):
+    """The fused-flux step (SEI_OPT_NB_FORM 2, with and without the one-launch ADER + volume +
+    traces kernel) on the 317-cell cut mesh: the last 32-cell block of the cell-local kernels and
+    the last 8-cell tile of the neighbour kernel are partial, and outflow faces carry no flux;
+    three steps within 1e-5 of the FP64 oracle."""
+    from seissol_gb300 import Context
+    base, _, _ = _ctx(order, 0, seed=23)
+    cells = base.get_cells()
+    dt = base.cfl_timestep(0.5)
+    base.close()
+    keep = 317
+    cut = {k: np.ascontiguousarray(v[:keep]) for k, v in cells.items()}
+    ft = np.array(cut["face_type"], dtype=np.int8)
+    nb = np.array(cut["neighbor"])
+    ft[nb >= keep] = 2
+    nb[nb >= keep] = 0
+    q0 = seeded_dofs(keep, order, 23)
+    ctx = Context(order, device=0, precision=PREC_F16X3)
+    ctx.set_cells(cut["star"], cut["AplusT"], cut["AminusT"], nb, cut["side"], cut["orient"], ft)
+    ctx.set_option(OPT_NB_FORM, 2)
+    ctx.set_option(1, fused)  # SEI_OPT_FUSED_LOCAL
+    ctx.set_dofs(q0)
+    ctx.run("all", dt, 3)
+    ctx.sync()
+    q_gpu = ctx.get_dofs()
+    ctx.close()
+    q_ref = oracle_py.Oracle(order).steps(q0, cut["star"].astype(np.float64), cut["AplusT"].astype(np.float64),
+                                          cut["AminusT"].astype(np.float64), nb, cut["side"], cut["orient"], dt, 3, ft)
+    errs = rel_l2_per_quantity(q_gpu, q_ref)
+    assert max(errs) < 1e-5, errs
