@@ -415,14 +415,19 @@ def dr_measurement(local, steps, order=4, dims=None, plane=3, warm_precision=0, 
     out = {}
     states, early = {}, {}
     k_early = min(20, steps)
-    # with a mixed-precision warm arm, an FP32 warm arm isolates the warm start's effect on the
-    # converged slip rates from that of the arithmetic
-    modes = ("plain", "warm") + (("warm_fp32",) if warm_precision else ())
-    for mode in modes:
-        ctx, n, nf = make(DR_SEED + 1, warm_precision if mode == "warm" else 0)
-        if mode != "plain":
+    # arms: the reference's float64 Newton from the previous slip rate (plain); the network's first
+    # guess alone (warm); the float32 pre-solve alone (refine32); both (warm_refine32).  With a
+    # mixed-precision arm, the FP32-kernel arms isolate the solver's effect from the arithmetic's.
+    arms = {"plain": (False, False, 0), "warm": (True, False, 0), "refine32": (False, True, 0),
+            "warm_refine32": (True, True, 0)}
+    if warm_precision:
+        arms["warm_refine32_mixed"] = (True, True, warm_precision)
+    for mode, (net, r32, prec) in arms.items():
+        ctx, n, nf = make(DR_SEED + 1, prec)
+        if net:
             ctx.mlp_set(params, norm)
             ctx.dr_warm_start(True)
+        ctx.set_option(6, int(r32))  # SEI_OPT_DR_REFINE32
         ctx.dr_reset_counters()
         ctx.run("all_dr", dt, k_early)
         ctx.sync()
@@ -433,6 +438,7 @@ def dr_measurement(local, steps, order=4, dims=None, plane=3, warm_precision=0, 
             ctx.sync()
             ms += ctx.last_run_ms()
         tot, npts, first = ctx.dr_newton_iterations(first=True)
+        it32 = ctx.dr_newton_iterations32()
         states[mode] = np.hypot(ctx.dr_state("slip_rate1"), ctx.dr_state("slip_rate2"))
         ctx.set_profiling(True)
         ctx.run("all_dr", dt, 1)
@@ -443,35 +449,48 @@ def dr_measurement(local, steps, order=4, dims=None, plane=3, warm_precision=0, 
         ctx.close()
         out[mode] = {"ms_per_step": ms / steps, "cell_updates_per_s": n * steps / (ms / 1e3),
                      "face_updates_per_s": nf * steps / (ms / 1e3), "fault_kernel_ms": fault_ms,
-                     "kernel_ms_one_step": step_kernels,
+                     "kernel_ms_one_step": step_kernels, "network_guess": net, "float32_presolve": r32,
                      "newton_iters_per_point_step": tot / (npts * steps),
-                     "first_solve_iters_per_point_step": first / (npts * steps)}
-    same = "warm_fp32" if warm_precision else "warm"
-    vp, vw = states["plain"], states[same]
-    return {"workload": f"elastic order {order}, {n:,}-tet periodic cube {dims[0]}x{dims[1]}x{dims[2]} cubes "
-                        f"(material +-{round(100 * perturb)}%), planar fault of {nf:,} faces x {(order + 1) ** 2} "
-                        "points, FVW rate-and-state (a ~ U[0.008,0.02], sn ~ U[-120,-40] MPa, tau ~ U[20,75] MPa, "
-                        f"V_init 1e-16), kernel all_dr, {steps} steps from the initial state",
-            "plain_path": "fp32", "warm_path": "f16x3" if warm_precision else "fp32",
-            **({"warm_start_fp32": out["warm_fp32"],
-                "mixed_warm_vs_plain_speedup": out["plain"]["ms_per_step"] / out["warm"]["ms_per_step"],
-                "max_rel_dV_mixed_warm_vs_plain": float((np.abs(vp - states["warm"]) / np.maximum(vp, 1e-30)).max())}
-               if warm_precision else {}),
-            "cells": n, "faces": nf, "steps": steps, "plain": out["plain"], "warm_start": out["warm"],
-            "first_solve_iteration_ratio": out["plain"]["first_solve_iters_per_point_step"]
-            / max(out["warm"]["first_solve_iters_per_point_step"], 1e-30),
-            "total_iteration_ratio": out["plain"]["newton_iters_per_point_step"]
-            / max(out["warm"]["newton_iters_per_point_step"], 1e-30),
-            "max_abs_dV": float(np.abs(vp - vw).max()),
-            "max_rel_dV": float((np.abs(vp - vw) / np.maximum(vp, 1e-30)).max()),
-            f"max_rel_dV_after_{k_early}_steps": float((np.abs(early["plain"] - early[same])
-                                                         / np.maximum(early["plain"], 1e-30)).max()),
-            "dV_between": f"plain and {same} (same arithmetic)",
-            "dV_note": "plain and warm-started runs are separate trajectories: every solve converges to the "
-                       "Newton tolerance, and the tolerance-level differences feed back through the wave field "
-                       "over the run",
-            "training": {"samples": nsamp, "adam_steps": 1500, "loss_first": loss0, "loss_last": loss1,
-                         "seconds_incl_recording": train_s}}
+                     "first_solve_iters_per_point_step": first / (npts * steps),
+                     "float32_iters_per_point_step": it32 / (npts * steps)}
+    head = "warm_refine32"
+    vp, vw = states["plain"], states[head]
+
+    def ratio(a, b, key):
+        return out[a][key] / max(out[b][key], 1e-30)
+
+    res = {"workload": f"elastic order {order}, {n:,}-tet periodic cube {dims[0]}x{dims[1]}x{dims[2]} cubes "
+                       f"(material +-{round(100 * perturb)}%), planar fault of {nf:,} faces x {(order + 1) ** 2} "
+                       "points, FVW rate-and-state (a ~ U[0.008,0.02], sn ~ U[-120,-40] MPa, tau ~ U[20,75] MPa, "
+                       f"V_init 1e-16), kernel all_dr, {steps} steps from the initial state",
+           "cells": n, "faces": nf, "steps": steps, "arms": out,
+           "plain": out["plain"], "warm_start": out[head],
+           "warm_start_arm": "network first guess + float32 pre-solve, float64 Newton polish (FP32 kernels)",
+           "newton_iters_note": "newton_iters are the float64 Newton iterations of the reference's solver "
+                                "(tolerance unchanged); float32_iters are the pre-solve's iterations on ln V",
+           "float64_iteration_ratio": ratio("plain", head, "newton_iters_per_point_step"),
+           "first_solve_float64_iteration_ratio": ratio("plain", head, "first_solve_iters_per_point_step"),
+           "network_alone_iteration_ratio": ratio("plain", "warm", "newton_iters_per_point_step"),
+           "network_first_solve_iteration_ratio": ratio("plain", "warm", "first_solve_iters_per_point_step"),
+           "network_float32_iteration_ratio": ratio("refine32", head, "float32_iters_per_point_step"),
+           "wall_speedup_vs_plain": ratio("plain", head, "ms_per_step"),
+           "wall_speedup_network_alone": ratio("plain", "warm", "ms_per_step"),
+           "wall_speedup_refine32_alone": ratio("plain", "refine32", "ms_per_step"),
+           "max_abs_dV": float(np.abs(vp - vw).max()),
+           "max_rel_dV": float((np.abs(vp - vw) / np.maximum(vp, 1e-30)).max()),
+           f"max_rel_dV_after_{k_early}_steps": float((np.abs(early["plain"] - early[head])
+                                                        / np.maximum(early["plain"], 1e-30)).max()),
+           "dV_between": f"plain and {head} (same arithmetic)",
+           "dV_note": "plain and warm-started runs are separate trajectories: every solve converges to the "
+                      "Newton tolerance, and the tolerance-level differences feed back through the wave field "
+                      "over the run; tests/test_gpu_mlp.py pins the per-solve identity from one shared state",
+           "training": {"samples": nsamp, "adam_steps": 1500, "loss_first": loss0, "loss_last": loss1,
+                        "seconds_incl_recording": train_s}}
+    if warm_precision:
+        res["mixed_warm_vs_plain_speedup"] = ratio("plain", "warm_refine32_mixed", "ms_per_step")
+        res["max_rel_dV_mixed_warm_vs_plain"] = float((np.abs(vp - states["warm_refine32_mixed"])
+                                                       / np.maximum(vp, 1e-30)).max())
+    return res
 
 
 def lts_fault_measurement(local, cycles):
@@ -512,11 +531,13 @@ def lts_fault_measurement(local, cycles):
     tr.close()
     train_s = time.perf_counter() - t0
     out, states = {}, {}
-    for mode in ("plain", "warm"):
+    arms = {"plain": (False, False), "warm": (True, False), "warm_refine32": (True, True)}
+    for mode, (net, r32) in arms.items():
         ctx, n, nf, ncl = make(DR_SEED + 1)
-        if mode == "warm":
+        if net:
             ctx.mlp_set(params, norm)
             ctx.dr_warm_start(True)
+        ctx.set_option(6, int(r32))  # SEI_OPT_DR_REFINE32
         start, dts = ctx.lts_clusters()
         sizes = np.diff(start)
         faces = ctx.dr_faces()
@@ -529,6 +550,7 @@ def lts_fault_measurement(local, cycles):
         ctx.sync()
         ms = ctx.last_run_ms()
         tot, npts, first = ctx.dr_newton_iterations(first=True)
+        it32 = ctx.dr_newton_iterations32()
         states[mode] = np.hypot(ctx.dr_state("slip_rate1"), ctx.dr_state("slip_rate2"))
         ctx.close()
         upd = int(sum(int(sz) * (1 << (ncl - 1 - k)) for k, sz in enumerate(sizes)))  # cell updates per cycle
@@ -537,18 +559,26 @@ def lts_fault_measurement(local, cycles):
                      "face_updates_per_s": dr_steps * cycles / (ms / 1e3),
                      "simulated_s_per_wall_s": float(dts[-1]) * cycles / (ms / 1e3),
                      "newton_iters_per_point_face_step": tot / max(npts / nf * dr_steps * cycles, 1),
-                     "first_solve_iters_per_point_face_step": first / max(npts / nf * dr_steps * cycles, 1)}
-    vp, vw = states["plain"], states["warm"]
+                     "first_solve_iters_per_point_face_step": first / max(npts / nf * dr_steps * cycles, 1),
+                     "float32_iters_per_point_face_step": it32 / max(npts / nf * dr_steps * cycles, 1),
+                     "network_guess": net, "float32_presolve": r32}
+    head = "warm_refine32"
+    vp, vw = states["plain"], states[head]
     return {"workload": f"elastic order 6, {n:,}-tet graded periodic cube 8x100x250 cubes (edges log-uniform in "
                         f"[50, 400] m, material +-10%), planar fault of {nf:,} faces x 49 points (FVW), "
                         f"{ncl} rate-2 clusters, {cycles} LTS cycles, FP32 kernels (LTS), graph replay",
             "cells": n, "faces": nf, "clusters": ncl, "cells_per_cluster": [int(v) for v in sizes],
             "faces_per_cluster": [int(v) for v in fcl], "cluster_dt": [float(v) for v in dts], "cycles": cycles,
-            "plain": out["plain"], "warm_start": out["warm"],
-            "first_solve_iteration_ratio": out["plain"]["first_solve_iters_per_point_face_step"]
-            / max(out["warm"]["first_solve_iters_per_point_face_step"], 1e-30),
-            "total_iteration_ratio": out["plain"]["newton_iters_per_point_face_step"]
+            "arms": out, "plain": out["plain"], "warm_start": out[head],
+            "warm_start_arm": "network first guess + float32 pre-solve, float64 Newton polish",
+            "float64_iteration_ratio": out["plain"]["newton_iters_per_point_face_step"]
+            / max(out[head]["newton_iters_per_point_face_step"], 1e-30),
+            "first_solve_float64_iteration_ratio": out["plain"]["first_solve_iters_per_point_face_step"]
+            / max(out[head]["first_solve_iters_per_point_face_step"], 1e-30),
+            "network_alone_iteration_ratio": out["plain"]["newton_iters_per_point_face_step"]
             / max(out["warm"]["newton_iters_per_point_face_step"], 1e-30),
+            "wall_speedup_vs_plain": out["plain"]["ms_per_cycle"] / out[head]["ms_per_cycle"],
+            "wall_speedup_network_alone": out["plain"]["ms_per_cycle"] / out["warm"]["ms_per_cycle"],
             "max_rel_dV": float((np.abs(vp - vw) / np.maximum(vp, 1e-30)).max()),
             "training": {"samples": int(len(samples)), "loss_first": loss0, "loss_last": loss1,
                          "seconds_incl_recording": train_s}}

@@ -200,6 +200,14 @@ int sei_evaluate_taylor(sei_ctx* ctx, const double* coeffs, float* out_device);
  * lift rDivM_i (the local integral then computes the volume term and the face traces only;
  * SEI_OPT_TC_LOCAL 0).  The separate local-integral and neighbour calls keep their full meaning. */
 #define SEI_OPT_NB_FORM 5
+/* SEI_OPT_DR_REFINE32: 1 makes every slip-rate solve of the fault kernel first iterate in float32
+ * on ln V from its start (the previous slip rate, or the network's guess on a first solve with
+ * the warm start on) until the step falls below 2e-6, then run the float64 Newton of the
+ * reference from there with the reference's tolerance (it falls back to the plain start if its
+ * residual stops falling), so the converged slip rates are those of the plain solve to within the
+ * Newton tolerance.  No counterpart in the reference; float64 is the scarce pipe of GB300.
+ * 0 (default): the float64 Newton alone. */
+#define SEI_OPT_DR_REFINE32 6
 int sei_set_option(sei_ctx* ctx, int option, int value);
 
 /* Autotuner (no counterpart in the reference, whose kernel shapes are fixed when its code is
@@ -289,6 +297,9 @@ int sei_dr_get_imposed(sei_ctx* ctx, float* plus, float* minus);
  * solves, *first (may be NULL) over the first solve of each time point (the solve a warm start
  * replaces); *solves_points = faces x points. */
 int sei_dr_newton_iterations(sei_ctx* ctx, int64_t* total, int64_t* solves_points, int64_t* first);
+/* Accumulated float32 pre-iterations (SEI_OPT_DR_REFINE32) over all points, solves and steps since
+ * the last reset (the float64 iterations are those of sei_dr_newton_iterations). */
+int sei_dr_newton_iterations32(sei_ctx* ctx, int64_t* total32);
 int sei_dr_reset_counters(sei_ctx* ctx);
 /* Runs only the fault kernel (after a step that stored the derivatives). */
 int sei_dr_faces_step(sei_ctx* ctx, double dt);

@@ -194,6 +194,84 @@ def gen_order(order: int) -> str:
             off += bc * NQ
             a("  }")
 
+    def emit_ck_lowreg():
+        """CK predictor with I parked in the exchange area as its rows become final.
+
+        The exchange keeps q-slabs of kB rows ([q][k][lane]).  Stage i reads rows [0, bp) and
+        leaves rows [bc, bp) untouched, so after it the rows [bc, bp) of I (no later stage adds
+        to them) are written there, each thread into its own column; only the rows still
+        accumulating stay in registers.  dQ(0) is not kept in registers at all: after stage 1,
+        c0 dQ(0) is read back from the exchange.  At the end the slabs hold all of I."""
+        a("""  __shared__ uint64_t sei_mbar;
+  const int cell0 = blockIdx.x * kCPB;
+  const int cnt = n - cell0 < kCPB ? n - cell0 : kCPB;
+  if (threadIdx.x == 0) sei_tc::mbarInit(&sei_mbar, 1);
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    if (lane == 0) sei_tc::mbarExpectTx(&sei_mbar, (unsigned)(cnt * 9 * kBp * 4));
+    __syncwarp();
+    if (lane < cnt) sei_tc::bulkCopyG2S(X + lane * kSt, Q + (size_t)(cell0 + lane) * 9 * kBp, 9 * kBp * 4, &sei_mbar);
+  }
+  if (!sei_tc::mbarWait(&sei_mbar, 0, 1u << 26)) {
+    if (threadIdx.x == 0 && status) atomicExch(status, 1);
+    (void)sei_tc::mbarWait(&sei_mbar, 0, 1u << 26);  // the copies in flight land before X is reused
+  }
+  const int dsl = derivs ? (dslot ? __ldg(dslot + cl) : cl) : -1;
+  float* dbase = (dsl >= 0 && valid) ? derivs + (size_t)dsl * kDerivSize : nullptr;
+  {
+    float z[kBp];
+    const float4* src = reinterpret_cast<const float4*>(X + lane * kSt + q * kBp);
+#pragma unroll
+    for (int k4 = 0; k4 < kBp / 4; ++k4) {
+      const float4 t = src[k4];
+      z[4 * k4] = t.x;
+      z[4 * k4 + 1] = t.y;
+      z[4 * k4 + 2] = t.z;
+      z[4 * k4 + 3] = t.w;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kB; ++k) Xq[k * 32] = z[k];
+    if (dbase) sei_store_col_scalar<kB>(dbase + q * kB, z);
+  }
+  __syncthreads();""")
+        off = B * NQ
+        ireg = 0  # rows of I held in registers (0 before stage 1)
+        for i in range(1, order):
+            bp, bc = nb3(order - i + 1), nb3(order - i)
+            a(f"  // ---- CK stage {i}: rows {bc} from {bp}")
+            a("  {")
+            a(f"    float zn[{bc}];")
+            a(f"#pragma unroll\n    for (int k = 0; k < {bc}; ++k) zn[k] = 0.f;")
+            cols = [_cols(G["kDivMT"][e], bc, bp) for e in range(3)]
+            for l in range(bp):
+                if not any(l in c for c in cols):
+                    continue
+                a(f"    {{ const float x0 = Xs0[{l * 32}], x1 = Xs1[{l * 32}], x2 = Xs2[{l * 32}];")
+                for e in range(3):
+                    if l in cols[e]:
+                        a(f"      const float y{e} = st[{e}][0] * x0 + st[{e}][1] * x1 + st[{e}][2] * x2;")
+                for e in range(3):
+                    for k, v in cols[e].get(l, []):
+                        a(f"      zn[{k}] = fmaf({flit(v)}, y{e}, zn[{k}]);")
+                a("    }")
+            a("    __syncthreads();")
+            if i == 1:
+                # I = c0 dQ(0) + c1 dQ(1) on rows < bc; rows [bc, bp) of I are c0 dQ(0), final
+                a(f"#pragma unroll\n    for (int k = 0; k < {bc}; ++k) I[k] = fmaf(coeffs.c[1], zn[k], coeffs.c[0] * Xq[k * 32]);")
+                a(f"#pragma unroll\n    for (int k = {bc}; k < {bp}; ++k) Xq[k * 32] = coeffs.c[0] * Xq[k * 32];")
+            else:
+                a(f"#pragma unroll\n    for (int k = 0; k < {bc}; ++k) I[k] = fmaf(coeffs.c[{i}], zn[k], I[k]);")
+                a(f"#pragma unroll\n    for (int k = {bc}; k < {bp}; ++k) Xq[k * 32] = I[k];")
+            if i < order - 1:
+                a(f"#pragma unroll\n    for (int k = 0; k < {bc}; ++k) Xq[k * 32] = zn[k];")
+            else:
+                a(f"#pragma unroll\n    for (int k = 0; k < {bc}; ++k) Xq[k * 32] = I[k];")
+            a(f"    if (dbase) sei_store_col_scalar<{bc}>(dbase + {off} + q * {bc}, zn);")
+            off += bc * NQ
+            a("  }")
+            a("  __syncthreads();")
+
     def emit_volume_flux(with_trace=False):
         emit_volume_part()
         emit_flux_part(with_trace)
@@ -308,20 +386,30 @@ sei_local_o{order}(int n, float* __restrict__ Q, float* __restrict__ Iout, const
     a("}")
 
     # ADER alone (Spacetime::computeAder)
+    ader_ctas = int(os.environ.get("SEI_GEN_ADER_CTAS", "3"))
+    lintv_ctas = int(os.environ.get("SEI_GEN_LINTV_CTAS", "2"))
     a(f"""
 // Cauchy-Kovalevskaya predictor alone: I = sum_i coeffs[i] dQ(i) (Q unchanged), optional derivatives.
-// Two CTAs per SM.  The block's 32 cells of Q arrive in shared memory by bulk copies and I leaves
-// the same way (one 16-byte-aligned copy per cell each way), so HBM sees whole contiguous rows
-// instead of every thread's strided column loads; status is set when a copy wait gives up.
-extern "C" __global__ void __launch_bounds__(288, 2)
+// {ader_ctas} CTAs per SM (rows of I that are final wait in shared memory, which keeps the registers
+// low).  The block's 32 cells of Q arrive in shared memory by bulk copies and I leaves the same
+// way (one 16-byte-aligned copy per cell each way), so HBM sees whole contiguous rows instead of
+// every thread's strided column loads; status is set when a copy wait gives up.
+extern "C" __global__ void __launch_bounds__(288, {ader_ctas})
 sei_ader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout, const float* __restrict__ star_nz,
                   SeiCoeffs coeffs, float* __restrict__ derivs, const int* __restrict__ dslot, int* __restrict__ status) {{""" + prologue)
-    emit_ck(staged=True)
-    a("""  // I of the block through X (its last reads ended with the stage barrier), then out by bulk copies
+    a(f"  float I[{nb3(order - 1)}];")
+    emit_ck_lowreg()
+    a("""  // I of the block, complete in the exchange slabs, to the staging layout, then out by bulk copies
   {
+    float Io[kBp];
+#pragma unroll
+    for (int k = 0; k < kB; ++k) Io[k] = Xq[k * 32];
+#pragma unroll
+    for (int k = kB; k < kBp; ++k) Io[k] = 0.f;
+    __syncthreads();
     float4* dst = reinterpret_cast<float4*>(X + lane * kSt + q * kBp);
 #pragma unroll
-    for (int k4 = 0; k4 < kBp / 4; ++k4) dst[k4] = make_float4(I[4 * k4], I[4 * k4 + 1], I[4 * k4 + 2], I[4 * k4 + 3]);
+    for (int k4 = 0; k4 < kBp / 4; ++k4) dst[k4] = make_float4(Io[4 * k4], Io[4 * k4 + 1], Io[4 * k4 + 2], Io[4 * k4 + 3]);
   }
   sei_tc::fenceProxyAsync();
   __syncthreads();
@@ -365,9 +453,9 @@ sei_lint_trace_o{order}(int n, float* __restrict__ Q, const float* __restrict__ 
 // cell stride kTs) and out by one bulk copy per cell; then the volume integral uses it as its
 // exchange, and its contribution, staged there ([cell][q][kBp]), is added to Q in L2 by one
 // bulk f32 reduce-add per cell, so the kernel never reads Q.  The traces before the volume keep
-// either I or the volume accumulator live, not both: two CTAs per SM.  status is set when the
-// copy wait gives up.
-extern "C" __global__ void __launch_bounds__(288, 2)
+// either I or the volume accumulator live, not both: {lintv_ctas} CTAs per SM.  status is set when
+// the copy wait gives up.
+extern "C" __global__ void __launch_bounds__(288, {lintv_ctas})
 sei_lintv_o{order}(int n, float* __restrict__ Q, const float* __restrict__ Iin, const float* __restrict__ star_nz,
                    float* __restrict__ trace, int tplane, int* __restrict__ status) {{""" + prologue)
     a("""  __shared__ uint64_t sei_mbar;

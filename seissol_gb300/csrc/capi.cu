@@ -67,6 +67,7 @@ struct sei_ctx {
   float* d_mlp = nullptr;  // trained warm-start network (nullptr: none)
   float mlp_norm[sei_mlp::kNorm] = {0};
   bool warm_start = false;
+  bool dr_refine32 = false;  // SEI_OPT_DR_REFINE32
   float* d_rec = nullptr;  // recorded training samples [rec_cap][6]
   unsigned* d_rec_count = nullptr;
   unsigned rec_cap = 0;
@@ -405,6 +406,7 @@ sei::DrArgs drArgs(sei_ctx* c, double dt) {
   a.state_tol = r.state_tol;
   a.max_newton = r.max_newton;
   a.max_outer = r.max_outer;
+  a.refine32 = c->dr_refine32 ? 1 : 0;
   // Gauss-Legendre time points on [0, dt] (TimeCluster.cpp:236-241), sub-steps (FrictionSolver.cpp:20-37)
   const int N = c->cfg.order;
   double x[8], w[8];
@@ -779,6 +781,10 @@ int sei_set_option(sei_ctx* c, int option, int value) {
       if (value < 0 || value > 2) return fail(c, SEI_ERR_ARG, "SEI_OPT_NB_FORM takes 0, 1 or 2");
       c->nb_form = value;
       return SEI_OK;
+    case SEI_OPT_DR_REFINE32:
+      c->dr_refine32 = value != 0;
+      dropLtsGraph(c);  // a recorded cycle holds the fault kernel's arguments
+      return SEI_OK;
     default:
       return fail(c, SEI_ERR_ARG, "unknown option");
   }
@@ -999,7 +1005,7 @@ int sei_dr_setup(sei_ctx* c, const sei_rs_params* p, int64_t* nfaces) {
   c->derivs = nullptr;
   bool ok = dalloc((void**)&c->derivs, 2 * nf * dsz) && dalloc((void**)&c->dslot, c->n * 4) &&
             dalloc((void**)&c->d_pc, nf * 4) && dalloc((void**)&c->d_mc, nf * 4) && dalloc((void**)&c->d_pslot, nf * 4) &&
-            dalloc((void**)&c->d_mslot, nf * 4) && dalloc((void**)&c->d_iters, 2 * nf * np * 4) &&
+            dalloc((void**)&c->d_mslot, nf * 4) && dalloc((void**)&c->d_iters, 3 * nf * np * 4) &&
             dalloc((void**)&c->d_ps, nf) && dalloc((void**)&c->d_ms, nf) && dalloc((void**)&c->d_rel, nf) &&
             dalloc((void**)&c->d_tinvt, nf * 81 * 4) && dalloc((void**)&c->d_fsp, nf * 81 * 4) &&
             dalloc((void**)&c->d_fsm, nf * 81 * 4) && dalloc((void**)&c->d_isp, nf * 9 * np * 4) &&
@@ -1023,7 +1029,7 @@ int sei_dr_setup(sei_ctx* c, const sei_rs_params* p, int64_t* nfaces) {
   SEI_CUDA(cudaMemcpy(c->d_fsm, F.fsm.data(), nf * 81 * 4, cudaMemcpyHostToDevice));
   SEI_CUDA(cudaMemcpy(c->d_imp, F.imp.data(), nf * 8 * 8, cudaMemcpyHostToDevice));
   SEI_CUDA(cudaMemcpy(c->d_state, st.data(), st.size() * 8, cudaMemcpyHostToDevice));
-  SEI_CUDA(cudaMemset(c->d_iters, 0, 2 * nf * np * 4));
+  SEI_CUDA(cudaMemset(c->d_iters, 0, 3 * nf * np * 4));
   SEI_CUDA(cudaMemset(c->d_isp, 0, nf * 9 * np * 4));
   SEI_CUDA(cudaMemset(c->d_ism, 0, nf * 9 * np * 4));
   SEI_CUDA(cudaMemset(c->derivs, 0, 2 * nf * dsz));
@@ -1109,10 +1115,23 @@ int sei_dr_newton_iterations(sei_ctx* c, int64_t* total, int64_t* points, int64_
   return SEI_OK;
 }
 
+int sei_dr_newton_iterations32(sei_ctx* c, int64_t* total32) {
+  if (!c || !total32) return SEI_ERR_ARG;
+  if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up");
+  const size_t np = (size_t)c->fault.nf * c->npts;
+  std::vector<int32_t> it(np);
+  SEI_CUDA(cudaMemcpyAsync(it.data(), c->d_iters + 2 * np, np * 4, cudaMemcpyDeviceToHost, c->stream));
+  SEI_CUDA(cudaStreamSynchronize(c->stream));
+  int64_t s = 0;
+  for (size_t i = 0; i < np; ++i) s += it[i];
+  *total32 = s;
+  return SEI_OK;
+}
+
 int sei_dr_reset_counters(sei_ctx* c) {
   if (!c) return SEI_ERR_ARG;
   if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up");
-  SEI_CUDA(cudaMemsetAsync(c->d_iters, 0, 2 * (size_t)c->fault.nf * c->npts * 4, c->stream));
+  SEI_CUDA(cudaMemsetAsync(c->d_iters, 0, 3 * (size_t)c->fault.nf * c->npts * 4, c->stream));
   return SEI_OK;
 }
 

@@ -18,8 +18,11 @@
 // An optional small network (5 -> 64 -> 64 -> 1, tanh) proposes the starting slip rate of the
 // first Newton solve of every time point: it is used when its residual is below that of the
 // plain start (previous slip rate), and the plain solve runs whenever the residual from the
-// network's start stops falling.  Optionally the converged first solves of the plain method
-// are recorded as training samples (normal stress, shear, state, a, b, log10 V).
+// network's start stops falling.  Optionally (refine32) every solve first iterates in float32 on
+// the log slip rate from its start (a few cheap iterations that reach ~1e-6 relative accuracy)
+// and the float64 Newton of the reference then only polishes; float64 is the scarce pipe of this
+// part.  Optionally the converged first solves of the plain method are recorded as training
+// samples (normal stress, shear, state, a, b, log10 V).
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -34,27 +37,12 @@ namespace {
 constexpr int kHidden = sei_mlp::kHidden;
 constexpr int kMlpParams = kHidden * 5 + kHidden + kHidden * kHidden + kHidden + kHidden + 1;
 constexpr double kAlmostZero = 1e-45;
-// range of the network's guess, natural log of m/s (1e-45 .. 1e3)
-constexpr double kLnGuessMin = -103.616329;
-constexpr double kLnGuessMax = 6.907755;
 
-__device__ __forceinline__ double cexpOf(double l) { return l > 0 ? exp(-l) : exp(l); }
 
 __device__ __forceinline__ bool largeBranch(double x, double explog) {
   int xexp = 0;
   (void)frexp(x, &xexp);
   return explog + (xexp > 0 ? xexp : 0) * 0.69314718055994530943 > 10.0 || explog >= 50.0;
-}
-
-// asinh(x * exp(explog)) with the large-argument form of RateAndStateCommon.h:46-74.
-__device__ __forceinline__ double arsinhexp(double x, double explog, double e) {
-  if (largeBranch(x, explog)) {
-    if (explog <= 0) e = 1 / e;
-    const double xa = fabs(x);
-    return (x >= 0 ? 1.0 : -1.0) * (explog + log(xa + sqrt(xa * xa + e * e)));
-  }
-  if (explog > 0) e = 1 / e;
-  return asinh(e * x);
 }
 
 // Natural log of a positive normal double, in float precision, without an FP64 transcendental:
@@ -64,6 +52,31 @@ __device__ __forceinline__ float lnPos(double v) {
   const int e = (int)((bits >> 52) & 0x7FF) - 1023;
   const double m = __longlong_as_double((bits & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL);
   return (float)e * 0.6931471806f + logf((float)m);
+}
+
+// asinh(x * exp(explog)) with the large-argument form of RateAndStateCommon.h:46-74 (the
+// reference passes e = exp(-|explog|), inverted where its branch needs; it is formed here only
+// where it is used).  When e < 2^-28 |x| (the usual case: e = exp(-psi / a) is tiny), the rounded
+// e^2 is below a quarter ulp of the rounded x^2, so their sum rounds to x^2, whose correctly
+// rounded square root is |x| exactly: the float64 square root is skipped with a bit-identical
+// result.  A float test in log space with half an e-fold of margin finds that case without the
+// float64 exponential; only the cases it cannot decide form e.
+__device__ __forceinline__ double arsinhexp(double x, double explog) {
+  if (largeBranch(x, explog)) {
+    const double xa = fabs(x);
+    double s;
+    if (explog > 0 && xa > 0 && (float)(-explog) < lnPos(xa) - 19.9084f) {  // 28 ln 2 + 0.5
+      s = xa + xa;
+    } else {
+      double e = exp(-fabs(explog));
+      if (explog <= 0) e = 1 / e;
+      s = e < 3.7252902984619140625e-9 * xa ? xa + xa : xa + sqrt(xa * xa + e * e);
+    }
+    return (x >= 0 ? 1.0 : -1.0) * (explog + log(s));
+  }
+  double e = exp(-fabs(explog));
+  if (explog > 0) e = 1 / e;
+  return asinh(e * x);
 }
 
 // State variable after a sub-step of length dt at slip rate v (RateAndState FVW law).  The
@@ -116,12 +129,6 @@ __device__ __forceinline__ double newtonDelta(double g, double v, float lnScale,
   return g * m * p2;
 }
 
-__device__ __forceinline__ double residual(const sei::DrArgs& A, double a, double psi, double sn, double tau,
-                                           double invEtaS, double v) {
-  const double cl = psi / a;
-  return -invEtaS * (fabs(sn) * a * arsinhexp(0.5 / A.v0 * v, cl, cexpOf(cl)) - tau) - v;
-}
-
 struct NewtonOut {
   double v, mu;
   int iters;
@@ -129,16 +136,15 @@ struct NewtonOut {
 };
 
 // Newton on g(V) = -(|sn| mu(V) - tau) / eta_s - V from v; stops early when |g| grows if bail.
-__device__ NewtonOut newton(const sei::DrArgs& A, double a, double psi, double sn, double tau, double invEtaS,
-                            double v, bool bail) {
-  const double clin = 0.5 / A.v0;
-  const double cl = psi / a;
-  const double ce = cexpOf(cl);
+__device__ NewtonOut newton(const sei::DrArgs& A, const LawInv& inv, double a, double inva, double psi, double sn,
+                            double tau, double invEtaS, double v, bool bail) {
+  const double clin = 0.5 * inv.v0;
+  const double cl = psi * inva;
   const float lnScale = (float)cl - lnPos(2.0 * A.v0);
   const float lnSna = logf((float)(invEtaS * fabs(sn) * a));
   double prev = 1e300;
   for (int i = 0; i < A.max_newton; ++i) {
-    const double mu = a * arsinhexp(clin * v, cl, ce);
+    const double mu = a * arsinhexp(clin * v, cl);
     const double g = -invEtaS * (fabs(sn) * mu - tau) - v;
     if (fabs(g) < A.newton_tol) return {v, mu, i, true};
     if (bail && !(fabs(g) < prev)) return {v, 0.0, i, false};
@@ -149,37 +155,95 @@ __device__ NewtonOut newton(const sei::DrArgs& A, double a, double psi, double s
   return {v, 0.0, A.max_newton, false};
 }
 
-// Network guess of the natural log of the converged slip rate (feature and output maps of mlp.cuh).
-__device__ double mlpGuess(const float* __restrict__ w, const float* nrm, double sn, double tau, double psi, double a,
-                           double b) {
-  double f[5];
-  sei_mlp::features(sn, tau, psi, a, b, f);
+// ---- float32 solve on u = ln V.  h(u) = |sn| a asinh(e^(u + lnScale)) + eta_s e^u - tau is -eta_s
+// times the residual g and increasing and convex in u, so Newton converges from either side once
+// it is right of the root.  asinh(y) = ln(2 y) beyond y = e^9 (error below 4e-9) and y below
+// y = e^-9 (relative error below 3e-9).
+struct Solve32 {
+  float an, etas, tau, lnScale;  // |sn| a, eta_s, tau, psi / a - ln(2 V0)
+};
+__device__ __forceinline__ float h32(const Solve32& S, float u, float* dh) {
+  const float ly = u + S.lnScale;
+  float ash, dash;  // asinh(y), y / sqrt(1 + y^2)
+  if (ly > 9.f) {
+    ash = ly + 0.6931471806f;
+    dash = 1.f;
+  } else if (ly < -9.f) {
+    ash = dash = expf(ly);
+  } else {
+    const float y = expf(ly);
+    const float r = sqrtf(fmaf(y, y, 1.f));
+    ash = asinhf(y);
+    dash = y / r;
+  }
+  const float ev = expf(u);
+  if (dh) *dh = fmaf(S.an, dash, S.etas * ev);
+  return fmaf(S.an, ash, fmaf(S.etas, ev, -S.tau));
+}
+// range of a start of the float64 solve, natural log of m/s (1e-45 .. 1e3)
+constexpr float kLnGuessMinF = -103.616329f, kLnGuessMaxF = 6.907755f;
+__device__ __forceinline__ float newton32(const Solve32& S, float u, int& its) {
+  its = 0;
+#pragma unroll 1
+  for (int i = 0; i < 16; ++i) {
+    float dh;
+    const float h = h32(S, u, &dh);
+    const float du = h / dh;
+    u = fminf(fmaxf(u - du, kLnGuessMinF), kLnGuessMaxF);
+    its = i + 1;
+    // a step at the float resolution of u (h carries a few ulp of tau): converged; also leaves on NaN
+    if (!(fabsf(du) > 1e-6f + 3e-7f * fabsf(u))) break;
+  }
+  return u;
+}
+// e^u as a double from float arithmetic: 2^k m with integer k and m = 2^(w - k) in [1, 2).
+__device__ __forceinline__ double expToDouble(float u) {
+  const float w = u * 1.4426950409f;
+  const float kf = floorf(w);
+  const double m = (double)exp2f(w - kf);
+  return m * __longlong_as_double((long long)((int)kf + 1023) << 52);
+}
+
+__device__ __forceinline__ float tanhApprox(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// Network guess of ln V in float arithmetic: the features and output map of mlp.cuh evaluated in
+// float (the training side uses float64; the guess only seeds a solve), tanh.approx activations.
+__device__ float mlpGuess32(const float* __restrict__ w, const float* nrm, float sn, float tau, float psi, float a,
+                            float b) {
+  float an = fabsf(sn) * a;
+  an = an > 1.f ? an : 1.f;
+  const float f[5] = {tau / an, psi / a, logf(an), a, b};
   float x[5];
 #pragma unroll
-  for (int i = 0; i < 5; ++i) x[i] = (float)((f[i] - nrm[i]) * nrm[5 + i]);
+  for (int i = 0; i < 5; ++i) x[i] = (f[i] - nrm[i]) * nrm[5 + i];
   const float* W1 = w;
   const float* b1 = W1 + kHidden * 5;
   const float* W2 = b1 + kHidden;
   const float* b2 = W2 + kHidden * kHidden;
   const float* W3 = b2 + kHidden;
-  const float b3 = W3[kHidden];
   float h1[kHidden];
 #pragma unroll 8
   for (int j = 0; j < kHidden; ++j) {
     float s = b1[j];
 #pragma unroll
     for (int i = 0; i < 5; ++i) s = fmaf(W1[j * 5 + i], x[i], s);
-    h1[j] = tanhf(s);
+    h1[j] = tanhApprox(s);
   }
-  float out = b3;
+  float out = W3[kHidden];
 #pragma unroll 4
   for (int j = 0; j < kHidden; ++j) {
     float s = b2[j];
 #pragma unroll
     for (int i = 0; i < kHidden; ++i) s = fmaf(W2[j * kHidden + i], h1[i], s);
-    out = fmaf(W3[j], tanhf(s), out);
+    out = fmaf(W3[j], tanhApprox(s), out);
   }
-  return sei_mlp::lnSlipRate(f, nrm[12], (double)out * nrm[11] + nrm[10]);
+  const float z = f[0] - f[1] - f[2];
+  const float base = z > 30.f ? z : log1pf(expf(z));
+  return nrm[12] + f[0] - f[1] - base - (out * nrm[11] + nrm[10]);
 }
 
 // Threads of one face (a multiple of the warp size covering the face points), faces per block.
@@ -281,6 +345,7 @@ __global__ void __launch_bounds__(128, 3)
   // reciprocal impedances, once per thread: FP64 divisions are costly on this part
   const double rzp = 1.0 / imp[0], rzs = 1.0 / imp[1], rzpn = 1.0 / imp[2], rzsn = 1.0 / imp[3];
   const double a = pt ? A.a[po] : 0.01;
+  const double inva = 1.0 / a;  // psi / a as psi * inva: one float64 division per thread, not per solve
   const size_t plane = (size_t)A.nfaces * NP;  // init holds sn0, tau1_0, tau2_0 as [3][nf][npts]
   const double sn0 = pt ? A.init[po] : 0.0;
   const double t10 = pt ? A.init[plane + po] : 0.0;
@@ -290,7 +355,7 @@ __global__ void __launch_bounds__(128, 3)
   double v1 = pt ? A.v1[po] : 1.0, v2 = pt ? A.v2[po] : 0.0;
   double slip1 = pt ? A.slip1[po] : 0.0, slip2 = pt ? A.slip2[po] : 0.0, slip = pt ? A.slip[po] : 0.0;
   double mu = 0.0, tr1 = 0.0, tr2 = 0.0;
-  int iters = 0, firstIters = 0;
+  int iters = 0, firstIters = 0, iters32 = 0;
   const LawInv inv{1.0 / A.v0, 1.0 / A.vw, 1.0 / A.l};
   double isP[6] = {0, 0, 0, 0, 0, 0}, isM[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll 1
@@ -317,18 +382,33 @@ __global__ void __launch_bounds__(128, 3)
         psib = stateUpdate(A, inv, a, sref, dt, lsr);
         NewtonOut r{};
         bool done = false;
-        if (useMlp && j == 0 && sei_mlp::usable(sn, tau, a)) {
-          // start from the network's guess when its residual is below the plain start's
-          const double lg = mlpGuess(sW, A.mlp_norm, sn, tau, psib, a, A.b);
-          const double g0 = exp(fmin(fmax(lg, kLnGuessMin), kLnGuessMax));
-          if (fabs(residual(A, a, psib, sn, tau, invEtaS, g0)) < fabs(residual(A, a, psib, sn, tau, invEtaS, vmag))) {
-            r = newton(A, a, psib, sn, tau, invEtaS, g0, true);
-            firstIters += r.iters;
+        const bool net = useMlp && j == 0 && sei_mlp::usable(sn, tau, a);
+        if (net || A.refine32) {
+          const Solve32 S{(float)(fabs(sn) * a), (float)etas, (float)tau, (float)(psib * inva) - lnPos(2.0 * A.v0)};
+          const float u0 = lnPos(vmag);
+          float u = u0;
+          if (net) {
+            // start from the network's guess when its residual is below the plain start's
+            // (float32 residuals: the comparison only picks a start)
+            const float lg = mlpGuess32(sW, A.mlp_norm, (float)sn, (float)tau, (float)psib, (float)a, (float)A.b);
+            const float ug = fminf(fmaxf(lg, kLnGuessMinF), kLnGuessMaxF);
+            if (fabsf(h32(S, ug, nullptr)) < fabsf(h32(S, u, nullptr))) u = ug;
+          }
+          if (A.refine32) {
+            int its = 0;
+            u = newton32(S, u, its);
+            iters32 += its;
+          }
+          // a start that float arithmetic cannot tell from the previous slip rate is not taken: the
+          // previous rate is often the float64 root already (no iteration at all)
+          if (!(fabsf(u - u0) <= 2e-6f + 6e-7f * fabsf(u0))) {
+            r = newton(A, inv, a, inva, psib, sn, tau, invEtaS, expToDouble(u), true);
+            (j == 0 ? firstIters : iters) += r.iters;
             done = r.conv;
           }
         }
         if (!done) {
-          r = newton(A, a, psib, sn, tau, invEtaS, vmag, false);
+          r = newton(A, inv, a, inva, psib, sn, tau, invEtaS, vmag, false);
           (j == 0 ? firstIters : iters) += r.iters;
           if (A.rec && j == 0 && r.conv && sei_mlp::usable(sn, tau, a)) {
             const unsigned idx = atomicAdd(A.rec_count, 1u);
@@ -352,8 +432,8 @@ __global__ void __launch_bounds__(128, 3)
     }
     if (pt) {
       psib = stateUpdate(A, inv, a, sref, dt, lsr);
-      const double clin = 0.5 / A.v0, cl = psib / a;
-      mu = a * arsinhexp(clin * vmag, cl, cexpOf(cl));
+      const double clin = 0.5 * inv.v0, cl = psib * inva;
+      mu = a * arsinhexp(clin * vmag, cl);
       const double strength = -mu * sn;
       slip += vmag * dt;
       const double div = strength + etas * vmag;
@@ -397,6 +477,7 @@ __global__ void __launch_bounds__(128, 3)
     A.trac2[po] = tr2;
     A.newton_iters[po] += iters + firstIters;
     A.newton_iters[(size_t)A.nfaces * NP + po] += firstIters;
+    A.newton_iters[2 * (size_t)A.nfaces * NP + po] += iters32;
   }
 
   // ---- 4./5. imposed states and nodal flux, plus side then minus side

@@ -153,10 +153,12 @@ struct DrArgs {
   double *psi, *v1, *v2, *slip1, *slip2, *slip, *mu, *trac1, *trac2;  // [nf][npts]
   float* isp;  // imposed states [nf][9][npts]
   float* ism;
-  int32_t* newton_iters;  // [2][nf][npts], accumulated: all solves, first solve of each time point
+  int32_t* newton_iters;  // [3][nf][npts], accumulated: float64 iterations of all solves, of the first
+                          // solve of each time point, float32 pre-iterations of all solves
   float* Q;               // DOFs [n][9][Bp] (nodal flux target)
   double f0, b, v0, l, muw, vw, newton_tol, state_tol;
   int max_newton, max_outer;
+  int refine32;         // 1: every solve iterates in float32 (log slip rate) before the float64 Newton
   double deltat[8], tweights[8];
   float coll[8][8];     // collocation coefficients t_s^p / p! of the time points
   const float* mlp;     // warm-start network parameters (nullptr: plain Newton)

@@ -129,6 +129,7 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_dr_set_state", i, [VP, i, VP])
     _sig(lib, "sei_dr_get_imposed", i, [VP, VP, VP])
     _sig(lib, "sei_dr_newton_iterations", i, [VP, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)])
+    _sig(lib, "sei_dr_newton_iterations32", i, [VP, C.POINTER(i64)])
     _sig(lib, "sei_dr_reset_counters", i, [VP])
     _sig(lib, "sei_dr_faces_step", i, [VP, d])
     _sig(lib, "sei_dr_get_slots", i, [VP, VP])
@@ -435,6 +436,12 @@ class Context:
         self._check(self.lib.sei_dr_newton_iterations(self.h, C.byref(t), C.byref(n), C.byref(f)),
                     "sei_dr_newton_iterations")
         return (t.value, n.value, f.value) if first else (t.value, n.value)
+
+    def dr_newton_iterations32(self):
+        """Float32 pre-iterations of all solves (SEI_OPT_DR_REFINE32) since the last reset."""
+        t = C.c_int64()
+        self._check(self.lib.sei_dr_newton_iterations32(self.h, C.byref(t)), "sei_dr_newton_iterations32")
+        return t.value
 
     def dr_reset_counters(self):
         self._check(self.lib.sei_dr_reset_counters(self.h), "sei_dr_reset_counters")

@@ -148,10 +148,86 @@ def test_warm_step_matches_oracle(built_lib, trained):
     q_gpu = ctx.get_dofs()
     for q in range(9):
         assert rel_l2(q_gpu[:, q] - q0[:, q], q_ref[:, q] - q0[:, q]) < 1e-4, q
+    # the kernel evaluates the network and the start comparison in float32 (tanh.approx), the
+    # oracle in float64: a start can flip where the two residuals are close
     tot, _, fst = ctx.dr_newton_iterations(first=True)
-    assert abs(fst - first.sum()) <= 0.05 * first.sum() + 5, (fst, first.sum())
-    assert abs(tot - iters.sum()) <= 0.05 * iters.sum() + 5, (tot, iters.sum())
+    assert abs(fst - first.sum()) <= 0.1 * first.sum() + 5, (fst, first.sum())
+    assert abs(tot - iters.sum()) <= 0.1 * iters.sum() + 5, (tot, iters.sum())
     ctx.close()
+
+
+OPT_DR_REFINE32 = 6
+STATE_FIELDS = ("psi", "slip_rate1", "slip_rate2", "slip1", "slip2", "slip", "mu", "traction1", "traction2")
+
+
+def _same_solution(a, b):
+    va = np.hypot(a.dr_state("slip_rate1"), a.dr_state("slip_rate2"))
+    vb = np.hypot(b.dr_state("slip_rate1"), b.dr_state("slip_rate2"))
+    assert (np.abs(va - vb) <= 1e-6 * va + 1e-12).all(), np.max(np.abs(va - vb) / (va + 1e-30))
+    assert np.abs(a.dr_state("psi") - b.dr_state("psi")).max() < 1e-9
+    qa, qb = a.get_dofs(), b.get_dofs()
+    assert np.abs(qa - qb).max() <= 1e-6 * np.abs(qa).max()
+
+
+@pytest.mark.parametrize("warm", [False, True])
+def test_float32_presolve_keeps_the_solution(built_lib, trained, warm):
+    """SEI_OPT_DR_REFINE32 (with and without the network's first guess): six steps give the plain
+    solve's slip rates, state and DOFs to the Newton tolerance, with fewer float64 Newton
+    iterations (the measured ratio over 200 steps of the fault workload is in the benchmark)."""
+    _, _, _, p, norm = trained
+    plain, _ = _fault(4)
+    ref, _ = _fault(4)
+    ref.set_option(OPT_DR_REFINE32, 1)
+    if warm:
+        ref.mlp_set(p, norm)
+        ref.dr_warm_start(True)
+    dt = plain.cfl_timestep(0.5)
+    for ctx in (plain, ref):
+        ctx.dr_reset_counters()
+        ctx.run("all_dr", dt, 6)
+        ctx.sync()
+    tot_p, npts = plain.dr_newton_iterations()
+    tot_r, _ = ref.dr_newton_iterations()
+    it32 = ref.dr_newton_iterations32()
+    print(f"float64 Newton iterations per point and step over 6 steps x {npts} points: plain {tot_p / npts / 6:.2f}, "
+          f"refined {tot_r / npts / 6:.2f} (+{it32 / npts / 6:.2f} float32); ratio {tot_p / max(tot_r, 1):.2f}")
+    assert plain.dr_newton_iterations32() == 0 and it32 > 0
+    assert tot_r < tot_p
+    _same_solution(plain, ref)
+    plain.close()
+    ref.close()
+
+
+def test_late_step_warm_and_plain_solves_agree(built_lib, trained):
+    """One state taken after 100 plain steps; the next step solved plain and warm-started (network
+    guess and float32 pre-solve) from that same state agrees point by point: the warm start
+    changes where each solve begins, not what it converges to."""
+    _, _, _, p, norm = trained
+    ctx, _ = _fault(4)
+    dt = ctx.cfl_timestep(0.5)
+    ctx.run("all_dr", dt, 100)
+    ctx.sync()
+    q100 = ctx.get_dofs()
+    s100 = {f: ctx.dr_state(f) for f in STATE_FIELDS}
+    assert np.hypot(s100["slip_rate1"], s100["slip_rate2"]).max() > 1e-6  # the fault is slipping
+    other, _ = _fault(4)
+    other.set_dofs(q100)
+    for f, v in s100.items():
+        other.dr_set_state(f, v)
+    other.mlp_set(p, norm)
+    other.dr_warm_start(True)
+    other.set_option(OPT_DR_REFINE32, 1)
+    for c in (ctx, other):
+        c.dr_reset_counters()
+        c.run("all_dr", dt, 1)
+        c.sync()
+    tot_p, npts, first_p = ctx.dr_newton_iterations(first=True)
+    tot_w, _, first_w = other.dr_newton_iterations(first=True)
+    print(f"step 101, {npts} points: float64 Newton iterations plain {tot_p} (first solves {first_p}), "
+          f"warm {tot_w} (first solves {first_w}, +{other.dr_newton_iterations32()} float32)")
+    _same_solution(ctx, other)
+    ctx.close()
+    other.close()
 
 
 def test_warm_start_needs_a_network(built_lib):
