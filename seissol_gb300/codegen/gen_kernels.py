@@ -575,6 +575,32 @@ sei_neighbor_o{order}(int n, float* __restrict__ Q, const float* __restrict__ I,
     a("  if (valid) sei_store_col<kBp>(Q + ((size_t)cell * 9 + q) * kBp, acc);")
     a("}")
 
+    # ---------------- face traces of listed pool blocks (local time stepping) ----------------
+    a(f"""
+// Face traces fMrT_f I of the pool blocks blk[e], e < m, into trace[4][tplane][9][kFP] (zero padded):
+// under local time stepping the half-step integrals a finer neighbour reads (their faces' traces
+// feed the tensor-core neighbour kernel).  One thread per (entry, quantity).
+extern "C" __global__ void __launch_bounds__(256)
+sei_trace_blocks_o{order}(int m, const int* __restrict__ blk, const float* __restrict__ pool, float* __restrict__ trace,
+                          int tplane) {{
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)m * 9) return;
+  const long e = t / 9;
+  const int q = (int)(t % 9);
+  const int b = __ldg(blk + e);
+  float I[kBp];
+  sei_load_col<kBp>(pool + ((size_t)b * 9 + q) * kBp, I);""")
+    for f in range(4):
+        a("  {")
+        a("    float T[kF];")
+        _matvec(L, "    ", G["fMrT"][f], "I", "T", F, B, True)
+        a(f"    float4* o = reinterpret_cast<float4*>(trace + (((size_t){f} * tplane + b) * 9 + q) * kFP);")
+        a("#pragma unroll\n    for (int m4 = 0; m4 < kFP / 4; ++m4)")
+        a("      o[m4] = make_float4(4 * m4 < kF ? T[4 * m4 < kF ? 4 * m4 : 0] : 0.f, 4 * m4 + 1 < kF ? T[4 * m4 + 1 < kF ? 4 * m4 + 1 : 0] : 0.f,")
+        a("                          4 * m4 + 2 < kF ? T[4 * m4 + 2 < kF ? 4 * m4 + 2 : 0] : 0.f, 4 * m4 + 3 < kF ? T[4 * m4 + 3 < kF ? 4 * m4 + 3 : 0] : 0.f);")
+        a("  }")
+    a("}")
+
     # ---------------- Taylor evaluation ----------------
     a(f"""
 // out[n][9][B] = sum_i coeffs[i] dQ(i) from packed derivatives [n][kDerivSize]; one thread per (cell, q).

@@ -97,6 +97,8 @@ struct sei_ctx {
   double lts_dt0 = 0.0;
   std::vector<int64_t> cl_start, b_start, g_start;  // [ncl + 1] each
   std::vector<int64_t> lts_perm;                    // new cell -> cell before sei_lts_setup
+  int64_t npool = 0;                                // pool blocks (cells, buffers, half-step blocks)
+  bool lts_trace = false;  // SEI_PREC_F16X3 under LTS: face traces of every pool block, [4][npool][9][FP]
   int32_t* d_src = nullptr;                         // [n][4] pool block read through each face (even sub-step)
   int32_t* d_src1 = nullptr;                        // the same for the odd sub-step of a coarser neighbour's step
   int32_t *d_bcell = nullptr, *d_bdst = nullptr;    // buffer entries, grouped by cluster
@@ -166,6 +168,8 @@ void freeArrays(sei_ctx* c) {
   if (c->lts_exec) cudaGraphExecDestroy(c->lts_exec);
   c->lts_exec = nullptr;
   c->lts = false;
+  c->lts_trace = false;
+  c->npool = 0;
   c->ncl = 0;
   for (void* p : {(void*)c->d_pc, (void*)c->d_mc, (void*)c->d_pslot, (void*)c->d_mslot, (void*)c->d_iters, (void*)c->d_ps,
                   (void*)c->d_ms, (void*)c->d_rel, (void*)c->d_tinvt, (void*)c->d_fsp, (void*)c->d_fsm, (void*)c->d_isp,
@@ -289,7 +293,14 @@ int launchAderOnly(sei_ctx* c, const sei::DeviceArrays& d, const float* coeffs) 
 // True when a step of kernel 'all' runs the local flux inside the tensor-core neighbour kernel
 // (SEI_OPT_NB_FORM 2): the local integral then computes the volume term and the traces only.
 bool fusedFlux(const sei_ctx* c) {
-  return c->cfg.precision == SEI_PREC_F16X3 && c->nb_form == 2 && c->tc_local == 0 && !c->lts && c->d_trace;
+  return c->cfg.precision == SEI_PREC_F16X3 && c->nb_form == 2 && (c->tc_local == 0 || c->lts) &&
+         (!c->lts || c->lts_trace) && c->d_trace;
+}
+
+// The tensor-core neighbour path with stored face traces is on: global stepping, or local time
+// stepping whose cycle keeps the traces of every pool block.
+bool traceNeighbor(const sei_ctx* c) {
+  return c->cfg.precision == SEI_PREC_F16X3 && c->d_trace && (!c->lts || c->lts_trace);
 }
 
 int launchLintOnly(sei_ctx* c, const sei::DeviceArrays& d, bool volumeOnly = false) {
@@ -297,10 +308,10 @@ int launchLintOnly(sei_ctx* c, const sei::DeviceArrays& d, bool volumeOnly = fal
   if (rc) return rc;
   // the traces cover every cell only outside local time stepping (whose kernels run per cluster);
   // a view of a range of cells writes its part ([4][n][9][FP], face-major)
-  float* trace = (c->cfg.precision == SEI_PREC_F16X3 && !c->lts)
+  float* trace = traceNeighbor(c)
                      ? c->d_trace + (size_t)d.first * 9 * ((sei::numFaceBasis(c->cfg.order) + 3) / 4 * 4)
                      : nullptr;
-  if (c->cfg.precision == SEI_PREC_F16X3 && c->tc_local) {
+  if (c->cfg.precision == SEI_PREC_F16X3 && c->tc_local && !c->lts) {
     const int lrc = c->tc_local == 1 ? sei::launchLintTransposed(c->cfg.order, d, trace, 0, c->d_status, c->sms, c->stream)
                                      : sei::launchLintTensorCore(c->cfg.order, d, trace, 0, c->d_status, c->sms, c->stream);
     if (lrc != 0) return fail(c, SEI_ERR_CUDA, "tensor-core local-integral kernel launch failed");
@@ -340,16 +351,18 @@ int launchLocal(sei_ctx* c, const sei::DeviceArrays& d, const float* coeffs, boo
 int launchNeighbor(sei_ctx* c, const sei::DeviceArrays& d, bool withLocal = false) {
   int rc = profMark(c, 1);
   if (rc) return rc;
-  if (c->cfg.precision == SEI_PREC_F16X3 && !c->lts && c->d_trace) {
+  if (traceNeighbor(c)) {
     // tensor-core path: the neighbour flux reads the stored face traces of I; they are
-    // recomputed first when I changed after the last local integral
-    if (!c->trace_valid) {
+    // recomputed first when I changed after the last local integral (under local time stepping
+    // the cycle keeps the traces of every pool block current)
+    if (!c->lts && !c->trace_valid) {
       if (sei::launchLintTransposed(c->cfg.order, d, c->d_trace, 1, c->d_status, c->sms, c->stream) != 0)
         return fail(c, SEI_ERR_CUDA, "tensor-core trace kernel launch failed");
       c->trace_valid = true;
     }
-    const int lrc = c->nb_form ? sei::launchNeighborTransposed(c->cfg.order, d, c->d_trace, c->d_status, c->sms,
-                                                               c->stream, withLocal && c->nb_form == 2)
+    const int lrc = (c->nb_form || c->lts)
+                        ? sei::launchNeighborTransposed(c->cfg.order, d, c->d_trace, c->d_status, c->sms, c->stream,
+                                                        withLocal && c->nb_form == 2)
                                : sei::launchNeighborTensorCore(c->cfg.order, d, c->d_trace, c->d_status, c->sms,
                                                                c->nb_ctas, c->stream);
     if (lrc != 0) return fail(c, SEI_ERR_CUDA, "tensor-core neighbour kernel launch failed");
@@ -1712,6 +1725,17 @@ int sei_lts_setup(sei_ctx* c, double cfl, int max_clusters, int* nclusters) {
   if (nD > 0 && cudaMalloc(&c->derivs, (size_t)nD * dsz * sizeof(float)) != cudaSuccess)
     return fail(c, SEI_ERR_OOM, "LTS derivative allocation");
   c->nslots = nD;
+  c->npool = n + nB + nS;
+  c->lts_trace = false;
+  if (c->cfg.precision == SEI_PREC_F16X3 && !c->visco) {
+    // the tensor-core neighbour path reads face traces through the pool indices of d_src
+    cudaFree(c->d_trace);
+    c->d_trace = nullptr;
+    const size_t tb = (size_t)c->npool * sei::traceFloatsPerCell(c->cfg.order) * sizeof(float);
+    if (cudaMalloc(&c->d_trace, tb) != cudaSuccess) return fail(c, SEI_ERR_OOM, "LTS trace allocation");
+    SEI_CUDA(cudaMemset(c->d_trace, 0, tb));
+    c->lts_trace = true;
+  }
   if ((rc = upload(c, &c->dslot, dsl)) || (rc = upload(c, &c->d_src, src)) || (rc = upload(c, &c->d_src1, src1)) ||
       (rc = upload(c, &c->d_bcell, fbc)) || (rc = upload(c, &c->d_bdst, fbd)) || (rc = upload(c, &c->d_gsrc, fgs)) ||
       (rc = upload(c, &c->d_gdst, fgd)) || (rc = upload(c, &c->d_gdst1, fgd1)))
@@ -1749,6 +1773,11 @@ sei::DeviceArrays rangeView(sei_ctx* c, int64_t s, int64_t e, bool neighbour, in
   d.nbr = (neighbour ? (parity ? c->d_src1 : c->d_src) : c->nbr) + s * 4;
   d.rel = c->rel + s * 4;
   d.ftype = c->ftype + s * 4;
+  d.status = c->d_status;
+  if (c->lts_trace) {  // traces addressed by pool block: plane stride npool, the range from cell s
+    d.first = (int)s;
+    d.ntotal = (int)c->npool;
+  }
   return d;
 }
 
@@ -1812,10 +1841,15 @@ int ltsCycle(sei_ctx* c) {
                                                      sei::numBasis(c->cfg.order), c->Bp, co, c->I, c->stream)
                        : c->k.taylorGather(m, c->d_gsrc + gs, dst, c->derivs, co, c->I, c->stream))
             return fail(c, SEI_ERR_CUDA, "LTS half-step kernel launch failed");
+          // the traces of the half-step blocks, which the finer neighbours' faces read
+          if (c->lts_trace && c->k.traceBlocks(m, dst, c->I, c->d_trace, (int)c->npool, c->stream))
+            return fail(c, SEI_ERR_CUDA, "LTS half-step trace kernel launch failed");
         }
       }
       const int64_t bs = c->b_start[cl], be = c->b_start[cl + 1];
-      if (be > bs) {
+      // the tensor-core path reads the buffer's traces (summed after the local integral below),
+      // not its time-integrated DOFs
+      if (be > bs && !c->lts_trace) {
         if ((rc = profMark(c, 4))) return rc;
         // a new step of the next coarser cluster begins when k / len is even
         if (sei::launchLtsBuffer((int)(be - bs), c->d_bcell + bs, c->d_bdst + bs, c->I, blk, ((k / len) % 2) == 0,
@@ -1825,8 +1859,15 @@ int ltsCycle(sei_ctx* c) {
       if (c->visco) {
         if ((rc = profMark(c, 3))) return rc;
         if (c->vk.lint(v, c->stream)) return fail(c, SEI_ERR_CUDA, "viscoelastic local-integral launch failed");
-      } else if ((rc = launchLintOnly(c, d))) {
+      } else if ((rc = launchLintOnly(c, d, fusedFlux(c)))) {
         return rc;
+      }
+      if (be > bs && c->lts_trace) {
+        if ((rc = profMark(c, 4))) return rc;
+        const int row = 9 * ((sei::numFaceBasis(c->cfg.order) + 3) / 4 * 4);
+        if (sei::launchLtsTraceBuffer((int)(be - bs), c->d_bcell + bs, c->d_bdst + bs, c->d_trace, c->npool, row,
+                                      ((k / len) % 2) == 0, c->stream))
+          return fail(c, SEI_ERR_CUDA, "LTS trace buffer kernel launch failed");
       }
     }
     for (int cl = 0; cl < c->ncl; ++cl) {
@@ -1853,7 +1894,7 @@ int ltsCycle(sei_ctx* c) {
           return fail(c, SEI_ERR_CUDA, "viscoelastic neighbour launch failed");
         continue;
       }
-      int rc = launchNeighbor(c, rangeView(c, s, e, true, parity));
+      int rc = launchNeighbor(c, rangeView(c, s, e, true, parity), fusedFlux(c));
       if (rc) return rc;
     }
   }

@@ -89,11 +89,16 @@ struct OrderKernels {
   double flopAder, flopLocal, flopNeighbor;  // non-zero flops per cell
   LaunchLintFn lintVol;       // volume + face traces, no local flux (the neighbour kernel applies it)
   LaunchLocalFn localVol;     // ADER + volume + face traces, one launch (I stays on chip)
+  // trace[4][tplane][9][FP] of the pool blocks blk[e], e < m (local time stepping)
+  int (*traceBlocks)(int m, const int32_t* blk, const float* pool, float* trace, int tplane, void* stream);
 };
 
 // pool[dst[e]] = (reset ? 0 : pool[dst[e]]) + pool[cell[e]] for e < m, blocks of blk floats
 // (integration buffers of local time stepping).
 int launchLtsBuffer(int m, const int32_t* cell, const int32_t* dst, float* pool, int blk, int reset, void* stream);
+// The same for face traces [4][plane][row] (row = 9 FP floats): all four faces of each entry.
+int launchLtsTraceBuffer(int m, const int32_t* cell, const int32_t* dst, float* trace, int64_t plane, int row,
+                         int reset, void* stream);
 
 bool kernelsForOrder(int order, OrderKernels& out);
 

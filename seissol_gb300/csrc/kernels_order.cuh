@@ -129,11 +129,19 @@ int launchTaylorGather(int m, const int32_t* src, const int32_t* dst, const floa
                                                                                        toCoeffs(coeffs), pool);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
+int launchTraceBlocks(int m, const int32_t* blk, const float* pool, float* trace, int tplane, void* stream) {
+  if (m <= 0) return 0;
+  const long threads = (long)m * 9;
+  K::SEI_CAT(sei_trace_blocks_o, SEI_ORDER)<<<(int)((threads + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      m, blk, pool, trace, tplane);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
 }  // namespace
 
 namespace sei {
 OrderKernels SEI_CAT(orderKernels, SEI_ORDER)() {
   return OrderKernels{launchLocal, launchNeighbor, launchTaylor, launchAder, launchLint, launchTaylorGather,
-                      K::kFlopAder, K::kFlopLocal, K::kFlopNeighbor, launchLintVol, launchLocalVol};
+                      K::kFlopAder, K::kFlopLocal, K::kFlopNeighbor, launchLintVol, launchLocalVol,
+                      launchTraceBlocks};
 }
 }  // namespace sei

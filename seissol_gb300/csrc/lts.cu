@@ -32,6 +32,30 @@ __global__ void sei_lts_buffer(int m, const int32_t* __restrict__ cell, const in
   }
 }
 
+// The buffer of the face traces: trace[f][dst[e]] (=|+=) trace[f][cell[e]] for the four faces f,
+// one thread per float4 of a (entry, face) row.
+__global__ void sei_lts_trace_buffer(int m, const int32_t* __restrict__ cell, const int32_t* __restrict__ dst,
+                                     float* __restrict__ trace, long long plane4, int row4, int reset) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)m * 4 * row4) return;
+  const long e = t / (4 * row4);
+  const int r = (int)(t - e * 4 * row4);
+  const int f = r / row4, j = r - f * row4;
+  float4* tr = reinterpret_cast<float4*>(trace) + (size_t)f * plane4;
+  const float4 v = tr[(size_t)__ldg(cell + e) * row4 + j];
+  float4* o = tr + (size_t)__ldg(dst + e) * row4 + j;
+  if (reset) {
+    *o = v;
+  } else {
+    float4 w = *o;
+    w.x += v.x;
+    w.y += v.y;
+    w.z += v.z;
+    w.w += v.w;
+    *o = w;
+  }
+}
+
 // One thread per (entry e, quantity q, basis k < bp), consecutive threads along k (coalesced):
 // pool[dst[e]][q][k] = sum_i coeffs[i] d[src[e]][i][q][k] for k < b, zero for b <= k < bp
 // (Taylor integral of stored full-row derivatives).
@@ -74,6 +98,17 @@ int launchLtsBuffer(int m, const int32_t* cell, const int32_t* dst, float* pool,
   const int blk4 = blk / 4;
   const long threads = (long)m * blk4;
   sei_lts_buffer<<<(int)((threads + 255) / 256), 256, 0, (cudaStream_t)stream>>>(m, cell, dst, pool, blk4, reset);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launchLtsTraceBuffer(int m, const int32_t* cell, const int32_t* dst, float* trace, int64_t plane, int row,
+                         int reset, void* stream) {
+  if (m <= 0) return 0;
+  if (row % 4) return -1;
+  const int row4 = row / 4;
+  const long threads = (long)m * 4 * row4;
+  sei_lts_trace_buffer<<<(int)((threads + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      m, cell, dst, trace, (long long)plane * row4, row4, reset);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -13,9 +13,9 @@ from tests.helpers import rel_l2_per_quantity, seeded_dofs
 pytestmark = pytest.mark.gpu
 
 
-def _graded_ctx(order, grading=6.0, dims=(8, 8, 8), seed=5):
+def _graded_ctx(order, grading=6.0, dims=(8, 8, 8), seed=5, precision=0):
     from seissol_gb300 import Context
-    ctx = Context(order, device=0)
+    ctx = Context(order, device=0, precision=precision)
     n = ctx.build_periodic_cube(*dims, perturb=0.05, seed=seed, grading=grading)
     return ctx, n
 
@@ -104,9 +104,9 @@ DR_FIELDS = dict(psi="psi", v1="slip_rate1", v2="slip_rate2", slip1="slip1", sli
                  trac1="traction1", trac2="traction2")
 
 
-def _fault_ctx(order, grading, dims=(8, 8, 8), seed=13):
+def _fault_ctx(order, grading, dims=(8, 8, 8), seed=13, precision=0):
     from seissol_gb300 import Context, RSParams
-    ctx = Context(order, device=0)
+    ctx = Context(order, device=0, precision=precision)
     n = ctx.build_periodic_cube(*dims, perturb=0.05, seed=seed, grading=grading, fault_plane=4)
     rs = RSParams.fault_config(seed=seed + 2)
     ctx.dr_setup(rs)
@@ -169,3 +169,77 @@ def test_lts_with_fault_matches_oracle(built_lib):
     assert (np.abs(v_gpu - v_ref) <= 1e-4 * np.abs(v_ref) + 1e-12).all()
     assert np.abs(ctx.dr_state("psi") - state["psi"]).max() < 1e-6
     ctx.close()
+
+
+PREC_F16X3 = 1
+OPT_NB_FORM = 5
+
+
+@pytest.mark.parametrize("form", [1, 2])
+@pytest.mark.parametrize("order", [4, 6])
+def test_lts_mixed_precision_matches_oracle(built_lib, order, form):
+    """Mixed precision under local time stepping: the tensor-core neighbour kernel reads the face
+    traces of the pool blocks (cells, integration buffers, half-step integrals) through the
+    cycle's source tables; with SEI_OPT_NB_FORM 2 the local flux joins it.  Two cycles within
+    1e-4 of the FP64 oracle (the LTS bar) and within 1e-5 of the FP32 LTS run."""
+    outs = []
+    for prec in (0, PREC_F16X3):
+        ctx, n = _graded_ctx(order, precision=prec)
+        ncl = ctx.lts_setup(0.5, 8)
+        assert ncl >= 2
+        if prec:
+            ctx.set_option(OPT_NB_FORM, form)
+        cells = ctx.get_cells()
+        start, dts = ctx.lts_clusters()
+        q0 = seeded_dofs(n, order, 7)
+        ctx.set_dofs(q0)
+        ctx.lts_run(2)
+        ctx.sync()
+        outs.append(ctx.get_dofs())
+        ctx.close()
+    cl = np.repeat(np.arange(len(dts)), np.diff(start))
+    q_ref = oracle_py.lts_cycles(oracle_py.Oracle(order), q0, cells, cl, dts[0], 2)
+    errs = rel_l2_per_quantity(outs[1], q_ref)
+    assert max(errs) < 1e-4, errs
+    assert max(rel_l2_per_quantity(outs[1], outs[0])) < 1e-5
+
+
+def test_lts_mixed_precision_graph_and_fault(built_lib):
+    """Mixed precision, local time stepping and the fault step together (the combined
+    configuration's path): one recorded cycle replayed gives the DOFs and fault state of directly
+    launched cycles bit for bit, and one cycle matches the FP64 restatement with the tolerances of
+    the FP32 test."""
+    order = 4
+    out = []
+    for graph in (0, 1):
+        ctx, n, params = _fault_ctx(order, 6.0, precision=PREC_F16X3)
+        ctx.lts_setup(0.5, 8)
+        ctx.set_option(OPT_NB_FORM, 2)
+        ctx.set_option(2, graph)  # SEI_OPT_LTS_GRAPH
+        q0 = seeded_dofs(n, order, 23)
+        ctx.set_dofs(q0)
+        if graph == 0:
+            cells = ctx.get_cells()
+            faces = ctx.dr_faces()
+            start, dts = ctx.lts_clusters()
+            state = {k: ctx.dr_state(v) for k, v in DR_FIELDS.items()}
+            dr = {"faces": faces, "params": params, "state": state, "a": ctx.dr_state("a"),
+                  "init": np.stack([ctx.dr_state("sn0"), ctx.dr_state("tau1_0"), ctx.dr_state("tau2_0")], axis=1)}
+            ctx.lts_run(1)
+            ctx.sync()
+            cl = np.repeat(np.arange(len(dts)), np.diff(start))
+            q_ref = oracle_py.lts_cycles(oracle_py.Oracle(order), q0, cells, cl, dts[0], 1, dr=dr)
+            errs = rel_l2_per_quantity(ctx.get_dofs(), q_ref)
+            assert max(errs) < 1e-4, errs
+            v_gpu = np.hypot(ctx.dr_state("slip_rate1"), ctx.dr_state("slip_rate2"))
+            v_ref = np.hypot(state["v1"], state["v2"])
+            assert (np.abs(v_gpu - v_ref) <= 1e-4 * np.abs(v_ref) + 1e-12).all()
+            ctx.lts_run(2)
+        else:
+            ctx.lts_run(1)
+            ctx.lts_run(2)
+        ctx.sync()
+        out.append((ctx.get_dofs(), ctx.dr_state("psi")))
+        ctx.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
