@@ -62,6 +62,12 @@ def bytes_per_cell(order, kernel):
         return 3 * dof + 4 * 72 + 4 * 324 + 4 + trace
     if kernel == "neighbor_tc":  # read Q, write Q, read the four neighbour traces, A- x4, relations
         return 2 * dof + trace + 4 * 324 + 16 + 4 + 4
+    if kernel == "neighbor_fused":  # the same plus the cell's own four traces and A+ x4 (local flux)
+        return 2 * dof + 2 * trace + 8 * 324 + 16 + 4 + 4
+    if kernel == "lintv":  # read I, Q += volume (read and write in L2), star non-zeros, write the traces
+        return 3 * dof + 4 * 72 + trace
+    if kernel == "localv":  # read Q, Q += volume, star non-zeros, write the traces (I stays on chip)
+        return 2 * dof + 4 * 72 + trace
     if kernel == "model":  # compulsory traffic of one fused cell update (reference data model)
         return 4 * dof + 4 * 72 + 4 * 324 + 4 * 324 + 16 + 4
     raise ValueError(kernel)
@@ -270,8 +276,9 @@ LTS_DIMS = (34, 34, 34)  # 39,304 cubes = 196,520 tets
 
 def lts_measurement(local, cycles, visco=True):
     """Rate-2 local time stepping on a graded cube: order 5, viscoelastic with 3 mechanisms (35 x 27;
-    Qp 100, Qs 50, fc 0.5 Hz, ratio 100) or elastic (35 x 9), 196,520 tets, cube edges log-uniform
-    in [50, 400] m per direction, material +-10 %, CFL 0.5; at most four clusters.
+    Qp 100, Qs 50, fc 0.5 Hz, ratio 100) or elastic (35 x 9), 196,520 tets, the LTS profile of the
+    mesh generator (x edges in four bands of 50 to 735 m on 60/25/10/5 % of the intervals, y and z
+    edges 1,600 m), material +-10 %, CFL 0.5; at most four clusters.
     One cycle advances every cluster by the coarsest step.  Reported: cell updates per second
     (a cell update = one step of one cell in its own cluster), the simulated time per wall second
     against global time stepping at the finest step (same kernels, same simulated time), with the
@@ -283,7 +290,7 @@ def lts_measurement(local, cycles, visco=True):
     out = {}
     for mode in ("direct", "graph"):
         ctx = Context(5, device=local)
-        n = ctx.build_periodic_cube(*LTS_DIMS, h=50.0, perturb=PERTURB, seed=SEED, grading=8.0)
+        n = ctx.build_periodic_cube(*LTS_DIMS, h=50.0, perturb=PERTURB, seed=SEED, grading=8.0, lts_profile=1)
         if visco:
             ctx.visco_setup(100.0, 50.0, 0.5, 100.0)
         ncl = ctx.lts_setup(0.5, 4)
@@ -312,13 +319,131 @@ def lts_measurement(local, cycles, visco=True):
         ctx.close()
     eq = ("viscoelastic order 5 (35x27, 3 mechanisms, Qp 100, Qs 50, fc 0.5 Hz, ratio 100)" if visco
           else "elastic order 5 (35x9)")
-    return {"workload": f"{eq}, 196,520-tet graded periodic cube 34^3 cubes x 5 tets, cube edges log-uniform in "
-                        "[50, 400] m per direction, material +-10%, CFL 0.5, at most 4 rate-2 clusters",
+    return {"workload": f"{eq}, 196,520-tet graded periodic cube 34^3 cubes x 5 tets, LTS profile (x edges in four "
+                        "bands 50 / 137 / 299 / 735 m on 60/25/10/5 % of the x intervals, y and z edges 1,600 m), "
+                        "material +-10%, CFL 0.5, at most 4 rate-2 clusters",
             "cells": n, "clusters": int(ncl), "cells_per_cluster": [int(x) for x in counts],
+            "cluster_split_percent": [round(100.0 * int(x) / n, 1) for x in counts],
             "cluster_dt": [float(x) for x in dts], "cycles": cycles, "direct": out["direct"], "graph": out["graph"],
             "global_stepping": out["global_stepping"],
             "lts_speedup_simulated_time": out["graph"]["simulated_s_per_wall_s"]
             / out["global_stepping"]["simulated_s_per_wall_s"]}
+
+
+def config1_measurement(local, steps=100):
+    """The plain proxy workload: elastic order 4 (20 x 9), 10,000 tets (10 x 10 x 20 cubes of
+    edge 100 m), homogeneous material (rho 2700, vp 6000, vs 3464), DOFs U[-1, 1], kernel 'all',
+    `steps` global steps.  Both GPU paths against the FP64 oracle on the same DOFs (relative L2
+    per quantity after the run), and the oracle's own single-thread CPU throughput."""
+    import numpy as np
+
+    from oracle import oracle_py
+    from seissol_gb300 import Context
+
+    dims = (10, 10, 20)
+    out, q32 = {}, None
+    for path in ("fp32", "f16x3"):
+        ctx = Context(4, device=local, precision=PATHS[path][0])
+        n = ctx.build_periodic_cube(*dims, h=100.0, rho=2700.0, vp=6000.0, vs=3464.0, perturb=0.0, seed=SEED)
+        if q32 is None:
+            q32 = np.random.default_rng(SEED).uniform(-1, 1, (n, 9, 20)).astype(np.float32)
+            cells, dt = ctx.get_cells(), ctx.cfl_timestep(0.5)
+        ctx.set_dofs(q32)
+        ctx.run("all", dt, 3)  # warm-up
+        ctx.set_dofs(q32)
+        ctx.run("all", dt, steps)
+        ctx.sync()
+        ms = ctx.last_run_ms()
+        out[path] = {"ms_per_step": ms / steps, "cell_updates_per_s": n * steps / (ms / 1e3), "dofs": ctx.get_dofs()}
+        ctx.close()
+    t0 = time.perf_counter()
+    ref = oracle_py.Oracle(4).steps(q32.astype(np.float64), cells["star"].astype(np.float64),
+                                    cells["AplusT"].astype(np.float64), cells["AminusT"].astype(np.float64),
+                                    cells["neighbor"], cells["side"], cells["orient"], dt, steps, cells["face_type"])
+    cpu_s = time.perf_counter() - t0
+    for path, r in out.items():
+        got = r.pop("dofs").astype(np.float64)
+        errs = [float(np.linalg.norm(got[:, k] - ref[:, k]) / np.linalg.norm(ref[:, k])) for k in range(9)]
+        r["rel_l2_vs_fp64_max"] = max(errs)
+        r["rel_l2_vs_fp64_per_quantity"] = errs
+    return {"workload": f"elastic order 4, {n:,}-tet periodic cube 10x10x20 cubes x 5 tets (edge 100 m), homogeneous "
+                        f"material, DOFs U[-1,1], kernel all, {steps} global steps, CFL 0.5",
+            "paths": out, "fp64_oracle": {"seconds": cpu_s, "cell_updates_per_s": n * steps / cpu_s, "cores": 1},
+            "note": "10,000 cells fill a fraction of the GPU: the GPU step time is launch-bound here"}
+
+
+def lts_accuracy(local, visco, cycles):
+    """Accuracy of the local-time-stepping paths on a small case of the same structure: order 5
+    viscoelastic (FP32 kernels) or order 6 elastic mixed precision with the fault (FVW, the fault
+    configuration's distributions, float32 pre-solve on), on the LTS mesh profile (h 50 m,
+    material +-10 %; 4 x 4 x 8 cubes = 640 tets viscoelastic, whose dense FP64 oracle is slow,
+    8 x 8 x 8 = 2,560 tets elastic), `cycles` LTS cycles from U[-1, 1] DOFs against the FP64
+    oracle: relative L2 per quantity, and for the fault the slip rate and state."""
+    import numpy as np
+
+    from oracle import dg_setup, oracle_py
+    from oracle import visco as V
+    from seissol_gb300 import Context, RSParams
+
+    order = 5 if visco else 6
+    ctx = Context(order, device=local, precision=0 if visco else PATHS["f16x3"][0])
+    dims = (4, 4, 8) if visco else (8, 8, 8)
+    n = ctx.build_periodic_cube(*dims, h=50.0, perturb=PERTURB, seed=SEED, grading=8.0, lts_profile=1,
+                                fault_plane=-1 if visco else 4)
+    dr = None
+    if visco:
+        ctx.visco_setup(100.0, 50.0, 0.5, 100.0)
+    else:
+        rs = RSParams.fault_config(seed=DR_SEED)
+        ctx.dr_setup(rs)
+        ctx.set_option(6, 1)  # SEI_OPT_DR_REFINE32
+    ncl = ctx.lts_setup(0.5, 4)
+    start, dts = ctx.lts_clusters()
+    cl = np.repeat(np.arange(ncl), np.diff(start))
+    coords, material, _ = ctx.get_geometry()
+    cells = ctx.get_cells()
+    nq = 27 if visco else 9
+    q0 = np.random.default_rng(SEED).uniform(-1, 1, (n, nq, ctx.B)).astype(np.float32)
+    ctx.set_dofs(q0)
+    if visco:
+        mats, thetas = [], []
+        for rho, mu, lam in material:
+            mu_u, lam_u, omega, theta = V.fit_attenuation(rho, mu, lam, 100.0, 50.0, 0.5, 100.0)
+            mats.append([rho, mu_u, lam_u])
+            thetas.append(theta)
+        ops = V.cell_operators(coords, np.array(mats), omega, np.array(thetas), cells["neighbor"])
+        ocells = {"star": np.concatenate([ops["star"], ops["ET"][:, None]], axis=1), "AplusT": ops["AplusT"],
+                  "AminusT": ops["AminusT"], "neighbor": cells["neighbor"], "side": cells["side"],
+                  "orient": cells["orient"], "face_type": cells["face_type"]}
+        oracle = V.ViscoLts(order)
+    else:
+        ocells, oracle = cells, oracle_py.Oracle(order)
+        fields = dict(psi="psi", v1="slip_rate1", v2="slip_rate2", slip1="slip1", slip2="slip2", slip="slip", mu="mu",
+                      trac1="traction1", trac2="traction2")
+        state = {k: ctx.dr_state(v) for k, v in fields.items()}
+        params = {k: getattr(rs, k) for k in ("f0", "b", "v0", "l", "muw", "vw", "newton_tol", "state_tol",
+                                              "max_newton", "max_outer")}
+        dr = {"faces": ctx.dr_faces(), "params": params, "state": state, "a": ctx.dr_state("a"),
+              "init": np.stack([ctx.dr_state("sn0"), ctx.dr_state("tau1_0"), ctx.dr_state("tau2_0")], axis=1)}
+    ctx.lts_run(cycles)
+    ctx.sync()
+    got = ctx.get_dofs().astype(np.float64)
+    t0 = time.perf_counter()
+    ref = oracle_py.lts_cycles(oracle, q0.astype(np.float64), ocells, cl, dts[0], cycles, dr=dr)
+    cpu_s = time.perf_counter() - t0
+    errs = [float(np.linalg.norm(got[:, k] - ref[:, k]) / np.linalg.norm(ref[:, k])) for k in range(nq)]
+    res = {"workload": (f"{'viscoelastic order 5 (27 quantities), FP32 kernels' if visco else 'elastic order 6, mixed precision, planar fault (FVW), float32 pre-solve'}"
+                        f", {n:,} tets of the LTS mesh profile ({dims[0]}x{dims[1]}x{dims[2]} cubes), {ncl} clusters "
+                        f"{[int(x) for x in np.diff(start)]}, {cycles} cycles = {cycles << (ncl - 1)} finest steps"),
+           "vs": "FP64 oracle (CPU)", "rel_l2_max": max(errs), "rel_l2_per_quantity": errs, "oracle_seconds": cpu_s}
+    if dr is not None:
+        vg = np.hypot(ctx.dr_state("slip_rate1"), ctx.dr_state("slip_rate2"))
+        vr = np.hypot(dr["state"]["v1"], dr["state"]["v2"])
+        res["slip_rate_max_rel"] = float((np.abs(vg - vr) / np.maximum(vr, 1e-30)).max())
+        res["slip_rate_rel_l2"] = float(np.linalg.norm(vg - vr) / np.linalg.norm(vr))
+        res["psi_max_abs"] = float(np.abs(ctx.dr_state("psi") - dr["state"]["psi"]).max())
+    ctx.close()
+    return res
 
 
 def visco_bytes_per_cell(kind):
@@ -495,20 +620,23 @@ def dr_measurement(local, steps, order=4, dims=None, plane=3, warm_precision=0, 
 
 def lts_fault_measurement(local, cycles):
     """The combined configuration with local time stepping: elastic order 6, 1,000,000 tets of a
-    graded periodic cube (8 x 100 x 250 cubes, edges log-uniform in [50, 400] m, material +-10%),
-    a planar fault of 50,000 faces x 49 points (FVW, the fault configuration's distributions), at
+    graded periodic cube (8 x 100 x 250 cubes, the LTS mesh profile along z: edges in four bands
+    of 50 to 735 m on 60/25/10/5 % of the z intervals, x and y edges 1,600 m; material +-10%), a
+    planar fault of 50,000 faces x 49 points (FVW, the fault configuration's distributions), at
     most 4 rate-2 clusters; both cells of a fault face share a cluster and the fault step runs in
-    its cluster's correction.  Arms over `cycles` LTS cycles: plain Newton, and the learned Newton
-    start (trained on samples of a plain run of another fault seed).  LTS runs the FP32 kernels
-    (its neighbour data are per-face pool blocks), so both arms share the arithmetic and the
-    slip-rate difference measures the warm start alone."""
+    its cluster's correction.  Arms over `cycles` LTS cycles (graph replay): FP32 kernels with
+    the plain Newton (the plain GPU path); mixed precision (tensor-core local + neighbour flux
+    from the pool blocks' face traces) with the plain Newton; mixed with the learned Newton start
+    (trained on samples of a plain run of another fault seed); and mixed with the learned start
+    and the float32 pre-solve."""
     import numpy as np
 
     from seissol_gb300 import Context, RSParams
 
-    def make(seed):
-        ctx = Context(6, device=local)
-        n = ctx.build_periodic_cube(8, 100, 250, h=50.0, perturb=PERTURB, seed=SEED, fault_plane=4, grading=8.0)
+    def make(seed, precision=0):
+        ctx = Context(6, device=local, precision=precision)
+        n = ctx.build_periodic_cube(8, 100, 250, h=50.0, perturb=PERTURB, seed=SEED, fault_plane=4, grading=8.0,
+                                    lts_profile=1)
         nf = ctx.dr_setup(RSParams.fault_config(seed=seed + 2))
         rng = np.random.default_rng(seed)
         ctx.set_dofs(rng.uniform(-1, 1, (n, 9, 56)).astype(np.float32))
@@ -531,9 +659,10 @@ def lts_fault_measurement(local, cycles):
     tr.close()
     train_s = time.perf_counter() - t0
     out, states = {}, {}
-    arms = {"plain": (False, False), "warm": (True, False), "warm_refine32": (True, True)}
-    for mode, (net, r32) in arms.items():
-        ctx, n, nf, ncl = make(DR_SEED + 1)
+    arms = {"plain": (0, False, False), "mixed": (1, False, False), "mixed_warm": (1, True, False),
+            "mixed_warm_refine32": (1, True, True)}
+    for mode, (prec, net, r32) in arms.items():
+        ctx, n, nf, ncl = make(DR_SEED + 1, prec)
         if net:
             ctx.mlp_set(params, norm)
             ctx.dr_warm_start(True)
@@ -551,58 +680,85 @@ def lts_fault_measurement(local, cycles):
         ms = ctx.last_run_ms()
         tot, npts, first = ctx.dr_newton_iterations(first=True)
         it32 = ctx.dr_newton_iterations32()
-        states[mode] = np.hypot(ctx.dr_state("slip_rate1"), ctx.dr_state("slip_rate2"))
+        states[mode] = (np.hypot(ctx.dr_state("slip_rate1"), ctx.dr_state("slip_rate2")), ctx.get_dofs())
         ctx.close()
         upd = int(sum(int(sz) * (1 << (ncl - 1 - k)) for k, sz in enumerate(sizes)))  # cell updates per cycle
         dr_steps = int(sum(int(f) * (1 << (ncl - 1 - k)) for k, f in enumerate(fcl)))  # face steps per cycle
+        per = max(npts / nf * dr_steps * cycles, 1)
         out[mode] = {"ms_per_cycle": ms / cycles, "cell_updates_per_s": upd * cycles / (ms / 1e3),
                      "face_updates_per_s": dr_steps * cycles / (ms / 1e3),
                      "simulated_s_per_wall_s": float(dts[-1]) * cycles / (ms / 1e3),
-                     "newton_iters_per_point_face_step": tot / max(npts / nf * dr_steps * cycles, 1),
-                     "first_solve_iters_per_point_face_step": first / max(npts / nf * dr_steps * cycles, 1),
-                     "float32_iters_per_point_face_step": it32 / max(npts / nf * dr_steps * cycles, 1),
+                     "newton_iters_per_point_face_step": tot / per, "first_solve_iters_per_point_face_step": first / per,
+                     "float32_iters_per_point_face_step": it32 / per, "precision": "f16x3" if prec else "fp32",
                      "network_guess": net, "float32_presolve": r32}
-    head = "warm_refine32"
-    vp, vw = states["plain"], states[head]
-    return {"workload": f"elastic order 6, {n:,}-tet graded periodic cube 8x100x250 cubes (edges log-uniform in "
-                        f"[50, 400] m, material +-10%), planar fault of {nf:,} faces x 49 points (FVW), "
-                        f"{ncl} rate-2 clusters, {cycles} LTS cycles, FP32 kernels (LTS), graph replay",
+    head = "mixed_warm"
+    vp, qp = states["plain"]
+    vm, qm = states["mixed"]
+    vw, qw = states[head]
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    return {"workload": f"elastic order 6, {n:,}-tet graded periodic cube 8x100x250 cubes (LTS mesh profile along z, "
+                        f"material +-10%), planar fault of {nf:,} faces x 49 points (FVW), {ncl} rate-2 clusters, "
+                        f"{cycles} LTS cycles, graph replay",
             "cells": n, "faces": nf, "clusters": ncl, "cells_per_cluster": [int(v) for v in sizes],
+            "cluster_split_percent": [round(100.0 * int(v) / n, 1) for v in sizes],
             "faces_per_cluster": [int(v) for v in fcl], "cluster_dt": [float(v) for v in dts], "cycles": cycles,
             "arms": out, "plain": out["plain"], "warm_start": out[head],
-            "warm_start_arm": "network first guess + float32 pre-solve, float64 Newton polish",
-            "float64_iteration_ratio": out["plain"]["newton_iters_per_point_face_step"]
+            "warm_start_arm": "mixed precision + network first guess",
+            "speedup_vs_plain_fp32": out["plain"]["ms_per_cycle"] / out[head]["ms_per_cycle"],
+            "mixed_vs_fp32_speedup_plain_newton": out["plain"]["ms_per_cycle"] / out["mixed"]["ms_per_cycle"],
+            "float64_iteration_ratio": out["mixed"]["newton_iters_per_point_face_step"]
             / max(out[head]["newton_iters_per_point_face_step"], 1e-30),
-            "first_solve_float64_iteration_ratio": out["plain"]["first_solve_iters_per_point_face_step"]
+            "first_solve_float64_iteration_ratio": out["mixed"]["first_solve_iters_per_point_face_step"]
             / max(out[head]["first_solve_iters_per_point_face_step"], 1e-30),
-            "network_alone_iteration_ratio": out["plain"]["newton_iters_per_point_face_step"]
-            / max(out["warm"]["newton_iters_per_point_face_step"], 1e-30),
-            "wall_speedup_vs_plain": out["plain"]["ms_per_cycle"] / out[head]["ms_per_cycle"],
-            "wall_speedup_network_alone": out["plain"]["ms_per_cycle"] / out["warm"]["ms_per_cycle"],
-            "max_rel_dV": float((np.abs(vp - vw) / np.maximum(vp, 1e-30)).max()),
+            "dofs_rel_l2_mixed_vs_fp32": rel(qm, qp), "dofs_rel_l2_mixed_warm_vs_fp32": rel(qw, qp),
+            "slip_rate_rel_l2_mixed_vs_fp32": rel(vm, vp), "slip_rate_rel_l2_warm_vs_mixed": rel(vw, vm),
             "training": {"samples": int(len(samples)), "loss_first": loss0, "loss_last": loss1,
                          "seconds_incl_recording": train_s}}
 
 
 PATHS = {"fp32": (0, 0), "f16x3": (1, 0), "f16x3_tc_local": (1, 1)}
 PATH_DESC = {"fp32": "FP32 CUDA cores (sparse, non-zero flops)",
-             "f16x3": "mixed: neighbour flux on tcgen05 tensor cores (split FP16 x3) from stored face traces, "
-                      "ADER and local integral FP32 CUDA cores",
+             "f16x3": "mixed: neighbour and local flux on tcgen05 tensor cores (split FP16 x3) from stored face "
+                      "traces, ADER and volume integral FP32 CUDA cores",
              "f16x3_tc_local": "mixed: local integral and neighbour flux on tcgen05 tensor cores (split FP16 x3), "
                                "ADER FP32 CUDA cores"}
 
 
 def kname(kind, path, tune=None):
-    """Name of the CUDA kernel behind a launch kind of the step (tune: the autotuner's choice)."""
-    tc_local = (tune or {}).get("tc_local", PATHS.get(path, (0, 0))[1])
-    nb_form = (tune or {}).get("nb_form", 1)
-    if kind == "lint" and path != "fp32" and tc_local:
+    """Name of the CUDA kernel behind a launch kind of the step ('ader', 'local' for the one-launch
+    cell-local kernel, 'lint', 'neighbor'; tune: the autotuner's choice, else the defaults)."""
+    t = tune or {}
+    tc_local = t.get("tc_local", PATHS.get(path, (0, 0))[1])
+    nb_form = t.get("nb_form", 2)
+    if path == "fp32":
+        return f"sei_{kind}_o{ORDER}"
+    if kind == "neighbor":
+        return f"sei_nbt<{ORDER}>" if nb_form else f"sei_nb_tc<{ORDER}>"
+    if kind == "lint" and tc_local:
         return f"sei_lintt<{ORDER}>" if tc_local == 1 else f"sei_lint_tc<{ORDER}>"
-    if kind == "neighbor" and path != "fp32":
-        return f"sei_nbt<{ORDER}>" if nb_form == 1 else f"sei_nb_tc<{ORDER}>"
-    if kind == "lint" and path != "fp32":
-        return f"sei_lint_trace_o{ORDER}"
+    if kind == "lint":
+        return f"sei_lintv_o{ORDER}" if nb_form == 2 else f"sei_lint_trace_o{ORDER}"
+    if kind == "local":
+        return f"sei_localv_o{ORDER}"
     return f"sei_{kind}_o{ORDER}"
+
+
+# algorithmic byte model of each kernel (bytes_per_cell kinds)
+BYTES_KIND = {"sei_ader": "ader", "sei_local": "local", "sei_lint": "lint", "sei_neighbor": "neighbor",
+              "sei_lint_trace": "lint_trace", "sei_lintt": "lint_tc", "sei_lint_tc": "lint_tc", "sei_nb_tc": "neighbor_tc",
+              "sei_lintv": "lintv", "sei_localv": "localv"}
+
+
+def bytes_kind(kind, path, tune=None):
+    name = kname(kind, path, tune)
+    if name.startswith("sei_nbt"):
+        t = tune or {}
+        fused = t.get("nb_form", 2) == 2 and not t.get("tc_local", PATHS.get(path, (0, 0))[1])
+        return "neighbor_fused" if fused else "neighbor_tc"
+    return BYTES_KIND[name.split("<")[0].rsplit("_o", 1)[0] if "<" not in name else name.split("<")[0]]
 
 
 def measure_path(args, world, local, path, hbm, peak_kind, e2e_steps=0):
@@ -655,8 +811,7 @@ def measure_path(args, world, local, path, hbm, peak_kind, e2e_steps=0):
     kernels = {names[k]: v[0] / v[1] for k, v in by_kind.items() if k in names and v[1] > 0}
     launches = sum(v[1] for v in by_kind.values())
     dom = max(kernels, key=kernels.get)
-    bkind = dom if path == "fp32" or dom == "ader" else f"{dom}_{'tc' if (dom == 'neighbor' or tc_local) else 'trace'}"
-    algo = bytes_per_cell(ORDER, bkind) * n
+    algo = bytes_per_cell(ORDER, bytes_kind(dom, path, tune)) * n
     achieved = algo / (kernels[dom] / 1e3) / 1e9
     traffic = None
     tf = os.path.join(ROOT, "profiles", "dram_traffic_per_cell.txt")
@@ -739,6 +894,12 @@ def run_ours(args, world, rank, local):
     comb_lts = None
     if rank == 0 and args.combined_lts_cycles > 0:
         comb_lts = lts_fault_measurement(local, args.combined_lts_cycles)
+        comb_lts["accuracy_small_case"] = lts_accuracy(local, visco=False, cycles=13)
+    if lts is not None:
+        lts["accuracy_small_case"] = lts_accuracy(local, visco=True, cycles=1)
+    cfg1 = None
+    if rank == 0 and args.config1_steps > 0:
+        cfg1 = config1_measurement(local, args.config1_steps)
 
     base = acc = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -759,7 +920,7 @@ def run_ours(args, world, rank, local):
                 "roofline": roof, "cpu_baseline": base, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": launches, "kernel_ms_per_step": kernels, "paths": paths_out,
                 "mixed_vs_fp32": ratio, "accuracy": acc, "dynamic_rupture": dr, "combined_o6_fault": comb,
-                "combined_o6_fault_lts": comb_lts,
+                "combined_o6_fault_lts": comb_lts, "proxy_o4_10k": cfg1,
                 "local_time_stepping": lts, "viscoelastic": vis}
         print(json.dumps(line))
     return 0
@@ -781,6 +942,8 @@ def main():
                     help="time the default variant of each path instead of the autotuned one")
     ap.add_argument("--dr-steps", type=int, default=200,
                     help="steps of the dynamic-rupture measurement (plain and warm-started); 0 skips it")
+    ap.add_argument("--config1-steps", type=int, default=100,
+                    help="steps of the order-4, 10,000-tet proxy workload against the FP64 oracle; 0 skips it")
     ap.add_argument("--combined-steps", type=int, default=10,
                     help="steps of the combined order-6 measurement (1M tets, 50,000-face fault); 0 skips it")
     ap.add_argument("--combined-lts-cycles", type=int, default=3,

@@ -51,8 +51,10 @@ extern "C" {
 /* Mixed precision: global-matrix contractions on the tensor cores (tcgen05 kind::f16), each
  * product split into three FP16 products (hi*hi + hi*lo + lo*hi) of power-of-two row-scaled
  * operands with FP32 accumulation; everything else FP32.  The neighbour flux always runs on the
- * tensor cores, from the face traces of I that the local integral stores; the local integral
- * runs on the tensor cores when SEI_OPT_TC_LOCAL is 1, else on the FP32 CUDA cores. */
+ * tensor cores, from the face traces of I that the local integral stores; by default
+ * (SEI_OPT_NB_FORM 2) the local flux of a step of kernel 'all' runs there too, from the cell's
+ * own traces, and the local integral keeps the volume term (FP32 CUDA cores; the tensor cores
+ * with SEI_OPT_TC_LOCAL 1 or 2, then with the local flux). */
 #define SEI_PREC_F16X3 1
 
 typedef struct sei_ctx sei_ctx;
@@ -81,10 +83,12 @@ typedef struct sei_cube_params {
    * cube-vertex plane fault_plane along x (x = fault_plane h when uniform). */
   double grading;
   /* 1 (with grading >= 8): the local-time-stepping profile of the graded mesh instead: only the
-   * x edges vary, in four octave bands [h, 2h), [2h, 4h), [4h, 8h) and 8h (the y and z edges are
-   * grading h) on 60 / 25 / 10 / 5 % of the x intervals, the bands rising and falling once along
-   * x so that neighbouring cells lie in the same or adjacent bands; rate-2 clustering then gives
-   * four clusters of about those shares.  0: as described for grading. */
+   * edges along the direction with the most intervals (x on ties) vary, in four bands of edge
+   * 1, 2.736, 5.98 and 14.7 h on 60 / 25 / 10 / 5 % of its intervals, rising and falling once so
+   * that neighbouring cells lie in the same or adjacent bands; the other edges are 32 h.  The
+   * band edges put every tet's CFL step (inradius about (w / 2) / (1 + w / 32 h) for edge w, wave
+   * speeds +-10 %) into octave b of the smallest, so rate-2 clustering gives four clusters of
+   * about those shares.  0: as described for grading. */
   int lts_profile;
 } sei_cube_params;
 
@@ -192,13 +196,15 @@ int sei_evaluate_taylor(sei_ctx* ctx, const double* coeffs, float* out_device);
 /* SEI_OPT_NB_CTAS (SEI_PREC_F16X3 only): persistent CTAs per SM of the rows-form tensor-core
  * neighbour kernel, 1..3 (default 3). */
 #define SEI_OPT_NB_CTAS 4
-/* SEI_OPT_NB_FORM (SEI_PREC_F16X3 only): layout of the tensor-core neighbour flux.  1 (default),
+/* SEI_OPT_NB_FORM (SEI_PREC_F16X3 only): layout of the tensor-core neighbour flux.  1,
  * transposed: the basis index on the TMEM lanes and a tile's (quantity, cell) pairs on the MMA
  * columns, so the per-cell 9 x 9 mixing stays in registers; 0, rows: a tile's (cell, quantity)
- * rows on the lanes, the mixing through shared memory; 2: transposed, and in a step of kernel
- * 'all' (or 'all_dr') the local flux of every face joins the neighbour flux before their common
- * lift rDivM_i (the local integral then computes the volume term and the face traces only;
- * SEI_OPT_TC_LOCAL 0).  The separate local-integral and neighbour calls keep their full meaning. */
+ * rows on the lanes, the mixing through shared memory; 2 (default): transposed, and in a step of
+ * kernel 'all' (or 'all_dr', or a local-time-stepping cycle) the local flux of every face joins
+ * the neighbour flux before their common lift rDivM_i (the local integral then computes the
+ * volume term and the face traces only; SEI_OPT_TC_LOCAL 0).  The separate local-integral and
+ * neighbour calls keep their full meaning.  Under local time stepping the transposed form is
+ * used for 0 too. */
 #define SEI_OPT_NB_FORM 5
 /* SEI_OPT_DR_REFINE32: 1 makes every slip-rate solve of the fault kernel first iterate in float32
  * on ln V from its start (the previous slip rate, or the network's guess on a first solve with

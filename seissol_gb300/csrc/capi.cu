@@ -84,7 +84,7 @@ struct sei_ctx {
   cudaStream_t copy_stream = nullptr;      // host <-> device copies of sei_run_host, beside the compute stream
   std::vector<cudaEvent_t> pipe_events;    // chunk events of the pipelined sei_run_host
   int nb_ctas = 3;        // SEI_OPT_NB_CTAS: persistent CTAs per SM of the rows-form tensor-core neighbour kernel
-  int nb_form = 1;        // SEI_OPT_NB_FORM: 1 transposed tensor-core neighbour kernel, 0 rows form
+  int nb_form = 2;        // SEI_OPT_NB_FORM: 2 transposed with the local flux fused in, 1 transposed, 0 rows form
   std::vector<cudaEvent_t> prof_events;
   std::vector<int> prof_kind;  // kind of the launch starting at event i: 0 ADER (or fused ADER + local),
                                // 1 neighbour, 2 fault, 3 local integral, 4 LTS gather / buffer, -1 end of run

@@ -191,8 +191,14 @@ void fluxSolver(double s, const Mat9& Ti, const Mat9& qgod, const Mat9& at, cons
 
 }  // namespace
 
-// Shares of the x (y, z) intervals in the octave bands of the local-time-stepping profile.
-constexpr double kLtsBandShare[4] = {0.47, 0.15, 0.05, 0.33};
+// The local-time-stepping profile: shares of the banded direction's intervals in the four bands,
+// the edge of each band and the edge of the other two directions (units of h).  A cube w x L x L (w << L) splits into tets of
+// inradius about (w / 2) / (1 + w / L), so the band edges are set for inradii 1.3 2^b times that
+// of band 0: with the material's +-10 % wave speeds every tet of band b then has a CFL step in
+// [2^b, 2^(b+1)) times the smallest one, i.e. lies in rate-2 cluster b.
+constexpr double kLtsBandShare[4] = {0.60, 0.25, 0.10, 0.05};
+constexpr double kLtsBandEdge[4] = {1.0, 2.736, 5.98, 14.7};
+constexpr double kLtsCrossEdge = 32.0;
 
 void buildPeriodicCube(const sei_cube_params& p, HostMesh& m) {
   // Even counts keep the alternating 5-tet split conforming across cubes; at least 4 cubes per
@@ -211,15 +217,19 @@ void buildPeriodicCube(const sei_cube_params& p, HostMesh& m) {
     for (int d = 0; d < 3; ++d) {
       pos[d].assign(cnt[d] + 1, 0.0);
       if (p.lts_profile == 1 && p.grading >= 8.0) {
-        // every direction: octave bands b = 0..3 of the edge on fixed shares of the intervals,
-        // rising then falling once (band sequence 0 .. 3 .. 0, each band split between the two
-        // slopes), so neighbouring cubes lie in the same or adjacent bands; the shares are set
-        // so that the smallest edge of a cube, which bounds its time step, falls in band b for
-        // about 60 / 25 / 10 / 5 % of the cubes
-        const double share[4] = {kLtsBandShare[0], kLtsBandShare[1], kLtsBandShare[2], kLtsBandShare[3]};
+        // the direction with the most intervals (x on ties): bands b = 0..3 of the edge on fixed
+        // shares of the intervals, rising then falling once (band sequence 0 .. 3 .. 0, each band
+        // split between the two slopes), so neighbouring cubes lie in the same or adjacent bands
+        // also across the periodic boundary; the other two directions: one long edge, so the
+        // banded edge bounds each tet's time step and rate-2 clustering follows the bands
+        const int banded = cnt[2] > cnt[1] && cnt[2] > cnt[0] ? 2 : (cnt[1] > cnt[0] ? 1 : 0);
+        if (d != banded) {
+          for (int i = 0; i < cnt[d]; ++i) pos[d][i + 1] = pos[d][i] + p.h * kLtsCrossEdge;
+          continue;
+        }
         int count[4], used = 0;
         for (int b = 3; b >= 1; --b) {
-          count[b] = std::max(1, (int)std::lround(share[b] * cnt[d]));
+          count[b] = std::max(1, (int)std::lround(kLtsBandShare[b] * cnt[d]));
           used += count[b];
         }
         count[0] = std::max(1, cnt[d] - used);
@@ -229,11 +239,7 @@ void buildPeriodicCube(const sei_cube_params& p, HostMesh& m) {
         for (int b = 3; b >= 0; --b)
           for (int k = 0; k < count[b] / 2; ++k) band.push_back(b);
         band.resize(cnt[d], 0);
-        for (int i = 0; i < cnt[d]; ++i) {
-          const int b = band[i];
-          const double w = p.h * std::ldexp(1.0, b);  // h, 2h, 4h, 8h
-          pos[d][i + 1] = pos[d][i] + w;
-        }
+        for (int i = 0; i < cnt[d]; ++i) pos[d][i + 1] = pos[d][i] + p.h * kLtsBandEdge[band[i]];
         continue;
       }
       for (int i = 0; i < cnt[d]; ++i) {
