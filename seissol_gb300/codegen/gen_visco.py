@@ -13,7 +13,9 @@ src/Equations/viscoelastic/Model/ViscoelasticSetup.h) have a structure these ker
 So a CTA holds 32 cells and 15 warps: warps 0..8 run the elastic column q exactly like the elastic
 kernels (premix with the star non-zeros, global matrices as FFMA literals), warps 9..14 run the
 strain column j = q - 9 through the same code with the strain sources (velocities) and
-coefficients, and then update the three memory variables j of their cell elementwise:
+coefficients, and then update the three memory variables j of their cell elementwise (the ADER
+kernel runs the same 15 column tasks on 16 cells per CTA, half a warp each, so that its larger
+shared memory still fits two CTAs on an SM):
 
   ADER    dQ_i(mem l j) = -omega_l (E_i(j) + dQ_{i-1}(mem l j)),  E_i = sum_e kDivMT_e (dQ_{i-1} S_e)
   volume  Q(mem l j) += -omega_l (V(j) + I(mem l j)),             V   = sum_e kDivM_e (I S_e)
@@ -90,13 +92,24 @@ PROLOGUE = """
     }"""
 
 
-def _premix_matvec(a, mats, dst, rows, cols, ind):
-    """dst[k] += sum_e mats[e][k, l] (st_e . (Xs0, Xs1, Xs2)[l]) over the non-zero columns l."""
+# The ADER kernel: 16 cells per CTA, thread (column task q < 15, cell lane < 16), 240 threads, so
+# its exchange X [9][B][16] and memory variables M, IM [18][B][16] take 100.8 KB at order 5 and two
+# CTAs share an SM (their stage barriers and compute overlap).
+CPBA = 16
+PROLOGUE_ADER = PROLOGUE.replace("const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;",
+                                 "const int q = threadIdx.x >> 4, lane = threadIdx.x & 15;") \
+                        .replace("const int cell = blockIdx.x * kCPB + lane;", "const int cell = blockIdx.x * kCPBA + lane;") \
+                        .replace("[9][kB][32]", "[9][kB][16]").replace("kB * 32 + lane", "kB * 16 + lane")
+
+
+def _premix_matvec(a, mats, dst, rows, cols, ind, w=32):
+    """dst[k] += sum_e mats[e][k, l] (st_e . (Xs0, Xs1, Xs2)[l]) over the non-zero columns l
+    (w cells per row of the exchange)."""
     cl = [_cols(m, rows, cols) for m in mats]
     for l in range(cols):
         if not any(l in c for c in cl):
             continue
-        a(f"{ind}{{ const float x0 = Xs0[{l * 32}], x1 = Xs1[{l * 32}], x2 = Xs2[{l * 32}];")
+        a(f"{ind}{{ const float x0 = Xs0[{l * w}], x1 = Xs1[{l * w}], x2 = Xs2[{l * w}];")
         for e in range(3):
             if l in cl[e]:
                 a(f"{ind}  const float y{e} = st[{e}][0] * x0 + st[{e}][1] * x1 + st[{e}][2] * x2;")
@@ -106,8 +119,9 @@ def _premix_matvec(a, mats, dst, rows, cols, ind):
         a(f"{ind}}}")
 
 
-def _theta_from_smem(a, base, ind):
-    """Stress column q < 6 of zn += sum_l theta coupling of the memory variables in shared memory."""
+def _theta_from_smem(a, base, ind, w=32):
+    """Stress column q < 6 of zn += sum_l theta coupling of the memory variables in shared memory
+    (w cells per row)."""
     a(f"""{ind}if (el && q < 6) {{
 {ind}#pragma unroll 1
 {ind}  for (int m = 0; m < 3; ++m) {{
@@ -116,9 +130,9 @@ def _theta_from_smem(a, base, ind):
 {ind}#pragma unroll 1
 {ind}    for (int jj = lo; jj < hi; ++jj) {{
 {ind}      const float c = q < 3 ? __ldg(th + (jj == q ? 0 : 1)) : __ldg(th + 2);
-{ind}      const float* src = {base} + (m * 6 + jj) * kB * 32 + lane;
+{ind}      const float* src = {base} + (m * 6 + jj) * kB * {w} + lane;
 {ind}#pragma unroll
-{ind}      for (int k = 0; k < kB; ++k) zn[k] = fmaf(c, src[k * 32], zn[k]);
+{ind}      for (int k = 0; k < kB; ++k) zn[k] = fmaf(c, src[k * {w}], zn[k]);
 {ind}    }}
 {ind}  }}
 {ind}}}""")
@@ -133,7 +147,7 @@ def gen_visco(order: int) -> str:
     a("// Do not edit.")
     a("#pragma once")
     a(f"namespace sei_v{order} {{")
-    a(f"constexpr int kOrder = {order}, kB = {B}, kBp = {padded(B)}, kF = {F}, kNQ = {NQ}, kCPB = {CPB};")
+    a(f"constexpr int kOrder = {order}, kB = {B}, kBp = {padded(B)}, kF = {F}, kNQ = {NQ}, kCPB = {CPB}, kCPBA = {CPBA};")
     a("// Stored derivatives of one cell: [stage][27][kB] (the source term keeps all basis rows).")
     a(f"constexpr int kDerivSize = {order} * {NQ} * {B};")
     _tables(L)
@@ -142,15 +156,17 @@ def gen_visco(order: int) -> str:
     a(f"""
 // Cauchy-Kovalevskaya predictor with the viscoelastic source term: I = sum_i coeffs[i] dQ(i).
 // Q, I [n][27][Bp]; star_nz [n][3][24] (elastic, unrelaxed moduli); grad [n][3][3]; theta [n][3][3];
-// omega: relaxation frequencies.  Shared memory: X [9][B][32], M and IM [18][B][32].
+// omega: relaxation frequencies.  16 cells per CTA, 240 threads (column task q = tid / 16: 0..8
+// elastic, 9..14 strain; cell lane = tid % 16); shared memory: X [9][B][16], M and IM [18][B][16]
+// (100.8 KB at order 5: two CTAs per SM).
 // derivs (nullable): derivative output [slots][kDerivSize]; the slot of a cell is dslot[cell]
 // (-1: not stored), or the cell itself when dslot is nullptr.
-extern "C" __global__ void __launch_bounds__(480, 1)
+extern "C" __global__ void __launch_bounds__(240, 2)
 sei_vader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout, const float* __restrict__ star_nz,
                    const float* __restrict__ grad, const float* __restrict__ theta, SeiOmega omega,
-                   SeiCoeffs coeffs, float* __restrict__ derivs, const int* __restrict__ dslot) {{""" + PROLOGUE)
-    a("""  float* M = X + 9 * kB * 32;    // memory variables of the current stage [l * 6 + j][kB][32]
-  float* IM = M + 18 * kB * 32;   // their time integral
+                   SeiCoeffs coeffs, float* __restrict__ derivs, const int* __restrict__ dslot) {{""" + PROLOGUE_ADER)
+    a("""  float* M = X + 9 * kB * 16;    // memory variables of the current stage [l * 6 + j][kB][16]
+  float* IM = M + 18 * kB * 16;   // their time integral
   float z[kBp];
   float I[kBp];
   const int dsl = derivs ? (dslot ? __ldg(dslot + cl) : cl) : -1;
@@ -164,12 +180,12 @@ sei_vader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout,
 #pragma unroll 1
     for (int m = 0; m < 3; ++m) {
       sei_load_col<kBp>(Q + ((size_t)cl * kNQ + 9 + 6 * m + jv) * kBp, z);
-      float* Mm = M + (m * 6 + jv) * kB * 32 + lane;
-      float* IMm = IM + (m * 6 + jv) * kB * 32 + lane;
+      float* Mm = M + (m * 6 + jv) * kB * 16 + lane;
+      float* IMm = IM + (m * 6 + jv) * kB * 16 + lane;
 #pragma unroll
       for (int k = 0; k < kB; ++k) {
-        Mm[k * 32] = z[k];
-        IMm[k * 32] = coeffs.c[0] * z[k];
+        Mm[k * 16] = z[k];
+        IMm[k * 16] = coeffs.c[0] * z[k];
       }
       if (dbase) sei_store_col_scalar<kB>(dbase + (9 + 6 * m + jv) * kB, z);
     }
@@ -178,13 +194,13 @@ sei_vader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout,
         a(f"  // ---- stage {i}")
         a("  {")
         a("    if (el) {")
-        a("#pragma unroll\n      for (int k = 0; k < kB; ++k) Xq[k * 32] = z[k];")
+        a("#pragma unroll\n      for (int k = 0; k < kB; ++k) Xq[k * 16] = z[k];")
         a("    }")
         a("    __syncthreads();")
         a("    float zn[kB];")
         a("#pragma unroll\n    for (int k = 0; k < kB; ++k) zn[k] = 0.f;")
-        _premix_matvec(a, G["kDivMT"], "zn", B, B, "    ")
-        _theta_from_smem(a, "M", "    ")
+        _premix_matvec(a, G["kDivMT"], "zn", B, B, "    ", w=16)
+        _theta_from_smem(a, "M", "    ", w=16)
         a("    __syncthreads();")
         a("    if (el) {")
         a(f"#pragma unroll\n      for (int k = 0; k < kB; ++k) {{ I[k] = fmaf(coeffs.c[{i}], zn[k], I[k]); z[k] = zn[k]; }}")
@@ -193,13 +209,13 @@ sei_vader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout,
         a("#pragma unroll 1")
         a("      for (int m = 0; m < 3; ++m) {")
         a("        const float w = -omega.w[m];")
-        a("        float* Mm = M + (m * 6 + jv) * kB * 32 + lane;")
-        a("        float* IMm = IM + (m * 6 + jv) * kB * 32 + lane;")
+        a("        float* Mm = M + (m * 6 + jv) * kB * 16 + lane;")
+        a("        float* IMm = IM + (m * 6 + jv) * kB * 16 + lane;")
         a("#pragma unroll")
         a("        for (int k = 0; k < kB; ++k) {")
-        a("          const float nw = w * (zn[k] + Mm[k * 32]);")
-        a("          Mm[k * 32] = nw;")
-        a(f"          IMm[k * 32] = fmaf(coeffs.c[{i}], nw, IMm[k * 32]);")
+        a("          const float nw = w * (zn[k] + Mm[k * 16]);")
+        a("          Mm[k * 16] = nw;")
+        a(f"          IMm[k * 16] = fmaf(coeffs.c[{i}], nw, IMm[k * 16]);")
         a(f"          if (dbase) dbase[{i} * kNQ * kB + (9 + 6 * m + jv) * kB + k] = nw;")
         a("        }")
         a("      }")
@@ -211,9 +227,9 @@ sei_vader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout,
     } else {
 #pragma unroll 1
       for (int m = 0; m < 3; ++m) {
-        const float* IMm = IM + (m * 6 + jv) * kB * 32 + lane;
+        const float* IMm = IM + (m * 6 + jv) * kB * 16 + lane;
 #pragma unroll
-        for (int k = 0; k < kB; ++k) z[k] = IMm[k * 32];
+        for (int k = 0; k < kB; ++k) z[k] = IMm[k * 16];
 #pragma unroll
         for (int k = kB; k < kBp; ++k) z[k] = 0.f;
         sei_store_col<kBp>(Iout + ((size_t)cell * kNQ + 9 + 6 * m + jv) * kBp, z);
