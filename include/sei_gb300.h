@@ -214,7 +214,12 @@ int sei_evaluate_taylor(sei_ctx* ctx, const double* coeffs, float* out_device);
  * Newton tolerance.  No counterpart in the reference; float64 is the scarce pipe of GB300.
  * 0 (default): the float64 Newton alone. */
 #define SEI_OPT_DR_REFINE32 6
+/* SEI_OPT_TUNE_FAIL_AT (tests only): sei_autotune fails on the host at candidate `value` (after its
+ * warm-up step, before its timing), as a variant whose launch failed would; -1 (default): never. */
+#define SEI_OPT_TUNE_FAIL_AT 7
 int sei_set_option(sei_ctx* ctx, int option, int value);
+/* The current value of an option (SEI_ERR_ARG for an unknown one). */
+int sei_get_option(sei_ctx* ctx, int option, int* value);
 
 /* Autotuner (no counterpart in the reference, whose kernel shapes are fixed when its code is
  * generated): times `steps` steps of kernel 'all' on the context's own mesh for every variant of

@@ -68,6 +68,7 @@ struct sei_ctx {
   float mlp_norm[sei_mlp::kNorm] = {0};
   bool warm_start = false;
   bool dr_refine32 = false;  // SEI_OPT_DR_REFINE32
+  int tune_fail_at = -1;     // SEI_OPT_TUNE_FAIL_AT: candidate the autotuner fails on the host (tests)
   float* d_rec = nullptr;  // recorded training samples [rec_cap][6]
   unsigned* d_rec_count = nullptr;
   unsigned rec_cap = 0;
@@ -798,8 +799,25 @@ int sei_set_option(sei_ctx* c, int option, int value) {
       c->dr_refine32 = value != 0;
       dropLtsGraph(c);  // a recorded cycle holds the fault kernel's arguments
       return SEI_OK;
+    case SEI_OPT_TUNE_FAIL_AT:
+      c->tune_fail_at = value;
+      return SEI_OK;
     default:
       return fail(c, SEI_ERR_ARG, "unknown option");
+  }
+}
+
+int sei_get_option(sei_ctx* c, int option, int* value) {
+  if (!c || !value) return SEI_ERR_ARG;
+  switch (option) {
+    case SEI_OPT_FUSED_LOCAL: *value = c->fused_local ? 1 : 0; return SEI_OK;
+    case SEI_OPT_LTS_GRAPH: *value = c->lts_graph ? 1 : 0; return SEI_OK;
+    case SEI_OPT_TC_LOCAL: *value = c->tc_local; return SEI_OK;
+    case SEI_OPT_NB_CTAS: *value = c->nb_ctas; return SEI_OK;
+    case SEI_OPT_NB_FORM: *value = c->nb_form; return SEI_OK;
+    case SEI_OPT_DR_REFINE32: *value = c->dr_refine32 ? 1 : 0; return SEI_OK;
+    case SEI_OPT_TUNE_FAIL_AT: *value = c->tune_fail_at; return SEI_OK;
+    default: return fail(c, SEI_ERR_ARG, "unknown option");
   }
 }
 
@@ -2051,13 +2069,15 @@ int sei_autotune(sei_ctx* c, double dt, int steps, sei_tune_result* out) {
     return done(fail(c, SEI_ERR_CUDA, "autotuner set-up"));
   double best = 1e300, worst = 0.0;
   Cand pick = cands[0];
-  for (const Cand& k : cands) {
+  for (size_t ci = 0; ci < cands.size(); ++ci) {
+    const Cand& k = cands[ci];
     c->fused_local = k.fused != 0;
     c->tc_local = k.tcLocal;
     c->nb_ctas = k.nbCtas;
     c->nb_form = k.nbForm;
     c->trace_valid = false;
     if ((rc = runKernel(c, SEI_KERNEL_ALL, dt, 1))) return done(rc);  // warm-up
+    if ((int)ci == c->tune_fail_at) return done(fail(c, SEI_ERR_CUDA, "autotuner: failure injected on the host"));
     if (cudaEventRecord(e0, c->stream) != cudaSuccess) return done(fail(c, SEI_ERR_CUDA, "event record"));
     if ((rc = runKernel(c, SEI_KERNEL_ALL, dt, steps))) return done(rc);
     float ms = 0.f;

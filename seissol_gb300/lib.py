@@ -116,6 +116,7 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_autotune", i, [VP, d, i, C.POINTER(_Tune)])
     _sig(lib, "sei_set_profiling", i, [VP, i])
     _sig(lib, "sei_set_option", i, [VP, i, i])
+    _sig(lib, "sei_get_option", i, [VP, i, C.POINTER(i)])
     _sig(lib, "sei_tc_gemm_check", i, [VP, VP, VP, i, i, i])
     _sig(lib, "sei_tc_layout_check", i, [VP, VP, VP, i, i, i, i, i, i])
     _sig(lib, "sei_check_wait_timeout", i, [VP, i, i])
@@ -362,6 +363,11 @@ class Context:
     # -- kernels ------------------------------------------------------------------------
     def set_option(self, option, value):
         self._check(self.lib.sei_set_option(self.h, option, int(value)), "sei_set_option")
+
+    def get_option(self, option):
+        v = C.c_int()
+        self._check(self.lib.sei_get_option(self.h, option, C.byref(v)), "sei_get_option")
+        return v.value
 
     def compute_ader(self, dt, coeffs=None):
         """Spacetime::computeAder: I = sum_i coeffs[i] dQ_i (coeffs default: integrate(0, dt))."""

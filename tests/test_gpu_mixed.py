@@ -271,3 +271,25 @@ def test_local_flux_in_neighbour_kernel_partial_blocks(built_lib, order, fused):
                                           cut["AminusT"].astype(np.float64), nb, cut["side"], cut["orient"], dt, 3, ft)
     errs = rel_l2_per_quantity(q_gpu, q_ref)
     assert max(errs) < 1e-5, errs
+
+
+def test_autotune_failure_restores_the_options(built_lib):
+    """A candidate that fails (injected on the host through SEI_OPT_TUNE_FAIL_AT) makes sei_autotune
+    return its error and leaves the context's options and DOFs as they were on entry."""
+    from seissol_gb300 import SeiError
+    ctx, n, q0 = _ctx(4, PREC_F16X3)
+    ctx.set_option(1, 1)  # SEI_OPT_FUSED_LOCAL
+    ctx.set_option(OPT_NB_FORM, 1)
+    ctx.set_option(4, 2)  # SEI_OPT_NB_CTAS
+    opts = (1, 3, 4, OPT_NB_FORM)
+    before = {o: ctx.get_option(o) for o in opts}
+    ctx.set_option(7, 3)  # SEI_OPT_TUNE_FAIL_AT: the fourth candidate fails
+    dt = ctx.cfl_timestep(0.5)
+    with pytest.raises(SeiError):
+        ctx.autotune(dt, 2)
+    assert {o: ctx.get_option(o) for o in opts} == before
+    assert np.array_equal(ctx.get_dofs(), q0)
+    ctx.set_option(7, -1)
+    r = ctx.autotune(dt, 2)
+    assert r["candidates"] == 14
+    ctx.close()
