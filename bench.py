@@ -853,6 +853,27 @@ def measure_path(args, world, local, path, hbm, peak_kind, e2e_steps=0):
         e2e = {"value": world * n * e2e_steps / el, "unit": UNIT, "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": nbytes, "steps": e2e_steps, "path": path,
                "call": "sei_run_host(SEI_KERNEL_ALL, dt, 1, dofs_in, dofs_out) with pinned host DOFs"}
+        # the copy ceiling: one cudaMemcpyAsync of the same bytes each way, pinned, CUDA events
+        dev = torch.empty((n, 9, B), dtype=torch.float32, device=f"cuda:{local}")
+        s = torch.cuda.Stream(device=local)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        with torch.cuda.stream(s):
+            dev.copy_(hin, non_blocking=True)  # warm-up
+            hout.copy_(dev, non_blocking=True)
+            ev[0].record(s)
+            dev.copy_(hin, non_blocking=True)
+            ev[1].record(s)
+            ev[2].record(s)
+            hout.copy_(dev, non_blocking=True)
+            ev[3].record(s)
+        s.synchronize()
+        h2d_ms, d2h_ms = ev[0].elapsed_time(ev[1]), ev[2].elapsed_time(ev[3])
+        e2e["copy_ceiling"] = {"h2d_gbs": nbytes / (h2d_ms / 1e3) / 1e9, "d2h_gbs": nbytes / (d2h_ms / 1e3) / 1e9,
+                               "ms_both_ways": h2d_ms + d2h_ms,
+                               "cell_updates_per_s_if_copies_alone": world * n / ((h2d_ms + d2h_ms) / 1e3),
+                               "how": "one cudaMemcpyAsync of the step's DOFs each way, pinned host memory, "
+                                      "CUDA events on a side stream"}
+        del dev
     ctx.close()
     return {"value": value, "ms": ms, "n": n, "kernels": kernels, "launches": launches, "roofline": roof,
             "clocks": clk.summary(), "e2e": e2e, "description": PATH_DESC[path], "autotune": tune}

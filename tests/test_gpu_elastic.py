@@ -237,3 +237,52 @@ def test_hundred_thousand_cells_one_step(built_lib, precision):
     assert max(errs) < 1e-5, errs
     upd = rel_l2_per_quantity(got - q0, ref - q0)
     assert max(upd) < 2e-5, upd  # the update itself, the single-application bar
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_benchmark_mesh_two_steps(built_lib, precision):
+    """The benchmark's own workload: order 6, 400,000 tets (40 x 40 x 50 cubes, material +-10 %,
+    the bench's seed), two steps of kernel 'all' on the FP32 and the mixed path against the
+    OpenMP FP64 oracle: 1e-5 relative L2 per quantity of the field, 2e-5 of the update."""
+    from seissol_gb300 import Context
+    order = 6
+    ctx = Context(order, device=0, precision=precision)
+    n = ctx.build_periodic_cube(40, 40, 50, perturb=0.1, seed=2024)
+    assert n == 400000
+    cells = ctx.get_cells()
+    q0 = seeded_dofs(n, order, 2024)
+    ctx.set_dofs(q0)
+    dt = ctx.cfl_timestep(0.5)
+    ctx.run("all", dt, 2)
+    ctx.sync()
+    got = ctx.get_dofs()
+    ctx.close()
+    ops = _ops64(cells)
+    ref = oracle_py.Oracle(order).steps(q0, ops["star"], ops["AplusT"], ops["AminusT"], cells["neighbor"], cells["side"],
+                                        cells["orient"], dt, 2, cells["face_type"])
+    errs = rel_l2_per_quantity(got, ref)
+    assert max(errs) < 1e-5, errs
+    upd = rel_l2_per_quantity(got - q0, ref - q0)
+    assert max(upd) < 2e-5, upd
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_benchmark_mesh_linearity(built_lib, precision):
+    """A size-independent property at the benchmark's full size (400,000 tets, order 6): a step is
+    linear in the DOFs, so step(a Q1 + b Q2) = a step(Q1) + b step(Q2) to float rounding
+    (1e-6 relative L2 per quantity)."""
+    from seissol_gb300 import Context
+    order = 6
+    ctx = Context(order, device=0, precision=precision)
+    n = ctx.build_periodic_cube(40, 40, 50, perturb=0.1, seed=2024)
+    dt = ctx.cfl_timestep(0.5)
+    q1, q2 = seeded_dofs(n, order, 1), seeded_dofs(n, order, 2)
+    out = []
+    for q in (q1, q2, (0.75 * q1.astype(np.float64) - 0.5 * q2).astype(np.float32)):
+        ctx.set_dofs(q)
+        ctx.run("all", dt, 1)
+        ctx.sync()
+        out.append(ctx.get_dofs().astype(np.float64))
+    ctx.close()
+    errs = rel_l2_per_quantity(out[2], 0.75 * out[0] - 0.5 * out[1])
+    assert max(errs) < 1e-6, errs
