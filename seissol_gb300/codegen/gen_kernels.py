@@ -328,26 +328,32 @@ def gen_order(order: int) -> str:
             a("  }")
 
     def emit_traces_volume_reduce():
-        """From I in registers: the four face traces through the shared area (one face at a time,
-        one bulk copy per cell out), then the volume integral, added to Q by bulk reduce-adds."""
-        a("  // ---- face traces fMrT_f I, one face at a time through the shared area")
-        for f in range(4):
-            a("  {")
-            a("    float T[kF];")
-            _matvec(L, "    ", G["fMrT"][f], "I", "T", F, B, True)
-            if f > 0:
-                a("    if (threadIdx.x < 32) sei_tc::bulkWaitRead();  // the previous face's copies have read the area")
-                a("    __syncthreads();")
-            a("    float4* stg = reinterpret_cast<float4*>(X + lane * kTs + q * kFP);")
-            a("#pragma unroll\n    for (int m4 = 0; m4 < kFP / 4; ++m4)")
-            a("      stg[m4] = make_float4(4 * m4 < kF ? T[4 * m4 < kF ? 4 * m4 : 0] : 0.f, 4 * m4 + 1 < kF ? T[4 * m4 + 1 < kF ? 4 * m4 + 1 : 0] : 0.f,")
-            a("                            4 * m4 + 2 < kF ? T[4 * m4 + 2 < kF ? 4 * m4 + 2 : 0] : 0.f, 4 * m4 + 3 < kF ? T[4 * m4 + 3 < kF ? 4 * m4 + 3 : 0] : 0.f);")
-            a("    sei_tc::fenceProxyAsync();")
-            a("    __syncthreads();")
-            a("    if (threadIdx.x < 32 && lane < cnt) {")
-            a(f"      sei_tc::bulkCopyS2G(trace + ((size_t){f} * tplane + cell0 + lane) * 9 * kFP, X + lane * kTs, 9 * kFP * 4);")
-            a("      sei_tc::bulkCommit();")
-            a("    }")
+        """From I in registers: the four face traces through the shared area (as many faces at a
+        time as the area holds, one bulk copy per cell and face out), then the volume integral,
+        added to Q by bulk reduce-adds."""
+        kst, kts = 9 * padded(B) + 4, 9 * padded(F) + 4
+        slots = max(1, min(4, max(9 * B * 32, 32 * kst) // (32 * kts)))
+        a(f"  // ---- face traces fMrT_f I, {slots} face(s) at a time through the shared area")
+        for g0 in range(0, 4, slots):
+            group = list(range(g0, min(4, g0 + slots)))
+            if g0 > 0:
+                a("  if (threadIdx.x < 32) sei_tc::bulkWaitRead();  // the previous faces' copies have read the area")
+                a("  __syncthreads();")
+            for f in group:
+                a("  {")
+                a("    float T[kF];")
+                _matvec(L, "    ", G["fMrT"][f], "I", "T", F, B, True)
+                a(f"    float4* stg = reinterpret_cast<float4*>(X + ({f - g0} * 32 + lane) * kTs + q * kFP);")
+                a("#pragma unroll\n    for (int m4 = 0; m4 < kFP / 4; ++m4)")
+                a("      stg[m4] = make_float4(4 * m4 < kF ? T[4 * m4 < kF ? 4 * m4 : 0] : 0.f, 4 * m4 + 1 < kF ? T[4 * m4 + 1 < kF ? 4 * m4 + 1 : 0] : 0.f,")
+                a("                            4 * m4 + 2 < kF ? T[4 * m4 + 2 < kF ? 4 * m4 + 2 : 0] : 0.f, 4 * m4 + 3 < kF ? T[4 * m4 + 3 < kF ? 4 * m4 + 3 : 0] : 0.f);")
+                a("  }")
+            a("  sei_tc::fenceProxyAsync();")
+            a("  __syncthreads();")
+            a("  if (threadIdx.x < 32 && lane < cnt) {")
+            for f in group:
+                a(f"    sei_tc::bulkCopyS2G(trace + ((size_t){f} * tplane + cell0 + lane) * 9 * kFP, X + ({f - g0} * 32 + lane) * kTs, 9 * kFP * 4);")
+            a("    sei_tc::bulkCommit();")
             a("  }")
         a("  if (threadIdx.x < 32) sei_tc::bulkWaitRead();")
         a("  __syncthreads();")
