@@ -22,10 +22,11 @@
 //           bulk copy each, issued as soon as the previous tile's mixing has read them;
 //   map     thread (face, q), faces ordered by orientation h so a warp mostly runs one branch:
 //           the trace row through fP_h diag(fM)^-1 in place (generated literal code);
-//   mix     thread (cell c, face i, octet of m): S for 8 m x 9 p in registers (flux matrices
-//           from shared memory); per column (p, c) the maximum over all faces and m (warp
-//           shuffles, then shared atomics) gives a power-of-two scale; S * 2^-e split into FP16
-//           hi + lo, the B operand (K-major), written over the trace buffer;
+//   mix     thread (cell c, face i = warp, group of KF / 4 m): S for those m x 9 p in registers
+//           (flux matrices from shared memory), all 128 threads busy; per column (p, c) the
+//           maximum over all faces and m (warp shuffles, then shared atomics) gives a
+//           power-of-two scale; S * 2^-e split into FP16 hi + lo, the B operand (K-major),
+//           written over the trace buffer;
 //   MMA     one thread: D = A_hi S_hi + A_hi S_lo + A_lo S_hi (FP32 accumulation in TMEM);
 //   epilogue  the next tile's gather is issued, then (.16x64b TMEM loads, all 32 threads of a
 //           warp) Q[c][p][k] += D[k, (p, c)] 2^{f_k} 2^{e_(p,c)} as f32 reductions performed in L2
@@ -65,8 +66,8 @@ struct NbtDims {
   static constexpr int KF = (FP + 7) / 8 * 8;   // K extent of one face
   static constexpr int K = 4 * KF;              // MMA K
   static constexpr int KC = K / 8;              // core-matrix chunks along K
-  static constexpr int OCT = KF / 8;            // octets of m per face
-  static constexpr int ITEMS = kNC * 4 * OCT;   // mixing threads
+  static constexpr int G = KF / 4;              // m per mixing thread: 4 groups per face, 128 threads
+  static constexpr int V = G % 4 == 0 ? 4 : 2;  // floats per vector load of a trace row
   static constexpr int CS = 4 * 9 * FP + 4;     // cell stride of the trace tile (floats; +4 spreads banks)
   static constexpr size_t kOpA = (size_t)64 * K * 2 * 2;
   static constexpr size_t kX = (size_t)kNC * CS * 4;
@@ -75,7 +76,7 @@ struct NbtDims {
   static constexpr size_t kAT = (size_t)kNC * 4 * 81 * 4;  // the tile's AminusT (or AplusT) rows
   static constexpr size_t kSmem = kOpA + kWG * (kWgBuf + 2 * kAT);
   static_assert(B <= 64, "M = 64 holds the basis");
-  static_assert(K % 16 == 0 && ITEMS % 32 == 0 && ITEMS <= 128, "whole MMA K steps and whole warps");
+  static_assert(K % 16 == 0 && G % 2 == 0 && G % V == 0, "whole MMA K steps, whole half2 pairs and vectors");
   static_assert(kX % 16 == 0 && kOpA % 1024 == 0 && kAT % 16 == 0, "16-byte regions");
 };
 
@@ -163,7 +164,7 @@ template <int ORD>
 __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const uint16_t* __restrict__ opA,
                                                         const float* __restrict__ scA) {
   using D = NbtDims<ORD>;
-  constexpr int B = D::B, Bp = D::Bp, F = D::F, FP = D::FP, KC = D::KC, OCT = D::OCT, CS = D::CS;
+  constexpr int B = D::B, Bp = D::Bp, F = D::F, FP = D::FP, KC = D::KC, CS = D::CS;
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ uint64_t mbarTab, mbarLdAll[kWG], mbarMmaAll[kWG], mbarAAll[kWG];
   __shared__ uint32_t tslot;
@@ -252,71 +253,93 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const u
                         4 * u + 3 < F ? s[4 * u + 3 < F ? 4 * u + 3 : 0] : 0.f);
     }
     wgSync(wg);
-    // ---- mix: S[m, (p, c)] for the 8 m of this thread's octet
+    // ---- mix: S[m, (p, c)] for the G = KF / 4 m of this thread's group: thread (cell c, face
+    // fi = warp, group mg = lane / 8), all 128 threads of the warpgroup busy
     ok = wgSyncAnd(wg, sei_tc::mbarWait(mbarA, aPhase, kMaxPolls));
     if (!ok) break;
     aPhase ^= 1;
     aPending = false;
-    const int c = wt & 7, g = wt >> 3, fi = g / OCT, oc = g % OCT;
-    float S[8][9];
+    constexpr int G = D::G, V = D::V;
+    const int c = wt & 7, fi = ww, mg = lane >> 3;
+    float S[G][9];
 #pragma unroll
-    for (int u = 0; u < 8; ++u)
+    for (int u = 0; u < G; ++u)
 #pragma unroll
       for (int p = 0; p < 9; ++p) S[u][p] = 0.f;
-    if (wt < D::ITEMS) {
-      if (A.aplus && c < cnt) {
-        // local flux of face fi from the cell's own trace: S += T_fi AplusT_fi (zero on DR faces)
-        const float* tr = A.trace + (((size_t)fi * A.ntotal + A.first + cell0 + c) * 9) * FP + 8 * oc;
-        const float* ap = Am + D::kAT / 4 + (c * 4 + fi) * 81;
+    if (A.aplus && c < cnt) {
+      // local flux of face fi from the cell's own trace: S += T_fi AplusT_fi (zero on DR faces)
+      const float* tr = A.trace + (((size_t)fi * A.ntotal + A.first + cell0 + c) * 9) * FP + G * mg;
+      const float* ap = Am + D::kAT / 4 + (c * 4 + fi) * 81;
 #pragma unroll 3
-        for (int q = 0; q < 9; ++q) {
-          float r[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      for (int q = 0; q < 9; ++q) {
+        float r[G];
 #pragma unroll
-          for (int h = 0; h < 2; ++h)
-            if (8 * oc + 4 * h < FP) {
-              const float4 y = __ldg(reinterpret_cast<const float4*>(tr + q * FP) + h);
+        for (int h = 0; h < G / V; ++h) {
+          if (G * mg + V * h < FP) {  // whole chunks inside the stored row
+            if constexpr (V == 4) {
+              const float4 y = __ldg(reinterpret_cast<const float4*>(tr + q * FP + 4 * h));
               r[4 * h] = y.x;
               r[4 * h + 1] = y.y;
               r[4 * h + 2] = y.z;
               r[4 * h + 3] = y.w;
+            } else {
+              const float2 y = __ldg(reinterpret_cast<const float2*>(tr + q * FP + 2 * h));
+              r[2 * h] = y.x;
+              r[2 * h + 1] = y.y;
             }
+          } else {
 #pragma unroll
-          for (int p = 0; p < 9; ++p) {
-            const float a = ap[q + 9 * p];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) S[u][p] = fmaf(r[u], a, S[u][p]);
+            for (int e = 0; e < V; ++e) r[V * h + e] = 0.f;
           }
         }
+#pragma unroll
+        for (int p = 0; p < 9; ++p) {
+          const float a = ap[q + 9 * p];
+#pragma unroll
+          for (int u = 0; u < G; ++u) S[u][p] = fmaf(r[u], a, S[u][p]);
+        }
       }
-      if (meta.reg[4 * c + fi]) {
-        const float* xr = X + c * CS + fi * 9 * FP + 8 * oc;
-        const float* am = Am + (c * 4 + fi) * 81;
+    }
+    if (meta.reg[4 * c + fi]) {
+      const float* xr = X + c * CS + fi * 9 * FP + G * mg;
+      const float* am = Am + (c * 4 + fi) * 81;
 #pragma unroll 3
-        for (int q = 0; q < 9; ++q) {
-          const float4 r0 = reinterpret_cast<const float4*>(xr + q * FP)[0];
-          const float4 r1 = reinterpret_cast<const float4*>(xr + q * FP)[1];
-          float r[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
+      for (int q = 0; q < 9; ++q) {
+        float r[G];
 #pragma unroll
-          for (int u = 0; u < 8; ++u)
-            if (8 * oc + u >= F) r[u] = 0.f;  // past the face basis (the next row at orders 4 and 5)
-#pragma unroll
-          for (int p = 0; p < 9; ++p) {
-            const float a = am[q + 9 * p];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) S[u][p] = fmaf(r[u], a, S[u][p]);
+        for (int h = 0; h < G / V; ++h) {
+          if constexpr (V == 4) {
+            const float4 y = reinterpret_cast<const float4*>(xr + q * FP)[h];
+            r[4 * h] = y.x;
+            r[4 * h + 1] = y.y;
+            r[4 * h + 2] = y.z;
+            r[4 * h + 3] = y.w;
+          } else {
+            const float2 y = reinterpret_cast<const float2*>(xr + q * FP)[h];
+            r[2 * h] = y.x;
+            r[2 * h + 1] = y.y;
           }
         }
-      }
-      // column maxima over this warp's faces and octets of cell c, then over the warps
 #pragma unroll
-      for (int p = 0; p < 9; ++p) {
-        float mx = 0.f;
+        for (int u = 0; u < G; ++u)
+          if (G * mg + u >= F) r[u] = 0.f;  // past the face basis (the next row at orders 4 and 5)
 #pragma unroll
-        for (int u = 0; u < 8; ++u) mx = fmaxf(mx, fabsf(S[u][p]));
-        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 8));
-        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
-        if (lane < 8) atomicMax(&smax[8 * p + c], __float_as_uint(mx));
+        for (int p = 0; p < 9; ++p) {
+          const float a = am[q + 9 * p];
+#pragma unroll
+          for (int u = 0; u < G; ++u) S[u][p] = fmaf(r[u], a, S[u][p]);
+        }
       }
+    }
+    // column maxima over this warp's groups of cell c, then over the warps (faces)
+#pragma unroll
+    for (int p = 0; p < 9; ++p) {
+      float mx = 0.f;
+#pragma unroll
+      for (int u = 0; u < G; ++u) mx = fmaxf(mx, fabsf(S[u][p]));
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 8));
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
+      if (lane < 8) atomicMax(&smax[8 * p + c], __float_as_uint(mx));
     }
     wgSync(wg);  // the maxima are complete and every read of the trace tile and flux matrices is done
     // the flux matrices of the warpgroup's next tile overlap the split, MMA and epilogue
@@ -325,23 +348,23 @@ __global__ void __launch_bounds__(128 * kWG, 1) sei_nbt(sei::TcNbArgs A, const u
       aPending = true;
     }
     if (wt < kCols) csc[wt] = sei_tc::pow2(sei_tc::pow2Exp(__uint_as_float(smax[wt])));
-    if (wt < D::ITEMS) {
+    {
+      // K index fi KF + G mg + u; the core matrix of 8 k holds k % 8 at 2-byte steps, so each
+      // pair (u, u + 1) is one aligned 4-byte store
 #pragma unroll
       for (int p = 0; p < 9; ++p) {
         const float sc = sei_tc::pow2(-sei_tc::pow2Exp(__uint_as_float(smax[8 * p + c])));
-        uint32_t hw[4], lw[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const float x0 = S[2 * u][p] * sc, x1 = S[2 * u + 1][p] * sc;
+        for (int u = 0; u < G; u += 2) {
+          const float x0 = S[u][p] * sc, x1 = S[u + 1][p] * sc;
           const __half2 h2 = __floats2half2_rn(x0, x1);
           const float2 b2 = __half22float2(h2);
           const __half2 l2 = __floats2half2_rn(x0 - b2.x, x1 - b2.y);
-          hw[u] = *reinterpret_cast<const uint32_t*>(&h2);
-          lw[u] = *reinterpret_cast<const uint32_t*>(&l2);
+          const int kk = fi * D::KF + G * mg + u;
+          const uint32_t off = ((uint32_t)(p * KC + kk / 8) * 128 + (uint32_t)c * 16) / 2 + (uint32_t)(kk % 8);
+          *reinterpret_cast<__half2*>(bHi + off) = h2;
+          *reinterpret_cast<__half2*>(bLo + off) = l2;
         }
-        const uint32_t off = ((uint32_t)(p * KC + fi * OCT + oc) * 128 + (uint32_t)c * 16) / 2;
-        *reinterpret_cast<uint4*>(bHi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-        *reinterpret_cast<uint4*>(bLo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
       }
     }
     sei_tc::fenceProxyAsync();
