@@ -217,6 +217,27 @@ int allocArrays(sei_ctx* c, int64_t n) {
   return SEI_OK;
 }
 
+// The checks of a caller's cell data, made before anything of the context changes: face types,
+// neighbours and relations in range, the used star entries finite.
+int validateCells(sei_ctx* c, int64_t n, const float* star, const int32_t* nbr, const int8_t* side, const int8_t* orient,
+                  const int8_t* ftype) {
+  if (n <= 0 || n > INT32_MAX) return fail(c, SEI_ERR_ARG, "cell count out of range");
+  for (int64_t i = 0; i < n * 4; ++i) {
+    if (ftype[i] < 0 || ftype[i] > 2) return fail(c, SEI_ERR_ARG, "face_type must be 0, 1 or 2");
+    if (ftype[i] == 0) {
+      if (nbr[i] < 0 || nbr[i] >= n) return fail(c, SEI_ERR_ARG, "regular face with neighbour out of range");
+      if (side[i] < 0 || side[i] > 3 || orient[i] < 0 || orient[i] > 2)
+        return fail(c, SEI_ERR_ARG, "face relation out of range (side 0..3, orientation 0..2)");
+    }
+  }
+  for (int64_t i = 0; i < n; ++i)
+    for (int e = 0; e < 3; ++e)
+      for (int z = 0; z < sei::kStarNnz; ++z)
+        if (!std::isfinite(star[(i * 3 + e) * 81 + sei::kStarNz[z][0] + 9 * sei::kStarNz[z][1]]))
+          return fail(c, SEI_ERR_NAN, "non-finite star matrix entry");
+  return SEI_OK;
+}
+
 int uploadCells(sei_ctx* c, int64_t n, const float* star, const float* aplus, const float* aminus,
                 const int32_t* nbr, const int8_t* side, const int8_t* orient, const int8_t* ftype) {
   std::vector<float> snz((size_t)n * 3 * sei::kStarNnz);
@@ -648,7 +669,9 @@ int sei_set_cells(sei_ctx* c, int64_t n, const float* star, const float* aplus, 
                   const int32_t* neighbor, const int8_t* side, const int8_t* orient, const int8_t* face_type) {
   if (!c || !star || !aplus || !aminus || !neighbor || !side || !orient || !face_type) return SEI_ERR_ARG;
   if (c->cfg.device < 0) return fail(c, SEI_ERR_STATE, "host-only context (device < 0) cannot hold cells");
-  int rc = allocArrays(c, n);
+  int rc = validateCells(c, n, star, neighbor, side, orient, face_type);  // a rejected call changes nothing
+  if (rc) return rc;
+  rc = allocArrays(c, n);
   if (rc) return rc;
   c->has_mesh = false;
   return uploadCells(c, n, star, aplus, aminus, neighbor, side, orient, face_type);
