@@ -618,6 +618,54 @@ def dr_measurement(local, steps, order=4, dims=None, plane=3, warm_precision=0, 
     return res
 
 
+def lsw_measurement(local, steps, order=4, dims=None, plane=3):
+    """The fault workload with linear slip weakening instead of rate and state: elastic order 4,
+    300,000 tets, a planar fault of 20,000 faces x 25 points, mu_s 0.677, mu_d 0.525, d_c 0.01 m,
+    sn0 ~ U[-125, -115] MPa, tau1_0 ~ U[62, 78] MPa, forced rupture at t = 0 on the faces of the
+    first tenth of the fault (a strip), kernel all_dr, `steps` steps timed with CUDA events; one
+    more profiled step gives the fault kernel's time.  Reported beside the rate-and-state numbers:
+    the law's own cost, the share of points that ruptured, and the accumulated slip."""
+    import numpy as np
+
+    from seissol_gb300 import Context, LSWParams
+
+    dims = dims or DR_DIMS
+    nb3 = order * (order + 1) * (order + 2) // 6
+    ctx = Context(order, device=local)
+    n = ctx.build_periodic_cube(*dims, perturb=0.0, seed=DR_SEED + 1, fault_plane=plane)
+    nf = ctx.dr_setup_lsw(LSWParams.fault_config(law=1, seed=DR_SEED + 3))
+    npts = (order + 1) ** 2
+    tf = np.full((nf, npts), 1e300)
+    tf[: nf // 10] = 0.0
+    ctx.dr_set_state("forced_rupture_time", tf)
+    rng = np.random.default_rng(DR_SEED + 1)
+    ctx.set_dofs(rng.uniform(-1, 1, (n, 9, nb3)).astype(np.float32))
+    dt = ctx.cfl_timestep(0.5)
+    ctx.run("all_dr", dt, 3)  # warm-up
+    ctx.sync()
+    ctx.run("all_dr", dt, steps)
+    ctx.sync()
+    ms = ctx.last_run_ms()
+    ctx.set_profiling(True)
+    ctx.run("all_dr", dt, 1)
+    ctx.sync()
+    by_kind = ctx.kernel_times_by_kind()
+    trup = ctx.dr_state("rupture_time")
+    slip = ctx.dr_state("slip")
+    res = {"workload": f"elastic order {order}, {n:,}-tet periodic cube {dims[0]}x{dims[1]}x{dims[2]} cubes, planar "
+                       f"fault of {nf:,} faces x {npts} points, linear slip weakening (mu_s 0.677, mu_d 0.525, "
+                       "d_c 0.01 m, sn0 ~ U[-125,-115] MPa, tau1_0 ~ U[62,78] MPa), forced rupture at t = 0 on "
+                       f"the first tenth of the faces, kernel all_dr, {steps} steps after 3 warm-up steps",
+           "cells": n, "faces": nf, "steps": steps, "ms_per_step": ms / steps,
+           "cell_updates_per_s": n * steps / (ms / 1e3), "face_updates_per_s": nf * steps / (ms / 1e3),
+           "fault_kernel_ms": by_kind["fault"][0],
+           "kernel_ms_one_step": {k: v[0] for k, v in by_kind.items() if v[1] > 0},
+           "ruptured_point_share": float((trup >= 0).mean()), "mean_slip_m": float(np.abs(slip).mean()),
+           "fault_time_s": ctx.dr_time()}
+    ctx.close()
+    return res
+
+
 def lts_fault_measurement(local, cycles):
     """The combined configuration with local time stepping: elastic order 6, 1,000,000 tets of a
     graded periodic cube (8 x 100 x 250 cubes, the LTS mesh profile along z: edges in four bands
@@ -900,6 +948,7 @@ def run_ours(args, world, rank, local):
     dr = None
     if rank == 0 and args.dr_steps > 0:
         dr = dr_measurement(local, args.dr_steps)
+        dr["linear_slip_weakening"] = lsw_measurement(local, args.dr_steps)
     lts = None
     if rank == 0 and args.lts_cycles > 0:
         lts = lts_measurement(local, args.lts_cycles)

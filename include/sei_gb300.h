@@ -121,6 +121,54 @@ typedef struct sei_rs_params {
 #define SEI_DR_SN0 10
 #define SEI_DR_TAU1_0 11
 #define SEI_DR_TAU2_0 12
+/* Linear slip weakening (sei_dr_setup_lsw): static and dynamic friction coefficients, critical slip
+ * distance, cohesion, forced rupture time (LTSLinearSlipWeakening, MuS .. ForcedRuptureTime). */
+#define SEI_DR_MU_S 13
+#define SEI_DR_MU_D 14
+#define SEI_DR_D_C 15
+#define SEI_DR_COHESION 16
+#define SEI_DR_FORCED_RUPTURE_TIME 17
+/* Outputs of both laws (BaseFrictionLaw.h:127-134): peak slip rate, rupture time (slip rate above
+ * 1e-3 m/s for the first time) and, slip weakening only, dynamic stress time (accumulated slip
+ * reaches d_c); a time is the start of the time point and is negative while pending. */
+#define SEI_DR_PEAK_SLIP_RATE 18
+#define SEI_DR_RUPTURE_TIME 19
+#define SEI_DR_DYN_STRESS_TIME 20
+/* Nucleation stresses added to sn0, tau1_0, tau2_0 over [s0, s0 + t0] (sei_dr_set_nucleation). */
+#define SEI_DR_NUC_SN 21
+#define SEI_DR_NUC_TAU1 22
+#define SEI_DR_NUC_TAU2 23
+/* Regularised strength of the bimaterial law (LTSLinearSlipWeakeningBimaterial::RegularizedStrength). */
+#define SEI_DR_REG_STRENGTH 24
+#define SEI_DR_NUM_FIELDS 25
+
+/* Friction laws (src/Initializer/Parameters/DRParameters.h FrictionLawType): rate and state with
+ * fast velocity weakening (FL 103, sei_dr_setup); linear slip weakening (FL 16 and FL 2), its
+ * bimaterial form with the Prakash-Clifton regularised strength (FL 6) and the thermal-pressurisation
+ * proxy (FL 1058), all three with sei_dr_setup_lsw. */
+#define SEI_LAW_FVW 0
+#define SEI_LAW_LSW 1
+#define SEI_LAW_LSW_BIMATERIAL 2
+#define SEI_LAW_LSW_TP_PROXY 3
+
+/* Linear-slip-weakening parameters: per-point fields start uniform (mu_s, mu_d, d_c, cohesion,
+ * forced_rupture_time) or seeded uniform random (sn0 in [sn_min, sn_max] <= 0, tau1_0 in
+ * [tau_min, tau_max], tau2_0 = 0), all settable per point with sei_dr_set_state.  t0 is t_0 of the
+ * parameter file: the ramp of the forced rupture (0: a step at the forced rupture time) and the
+ * nucleation duration; healing_threshold is lsw_healingthreshold (-1: no healing); v_star and
+ * prakash_length the Prakash-Clifton constants (pc_vstar, pc_prakashlength; law 2);
+ * tp_proxy_exponent tpproxyexponent (law 3; reference default 1/3). */
+typedef struct sei_lsw_params {
+  int law;
+  double mu_s, mu_d, d_c, cohesion;
+  double sn_min, sn_max, tau_min, tau_max;
+  double forced_rupture_time;
+  double t0;
+  double healing_threshold;
+  double v_star, prakash_length;
+  double tp_proxy_exponent;
+  uint64_t seed;
+} sei_lsw_params;
 
 /* PerformanceEstimate of the reference (src/Monitoring/Metric.h:8-60), per cell and step. */
 typedef struct sei_perf {
@@ -294,6 +342,25 @@ int sei_lts_permutation(sei_ctx* ctx, int64_t* perm /*[n]*/);
  * the fault kernel (interpolation at the Gauss-Legendre time points, friction, imposed state,
  * nodal flux into both cells), the neighbour flux of the regular faces. */
 int sei_dr_setup(sei_ctx* ctx, const sei_rs_params* p, int64_t* nfaces);
+/* The fault with linear slip weakening (src/DynamicRupture/FrictionLaws/CpuImpl/LinearSlipWeakening.h:27-170):
+ * per time point the strength -cohesion - mu min(sn, 0), the slip rate max(0, (|tau| - strength) / eta_s),
+ * the accumulated slip (grown by the slip rate resampled over the face for SEI_LAW_LSW, by the slip
+ * rate itself for the other two), the state from it and the forced rupture, mu = mu_s - (mu_s - mu_d)
+ * state, healing.  Replaces an earlier fault set-up of the context; SEI_DR_SLIP holds the
+ * accumulated slip magnitude, SEI_DR_PSI and SEI_DR_A are unused. */
+int sei_dr_setup_lsw(sei_ctx* ctx, const sei_lsw_params* p, int64_t* nfaces);
+/* Friction law of the fault (SEI_LAW_*), -1 without one. */
+int sei_dr_law(const sei_ctx* ctx);
+/* Gaussian nucleation (FrictionSolverCommon.h:503-531 with src/Numerical/GaussianNucleationFunction.h):
+ * at every time point ending at t in [s0, s0 + t0] the initial stresses grow by the nucleation
+ * fields SEI_DR_NUC_* times smoothStep(t - s0) - smoothStep(t - s0 - dt), one nucleation as the
+ * parameter file's default nucleationcount.  t0 is shared with the slip-weakening forced-rupture
+ * ramp, as t_0 in the reference.  on = 0 turns it off (t0, s0 ignored). */
+int sei_dr_set_nucleation(sei_ctx* ctx, int on, double t0, double s0);
+/* Fault time: 0 after a fault set-up, advanced by dt per step (by the cycle length per LTS cycle);
+ * the forced rupture, the nucleation and the output times read it. */
+int sei_dr_get_time(sei_ctx* ctx, double* t);
+int sei_dr_set_time(sei_ctx* ctx, double t);
 int sei_dr_num_points(int order);
 int64_t sei_dr_num_faces(const sei_ctx* ctx);
 /* Per face: cells [nf][2] (plus, minus), sides [nf][3] (plus side, minus side, face relation 1..3),

@@ -15,6 +15,15 @@
  *   imposed state        FrictionSolverCommon.h:333-420
  *   nodal flux           dynamic_rupture.py:174-190 (Q += V3mTo2nTWDivM(side, rel) . imposed . fluxSolver)
  *   time sub-steps       src/DynamicRupture/FrictionLaws/FrictionSolver.cpp:20-37
+ *   evaluate loop        CpuImpl/BaseFrictionLaw.h:49-160 (per time point: nucleation, friction,
+ *                        rupture-front, dynamic-stress and peak-slip-rate outputs)
+ *   nucleation           FrictionSolverCommon.h:503-531 (adjustInitialStress) with the smooth step
+ *                        of src/Numerical/GaussianNucleationFunction.h
+ *   linear slip weakening CpuImpl/LinearSlipWeakening.h (strength, slip rate and traction,
+ *                        state from the accumulated slip with forced rupture, friction with
+ *                        healing) and its specialisations NoSpecialization (resampled slip rate,
+ *                        LinearSlipWeakening.cpp), BiMaterialFault (Prakash-Clifton regularised
+ *                        strength) and TPApprox; initial values LinearSlipWeakeningInitializer.cpp:24-50
  *
  * Layouts: per fault face, QInterpolated[ts][9][npts] (points fastest, as the reference's
  * QInterpolated view), imposed state [9][npts]; 9x9 matrices column-major (q + 9 p);
@@ -90,6 +99,45 @@ typedef struct {
 typedef struct {
   double zp, zs, zpn, zsn, etap, etas, inv_etas;
 } oracle_imp;
+
+/* Fault time, nucleation, outputs and linear-slip-weakening fields of one fault step (all
+ * per-point arrays [nfaces][npts], nucleation stresses [nfaces][3][npts] as init). */
+typedef struct {
+  double time;     /* fault time at the start of the step */
+  double t0, s0;   /* nucleation duration and start; t0 also ramps the forced rupture */
+  int nucleate;    /* nonzero: add nuc x the smooth-step increment to the initial stresses */
+  const double* nuc;
+  double* peak;    /* peak slip rate */
+  double* trup;    /* rupture time, negative while pending */
+  double* tdyn;    /* dynamic stress time (slip weakening), negative while pending */
+  int law;         /* 1 linear slip weakening, 2 bimaterial (Prakash-Clifton), 3 TP proxy */
+  double healing, v_star, prakash_length, tp_exponent;
+  const double *mu_s, *mu_d, *d_c, *cohesion, *t_forced;
+  double* reg;     /* regularised strength (law 2) */
+} oracle_dr_aux;
+
+/* smoothStep and the nucleation of one time point ending at t_end over dt. */
+static double smooth_step(double t, double t0) {
+  if (t <= 0) return 0.0;
+  if (t < t0) {
+    const double tau = t - t0;
+    return exp(tau * tau / (t * (t - 2 * t0)));
+  }
+  return 1.0;
+}
+
+static void nucleate(const oracle_dr_aux* x, int64_t f, int npts, double* init, double t_end, double dt) {
+  if (!x || !x->nucleate || !(t_end <= x->t0 + x->s0 && t_end >= x->s0)) return;
+  const double g = smooth_step(t_end - x->s0, x->t0) - smooth_step(t_end - x->s0 - dt, x->t0);
+  for (int i = 0; i < 3 * npts; ++i) init[(size_t)f * 3 * npts + i] += x->nuc[(size_t)f * 3 * npts + i] * g;
+}
+
+/* Rupture-front and peak-slip-rate outputs of one point (FrictionSolverCommon.h:546-592). */
+static void outputs(const oracle_dr_aux* x, size_t i, double v, double t_start) {
+  if (!x) return;
+  if (x->trup && x->trup[i] < 0 && v > 0.001) x->trup[i] = t_start;
+  if (x->peak && v > x->peak[i]) x->peak[i] = v;
+}
 
 static double sq(double x) { return x * x; }
 
@@ -239,12 +287,12 @@ double oracle_mlp_forward(const float* w, const float* norm, double sn, double t
  * appended as [6] floats at rec[(*rec_count)++] (up to rec_cap). */
 
 void oracle_dr_friction(int npts, int nts, int64_t nfaces, const oracle_rs_params* P, const oracle_imp* imp,
-                        const real* qip, const real* qim, const double* a, const double* init, double* psi,
+                        const real* qip, const real* qim, const double* a, double* init, double* psi,
                         double* v1, double* v2, double* slip1, double* slip2, double* slip, double* mu,
                         double* trac1, double* trac2, const double* deltat, const double* tweights,
                         const double* resample, real* isp, real* ism, int64_t* newton_iters,
                         const float* mlp, const float* mlp_norm, int64_t* first_iters, float* rec,
-                        int64_t rec_cap, int64_t* rec_count) {
+                        int64_t rec_cap, int64_t* rec_count, const oracle_dr_aux* aux) {
 #pragma omp parallel
   {
     double* buf = (double*)malloc(sizeof(double) * (size_t)npts * 12);
@@ -277,8 +325,10 @@ void oracle_dr_friction(int npts, int nts, int64_t nfaces, const oracle_rs_param
         }
       }
       for (int k = 0; k < npts; ++k) psib[k] = psi[fo + k];
+      double t_start = aux ? aux->time : 0.0;
       for (int s = 0; s < nts; ++s) {
         const double dt = deltat[s];
+        nucleate(aux, f, npts, init, t_start + dt, dt);
         for (int k = 0; k < npts; ++k) {
           const double sn0 = init[(size_t)f * 3 * npts + k];
           const double t10 = init[(size_t)f * 3 * npts + npts + k];
@@ -364,7 +414,9 @@ void oracle_dr_friction(int npts, int nts, int64_t nfaces, const oracle_rs_param
           tr[(1 * nts + s) * npts + k] = tr2;
           v1[fo + k] = sr1;
           v2[fo + k] = sr2;
+          outputs(aux, fo + k, vmag[k], t_start);
         }
+        t_start += dt;
       }
       /* resample the state variable increment (FastVelocityWeakeningLaw.h:98-106) */
       for (int k = 0; k < npts; ++k) dpsi[k] = psib[k] - psi[fo + k];
@@ -413,6 +465,139 @@ void oracle_dr_friction(int npts, int nts, int64_t nfaces, const oracle_rs_param
     free(convo);
   }
 }
+
+#define QP(q) ((double)P_[k + (size_t)npts * (q)])
+#define QM(q) ((double)M_[k + (size_t)npts * (q)])
+/* Linear slip weakening, one time step of all faces (CpuImpl/LinearSlipWeakening.h:27-170 inside
+ * the evaluate loop of CpuImpl/BaseFrictionLaw.h:49-160).  Per time point: nucleation of the
+ * initial stresses; strength -cohesion - mu min(sn_total, 0) (law 2: regularised towards it with
+ * exp(-(max(V_prev, 0) + v_star) dt / L), BiMaterialFault::strengthHook); slip rate
+ * max(0, (|tau_total| - strength) / eta_s) split along the total traction; tractions and slips;
+ * the accumulated slip grows by the slip rate resampled over the face (law 1, resample matrix) or
+ * by the slip rate itself (laws 2, 3); state min(|slip| / d_c, 1) (law 3: 1 - (1 + |slip| /
+ * d_c)^-p), at least the forced-rupture ramp of the time point's end; mu = mu_s - (mu_s - mu_d)
+ * state, back to mu_s where the peak slip rate passed the healing threshold and the slip rate is
+ * below it; outputs.  State fields as oracle_dr_friction, slip = accumulated slip magnitude. */
+void oracle_dr_friction_lsw(int npts, int nts, int64_t nfaces, const oracle_imp* imp, const real* qip, const real* qim,
+                            double* init, double* v1, double* v2, double* slip1, double* slip2, double* slip,
+                            double* mu, double* trac1, double* trac2, const double* deltat, const double* tweights,
+                            const double* resample, real* isp, real* ism, const oracle_dr_aux* x) {
+  double* fs = (double*)malloc(sizeof(double) * 3 * (size_t)nts * npts);
+  double* tr = (double*)malloc(sizeof(double) * 2 * (size_t)nts * npts);
+  double* vm = (double*)malloc(sizeof(double) * (size_t)npts);
+  double* rv = (double*)malloc(sizeof(double) * (size_t)npts);
+  double* isacc = (double*)malloc(sizeof(double) * 18 * (size_t)npts);
+  for (int64_t f = 0; f < nfaces; ++f) {
+    const oracle_imp* im = imp + f;
+    const size_t fo = (size_t)f * npts;
+    for (int s = 0; s < nts; ++s) {
+      const real* P_ = qip + ((size_t)f * nts + s) * 9 * npts;
+      const real* M_ = qim + ((size_t)f * nts + s) * 9 * npts;
+      for (int k = 0; k < npts; ++k) {
+        fs[(0 * nts + s) * npts + k] = im->etap * (QM(6) - QP(6) + QP(0) / im->zp + QM(0) / im->zpn);
+        fs[(1 * nts + s) * npts + k] = im->etas * (QM(7) - QP(7) + QP(3) / im->zs + QM(3) / im->zsn);
+        fs[(2 * nts + s) * npts + k] = im->etas * (QM(8) - QP(8) + QP(5) / im->zs + QM(5) / im->zsn);
+      }
+    }
+    /* slip-rate magnitude of the previous time point (the bimaterial strength reads it) */
+    for (int k = 0; k < npts; ++k) vm[k] = sqrt(v1[fo + k] * v1[fo + k] + v2[fo + k] * v2[fo + k]);
+    double t_start = x->time;
+    for (int s = 0; s < nts; ++s) {
+      const double dt = deltat[s], t_end = t_start + dt;
+      nucleate(x, f, npts, init, t_end, dt);
+      for (int k = 0; k < npts; ++k) {
+        const double* in = init + (size_t)f * 3 * npts;
+        const double sn = in[k] + fs[(0 * nts + s) * npts + k];
+        double strength = -x->cohesion[fo + k] - mu[fo + k] * (sn < 0 ? sn : 0.0);
+        if (x->law == 2) {
+          const double e = -((vm[k] > 0 ? vm[k] : 0.0) + x->v_star) * dt / x->prakash_length;
+          strength = x->reg[fo + k] * exp(e) + strength * -expm1(e);
+          x->reg[fo + k] = strength;
+        }
+        const double st1 = fs[(1 * nts + s) * npts + k], st2 = fs[(2 * nts + s) * npts + k];
+        const double tt1 = in[npts + k] + st1, tt2 = in[2 * npts + k] + st2;
+        const double tau = sqrt(tt1 * tt1 + tt2 * tt2);
+        double v = (tau - strength) * im->inv_etas;
+        v = v > 0 ? v : 0.0;
+        const double div = strength + im->etas * v;
+        const double sr1 = v * tt1 / div, sr2 = v * tt2 / div;
+        v1[fo + k] = sr1;
+        v2[fo + k] = sr2;
+        const double t1 = st1 - im->etas * sr1, t2 = st2 - im->etas * sr2;
+        trac1[fo + k] = t1;
+        trac2[fo + k] = t2;
+        tr[(0 * nts + s) * npts + k] = t1;
+        tr[(1 * nts + s) * npts + k] = t2;
+        slip1[fo + k] += sr1 * dt;
+        slip2[fo + k] += sr2 * dt;
+        vm[k] = v;
+      }
+      for (int k = 0; k < npts; ++k) {
+        double r = vm[k];
+        if (x->law == 1) {
+          r = 0;
+          for (int j = 0; j < npts; ++j) r += resample[k + (size_t)npts * j] * vm[j];
+        }
+        rv[k] = r;
+      }
+      for (int k = 0; k < npts; ++k) {
+        const size_t i = fo + k;
+        slip[i] += rv[k] * dt;
+        const double ratio = fabs(slip[i]) / x->d_c[i];
+        double state = x->law == 3 ? 1.0 - pow(1.0 + ratio, -x->tp_exponent) : (ratio < 1.0 ? ratio : 1.0);
+        double f2;
+        if (x->t0 == 0) {
+          f2 = t_end >= x->t_forced[i] ? 1.0 : 0.0;
+        } else {
+          f2 = (t_end - x->t_forced[i]) / x->t0;
+          f2 = f2 < 0 ? 0.0 : (f2 > 1 ? 1.0 : f2);
+        }
+        state = state > f2 ? state : f2;
+        mu[i] = x->mu_s[i] - (x->mu_s[i] - x->mu_d[i]) * state;
+        if (x->peak[i] > x->healing && vm[k] < x->healing) mu[i] = x->mu_s[i];
+        outputs(x, i, vm[k], t_start);
+        if (x->tdyn && x->tdyn[i] < 0 && fabs(slip[i]) >= x->d_c[i]) x->tdyn[i] = t_start;
+      }
+      t_start = t_end;
+    }
+    /* imposed state (FrictionSolverCommon.h:333-420) */
+    memset(isacc, 0, sizeof(double) * 18 * (size_t)npts);
+    for (int s = 0; s < nts; ++s) {
+      const double w = tweights[s];
+      const real* P_ = qip + ((size_t)f * nts + s) * 9 * npts;
+      const real* M_ = qim + ((size_t)f * nts + s) * 9 * npts;
+      for (int k = 0; k < npts; ++k) {
+        const double sn = fs[(0 * nts + s) * npts + k];
+        const double t1 = tr[(0 * nts + s) * npts + k], t2 = tr[(1 * nts + s) * npts + k];
+        double* m_ = isacc;
+        double* p_ = isacc + 9 * npts;
+        m_[0 * npts + k] += w * sn;
+        m_[3 * npts + k] += w * t1;
+        m_[5 * npts + k] += w * t2;
+        m_[6 * npts + k] += w * (QM(6) - (sn - QM(0)) / im->zpn);
+        m_[7 * npts + k] += w * (QM(7) - (t1 - QM(3)) / im->zsn);
+        m_[8 * npts + k] += w * (QM(8) - (t2 - QM(5)) / im->zsn);
+        p_[0 * npts + k] += w * sn;
+        p_[3 * npts + k] += w * t1;
+        p_[5 * npts + k] += w * t2;
+        p_[6 * npts + k] += w * (QP(6) + (sn - QP(0)) / im->zp);
+        p_[7 * npts + k] += w * (QP(7) + (t1 - QP(3)) / im->zs);
+        p_[8 * npts + k] += w * (QP(8) + (t2 - QP(5)) / im->zs);
+      }
+    }
+    for (int i = 0; i < 9 * npts; ++i) {
+      ism[(size_t)f * 9 * npts + i] = (real)isacc[i];
+      isp[(size_t)f * 9 * npts + i] = (real)isacc[9 * npts + i];
+    }
+  }
+  free(fs);
+  free(tr);
+  free(vm);
+  free(rv);
+  free(isacc);
+}
+#undef QP
+#undef QM
 
 /* Q(cell) += V3mTo2nTWDivM(side, rel) . imposed . fluxSolver for one side of every face. */
 void oracle_dr_nodal_flux(int order, int npts, int64_t nfaces, const int32_t* cell, const int8_t* side,

@@ -121,6 +121,34 @@ class RSParamsC(C.Structure):
 STATE_FIELDS = ("psi", "v1", "v2", "slip1", "slip2", "slip", "mu", "trac1", "trac2")
 
 
+class DrAuxC(C.Structure):
+    """oracle_dr_aux: fault time, nucleation, outputs and the slip-weakening fields."""
+    _fields_ = [("time", C.c_double), ("t0", C.c_double), ("s0", C.c_double), ("nucleate", C.c_int),
+                ("nuc", C.c_void_p), ("peak", C.c_void_p), ("trup", C.c_void_p), ("tdyn", C.c_void_p),
+                ("law", C.c_int), ("healing", C.c_double), ("v_star", C.c_double), ("prakash_length", C.c_double),
+                ("tp_exponent", C.c_double), ("mu_s", C.c_void_p), ("mu_d", C.c_void_p), ("d_c", C.c_void_p),
+                ("cohesion", C.c_void_p), ("t_forced", C.c_void_p), ("reg", C.c_void_p)]
+
+
+AUX_ARRAYS = ("nuc", "peak", "trup", "tdyn", "mu_s", "mu_d", "d_c", "cohesion", "t_forced", "reg")
+
+
+def _aux_struct(aux):
+    """Builds DrAuxC from a dict (scalars: time, t0, s0, nucleate, law, healing, v_star,
+    prakash_length, tp_exponent; float64 arrays [nf, npts], nuc [nf, 3, npts], converted in place)."""
+    if aux is None:
+        return None
+    for k in AUX_ARRAYS:
+        if aux.get(k) is not None:
+            aux[k] = np.ascontiguousarray(aux[k], np.float64)
+    ptr = lambda k: aux[k].ctypes.data if aux.get(k) is not None else None
+    return DrAuxC(aux.get("time", 0.0), aux.get("t0", 0.0), aux.get("s0", 0.0), int(aux.get("nucleate", 0)),
+                  ptr("nuc"), ptr("peak"), ptr("trup"), ptr("tdyn"), int(aux.get("law", 0)),
+                  aux.get("healing", -1.0), aux.get("v_star", 0.0), aux.get("prakash_length", 1.0),
+                  aux.get("tp_exponent", 1.0 / 3.0), ptr("mu_s"), ptr("mu_d"), ptr("d_c"), ptr("cohesion"),
+                  ptr("t_forced"), ptr("reg"))
+
+
 def dr_collocation(order, dt):
     """Time points, weights, friction sub-steps and collocation coefficients t_s^p / p!."""
     tp, tw = dg_setup.gauss_legendre_time(order, dt)
@@ -141,9 +169,11 @@ class DROracle:
         self.tw = np.ascontiguousarray(np.stack([np.asfortranarray(v).ravel(order="F") for v in m["V3mTo2nTWDivM"]]))
         self.res = np.ascontiguousarray(np.asfortranarray(m["resample"]).ravel(order="F"))
         self.f = faces
-        self.P = RSParamsC(params["f0"], params["b"], params["v0"], params["l"], params["muw"], params["vw"],
-                           params["newton_tol"], params["state_tol"], params["max_newton"], params["max_outer"])
-        for fn in ("oracle_dr_interpolate", "oracle_dr_friction", "oracle_dr_nodal_flux", "oracle_dr_precompute"):
+        # rate-and-state constants (unused by the slip-weakening laws, which may pass {})
+        self.P = RSParamsC(*[params.get(k, 0) for k in ("f0", "b", "v0", "l", "muw", "vw", "newton_tol", "state_tol",
+                                                         "max_newton", "max_outer")])
+        for fn in ("oracle_dr_interpolate", "oracle_dr_friction", "oracle_dr_friction_lsw", "oracle_dr_nodal_flux",
+                   "oracle_dr_precompute"):
             getattr(self.L, fn).restype = None
 
     def interpolate(self, derivs_per_face, side, rel, coll):
@@ -159,8 +189,12 @@ class DROracle:
                                      _p(tinvt), _p(self.v3m), _p(np.ascontiguousarray(coll, np.float64)), _p(out))
         return out
 
-    def friction(self, qip, qim, state, a, init, deltat, tweights, mlp=None, record=None, first_iters=None):
+    def friction(self, qip, qim, state, a, init, deltat, tweights, mlp=None, record=None, first_iters=None,
+                 aux=None):
         """Updates state (dict of [nf, npts] float64 arrays) in place; returns imposed states and iterations.
+
+        init [nf, 3, npts] (sn0, tau1_0, tau2_0) changes in place under nucleation; aux: optional
+        dict of the fault time, nucleation and outputs (_aux_struct).
 
         record: optional [cap, 6] float32 array with a one-element int64 counter, (rec, count),
         receiving the samples of plainly started, converged first solves; first_iters: optional
@@ -173,13 +207,15 @@ class DROracle:
         iters = np.zeros((nf, self.npts), np.int64)
         for k in STATE_FIELDS:
             state[k] = np.ascontiguousarray(state[k], np.float64)
+        initc = np.ascontiguousarray(init, np.float64)
+        ax = _aux_struct(aux)
         w = n = None
         if mlp is not None:
             w = np.ascontiguousarray(mlp[0], np.float32)
             n = np.ascontiguousarray(mlp[1], np.float32)
         self.L.oracle_dr_friction(self.npts, nts, C.c_int64(nf), C.byref(self.P), _p(imp),
                                   _p(np.ascontiguousarray(qip, self.dtype)), _p(np.ascontiguousarray(qim, self.dtype)),
-                                  _p(np.ascontiguousarray(a, np.float64)), _p(np.ascontiguousarray(init, np.float64)),
+                                  _p(np.ascontiguousarray(a, np.float64)), _p(initc),
                                   *[_p(state[k]) for k in STATE_FIELDS],
                                   _p(np.ascontiguousarray(deltat, np.float64)),
                                   _p(np.ascontiguousarray(tweights, np.float64)), _p(self.res), _p(isp), _p(ism),
@@ -187,8 +223,34 @@ class DROracle:
                                   _p(first_iters) if first_iters is not None else None,
                                   _p(record[0]) if record is not None else None,
                                   C.c_int64(record[0].shape[0] if record is not None else 0),
-                                  _p(record[1]) if record is not None else None)
+                                  _p(record[1]) if record is not None else None,
+                                  C.byref(ax) if ax is not None else None)
+        if initc is not init:
+            init[...] = initc
         return isp, ism, iters
+
+    def friction_lsw(self, qip, qim, state, init, deltat, tweights, aux):
+        """Linear slip weakening (aux["law"] 1, 2 or 3): updates state, init and the aux arrays in
+        place; returns the imposed states."""
+        nf = qip.shape[0]
+        nts = qip.shape[1]
+        imp = np.ascontiguousarray(self.f["imp"][:, :7], np.float64)
+        isp = np.zeros((nf, 9, self.npts), self.dtype)
+        ism = np.zeros((nf, 9, self.npts), self.dtype)
+        for k in STATE_FIELDS:
+            state[k] = np.ascontiguousarray(state[k], np.float64)
+        initc = np.ascontiguousarray(init, np.float64)
+        ax = _aux_struct(aux)
+        self.L.oracle_dr_friction_lsw(self.npts, nts, C.c_int64(nf), _p(imp),
+                                      _p(np.ascontiguousarray(qip, self.dtype)),
+                                      _p(np.ascontiguousarray(qim, self.dtype)), _p(initc),
+                                      *[_p(state[k]) for k in STATE_FIELDS[1:]],
+                                      _p(np.ascontiguousarray(deltat, np.float64)),
+                                      _p(np.ascontiguousarray(tweights, np.float64)), _p(self.res), _p(isp), _p(ism),
+                                      C.byref(ax))
+        if initc is not init:
+            init[...] = initc
+        return isp, ism
 
     def nodal_flux(self, Q, cells, side, rel, imposed, flux):
         Q = np.array(Q, dtype=self.dtype, order="C")
@@ -200,8 +262,11 @@ class DROracle:
         return Q
 
 
-def dr_full_step(o, dro, Q, cells, faces, state, a, init, dt, mlp=None, record=None, first_iters=None):
-    """One step of proxy kernel all_dr in FP64: ADER + local, fault, neighbour (the GPU's order)."""
+def dr_full_step(o, dro, Q, cells, faces, state, a, init, dt, mlp=None, record=None, first_iters=None, aux=None):
+    """One step of proxy kernel all_dr in FP64: ADER + local, fault, neighbour (the GPU's order).
+
+    aux: fault time, nucleation, outputs and (law 1-3) the slip-weakening fields; its time
+    advances by dt."""
     order = o.order
     ft = cells["face_type"]
     coeffs = dg_setup.taylor_integrate(order, 0.0, dt)
@@ -213,7 +278,13 @@ def dr_full_step(o, dro, Q, cells, faces, state, a, init, dt, mlp=None, record=N
     ps, ms, rel = faces["sides"][:, 0], faces["sides"][:, 1], faces["sides"][:, 2]
     qip = dro.interpolate(d[pc], ps, np.zeros_like(ps), coll)
     qim = dro.interpolate(d[mc], ms, rel, coll)
-    isp, ism, iters = dro.friction(qip, qim, state, a, init, deltat, tw, mlp, record, first_iters)
+    if aux is not None and aux.get("law", 0) != 0:
+        isp, ism = dro.friction_lsw(qip, qim, state, init, deltat, tw, aux)
+        iters = np.zeros(state["v1"].shape, np.int64)
+    else:
+        isp, ism, iters = dro.friction(qip, qim, state, a, init, deltat, tw, mlp, record, first_iters, aux)
+    if aux is not None:
+        aux["time"] = aux.get("time", 0.0) + dt
     Q = dro.nodal_flux(Q, pc, ps, np.zeros_like(ps), isp, faces["fluxSolverPlus"])
     Q = dro.nodal_flux(Q, mc, ms, rel, ism, faces["fluxSolverMinus"])
     Q = o.neighbor(Q, I, cells["AminusT"].astype(np.float64), cells["neighbor"], cells["side"], cells["orient"], ft)
@@ -247,9 +318,10 @@ def lts_clusters(dt, neighbor, face_type, max_clusters, fault_cells=None):
         cl = new
 
 
-def _dr_cluster_step(o, dr, Q, derivs, fsel, dt):
+def _dr_cluster_step(o, dr, Q, derivs, fsel, dt, time=0.0):
     """The fault step of the faces fsel over one step dt of their cluster, from the derivatives
-    stored at the start of that step; updates dr["state"] in place and returns Q."""
+    stored at the start of that step (fault time `time`); updates dr["state"] (and dr["init"],
+    dr["aux"]) in place and returns Q."""
     faces, params = dr["faces"], dr["params"]
     sub = {k: np.asarray(v)[fsel] for k, v in faces.items()}
     dro = DROracle(o.order, sub, params)
@@ -259,9 +331,23 @@ def _dr_cluster_step(o, dr, Q, derivs, fsel, dt):
     ps, ms, rel = sub["sides"][:, 0], sub["sides"][:, 1], sub["sides"][:, 2]
     qip = dro.interpolate(derivs[pc], ps, np.zeros_like(ps), coll)
     qim = dro.interpolate(derivs[mc], ms, rel, coll)
-    isp, ism, _ = dro.friction(qip, qim, state, dr["a"][fsel], dr["init"][fsel], deltat, tw)
+    init = np.ascontiguousarray(dr["init"][fsel], np.float64)
+    aux = None
+    if dr.get("aux") is not None:
+        aux = {k: (np.ascontiguousarray(v[fsel]) if k in AUX_ARRAYS and v is not None else v)
+               for k, v in dr["aux"].items()}
+        aux["time"] = time
+    if aux is not None and aux.get("law", 0) != 0:
+        isp, ism = dro.friction_lsw(qip, qim, state, init, deltat, tw, aux)
+    else:
+        isp, ism, _ = dro.friction(qip, qim, state, dr["a"][fsel], init, deltat, tw, aux=aux)
     for k, v in state.items():
         dr["state"][k][fsel] = v
+    dr["init"][fsel] = init
+    if aux is not None:
+        for k in AUX_ARRAYS:
+            if dr["aux"].get(k) is not None:
+                dr["aux"][k][fsel] = aux[k]
     Q = dro.nodal_flux(Q, pc, ps, np.zeros_like(ps), isp, sub["fluxSolverPlus"])
     return dro.nodal_flux(Q, mc, ms, rel, ism, sub["fluxSolverMinus"])
 
@@ -269,9 +355,11 @@ def _dr_cluster_step(o, dr, Q, derivs, fsel, dt):
 def lts_cycles(o, Q, cells, cluster, dt0, ncycles, dr=None):
     """Rate-2 LTS (TimeCluster.cpp:358-440, 695-717; TimeCommon.cpp:40-87) in FP64.
 
-    dr (optional): {"faces", "params", "state", "a", "init"} of a fault whose faces join their
-    cells' cluster: each cluster's correction runs the fault step of its faces over its own time
-    step before the neighbour flux (TimeCluster.cpp:804-823); dr["state"] is updated in place.
+    dr (optional): {"faces", "params", "state", "a", "init"[, "aux"]} of a fault whose faces join
+    their cells' cluster: each cluster's correction runs the fault step of its faces over its own
+    time step before the neighbour flux (TimeCluster.cpp:804-823); dr["state"] is updated in
+    place, and dr["aux"] (fault time at the cycle start, nucleation, outputs, slip-weakening
+    fields) too, its time advancing by the cycle length.
 
     Every cycle advances all clusters by dt0 2^(C-1).  At sub-step k of the finest cluster the
     clusters whose step starts there predict (ADER with derivatives, integration buffer of cells
@@ -337,6 +425,9 @@ def lts_cycles(o, Q, cells, cluster, dt0, ncycles, dr=None):
                 if dr is not None:
                     fsel = np.nonzero(cluster[dr["faces"]["cells"][:, 0]] == c)[0]
                     if fsel.size:
-                        Q = _dr_cluster_step(o, dr, Q, derivs, fsel, dt0 * ln)
+                        t = dr["aux"].get("time", 0.0) + (k + 1 - ln) * dt0 if dr.get("aux") is not None else 0.0
+                        Q = _dr_cluster_step(o, dr, Q, derivs, fsel, dt0 * ln, t)
                 Q[idx] = o.neighbor(Q[idx], pool, aminus[idx], pidx, side[idx], orient[idx], ft[idx])
+        if dr is not None and dr.get("aux") is not None:
+            dr["aux"]["time"] = dr["aux"].get("time", 0.0) + steps * dt0
     return Q

@@ -13,6 +13,7 @@ from .lib import (  # noqa: F401
     mlp_num_params,
     Context,
     RSParams,
+    LSWParams,
     DR_FIELDS,
     SeiError,
     KERNELS,

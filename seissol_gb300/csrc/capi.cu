@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstring>
 #include <exception>
+#include <limits>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -63,7 +64,12 @@ struct sei_ctx {
   int32_t *d_pc = nullptr, *d_mc = nullptr, *d_pslot = nullptr, *d_mslot = nullptr, *d_iters = nullptr;
   uint8_t *d_ps = nullptr, *d_ms = nullptr, *d_rel = nullptr;
   float *d_tinvt = nullptr, *d_fsp = nullptr, *d_fsm = nullptr, *d_isp = nullptr, *d_ism = nullptr;
-  double *d_imp = nullptr, *d_state = nullptr;  // state: 13 fields x [nf][npts]
+  double *d_imp = nullptr, *d_state = nullptr;  // state: SEI_DR_NUM_FIELDS fields x [nf][npts]
+  double* d_time = nullptr;                       // fault time at the start of the next step
+  int dr_law = SEI_LAW_FVW;
+  sei_lsw_params lsw{};
+  bool dr_nucleate = false;
+  double dr_t0 = 0.0, dr_s0 = 0.0;  // nucleation duration / start (t0 also ramps the forced rupture)
   float* d_mlp = nullptr;  // trained warm-start network (nullptr: none)
   float mlp_norm[sei_mlp::kNorm] = {0};
   bool warm_start = false;
@@ -144,6 +150,21 @@ void dropLtsGraph(sei_ctx* c) {
     if (e_ != cudaSuccess) return cudaFail(c, e_, #call); \
   } while (0)
 
+void freeFault(sei_ctx* c) {
+  for (void* p : {(void*)c->d_pc, (void*)c->d_mc, (void*)c->d_pslot, (void*)c->d_mslot, (void*)c->d_iters, (void*)c->d_ps,
+                  (void*)c->d_ms, (void*)c->d_rel, (void*)c->d_tinvt, (void*)c->d_fsp, (void*)c->d_fsm, (void*)c->d_isp,
+                  (void*)c->d_ism, (void*)c->d_imp, (void*)c->d_state, (void*)c->d_time})
+    cudaFree(p);
+  c->d_pc = c->d_mc = c->d_pslot = c->d_mslot = c->d_iters = nullptr;
+  c->d_ps = c->d_ms = c->d_rel = nullptr;
+  c->d_tinvt = c->d_fsp = c->d_fsm = c->d_isp = c->d_ism = nullptr;
+  c->d_imp = c->d_state = c->d_time = nullptr;
+  c->dr_ready = false;
+  c->dr_law = SEI_LAW_FVW;
+  c->dr_nucleate = false;
+  c->dr_t0 = c->dr_s0 = 0.0;
+}
+
 void freeArrays(sei_ctx* c) {
   cudaFree(c->Q);
   cudaFree(c->I);
@@ -172,16 +193,8 @@ void freeArrays(sei_ctx* c) {
   c->lts_trace = false;
   c->npool = 0;
   c->ncl = 0;
-  for (void* p : {(void*)c->d_pc, (void*)c->d_mc, (void*)c->d_pslot, (void*)c->d_mslot, (void*)c->d_iters, (void*)c->d_ps,
-                  (void*)c->d_ms, (void*)c->d_rel, (void*)c->d_tinvt, (void*)c->d_fsp, (void*)c->d_fsm, (void*)c->d_isp,
-                  (void*)c->d_ism, (void*)c->d_imp, (void*)c->d_state})
-    cudaFree(p);
-  c->d_pc = c->d_mc = c->d_pslot = c->d_mslot = c->d_iters = nullptr;
-  c->d_ps = c->d_ms = c->d_rel = nullptr;
-  c->d_tinvt = c->d_fsp = c->d_fsm = c->d_isp = c->d_ism = nullptr;
-  c->d_imp = c->d_state = nullptr;
+  freeFault(c);
   c->dslot = nullptr;
-  c->dr_ready = false;
   c->Q = c->I = c->derivs = c->star_nz = c->aplus = c->aminus = nullptr;
   c->nbr = nullptr;
   c->rel = c->ftype = nullptr;
@@ -462,6 +475,26 @@ sei::DrArgs drArgs(sei_ctx* c, double dt) {
   a.rec = c->d_rec;
   a.rec_count = c->d_rec_count;
   a.rec_cap = c->rec_cap;
+  a.law = c->dr_law;
+  a.time = c->d_time;
+  a.time_offset = 0.0;
+  a.t0 = c->dr_t0;
+  a.s0 = c->dr_s0;
+  a.nucleate = c->dr_nucleate ? 1 : 0;
+  a.nuc = field(SEI_DR_NUC_SN);  // nucleation sn, tau1, tau2: consecutive fields
+  a.peak = field(SEI_DR_PEAK_SLIP_RATE);
+  a.trup = field(SEI_DR_RUPTURE_TIME);
+  a.tdyn = field(SEI_DR_DYN_STRESS_TIME);
+  a.mu_s = field(SEI_DR_MU_S);
+  a.mu_d = field(SEI_DR_MU_D);
+  a.d_c = field(SEI_DR_D_C);
+  a.cohesion = field(SEI_DR_COHESION);
+  a.t_forced = field(SEI_DR_FORCED_RUPTURE_TIME);
+  a.reg = field(SEI_DR_REG_STRENGTH);
+  a.healing = c->lsw.healing_threshold;
+  a.v_star = c->lsw.v_star;
+  a.prakash_length = c->lsw.prakash_length > 0 ? c->lsw.prakash_length : 1.0;
+  a.tp_exponent = c->lsw.tp_proxy_exponent;
   return a;
 }
 
@@ -470,6 +503,7 @@ int launchDr(sei_ctx* c, double dt) {
   int rc = profMark(c, 2);
   if (rc) return rc;
   if (sei::launchDrFaces(c->cfg.order, drArgs(c, dt), c->stream) != 0) return fail(c, SEI_ERR_CUDA, "fault kernel launch failed");
+  if (sei::launchDrAdvanceTime(c->d_time, dt, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "fault time launch failed");
   return SEI_OK;
 }
 
@@ -1011,40 +1045,26 @@ int sei_dr_num_points(int order) { return (order >= 2 && order <= 6) ? sei::drNu
 
 int64_t sei_dr_num_faces(const sei_ctx* c) { return (c && c->has_fault) ? c->fault.nf : 0; }
 
-int sei_dr_setup(sei_ctx* c, const sei_rs_params* p, int64_t* nfaces) {
-  int rc = checkReady(c);
-  if (rc) return rc;
-  if (!p) return fail(c, SEI_ERR_ARG, "null parameters");
-  if (!c->has_fault) return fail(c, SEI_ERR_STATE, "mesh has no fault (fault_plane < 0)");
-  if (c->lts) return fail(c, SEI_ERR_STATE, "set up dynamic rupture before local time stepping");
-  if (!(p->a_min > 0) || p->a_max < p->a_min || !(p->v0 > 0) || !(p->l > 0) || !(p->vw > 0) || !(p->v_init > 0) ||
-      p->max_newton <= 0 || p->max_outer <= 0 || !(p->newton_tol > 0) || !(p->state_tol > 0) || p->sn_max > 0)
-    return fail(c, SEI_ERR_ARG, "invalid rate-and-state parameters");
-  c->rs = *p;
-  const int64_t nf = c->fault.nf;
-  const int np = sei::drNumPoints(c->cfg.order);
-  c->npts = np;
-  // host initial state
-  std::vector<double> st((size_t)13 * nf * np, 0.0);
-  auto field = [&](int k) { return st.data() + (size_t)k * nf * np; };
-  uint64_t z = p->seed;
-  auto uni = [&](double lo, double hi) {
+namespace {
+// Seeded uniform numbers for the initial fault state (splitmix64).
+struct FaultRng {
+  uint64_t z;
+  double operator()(double lo, double hi) {
     z += 0x9E3779B97F4A7C15ull;
     uint64_t x = z;
     x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
     x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
     x ^= x >> 31;
     return lo + (hi - lo) * ((x >> 11) * (1.0 / 9007199254740992.0));
-  };
-  for (int64_t i = 0; i < nf * np; ++i) {
-    const double a = uni(p->a_min, p->a_max);
-    field(SEI_DR_A)[i] = a;
-    field(SEI_DR_SN0)[i] = uni(p->sn_min, p->sn_max);
-    field(SEI_DR_TAU1_0)[i] = uni(p->tau_min, p->tau_max);
-    field(SEI_DR_TAU2_0)[i] = 0.0;
-    field(SEI_DR_SLIP_RATE1)[i] = p->v_init;
-    field(SEI_DR_PSI)[i] = sei::fvwSteadyState(p->v_init, a, p->b, p->f0, p->v0, p->muw, p->vw);
   }
+};
+
+// Fault arrays on the device from the host initial state st [SEI_DR_NUM_FIELDS][nf][npts]
+// (replaces any earlier fault set-up of the context).
+int drInstall(sei_ctx* c, const std::vector<double>& st) {
+  const int64_t nf = c->fault.nf;
+  const int np = c->npts;
+  freeFault(c);
   // derivative slots: every fault cell stores its derivatives
   std::vector<int32_t> slot(c->n, -1), ps(nf), ms(nf);
   for (int64_t f = 0; f < nf; ++f) {
@@ -1057,6 +1077,8 @@ int sei_dr_setup(sei_ctx* c, const sei_rs_params* p, int64_t* nfaces) {
   const size_t dsz = (size_t)sei::derivativesSize(c->cfg.order) * sizeof(float);
   cudaFree(c->derivs);
   c->derivs = nullptr;
+  cudaFree(c->dslot);
+  c->dslot = nullptr;
   bool ok = dalloc((void**)&c->derivs, 2 * nf * dsz) && dalloc((void**)&c->dslot, c->n * 4) &&
             dalloc((void**)&c->d_pc, nf * 4) && dalloc((void**)&c->d_mc, nf * 4) && dalloc((void**)&c->d_pslot, nf * 4) &&
             dalloc((void**)&c->d_mslot, nf * 4) && dalloc((void**)&c->d_iters, 3 * nf * np * 4) &&
@@ -1064,7 +1086,7 @@ int sei_dr_setup(sei_ctx* c, const sei_rs_params* p, int64_t* nfaces) {
             dalloc((void**)&c->d_tinvt, nf * 81 * 4) && dalloc((void**)&c->d_fsp, nf * 81 * 4) &&
             dalloc((void**)&c->d_fsm, nf * 81 * 4) && dalloc((void**)&c->d_isp, nf * 9 * np * 4) &&
             dalloc((void**)&c->d_ism, nf * 9 * np * 4) && dalloc((void**)&c->d_imp, nf * 8 * 8) &&
-            dalloc((void**)&c->d_state, st.size() * 8);
+            dalloc((void**)&c->d_state, st.size() * 8) && dalloc((void**)&c->d_time, sizeof(double));
   if (!ok) {
     cudaGetLastError();
     return fail(c, SEI_ERR_OOM, "device allocation for the fault failed");
@@ -1087,9 +1109,129 @@ int sei_dr_setup(sei_ctx* c, const sei_rs_params* p, int64_t* nfaces) {
   SEI_CUDA(cudaMemset(c->d_isp, 0, nf * 9 * np * 4));
   SEI_CUDA(cudaMemset(c->d_ism, 0, nf * 9 * np * 4));
   SEI_CUDA(cudaMemset(c->derivs, 0, 2 * nf * dsz));
+  SEI_CUDA(cudaMemset(c->d_time, 0, sizeof(double)));
   c->dr_ready = true;
   c->nslots = 2 * nf;
+  return SEI_OK;
+}
+
+// Host initial state with the fields both laws share: rupture and dynamic-stress times pending
+// (negative), no forced rupture, zero nucleation stresses and peak slip rate.
+std::vector<double> drInitialState(int64_t nf, int np) {
+  std::vector<double> st((size_t)SEI_DR_NUM_FIELDS * nf * np, 0.0);
+  const size_t pl = (size_t)nf * np;
+  std::fill_n(st.data() + SEI_DR_RUPTURE_TIME * pl, pl, -1.0);
+  std::fill_n(st.data() + SEI_DR_DYN_STRESS_TIME * pl, pl, -1.0);
+  std::fill_n(st.data() + SEI_DR_FORCED_RUPTURE_TIME * pl, pl, std::numeric_limits<double>::max());
+  return st;
+}
+
+int drSetupCheck(sei_ctx* c, const void* p) {
+  int rc = checkReady(c);
+  if (rc) return rc;
+  if (!p) return fail(c, SEI_ERR_ARG, "null parameters");
+  if (!c->has_fault) return fail(c, SEI_ERR_STATE, "mesh has no fault (fault_plane < 0)");
+  if (c->lts) return fail(c, SEI_ERR_STATE, "set up dynamic rupture before local time stepping");
+  return SEI_OK;
+}
+}  // namespace
+
+int sei_dr_setup(sei_ctx* c, const sei_rs_params* p, int64_t* nfaces) {
+  int rc = drSetupCheck(c, p);
+  if (rc) return rc;
+  if (!(p->a_min > 0) || p->a_max < p->a_min || !(p->v0 > 0) || !(p->l > 0) || !(p->vw > 0) || !(p->v_init > 0) ||
+      p->max_newton <= 0 || p->max_outer <= 0 || !(p->newton_tol > 0) || !(p->state_tol > 0) || p->sn_max > 0)
+    return fail(c, SEI_ERR_ARG, "invalid rate-and-state parameters");
+  c->rs = *p;
+  const int64_t nf = c->fault.nf;
+  const int np = sei::drNumPoints(c->cfg.order);
+  c->npts = np;
+  std::vector<double> st = drInitialState(nf, np);
+  auto field = [&](int k) { return st.data() + (size_t)k * nf * np; };
+  FaultRng uni{p->seed};
+  for (int64_t i = 0; i < nf * np; ++i) {
+    const double a = uni(p->a_min, p->a_max);
+    field(SEI_DR_A)[i] = a;
+    field(SEI_DR_SN0)[i] = uni(p->sn_min, p->sn_max);
+    field(SEI_DR_TAU1_0)[i] = uni(p->tau_min, p->tau_max);
+    field(SEI_DR_TAU2_0)[i] = 0.0;
+    field(SEI_DR_SLIP_RATE1)[i] = p->v_init;
+    field(SEI_DR_PSI)[i] = sei::fvwSteadyState(p->v_init, a, p->b, p->f0, p->v0, p->muw, p->vw);
+  }
+  if ((rc = drInstall(c, st))) return rc;
+  c->dr_law = SEI_LAW_FVW;
   if (nfaces) *nfaces = nf;
+  return SEI_OK;
+}
+
+int sei_dr_setup_lsw(sei_ctx* c, const sei_lsw_params* p, int64_t* nfaces) {
+  int rc = drSetupCheck(c, p);
+  if (rc) return rc;
+  if (p->law != SEI_LAW_LSW && p->law != SEI_LAW_LSW_BIMATERIAL && p->law != SEI_LAW_LSW_TP_PROXY)
+    return fail(c, SEI_ERR_ARG, "law must be SEI_LAW_LSW, SEI_LAW_LSW_BIMATERIAL or SEI_LAW_LSW_TP_PROXY");
+  if (!(p->d_c > 0) || !std::isfinite(p->mu_s) || !std::isfinite(p->mu_d) || !std::isfinite(p->cohesion) ||
+      !(p->t0 >= 0) || p->sn_max > 0 || p->sn_min > p->sn_max || p->tau_min > p->tau_max ||
+      (p->law == SEI_LAW_LSW_BIMATERIAL && !(p->prakash_length > 0)) ||
+      (p->law == SEI_LAW_LSW_TP_PROXY && !(p->tp_proxy_exponent > 0)))
+    return fail(c, SEI_ERR_ARG, "invalid linear-slip-weakening parameters");
+  c->rs = sei_rs_params{};
+  c->lsw = *p;
+  const int64_t nf = c->fault.nf;
+  const int np = sei::drNumPoints(c->cfg.order);
+  c->npts = np;
+  std::vector<double> st = drInitialState(nf, np);
+  auto field = [&](int k) { return st.data() + (size_t)k * nf * np; };
+  FaultRng uni{p->seed};
+  for (int64_t i = 0; i < nf * np; ++i) {
+    const double sn = uni(p->sn_min, p->sn_max);
+    field(SEI_DR_SN0)[i] = sn;
+    field(SEI_DR_TAU1_0)[i] = uni(p->tau_min, p->tau_max);
+    field(SEI_DR_MU_S)[i] = p->mu_s;
+    field(SEI_DR_MU_D)[i] = p->mu_d;
+    field(SEI_DR_D_C)[i] = p->d_c;
+    field(SEI_DR_COHESION)[i] = p->cohesion;
+    field(SEI_DR_FORCED_RUPTURE_TIME)[i] = p->forced_rupture_time;
+    field(SEI_DR_MU)[i] = p->mu_s;  // LinearSlipWeakeningInitializer.cpp:43
+    // LinearSlipWeakeningInitializer.cpp:82-85
+    field(SEI_DR_REG_STRENGTH)[i] = -p->cohesion - p->mu_s * std::min(0.0, sn);
+  }
+  if ((rc = drInstall(c, st))) return rc;
+  c->dr_law = p->law;
+  c->dr_t0 = p->t0;
+  if (nfaces) *nfaces = nf;
+  return SEI_OK;
+}
+
+int sei_dr_law(const sei_ctx* c) { return (c && c->dr_ready) ? c->dr_law : -1; }
+
+int sei_dr_set_nucleation(sei_ctx* c, int on, double t0, double s0) {
+  int rc = checkReady(c);
+  if (rc) return rc;
+  if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up");
+  if (on && (!(t0 > 0) || !std::isfinite(s0))) return fail(c, SEI_ERR_ARG, "nucleation needs t0 > 0 and a finite s0");
+  c->dr_nucleate = on != 0;
+  if (on) {
+    c->dr_t0 = t0;
+    c->dr_s0 = s0;
+  }
+  dropLtsGraph(c);
+  return SEI_OK;
+}
+
+int sei_dr_get_time(sei_ctx* c, double* t) {
+  if (!c || !t) return SEI_ERR_ARG;
+  if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up");
+  SEI_CUDA(cudaMemcpyAsync(t, c->d_time, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  SEI_CUDA(cudaStreamSynchronize(c->stream));
+  return SEI_OK;
+}
+
+int sei_dr_set_time(sei_ctx* c, double t) {
+  if (!c) return SEI_ERR_ARG;
+  if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up");
+  if (!std::isfinite(t) || t < 0) return fail(c, SEI_ERR_ARG, "fault time must be finite and >= 0");
+  SEI_CUDA(cudaMemcpyAsync(c->d_time, &t, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  SEI_CUDA(cudaStreamSynchronize(c->stream));
   return SEI_OK;
 }
 
@@ -1119,7 +1261,7 @@ int sei_dr_get_faces(sei_ctx* c, int32_t* cells, int8_t* sides, float* tinvt, fl
 static int drField(sei_ctx* c, int field, double*& dev) {
   if (!c) return SEI_ERR_ARG;
   if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up");
-  if (field < 0 || field > 12) return fail(c, SEI_ERR_ARG, "unknown friction-state field");
+  if (field < 0 || field >= SEI_DR_NUM_FIELDS) return fail(c, SEI_ERR_ARG, "unknown friction-state field");
   dev = c->d_state + (size_t)field * c->fault.nf * c->npts;
   return SEI_OK;
 }
@@ -1315,6 +1457,7 @@ int sei_mlp_train(sei_ctx* c, const float* samples, int64_t n, int steps, float 
   std::vector<float> X, T;
   splitSamples(samples, n, X, T);
   if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up (the network needs V0)");
+  if (c->dr_law != SEI_LAW_FVW) return fail(c, SEI_ERR_STATE, "the network serves the rate-and-state law");
   float norm[sei_mlp::kNorm];
   sampleNorm(samples, n, c->rs.v0, norm);
   const int np = sei::mlpNumParams();
@@ -1400,6 +1543,7 @@ int sei_mlp_set(sei_ctx* c, const float* params, const float* norm) {
 int sei_dr_warm_start(sei_ctx* c, int on) {
   if (!c) return SEI_ERR_ARG;
   if (on && !c->d_mlp) return fail(c, SEI_ERR_STATE, "no trained network (sei_mlp_train or sei_mlp_set)");
+  if (on && c->dr_ready && c->dr_law != SEI_LAW_FVW) return fail(c, SEI_ERR_STATE, "the warm start serves the rate-and-state law");
   c->warm_start = on != 0;
   dropLtsGraph(c);
   return SEI_OK;
@@ -1923,6 +2067,7 @@ int ltsCycle(sei_ctx* c) {
         int rc = profMark(c, 2);
         if (rc) return rc;
         sei::DrArgs a = drArgs(c, c->lts_dt0 * (double)len);
+        a.time_offset = c->lts_dt0 * (double)(k + 1 - len);  // this step's start within the cycle
         a.fidx = c->d_fidx;
         a.face_begin = (int)c->f_start[cl];
         a.face_count = (int)(c->f_start[cl + 1] - c->f_start[cl]);
@@ -1939,6 +2084,10 @@ int ltsCycle(sei_ctx* c) {
       if (rc) return rc;
     }
   }
+  // the fault time moves on by one cycle (the fault kernels above read it as their base)
+  if (!c->f_start.empty() && c->f_start.back() > 0 &&
+      sei::launchDrAdvanceTime(c->d_time, c->lts_dt0 * (double)steps, c->stream) != 0)
+    return fail(c, SEI_ERR_CUDA, "fault time launch failed");
   return SEI_OK;
 }
 }  // namespace

@@ -269,7 +269,20 @@ __device__ __forceinline__ void faceSync(int fs) {
 // the two warps of a face at orders 5 and 6 leave the loop independently.
 __device__ __forceinline__ bool warpAll(bool c) { return __all_sync(0xffffffffu, c); }
 
-template <int N, int B, int NP>
+// smoothStep of the Gaussian nucleation (src/Numerical/GaussianNucleationFunction.h).
+__device__ double smoothStep(double t, double t0) {
+  if (t <= 0.0) return 0.0;
+  if (t < t0) {
+    const double tau = t - t0;
+    return exp(tau * tau / (t * (t - 2.0 * t0)));
+  }
+  return 1.0;
+}
+
+// RS: rate and state with fast velocity weakening (Newton solve of the slip rate, resampled state
+// increment); otherwise linear slip weakening (law 1: resampled slip rate; 2: bimaterial
+// regularised strength; 3: TP proxy state), CpuImpl/LinearSlipWeakening.h:27-170.
+template <int N, int B, int NP, bool RS>
 __global__ void __launch_bounds__(128, 3)
     sei_dr_faces(sei::DrArgs A, const float* __restrict__ V3m, const float* __restrict__ TW,
                  const double* __restrict__ R) {
@@ -283,8 +296,8 @@ __global__ void __launch_bounds__(128, 3)
   __shared__ float sJ[FPB][B * 9];
   __shared__ float sG[FPB][NP * 9];
   __shared__ double sD[FPB][TPF];
-  __shared__ float sW[kMlpParams];
-  const bool useMlp = A.mlp != nullptr;
+  __shared__ float sW[RS ? kMlpParams : 1];
+  const bool useMlp = RS && A.mlp != nullptr;
   if (useMlp)
     for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) sW[i] = A.mlp[i];
   __syncthreads();
@@ -338,23 +351,37 @@ __global__ void __launch_bounds__(128, 3)
     }
   };
 
-  // ---- 2. friction (lanes < NP own one point each)
+  // ---- 2. friction (lanes < NP own one point each), per time point as the evaluate loop of
+  // CpuImpl/BaseFrictionLaw.h:103-137: nucleation, friction, rupture-front and peak outputs
   const size_t po = (size_t)f * NP + k;
   const double* imp = A.imp + (size_t)f * 8;
   const double etap = imp[4], etas = imp[5], invEtaS = imp[6];
   // reciprocal impedances, once per thread: FP64 divisions are costly on this part
   const double rzp = 1.0 / imp[0], rzs = 1.0 / imp[1], rzpn = 1.0 / imp[2], rzsn = 1.0 / imp[3];
-  const double a = pt ? A.a[po] : 0.01;
+  const double a = RS && pt ? A.a[po] : 0.01;
   const double inva = 1.0 / a;  // psi / a as psi * inva: one float64 division per thread, not per solve
   const size_t plane = (size_t)A.nfaces * NP;  // init holds sn0, tau1_0, tau2_0 as [3][nf][npts]
-  const double sn0 = pt ? A.init[po] : 0.0;
-  const double t10 = pt ? A.init[plane + po] : 0.0;
-  const double t20 = pt ? A.init[2 * plane + po] : 0.0;
-  double psiStored = pt ? A.psi[po] : 0.0;
+  double sn0 = pt ? A.init[po] : 0.0;
+  double t10 = pt ? A.init[plane + po] : 0.0;
+  double t20 = pt ? A.init[2 * plane + po] : 0.0;
+  const bool nucleating = A.nucleate != 0;
+  const double nsn = nucleating && pt ? A.nuc[po] : 0.0;
+  const double nt1 = nucleating && pt ? A.nuc[plane + po] : 0.0;
+  const double nt2 = nucleating && pt ? A.nuc[2 * plane + po] : 0.0;
+  double psiStored = RS && pt ? A.psi[po] : 0.0;
   double psib = psiStored;
   double v1 = pt ? A.v1[po] : 1.0, v2 = pt ? A.v2[po] : 0.0;
   double slip1 = pt ? A.slip1[po] : 0.0, slip2 = pt ? A.slip2[po] : 0.0, slip = pt ? A.slip[po] : 0.0;
-  double mu = 0.0, tr1 = 0.0, tr2 = 0.0;
+  double mu = !RS && pt ? A.mu[po] : 0.0, tr1 = 0.0, tr2 = 0.0;
+  double peak = pt ? A.peak[po] : 0.0, trup = pt ? A.trup[po] : 0.0;
+  // slip weakening fields
+  const double muS = !RS && pt ? A.mu_s[po] : 0.0, muD = !RS && pt ? A.mu_d[po] : 0.0;
+  const double dc = !RS && pt ? A.d_c[po] : 1.0, coh = !RS && pt ? A.cohesion[po] : 0.0;
+  const double tForced = !RS && pt ? A.t_forced[po] : 0.0;
+  double tdyn = !RS && pt ? A.tdyn[po] : 0.0;
+  double reg = !RS && pt && A.law == 2 ? A.reg[po] : 0.0;
+  double vmag = sqrt(v1 * v1 + v2 * v2);  // slip-rate magnitude of the previous time point (slip weakening)
+  double tStart = (A.time ? *A.time : 0.0) + A.time_offset;
   int iters = 0, firstIters = 0, iters32 = 0;
   const LawInv inv{1.0 / A.v0, 1.0 / A.vw, 1.0 / A.l};
   double isP[6] = {0, 0, 0, 0, 0, 0}, isM[6] = {0, 0, 0, 0, 0, 0};
@@ -363,87 +390,144 @@ __global__ void __launch_bounds__(128, 3)
     float qc[2][6];
     interpolate(s, qc);
     const double dt = A.deltat[s];
+    const double tEnd = tStart + dt;
+    // nucleation (FrictionSolverCommon.h:503-531) before the friction of this time point
+    if (nucleating && tEnd <= A.t0 + A.s0 && tEnd >= A.s0) {
+      const double g = smoothStep(tEnd - A.s0, A.t0) - smoothStep(tEnd - A.s0 - dt, A.t0);
+      sn0 += nsn * g;
+      t10 += nt1 * g;
+      t20 += nt2 * g;
+    }
     // precompute stress (etaPDamp = 1): qi order N, T1, T2, U, V, W
     const double fsn = etap * ((double)qc[1][3] - qc[0][3] + qc[0][0] * rzp + qc[1][0] * rzpn);
     const double ft1 = etas * ((double)qc[1][4] - qc[0][4] + qc[0][1] * rzs + qc[1][1] * rzsn);
     const double ft2 = etas * ((double)qc[1][5] - qc[0][5] + qc[0][2] * rzs + qc[1][2] * rzsn);
-    double sn = fsn + sn0;
-    sn = sn < 0 ? sn : 0.0;
-    const double sref = psib;
     const double tt1 = t10 + ft1, tt2 = t20 + ft2;
     const double tau = sqrt(tt1 * tt1 + tt2 * tt2);
-    double vmag = sqrt(v1 * v1 + v2 * v2);
-    vmag = vmag < kAlmostZero ? kAlmostZero : vmag;
-    double lsr = vmag;
+    if constexpr (RS) {
+      double sn = fsn + sn0;
+      sn = sn < 0 ? sn : 0.0;
+      const double sref = psib;
+      vmag = sqrt(v1 * v1 + v2 * v2);  // RateAndState.h:150-153
+      vmag = vmag < kAlmostZero ? kAlmostZero : vmag;
+      double lsr = vmag;
 #pragma unroll 1
-    for (int j = 0; j < A.max_outer; ++j) {
-      bool conv = true;
-      if (pt) {
-        psib = stateUpdate(A, inv, a, sref, dt, lsr);
-        NewtonOut r{};
-        bool done = false;
-        const bool net = useMlp && j == 0 && sei_mlp::usable(sn, tau, a);
-        if (net || A.refine32) {
-          const Solve32 S{(float)(fabs(sn) * a), (float)etas, (float)tau, (float)(psib * inva) - lnPos(2.0 * A.v0)};
-          const float u0 = lnPos(vmag);
-          float u = u0;
-          if (net) {
-            // start from the network's guess when its residual is below the plain start's
-            // (float32 residuals: the comparison only picks a start)
-            const float lg = mlpGuess32(sW, A.mlp_norm, (float)sn, (float)tau, (float)psib, (float)a, (float)A.b);
-            const float ug = fminf(fmaxf(lg, kLnGuessMinF), kLnGuessMaxF);
-            if (fabsf(h32(S, ug, nullptr)) < fabsf(h32(S, u, nullptr))) u = ug;
-          }
-          if (A.refine32) {
-            int its = 0;
-            u = newton32(S, u, its);
-            iters32 += its;
-          }
-          // a start that float arithmetic cannot tell from the previous slip rate is not taken: the
-          // previous rate is often the float64 root already (no iteration at all)
-          if (!(fabsf(u - u0) <= 2e-6f + 6e-7f * fabsf(u0))) {
-            r = newton(A, inv, a, inva, psib, sn, tau, invEtaS, expToDouble(u), true);
-            (j == 0 ? firstIters : iters) += r.iters;
-            done = r.conv;
-          }
-        }
-        if (!done) {
-          r = newton(A, inv, a, inva, psib, sn, tau, invEtaS, vmag, false);
-          (j == 0 ? firstIters : iters) += r.iters;
-          if (A.rec && j == 0 && r.conv && sei_mlp::usable(sn, tau, a)) {
-            const unsigned idx = atomicAdd(A.rec_count, 1u);
-            if (idx < A.rec_cap) {
-              float* o = A.rec + (size_t)idx * 6;
-              o[0] = (float)sn;
-              o[1] = (float)tau;
-              o[2] = (float)psib;
-              o[3] = (float)a;
-              o[4] = (float)A.b;
-              o[5] = (float)log10(r.v);
+      for (int j = 0; j < A.max_outer; ++j) {
+        bool conv = true;
+        if (pt) {
+          psib = stateUpdate(A, inv, a, sref, dt, lsr);
+          NewtonOut r{};
+          bool done = false;
+          const bool net = useMlp && j == 0 && sei_mlp::usable(sn, tau, a);
+          if (net || A.refine32) {
+            const Solve32 S{(float)(fabs(sn) * a), (float)etas, (float)tau, (float)(psib * inva) - lnPos(2.0 * A.v0)};
+            const float u0 = lnPos(vmag);
+            float u = u0;
+            if (net) {
+              // start from the network's guess when its residual is below the plain start's
+              // (float32 residuals: the comparison only picks a start)
+              const float lg = mlpGuess32(sW, A.mlp_norm, (float)sn, (float)tau, (float)psib, (float)a, (float)A.b);
+              const float ug = fminf(fmaxf(lg, kLnGuessMinF), kLnGuessMaxF);
+              if (fabsf(h32(S, ug, nullptr)) < fabsf(h32(S, u, nullptr))) u = ug;
+            }
+            if (A.refine32) {
+              int its = 0;
+              u = newton32(S, u, its);
+              iters32 += its;
+            }
+            // a start that float arithmetic cannot tell from the previous slip rate is not taken: the
+            // previous rate is often the float64 root already (no iteration at all)
+            if (!(fabsf(u - u0) <= 2e-6f + 6e-7f * fabsf(u0))) {
+              r = newton(A, inv, a, inva, psib, sn, tau, invEtaS, expToDouble(u), true);
+              (j == 0 ? firstIters : iters) += r.iters;
+              done = r.conv;
             }
           }
+          if (!done) {
+            r = newton(A, inv, a, inva, psib, sn, tau, invEtaS, vmag, false);
+            (j == 0 ? firstIters : iters) += r.iters;
+            if (A.rec && j == 0 && r.conv && sei_mlp::usable(sn, tau, a)) {
+              const unsigned idx = atomicAdd(A.rec_count, 1u);
+              if (idx < A.rec_cap) {
+                float* o = A.rec + (size_t)idx * 6;
+                o[0] = (float)sn;
+                o[1] = (float)tau;
+                o[2] = (float)psib;
+                o[3] = (float)a;
+                o[4] = (float)A.b;
+                o[5] = (float)log10(r.v);
+              }
+            }
+          }
+          lsr = 0.5 * (vmag + r.v);
+          conv = fabs(vmag - r.v) < A.state_tol;
+          vmag = r.v;
+          mu = r.mu;
         }
-        lsr = 0.5 * (vmag + r.v);
-        conv = fabs(vmag - r.v) < A.state_tol;
-        vmag = r.v;
-        mu = r.mu;
+        if (warpAll(conv)) break;
       }
-      if (warpAll(conv)) break;
-    }
-    if (pt) {
-      psib = stateUpdate(A, inv, a, sref, dt, lsr);
-      const double clin = 0.5 * inv.v0, cl = psib * inva;
-      mu = a * arsinhexp(clin * vmag, cl);
-      const double strength = -mu * sn;
-      slip += vmag * dt;
-      const double div = strength + etas * vmag;
-      const double vd = vmag / div;
-      v1 = vd * tt1;
-      v2 = vd * tt2;
+      if (pt) {
+        psib = stateUpdate(A, inv, a, sref, dt, lsr);
+        const double clin = 0.5 * inv.v0, cl = psib * inva;
+        mu = a * arsinhexp(clin * vmag, cl);
+        const double strength = -mu * sn;
+        slip += vmag * dt;
+        const double div = strength + etas * vmag;
+        const double vd = vmag / div;
+        v1 = vd * tt1;
+        v2 = vd * tt2;
+        tr1 = ft1 - etas * v1;
+        tr2 = ft2 - etas * v2;
+        slip1 += v1 * dt;
+        slip2 += v2 * dt;
+      }
+    } else {
+      // strength from the friction coefficient of the previous time point
+      const double snt = sn0 + fsn;
+      double strength = -coh - mu * (snt < 0.0 ? snt : 0.0);
+      if (A.law == 2) {
+        const double e = -((vmag > 0.0 ? vmag : 0.0) + A.v_star) * dt / A.prakash_length;
+        strength = reg * exp(e) + strength * -expm1(e);
+        reg = strength;
+      }
+      double v = (tau - strength) * invEtaS;
+      v = v > 0.0 ? v : 0.0;
+      const double div = strength + etas * v;
+      v1 = v * tt1 / div;
+      v2 = v * tt2 / div;
       tr1 = ft1 - etas * v1;
       tr2 = ft2 - etas * v2;
       slip1 += v1 * dt;
       slip2 += v2 * dt;
+      vmag = v;
+      // the accumulated slip grows by the slip rate resampled over the face (law 1)
+      double rv = v;
+      if (A.law == 1) {
+        sD[warp][lane] = pt ? v : 0.0;
+        faceSync<TPF>(warp);
+        rv = 0.0;
+        for (int j = 0; j < NP; ++j) rv += R[k * NP + j] * sD[warp][j];
+        faceSync<TPF>(warp);
+      }
+      slip += rv * dt;
+      const double ratio = fabs(slip) / dc;
+      double state = A.law == 3 ? 1.0 - pow(1.0 + ratio, -A.tp_exponent) : (ratio < 1.0 ? ratio : 1.0);
+      double f2;
+      if (A.t0 == 0.0) {
+        f2 = tEnd >= tForced ? 1.0 : 0.0;
+      } else {
+        f2 = (tEnd - tForced) / A.t0;
+        f2 = f2 < 0.0 ? 0.0 : (f2 > 1.0 ? 1.0 : f2);
+      }
+      state = state > f2 ? state : f2;
+      mu = muS - (muS - muD) * state;
+      if (peak > A.healing && v < A.healing) mu = muS;
+      if (tdyn < 0.0 && fabs(slip) >= dc) tdyn = tStart;
+    }
+    if (pt) {
+      // rupture front and peak slip rate (FrictionSolverCommon.h:546-592)
+      if (trup < 0.0 && vmag > 0.001) trup = tStart;
+      peak = vmag > peak ? vmag : peak;
       const double w = A.tweights[s];
       isM[0] += w * fsn;
       isM[1] += w * tr1;
@@ -458,15 +542,33 @@ __global__ void __launch_bounds__(128, 3)
       isP[4] += w * (qc[0][4] + (tr1 - qc[0][1]) * rzs);
       isP[5] += w * (qc[0][5] + (tr2 - qc[0][2]) * rzs);
     }
+    tStart = tEnd;
   }
 
-  // ---- 3. resample the state-variable increment over the face
-  sD[warp][lane] = pt ? psib - psiStored : 0.0;
-  faceSync<TPF>(warp);
+  // ---- 3. resample the state-variable increment over the face (rate and state)
+  if constexpr (RS) {
+    sD[warp][lane] = pt ? psib - psiStored : 0.0;
+    faceSync<TPF>(warp);
+    if (pt) {
+      double v = 0.0;
+      for (int j = 0; j < NP; ++j) v += R[k * NP + j] * sD[warp][j];
+      A.psi[po] = psiStored + v;
+      A.newton_iters[po] += iters + firstIters;
+      A.newton_iters[(size_t)A.nfaces * NP + po] += firstIters;
+      A.newton_iters[2 * (size_t)A.nfaces * NP + po] += iters32;
+    }
+  } else if (pt) {
+    A.tdyn[po] = tdyn;
+    if (A.law == 2) A.reg[po] = reg;
+  }
   if (pt) {
-    double v = 0.0;
-    for (int j = 0; j < NP; ++j) v += R[k * NP + j] * sD[warp][j];
-    A.psi[po] = psiStored + v;
+    if (nucleating) {
+      A.init[po] = sn0;
+      A.init[plane + po] = t10;
+      A.init[2 * plane + po] = t20;
+    }
+    A.peak[po] = peak;
+    A.trup[po] = trup;
     A.v1[po] = v1;
     A.v2[po] = v2;
     A.slip1[po] = slip1;
@@ -475,9 +577,6 @@ __global__ void __launch_bounds__(128, 3)
     A.mu[po] = mu;
     A.trac1[po] = tr1;
     A.trac2[po] = tr2;
-    A.newton_iters[po] += iters + firstIters;
-    A.newton_iters[(size_t)A.nfaces * NP + po] += firstIters;
-    A.newton_iters[2 * (size_t)A.nfaces * NP + po] += iters32;
   }
 
   // ---- 4./5. imposed states and nodal flux, plus side then minus side
@@ -516,11 +615,19 @@ __global__ void __launch_bounds__(128, 3)
 template <int N, int B, int NP>
 int launch(const sei::DrArgs& a, const float* v3m, const float* tw, const double* res, void* stream) {
   if (a.face_count <= 0) return 0;
+  if (a.law < 0 || a.law > 3 || !a.peak || !a.trup || (a.nucleate && !a.nuc) ||
+      (a.law != 0 && (!a.mu_s || !a.mu_d || !a.d_c || !a.cohesion || !a.t_forced || !a.tdyn)) || (a.law == 2 && !a.reg))
+    return -1;
   constexpr int FPB = FaceGroup<NP>::kFaces;
   const int blocks = (a.face_count + FPB - 1) / FPB;
-  sei_dr_faces<N, B, NP><<<blocks, 128, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
+  if (a.law == 0)
+    sei_dr_faces<N, B, NP, true><<<blocks, 128, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
+  else
+    sei_dr_faces<N, B, NP, false><<<blocks, 128, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
+
+__global__ void sei_dr_advance_time(double* t, double dt) { *t += dt; }
 
 template <typename T>
 const T* symbolAddress(const T& sym) {
@@ -534,6 +641,11 @@ const T* symbolAddress(const T& sym) {
 namespace sei {
 
 int drNumPoints(int order) { return (order + 1) * (order + 1); }
+
+int launchDrAdvanceTime(double* t, double dt, void* stream) {
+  sei_dr_advance_time<<<1, 1, 0, (cudaStream_t)stream>>>(t, dt);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
 
 int launchDrFaces(int order, const DrArgs& a, void* stream) {
   // One thread per face point: orders 4 (25 points), 5 (36) and 6 (49).  Device addresses of

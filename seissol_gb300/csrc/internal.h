@@ -154,7 +154,7 @@ struct DrArgs {
   const float* fsm;
   const double* imp;   // [nf][8]: zp, zs, zpn, zsn, etap, etas, inv_etas, unused
   const double* a;     // [nf][npts]
-  const double* init;  // [3][nf][npts]: sn0, tau1_0, tau2_0
+  double* init;        // [3][nf][npts]: sn0, tau1_0, tau2_0 (nucleation adds to them)
   double *psi, *v1, *v2, *slip1, *slip2, *slip, *mu, *trac1, *trac2;  // [nf][npts]
   float* isp;  // imposed states [nf][9][npts]
   float* ism;
@@ -171,7 +171,21 @@ struct DrArgs {
   float* rec;           // training samples [rec_cap][6] (nullptr: not recorded)
   unsigned* rec_count;
   unsigned rec_cap;
+  // friction law: 0 rate and state with fast velocity weakening, 1 linear slip weakening,
+  // 2 linear slip weakening with the bimaterial (Prakash-Clifton) strength, 3 the TP proxy
+  int law;
+  const double* time;  // device scalar: fault time at the start of the current step or LTS cycle
+  double time_offset;  // start of this launch's step relative to *time
+  double t0, s0;       // nucleation duration and start; t0 also ramps the forced rupture
+  int nucleate;        // 1: nucleation stresses nuc [3][nf][npts] are added over [s0, s0 + t0]
+  const double* nuc;
+  double *peak, *trup, *tdyn;  // [nf][npts] peak slip rate, rupture and dynamic-stress times
+  const double *mu_s, *mu_d, *d_c, *cohesion, *t_forced;  // slip weakening, [nf][npts]
+  double* reg;                                            // regularised strength (law 2)
+  double healing, v_star, prakash_length, tp_exponent;
 };
+// Adds dt to the device fault time t.
+int launchDrAdvanceTime(double* t, double dt, void* stream);
 int launchDrFaces(int order, const DrArgs& a, void* stream);
 int drNumPoints(int order);
 }  // namespace sei

@@ -54,8 +54,30 @@ class RSParams(C.Structure):
         return cls(**d)
 
 
+class LSWParams(C.Structure):
+    """sei_lsw_params: linear slip weakening (law 1), its bimaterial form (2) or the TP proxy (3)."""
+    _fields_ = [("law", C.c_int)] + \
+               [(n, C.c_double) for n in ("mu_s", "mu_d", "d_c", "cohesion", "sn_min", "sn_max", "tau_min", "tau_max",
+                                          "forced_rupture_time", "t0", "healing_threshold", "v_star",
+                                          "prakash_length", "tp_proxy_exponent")] + [("seed", C.c_uint64)]
+
+    @classmethod
+    def fault_config(cls, law=1, seed=7, **kw):
+        """Slip-weakening set-up of the planar-fault workload: mu_s 0.677, mu_d 0.525 and stresses near
+        those of the SCEC TPV5 benchmark (sn0 ~ U[-125, -115] MPa, tau1_0 ~ U[62, 78] MPa, below the
+        static strength), d_c 0.01 m so that weakening completes within a few steps of 100 m cells,
+        no forced rupture (set SEI_DR_FORCED_RUPTURE_TIME per point), no healing."""
+        d = dict(law=law, mu_s=0.677, mu_d=0.525, d_c=0.01, cohesion=0.0, sn_min=-125e6, sn_max=-115e6,
+                 tau_min=62e6, tau_max=78e6, forced_rupture_time=1e300, t0=0.0, healing_threshold=-1.0,
+                 v_star=0.1, prakash_length=1.0, tp_proxy_exponent=1.0 / 3.0, seed=seed)
+        d.update(kw)
+        return cls(**d)
+
+
 DR_FIELDS = {"psi": 0, "slip_rate1": 1, "slip_rate2": 2, "slip1": 3, "slip2": 4, "slip": 5, "mu": 6, "traction1": 7,
-             "traction2": 8, "a": 9, "sn0": 10, "tau1_0": 11, "tau2_0": 12}
+             "traction2": 8, "a": 9, "sn0": 10, "tau1_0": 11, "tau2_0": 12, "mu_s": 13, "mu_d": 14, "d_c": 15,
+             "cohesion": 16, "forced_rupture_time": 17, "peak_slip_rate": 18, "rupture_time": 19,
+             "dyn_stress_time": 20, "nuc_sn": 21, "nuc_tau1": 22, "nuc_tau2": 23, "reg_strength": 24}
 
 
 class _Perf(C.Structure):
@@ -123,6 +145,11 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_tc_ld_probe", i, [i, VP])
     _sig(lib, "sei_device_clock_khz", i, [i, C.POINTER(C.c_int)])
     _sig(lib, "sei_dr_setup", i, [VP, C.POINTER(RSParams), C.POINTER(i64)])
+    _sig(lib, "sei_dr_setup_lsw", i, [VP, C.POINTER(LSWParams), C.POINTER(i64)])
+    _sig(lib, "sei_dr_law", i, [VP])
+    _sig(lib, "sei_dr_set_nucleation", i, [VP, i, C.c_double, C.c_double])
+    _sig(lib, "sei_dr_get_time", i, [VP, C.POINTER(C.c_double)])
+    _sig(lib, "sei_dr_set_time", i, [VP, C.c_double])
     _sig(lib, "sei_dr_num_points", i, [i])
     _sig(lib, "sei_dr_num_faces", i64, [VP])
     _sig(lib, "sei_dr_get_faces", i, [VP, VP, VP, VP, VP, VP, VP])
@@ -405,6 +432,27 @@ class Context:
         self.nfaces = nf.value
         self.npts = self.lib.sei_dr_num_points(self.order)
         return self.nfaces
+
+    def dr_setup_lsw(self, params: "LSWParams"):
+        nf = C.c_int64()
+        self._check(self.lib.sei_dr_setup_lsw(self.h, C.byref(params), C.byref(nf)), "sei_dr_setup_lsw")
+        self.nfaces = nf.value
+        self.npts = self.lib.sei_dr_num_points(self.order)
+        return self.nfaces
+
+    def dr_law(self):
+        return self.lib.sei_dr_law(self.h)
+
+    def dr_set_nucleation(self, on=True, t0=0.0, s0=0.0):
+        self._check(self.lib.sei_dr_set_nucleation(self.h, int(on), t0, s0), "sei_dr_set_nucleation")
+
+    def dr_time(self):
+        t = C.c_double()
+        self._check(self.lib.sei_dr_get_time(self.h, C.byref(t)), "sei_dr_get_time")
+        return t.value
+
+    def dr_set_time(self, t):
+        self._check(self.lib.sei_dr_set_time(self.h, float(t)), "sei_dr_set_time")
 
     def dr_faces(self):
         nf = self.lib.sei_dr_num_faces(self.h)
