@@ -191,12 +191,47 @@ const char* sei_last_error(const sei_ctx* ctx);
  * uploads it and seeds the DOFs U[-1, 1].  Returns the cell count. */
 int sei_build_periodic_cube(sei_ctx* ctx, const sei_cube_params* p, int64_t* ncells);
 
+/* ---- mesh ingestion: the arrays of a PUML mesh (docs/puml-mesh-format.rst, read by
+ * src/Geometry/PUMLReader.cpp; the HDF5 file itself is read by the caller) ----
+ * Boundary formats: i32 (one uint32 per cell, 8 bits per face), i64 (one uint64 per cell, 16 bits
+ * per face), i32x4 (one int32 per face).  Boundary conditions (default face map,
+ * src/Initializer/FaceMap.cpp:100-110): 0 and 6 regular; 3 and above 64 dynamic rupture;
+ * 1 free surface and 5 outflow (absorbing), both without a neighbour flux, the free surface with
+ * the free-surface Godunov state in its local flux (src/Model/Common.h:319-364); 2 (gravity free
+ * surface), 4 (Dirichlet) and 7 (analytical) return SEI_ERR_UNSUPPORTED.
+ * Fault plus side (src/Geometry/MeshReader.cpp:150-170): SEI_FAULT_REF_POINT, the cell on the
+ * reference point's side of the face; SEI_FAULT_REF_NORMAL, the cell whose outward face normal
+ * has a positive dot product with the reference vector. */
+#define SEI_BOUNDARY_I32 0
+#define SEI_BOUNDARY_I64 1
+#define SEI_BOUNDARY_I32X4 2
+#define SEI_FAULT_REF_POINT 0
+#define SEI_FAULT_REF_NORMAL 1
+typedef struct sei_mesh {
+  int64_t nvertices;
+  const double* geometry;  /* [nvertices][3] */
+  int64_t ncells;
+  const int64_t* connect;  /* [ncells][4] vertex ids, every tetrahedron positively oriented */
+  const void* boundary;    /* per boundary_format; NULL: every face regular */
+  int boundary_format;
+  const int64_t* identify; /* topology format identify-vertex: [nvertices] topological vertex of each
+                              vertex (periodic or stitched meshes); NULL: geometric topology */
+  const double* material;  /* [ncells][3] rho, mu, lambda (the caller's material model per cell) */
+  double fault_ref[3];
+  int fault_ref_method;
+} sei_mesh;
+/* Builds cells, face relations, operators and the fault faces of a PUML mesh, uploads them and
+ * zeroes the DOFs; *ncells and *nfaults (either may be NULL) receive the cell and fault-face counts.
+ * A rejected mesh changes nothing.  Cells may have several fault faces.  A fault is set up with
+ * sei_dr_setup or sei_dr_setup_lsw as on the synthetic cube. */
+int sei_set_mesh(sei_ctx* ctx, const sei_mesh* mesh, int64_t* ncells, int64_t* nfaults);
+
 /* Generic mesh upload (drop-in for the LTS storage of one layer). */
 int sei_set_cells(sei_ctx* ctx, int64_t ncells, const float* star, const float* aplus, const float* aminus,
                   const int32_t* neighbor, const int8_t* side, const int8_t* orient, const int8_t* face_type);
 int64_t sei_num_cells(const sei_ctx* ctx);
 
-/* Host copies of what sei_build_periodic_cube made (for checking against independent set-ups). */
+/* Host copies of what sei_build_periodic_cube or sei_set_mesh made (for checking against independent set-ups). */
 int sei_get_cells(sei_ctx* ctx, float* star, float* aplus, float* aminus, int32_t* neighbor, int8_t* side,
                   int8_t* orient, int8_t* face_type);
 int sei_get_geometry(sei_ctx* ctx, double* vertices /*[n][4][3]*/, double* material /*[n][3] rho, mu, lambda*/,
@@ -207,7 +242,8 @@ int sei_cfl_timestep(sei_ctx* ctx, double cfl, double* dt);
 int sei_set_dofs(sei_ctx* ctx, const float* dofs);
 int sei_get_dofs(sei_ctx* ctx, float* dofs);
 int sei_get_time_integrated(sei_ctx* ctx, float* tint);
-/* Stored CK derivatives: [n][size] with store_derivatives, or [2 nfaces][size] by fault slot after sei_dr_setup. */
+/* Stored CK derivatives: [n][size] with store_derivatives, or [slots][size] by fault slot after sei_dr_setup (one
+ * slot per fault cell, sei_dr_get_slots; 2 nfaces when no cell has two fault faces). */
 int sei_get_derivatives(sei_ctx* ctx, float* derivs);
 int sei_derivatives_size(int order);
 

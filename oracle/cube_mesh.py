@@ -48,3 +48,41 @@ def periodic_cube(nx, ny, nz, h=100.0):
                 topo.append(ids)
                 coords.append(xyz)
     return np.array(topo, dtype=np.int64), np.array(coords, dtype=float)
+
+
+def box_mesh(nx, ny, nz, h=100.0, fault_x=None, fault_y=None, fault_y_tag=65):
+    """A bounded box of PUML arrays (TEST INFRASTRUCTURE ONLY): geometry [nv, 3] on the
+    (nx + 1)(ny + 1)(nz + 1) grid, connect [n, 4] (the cube split above, positively oriented),
+    boundary [n] (i32: 8 bits per face) with 1 (free surface) on the top z = nz h, 5 (outflow) on
+    the other sides, 3 on the cube-vertex plane x = fault_x h and fault_y_tag on y = fault_y h
+    (interior planes; None: none).  Cells whose tetrahedron touches both planes carry two fault faces."""
+    assert nx % 2 == 0 and ny % 2 == 0 and nz % 2 == 0
+    vid = lambda i, j, k: i + (nx + 1) * (j + (ny + 1) * k)
+    geometry = np.array([(i * h, j * h, k * h) for k in range(nz + 1) for j in range(ny + 1) for i in range(nx + 1)])
+    connect, grid = [], []
+    for parity in (0, 1):
+        for t in _tets(parity):
+            for k in range(nz):
+                for j in range(ny):
+                    for i in range(nx):
+                        if (i + j + k) % 2 != parity:
+                            continue
+                        connect.append([vid(i + a, j + b, k + c) for (a, b, c) in t])
+                        grid.append([(i + a, j + b, k + c) for (a, b, c) in t])
+    connect = np.array(connect, dtype=np.int64)
+    grid = np.array(grid)
+    face2nodes = ((0, 2, 1), (0, 1, 3), (0, 3, 2), (1, 2, 3))
+    boundary = np.zeros(len(connect), dtype=np.uint32)
+    for c in range(len(connect)):
+        for f, nodes in enumerate(face2nodes):
+            g = grid[c, list(nodes)]
+            code = 0
+            for axis, top in ((0, nx), (1, ny), (2, nz)):
+                if (g[:, axis] == 0).all() or (g[:, axis] == top).all():
+                    code = 1 if axis == 2 and (g[:, 2] == nz).all() else 5
+            if fault_x is not None and (g[:, 0] == fault_x).all():
+                code = 3
+            if fault_y is not None and (g[:, 1] == fault_y).all():
+                code = fault_y_tag
+            boundary[c] |= np.uint32(code) << np.uint32(8 * f)
+    return geometry, connect, boundary

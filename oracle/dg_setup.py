@@ -278,6 +278,32 @@ def godunov_state(local, neighbor):
     return np.eye(9) - god, god
 
 
+def free_surface_state(local):
+    """Transposed Godunov state of a free-surface face (src/Model/Common.h:319-364, elastic):
+    S = -(R21 R11^-1) from the traction rows (0, 3, 5) and velocity rows (6, 7, 8) of the first
+    three columns of the eigenvector matrix R (ElasticSetup.h:80-118), placed as QgodLocal(t_i, v_j)
+    = S(j, i), with the identity on the velocities; the neighbour state is unused (zero here)."""
+    rl, ml, ll = local
+    R = np.zeros((9, 3))
+    R[0, 0] = ll + 2 * ml
+    R[1, 0] = ll
+    R[2, 0] = ll
+    R[6, 0] = math.sqrt((ll + 2 * ml) / rl)
+    R[3, 1] = ml
+    R[7, 1] = math.sqrt(ml / rl)
+    R[5, 2] = ml
+    R[8, 2] = math.sqrt(ml / rl)
+    tr, vel = [0, 3, 5], [6, 7, 8]
+    S = -(R[vel] @ np.linalg.inv(R[tr]))
+    q = np.zeros((9, 9))
+    for i, t in enumerate(tr):
+        for j, v in enumerate(vel):
+            q[t, v] = S[j, i]
+    for v in vel:
+        q[v, v] = 1.0
+    return q, np.zeros((9, 9))
+
+
 def rotation_matrices(n, s, t):
     """Face rotation T and its inverse Tinv (ElasticSetup.h:182-198, Transformation.cpp:110-290)."""
     T = np.zeros((9, 9))
@@ -312,12 +338,13 @@ def reference_jacobian(x, y, z):
     return Ji[0], Ji[1], Ji[2]
 
 
-def cell_operators(coords: np.ndarray, material: np.ndarray, neighbor: np.ndarray, face_type=None):
+def cell_operators(coords: np.ndarray, material: np.ndarray, neighbor: np.ndarray, face_type=None, bc=None):
     """Star matrices and flux solvers for every cell.
 
     coords: [n, 4, 3] vertex coordinates (geometric, unwrapped); material: [n, 3] (rho, mu, lambda);
     neighbor: [n, 4] neighbour ids (material of the neighbour enters the Godunov state).
-    face_type: optional [n, 4] (0 regular, 1 dynamic rupture).  Returns dict with
+    face_type: optional [n, 4] (0 regular, 1 dynamic rupture); bc: optional [n, 4] boundary
+    conditions (1: free surface, whose local flux takes free_surface_state).  Returns dict with
     star [n, 3, 9, 9], AplusT [n, 4, 9, 9], AminusT [n, 4, 9, 9] (numpy [q, p] = view (q, p)).
     """
     n = coords.shape[0]
@@ -346,7 +373,10 @@ def cell_operators(coords: np.ndarray, material: np.ndarray, neighbor: np.ndarra
             t1 = t1 / np.linalg.norm(t1)
             t2 = t2 / np.linalg.norm(t2)
             nbm = material[neighbor[c, f]] if neighbor[c, f] >= 0 else material[c]
-            qgl, qgn = godunov_state(material[c], nbm)
+            if bc is not None and bc[c, f] == 1:
+                qgl, qgn = free_surface_state(material[c])
+            else:
+                qgl, qgn = godunov_state(material[c], nbm)
             Atil = coefficient_matrix_T(rho, mu, lam, 0)  # isotropic: rotation has no effect
             T, Ti = rotation_matrices(nrm, t1, t2)
             scale = -2.0 * area / (6.0 * vol)

@@ -699,6 +699,42 @@ int sei_build_periodic_cube(sei_ctx* c, const sei_cube_params* p, int64_t* ncell
   return SEI_OK;
 }
 
+int sei_set_mesh(sei_ctx* c, const sei_mesh* p, int64_t* ncells, int64_t* nfaults) {
+  if (!c || !p) return SEI_ERR_ARG;
+  sei::HostMesh mesh;
+  sei::HostFault fault;
+  std::vector<float> star, aplus, aminus;
+  try {
+    sei::ingestMesh(*p, mesh, fault);
+    sei::buildOperators(mesh, star, aplus, aminus);
+  } catch (const std::domain_error& e) {
+    return fail(c, SEI_ERR_UNSUPPORTED, e.what());
+  } catch (const std::bad_alloc&) {
+    return fail(c, SEI_ERR_OOM, "host allocation failed");
+  } catch (const std::exception& e) {
+    return fail(c, SEI_ERR_ARG, e.what());
+  }
+  const int64_t n = mesh.n;
+  if (c->cfg.device >= 0) {
+    int rc = allocArrays(c, n);
+    if (rc) return rc;
+    rc = uploadCells(c, n, star.data(), aplus.data(), aminus.data(), mesh.nbr.data(), mesh.side.data(),
+                     mesh.orient.data(), mesh.ftype.data());
+    if (rc) return rc;
+    SEI_CUDA(cudaMemset(c->Q, 0, (size_t)n * c->nq * c->Bp * sizeof(float)));
+  }
+  c->mesh = std::move(mesh);
+  c->fault = std::move(fault);
+  c->h_star = std::move(star);
+  c->h_aplus = std::move(aplus);
+  c->h_aminus = std::move(aminus);
+  c->has_fault = c->fault.nf > 0;
+  c->has_mesh = true;
+  if (ncells) *ncells = n;
+  if (nfaults) *nfaults = c->fault.nf;
+  return SEI_OK;
+}
+
 int sei_set_cells(sei_ctx* c, int64_t n, const float* star, const float* aplus, const float* aminus,
                   const int32_t* neighbor, const int8_t* side, const int8_t* orient, const int8_t* face_type) {
   if (!c || !star || !aplus || !aminus || !neighbor || !side || !orient || !face_type) return SEI_ERR_ARG;
@@ -1065,13 +1101,16 @@ int drInstall(sei_ctx* c, const std::vector<double>& st) {
   const int64_t nf = c->fault.nf;
   const int np = c->npts;
   freeFault(c);
-  // derivative slots: every fault cell stores its derivatives
+  // derivative slots: one per fault cell, in order of first appearance (plus, then minus side of
+  // each face: slots 2f and 2f + 1 when no cell has two fault faces)
   std::vector<int32_t> slot(c->n, -1), ps(nf), ms(nf);
+  int32_t nslots = 0;
   for (int64_t f = 0; f < nf; ++f) {
-    ps[f] = (int32_t)(2 * f);
-    ms[f] = (int32_t)(2 * f + 1);
-    slot[c->fault.plus_cell[f]] = ps[f];
-    slot[c->fault.minus_cell[f]] = ms[f];
+    for (int sd = 0; sd < 2; ++sd) {
+      const int32_t cell = sd ? c->fault.minus_cell[f] : c->fault.plus_cell[f];
+      if (slot[cell] < 0) slot[cell] = nslots++;
+      (sd ? ms : ps)[f] = slot[cell];
+    }
   }
   auto dalloc = [&](void** ptr, size_t bytes) { return cudaMalloc(ptr, bytes) == cudaSuccess; };
   const size_t dsz = (size_t)sei::derivativesSize(c->cfg.order) * sizeof(float);
@@ -1079,7 +1118,7 @@ int drInstall(sei_ctx* c, const std::vector<double>& st) {
   c->derivs = nullptr;
   cudaFree(c->dslot);
   c->dslot = nullptr;
-  bool ok = dalloc((void**)&c->derivs, 2 * nf * dsz) && dalloc((void**)&c->dslot, c->n * 4) &&
+  bool ok = dalloc((void**)&c->derivs, nslots * dsz) && dalloc((void**)&c->dslot, c->n * 4) &&
             dalloc((void**)&c->d_pc, nf * 4) && dalloc((void**)&c->d_mc, nf * 4) && dalloc((void**)&c->d_pslot, nf * 4) &&
             dalloc((void**)&c->d_mslot, nf * 4) && dalloc((void**)&c->d_iters, 3 * nf * np * 4) &&
             dalloc((void**)&c->d_ps, nf) && dalloc((void**)&c->d_ms, nf) && dalloc((void**)&c->d_rel, nf) &&
@@ -1108,10 +1147,10 @@ int drInstall(sei_ctx* c, const std::vector<double>& st) {
   SEI_CUDA(cudaMemset(c->d_iters, 0, 3 * nf * np * 4));
   SEI_CUDA(cudaMemset(c->d_isp, 0, nf * 9 * np * 4));
   SEI_CUDA(cudaMemset(c->d_ism, 0, nf * 9 * np * 4));
-  SEI_CUDA(cudaMemset(c->derivs, 0, 2 * nf * dsz));
+  SEI_CUDA(cudaMemset(c->derivs, 0, nslots * dsz));
   SEI_CUDA(cudaMemset(c->d_time, 0, sizeof(double)));
   c->dr_ready = true;
-  c->nslots = 2 * nf;
+  c->nslots = nslots;
   return SEI_OK;
 }
 

@@ -606,7 +606,7 @@ __global__ void __launch_bounds__(128, 3)
       const int l = e % B, p = e / B;
       float v = 0.f;
       for (int kk = 0; kk < NP; ++kk) v = fmaf(__ldg(W + l * NP + kk), sG[warp][kk * 9 + p], v);
-      q[p * Bp + l] += v;
+      atomicAdd(q + p * Bp + l, v);  // a cell may have several fault faces, in other CTAs
     }
     faceSync<TPF>(warp);
   }

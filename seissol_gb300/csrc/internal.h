@@ -29,6 +29,7 @@ struct HostMesh {
   std::vector<double> material;  // [n][3] rho, mu, lambda
   std::vector<int32_t> nbr;      // [n][4]
   std::vector<int8_t> side, orient, ftype;
+  std::vector<int8_t> bc;  // [n][4] boundary condition of a boundary face (1 free surface, 5 absorbing), else 0; empty: none
   double fault_x = 0.0;  // x of the cube's fault plane (cube vertex plane fault_plane), when built
 };
 
@@ -204,6 +205,10 @@ struct HostFault {
 // Fault faces on the plane x = xf (one cube-vertex plane of the mesh; h is the length scale of
 // the coordinate comparison).
 void buildPlanarFault(HostMesh& m, double xf, double h, HostFault& f);
+// Mesh from PUML arrays: cells, face relations, boundary conditions and the fault faces (plus
+// side by the fault reference point).  Throws std::invalid_argument on bad input and
+// std::domain_error on boundary conditions this build does not support.
+void ingestMesh(const sei_mesh& p, HostMesh& m, HostFault& f);
 void faultFaceData(const HostMesh& m, HostFault& f);
 // Steady-state state variable of the fast-velocity-weakening law at slip rate v.
 double fvwSteadyState(double v, double a, double b, double f0, double v0, double muw, double vw);

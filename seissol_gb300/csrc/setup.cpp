@@ -16,6 +16,7 @@
 #include <array>
 #include <cmath>
 #include <map>
+#include <string>
 #include <stdexcept>
 #include <vector>
 
@@ -130,6 +131,33 @@ void godunovState(const double* loc, const double* nb, Mat9& local, Mat9& neigh)
       neigh[i * 9 + j] = rhs[i * 9 + j];
       local[i * 9 + j] = (i == j ? 1.0 : 0.0) - rhs[i * 9 + j];
     }
+}
+
+// Transposed Godunov state of a free-surface face (src/Model/Common.h:319-364, elastic case):
+// S = -(R21 R11^-1) from the traction rows (0, 3, 5) and velocity rows (6, 7, 8) of the first three
+// eigenvectors, set as local(t_i, v_j) = S(j, i), and the identity on the velocities.  R11 and R21
+// are diagonal for an isotropic solid.  The neighbour state is unused (no neighbour flux); it is zero.
+void freeSurfaceState(const double* loc, Mat9& local, Mat9& neigh) {
+  const double r = loc[0], mu = loc[1], lam = loc[2];
+  local.fill(0.0);
+  neigh.fill(0.0);
+  local[0 * 9 + 6] = -(std::sqrt((lam + 2 * mu) / r) * (1.0 / (lam + 2 * mu)));
+  local[3 * 9 + 7] = -(std::sqrt(mu / r) * (1.0 / mu));
+  local[5 * 9 + 8] = -(std::sqrt(mu / r) * (1.0 / mu));
+  local[6 * 9 + 6] = local[7 * 9 + 7] = local[8 * 9 + 8] = 1.0;
+}
+
+// Godunov states of face f of cell c: the free-surface state on a free-surface boundary, else the
+// regular state with the neighbour's material (the cell's own on a boundary face,
+// CellLocalMatrices.cpp:170-177).
+void faceGodunov(const HostMesh& m, int64_t c, int f, Mat9& local, Mat9& neigh) {
+  const double* mat = &m.material[c * 3];
+  if (!m.bc.empty() && m.bc[c * 4 + f] == 1) {
+    freeSurfaceState(mat, local, neigh);
+    return;
+  }
+  const int32_t nb = m.nbr[c * 4 + f];
+  godunovState(mat, nb >= 0 ? &m.material[(int64_t)nb * 3] : mat, local, neigh);
 }
 
 void rotation(const Vec3& n, const Vec3& s, const Vec3& t, Mat9& T, Mat9& Ti) {
@@ -395,10 +423,8 @@ void buildOperators(const HostMesh& m, std::vector<float>& star, std::vector<flo
       nrm = scale(nrm, 1.0 / norm(nrm));
       t1 = scale(t1, 1.0 / norm(t1));
       t2 = scale(t2, 1.0 / norm(t2));
-      const int32_t nb = m.nbr[c * 4 + f];
-      const double* nmat = nb >= 0 ? &m.material[(int64_t)nb * 3] : mat;
       Mat9 qgl, qgn, T, Ti;
-      godunovState(mat, nmat, qgl, qgn);
+      faceGodunov(m, c, f, qgl, qgn);
       rotation(nrm, t1, t2, T, Ti);
       const double fs = -2.0 * area / (6.0 * volume);
       const bool dr = m.ftype[c * 4 + f] == 1;
@@ -487,7 +513,6 @@ void buildViscoOperators(const HostMesh& m, std::vector<float>& grad, std::vecto
   wminus.assign(m.n * 4 * 54, 0.f);
 #pragma omp parallel for schedule(static)
   for (int64_t c = 0; c < m.n; ++c) {
-    const double* mat = &m.material[c * 3];
     Vec3 v[4];
     for (int k = 0; k < 4; ++k) v[k] = {m.coords[c * 12 + k * 3], m.coords[c * 12 + k * 3 + 1], m.coords[c * 12 + k * 3 + 2]};
     const Vec3 e1 = sub(v[1], v[0]), e2 = sub(v[2], v[0]), e3 = sub(v[3], v[0]);
@@ -506,10 +531,8 @@ void buildViscoOperators(const HostMesh& m, std::vector<float>& grad, std::vecto
       nrm = scale(nrm, 1.0 / norm(nrm));
       t1 = scale(t1, 1.0 / norm(t1));
       t2 = scale(t2, 1.0 / norm(t2));
-      const int32_t nb = m.nbr[c * 4 + f];
-      const double* nmat = nb >= 0 ? &m.material[(int64_t)nb * 3] : mat;
       Mat9 qgl, qgn, T, Ti;
-      godunovState(mat, nmat, qgl, qgn);
+      faceGodunov(m, c, f, qgl, qgn);
       rotation(nrm, t1, t2, T, Ti);
       const double fs = -2.0 * area / (6.0 * volume);
       const bool dr = m.ftype[c * 4 + f] == 1;
@@ -567,15 +590,19 @@ void permuteCells(HostMesh& m, const std::vector<int64_t>& order) {
   if ((int64_t)order.size() != n) throw std::invalid_argument("permutation size");
   std::vector<int64_t> topo(n * 4);
   std::vector<double> coords(n * 12), material(n * 3);
+  std::vector<int8_t> bc(m.bc.empty() ? 0 : n * 4);
   for (int64_t i = 0; i < n; ++i) {
     const int64_t o = order[i];
     for (int k = 0; k < 4; ++k) topo[i * 4 + k] = m.topo[o * 4 + k];
     for (int k = 0; k < 12; ++k) coords[i * 12 + k] = m.coords[o * 12 + k];
     for (int k = 0; k < 3; ++k) material[i * 3 + k] = m.material[o * 3 + k];
+    if (!bc.empty())
+      for (int k = 0; k < 4; ++k) bc[i * 4 + k] = m.bc[o * 4 + k];  // face numbering stays with the cell
   }
   m.topo.swap(topo);
   m.coords.swap(coords);
   m.material.swap(material);
+  m.bc.swap(bc);
   computeFaceRelations(m);
 }
 
@@ -618,6 +645,129 @@ void buildPlanarFault(HostMesh& m, double xf, double h, HostFault& F) {
   for (int64_t c = 0; c < m.n; ++c)
     if (drCount[c] > 1) throw std::invalid_argument("a cell with more than one dynamic-rupture face is not supported");
   if (F.nf == 0) throw std::invalid_argument("fault plane has no faces (plane index outside the mesh?)");
+}
+
+void ingestMesh(const sei_mesh& p, HostMesh& m, HostFault& F) {
+  const int kMissing[4] = {3, 2, 1, 0};  // FACE2MISSINGNODE
+  if (p.nvertices <= 0 || p.ncells <= 0 || !p.geometry || !p.connect || !p.material)
+    throw std::invalid_argument("mesh needs vertices, cells, connectivity and materials");
+  if (p.ncells > (int64_t)1 << 30) throw std::invalid_argument("more than 2^30 cells");
+  if (p.boundary && (p.boundary_format < SEI_BOUNDARY_I32 || p.boundary_format > SEI_BOUNDARY_I32X4))
+    throw std::invalid_argument("unknown boundary format");
+  if (p.fault_ref_method != SEI_FAULT_REF_POINT && p.fault_ref_method != SEI_FAULT_REF_NORMAL)
+    throw std::invalid_argument("unknown fault reference method");
+  const int64_t n = p.ncells;
+  m = HostMesh();
+  F = HostFault();
+  m.n = n;
+  m.topo.resize(n * 4);
+  m.coords.resize(n * 12);
+  m.material.assign(p.material, p.material + n * 3);
+  for (int64_t c = 0; c < n; ++c) {
+    const double r = m.material[c * 3], mu = m.material[c * 3 + 1], lam = m.material[c * 3 + 2];
+    if (!(r > 0) || !(mu > 0) || !(lam + 2 * mu > 0) || !std::isfinite(r) || !std::isfinite(mu) || !std::isfinite(lam))
+      throw std::invalid_argument("cell " + std::to_string(c) + ": material needs rho > 0, mu > 0, lambda + 2 mu > 0");
+    for (int k = 0; k < 4; ++k) {
+      const int64_t v = p.connect[c * 4 + k];
+      if (v < 0 || v >= p.nvertices) throw std::invalid_argument("cell " + std::to_string(c) + ": vertex id out of range");
+      int64_t t = v;
+      if (p.identify) {
+        t = p.identify[v];
+        if (t < 0 || t >= p.nvertices) throw std::invalid_argument("identify: vertex id out of range");
+      }
+      m.topo[c * 4 + k] = t;
+      for (int x = 0; x < 3; ++x) {
+        const double q = p.geometry[v * 3 + x];
+        if (!std::isfinite(q)) throw std::invalid_argument("non-finite vertex coordinate");
+        m.coords[c * 12 + k * 3 + x] = q;
+      }
+    }
+    // positive orientation (PUML convention): det [v1 - v0, v2 - v0, v3 - v0] > 0
+    const double* w = &m.coords[c * 12];
+    const Vec3 e1{w[3] - w[0], w[4] - w[1], w[5] - w[2]}, e2{w[6] - w[0], w[7] - w[1], w[8] - w[2]},
+        e3{w[9] - w[0], w[10] - w[1], w[11] - w[2]};
+    if (!(dot(e1, cross(e2, e3)) > 0))
+      throw std::invalid_argument("cell " + std::to_string(c) + " is not positively oriented");
+  }
+  computeFaceRelations(m);
+  // boundary condition of every face (docs/puml-mesh-format.rst; the default face map of
+  // src/Initializer/FaceMap.cpp:100-110: 0, 6 regular; 1 free surface; 2 gravity free surface;
+  // 3 and above 64 dynamic rupture; 4 Dirichlet; 5 outflow; 7 analytical)
+  auto code = [&](int64_t c, int f) -> int64_t {
+    if (!p.boundary) return 0;
+    switch (p.boundary_format) {
+      case SEI_BOUNDARY_I32: return (int64_t)((static_cast<const uint32_t*>(p.boundary)[c] >> (8 * f)) & 0xFFu);
+      case SEI_BOUNDARY_I64: return (int64_t)((static_cast<const uint64_t*>(p.boundary)[c] >> (16 * f)) & 0xFFFFu);
+      default: return (int64_t)static_cast<const int32_t*>(p.boundary)[c * 4 + f];
+    }
+  };
+  m.bc.assign(n * 4, 0);
+  std::vector<char> dr(n * 4, 0);
+  for (int64_t c = 0; c < n; ++c)
+    for (int f = 0; f < 4; ++f) {
+      const int64_t b = code(c, f);
+      const int32_t d = m.nbr[c * 4 + f];
+      const std::string where = "cell " + std::to_string(c) + " face " + std::to_string(f);
+      if (b == 0 || b == 6) {
+        if (d < 0) throw std::invalid_argument(where + ": regular face without a neighbour");
+      } else if (b == 3 || b > 64) {
+        if (d < 0) throw std::invalid_argument(where + ": dynamic-rupture face without a neighbour");
+        dr[c * 4 + f] = 1;
+        dr[(int64_t)d * 4 + m.side[c * 4 + f]] = 1;
+      } else if (b == 1 || b == 5) {
+        if (d >= 0) throw std::invalid_argument(where + ": boundary condition on a face with a neighbour");
+        m.bc[c * 4 + f] = (int8_t)b;
+      } else if (b == 2 || b == 4 || b == 7) {
+        throw std::domain_error(where + ": boundary condition " + std::to_string(b) +
+                                " (gravity free surface, Dirichlet or analytical) is not supported");
+      } else {
+        throw std::invalid_argument(where + ": boundary condition " + std::to_string(b) + " is not defined");
+      }
+    }
+  for (int64_t c = 0; c < n; ++c)
+    for (int f = 0; f < 4; ++f)
+      if (m.nbr[c * 4 + f] < 0 && m.bc[c * 4 + f] == 0)
+        throw std::invalid_argument("cell " + std::to_string(c) + " face " + std::to_string(f) +
+                                    ": mesh boundary without a boundary condition");
+  // fault faces, each from its plus side: the cell on the reference point's side of the face
+  // (Point), or whose outward face normal points along the reference vector (Normal)
+  // (src/Geometry/MeshReader.cpp:150-170)
+  const Vec3 ref{p.fault_ref[0], p.fault_ref[1], p.fault_ref[2]};
+  auto isPlus = [&](int64_t c, int f, bool& onPlane) {
+    const double* w = &m.coords[c * 12];
+    auto vx = [&](int k) { return Vec3{w[k * 3], w[k * 3 + 1], w[k * 3 + 2]}; };
+    const Vec3 a = vx(kFace2Nodes[f][0]);
+    const Vec3 nrm = cross(sub(vx(kFace2Nodes[f][1]), a), sub(vx(kFace2Nodes[f][2]), a));
+    const double s = p.fault_ref_method == SEI_FAULT_REF_POINT
+                         ? dot(sub(ref, a), nrm) * dot(sub(vx(kMissing[f]), a), nrm)
+                         : dot(ref, nrm);
+    onPlane = s == 0.0;
+    return s > 0.0;
+  };
+  for (int64_t c = 0; c < n; ++c)
+    for (int f = 0; f < 4; ++f) {
+      if (!dr[c * 4 + f]) continue;
+      m.ftype[c * 4 + f] = 1;
+      bool onPlane = false;
+      if (!isPlus(c, f, onPlane)) {
+        if (onPlane)
+          throw std::invalid_argument("fault reference decides no side of the face of cell " + std::to_string(c));
+        continue;
+      }
+      const int32_t d = m.nbr[c * 4 + f];
+      const int j = m.side[c * 4 + f];
+      bool dPlane = false;
+      if (isPlus(d, j, dPlane))
+        throw std::invalid_argument("fault reference puts both cells of a face on the plus side (cell " +
+                                    std::to_string(c) + ")");
+      F.plus_cell.push_back((int32_t)c);
+      F.plus_side.push_back((uint8_t)f);
+      F.minus_cell.push_back(d);
+      F.minus_side.push_back((uint8_t)j);
+      F.rel.push_back((uint8_t)(m.orient[c * 4 + f] + 1));
+    }
+  F.nf = (int64_t)F.plus_cell.size();
+  if (F.nf > 0) faultFaceData(m, F);
 }
 
 void faultFaceData(const HostMesh& m, HostFault& F) {

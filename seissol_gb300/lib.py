@@ -80,6 +80,16 @@ DR_FIELDS = {"psi": 0, "slip_rate1": 1, "slip_rate2": 2, "slip1": 3, "slip2": 4,
              "dyn_stress_time": 20, "nuc_sn": 21, "nuc_tau1": 22, "nuc_tau2": 23, "reg_strength": 24}
 
 
+class _Mesh(C.Structure):
+    _fields_ = [("nvertices", C.c_int64), ("geometry", C.c_void_p), ("ncells", C.c_int64), ("connect", C.c_void_p),
+                ("boundary", C.c_void_p), ("boundary_format", C.c_int), ("identify", C.c_void_p),
+                ("material", C.c_void_p), ("fault_ref", C.c_double * 3), ("fault_ref_method", C.c_int)]
+
+
+BOUNDARY_FORMATS = {"i32": 0, "i64": 1, "i32x4": 2}
+FAULT_REF_METHODS = {"point": 0, "normal": 1}
+
+
 class _Perf(C.Structure):
     _fields_ = [("nonzero_flop", C.c_double), ("hardware_flop", C.c_double), ("bytes", C.c_double)]
 
@@ -146,6 +156,7 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_device_clock_khz", i, [i, C.POINTER(C.c_int)])
     _sig(lib, "sei_dr_setup", i, [VP, C.POINTER(RSParams), C.POINTER(i64)])
     _sig(lib, "sei_dr_setup_lsw", i, [VP, C.POINTER(LSWParams), C.POINTER(i64)])
+    _sig(lib, "sei_set_mesh", i, [VP, C.POINTER(_Mesh), C.POINTER(i64), C.POINTER(i64)])
     _sig(lib, "sei_dr_law", i, [VP])
     _sig(lib, "sei_dr_set_nucleation", i, [VP, i, C.c_double, C.c_double])
     _sig(lib, "sei_dr_get_time", i, [VP, C.POINTER(C.c_double)])
@@ -330,6 +341,28 @@ class Context:
         self._check(self.lib.sei_build_periodic_cube(self.h, C.byref(p), C.byref(n)), "sei_build_periodic_cube")
         self.n = n.value
         return self.n
+
+    def set_mesh(self, geometry, connect, material, boundary=None, boundary_format="i32", identify=None,
+                 fault_ref=(0.0, 0.0, 0.0), fault_ref_method="point"):
+        """Mesh from the arrays of a PUML file (sei_set_mesh): geometry [nv, 3], connect [n, 4],
+        material [n, 3] (rho, mu, lambda), boundary [n] (i32 / i64) or [n, 4] (i32x4), identify [nv]
+        (identify-vertex topology).  Returns (cells, fault faces)."""
+        geo = np.ascontiguousarray(geometry, np.float64)
+        con = np.ascontiguousarray(connect, np.int64)
+        mat = np.ascontiguousarray(material, np.float64)
+        bnd = None
+        if boundary is not None:
+            dt = {"i32": np.uint32, "i64": np.uint64, "i32x4": np.int32}[boundary_format]
+            bnd = np.ascontiguousarray(boundary, dt)
+        idn = np.ascontiguousarray(identify, np.int64) if identify is not None else None
+        m = _Mesh(geo.shape[0], geo.ctypes.data, con.shape[0], con.ctypes.data,
+                  bnd.ctypes.data if bnd is not None else None, BOUNDARY_FORMATS[boundary_format],
+                  idn.ctypes.data if idn is not None else None, mat.ctypes.data,
+                  (C.c_double * 3)(*fault_ref), FAULT_REF_METHODS[fault_ref_method])
+        n, nf = C.c_int64(), C.c_int64()
+        self._check(self.lib.sei_set_mesh(self.h, C.byref(m), C.byref(n), C.byref(nf)), "sei_set_mesh")
+        self.n = n.value
+        return self.n, nf.value
 
     def set_cells(self, star, aplus, aminus, neighbor, side, orient, face_type):
         n = star.shape[0]

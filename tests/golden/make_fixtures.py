@@ -5,7 +5,7 @@ Run in a checkout that has the reference source tree (default location given by
 compiled or imported.  Outputs:
 
 * ``godunov_elastic.json``  -- Godunov-state matrices of ``tests/Model/Values.h``
-  (homogeneous and heterogeneous elastic cases) with the two materials.
+  (homogeneous and heterogeneous elastic cases, free-surface boundary) with the two materials.
 * ``dr_matrices_pin.json`` -- for ``codegen/matrices/dr_stroud_matrices_{4,5,6}.json``: the
   quadrature points and weights in full and the same summary as below for V3mTo2n,
   V3mTo2nTWDivM and resample.
@@ -26,7 +26,7 @@ def parse_values_h(path):
     text = open(path).read()
     out = {}
     for name in ("SolutionHomogeneousLocal", "SolutionHomogeneousNeighbor",
-                 "SolutionHeterogeneousLocal", "SolutionHeterogeneousNeighbor"):
+                 "SolutionHeterogeneousLocal", "SolutionHeterogeneousNeighbor", "SolutionBoundary"):
         m = re.search(name + r"\s*=\s*\{(.*?)\};", text, re.S)
         body = m.group(1)
         rows = []
