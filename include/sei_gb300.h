@@ -370,6 +370,37 @@ int sei_lts_run(sei_ctx* ctx, int ncycles);
 int sei_lts_clusters(sei_ctx* ctx, int* nclusters, int64_t* start, double* dt);
 int sei_lts_permutation(sei_ctx* ctx, int64_t* perm /*[n]*/);
 
+/* ---- output: receivers and fault snapshots, staged to the host asynchronously ----
+ * Receivers (src/Kernels/Receiver.cpp:118-214, src/ResultWriter/ReceiverWriter.cpp): at the start
+ * of every full step (kernels all and all_dr of sei_run) the CK derivatives of the receiver cells
+ * give the solution at each sampling time inside the step, projected onto the basis functions at
+ * the receiver point; rotation and strain come from the basis gradients (Receiver.cpp:271-302).
+ * sei_receivers_setup locates the points (the lowest cell id among the cells that contain a point;
+ * a point outside the mesh is an error), keeps the quantities of quantity_mask (bit q: quantity q of
+ * xx, yy, zz, xy, yz, xz, u, v, w) and the derived ones of `derived`, and samples at sim_time,
+ * sim_time + interval, ... (sei_get_time).  n = 0 removes the receivers.  Rows are staged on the
+ * device and copied to pinned host memory on their own stream while the next steps run;
+ * sei_receivers_read waits for the copies and returns up to max_samples samples, oldest first,
+ * as [samples][receivers][columns]: time, the kept quantities, rot1-3, then eps_xx, eps_xy,
+ * eps_xz, eps_yy, eps_yz, eps_zz.  Elastic global stepping only (SEI_ERR_UNSUPPORTED under local
+ * time stepping or with the viscoelastic equations).  A new mesh removes the receivers. */
+#define SEI_RECV_ROTATION 1
+#define SEI_RECV_STRAIN 2
+int sei_receivers_setup(sei_ctx* ctx, int64_t n, const double* xyz /*[n][3]*/, double interval, unsigned quantity_mask,
+                        int derived, int64_t* cells /*[n] containing cell, may be NULL*/);
+int sei_receivers_columns(const sei_ctx* ctx);
+int sei_receivers_read(sei_ctx* ctx, double* out, int64_t max_samples, int64_t* nsamples);
+/* Simulation time: the start of the next full step; advanced by dt per full step. */
+int sei_get_time(const sei_ctx* ctx, double* t);
+int sei_set_time(sei_ctx* ctx, double t);
+/* Fault snapshots (the raw per-point counterpart of src/DynamicRupture/Output): after every
+ * `every`-th full step, the fault time and the given fields (SEI_DR_*, each [nf][npts]) are copied on
+ * the device into a staging ring and from there to pinned host memory on their own stream.
+ * sei_fault_output_read returns up to max_snapshots snapshots, oldest first, each
+ * 1 + nfields nf npts doubles.  every = 0 turns it off; a new fault set-up turns it off. */
+int sei_fault_output_setup(sei_ctx* ctx, int every, const int* fields, int nfields);
+int sei_fault_output_read(sei_ctx* ctx, double* out, int64_t max_snapshots, int64_t* nsnapshots);
+
 /* ---- dynamic rupture (built with fault_plane >= 0; orders 4-6: (order + 1)^2 = 25, 36, 49 face points) ----
  * Replaces DynamicRupture::spaceTimeInterpolation + FrictionSolver::evaluate + the DR branch of
  * Neighbor::computeNeighborsIntegral (src/Kernels/DynamicRupture.cpp:57-168,

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "output.h"
 #include "mlp.cuh"
 
 namespace sei {
@@ -74,6 +75,22 @@ struct sei_ctx {
   float mlp_norm[sei_mlp::kNorm] = {0};
   bool warm_start = false;
   bool dr_refine32 = false;  // SEI_OPT_DR_REFINE32
+  // receivers: the cells in a compact copy (unique cells), basis values at the points
+  double sim_time = 0.0;  // start of the next global step (receiver clock)
+  int64_t nrecv = 0, nrecv_cells = 0;
+  std::vector<int64_t> recv_cell;
+  int32_t *d_recv_ucell = nullptr, *d_recv_slot = nullptr;
+  float *d_recv_q = nullptr, *d_recv_i = nullptr, *d_recv_star = nullptr, *d_recv_derivs = nullptr;
+  float *d_recv_phi = nullptr, *d_recv_dphi = nullptr;
+  double recv_interval = 0.0, recv_next = 0.0;
+  unsigned recv_qmask = 0;
+  int recv_derived = 0, recv_ncols = 0;
+  sei::Stager recv_stage;
+  // fault snapshots every fault_every full steps
+  int fault_every = 0;
+  int64_t fault_steps = 0;
+  std::vector<int> fault_fields;
+  sei::Stager fault_stage;
   int tune_fail_at = -1;     // SEI_OPT_TUNE_FAIL_AT: candidate the autotuner fails on the host (tests)
   float* d_rec = nullptr;  // recorded training samples [rec_cap][6]
   unsigned* d_rec_count = nullptr;
@@ -163,9 +180,27 @@ void freeFault(sei_ctx* c) {
   c->dr_law = SEI_LAW_FVW;
   c->dr_nucleate = false;
   c->dr_t0 = c->dr_s0 = 0.0;
+  c->fault_every = 0;  // snapshots describe the fault that is gone
+  c->fault_fields.clear();
+  c->fault_stage.release();
+}
+
+void freeOutput(sei_ctx* c) {
+  for (void* p : {(void*)c->d_recv_ucell, (void*)c->d_recv_slot, (void*)c->d_recv_q, (void*)c->d_recv_i,
+                  (void*)c->d_recv_star, (void*)c->d_recv_derivs, (void*)c->d_recv_phi, (void*)c->d_recv_dphi})
+    cudaFree(p);
+  c->d_recv_ucell = c->d_recv_slot = nullptr;
+  c->d_recv_q = c->d_recv_i = c->d_recv_star = c->d_recv_derivs = c->d_recv_phi = c->d_recv_dphi = nullptr;
+  c->nrecv = c->nrecv_cells = 0;
+  c->recv_cell.clear();
+  c->recv_stage.release();
+  c->fault_every = 0;
+  c->fault_fields.clear();
+  c->fault_stage.release();
 }
 
 void freeArrays(sei_ctx* c) {
+  freeOutput(c);
   cudaFree(c->Q);
   cudaFree(c->I);
   cudaFree(c->derivs);
@@ -545,12 +580,71 @@ int runVisco(sei_ctx* c, int kernel, double dt, int steps, const double* given =
       rc = fail(c, SEI_ERR_CUDA, "viscoelastic local-integral launch failed");
     if (!rc && nbr && !(rc = profMark(c, 1)) && c->vk.neighbor(v, c->stream))
       rc = fail(c, SEI_ERR_CUDA, "viscoelastic neighbour launch failed");
+    if (!rc && kernel == SEI_KERNEL_ALL) c->sim_time += dt;
   }
   if (!rc) rc = profMark(c, -1);
   return rc;
 }
 
 // given: time-basis coefficients of the predictor's time integral (nullptr: MonomialBasis::integrate(0, dt))
+// Receiver samples of the step [sim_time, sim_time + dt) from the DOFs at its start
+// (Receiver.cpp:118-214): the CK derivatives of the receiver cells (ADER on their compact copy),
+// then the samples in batches of kRecvMaxSamples.
+int recordReceivers(sei_ctx* c, double dt) {
+  const double T = c->sim_time;
+  if (c->nrecv == 0 || !(c->recv_next < T + dt)) return SEI_OK;
+  const int blk = 9 * c->Bp;
+  if (sei::launchGatherRows((int)c->nrecv_cells, c->d_recv_ucell, c->Q, c->d_recv_q, blk, c->stream))
+    return fail(c, SEI_ERR_CUDA, "receiver gather launch failed");
+  float co[8];
+  taylorCoeffs(c->cfg.order, dt, co);
+  sei::DeviceArrays d{};
+  d.n = (int)c->nrecv_cells;
+  d.Q = c->d_recv_q;
+  d.I = c->d_recv_i;
+  d.derivs = c->d_recv_derivs;
+  d.dslot = nullptr;
+  d.star_nz = c->d_recv_star;
+  if (c->k.ader(d, co, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "receiver ADER launch failed");
+  sei::RecvEvalArgs a{};
+  a.nrecv = (int)c->nrecv;
+  a.slot = c->d_recv_slot;
+  a.derivs = c->d_recv_derivs;
+  a.phi = c->d_recv_phi;
+  a.dphi = c->d_recv_dphi;
+  a.time0 = T;
+  a.qmask = c->recv_qmask;
+  a.derived = c->recv_derived;
+  a.ncols = c->recv_ncols;
+  while (c->recv_next < T + dt) {
+    a.nsamples = 0;
+    while (a.nsamples < sei::kRecvMaxSamples && c->recv_next < T + dt) {
+      a.offset[a.nsamples++] = c->recv_next - T;
+      c->recv_next += c->recv_interval;  // ReceiverCluster::calcReceivers adds the interval likewise
+    }
+    int err = 0;
+    a.out = static_cast<double*>(c->recv_stage.reserve((size_t)a.nsamples * c->nrecv, c->stream, &err));
+    if (!a.out) return fail(c, SEI_ERR_CUDA, "receiver staging failed");
+    if (sei::launchRecvEval(c->cfg.order, a, c->stream)) return fail(c, SEI_ERR_CUDA, "receiver evaluation launch failed");
+  }
+  return SEI_OK;
+}
+
+// A snapshot of the selected fault fields after every fault_every-th full step: the fault time,
+// then each field [nf][npts], copied on the device into the staging ring.
+int recordFault(sei_ctx* c) {
+  if (c->fault_every <= 0 || !c->dr_ready || ++c->fault_steps % c->fault_every) return SEI_OK;
+  int err = 0;
+  double* row = static_cast<double*>(c->fault_stage.reserve(1, c->stream, &err));
+  if (!row) return fail(c, SEI_ERR_CUDA, "fault output staging failed");
+  const size_t plane = (size_t)c->fault.nf * c->npts;
+  SEI_CUDA(cudaMemcpyAsync(row, c->d_time, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  for (size_t i = 0; i < c->fault_fields.size(); ++i)
+    SEI_CUDA(cudaMemcpyAsync(row + 1 + i * plane, c->d_state + (size_t)c->fault_fields[i] * plane, plane * sizeof(double),
+                             cudaMemcpyDeviceToDevice, c->stream));
+  return SEI_OK;
+}
+
 int runKernel(sei_ctx* c, int kernel, double dt, int steps, const double* given = nullptr) {
   if (c->visco) return runVisco(c, kernel, dt, steps, given);
   float coeffs[8];
@@ -560,7 +654,9 @@ int runKernel(sei_ctx* c, int kernel, double dt, int steps, const double* given 
   sei::DeviceArrays d = arrays(c);
   c->prof_used = 0;
   int rc = SEI_OK;
+  const bool fullStep = kernel == SEI_KERNEL_ALL || kernel == SEI_KERNEL_ALL_DR;
   for (int s = 0; s < steps && rc == SEI_OK; ++s) {
+    if (fullStep && (rc = recordReceivers(c, dt))) return rc;
     switch (kernel) {
       case SEI_KERNEL_ALL:
         rc = launchLocal(c, d, coeffs, fusedFlux(c));
@@ -589,6 +685,10 @@ int runKernel(sei_ctx* c, int kernel, double dt, int steps, const double* given 
         break;
       default:
         return fail(c, SEI_ERR_UNSUPPORTED, "kernel not supported by this build");
+    }
+    if (fullStep && rc == SEI_OK) {
+      c->sim_time += dt;
+      rc = recordFault(c);
     }
   }
   if (!rc) rc = profMark(c, -1);
@@ -1018,7 +1118,7 @@ int sei_run_host(sei_ctx* c, int kernel, double dt, int nsteps, const float* dof
   int rc = checkReady(c);
   if (rc) return rc;
   if (!dofs_in || !dofs_out) return fail(c, SEI_ERR_ARG, "null host buffer");
-  if (kernel == SEI_KERNEL_ALL && nsteps >= 1 && !c->lts && !c->visco && c->B == c->Bp &&
+  if (kernel == SEI_KERNEL_ALL && nsteps >= 1 && !c->lts && !c->visco && c->B == c->Bp && c->nrecv == 0 &&
       !(c->fused_local && c->cfg.precision == SEI_PREC_FP32)) {
     rc = runHostPipelined(c, dt, nsteps, dofs_in, dofs_out);
     if (rc) return rc;
@@ -1074,6 +1174,157 @@ int sei_last_run_ms(sei_ctx* c, double* ms) {
   float f = 0;
   SEI_CUDA(cudaEventElapsedTime(&f, c->ev0, c->ev1));
   *ms = f;
+  return SEI_OK;
+}
+
+int sei_receivers_setup(sei_ctx* c, int64_t n, const double* xyz, double interval, unsigned qmask, int derived,
+                        int64_t* cells) {
+  int rc = checkReady(c);
+  if (rc) return rc;
+  if (!c->has_mesh) return fail(c, SEI_ERR_STATE, "receivers need a mesh built by the context");
+  if (c->visco) return fail(c, SEI_ERR_UNSUPPORTED, "receivers of the viscoelastic equations are not supported");
+  if (c->lts) return fail(c, SEI_ERR_UNSUPPORTED, "receivers under local time stepping are not supported");
+  if (n < 0 || (n > 0 && !xyz) || !(interval > 0) || !std::isfinite(interval) || qmask > 0x1FFu ||
+      (derived & ~(SEI_RECV_ROTATION | SEI_RECV_STRAIN)))
+    return fail(c, SEI_ERR_ARG, "receivers: n >= 0, points, interval > 0, quantity mask of 9 bits, derived flags");
+  std::vector<int64_t> cell;
+  std::vector<double> xez;
+  sei::locatePoints(c->mesh, n, xyz, cell, xez);
+  for (int64_t r = 0; r < n; ++r)
+    if (cell[r] < 0) return fail(c, SEI_ERR_ARG, "receiver " + std::to_string(r) + " lies outside the mesh");
+  // a rejected call changes nothing: the old receivers go only now
+  for (void* p : {(void*)c->d_recv_ucell, (void*)c->d_recv_slot, (void*)c->d_recv_q, (void*)c->d_recv_i,
+                  (void*)c->d_recv_star, (void*)c->d_recv_derivs, (void*)c->d_recv_phi, (void*)c->d_recv_dphi})
+    cudaFree(p);
+  c->d_recv_ucell = c->d_recv_slot = nullptr;
+  c->d_recv_q = c->d_recv_i = c->d_recv_star = c->d_recv_derivs = c->d_recv_phi = c->d_recv_dphi = nullptr;
+  c->recv_stage.release();
+  c->nrecv = c->nrecv_cells = 0;
+  c->recv_cell.clear();
+  if (n == 0) return SEI_OK;
+  const int order = c->cfg.order, B = sei::numBasis(order);
+  std::vector<int32_t> ucell, slot(n);
+  std::vector<int64_t> index(c->n, -1);
+  std::vector<float> phi((size_t)n * B), dphi((size_t)n * 3 * B);
+  std::vector<double> p(B), dp(3 * B);
+  for (int64_t r = 0; r < n; ++r) {
+    const int64_t cl = cell[r];
+    if (index[cl] < 0) {
+      index[cl] = (int64_t)ucell.size();
+      ucell.push_back((int32_t)cl);
+    }
+    slot[r] = (int32_t)index[cl];
+    // d xi_r / d x: rows of the inverse of [v1 - v0, v2 - v0, v3 - v0]
+    const double* v = &c->mesh.coords[cl * 12];
+    double e[3][3];
+    for (int k = 0; k < 3; ++k)
+      for (int x = 0; x < 3; ++x) e[k][x] = v[(k + 1) * 3 + x] - v[x];
+    auto cross = [](const double* a, const double* b, double* o) {
+      o[0] = a[1] * b[2] - a[2] * b[1];
+      o[1] = a[2] * b[0] - a[0] * b[2];
+      o[2] = a[0] * b[1] - a[1] * b[0];
+    };
+    double g[3][3];
+    cross(e[1], e[2], g[0]);
+    cross(e[2], e[0], g[1]);
+    cross(e[0], e[1], g[2]);
+    const double det = e[0][0] * g[0][0] + e[0][1] * g[0][1] + e[0][2] * g[0][2];
+    for (int k = 0; k < 3; ++k)
+      for (int x = 0; x < 3; ++x) g[k][x] /= det;
+    sei::basisAtPoint(order, &xez[r * 3], g, p.data(), dp.data());
+    for (int l = 0; l < B; ++l) phi[(size_t)r * B + l] = (float)p[l];
+    for (int k = 0; k < 3 * B; ++k) dphi[(size_t)r * 3 * B + k] = (float)dp[k];
+  }
+  const int64_t m = (int64_t)ucell.size();
+  const size_t blk = (size_t)9 * c->Bp, dsz = (size_t)sei::derivativesSize(order);
+  auto dalloc = [&](void** ptr, size_t bytes) { return cudaMalloc(ptr, bytes) == cudaSuccess; };
+  bool ok = dalloc((void**)&c->d_recv_ucell, m * 4) && dalloc((void**)&c->d_recv_slot, n * 4) &&
+            dalloc((void**)&c->d_recv_q, m * blk * 4) && dalloc((void**)&c->d_recv_i, m * blk * 4) &&
+            dalloc((void**)&c->d_recv_star, m * 3 * sei::kStarNnz * 4) && dalloc((void**)&c->d_recv_derivs, m * dsz * 4) &&
+            dalloc((void**)&c->d_recv_phi, phi.size() * 4) && dalloc((void**)&c->d_recv_dphi, dphi.size() * 4);
+  if (!ok) {
+    cudaGetLastError();
+    return fail(c, SEI_ERR_OOM, "device allocation for the receivers failed");
+  }
+  SEI_CUDA(cudaMemcpy(c->d_recv_ucell, ucell.data(), m * 4, cudaMemcpyHostToDevice));
+  SEI_CUDA(cudaMemcpy(c->d_recv_slot, slot.data(), n * 4, cudaMemcpyHostToDevice));
+  SEI_CUDA(cudaMemcpy(c->d_recv_phi, phi.data(), phi.size() * 4, cudaMemcpyHostToDevice));
+  SEI_CUDA(cudaMemcpy(c->d_recv_dphi, dphi.data(), dphi.size() * 4, cudaMemcpyHostToDevice));
+  if (sei::launchGatherRows((int)m, c->d_recv_ucell, c->star_nz, c->d_recv_star, 3 * sei::kStarNnz, c->stream))
+    return fail(c, SEI_ERR_CUDA, "receiver gather launch failed");
+  c->recv_qmask = qmask;
+  c->recv_derived = derived;
+  c->recv_ncols = 1 + __builtin_popcount(qmask) + ((derived & SEI_RECV_ROTATION) ? 3 : 0) +
+                  ((derived & SEI_RECV_STRAIN) ? 6 : 0);
+  const size_t rowBytes = (size_t)c->recv_ncols * sizeof(double);
+  const size_t rows = std::max<size_t>((size_t)n * sei::kRecvMaxSamples,
+                                       std::min<size_t>((size_t)n * 1024, ((size_t)64 << 20) / rowBytes));
+  if (c->recv_stage.init(rowBytes, rows) != 0) return fail(c, SEI_ERR_OOM, "receiver staging allocation failed");
+  c->nrecv = n;
+  c->nrecv_cells = m;
+  c->recv_cell = cell;
+  c->recv_interval = interval;
+  c->recv_next = c->sim_time;
+  if (cells) std::copy(cell.begin(), cell.end(), cells);
+  return SEI_OK;
+}
+
+int sei_receivers_columns(const sei_ctx* c) { return (c && c->nrecv > 0) ? c->recv_ncols : 0; }
+
+int sei_receivers_read(sei_ctx* c, double* out, int64_t max_samples, int64_t* nsamples) {
+  if (!c || !nsamples || max_samples < 0) return SEI_ERR_ARG;
+  *nsamples = 0;
+  if (c->nrecv == 0) return SEI_OK;
+  size_t rows = 0;
+  if (c->recv_stage.drain(c->stream, out, (size_t)max_samples * c->nrecv, &rows) != 0)
+    return fail(c, SEI_ERR_CUDA, "receiver staging copy failed");
+  *nsamples = (int64_t)(rows / c->nrecv);
+  return SEI_OK;
+}
+
+int sei_get_time(const sei_ctx* c, double* t) {
+  if (!c || !t) return SEI_ERR_ARG;
+  *t = c->sim_time;
+  return SEI_OK;
+}
+
+int sei_set_time(sei_ctx* c, double t) {
+  if (!c || !std::isfinite(t) || t < 0) return c ? fail(c, SEI_ERR_ARG, "time must be finite and >= 0") : SEI_ERR_ARG;
+  c->sim_time = t;
+  c->recv_next = t;
+  return SEI_OK;
+}
+
+int sei_fault_output_setup(sei_ctx* c, int every, const int* fields, int nfields) {
+  int rc = checkReady(c);
+  if (rc) return rc;
+  if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up");
+  if (every < 0 || nfields < 0 || (every > 0 && (nfields == 0 || !fields)))
+    return fail(c, SEI_ERR_ARG, "fault output: every >= 0 and at least one field");
+  for (int i = 0; i < nfields && every > 0; ++i)
+    if (fields[i] < 0 || fields[i] >= SEI_DR_NUM_FIELDS) return fail(c, SEI_ERR_ARG, "unknown friction-state field");
+  c->fault_stage.release();
+  c->fault_every = 0;
+  c->fault_fields.clear();
+  if (every == 0) return SEI_OK;
+  const size_t rowBytes = (1 + (size_t)nfields * c->fault.nf * c->npts) * sizeof(double);
+  const size_t rows = std::max<size_t>(1, std::min<size_t>(64, ((size_t)256 << 20) / rowBytes));
+  if (c->fault_stage.init(rowBytes, rows) != 0) return fail(c, SEI_ERR_OOM, "fault output staging allocation failed");
+  c->fault_fields.assign(fields, fields + nfields);
+  c->fault_every = every;
+  c->fault_steps = 0;
+  dropLtsGraph(c);
+  return SEI_OK;
+}
+
+int sei_fault_output_read(sei_ctx* c, double* out, int64_t max_snapshots, int64_t* nsnapshots) {
+  if (!c || !nsnapshots || max_snapshots < 0) return SEI_ERR_ARG;
+  *nsnapshots = 0;
+  if (c->fault_every == 0) return SEI_OK;
+  size_t rows = 0;
+  if (c->fault_stage.drain(c->stream, out, (size_t)max_snapshots, &rows) != 0)
+    return fail(c, SEI_ERR_CUDA, "fault output staging copy failed");
+  *nsnapshots = (int64_t)rows;
   return SEI_OK;
 }
 
@@ -2159,6 +2410,7 @@ int sei_lts_run(sei_ctx* c, int ncycles) {
     } else {
       rc = ltsCycle(c);
     }
+    if (rc == SEI_OK) c->sim_time += c->lts_dt0 * (double)((int64_t)1 << (c->ncl - 1));
   }
   if (!rc) rc = profMark(c, -1);
   SEI_CUDA(cudaEventRecord(c->ev1, c->stream));

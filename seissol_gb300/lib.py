@@ -157,6 +157,13 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_dr_setup", i, [VP, C.POINTER(RSParams), C.POINTER(i64)])
     _sig(lib, "sei_dr_setup_lsw", i, [VP, C.POINTER(LSWParams), C.POINTER(i64)])
     _sig(lib, "sei_set_mesh", i, [VP, C.POINTER(_Mesh), C.POINTER(i64), C.POINTER(i64)])
+    _sig(lib, "sei_receivers_setup", i, [VP, i64, VP, C.c_double, C.c_uint, i, VP])
+    _sig(lib, "sei_receivers_columns", i, [VP])
+    _sig(lib, "sei_receivers_read", i, [VP, VP, i64, C.POINTER(i64)])
+    _sig(lib, "sei_get_time", i, [VP, C.POINTER(C.c_double)])
+    _sig(lib, "sei_set_time", i, [VP, C.c_double])
+    _sig(lib, "sei_fault_output_setup", i, [VP, i, VP, i])
+    _sig(lib, "sei_fault_output_read", i, [VP, VP, i64, C.POINTER(i64)])
     _sig(lib, "sei_dr_law", i, [VP])
     _sig(lib, "sei_dr_set_nucleation", i, [VP, i, C.c_double, C.c_double])
     _sig(lib, "sei_dr_get_time", i, [VP, C.POINTER(C.c_double)])
@@ -363,6 +370,65 @@ class Context:
         self._check(self.lib.sei_set_mesh(self.h, C.byref(m), C.byref(n), C.byref(nf)), "sei_set_mesh")
         self.n = n.value
         return self.n, nf.value
+
+    # -- output ----------------------------------------------------------------------
+    def receivers_setup(self, points, interval, quantities=range(9), rotation=False, strain=False):
+        """Receivers at points [n, 3] sampled every `interval` (sei_receivers_setup); returns the
+        containing cells.  quantities: indices 0..8 kept in the output."""
+        pts = np.ascontiguousarray(points, np.float64).reshape(-1, 3)
+        mask = 0
+        for q in quantities:
+            mask |= 1 << int(q)
+        cells = np.empty(len(pts), np.int64)
+        derived = (1 if rotation else 0) | (2 if strain else 0)
+        self._check(self.lib.sei_receivers_setup(self.h, len(pts), _ptr(pts) if len(pts) else None, float(interval),
+                                                 mask, derived, _ptr(cells) if len(pts) else None),
+                    "sei_receivers_setup")
+        self.nrecv = len(pts)
+        return cells
+
+    def receivers_read(self, max_samples=1 << 20):
+        """Samples staged so far: array [samples, receivers, columns] (column 0 is the time)."""
+        ncols = self.lib.sei_receivers_columns(self.h)
+        if ncols == 0:
+            return np.zeros((0, 0, 0))
+        total = []
+        while True:
+            chunk = np.empty((1024, self.nrecv, ncols), np.float64)
+            got = C.c_int64()
+            self._check(self.lib.sei_receivers_read(self.h, _ptr(chunk), 1024, C.byref(got)), "sei_receivers_read")
+            total.append(chunk[: got.value])
+            if got.value < 1024 or sum(len(t) for t in total) >= max_samples:
+                break
+        return np.concatenate(total)
+
+    def time(self):
+        t = C.c_double()
+        self._check(self.lib.sei_get_time(self.h, C.byref(t)), "sei_get_time")
+        return t.value
+
+    def set_time(self, t):
+        self._check(self.lib.sei_set_time(self.h, float(t)), "sei_set_time")
+
+    def fault_output_setup(self, every, fields):
+        ids = np.ascontiguousarray([DR_FIELDS[f] if isinstance(f, str) else int(f) for f in fields], np.int32)
+        self._check(self.lib.sei_fault_output_setup(self.h, int(every), _ptr(ids) if len(ids) else None, len(ids)),
+                    "sei_fault_output_setup")
+        self.fault_fields = len(ids)
+
+    def fault_output_read(self):
+        """Snapshots so far: (times [k], fields [k, nfields, nfaces, npts])."""
+        per = 1 + self.fault_fields * self.nfaces * self.npts
+        out = []
+        while True:
+            chunk = np.empty((16, per), np.float64)
+            got = C.c_int64()
+            self._check(self.lib.sei_fault_output_read(self.h, _ptr(chunk), 16, C.byref(got)), "sei_fault_output_read")
+            out.append(chunk[: got.value])
+            if got.value < 16:
+                break
+        a = np.concatenate(out)
+        return a[:, 0], a[:, 1:].reshape(len(a), self.fault_fields, self.nfaces, self.npts)
 
     def set_cells(self, star, aplus, aminus, neighbor, side, orient, face_type):
         n = star.shape[0]

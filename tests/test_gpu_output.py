@@ -1,0 +1,151 @@
+"""Output path on the GPU: receivers and fault snapshots against the FP64 restatement.
+
+Receivers (src/Kernels/Receiver.cpp:118-302): periodic cube 4 x 4 x 4 (320 tets, material
++-5 %), 14 points (two sharing a cell), 3 samples per step.  For each step the oracle takes the
+GPU's DOFs at the step start (so each step is compared alone): CK derivatives in float64, the
+Taylor expansion at the sampling times, projection onto the basis at the point.  Cells and
+sampling times exact; values, rotation and strain within 2e-5 of each column's largest magnitude.
+Staging: 2,400 samples of 3 receivers (40 per step, several flushes of the device ring, a read
+in the middle) come out complete and in order.  Fault snapshots equal the fault state read
+directly after the same steps.
+"""
+import numpy as np
+import pytest
+
+from oracle import dg_setup, oracle_py, receivers
+from tests.helpers import seeded_dofs
+
+pytestmark = pytest.mark.gpu
+
+
+def _cube(order, precision=0, fault_plane=-1):
+    from seissol_gb300 import Context
+    ctx = Context(order, device=0, precision=precision)
+    n = ctx.build_periodic_cube(4, 4, 4, perturb=0.05, seed=2, fault_plane=fault_plane)
+    return ctx, n
+
+
+def _times(t0, interval, dt, steps):
+    """Sampling times by repeated addition, grouped per step (ReceiverCluster::calcReceivers)."""
+    out, nxt, T = [], t0, t0
+    for _ in range(steps):
+        cur = []
+        while nxt < T + dt:
+            cur.append(nxt)
+            nxt += interval
+        out.append(cur)
+        T += dt
+    return out
+
+
+@pytest.mark.parametrize("order,precision", [(4, 0), (5, 0), (6, 0), (6, 1)])
+def test_receivers_match_oracle(built_lib, order, precision):
+    ctx, n = _cube(order, precision)
+    rng = np.random.default_rng(order)
+    pts = rng.uniform(5.0, 395.0, (12, 3))
+    coords, material, _ = ctx.get_geometry()
+    c3, _ = receivers.locate(coords, pts[3:4])
+    pts = np.vstack([pts, coords[c3[0]].mean(axis=0), [100.0, 100.0, 100.0]])  # a second point in one cell; a vertex
+    q0 = seeded_dofs(n, order, 4)
+    ctx.set_dofs(q0)
+    dt = ctx.cfl_timestep(0.5)
+    cells = ctx.receivers_setup(pts, dt / 3.0, rotation=True, strain=True)
+    ref_cells, xez = receivers.locate(coords, pts)
+    assert np.array_equal(cells, ref_cells)
+    assert cells[12] == cells[3]
+    star = ctx.get_cells()["star"].astype(np.float64)
+    o = oracle_py.Oracle(order)
+    coeffs = dg_setup.taylor_integrate(order, 0.0, dt)
+    times = _times(0.0, dt / 3.0, dt, 4)
+    want = []
+    for s in range(4):
+        q = ctx.get_dofs()
+        _, d = o.ader(q.astype(np.float64), star, coeffs, want_derivs=True)
+        T = s * dt
+        rows = []
+        for r in range(len(pts)):
+            phi, dphi = receivers.basis_at(order, xez[r], coords[cells[r]])
+            rr = receivers.sample(order, d[cells[r]], phi, dphi, [t - T for t in times[s]], rotation=True, strain=True)
+            rr[:, 0] += T
+            rows.append(rr)
+        want.append(np.stack(rows, axis=1))  # [samples, receivers, columns]
+        ctx.run("all", dt, 1)
+    ctx.sync()
+    want = np.concatenate(want)
+    got = ctx.receivers_read()
+    assert got.shape == want.shape == (sum(len(t) for t in times), len(pts), 1 + 9 + 3 + 6)
+    assert np.array_equal(got[:, :, 0], np.broadcast_to(np.concatenate(times)[:, None], got.shape[:2]))
+    scale = np.abs(want).max(axis=(0, 1))
+    err = np.abs(got - want).max(axis=(0, 1)) / np.maximum(scale, 1e-30)
+    assert err[1:].max() < 2e-5, err
+    assert abs(ctx.time() - 4 * dt) < 1e-15
+    ctx.close()
+
+
+def test_receiver_staging_many_samples(built_lib):
+    ctx, n = _cube(4)
+    ctx.set_dofs(seeded_dofs(n, 4, 6))
+    dt = ctx.cfl_timestep(0.5)
+    pts = np.array([[50.0, 60.0, 70.0], [210.0, 120.0, 330.0], [390.0, 10.0, 200.0]])
+    ctx.receivers_setup(pts, dt / 40.0, quantities=[6, 7, 8])
+    ctx.run("all", dt, 30)
+    first = ctx.receivers_read()
+    ctx.run("all", dt, 30)
+    second = ctx.receivers_read()
+    times = np.concatenate(_times(0.0, dt / 40.0, dt, 60))
+    got = np.concatenate([first, second])
+    assert got.shape == (len(times), 3, 4)
+    assert np.array_equal(got[:, 0, 0], times) and np.array_equal(got[:, 2, 0], times)
+    assert len(first) == sum(len(t) for t in _times(0.0, dt / 40.0, dt, 30))
+    assert np.isfinite(got).all()
+    assert len(ctx.receivers_read()) == 0
+    ctx.close()
+
+
+def test_fault_snapshots_equal_state(built_lib):
+    from seissol_gb300 import LSWParams
+    ctx, n = _cube(4, fault_plane=2)
+    nf = ctx.dr_setup_lsw(LSWParams.fault_config(seed=3))
+    tf = np.full((nf, 25), 1e300)
+    tf[: nf // 2] = 0.0
+    ctx.dr_set_state("forced_rupture_time", tf)
+    ctx.set_dofs(seeded_dofs(n, 4, 8))
+    fields = ["slip_rate1", "slip", "rupture_time", "mu"]
+    ctx.fault_output_setup(2, fields)
+    dt = ctx.cfl_timestep(0.5)
+    direct = []
+    for s in range(6):
+        ctx.run("all_dr", dt, 1)
+        ctx.sync()
+        if s % 2 == 1:
+            direct.append((ctx.dr_time(), np.stack([ctx.dr_state(f) for f in fields])))
+    times, snaps = ctx.fault_output_read()
+    assert len(times) == 3
+    for k, (t, st) in enumerate(direct):
+        assert times[k] == t
+        assert np.array_equal(snaps[k], st)
+    assert (snaps[-1][2] >= 0).any()  # ruptured points carry their rupture time
+    ctx.close()
+
+
+def test_output_errors(built_lib):
+    from seissol_gb300 import SeiError
+    ctx, n = _cube(4)
+    with pytest.raises(SeiError) as e:
+        ctx.receivers_setup([[1e5, 0.0, 0.0]], 1e-3)
+    assert e.value.code == -1 and "outside" in str(e.value)
+    with pytest.raises(SeiError) as e:
+        ctx.fault_output_setup(1, ["slip"])
+    assert e.value.code == -6
+    ctx.receivers_setup([[10.0, 10.0, 10.0]], 1e-3)
+    ctx.receivers_setup([], 1e-3)  # removes them
+    assert ctx.lib.sei_receivers_columns(ctx.h) == 0
+    ctx.close()
+    from seissol_gb300 import Context
+    ctx = Context(4, device=0)
+    ctx.build_periodic_cube(8, 8, 8, perturb=0.05, seed=13, grading=6.0)
+    ctx.lts_setup(0.5, 4)
+    with pytest.raises(SeiError) as e:
+        ctx.receivers_setup([[10.0, 10.0, 10.0]], 1e-3)
+    assert e.value.code == -7
+    ctx.close()
