@@ -150,6 +150,9 @@ typedef struct sei_rs_params {
 #define SEI_LAW_LSW 1
 #define SEI_LAW_LSW_BIMATERIAL 2
 #define SEI_LAW_LSW_TP_PROXY 3
+#define SEI_LAW_RS_AGING 4  /* FL 3: rate and state, aging law (CpuImpl/AgingLaw.h) */
+#define SEI_LAW_RS_SLIP 5   /* FL 4: rate and state, slip law (CpuImpl/SlipLaw.h) */
+#define SEI_LAW_RS_SEVERE 6 /* FL 7: severe velocity weakening (CpuImpl/SevereVelocityWeakeningLaw.h) */
 
 /* Linear-slip-weakening parameters: per-point fields start uniform (mu_s, mu_d, d_c, cohesion,
  * forced_rupture_time) or seeded uniform random (sn0 in [sn_min, sn_max] <= 0, tau1_0 in
@@ -409,6 +412,13 @@ int sei_fault_output_read(sei_ctx* ctx, double* out, int64_t max_snapshots, int6
  * the fault kernel (interpolation at the Gauss-Legendre time points, friction, imposed state,
  * nodal flux into both cells), the neighbour flux of the regular faces. */
 int sei_dr_setup(sei_ctx* ctx, const sei_rs_params* p, int64_t* nfaces);
+/* A rate-and-state fault with the law SEI_LAW_FVW (= sei_dr_setup), SEI_LAW_RS_AGING, SEI_LAW_RS_SLIP or
+ * SEI_LAW_RS_SEVERE.  The slow laws take mu = a asinh(V / (2 V0) exp((f0 + b ln(V0 theta / L)) / a))
+ * (SlowVelocityWeakeningLaw.h:38-52), severe velocity weakening mu = f0 + a V / (V + V0) -
+ * b theta / (theta + L); their state variable theta (SEI_DR_PSI) starts at steady sliding at v_init
+ * (L / V, or V L / V0) and is kept as it is after each step, not resampled.  muw and vw are unused
+ * by them; the learned warm start and the float32 pre-solve serve the fast law only. */
+int sei_dr_setup_rate_state(sei_ctx* ctx, const sei_rs_params* p, int law, int64_t* nfaces);
 /* The fault with linear slip weakening (src/DynamicRupture/FrictionLaws/CpuImpl/LinearSlipWeakening.h:27-170):
  * per time point the strength -cohesion - mu min(sn, 0), the slip rate max(0, (|tau| - strength) / eta_s),
  * the accumulated slip (grown by the slip rate resampled over the face for SEI_LAW_LSW, by the slip

@@ -110,7 +110,9 @@ typedef struct {
   double* peak;    /* peak slip rate */
   double* trup;    /* rupture time, negative while pending */
   double* tdyn;    /* dynamic stress time (slip weakening), negative while pending */
-  int law;         /* 1 linear slip weakening, 2 bimaterial (Prakash-Clifton), 3 TP proxy */
+  int law;         /* oracle_dr_friction_lsw: 1 linear slip weakening, 2 bimaterial (Prakash-Clifton),
+                    * 3 TP proxy; oracle_dr_friction: 0 fast velocity weakening, 4 aging, 5 slip,
+                    * 6 severe velocity weakening */
   double healing, v_star, prakash_length, tp_exponent;
   const double *mu_s, *mu_d, *d_c, *cohesion, *t_forced;
   double* reg;     /* regularised strength (law 2) */
@@ -188,6 +190,58 @@ static double state_update(const oracle_rs_params* P, double a, double psi_ref, 
 }
 
 #define ALMOST_ZERO 1e-45
+
+/* Rate-and-state laws of the slow family and severe velocity weakening (law 4 aging, 5 slip,
+ * 6 severe velocity weakening): state updates (CpuImpl/AgingLaw.h, SlipLaw.h,
+ * SevereVelocityWeakeningLaw.h:14-29) on the state variable theta; law 0 is the fast law above. */
+static double law_state_update(const oracle_rs_params* P, int law, double a, double ref, double dt, double v) {
+  if (law == 4) {
+    const double pre = -v * (dt / P->l);
+    return ref * exp(pre) + P->l / v * -expm1(pre);
+  }
+  if (law == 5) return P->l / v * pow(v * ref / P->l, exp(-v * (dt / P->l)));
+  if (law == 6) {
+    const double steady = v * P->l / P->v0;
+    const double pre = -P->v0 * (dt / P->l);
+    return steady * -expm1(pre) + exp(pre) * ref;
+  }
+  return state_update(P, a, ref, dt, v);
+}
+
+/* The exponent argument psi of mu = a asinh(V / (2 V0) exp(psi / a)): the state itself for the fast
+ * law, f0 + b ln(V0 theta / L) for the slow laws (SlowVelocityWeakeningLaw.h:38-52). */
+static double psi_eff(const oracle_rs_params* P, int law, double state) {
+  return law == 0 ? state : P->f0 + P->b * log(P->v0 * state / P->l);
+}
+
+/* Severe velocity weakening: mu = f0 + a V / (V + V0) - b theta / (theta + L) and the generic
+ * Newton of RateAndState.h:327-385 (the residual tested before each update). */
+static double svw_mu(const oracle_rs_params* P, double a, double theta, double v) {
+  return P->f0 + a * v / (v + P->v0) - P->b * theta / (theta + P->l);
+}
+
+static int newton_svw(const oracle_rs_params* P, double a, double theta, double sn, double tau, double inv_etas,
+                      double guess, double* vout, double* muout, int* conv) {
+  double v = guess;
+  for (int i = 0; i < P->max_newton; ++i) {
+    const double mu = svw_mu(P, a, theta, v);
+    const double g = -inv_etas * (fabs(sn) * mu - tau) - v;
+    if (fabs(g) < P->newton_tol) {
+      *vout = v;
+      *muout = mu;
+      *conv = 1;
+      return i;
+    }
+    const double d = v + P->v0;
+    const double dg = -inv_etas * (fabs(sn) * a * P->v0 / (d * d)) - 1.0;
+    v = v - g / dg;
+    if (v < ALMOST_ZERO) v = ALMOST_ZERO;
+  }
+  *vout = v;
+  *muout = 0.0;
+  *conv = 0;
+  return P->max_newton;
+}
 
 /* Newton solve of g(V) = -(|sn| mu(V, psi) - tau) / eta_s - V = 0 from guess v0; returns the
  * iteration count (number of updates made) and sets *conv.  With bail, the solve gives up as
@@ -293,6 +347,8 @@ void oracle_dr_friction(int npts, int nts, int64_t nfaces, const oracle_rs_param
                         const double* resample, real* isp, real* ism, int64_t* newton_iters,
                         const float* mlp, const float* mlp_norm, int64_t* first_iters, float* rec,
                         int64_t rec_cap, int64_t* rec_count, const oracle_dr_aux* aux) {
+  const int law = aux ? aux->law : 0; /* 0 fast velocity weakening, 4 aging, 5 slip, 6 severe */
+  if (law != 0) mlp = NULL, rec = NULL;
 #pragma omp parallel
   {
     double* buf = (double*)malloc(sizeof(double) * (size_t)npts * 12);
@@ -350,9 +406,21 @@ void oracle_dr_friction(int npts, int nts, int64_t nfaces, const oracle_rs_param
           int all = 1;
           for (int k = g0; k < g1; ++k) {
             const double ak = a[fo + k];
-            psib[k] = state_update(P, ak, sref[k], dt, lsr[k]);
+            psib[k] = law_state_update(P, law, ak, sref[k], dt, lsr[k]);
             double vnew = 0, munew = 0;
             int conv = 0, its = 0;
+            if (law == 6) {
+              its = newton_svw(P, ak, psib[k], sns[k], taus[k], im->inv_etas, vmag[k], &vnew, &munew, &conv);
+              newton_iters[fo + k] += its;
+              if (first_iters && j == 0) first_iters[fo + k] += its;
+              lsr[k] = 0.5 * (vmag[k] + vnew);
+              convo[k] = fabs(vmag[k] - vnew) < P->state_tol;
+              vmag[k] = vnew;
+              mu[fo + k] = munew;
+              all &= convo[k];
+              continue;
+            }
+            const double pe = psi_eff(P, law, psib[k]);
             if (mlp && j == 0 && mlp_usable(sns[k], taus[k], ak)) {
               double lg = oracle_mlp_forward(mlp, mlp_norm, sns[k], taus[k], psib[k], ak, P->b);
               lg = lg < -103.616329 ? -103.616329 : (lg > 6.907755 ? 6.907755 : lg); /* 1e-45 .. 1e3 m/s */
@@ -363,7 +431,7 @@ void oracle_dr_friction(int npts, int nts, int64_t nfaces, const oracle_rs_param
               if (fabs(rg) < fabs(rp)) its += newton(P, ak, psib[k], sns[k], taus[k], im->inv_etas, g0, &vnew, &munew, &conv, 1);
             }
             if (!conv) {
-              its += newton(P, ak, psib[k], sns[k], taus[k], im->inv_etas, vmag[k], &vnew, &munew, &conv, 0);
+              its += newton(P, ak, pe, sns[k], taus[k], im->inv_etas, vmag[k], &vnew, &munew, &conv, 0);
               if (rec && j == 0 && conv && mlp_usable(sns[k], taus[k], ak)) {
                 int64_t idx;
 #pragma omp atomic capture
@@ -392,10 +460,11 @@ void oracle_dr_friction(int npts, int nts, int64_t nfaces, const oracle_rs_param
         }
         for (int k = 0; k < npts; ++k) {
           const double ak = a[fo + k];
-          psib[k] = state_update(P, ak, sref[k], dt, lsr[k]);
+          psib[k] = law_state_update(P, law, ak, sref[k], dt, lsr[k]);
           const double clin = 0.5 / P->v0;
-          const double cexplog = psib[k] / ak;
-          const double m = ak * arsinhexp(clin * vmag[k], cexplog, compute_cexp(cexplog));
+          const double cexplog = psi_eff(P, law, psib[k]) / ak;
+          const double m =
+              law == 6 ? svw_mu(P, ak, psib[k], vmag[k]) : ak * arsinhexp(clin * vmag[k], cexplog, compute_cexp(cexplog));
           mu[fo + k] = m;
           const double strength = -m * sns[k];
           const double t10 = init[(size_t)f * 3 * npts + npts + k];
@@ -418,12 +487,13 @@ void oracle_dr_friction(int npts, int nts, int64_t nfaces, const oracle_rs_param
         }
         t_start += dt;
       }
-      /* resample the state variable increment (FastVelocityWeakeningLaw.h:98-106) */
+      /* resample the state variable increment (FastVelocityWeakeningLaw.h:98-106); the other
+       * laws copy the state (SlowVelocityWeakeningLaw.h:66-72) */
       for (int k = 0; k < npts; ++k) dpsi[k] = psib[k] - psi[fo + k];
       for (int k = 0; k < npts; ++k) {
         double v = 0;
         for (int j = 0; j < npts; ++j) v += resample[k + (size_t)npts * j] * dpsi[j];
-        vt[k] = psi[fo + k] + v;
+        vt[k] = law == 0 ? psi[fo + k] + v : psib[k];
       }
       for (int k = 0; k < npts; ++k) psi[fo + k] = vt[k];
       /* imposed state */

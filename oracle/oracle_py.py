@@ -278,7 +278,7 @@ def dr_full_step(o, dro, Q, cells, faces, state, a, init, dt, mlp=None, record=N
     ps, ms, rel = faces["sides"][:, 0], faces["sides"][:, 1], faces["sides"][:, 2]
     qip = dro.interpolate(d[pc], ps, np.zeros_like(ps), coll)
     qim = dro.interpolate(d[mc], ms, rel, coll)
-    if aux is not None and aux.get("law", 0) != 0:
+    if aux is not None and aux.get("law", 0) in (1, 2, 3):
         isp, ism = dro.friction_lsw(qip, qim, state, init, deltat, tw, aux)
         iters = np.zeros(state["v1"].shape, np.int64)
     else:
@@ -337,7 +337,7 @@ def _dr_cluster_step(o, dr, Q, derivs, fsel, dt, time=0.0):
         aux = {k: (np.ascontiguousarray(v[fsel]) if k in AUX_ARRAYS and v is not None else v)
                for k, v in dr["aux"].items()}
         aux["time"] = time
-    if aux is not None and aux.get("law", 0) != 0:
+    if aux is not None and aux.get("law", 0) in (1, 2, 3):
         isp, ism = dro.friction_lsw(qip, qim, state, init, deltat, tw, aux)
     else:
         isp, ism, _ = dro.friction(qip, qim, state, dr["a"][fsel], init, deltat, tw, aux=aux)

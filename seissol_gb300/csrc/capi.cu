@@ -505,7 +505,7 @@ sei::DrArgs drArgs(sei_ctx* c, double dt) {
     }
   }
   a.deltat[N - 1] += x[0] * dt;
-  a.mlp = c->warm_start ? c->d_mlp : nullptr;
+  a.mlp = c->warm_start && c->dr_law == SEI_LAW_FVW ? c->d_mlp : nullptr;
   for (int i = 0; i < sei_mlp::kNorm; ++i) a.mlp_norm[i] = c->mlp_norm[i];
   a.rec = c->d_rec;
   a.rec_count = c->d_rec_count;
@@ -1427,8 +1427,14 @@ int drSetupCheck(sei_ctx* c, const void* p) {
 }  // namespace
 
 int sei_dr_setup(sei_ctx* c, const sei_rs_params* p, int64_t* nfaces) {
+  return sei_dr_setup_rate_state(c, p, SEI_LAW_FVW, nfaces);
+}
+
+int sei_dr_setup_rate_state(sei_ctx* c, const sei_rs_params* p, int law, int64_t* nfaces) {
   int rc = drSetupCheck(c, p);
   if (rc) return rc;
+  if (law != SEI_LAW_FVW && law != SEI_LAW_RS_AGING && law != SEI_LAW_RS_SLIP && law != SEI_LAW_RS_SEVERE)
+    return fail(c, SEI_ERR_ARG, "law must be a rate-and-state law (SEI_LAW_FVW, _RS_AGING, _RS_SLIP, _RS_SEVERE)");
   if (!(p->a_min > 0) || p->a_max < p->a_min || !(p->v0 > 0) || !(p->l > 0) || !(p->vw > 0) || !(p->v_init > 0) ||
       p->max_newton <= 0 || p->max_outer <= 0 || !(p->newton_tol > 0) || !(p->state_tol > 0) || p->sn_max > 0)
     return fail(c, SEI_ERR_ARG, "invalid rate-and-state parameters");
@@ -1446,10 +1452,14 @@ int sei_dr_setup(sei_ctx* c, const sei_rs_params* p, int64_t* nfaces) {
     field(SEI_DR_TAU1_0)[i] = uni(p->tau_min, p->tau_max);
     field(SEI_DR_TAU2_0)[i] = 0.0;
     field(SEI_DR_SLIP_RATE1)[i] = p->v_init;
-    field(SEI_DR_PSI)[i] = sei::fvwSteadyState(p->v_init, a, p->b, p->f0, p->v0, p->muw, p->vw);
+    // the state at steady sliding at v_init: psi of the fast law, theta = L / V (aging, slip),
+    // theta = V L / V0 (severe velocity weakening)
+    field(SEI_DR_PSI)[i] = law == SEI_LAW_FVW      ? sei::fvwSteadyState(p->v_init, a, p->b, p->f0, p->v0, p->muw, p->vw)
+                           : law == SEI_LAW_RS_SEVERE ? p->v_init * p->l / p->v0
+                                                      : p->l / p->v_init;
   }
   if ((rc = drInstall(c, st))) return rc;
-  c->dr_law = SEI_LAW_FVW;
+  c->dr_law = law;
   if (nfaces) *nfaces = nf;
   return SEI_OK;
 }

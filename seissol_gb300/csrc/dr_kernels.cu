@@ -155,6 +155,41 @@ __device__ NewtonOut newton(const sei::DrArgs& A, const LawInv& inv, double a, d
   return {v, 0.0, A.max_newton, false};
 }
 
+// ---- the other rate-and-state laws (law 4 aging, 5 slip, 6 severe velocity weakening) on the
+// state variable theta: state updates of CpuImpl/AgingLaw.h, SlipLaw.h and
+// SevereVelocityWeakeningLaw.h:14-29; the slow laws' friction is the fast law's asinh form with
+// psi = f0 + b ln(V0 theta / L) (SlowVelocityWeakeningLaw.h:38-52).
+__device__ double slowStateUpdate(const sei::DrArgs& A, const LawInv& inv, double ref, double dt, double v) {
+  if (A.law == 4) {
+    const double pre = -v * (dt * inv.l);
+    return ref * exp(pre) + A.l / v * -expm1(pre);
+  }
+  if (A.law == 5) return A.l / v * pow(v * ref * inv.l, exp(-v * (dt * inv.l)));
+  const double pre = -A.v0 * (dt * inv.l);
+  return v * A.l * inv.v0 * -expm1(pre) + exp(pre) * ref;
+}
+
+__device__ __forceinline__ double psiEff(const sei::DrArgs& A, const LawInv& inv, double state) {
+  return A.law == 0 ? state : A.f0 + A.b * log(A.v0 * state * inv.l);
+}
+
+// Severe velocity weakening: mu = f0 + a V / (V + V0) - b theta / (theta + L), generic Newton
+// (RateAndState.h:327-385).
+__device__ NewtonOut newtonSvw(const sei::DrArgs& A, double a, double theta, double sn, double tau, double invEtaS,
+                               double v) {
+  const double c = A.b * theta / (theta + A.l);
+  for (int i = 0; i < A.max_newton; ++i) {
+    const double mu = A.f0 + a * v / (v + A.v0) - c;
+    const double g = -invEtaS * (fabs(sn) * mu - tau) - v;
+    if (fabs(g) < A.newton_tol) return {v, mu, i, true};
+    const double d = v + A.v0;
+    const double dg = -invEtaS * (fabs(sn) * a * A.v0 / (d * d)) - 1.0;
+    v = v - g / dg;
+    v = v < kAlmostZero ? kAlmostZero : v;
+  }
+  return {v, 0.0, A.max_newton, false};
+}
+
 // ---- float32 solve on u = ln V.  h(u) = |sn| a asinh(e^(u + lnScale)) + eta_s e^u - tau is -eta_s
 // times the residual g and increasing and convex in u, so Newton converges from either side once
 // it is right of the root.  asinh(y) = ln(2 y) beyond y = e^9 (error below 4e-9) and y below
@@ -279,13 +314,15 @@ __device__ double smoothStep(double t, double t0) {
   return 1.0;
 }
 
-// RS: rate and state with fast velocity weakening (Newton solve of the slip rate, resampled state
-// increment); otherwise linear slip weakening (law 1: resampled slip rate; 2: bimaterial
-// regularised strength; 3: TP proxy state), CpuImpl/LinearSlipWeakening.h:27-170.
-template <int N, int B, int NP, bool RS>
+// FAM 0: rate and state with fast velocity weakening (Newton solve of the slip rate, resampled
+// state increment); FAM 1: the other rate-and-state laws, 4 aging, 5 slip, 6 severe velocity
+// weakening (state kept as it is); FAM 2: linear slip weakening (law 1: resampled slip rate;
+// 2: bimaterial regularised strength; 3: TP proxy state), CpuImpl/LinearSlipWeakening.h:27-170.
+template <int N, int B, int NP, int FAM>
 __global__ void __launch_bounds__(128, 3)
     sei_dr_faces(sei::DrArgs A, const float* __restrict__ V3m, const float* __restrict__ TW,
                  const double* __restrict__ R) {
+  constexpr bool RS = FAM != 2;
   constexpr int TPF = FaceGroup<NP>::kThreads, FPB = FaceGroup<NP>::kFaces;
   constexpr int Bp = (B + 3) / 4 * 4;
   constexpr int kQsel[6] = {0, 3, 5, 6, 7, 8};
@@ -296,8 +333,8 @@ __global__ void __launch_bounds__(128, 3)
   __shared__ float sJ[FPB][B * 9];
   __shared__ float sG[FPB][NP * 9];
   __shared__ double sD[FPB][TPF];
-  __shared__ float sW[RS ? kMlpParams : 1];
-  const bool useMlp = RS && A.mlp != nullptr;
+  __shared__ float sW[FAM == 0 ? kMlpParams : 1];
+  const bool useMlp = FAM == 0 && A.mlp != nullptr;
   if (useMlp)
     for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) sW[i] = A.mlp[i];
   __syncthreads();
@@ -415,11 +452,23 @@ __global__ void __launch_bounds__(128, 3)
       for (int j = 0; j < A.max_outer; ++j) {
         bool conv = true;
         if (pt) {
-          psib = stateUpdate(A, inv, a, sref, dt, lsr);
           NewtonOut r{};
           bool done = false;
+          double pe;
+          if constexpr (FAM == 0) {
+            psib = stateUpdate(A, inv, a, sref, dt, lsr);
+            pe = psib;
+          } else {
+            psib = slowStateUpdate(A, inv, sref, dt, lsr);
+            pe = psiEff(A, inv, psib);
+            if (A.law == 6) {
+              r = newtonSvw(A, a, psib, sn, tau, invEtaS, vmag);
+              (j == 0 ? firstIters : iters) += r.iters;
+              done = true;
+            }
+          }
           const bool net = useMlp && j == 0 && sei_mlp::usable(sn, tau, a);
-          if (net || A.refine32) {
+          if (FAM == 0 && (net || A.refine32)) {
             const Solve32 S{(float)(fabs(sn) * a), (float)etas, (float)tau, (float)(psib * inva) - lnPos(2.0 * A.v0)};
             const float u0 = lnPos(vmag);
             float u = u0;
@@ -444,9 +493,9 @@ __global__ void __launch_bounds__(128, 3)
             }
           }
           if (!done) {
-            r = newton(A, inv, a, inva, psib, sn, tau, invEtaS, vmag, false);
+            r = newton(A, inv, a, inva, pe, sn, tau, invEtaS, vmag, false);
             (j == 0 ? firstIters : iters) += r.iters;
-            if (A.rec && j == 0 && r.conv && sei_mlp::usable(sn, tau, a)) {
+            if (FAM == 0 && A.rec && j == 0 && r.conv && sei_mlp::usable(sn, tau, a)) {
               const unsigned idx = atomicAdd(A.rec_count, 1u);
               if (idx < A.rec_cap) {
                 float* o = A.rec + (size_t)idx * 6;
@@ -467,9 +516,16 @@ __global__ void __launch_bounds__(128, 3)
         if (warpAll(conv)) break;
       }
       if (pt) {
-        psib = stateUpdate(A, inv, a, sref, dt, lsr);
-        const double clin = 0.5 * inv.v0, cl = psib * inva;
-        mu = a * arsinhexp(clin * vmag, cl);
+        if constexpr (FAM == 0) {
+          psib = stateUpdate(A, inv, a, sref, dt, lsr);
+          mu = a * arsinhexp(0.5 * inv.v0 * vmag, psib * inva);
+        } else {
+          psib = slowStateUpdate(A, inv, sref, dt, lsr);
+          if (A.law == 6)
+            mu = A.f0 + a * vmag / (vmag + A.v0) - A.b * psib / (psib + A.l);
+          else
+            mu = a * arsinhexp(0.5 * inv.v0 * vmag, psiEff(A, inv, psib) * inva);
+        }
         const double strength = -mu * sn;
         slip += vmag * dt;
         const double div = strength + etas * vmag;
@@ -545,14 +601,19 @@ __global__ void __launch_bounds__(128, 3)
     tStart = tEnd;
   }
 
-  // ---- 3. resample the state-variable increment over the face (rate and state)
+  // ---- 3. resample the state-variable increment over the face (fast rate and state; the other
+  // rate-and-state laws keep their state as it is, SlowVelocityWeakeningLaw.h:66-72)
   if constexpr (RS) {
-    sD[warp][lane] = pt ? psib - psiStored : 0.0;
-    faceSync<TPF>(warp);
+    constexpr bool resample = FAM == 0;
+    if constexpr (resample) {
+      sD[warp][lane] = pt ? psib - psiStored : 0.0;
+      faceSync<TPF>(warp);
+    }
     if (pt) {
       double v = 0.0;
-      for (int j = 0; j < NP; ++j) v += R[k * NP + j] * sD[warp][j];
-      A.psi[po] = psiStored + v;
+      if constexpr (resample)
+        for (int j = 0; j < NP; ++j) v += R[k * NP + j] * sD[warp][j];
+      A.psi[po] = resample ? psiStored + v : psib;
       A.newton_iters[po] += iters + firstIters;
       A.newton_iters[(size_t)A.nfaces * NP + po] += firstIters;
       A.newton_iters[2 * (size_t)A.nfaces * NP + po] += iters32;
@@ -615,15 +676,18 @@ __global__ void __launch_bounds__(128, 3)
 template <int N, int B, int NP>
 int launch(const sei::DrArgs& a, const float* v3m, const float* tw, const double* res, void* stream) {
   if (a.face_count <= 0) return 0;
-  if (a.law < 0 || a.law > 3 || !a.peak || !a.trup || (a.nucleate && !a.nuc) ||
-      (a.law != 0 && (!a.mu_s || !a.mu_d || !a.d_c || !a.cohesion || !a.t_forced || !a.tdyn)) || (a.law == 2 && !a.reg))
+  if (a.law < 0 || a.law > 6 || !a.peak || !a.trup || (a.nucleate && !a.nuc) ||
+      (a.law >= 1 && a.law <= 3 && (!a.mu_s || !a.mu_d || !a.d_c || !a.cohesion || !a.t_forced || !a.tdyn)) ||
+      (a.law == 2 && !a.reg))
     return -1;
   constexpr int FPB = FaceGroup<NP>::kFaces;
   const int blocks = (a.face_count + FPB - 1) / FPB;
   if (a.law == 0)
-    sei_dr_faces<N, B, NP, true><<<blocks, 128, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
+    sei_dr_faces<N, B, NP, 0><<<blocks, 128, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
+  else if (a.law >= 4)
+    sei_dr_faces<N, B, NP, 1><<<blocks, 128, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
   else
-    sei_dr_faces<N, B, NP, false><<<blocks, 128, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
+    sei_dr_faces<N, B, NP, 2><<<blocks, 128, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -156,6 +156,7 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_device_clock_khz", i, [i, C.POINTER(C.c_int)])
     _sig(lib, "sei_dr_setup", i, [VP, C.POINTER(RSParams), C.POINTER(i64)])
     _sig(lib, "sei_dr_setup_lsw", i, [VP, C.POINTER(LSWParams), C.POINTER(i64)])
+    _sig(lib, "sei_dr_setup_rate_state", i, [VP, C.POINTER(RSParams), i, C.POINTER(i64)])
     _sig(lib, "sei_set_mesh", i, [VP, C.POINTER(_Mesh), C.POINTER(i64), C.POINTER(i64)])
     _sig(lib, "sei_receivers_setup", i, [VP, i64, VP, C.c_double, C.c_uint, i, VP])
     _sig(lib, "sei_receivers_columns", i, [VP])
@@ -528,6 +529,15 @@ class Context:
     def dr_setup(self, params: "RSParams"):
         nf = C.c_int64()
         self._check(self.lib.sei_dr_setup(self.h, C.byref(params), C.byref(nf)), "sei_dr_setup")
+        self.nfaces = nf.value
+        self.npts = self.lib.sei_dr_num_points(self.order)
+        return self.nfaces
+
+    def dr_setup_rate_state(self, params: "RSParams", law: int):
+        """Rate-and-state fault with law 0 (fast velocity weakening), 4 (aging), 5 (slip) or 6 (severe)."""
+        nf = C.c_int64()
+        self._check(self.lib.sei_dr_setup_rate_state(self.h, C.byref(params), int(law), C.byref(nf)),
+                    "sei_dr_setup_rate_state")
         self.nfaces = nf.value
         self.npts = self.lib.sei_dr_num_points(self.order)
         return self.nfaces
