@@ -392,6 +392,11 @@ int sei_lts_permutation(sei_ctx* ctx, int64_t* perm /*[n]*/);
 int sei_receivers_setup(sei_ctx* ctx, int64_t n, const double* xyz /*[n][3]*/, double interval, unsigned quantity_mask,
                         int derived, int64_t* cells /*[n] containing cell, may be NULL*/);
 int sei_receivers_columns(const sei_ctx* ctx);
+/* Basis functions phi [B] (B = order (order + 1) (order + 2) / 6, the reference ordering) and their
+ * derivatives dphi [3][B] along xi, eta, zeta at reference point xez, as a receiver samples them
+ * (src/Numerical/BasisFunction.h SampledBasisFunctions, SampledBasisFunctionDerivatives);
+ * context-free, host only; dphi may be NULL.  Orders 1 to 8. */
+int sei_basis_functions(int order, const double* xez /*[3]*/, double* phi, double* dphi);
 int sei_receivers_read(sei_ctx* ctx, double* out, int64_t max_samples, int64_t* nsamples);
 /* Simulation time: the start of the next full step; advanced by dt per full step. */
 int sei_get_time(const sei_ctx* ctx, double* t);

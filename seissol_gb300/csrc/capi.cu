@@ -1269,6 +1269,15 @@ int sei_receivers_setup(sei_ctx* c, int64_t n, const double* xyz, double interva
   return SEI_OK;
 }
 
+int sei_basis_functions(int order, const double* xez, double* phi, double* dphi) {
+  if (order < 1 || order > 8 || !xez || !phi) return SEI_ERR_ARG;
+  const double identity[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  std::vector<double> d((size_t)3 * sei::numBasis(order));
+  sei::basisAtPoint(order, xez, identity, phi, d.data());
+  if (dphi) std::copy(d.begin(), d.end(), dphi);
+  return SEI_OK;
+}
+
 int sei_receivers_columns(const sei_ctx* c) { return (c && c->nrecv > 0) ? c->recv_ncols : 0; }
 
 int sei_receivers_read(sei_ctx* c, double* out, int64_t max_samples, int64_t* nsamples) {

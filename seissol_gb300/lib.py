@@ -160,6 +160,7 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_set_mesh", i, [VP, C.POINTER(_Mesh), C.POINTER(i64), C.POINTER(i64)])
     _sig(lib, "sei_receivers_setup", i, [VP, i64, VP, C.c_double, C.c_uint, i, VP])
     _sig(lib, "sei_receivers_columns", i, [VP])
+    _sig(lib, "sei_basis_functions", i, [i, VP, VP, VP])
     _sig(lib, "sei_receivers_read", i, [VP, VP, i64, C.POINTER(i64)])
     _sig(lib, "sei_get_time", i, [VP, C.POINTER(C.c_double)])
     _sig(lib, "sei_set_time", i, [VP, C.c_double])

@@ -6,6 +6,8 @@ compiled or imported.  Outputs:
 
 * ``godunov_elastic.json``  -- Godunov-state matrices of ``tests/Model/Values.h``
   (homogeneous and heterogeneous elastic cases, free-surface boundary) with the two materials.
+* ``basis_functions.json`` -- basis-function values and reference-coordinate derivatives at
+  (0.3, 0.3, 0.3) of ``tests/Numerical/BasisFunctions.t.h``.
 * ``dr_matrices_pin.json`` -- for ``codegen/matrices/dr_stroud_matrices_{4,5,6}.json``: the
   quadrature points and weights in full and the same summary as below for V3mTo2n,
   V3mTo2nTWDivM and resample.
@@ -45,6 +47,23 @@ def parse_values_h(path):
     out["MaterialVal2"] = [float(x) for x in m.group(2).split(",")]
     out["_layout"] = "golden[j][i] == QgodView(i, j); materials are (rho, mu, lambda)"
     return out
+
+
+def parse_basis_tests(path):
+    """Values and reference-coordinate derivatives of the basis functions at (0.3, 0.3, 0.3),
+    tests/Numerical/BasisFunctions.t.h (orders up to 6: 56 functions)."""
+    text = open(path).read()
+    num = r"-?[0-9.]+(?:e-?[0-9]+)?"
+    i = text.index("precomputedValues", text.index("Sampled Basis Functions"))
+    body = text[i: text.index("};", i)]
+    values = [float(x) for x in re.findall(num, body[body.index("{"):])]
+    j = text.index("precomputedValues", text.index("Sampled Derivatives Functions"))
+    body = text[j: text.index("}}};", j) + 4]
+    groups = re.findall(r"\{([^{}]*)\}", body)
+    derivs = [[float(x) for x in re.findall(num, g)] for g in groups if re.search(num, g)]
+    assert len(values) == 56 and len(derivs) == 3 and all(len(d) == 56 for d in derivs)
+    return {"point": [0.3, 0.3, 0.3], "values": values, "derivatives": derivs,
+            "_layout": "derivatives[direction][function], direction = d/dxi, d/deta, d/dzeta"}
 
 
 def parse_xml(path):
@@ -90,6 +109,8 @@ def main():
         ap.error("name the reference tree with --reference or SEI_REFERENCE_ROOT")
     g = parse_values_h(os.path.join(a.reference, "tests/Model/Values.h"))
     json.dump(g, open(os.path.join(HERE, "godunov_elastic.json"), "w"), indent=1)
+    json.dump(parse_basis_tests(os.path.join(a.reference, "tests/Numerical/BasisFunctions.t.h")),
+              open(os.path.join(HERE, "basis_functions.json"), "w"), indent=1)
     pin = {}
     for b in (20, 35, 56):
         pin[str(b)] = parse_xml(os.path.join(a.reference, f"codegen/matrices/matrices_{b}.xml"))
