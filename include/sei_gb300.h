@@ -140,7 +140,14 @@ typedef struct sei_rs_params {
 #define SEI_DR_NUC_TAU2 23
 /* Regularised strength of the bimaterial law (LTSLinearSlipWeakeningBimaterial::RegularizedStrength). */
 #define SEI_DR_REG_STRENGTH 24
-#define SEI_DR_NUM_FIELDS 25
+/* Imposed slip rates (sei_dr_setup_imposed): slip direction (along tangent 1 and 2), onset time,
+ * and the source time function's tau_S and tau_R (Yoffe) or rise time (SEI_DR_TAU_S, Gaussian). */
+#define SEI_DR_SLIP_DIR1 25
+#define SEI_DR_SLIP_DIR2 26
+#define SEI_DR_ONSET_TIME 27
+#define SEI_DR_TAU_S 28
+#define SEI_DR_TAU_R 29
+#define SEI_DR_NUM_FIELDS 30
 
 /* Friction laws (src/Initializer/Parameters/DRParameters.h FrictionLawType): rate and state with
  * fast velocity weakening (FL 103, sei_dr_setup); linear slip weakening (FL 16 and FL 2), its
@@ -153,6 +160,20 @@ typedef struct sei_rs_params {
 #define SEI_LAW_RS_AGING 4  /* FL 3: rate and state, aging law (CpuImpl/AgingLaw.h) */
 #define SEI_LAW_RS_SLIP 5   /* FL 4: rate and state, slip law (CpuImpl/SlipLaw.h) */
 #define SEI_LAW_RS_SEVERE 6 /* FL 7: severe velocity weakening (CpuImpl/SevereVelocityWeakeningLaw.h) */
+#define SEI_LAW_ISR_YOFFE 7    /* FL 33: imposed slip rate, regularised Yoffe function */
+#define SEI_LAW_ISR_GAUSSIAN 8 /* FL 34: imposed slip rate, Gaussian (smooth step) */
+#define SEI_LAW_ISR_DELTA 9    /* FL 35: imposed slip rate, delta pulse */
+
+/* Imposed slip rates (CpuImpl/ImposedSlipRates.h, SourceTimeFunction.cpp): the slip rate is the
+ * slip direction times the source time function at the end of each time point; the traction is
+ * the fault stress minus eta_s times the slip rate.  Per-point fields start uniform (direction,
+ * onset time, tau_s, tau_r; the Gaussian's rise time is tau_s) with initial stresses sn0, tau1_0. */
+typedef struct sei_isr_params {
+  int law;
+  double slip_dir1, slip_dir2;
+  double onset_time, tau_s, tau_r;
+  double sn0, tau1_0;
+} sei_isr_params;
 
 /* Linear-slip-weakening parameters: per-point fields start uniform (mu_s, mu_d, d_c, cohesion,
  * forced_rupture_time) or seeded uniform random (sn0 in [sn_min, sn_max] <= 0, tau1_0 in
@@ -431,6 +452,8 @@ int sei_dr_setup_rate_state(sei_ctx* ctx, const sei_rs_params* p, int law, int64
  * state, healing.  Replaces an earlier fault set-up of the context; SEI_DR_SLIP holds the
  * accumulated slip magnitude, SEI_DR_PSI and SEI_DR_A are unused. */
 int sei_dr_setup_lsw(sei_ctx* ctx, const sei_lsw_params* p, int64_t* nfaces);
+/* The fault with an imposed slip rate (SEI_LAW_ISR_*); replaces an earlier fault set-up. */
+int sei_dr_setup_imposed(sei_ctx* ctx, const sei_isr_params* p, int64_t* nfaces);
 /* Friction law of the fault (SEI_LAW_*), -1 without one. */
 int sei_dr_law(const sei_ctx* ctx);
 /* Gaussian nucleation (FrictionSolverCommon.h:503-531 with src/Numerical/GaussianNucleationFunction.h):

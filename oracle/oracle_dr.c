@@ -666,6 +666,125 @@ void oracle_dr_friction_lsw(int npts, int nts, int64_t nfaces, const oracle_imp*
   free(rv);
   free(isacc);
 }
+
+/* Regularised Yoffe function (Tinti et al. 2005, closed form of the Yoffe function of rise time
+ * tR convolved with a triangle of half width tS; Numerical/RegularizedYoffe.h). */
+double oracle_regularized_yoffe(double t, double tS, double tR) {
+  const double pi = 3.14159265358979323846;
+  const double k = 2.0 / (pi * tR * tS * tS);
+  if (t <= 0.0 || t >= tR + 2.0 * tS) return 0.0;
+#define C1 ((0.5 * t + 0.25 * tR) * sqrt(t * (tR - t)) + (t * tR - tR * tR) * asin(sqrt(t / tR)) - \
+            0.75 * tR * tR * atan(sqrt((tR - t) / t)))
+#define C2 (0.375 * pi * tR * tR)
+#define C3 ((tS - t - 0.5 * tR) * sqrt((t - tS) * (tR - t + tS)) + tR * (2.0 * tR - 2.0 * t + 2.0 * tS) * asin(sqrt((t - tS) / tR)) + \
+            1.5 * tR * tR * atan(sqrt((tR - t + tS) / (t - tS))))
+#define C4 ((-tS + 0.5 * t + 0.25 * tR) * sqrt((t - 2.0 * tS) * (tR - t + 2.0 * tS)) - \
+            tR * (tR - t + 2.0 * tS) * asin(sqrt((t - 2.0 * tS) / tR)) - 0.75 * tR * tR * atan(sqrt((tR - t + 2.0 * tS) / (t - 2.0 * tS))))
+#define C5 (0.5 * pi * tR * (t - tR))
+#define C6 (0.5 * pi * tR * (2.0 * tS - t + tR))
+  double r;
+  if (t <= tS) r = C1 + C2;
+  else if (tR > 2.0 * tS) r = t <= 2.0 * tS ? C1 - C2 + C3 : (t < tR ? C1 + C3 + C4 : (t < tR + tS ? C3 + C4 + C5 : C4 + C6));
+  else r = t < tR ? C1 - C2 + C3 : (t <= 2.0 * tS ? C5 + C3 - C2 : (t < tR + tS ? C3 + C4 + C5 : C4 + C6));
+#undef C1
+#undef C2
+#undef C3
+#undef C4
+#undef C5
+#undef C6
+  return k * r;
+}
+
+/* Imposed slip rates, one time step of all faces (CpuImpl/ImposedSlipRates.h:21-60 in the evaluate
+ * loop of BaseFrictionLaw.h:103-137): per time point the source time function at the point's end
+ * (law 7 regularised Yoffe of (t - onset, tau_S, tau_R), 8 Gaussian smooth-step increment over
+ * the sub-step with rise time tau_S divided by it, 9 delta pulse 1/dt on (0, dt]), slip rate =
+ * direction x STF, traction = fault stress - eta_s x slip rate, slips, outputs.  dir1, dir2, onset,
+ * taus, taur are [nfaces][npts]; state fields as oracle_dr_friction (slip = accumulated magnitude). */
+void oracle_dr_friction_isr(int npts, int nts, int64_t nfaces, const oracle_imp* imp, const real* qip, const real* qim,
+                            double* init, double* v1, double* v2, double* slip1, double* slip2, double* slip,
+                            double* trac1, double* trac2, const double* deltat, const double* tweights,
+                            const double* dir1, const double* dir2, const double* onset, const double* taus,
+                            const double* taur, real* isp, real* ism, const oracle_dr_aux* x) {
+  double* fs = (double*)malloc(sizeof(double) * 3 * (size_t)nts * npts);
+  double* tr = (double*)malloc(sizeof(double) * 2 * (size_t)nts * npts);
+  double* isacc = (double*)malloc(sizeof(double) * 18 * (size_t)npts);
+  for (int64_t f = 0; f < nfaces; ++f) {
+    const oracle_imp* im = imp + f;
+    const size_t fo = (size_t)f * npts;
+    for (int s = 0; s < nts; ++s) {
+      const real* P_ = qip + ((size_t)f * nts + s) * 9 * npts;
+      const real* M_ = qim + ((size_t)f * nts + s) * 9 * npts;
+      for (int k = 0; k < npts; ++k) {
+        fs[(0 * nts + s) * npts + k] = im->etap * (QM(6) - QP(6) + QP(0) / im->zp + QM(0) / im->zpn);
+        fs[(1 * nts + s) * npts + k] = im->etas * (QM(7) - QP(7) + QP(3) / im->zs + QM(3) / im->zsn);
+        fs[(2 * nts + s) * npts + k] = im->etas * (QM(8) - QP(8) + QP(5) / im->zs + QM(5) / im->zsn);
+      }
+    }
+    double t_start = x->time;
+    for (int s = 0; s < nts; ++s) {
+      const double dt = deltat[s], t_end = t_start + dt;
+      nucleate(x, f, npts, init, t_end, dt);
+      for (int k = 0; k < npts; ++k) {
+        const size_t i = fo + k;
+        const double t = t_end - onset[i];
+        double stf;
+        if (x->law == 7)
+          stf = oracle_regularized_yoffe(t, taus[i], taur[i]);
+        else if (x->law == 8)
+          stf = (smooth_step(t, taus[i]) - smooth_step(t - dt, taus[i])) / dt;
+        else
+          stf = t > 0 && t <= dt ? 1.0 / dt : 0.0;
+        const double st1 = fs[(1 * nts + s) * npts + k], st2 = fs[(2 * nts + s) * npts + k];
+        v1[i] = dir1[i] * stf;
+        v2[i] = dir2[i] * stf;
+        const double t1 = st1 - im->etas * v1[i], t2 = st2 - im->etas * v2[i];
+        trac1[i] = t1;
+        trac2[i] = t2;
+        tr[(0 * nts + s) * npts + k] = t1;
+        tr[(1 * nts + s) * npts + k] = t2;
+        const double vm = sqrt(v1[i] * v1[i] + v2[i] * v2[i]);
+        slip1[i] += v1[i] * dt;
+        slip2[i] += v2[i] * dt;
+        slip[i] += vm * dt;
+        outputs(x, i, vm, t_start);
+      }
+      t_start = t_end;
+    }
+    memset(isacc, 0, sizeof(double) * 18 * (size_t)npts);
+    for (int s = 0; s < nts; ++s) {
+      const double w = tweights[s];
+      const real* P_ = qip + ((size_t)f * nts + s) * 9 * npts;
+      const real* M_ = qim + ((size_t)f * nts + s) * 9 * npts;
+      for (int k = 0; k < npts; ++k) {
+        const double sn = fs[(0 * nts + s) * npts + k];
+        const double t1 = tr[(0 * nts + s) * npts + k], t2 = tr[(1 * nts + s) * npts + k];
+        double* m_ = isacc;
+        double* p_ = isacc + 9 * npts;
+        m_[0 * npts + k] += w * sn;
+        m_[3 * npts + k] += w * t1;
+        m_[5 * npts + k] += w * t2;
+        m_[6 * npts + k] += w * (QM(6) - (sn - QM(0)) / im->zpn);
+        m_[7 * npts + k] += w * (QM(7) - (t1 - QM(3)) / im->zsn);
+        m_[8 * npts + k] += w * (QM(8) - (t2 - QM(5)) / im->zsn);
+        p_[0 * npts + k] += w * sn;
+        p_[3 * npts + k] += w * t1;
+        p_[5 * npts + k] += w * t2;
+        p_[6 * npts + k] += w * (QP(6) + (sn - QP(0)) / im->zp);
+        p_[7 * npts + k] += w * (QP(7) + (t1 - QP(3)) / im->zs);
+        p_[8 * npts + k] += w * (QP(8) + (t2 - QP(5)) / im->zs);
+      }
+    }
+    for (int i = 0; i < 9 * npts; ++i) {
+      ism[(size_t)f * 9 * npts + i] = (real)isacc[i];
+      isp[(size_t)f * 9 * npts + i] = (real)isacc[9 * npts + i];
+    }
+  }
+  free(fs);
+  free(tr);
+  free(isacc);
+}
+
 #undef QP
 #undef QM
 

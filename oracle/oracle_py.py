@@ -130,7 +130,8 @@ class DrAuxC(C.Structure):
                 ("cohesion", C.c_void_p), ("t_forced", C.c_void_p), ("reg", C.c_void_p)]
 
 
-AUX_ARRAYS = ("nuc", "peak", "trup", "tdyn", "mu_s", "mu_d", "d_c", "cohesion", "t_forced", "reg")
+AUX_ARRAYS = ("nuc", "peak", "trup", "tdyn", "mu_s", "mu_d", "d_c", "cohesion", "t_forced", "reg", "dir1", "dir2",
+              "onset", "taus", "taur")
 
 
 def _aux_struct(aux):
@@ -172,8 +173,8 @@ class DROracle:
         # rate-and-state constants (unused by the slip-weakening laws, which may pass {})
         self.P = RSParamsC(*[params.get(k, 0) for k in ("f0", "b", "v0", "l", "muw", "vw", "newton_tol", "state_tol",
                                                          "max_newton", "max_outer")])
-        for fn in ("oracle_dr_interpolate", "oracle_dr_friction", "oracle_dr_friction_lsw", "oracle_dr_nodal_flux",
-                   "oracle_dr_precompute"):
+        for fn in ("oracle_dr_interpolate", "oracle_dr_friction", "oracle_dr_friction_lsw", "oracle_dr_friction_isr",
+                   "oracle_dr_nodal_flux", "oracle_dr_precompute"):
             getattr(self.L, fn).restype = None
 
     def interpolate(self, derivs_per_face, side, rel, coll):
@@ -252,6 +253,32 @@ class DROracle:
             init[...] = initc
         return isp, ism
 
+    def friction_isr(self, qip, qim, state, init, deltat, tweights, aux):
+        """Imposed slip rates (aux["law"] 7, 8 or 9; aux arrays dir1, dir2, onset, taus, taur):
+        updates state, init and the aux outputs in place; returns the imposed states."""
+        nf = qip.shape[0]
+        nts = qip.shape[1]
+        imp = np.ascontiguousarray(self.f["imp"][:, :7], np.float64)
+        isp = np.zeros((nf, 9, self.npts), self.dtype)
+        ism = np.zeros((nf, 9, self.npts), self.dtype)
+        for k in STATE_FIELDS:
+            state[k] = np.ascontiguousarray(state[k], np.float64)
+        initc = np.ascontiguousarray(init, np.float64)
+        for k in ("dir1", "dir2", "onset", "taus", "taur"):
+            aux[k] = np.ascontiguousarray(aux[k], np.float64)
+        ax = _aux_struct(aux)
+        self.L.oracle_dr_friction_isr(self.npts, nts, C.c_int64(nf), _p(imp),
+                                      _p(np.ascontiguousarray(qip, self.dtype)),
+                                      _p(np.ascontiguousarray(qim, self.dtype)), _p(initc),
+                                      *[_p(state[k]) for k in ("v1", "v2", "slip1", "slip2", "slip", "trac1", "trac2")],
+                                      _p(np.ascontiguousarray(deltat, np.float64)),
+                                      _p(np.ascontiguousarray(tweights, np.float64)),
+                                      *[_p(aux[k]) for k in ("dir1", "dir2", "onset", "taus", "taur")],
+                                      _p(isp), _p(ism), C.byref(ax))
+        if initc is not init:
+            init[...] = initc
+        return isp, ism
+
     def nodal_flux(self, Q, cells, side, rel, imposed, flux):
         Q = np.array(Q, dtype=self.dtype, order="C")
         fl = np.ascontiguousarray(np.swapaxes(flux, -1, -2), np.float64)
@@ -280,6 +307,9 @@ def dr_full_step(o, dro, Q, cells, faces, state, a, init, dt, mlp=None, record=N
     qim = dro.interpolate(d[mc], ms, rel, coll)
     if aux is not None and aux.get("law", 0) in (1, 2, 3):
         isp, ism = dro.friction_lsw(qip, qim, state, init, deltat, tw, aux)
+        iters = np.zeros(state["v1"].shape, np.int64)
+    elif aux is not None and aux.get("law", 0) in (7, 8, 9):
+        isp, ism = dro.friction_isr(qip, qim, state, init, deltat, tw, aux)
         iters = np.zeros(state["v1"].shape, np.int64)
     else:
         isp, ism, iters = dro.friction(qip, qim, state, a, init, deltat, tw, mlp, record, first_iters, aux)
@@ -339,6 +369,8 @@ def _dr_cluster_step(o, dr, Q, derivs, fsel, dt, time=0.0):
         aux["time"] = time
     if aux is not None and aux.get("law", 0) in (1, 2, 3):
         isp, ism = dro.friction_lsw(qip, qim, state, init, deltat, tw, aux)
+    elif aux is not None and aux.get("law", 0) in (7, 8, 9):
+        isp, ism = dro.friction_isr(qip, qim, state, init, deltat, tw, aux)
     else:
         isp, ism, _ = dro.friction(qip, qim, state, dr["a"][fsel], init, deltat, tw, aux=aux)
     for k, v in state.items():

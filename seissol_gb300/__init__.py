@@ -14,6 +14,7 @@ from .lib import (  # noqa: F401
     Context,
     RSParams,
     LSWParams,
+    ISRParams,
     DR_FIELDS,
     SeiError,
     KERNELS,

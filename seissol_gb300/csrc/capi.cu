@@ -530,6 +530,11 @@ sei::DrArgs drArgs(sei_ctx* c, double dt) {
   a.v_star = c->lsw.v_star;
   a.prakash_length = c->lsw.prakash_length > 0 ? c->lsw.prakash_length : 1.0;
   a.tp_exponent = c->lsw.tp_proxy_exponent;
+  a.dir1 = field(SEI_DR_SLIP_DIR1);
+  a.dir2 = field(SEI_DR_SLIP_DIR2);
+  a.onset = field(SEI_DR_ONSET_TIME);
+  a.taus = field(SEI_DR_TAU_S);
+  a.taur = field(SEI_DR_TAU_R);
   return a;
 }
 
@@ -1507,6 +1512,34 @@ int sei_dr_setup_lsw(sei_ctx* c, const sei_lsw_params* p, int64_t* nfaces) {
   if ((rc = drInstall(c, st))) return rc;
   c->dr_law = p->law;
   c->dr_t0 = p->t0;
+  if (nfaces) *nfaces = nf;
+  return SEI_OK;
+}
+
+int sei_dr_setup_imposed(sei_ctx* c, const sei_isr_params* p, int64_t* nfaces) {
+  int rc = drSetupCheck(c, p);
+  if (rc) return rc;
+  if (p->law != SEI_LAW_ISR_YOFFE && p->law != SEI_LAW_ISR_GAUSSIAN && p->law != SEI_LAW_ISR_DELTA)
+    return fail(c, SEI_ERR_ARG, "law must be SEI_LAW_ISR_YOFFE, SEI_LAW_ISR_GAUSSIAN or SEI_LAW_ISR_DELTA");
+  if (!std::isfinite(p->slip_dir1) || !std::isfinite(p->slip_dir2) || !std::isfinite(p->onset_time) ||
+      !std::isfinite(p->sn0) || !std::isfinite(p->tau1_0) ||
+      (p->law == SEI_LAW_ISR_YOFFE && !(p->tau_s > 0 && p->tau_r > 0)) || (p->law == SEI_LAW_ISR_GAUSSIAN && !(p->tau_s > 0)))
+    return fail(c, SEI_ERR_ARG, "invalid imposed-slip-rate parameters");
+  c->rs = sei_rs_params{};
+  const int64_t nf = c->fault.nf;
+  const int np = sei::drNumPoints(c->cfg.order);
+  c->npts = np;
+  std::vector<double> st = drInitialState(nf, np);
+  auto fill = [&](int k, double v) { std::fill_n(st.data() + (size_t)k * nf * np, (size_t)nf * np, v); };
+  fill(SEI_DR_SN0, p->sn0);
+  fill(SEI_DR_TAU1_0, p->tau1_0);
+  fill(SEI_DR_SLIP_DIR1, p->slip_dir1);
+  fill(SEI_DR_SLIP_DIR2, p->slip_dir2);
+  fill(SEI_DR_ONSET_TIME, p->onset_time);
+  fill(SEI_DR_TAU_S, p->tau_s);
+  fill(SEI_DR_TAU_R, p->tau_r);
+  if ((rc = drInstall(c, st))) return rc;
+  c->dr_law = p->law;
   if (nfaces) *nfaces = nf;
   return SEI_OK;
 }

@@ -314,15 +314,50 @@ __device__ double smoothStep(double t, double t0) {
   return 1.0;
 }
 
+// Regularised Yoffe function: the Yoffe slip-rate function of rise time tau_R convolved with a
+// triangle of half width tau_S (Tinti et al. 2005, closed form; Numerical/RegularizedYoffe.h).
+__device__ double regularizedYoffe(double t, double tS, double tR) {
+  const double k = 2.0 / (M_PI * tR * tS * tS);
+  auto c1 = [&] {
+    return (0.5 * t + 0.25 * tR) * sqrt(t * (tR - t)) + (t * tR - tR * tR) * asin(sqrt(t / tR)) -
+           0.75 * tR * tR * atan(sqrt((tR - t) / t));
+  };
+  auto c2 = [&] { return 0.375 * M_PI * tR * tR; };
+  auto c3 = [&] {
+    return (tS - t - 0.5 * tR) * sqrt((t - tS) * (tR - t + tS)) + tR * (2.0 * tR - 2.0 * t + 2.0 * tS) * asin(sqrt((t - tS) / tR)) +
+           1.5 * tR * tR * atan(sqrt((tR - t + tS) / (t - tS)));
+  };
+  auto c4 = [&] {
+    return (-tS + 0.5 * t + 0.25 * tR) * sqrt((t - 2.0 * tS) * (tR - t + 2.0 * tS)) -
+           tR * (tR - t + 2.0 * tS) * asin(sqrt((t - 2.0 * tS) / tR)) -
+           0.75 * tR * tR * atan(sqrt((tR - t + 2.0 * tS) / (t - 2.0 * tS)));
+  };
+  auto c5 = [&] { return 0.5 * M_PI * tR * (t - tR); };
+  auto c6 = [&] { return 0.5 * M_PI * tR * (2.0 * tS - t + tR); };
+  if (t <= 0.0 || t >= tR + 2.0 * tS) return 0.0;
+  if (t <= tS) return k * (c1() + c2());
+  if (tR > 2.0 * tS) {
+    if (t <= 2.0 * tS) return k * (c1() - c2() + c3());
+    if (t < tR) return k * (c1() + c3() + c4());
+    if (t < tR + tS) return k * (c3() + c4() + c5());
+    return k * (c4() + c6());
+  }
+  if (t < tR) return k * (c1() - c2() + c3());
+  if (t <= 2.0 * tS) return k * (c5() + c3() - c2());
+  if (t < tR + tS) return k * (c3() + c4() + c5());
+  return k * (c4() + c6());
+}
+
 // FAM 0: rate and state with fast velocity weakening (Newton solve of the slip rate, resampled
 // state increment); FAM 1: the other rate-and-state laws, 4 aging, 5 slip, 6 severe velocity
 // weakening (state kept as it is); FAM 2: linear slip weakening (law 1: resampled slip rate;
-// 2: bimaterial regularised strength; 3: TP proxy state), CpuImpl/LinearSlipWeakening.h:27-170.
+// 2: bimaterial regularised strength; 3: TP proxy state), CpuImpl/LinearSlipWeakening.h:27-170;
+// FAM 3: imposed slip rates (7 Yoffe, 8 Gaussian, 9 delta), CpuImpl/ImposedSlipRates.h:21-60.
 template <int N, int B, int NP, int FAM>
 __global__ void __launch_bounds__(128, 3)
     sei_dr_faces(sei::DrArgs A, const float* __restrict__ V3m, const float* __restrict__ TW,
                  const double* __restrict__ R) {
-  constexpr bool RS = FAM != 2;
+  constexpr bool RS = FAM <= 1;
   constexpr int TPF = FaceGroup<NP>::kThreads, FPB = FaceGroup<NP>::kFaces;
   constexpr int Bp = (B + 3) / 4 * 4;
   constexpr int kQsel[6] = {0, 3, 5, 6, 7, 8};
@@ -409,14 +444,18 @@ __global__ void __launch_bounds__(128, 3)
   double psib = psiStored;
   double v1 = pt ? A.v1[po] : 1.0, v2 = pt ? A.v2[po] : 0.0;
   double slip1 = pt ? A.slip1[po] : 0.0, slip2 = pt ? A.slip2[po] : 0.0, slip = pt ? A.slip[po] : 0.0;
-  double mu = !RS && pt ? A.mu[po] : 0.0, tr1 = 0.0, tr2 = 0.0;
+  double mu = FAM == 2 && pt ? A.mu[po] : 0.0, tr1 = 0.0, tr2 = 0.0;
   double peak = pt ? A.peak[po] : 0.0, trup = pt ? A.trup[po] : 0.0;
   // slip weakening fields
-  const double muS = !RS && pt ? A.mu_s[po] : 0.0, muD = !RS && pt ? A.mu_d[po] : 0.0;
-  const double dc = !RS && pt ? A.d_c[po] : 1.0, coh = !RS && pt ? A.cohesion[po] : 0.0;
-  const double tForced = !RS && pt ? A.t_forced[po] : 0.0;
-  double tdyn = !RS && pt ? A.tdyn[po] : 0.0;
-  double reg = !RS && pt && A.law == 2 ? A.reg[po] : 0.0;
+  const double muS = FAM == 2 && pt ? A.mu_s[po] : 0.0, muD = FAM == 2 && pt ? A.mu_d[po] : 0.0;
+  const double dc = FAM == 2 && pt ? A.d_c[po] : 1.0, coh = FAM == 2 && pt ? A.cohesion[po] : 0.0;
+  const double tForced = FAM == 2 && pt ? A.t_forced[po] : 0.0;
+  double tdyn = FAM == 2 && pt ? A.tdyn[po] : 0.0;
+  double reg = FAM == 2 && pt && A.law == 2 ? A.reg[po] : 0.0;
+  // imposed slip rates
+  const double dir1 = FAM == 3 && pt ? A.dir1[po] : 0.0, dir2 = FAM == 3 && pt ? A.dir2[po] : 0.0;
+  const double onset = FAM == 3 && pt ? A.onset[po] : 0.0;
+  const double tauS = FAM == 3 && pt ? A.taus[po] : 1.0, tauR = FAM == 3 && pt ? A.taur[po] : 1.0;
   double vmag = sqrt(v1 * v1 + v2 * v2);  // slip-rate magnitude of the previous time point (slip weakening)
   double tStart = (A.time ? *A.time : 0.0) + A.time_offset;
   int iters = 0, firstIters = 0, iters32 = 0;
@@ -537,6 +576,24 @@ __global__ void __launch_bounds__(128, 3)
         slip1 += v1 * dt;
         slip2 += v2 * dt;
       }
+    } else if constexpr (FAM == 3) {
+      // the source time function at the time point's end (SourceTimeFunction.cpp)
+      const double t = tEnd - onset;
+      double stf;
+      if (A.law == 7)
+        stf = regularizedYoffe(t, tauS, tauR);
+      else if (A.law == 8)
+        stf = (smoothStep(t, tauS) - smoothStep(t - dt, tauS)) / dt;
+      else
+        stf = t > 0.0 && t <= dt ? 1.0 / dt : 0.0;
+      v1 = dir1 * stf;
+      v2 = dir2 * stf;
+      tr1 = ft1 - etas * v1;
+      tr2 = ft2 - etas * v2;
+      vmag = sqrt(v1 * v1 + v2 * v2);
+      slip1 += v1 * dt;
+      slip2 += v2 * dt;
+      slip += vmag * dt;
     } else {
       // strength from the friction coefficient of the previous time point
       const double snt = sn0 + fsn;
@@ -618,7 +675,7 @@ __global__ void __launch_bounds__(128, 3)
       A.newton_iters[(size_t)A.nfaces * NP + po] += firstIters;
       A.newton_iters[2 * (size_t)A.nfaces * NP + po] += iters32;
     }
-  } else if (pt) {
+  } else if (FAM == 2 && pt) {
     A.tdyn[po] = tdyn;
     if (A.law == 2) A.reg[po] = reg;
   }
@@ -676,16 +733,18 @@ __global__ void __launch_bounds__(128, 3)
 template <int N, int B, int NP>
 int launch(const sei::DrArgs& a, const float* v3m, const float* tw, const double* res, void* stream) {
   if (a.face_count <= 0) return 0;
-  if (a.law < 0 || a.law > 6 || !a.peak || !a.trup || (a.nucleate && !a.nuc) ||
+  if (a.law < 0 || a.law > 9 || !a.peak || !a.trup || (a.nucleate && !a.nuc) ||
       (a.law >= 1 && a.law <= 3 && (!a.mu_s || !a.mu_d || !a.d_c || !a.cohesion || !a.t_forced || !a.tdyn)) ||
-      (a.law == 2 && !a.reg))
+      (a.law == 2 && !a.reg) || (a.law >= 7 && (!a.dir1 || !a.dir2 || !a.onset || !a.taus || !a.taur)))
     return -1;
   constexpr int FPB = FaceGroup<NP>::kFaces;
   const int blocks = (a.face_count + FPB - 1) / FPB;
   if (a.law == 0)
     sei_dr_faces<N, B, NP, 0><<<blocks, 128, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
-  else if (a.law >= 4)
+  else if (a.law >= 4 && a.law <= 6)
     sei_dr_faces<N, B, NP, 1><<<blocks, 128, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
+  else if (a.law >= 7)
+    sei_dr_faces<N, B, NP, 3><<<blocks, 128, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
   else
     sei_dr_faces<N, B, NP, 2><<<blocks, 128, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;

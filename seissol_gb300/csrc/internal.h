@@ -172,8 +172,9 @@ struct DrArgs {
   float* rec;           // training samples [rec_cap][6] (nullptr: not recorded)
   unsigned* rec_count;
   unsigned rec_cap;
-  // friction law: 0 rate and state with fast velocity weakening, 1 linear slip weakening,
-  // 2 linear slip weakening with the bimaterial (Prakash-Clifton) strength, 3 the TP proxy
+  // friction law (SEI_LAW_*): 0 rate and state with fast velocity weakening, 1 linear slip
+  // weakening, 2 its bimaterial (Prakash-Clifton) form, 3 the TP proxy, 4-6 the aging, slip and
+  // severe rate-and-state laws, 7-9 imposed slip rates (Yoffe, Gaussian, delta)
   int law;
   const double* time;  // device scalar: fault time at the start of the current step or LTS cycle
   double time_offset;  // start of this launch's step relative to *time
@@ -184,6 +185,7 @@ struct DrArgs {
   const double *mu_s, *mu_d, *d_c, *cohesion, *t_forced;  // slip weakening, [nf][npts]
   double* reg;                                            // regularised strength (law 2)
   double healing, v_star, prakash_length, tp_exponent;
+  const double *dir1, *dir2, *onset, *taus, *taur;  // imposed slip rates, [nf][npts]
 };
 // Adds dt to the device fault time t.
 int launchDrAdvanceTime(double* t, double dt, void* stream);
