@@ -406,8 +406,12 @@ int sei_lts_permutation(sei_ctx* ctx, int64_t* perm /*[n]*/);
  * device and copied to pinned host memory on their own stream while the next steps run;
  * sei_receivers_read waits for the copies and returns up to max_samples samples, oldest first,
  * as [samples][receivers][columns]: time, the kept quantities, rot1-3, then eps_xx, eps_xy,
- * eps_xz, eps_yy, eps_yz, eps_zz.  Elastic global stepping only (SEI_ERR_UNSUPPORTED under local
- * time stepping or with the viscoelastic equations).  A new mesh removes the receivers. */
+ * eps_xz, eps_yy, eps_yz, eps_zz.  Under local time stepping each cluster samples its receivers at
+ * the start of each of its own steps (the times are the same sequence for all); a sample is
+ * returned once every receiver has it, and cycles run without graph replay while receivers are
+ * set.  sei_lts_setup locates existing receivers again on the reordered cells and restarts their
+ * clocks.  Elastic equations only (SEI_ERR_UNSUPPORTED with the viscoelastic ones).  A new mesh
+ * removes the receivers. */
 #define SEI_RECV_ROTATION 1
 #define SEI_RECV_STRAIN 2
 int sei_receivers_setup(sei_ctx* ctx, int64_t n, const double* xyz /*[n][3]*/, double interval, unsigned quantity_mask,
@@ -419,7 +423,9 @@ int sei_receivers_columns(const sei_ctx* ctx);
  * context-free, host only; dphi may be NULL.  Orders 1 to 8. */
 int sei_basis_functions(int order, const double* xez /*[3]*/, double* phi, double* dphi);
 int sei_receivers_read(sei_ctx* ctx, double* out, int64_t max_samples, int64_t* nsamples);
-/* Simulation time: the start of the next full step; advanced by dt per full step. */
+/* Simulation time: the start of the next full step; advanced by dt per full step (by the cycle
+ * length per LTS cycle).  sei_set_time restarts the receivers' sampling at t (unread samples are
+ * dropped). */
 int sei_get_time(const sei_ctx* ctx, double* t);
 int sei_set_time(sei_ctx* ctx, double t);
 /* Fault snapshots (the raw per-point counterpart of src/DynamicRupture/Output): after every

@@ -384,14 +384,15 @@ def _dr_cluster_step(o, dr, Q, derivs, fsel, dt, time=0.0):
     return dro.nodal_flux(Q, mc, ms, rel, ism, sub["fluxSolverMinus"])
 
 
-def lts_cycles(o, Q, cells, cluster, dt0, ncycles, dr=None):
+def lts_cycles(o, Q, cells, cluster, dt0, ncycles, dr=None, on_predict=None):
     """Rate-2 LTS (TimeCluster.cpp:358-440, 695-717; TimeCommon.cpp:40-87) in FP64.
 
     dr (optional): {"faces", "params", "state", "a", "init"[, "aux"]} of a fault whose faces join
     their cells' cluster: each cluster's correction runs the fault step of its faces over its own
     time step before the neighbour flux (TimeCluster.cpp:804-823); dr["state"] is updated in
     place, and dr["aux"] (fault time at the cycle start, nucleation, outputs, slip-weakening
-    fields) too, its time advancing by the cycle length.
+    fields) too, its time advancing by the cycle length.  on_predict(cluster, step start offset in
+    the run, its time step, Q) is called before each cluster's predictor (receivers).
 
     Every cycle advances all clusters by dt0 2^(C-1).  At sub-step k of the finest cluster the
     clusters whose step starts there predict (ADER with derivatives, integration buffer of cells
@@ -413,7 +414,7 @@ def lts_cycles(o, Q, cells, cluster, dt0, ncycles, dr=None):
     ncl_of = np.where(regular, cluster[np.where(regular, nb, 0)], cluster[:, None])
     has_coarser = (regular & (ncl_of > cluster[:, None])).any(axis=1)
     steps = 1 << (ncl - 1)
-    for _ in range(ncycles):
+    for cyc in range(ncycles):
         for k in range(steps):
             for c in range(ncl):
                 ln = 1 << c
@@ -422,6 +423,8 @@ def lts_cycles(o, Q, cells, cluster, dt0, ncycles, dr=None):
                 idx = np.nonzero(cluster == c)[0]
                 if idx.size == 0:
                     continue
+                if on_predict is not None:
+                    on_predict(c, (cyc * steps + k) * dt0, ln * dt0, Q)
                 Ic, d = o.ader(Q[idx], star[idx], dg_setup.taylor_integrate(order, 0.0, dt0 * ln), want_derivs=True)
                 I[idx] = Ic
                 if derivs is None:

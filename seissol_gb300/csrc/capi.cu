@@ -6,6 +6,7 @@
 #include <cstring>
 #include <exception>
 #include <limits>
+#include <map>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -82,10 +83,25 @@ struct sei_ctx {
   int32_t *d_recv_ucell = nullptr, *d_recv_slot = nullptr;
   float *d_recv_q = nullptr, *d_recv_i = nullptr, *d_recv_star = nullptr, *d_recv_derivs = nullptr;
   float *d_recv_phi = nullptr, *d_recv_dphi = nullptr;
-  double recv_interval = 0.0, recv_next = 0.0;
+  double recv_interval = 0.0;
   unsigned recv_qmask = 0;
   int recv_derived = 0, recv_ncols = 0;
   sei::Stager recv_stage;
+  // receiver groups: every receiver (global steps), then one per LTS cluster; each group samples
+  // the shared time sequence t_0, t_0 + interval, ... (repeated addition) with its own cursor
+  std::vector<double> recv_xyz;
+  int32_t* d_recv_list = nullptr;    // [2 nrecv]: all receivers in order, then grouped by cluster
+  std::vector<int32_t> h_recv_list;
+  std::vector<int64_t> recv_gstart;  // [ncl + 1] group offsets into the grouped half
+  std::vector<int64_t> recv_next;    // next sample index per group: clusters, then global steps
+  std::vector<double> recv_times;
+  struct RecvLaunch {
+    int64_t k0, first, count;  // rows: m samples x count receivers h_recv_list[first ...]
+    int m;
+  };
+  std::vector<RecvLaunch> recv_log;
+  std::map<int64_t, std::pair<std::vector<double>, int64_t>> recv_pending;  // sample -> rows, receivers done
+  int64_t recv_emit = 0;
   // fault snapshots every fault_every full steps
   int fault_every = 0;
   int64_t fault_steps = 0;
@@ -187,12 +203,16 @@ void freeFault(sei_ctx* c) {
 
 void freeOutput(sei_ctx* c) {
   for (void* p : {(void*)c->d_recv_ucell, (void*)c->d_recv_slot, (void*)c->d_recv_q, (void*)c->d_recv_i,
-                  (void*)c->d_recv_star, (void*)c->d_recv_derivs, (void*)c->d_recv_phi, (void*)c->d_recv_dphi})
+                  (void*)c->d_recv_star, (void*)c->d_recv_derivs, (void*)c->d_recv_phi, (void*)c->d_recv_dphi,
+                  (void*)c->d_recv_list})
     cudaFree(p);
-  c->d_recv_ucell = c->d_recv_slot = nullptr;
+  c->d_recv_ucell = c->d_recv_slot = c->d_recv_list = nullptr;
   c->d_recv_q = c->d_recv_i = c->d_recv_star = c->d_recv_derivs = c->d_recv_phi = c->d_recv_dphi = nullptr;
   c->nrecv = c->nrecv_cells = 0;
   c->recv_cell.clear();
+  c->recv_xyz.clear();
+  c->recv_log.clear();
+  c->recv_pending.clear();
   c->recv_stage.release();
   c->fault_every = 0;
   c->fault_fields.clear();
@@ -592,12 +612,19 @@ int runVisco(sei_ctx* c, int kernel, double dt, int steps, const double* given =
 }
 
 // given: time-basis coefficients of the predictor's time integral (nullptr: MonomialBasis::integrate(0, dt))
-// Receiver samples of the step [sim_time, sim_time + dt) from the DOFs at its start
+double recvTime(sei_ctx* c, int64_t k) {
+  while ((int64_t)c->recv_times.size() <= k) c->recv_times.push_back(c->recv_times.back() + c->recv_interval);
+  return c->recv_times[k];
+}
+
+// Receiver samples of group g for the step [T, T + dt) from the DOFs at its start
 // (Receiver.cpp:118-214): the CK derivatives of the receiver cells (ADER on their compact copy),
-// then the samples in batches of kRecvMaxSamples.
-int recordReceivers(sei_ctx* c, double dt) {
-  const double T = c->sim_time;
-  if (c->nrecv == 0 || !(c->recv_next < T + dt)) return SEI_OK;
+// then the group's receivers h_recv_list[first, first + count) at every sampling time inside the
+// step, in batches of kRecvMaxSamples; each batch is logged for the host-side assembly.
+int recordReceivers(sei_ctx* c, int g, double T, double dt, int64_t first, int64_t count) {
+  if (c->nrecv == 0 || count == 0) return SEI_OK;
+  int64_t& k = c->recv_next[g];
+  if (!(recvTime(c, k) < T + dt)) return SEI_OK;
   const int blk = 9 * c->Bp;
   if (sei::launchGatherRows((int)c->nrecv_cells, c->d_recv_ucell, c->Q, c->d_recv_q, blk, c->stream))
     return fail(c, SEI_ERR_CUDA, "receiver gather launch failed");
@@ -612,7 +639,8 @@ int recordReceivers(sei_ctx* c, double dt) {
   d.star_nz = c->d_recv_star;
   if (c->k.ader(d, co, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "receiver ADER launch failed");
   sei::RecvEvalArgs a{};
-  a.nrecv = (int)c->nrecv;
+  a.nrecv = (int)count;
+  a.list = c->d_recv_list + first;
   a.slot = c->d_recv_slot;
   a.derivs = c->d_recv_derivs;
   a.phi = c->d_recv_phi;
@@ -621,16 +649,15 @@ int recordReceivers(sei_ctx* c, double dt) {
   a.qmask = c->recv_qmask;
   a.derived = c->recv_derived;
   a.ncols = c->recv_ncols;
-  while (c->recv_next < T + dt) {
+  while (recvTime(c, k) < T + dt) {
+    const int64_t k0 = k;
     a.nsamples = 0;
-    while (a.nsamples < sei::kRecvMaxSamples && c->recv_next < T + dt) {
-      a.offset[a.nsamples++] = c->recv_next - T;
-      c->recv_next += c->recv_interval;  // ReceiverCluster::calcReceivers adds the interval likewise
-    }
+    while (a.nsamples < sei::kRecvMaxSamples && recvTime(c, k) < T + dt) a.offset[a.nsamples++] = recvTime(c, k++) - T;
     int err = 0;
-    a.out = static_cast<double*>(c->recv_stage.reserve((size_t)a.nsamples * c->nrecv, c->stream, &err));
+    a.out = static_cast<double*>(c->recv_stage.reserve((size_t)a.nsamples * count, c->stream, &err));
     if (!a.out) return fail(c, SEI_ERR_CUDA, "receiver staging failed");
     if (sei::launchRecvEval(c->cfg.order, a, c->stream)) return fail(c, SEI_ERR_CUDA, "receiver evaluation launch failed");
+    c->recv_log.push_back({k0, first, count, a.nsamples});
   }
   return SEI_OK;
 }
@@ -661,7 +688,9 @@ int runKernel(sei_ctx* c, int kernel, double dt, int steps, const double* given 
   int rc = SEI_OK;
   const bool fullStep = kernel == SEI_KERNEL_ALL || kernel == SEI_KERNEL_ALL_DR;
   for (int s = 0; s < steps && rc == SEI_OK; ++s) {
-    if (fullStep && (rc = recordReceivers(c, dt))) return rc;
+    if (fullStep && c->nrecv &&
+        (rc = recordReceivers(c, (int)c->recv_next.size() - 1, c->sim_time, dt, 0, c->nrecv)))
+      return rc;
     switch (kernel) {
       case SEI_KERNEL_ALL:
         rc = launchLocal(c, d, coeffs, fusedFlux(c));
@@ -1188,7 +1217,6 @@ int sei_receivers_setup(sei_ctx* c, int64_t n, const double* xyz, double interva
   if (rc) return rc;
   if (!c->has_mesh) return fail(c, SEI_ERR_STATE, "receivers need a mesh built by the context");
   if (c->visco) return fail(c, SEI_ERR_UNSUPPORTED, "receivers of the viscoelastic equations are not supported");
-  if (c->lts) return fail(c, SEI_ERR_UNSUPPORTED, "receivers under local time stepping are not supported");
   if (n < 0 || (n > 0 && !xyz) || !(interval > 0) || !std::isfinite(interval) || qmask > 0x1FFu ||
       (derived & ~(SEI_RECV_ROTATION | SEI_RECV_STRAIN)))
     return fail(c, SEI_ERR_ARG, "receivers: n >= 0, points, interval > 0, quantity mask of 9 bits, derived flags");
@@ -1198,14 +1226,19 @@ int sei_receivers_setup(sei_ctx* c, int64_t n, const double* xyz, double interva
   for (int64_t r = 0; r < n; ++r)
     if (cell[r] < 0) return fail(c, SEI_ERR_ARG, "receiver " + std::to_string(r) + " lies outside the mesh");
   // a rejected call changes nothing: the old receivers go only now
+  std::vector<double> points(xyz, xyz + 3 * n);
   for (void* p : {(void*)c->d_recv_ucell, (void*)c->d_recv_slot, (void*)c->d_recv_q, (void*)c->d_recv_i,
-                  (void*)c->d_recv_star, (void*)c->d_recv_derivs, (void*)c->d_recv_phi, (void*)c->d_recv_dphi})
+                  (void*)c->d_recv_star, (void*)c->d_recv_derivs, (void*)c->d_recv_phi, (void*)c->d_recv_dphi,
+                  (void*)c->d_recv_list})
     cudaFree(p);
-  c->d_recv_ucell = c->d_recv_slot = nullptr;
+  c->d_recv_ucell = c->d_recv_slot = c->d_recv_list = nullptr;
   c->d_recv_q = c->d_recv_i = c->d_recv_star = c->d_recv_derivs = c->d_recv_phi = c->d_recv_dphi = nullptr;
   c->recv_stage.release();
   c->nrecv = c->nrecv_cells = 0;
   c->recv_cell.clear();
+  c->recv_xyz.clear();
+  c->recv_log.clear();
+  c->recv_pending.clear();
   if (n == 0) return SEI_OK;
   const int order = c->cfg.order, B = sei::numBasis(order);
   std::vector<int32_t> ucell, slot(n);
@@ -1241,12 +1274,32 @@ int sei_receivers_setup(sei_ctx* c, int64_t n, const double* xyz, double interva
     for (int k = 0; k < 3 * B; ++k) dphi[(size_t)r * 3 * B + k] = (float)dp[k];
   }
   const int64_t m = (int64_t)ucell.size();
+  // groups: every receiver in order, then the receivers of each LTS cluster
+  const int ncl = c->lts ? c->ncl : 0;
+  std::vector<int32_t> list(2 * n);
+  std::vector<int64_t> gstart(ncl + 1, 0);
+  std::vector<int> grp(n, 0);
+  for (int64_t r = 0; r < n; ++r) {
+    list[r] = (int32_t)r;
+    if (ncl) {
+      int g = 0;
+      while (g + 1 < ncl && cell[r] >= c->cl_start[g + 1]) ++g;
+      grp[r] = g;
+      ++gstart[g + 1];
+    }
+  }
+  for (int g = 0; g < ncl; ++g) gstart[g + 1] += gstart[g];
+  {
+    std::vector<int64_t> fillp(gstart.begin(), gstart.end());
+    for (int64_t r = 0; r < n; ++r) list[n + (ncl ? fillp[grp[r]]++ : r)] = (int32_t)r;
+  }
   const size_t blk = (size_t)9 * c->Bp, dsz = (size_t)sei::derivativesSize(order);
   auto dalloc = [&](void** ptr, size_t bytes) { return cudaMalloc(ptr, bytes) == cudaSuccess; };
   bool ok = dalloc((void**)&c->d_recv_ucell, m * 4) && dalloc((void**)&c->d_recv_slot, n * 4) &&
             dalloc((void**)&c->d_recv_q, m * blk * 4) && dalloc((void**)&c->d_recv_i, m * blk * 4) &&
             dalloc((void**)&c->d_recv_star, m * 3 * sei::kStarNnz * 4) && dalloc((void**)&c->d_recv_derivs, m * dsz * 4) &&
-            dalloc((void**)&c->d_recv_phi, phi.size() * 4) && dalloc((void**)&c->d_recv_dphi, dphi.size() * 4);
+            dalloc((void**)&c->d_recv_phi, phi.size() * 4) && dalloc((void**)&c->d_recv_dphi, dphi.size() * 4) &&
+            dalloc((void**)&c->d_recv_list, list.size() * 4);
   if (!ok) {
     cudaGetLastError();
     return fail(c, SEI_ERR_OOM, "device allocation for the receivers failed");
@@ -1255,6 +1308,7 @@ int sei_receivers_setup(sei_ctx* c, int64_t n, const double* xyz, double interva
   SEI_CUDA(cudaMemcpy(c->d_recv_slot, slot.data(), n * 4, cudaMemcpyHostToDevice));
   SEI_CUDA(cudaMemcpy(c->d_recv_phi, phi.data(), phi.size() * 4, cudaMemcpyHostToDevice));
   SEI_CUDA(cudaMemcpy(c->d_recv_dphi, dphi.data(), dphi.size() * 4, cudaMemcpyHostToDevice));
+  SEI_CUDA(cudaMemcpy(c->d_recv_list, list.data(), list.size() * 4, cudaMemcpyHostToDevice));
   if (sei::launchGatherRows((int)m, c->d_recv_ucell, c->star_nz, c->d_recv_star, 3 * sei::kStarNnz, c->stream))
     return fail(c, SEI_ERR_CUDA, "receiver gather launch failed");
   c->recv_qmask = qmask;
@@ -1269,7 +1323,12 @@ int sei_receivers_setup(sei_ctx* c, int64_t n, const double* xyz, double interva
   c->nrecv_cells = m;
   c->recv_cell = cell;
   c->recv_interval = interval;
-  c->recv_next = c->sim_time;
+  c->recv_xyz = std::move(points);
+  c->h_recv_list = std::move(list);
+  c->recv_gstart = std::move(gstart);
+  c->recv_next.assign(ncl + 1, 0);
+  c->recv_times.assign(1, c->sim_time);
+  c->recv_emit = 0;
   if (cells) std::copy(cell.begin(), cell.end(), cells);
   return SEI_OK;
 }
@@ -1289,10 +1348,37 @@ int sei_receivers_read(sei_ctx* c, double* out, int64_t max_samples, int64_t* ns
   if (!c || !nsamples || max_samples < 0) return SEI_ERR_ARG;
   *nsamples = 0;
   if (c->nrecv == 0) return SEI_OK;
-  size_t rows = 0;
-  if (c->recv_stage.drain(c->stream, out, (size_t)max_samples * c->nrecv, &rows) != 0)
+  // every staged row, then each logged launch's rows into their samples
+  const size_t nc = (size_t)c->recv_ncols;
+  size_t total = 0;
+  for (const auto& L : c->recv_log) total += (size_t)L.m * L.count;
+  std::vector<double> rows(total * nc);
+  size_t got = 0;
+  if (c->recv_stage.drain(c->stream, rows.data(), total, &got) != 0 || got != total)
     return fail(c, SEI_ERR_CUDA, "receiver staging copy failed");
-  *nsamples = (int64_t)(rows / c->nrecv);
+  size_t pos = 0;
+  for (const auto& L : c->recv_log)
+    for (int sm = 0; sm < L.m; ++sm) {
+      auto& P = c->recv_pending[L.k0 + sm];
+      if (P.first.empty()) P.first.assign((size_t)c->nrecv * nc, 0.0);
+      for (int64_t j = 0; j < L.count; ++j, ++pos) {
+        const int32_t r = c->h_recv_list[L.first + j];
+        std::copy_n(&rows[pos * nc], nc, &P.first[(size_t)r * nc]);
+      }
+      P.second += L.count;
+    }
+  c->recv_log.clear();
+  // complete samples, in order
+  int64_t done = 0;
+  while (done < max_samples) {
+    auto it = c->recv_pending.find(c->recv_emit);
+    if (it == c->recv_pending.end() || it->second.second < c->nrecv) break;
+    if (out) std::copy(it->second.first.begin(), it->second.first.end(), out + (size_t)done * c->nrecv * nc);
+    c->recv_pending.erase(it);
+    ++c->recv_emit;
+    ++done;
+  }
+  *nsamples = done;
   return SEI_OK;
 }
 
@@ -1305,7 +1391,12 @@ int sei_get_time(const sei_ctx* c, double* t) {
 int sei_set_time(sei_ctx* c, double t) {
   if (!c || !std::isfinite(t) || t < 0) return c ? fail(c, SEI_ERR_ARG, "time must be finite and >= 0") : SEI_ERR_ARG;
   c->sim_time = t;
-  c->recv_next = t;
+  if (c->nrecv > 0) {
+    // the receivers sample from t on: set them up again (samples not yet read are dropped)
+    const std::vector<double> pts = c->recv_xyz;
+    return sei_receivers_setup(c, (int64_t)pts.size() / 3, pts.data(), c->recv_interval, c->recv_qmask,
+                               c->recv_derived, nullptr);
+  }
   return SEI_OK;
 }
 
@@ -2281,6 +2372,12 @@ int sei_lts_setup(sei_ctx* c, double cfl, int max_clusters, int* nclusters) {
   c->g_start = gst;
   c->lts_perm = order;
   if (nclusters) *nclusters = ncl;
+  if (c->nrecv > 0) {
+    // the cells moved: locate the receivers again on the reordered mesh (their clocks restart)
+    const std::vector<double> pts = c->recv_xyz;
+    const int derived = c->recv_derived;
+    return sei_receivers_setup(c, (int64_t)pts.size() / 3, pts.data(), c->recv_interval, c->recv_qmask, derived, nullptr);
+  }
   return SEI_OK;
 }
 
@@ -2335,6 +2432,7 @@ sei::ViscoArrays viscoRangeView(sei_ctx* c, int64_t s, int64_t e, bool neighbour
 // faces of the cluster, neighbour flux) of the clusters whose step ends at k + 1 (TimeCluster
 // predict / correct, TimeCommon::computeIntegrals).
 int ltsCycle(sei_ctx* c) {
+  int rc0 = SEI_OK;
   const int blk = c->nq * c->Bp;
   const int64_t steps = (int64_t)1 << (c->ncl - 1);
   float co[8];
@@ -2345,6 +2443,10 @@ int ltsCycle(sei_ctx* c) {
       const int64_t s = c->cl_start[cl], e = c->cl_start[cl + 1];
       if (s == e) continue;
       const double dtc = c->lts_dt0 * (double)len;
+      if (c->nrecv && (rc0 = recordReceivers(c, cl, c->sim_time + c->lts_dt0 * (double)k, dtc,
+                                             c->nrecv + c->recv_gstart[cl],
+                                             c->recv_gstart[cl + 1] - c->recv_gstart[cl])))
+        return rc0;
       taylorCoeffs(c->cfg.order, dtc, co);
       sei::DeviceArrays d = rangeView(c, s, e, false);
       const sei::ViscoArrays v = c->visco ? viscoRangeView(c, s, e, false) : sei::ViscoArrays{};
@@ -2440,7 +2542,9 @@ int sei_lts_run(sei_ctx* c, int ncycles) {
   if (!c->lts) return fail(c, SEI_ERR_STATE, "local time stepping not set up (sei_lts_setup)");
   if (ncycles < 0) return fail(c, SEI_ERR_ARG, "ncycles < 0");
   c->prof_used = 0;
-  if (c->lts_graph && !c->lts_exec && ncycles > 0) {
+  // receivers change their launches from cycle to cycle (sample counts, staging): no graph then
+  const bool graph = c->lts_graph && c->nrecv == 0;
+  if (graph && !c->lts_exec && ncycles > 0) {
     // record one cycle (relaxed mode: the launchers set kernel attributes while recording)
     SEI_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
     c->capturing = true;
@@ -2457,7 +2561,7 @@ int sei_lts_run(sei_ctx* c, int ncycles) {
   }
   SEI_CUDA(cudaEventRecord(c->ev0, c->stream));
   for (int i = 0; i < ncycles && rc == SEI_OK; ++i) {
-    if (c->lts_graph) {
+    if (graph) {
       if (cudaGraphLaunch(c->lts_exec, c->stream) != cudaSuccess) rc = fail(c, SEI_ERR_CUDA, "cudaGraphLaunch failed");
     } else {
       rc = ltsCycle(c);

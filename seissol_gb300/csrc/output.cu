@@ -40,18 +40,19 @@ __global__ void __launch_bounds__(128) sei_recv_eval(sei::RecvEvalArgs A) {
   constexpr int L = (B + 31) / 32;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= A.nrecv) return;
+  const int r = A.list[warp];
   int dsz = 0;
 #pragma unroll
   for (int i = 0; i < N; ++i) dsz += (N - i) * (N - i + 1) * (N - i + 2) / 6 * 9;
-  const float* d = A.derivs + (size_t)A.slot[warp] * dsz;
+  const float* d = A.derivs + (size_t)A.slot[r] * dsz;
   float phi[L], dphi[L][3];
 #pragma unroll
   for (int u = 0; u < L; ++u) {
     const int l = lane + 32 * u;
     const bool on = l < B;
-    phi[u] = on ? A.phi[(size_t)warp * B + l] : 0.f;
+    phi[u] = on ? A.phi[(size_t)r * B + l] : 0.f;
 #pragma unroll
-    for (int x = 0; x < 3; ++x) dphi[u][x] = on && A.derived ? A.dphi[((size_t)warp * 3 + x) * B + l] : 0.f;
+    for (int x = 0; x < 3; ++x) dphi[u][x] = on && A.derived ? A.dphi[((size_t)r * 3 + x) * B + l] : 0.f;
   }
   for (int s = 0; s < A.nsamples; ++s) {
     // Taylor coefficients t^i / i! at the sample's offset from the expansion point

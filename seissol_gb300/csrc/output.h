@@ -44,8 +44,9 @@ class Stager {
 constexpr int kRecvMaxSamples = 32;  // samples per evaluation launch
 
 struct RecvEvalArgs {
-  int nrecv;
-  const int32_t* slot;  // [nrecv] row of derivs: the receiver's cell in the compact copy
+  int nrecv;            // receivers of this launch
+  const int32_t* list;  // [nrecv] their indices (the rows of slot, phi, dphi)
+  const int32_t* slot;  // [receivers] row of derivs: the receiver's cell in the compact copy
   const float* derivs;  // [cells][derivativesSize]
   const float* phi;     // [nrecv][B] basis functions at the receiver
   const float* dphi;    // [nrecv][3][B] their gradients in global coordinates
@@ -55,7 +56,7 @@ struct RecvEvalArgs {
   unsigned qmask;                  // quantities written (bit q: quantity q)
   int derived;                     // SEI_RECV_ROTATION | SEI_RECV_STRAIN
   int ncols;
-  double* out;  // [nsamples][nrecv][ncols]
+  double* out;  // [nsamples][nrecv][ncols], receivers in list order
 };
 
 int launchGatherRows(int m, const int32_t* src, const float* in, float* out, int rowFloats, void* stream);

@@ -143,9 +143,87 @@ def test_output_errors(built_lib):
     ctx.close()
     from seissol_gb300 import Context
     ctx = Context(4, device=0)
-    ctx.build_periodic_cube(8, 8, 8, perturb=0.05, seed=13, grading=6.0)
-    ctx.lts_setup(0.5, 4)
+    ctx.build_periodic_cube(4, 4, 4, seed=13)
+    ctx.visco_setup(50.0, 25.0, 1.0, 100.0)
     with pytest.raises(SeiError) as e:
         ctx.receivers_setup([[10.0, 10.0, 10.0]], 1e-3)
     assert e.value.code == -7
+    ctx.close()
+
+
+def test_receivers_under_lts_match_oracle(built_lib):
+    """Graded cube in several rate-2 clusters, 10 receivers sampled every 0.73 dt0 over two
+    cycles: each cluster samples its receivers at the start of its own steps; against the LTS
+    restatement (FP64 trajectory, so 1e-4 of each column's largest magnitude); times exact.
+    The interval keeps samples off the step boundaries: a sample on a boundary belongs to one
+    step or the next depending on the last bit of the step time, and the predictor's value at a
+    step's end differs from the corrected one at the next step's start.  Receivers set before
+    the LTS set-up are located again on the reordered cells."""
+    from tests.test_gpu_lts import _graded_ctx
+    order = 4
+    ctx, n = _graded_ctx(order)
+    coords0, _, _ = ctx.get_geometry()
+    lo, hi = coords0.min(axis=(0, 1)), coords0.max(axis=(0, 1))
+    pts = lo + (hi - lo) * np.random.default_rng(3).uniform(0.05, 0.95, (10, 3))
+    ctx.receivers_setup(pts, 1e-3)
+    ncl = ctx.lts_setup(0.5, 8)
+    assert ncl >= 2 and ctx.lib.sei_receivers_columns(ctx.h) == 1 + 9
+    coords, material, _ = ctx.get_geometry()
+    cells = ctx.get_cells()
+    vp = np.sqrt((material[:, 2] + 2 * material[:, 1]) / material[:, 0])
+    cl, dt0 = oracle_py.lts_clusters(dg_setup.cfl_timestep(coords, vp, order, 0.5), cells["neighbor"],
+                                     cells["face_type"], 8)
+    interval = 0.73 * dt0
+    rc = ctx.receivers_setup(pts, interval, rotation=True)
+    ref_cells, xez = receivers.locate(coords, pts)
+    assert np.array_equal(rc, ref_cells)
+    assert len(set(cl[rc])) >= 2  # receivers in more than one cluster
+    q0 = seeded_dofs(n, order, 5)
+    ctx.set_dofs(q0)
+    ctx.lts_run(2)
+    ctx.sync()
+    got = ctx.receivers_read()
+    # the restatement, sampled at each cluster's predictor
+    o = oracle_py.Oracle(order)
+    star = cells["star"].astype(np.float64)
+    times = [0.0]
+    cursor = {}
+    samples = {}
+
+    def t_of(k):
+        while len(times) <= k:
+            times.append(times[-1] + interval)
+        return times[k]
+
+    def on_predict(c, T, dtc, Q):
+        recs = [r for r in range(len(pts)) if cl[rc[r]] == c]
+        k = cursor.get(c, 0)
+        ks = []
+        while recs and t_of(k) < T + dtc:
+            ks.append(k)
+            k += 1
+        cursor[c] = k
+        if not ks:
+            return
+        _, d = o.ader(np.asarray(Q, np.float64)[rc[recs]], star[rc[recs]],
+                      dg_setup.taylor_integrate(order, 0.0, dtc), want_derivs=True)
+        for j, r in enumerate(recs):
+            phi, dphi = receivers.basis_at(order, xez[r], coords[rc[r]])
+            rows = receivers.sample(order, d[j], phi, dphi, [t_of(k) - T for k in ks], rotation=True)
+            rows[:, 0] += T
+            for k, row in zip(ks, rows):
+                samples.setdefault(k, {})[r] = row
+
+    oracle_py.lts_cycles(o, q0, cells, cl, dt0, 2, on_predict=on_predict)
+    complete = []
+    for k in range(len(times)):
+        if len(samples.get(k, {})) < len(pts):
+            break
+        complete.append(np.stack([samples[k][r] for r in range(len(pts))]))
+    want = np.stack(complete)
+    assert got.shape == want.shape, (got.shape, want.shape)
+    assert np.array_equal(got[:, :, 0], want[:, :, 0])
+    scale = np.abs(want).max(axis=(0, 1))
+    err = np.abs(got - want).max(axis=(0, 1)) / np.maximum(scale, 1e-30)
+    assert err[1:].max() < 1e-4, err
     ctx.close()
