@@ -147,7 +147,26 @@ typedef struct sei_rs_params {
 #define SEI_DR_ONSET_TIME 27
 #define SEI_DR_TAU_S 28
 #define SEI_DR_TAU_R 29
-#define SEI_DR_NUM_FIELDS 30
+/* Thermal pressurisation (sei_dr_set_thermal_pressurization): shear-zone half width, hydraulic
+ * diffusivity (tp_halfwidthshearzone, tp_hydraulicdiffusivity), temperature and pore pressure. */
+#define SEI_DR_TP_HALF_WIDTH 30
+#define SEI_DR_TP_HYDRAULIC_DIFFUSIVITY 31
+#define SEI_DR_TP_TEMPERATURE 32
+#define SEI_DR_TP_PRESSURE 33
+#define SEI_DR_NUM_FIELDS 34
+
+/* Thermal pressurisation of the rate-and-state laws (CpuImpl/ThermalPressurization/
+ * ThermalPressurization.cpp, TPCommon.h): per point, 60 Fourier modes of temperature and pore
+ * pressure across the shear zone diffuse and gain the frictional heat tau V of a Gaussian source;
+ * the pore pressure lowers the effective normal stress in every pass of the slip-rate solve and
+ * the modes advance after it (RateAndState.h:40-76, 185-215, 420-432).  Parameter names of the
+ * reference: tp_thermaldiffusivity, tp_heatcapacity, tp_undrainedtpresponse, tp_initemp,
+ * tp_inipressure; the per-point fields start at half_width_shear_zone and hydraulic_diffusivity. */
+typedef struct sei_tp_params {
+  double thermal_diffusivity, heat_capacity, undrained_tp_response;
+  double initial_temperature, initial_pressure;
+  double half_width_shear_zone, hydraulic_diffusivity;
+} sei_tp_params;
 
 /* Friction laws (src/Initializer/Parameters/DRParameters.h FrictionLawType): rate and state with
  * fast velocity weakening (FL 103, sei_dr_setup); linear slip weakening (FL 16 and FL 2), its
@@ -460,6 +479,10 @@ int sei_dr_setup_rate_state(sei_ctx* ctx, const sei_rs_params* p, int law, int64
 int sei_dr_setup_lsw(sei_ctx* ctx, const sei_lsw_params* p, int64_t* nfaces);
 /* The fault with an imposed slip rate (SEI_LAW_ISR_*); replaces an earlier fault set-up. */
 int sei_dr_setup_imposed(sei_ctx* ctx, const sei_isr_params* p, int64_t* nfaces);
+/* Turns thermal pressurisation on (modes zeroed, fields set from p) or off, for a rate-and-state
+ * fault (SEI_LAW_FVW or SEI_LAW_RS_*); the learned warm start and the float32 pre-solve are
+ * skipped while it is on. */
+int sei_dr_set_thermal_pressurization(sei_ctx* ctx, int on, const sei_tp_params* p);
 /* Friction law of the fault (SEI_LAW_*), -1 without one. */
 int sei_dr_law(const sei_ctx* ctx);
 /* Gaussian nucleation (FrictionSolverCommon.h:503-531 with src/Numerical/GaussianNucleationFunction.h):

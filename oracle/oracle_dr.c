@@ -116,7 +116,55 @@ typedef struct {
   double healing, v_star, prakash_length, tp_exponent;
   const double *mu_s, *mu_d, *d_c, *cohesion, *t_forced;
   double* reg;     /* regularised strength (law 2) */
+  /* thermal pressurisation of the rate-and-state laws (tp != 0): thermal diffusivity, heat
+   * capacity, undrained response Lambda, initial temperature and pressure; per point the shear
+   * zone half width and hydraulic diffusivity; state: 60 Fourier modes of temperature (theta)
+   * and pressure (sigma), [nfaces][60][npts]; outputs temperature and pressure [nfaces][npts] */
+  int tp;
+  double tp_alpha, tp_rhoc, tp_lambda, tp_t0, tp_p0;
+  const double *tp_hw, *tp_hyd;
+  double *tp_theta, *tp_sigma, *tp_temp, *tp_pres;
 } oracle_dr_aux;
+
+#define TP_MODES 60
+/* Thermal pressurisation (CpuImpl/ThermalPressurization/ThermalPressurization.cpp:27-107,
+ * TPCommon.h): the modes' wave numbers, inverse-transform weights and Gaussian heat source. */
+static double tp_grid(int i) { return 10.0 * exp(-0.3 * (TP_MODES - i - 1)); }
+static double tp_inv(int i) {
+  const double c = sqrt(2.0 / 3.14159265358979323846) * tp_grid(i);
+  return i == 0 ? c * (1.0 + 0.3) : (i == TP_MODES - 1 ? c * 0.5 * 0.3 : c * 0.3);
+}
+static double tp_heat(int i) { return 1.0 / sqrt(2.0 * 3.14159265358979323846) * exp(-0.5 * tp_grid(i) * tp_grid(i)); }
+
+/* Fluid pressure of point (face f, index k) after dt with slip rate v, friction mu and normal
+ * stress sn; the modes advance only with save.  Sets the point's temperature and pressure. */
+static double tp_pressure(const oracle_dr_aux* x, int64_t f, int npts, int k, double sn, double mu, double v, double dt,
+                          int save) {
+  const size_t i = (size_t)f * npts + k;
+  const double hw = x->tp_hw[i], hyd = x->tp_hyd[i];
+  const double tauv = -mu * sn * v;
+  const double lp = x->tp_lambda * x->tp_alpha / (hyd - x->tp_alpha);
+  double tu = 0.0, pu = 0.0;
+  for (int m = 0; m < TP_MODES; ++m) {
+    const size_t mi = ((size_t)f * TP_MODES + m) * npts + k;
+    const double g2 = (tp_grid(m) / hw) * (tp_grid(m) / hw);
+    const double th = x->tp_alpha * g2, sg = hyd * g2;
+    const double om = tauv * tp_heat(m);
+    const double tn = x->tp_theta[mi] * exp(-th * dt) + om / (x->tp_rhoc * th) * -expm1(-th * dt);
+    const double sn_ = x->tp_sigma[mi] * exp(-sg * dt) + om * (x->tp_lambda + lp) / (x->tp_rhoc * sg) * -expm1(-sg * dt);
+    const double w = tp_inv(m) / hw;
+    tu += w * tn;
+    pu += w * sn_;
+    if (save) {
+      x->tp_theta[mi] = tn;
+      x->tp_sigma[mi] = sn_;
+    }
+  }
+  pu -= lp * tu;
+  x->tp_temp[i] = tu + x->tp_t0;
+  x->tp_pres[i] = -pu + x->tp_p0;
+  return x->tp_pres[i];
+}
 
 /* smoothStep and the nucleation of one time point ending at t_end over dt. */
 static double smooth_step(double t, double t0) {
@@ -348,7 +396,8 @@ void oracle_dr_friction(int npts, int nts, int64_t nfaces, const oracle_rs_param
                         const float* mlp, const float* mlp_norm, int64_t* first_iters, float* rec,
                         int64_t rec_cap, int64_t* rec_count, const oracle_dr_aux* aux) {
   const int law = aux ? aux->law : 0; /* 0 fast velocity weakening, 4 aging, 5 slip, 6 severe */
-  if (law != 0) mlp = NULL, rec = NULL;
+  const int tp = aux && aux->tp;
+  if (law != 0 || tp) mlp = NULL, rec = NULL;
 #pragma omp parallel
   {
     double* buf = (double*)malloc(sizeof(double) * (size_t)npts * 12);
@@ -389,7 +438,7 @@ void oracle_dr_friction(int npts, int nts, int64_t nfaces, const oracle_rs_param
           const double sn0 = init[(size_t)f * 3 * npts + k];
           const double t10 = init[(size_t)f * 3 * npts + npts + k];
           const double t20 = init[(size_t)f * 3 * npts + 2 * npts + k];
-          double sn = fs[(0 * nts + s) * npts + k] + sn0;
+          double sn = fs[(0 * nts + s) * npts + k] + sn0 - (tp ? aux->tp_pres[fo + k] : 0.0);
           sns[k] = sn < 0 ? sn : 0.0;
           sref[k] = psib[k];
           const double tt1 = t10 + fs[(1 * nts + s) * npts + k];
@@ -407,6 +456,11 @@ void oracle_dr_friction(int npts, int nts, int64_t nfaces, const oracle_rs_param
           for (int k = g0; k < g1; ++k) {
             const double ak = a[fo + k];
             psib[k] = law_state_update(P, law, ak, sref[k], dt, lsr[k]);
+            if (tp) { /* pressure of this pass from the previous pass's stress and friction */
+              const double pr = tp_pressure(aux, f, npts, k, sns[k], mu[fo + k], lsr[k], dt, 0);
+              const double sn = fs[(0 * nts + s) * npts + k] + init[(size_t)f * 3 * npts + k] - pr;
+              sns[k] = sn < 0 ? sn : 0.0;
+            }
             double vnew = 0, munew = 0;
             int conv = 0, its = 0;
             if (law == 6) {
@@ -460,6 +514,11 @@ void oracle_dr_friction(int npts, int nts, int64_t nfaces, const oracle_rs_param
         }
         for (int k = 0; k < npts; ++k) {
           const double ak = a[fo + k];
+          if (tp) { /* the modes advance with the pass's final slip rate */
+            const double pr = tp_pressure(aux, f, npts, k, sns[k], mu[fo + k], lsr[k], dt, 1);
+            const double sn = fs[(0 * nts + s) * npts + k] + init[(size_t)f * 3 * npts + k] - pr;
+            sns[k] = sn < 0 ? sn : 0.0;
+          }
           psib[k] = law_state_update(P, law, ak, sref[k], dt, lsr[k]);
           const double clin = 0.5 / P->v0;
           const double cexplog = psi_eff(P, law, psib[k]) / ak;
@@ -787,6 +846,12 @@ void oracle_dr_friction_isr(int npts, int nts, int64_t nfaces, const oracle_imp*
 
 #undef QP
 #undef QM
+
+/* One thermal-pressurisation update of point k of face f (test hook of tp_pressure). */
+double oracle_dr_tp_point(const oracle_dr_aux* x, int64_t f, int npts, int k, double sn, double mu, double v, double dt,
+                          int save) {
+  return tp_pressure(x, f, npts, k, sn, mu, v, dt, save);
+}
 
 /* Q(cell) += V3mTo2nTWDivM(side, rel) . imposed . fluxSolver for one side of every face. */
 void oracle_dr_nodal_flux(int order, int npts, int64_t nfaces, const int32_t* cell, const int8_t* side,

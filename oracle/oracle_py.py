@@ -127,11 +127,14 @@ class DrAuxC(C.Structure):
                 ("nuc", C.c_void_p), ("peak", C.c_void_p), ("trup", C.c_void_p), ("tdyn", C.c_void_p),
                 ("law", C.c_int), ("healing", C.c_double), ("v_star", C.c_double), ("prakash_length", C.c_double),
                 ("tp_exponent", C.c_double), ("mu_s", C.c_void_p), ("mu_d", C.c_void_p), ("d_c", C.c_void_p),
-                ("cohesion", C.c_void_p), ("t_forced", C.c_void_p), ("reg", C.c_void_p)]
+                ("cohesion", C.c_void_p), ("t_forced", C.c_void_p), ("reg", C.c_void_p),
+                ("tp", C.c_int), ("tp_alpha", C.c_double), ("tp_rhoc", C.c_double), ("tp_lambda", C.c_double),
+                ("tp_t0", C.c_double), ("tp_p0", C.c_double), ("tp_hw", C.c_void_p), ("tp_hyd", C.c_void_p),
+                ("tp_theta", C.c_void_p), ("tp_sigma", C.c_void_p), ("tp_temp", C.c_void_p), ("tp_pres", C.c_void_p)]
 
 
 AUX_ARRAYS = ("nuc", "peak", "trup", "tdyn", "mu_s", "mu_d", "d_c", "cohesion", "t_forced", "reg", "dir1", "dir2",
-              "onset", "taus", "taur")
+              "onset", "taus", "taur", "tp_hw", "tp_hyd", "tp_theta", "tp_sigma", "tp_temp", "tp_pres")
 
 
 def _aux_struct(aux):
@@ -147,7 +150,9 @@ def _aux_struct(aux):
                   ptr("nuc"), ptr("peak"), ptr("trup"), ptr("tdyn"), int(aux.get("law", 0)),
                   aux.get("healing", -1.0), aux.get("v_star", 0.0), aux.get("prakash_length", 1.0),
                   aux.get("tp_exponent", 1.0 / 3.0), ptr("mu_s"), ptr("mu_d"), ptr("d_c"), ptr("cohesion"),
-                  ptr("t_forced"), ptr("reg"))
+                  ptr("t_forced"), ptr("reg"), int(aux.get("tp", 0)), aux.get("tp_alpha", 0.0), aux.get("tp_rhoc", 1.0),
+                  aux.get("tp_lambda", 0.0), aux.get("tp_t0", 0.0), aux.get("tp_p0", 0.0), ptr("tp_hw"), ptr("tp_hyd"),
+                  ptr("tp_theta"), ptr("tp_sigma"), ptr("tp_temp"), ptr("tp_pres"))
 
 
 def dr_collocation(order, dt):

@@ -15,6 +15,7 @@ from .lib import (  # noqa: F401
     RSParams,
     LSWParams,
     ISRParams,
+    TPParams,
     DR_FIELDS,
     SeiError,
     KERNELS,

@@ -71,6 +71,9 @@ struct sei_ctx {
   int dr_law = SEI_LAW_FVW;
   sei_lsw_params lsw{};
   bool dr_nucleate = false;
+  bool dr_tp = false;  // thermal pressurisation
+  sei_tp_params tp{};
+  double* d_tp = nullptr;  // modes [2][60][nf][npts]: temperature, then pressure
   double dr_t0 = 0.0, dr_s0 = 0.0;  // nucleation duration / start (t0 also ramps the forced rupture)
   float* d_mlp = nullptr;  // trained warm-start network (nullptr: none)
   float mlp_norm[sei_mlp::kNorm] = {0};
@@ -186,8 +189,10 @@ void dropLtsGraph(sei_ctx* c) {
 void freeFault(sei_ctx* c) {
   for (void* p : {(void*)c->d_pc, (void*)c->d_mc, (void*)c->d_pslot, (void*)c->d_mslot, (void*)c->d_iters, (void*)c->d_ps,
                   (void*)c->d_ms, (void*)c->d_rel, (void*)c->d_tinvt, (void*)c->d_fsp, (void*)c->d_fsm, (void*)c->d_isp,
-                  (void*)c->d_ism, (void*)c->d_imp, (void*)c->d_state, (void*)c->d_time})
+                  (void*)c->d_ism, (void*)c->d_imp, (void*)c->d_state, (void*)c->d_time, (void*)c->d_tp})
     cudaFree(p);
+  c->d_tp = nullptr;
+  c->dr_tp = false;
   c->d_pc = c->d_mc = c->d_pslot = c->d_mslot = c->d_iters = nullptr;
   c->d_ps = c->d_ms = c->d_rel = nullptr;
   c->d_tinvt = c->d_fsp = c->d_fsm = c->d_isp = c->d_ism = nullptr;
@@ -550,6 +555,18 @@ sei::DrArgs drArgs(sei_ctx* c, double dt) {
   a.v_star = c->lsw.v_star;
   a.prakash_length = c->lsw.prakash_length > 0 ? c->lsw.prakash_length : 1.0;
   a.tp_exponent = c->lsw.tp_proxy_exponent;
+  a.tp = c->dr_tp ? 1 : 0;
+  a.tp_alpha = c->tp.thermal_diffusivity;
+  a.tp_rhoc = c->tp.heat_capacity;
+  a.tp_lambda = c->tp.undrained_tp_response;
+  a.tp_t0 = c->tp.initial_temperature;
+  a.tp_p0 = c->tp.initial_pressure;
+  a.tp_hw = field(SEI_DR_TP_HALF_WIDTH);
+  a.tp_hyd = field(SEI_DR_TP_HYDRAULIC_DIFFUSIVITY);
+  a.tp_temp = field(SEI_DR_TP_TEMPERATURE);
+  a.tp_pres = field(SEI_DR_TP_PRESSURE);
+  a.tp_theta = c->d_tp;
+  a.tp_sigma = c->d_tp ? c->d_tp + (size_t)sei::kTpModes * nf * np : nullptr;
   a.dir1 = field(SEI_DR_SLIP_DIR1);
   a.dir2 = field(SEI_DR_SLIP_DIR2);
   a.onset = field(SEI_DR_ONSET_TIME);
@@ -1632,6 +1649,43 @@ int sei_dr_setup_imposed(sei_ctx* c, const sei_isr_params* p, int64_t* nfaces) {
   if ((rc = drInstall(c, st))) return rc;
   c->dr_law = p->law;
   if (nfaces) *nfaces = nf;
+  return SEI_OK;
+}
+
+int sei_dr_set_thermal_pressurization(sei_ctx* c, int on, const sei_tp_params* p) {
+  int rc = checkReady(c);
+  if (rc) return rc;
+  if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up");
+  if (c->dr_law != SEI_LAW_FVW && c->dr_law != SEI_LAW_RS_AGING && c->dr_law != SEI_LAW_RS_SLIP &&
+      c->dr_law != SEI_LAW_RS_SEVERE)
+    return fail(c, SEI_ERR_STATE, "thermal pressurisation needs a rate-and-state law");
+  dropLtsGraph(c);
+  cudaFree(c->d_tp);
+  c->d_tp = nullptr;
+  c->dr_tp = false;
+  if (!on) return SEI_OK;
+  if (!p || !(p->thermal_diffusivity > 0) || !(p->heat_capacity > 0) || !std::isfinite(p->undrained_tp_response) ||
+      !std::isfinite(p->initial_temperature) || !std::isfinite(p->initial_pressure) || !(p->half_width_shear_zone > 0) ||
+      !(p->hydraulic_diffusivity > 0) || p->hydraulic_diffusivity == p->thermal_diffusivity)
+    return fail(c, SEI_ERR_ARG, "invalid thermal-pressurisation parameters");
+  const size_t plane = (size_t)c->fault.nf * c->npts;
+  if (cudaMalloc(&c->d_tp, 2 * sei::kTpModes * plane * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    c->d_tp = nullptr;
+    return fail(c, SEI_ERR_OOM, "device allocation for thermal pressurisation failed");
+  }
+  SEI_CUDA(cudaMemsetAsync(c->d_tp, 0, 2 * sei::kTpModes * plane * sizeof(double), c->stream));
+  std::vector<double> v(plane);
+  const double init[4] = {p->half_width_shear_zone, p->hydraulic_diffusivity, p->initial_temperature, p->initial_pressure};
+  for (int f = 0; f < 4; ++f) {
+    std::fill(v.begin(), v.end(), init[f]);
+    SEI_CUDA(cudaMemcpy(c->d_state + (size_t)(SEI_DR_TP_HALF_WIDTH + f) * plane, v.data(), plane * sizeof(double),
+                        cudaMemcpyHostToDevice));
+  }
+  if (sei::launchTpTables(c->stream) != 0) return fail(c, SEI_ERR_CUDA, "thermal-pressurisation table launch failed");
+  SEI_CUDA(cudaStreamSynchronize(c->stream));
+  c->tp = *p;
+  c->dr_tp = true;
   return SEI_OK;
 }
 

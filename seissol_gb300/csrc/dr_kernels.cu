@@ -314,6 +314,50 @@ __device__ double smoothStep(double t, double t0) {
   return 1.0;
 }
 
+// ---- thermal pressurisation (CpuImpl/ThermalPressurization/ThermalPressurization.cpp:27-107,
+// TPCommon.h): wave numbers 10 e^(-0.3 (59 - i)), inverse-transform weights, Gaussian heat source
+__device__ double gTp[3][sei::kTpModes];
+
+__global__ void sei_tp_tables() {
+  const int i = threadIdx.x;
+  if (i >= sei::kTpModes) return;
+  const double k = 10.0 * exp(-0.3 * (sei::kTpModes - i - 1));
+  const double c = sqrt(2.0 / M_PI) * k;
+  gTp[0][i] = k;
+  gTp[1][i] = i == 0 ? c * (1.0 + 0.3) : (i == sei::kTpModes - 1 ? c * 0.5 * 0.3 : c * 0.3);
+  gTp[2][i] = 1.0 / sqrt(2.0 * M_PI) * exp(-0.5 * k * k);
+}
+
+// Fluid pressure of point po after dt at slip rate v, friction mu and normal stress sn; the modes
+// advance only with save.  temp receives the temperature.
+__device__ double tpPressure(const sei::DrArgs& A, size_t po, size_t plane, double hw, double hyd, double sn,
+                             double mu, double v, double dt, bool save, double& temp) {
+  const double tauv = -mu * sn * v;
+  const double lp = A.tp_lambda * A.tp_alpha / (hyd - A.tp_alpha);
+  double tu = 0.0, pu = 0.0;
+#pragma unroll 1
+  for (int m = 0; m < sei::kTpModes; ++m) {
+    const double g = gTp[0][m] / hw;
+    const double g2 = g * g;
+    const double th = A.tp_alpha * g2, sg = hyd * g2;
+    const double om = tauv * gTp[2][m];
+    double* pt = A.tp_theta + (size_t)m * plane + po;
+    double* ps = A.tp_sigma + (size_t)m * plane + po;
+    const double tn = *pt * exp(-th * dt) + om / (A.tp_rhoc * th) * -expm1(-th * dt);
+    const double sn2 = *ps * exp(-sg * dt) + om * (A.tp_lambda + lp) / (A.tp_rhoc * sg) * -expm1(-sg * dt);
+    const double w = gTp[1][m] / hw;
+    tu += w * tn;
+    pu += w * sn2;
+    if (save) {
+      *pt = tn;
+      *ps = sn2;
+    }
+  }
+  pu -= lp * tu;
+  temp = tu + A.tp_t0;
+  return -pu + A.tp_p0;
+}
+
 // Regularised Yoffe function: the Yoffe slip-rate function of rise time tau_R convolved with a
 // triangle of half width tau_S (Tinti et al. 2005, closed form; Numerical/RegularizedYoffe.h).
 __device__ double regularizedYoffe(double t, double tS, double tR) {
@@ -353,7 +397,7 @@ __device__ double regularizedYoffe(double t, double tS, double tR) {
 // weakening (state kept as it is); FAM 2: linear slip weakening (law 1: resampled slip rate;
 // 2: bimaterial regularised strength; 3: TP proxy state), CpuImpl/LinearSlipWeakening.h:27-170;
 // FAM 3: imposed slip rates (7 Yoffe, 8 Gaussian, 9 delta), CpuImpl/ImposedSlipRates.h:21-60.
-template <int N, int B, int NP, int FAM>
+template <int N, int B, int NP, int FAM, bool TPK>
 __global__ void __launch_bounds__(128, 3)
     sei_dr_faces(sei::DrArgs A, const float* __restrict__ V3m, const float* __restrict__ TW,
                  const double* __restrict__ R) {
@@ -369,7 +413,7 @@ __global__ void __launch_bounds__(128, 3)
   __shared__ float sG[FPB][NP * 9];
   __shared__ double sD[FPB][TPF];
   __shared__ float sW[FAM == 0 ? kMlpParams : 1];
-  const bool useMlp = FAM == 0 && A.mlp != nullptr;
+  const bool useMlp = FAM == 0 && !TPK && A.mlp != nullptr;
   if (useMlp)
     for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) sW[i] = A.mlp[i];
   __syncthreads();
@@ -444,7 +488,10 @@ __global__ void __launch_bounds__(128, 3)
   double psib = psiStored;
   double v1 = pt ? A.v1[po] : 1.0, v2 = pt ? A.v2[po] : 0.0;
   double slip1 = pt ? A.slip1[po] : 0.0, slip2 = pt ? A.slip2[po] : 0.0, slip = pt ? A.slip[po] : 0.0;
-  double mu = FAM == 2 && pt ? A.mu[po] : 0.0, tr1 = 0.0, tr2 = 0.0;
+  double mu = (FAM == 2 || TPK) && pt ? A.mu[po] : 0.0, tr1 = 0.0, tr2 = 0.0;
+  // thermal pressurisation: pressure and temperature of the point, its zone width and diffusivity
+  double tpP = TPK && pt ? A.tp_pres[po] : 0.0, tpT = TPK && pt ? A.tp_temp[po] : 0.0;
+  const double tpHw = TPK && pt ? A.tp_hw[po] : 1.0, tpHyd = TPK && pt ? A.tp_hyd[po] : 1.0;
   double peak = pt ? A.peak[po] : 0.0, trup = pt ? A.trup[po] : 0.0;
   // slip weakening fields
   const double muS = FAM == 2 && pt ? A.mu_s[po] : 0.0, muD = FAM == 2 && pt ? A.mu_d[po] : 0.0;
@@ -481,7 +528,7 @@ __global__ void __launch_bounds__(128, 3)
     const double tt1 = t10 + ft1, tt2 = t20 + ft2;
     const double tau = sqrt(tt1 * tt1 + tt2 * tt2);
     if constexpr (RS) {
-      double sn = fsn + sn0;
+      double sn = fsn + sn0 - tpP;  // effective normal stress (RateAndState.h:420-432)
       sn = sn < 0 ? sn : 0.0;
       const double sref = psib;
       vmag = sqrt(v1 * v1 + v2 * v2);  // RateAndState.h:150-153
@@ -494,6 +541,12 @@ __global__ void __launch_bounds__(128, 3)
           NewtonOut r{};
           bool done = false;
           double pe;
+          if constexpr (TPK) {
+            // the pressure of this pass from the previous pass's stress and friction
+            tpP = tpPressure(A, po, plane, tpHw, tpHyd, sn, mu, lsr, dt, false, tpT);
+            sn = fsn + sn0 - tpP;
+            sn = sn < 0 ? sn : 0.0;
+          }
           if constexpr (FAM == 0) {
             psib = stateUpdate(A, inv, a, sref, dt, lsr);
             pe = psib;
@@ -507,7 +560,7 @@ __global__ void __launch_bounds__(128, 3)
             }
           }
           const bool net = useMlp && j == 0 && sei_mlp::usable(sn, tau, a);
-          if (FAM == 0 && (net || A.refine32)) {
+          if (FAM == 0 && !TPK && (net || A.refine32)) {
             const Solve32 S{(float)(fabs(sn) * a), (float)etas, (float)tau, (float)(psib * inva) - lnPos(2.0 * A.v0)};
             const float u0 = lnPos(vmag);
             float u = u0;
@@ -555,6 +608,12 @@ __global__ void __launch_bounds__(128, 3)
         if (warpAll(conv)) break;
       }
       if (pt) {
+        if constexpr (TPK) {
+          // the modes advance with the final pass's slip rate and friction
+          tpP = tpPressure(A, po, plane, tpHw, tpHyd, sn, mu, lsr, dt, true, tpT);
+          sn = fsn + sn0 - tpP;
+          sn = sn < 0 ? sn : 0.0;
+        }
         if constexpr (FAM == 0) {
           psib = stateUpdate(A, inv, a, sref, dt, lsr);
           mu = a * arsinhexp(0.5 * inv.v0 * vmag, psib * inva);
@@ -680,6 +739,10 @@ __global__ void __launch_bounds__(128, 3)
     if (A.law == 2) A.reg[po] = reg;
   }
   if (pt) {
+    if constexpr (TPK) {
+      A.tp_pres[po] = tpP;
+      A.tp_temp[po] = tpT;
+    }
     if (nucleating) {
       A.init[po] = sn0;
       A.init[plane + po] = t10;
@@ -735,18 +798,25 @@ int launch(const sei::DrArgs& a, const float* v3m, const float* tw, const double
   if (a.face_count <= 0) return 0;
   if (a.law < 0 || a.law > 9 || !a.peak || !a.trup || (a.nucleate && !a.nuc) ||
       (a.law >= 1 && a.law <= 3 && (!a.mu_s || !a.mu_d || !a.d_c || !a.cohesion || !a.t_forced || !a.tdyn)) ||
-      (a.law == 2 && !a.reg) || (a.law >= 7 && (!a.dir1 || !a.dir2 || !a.onset || !a.taus || !a.taur)))
+      (a.law == 2 && !a.reg) || (a.law >= 7 && (!a.dir1 || !a.dir2 || !a.onset || !a.taus || !a.taur)) ||
+      (a.tp && ((a.law != 0 && (a.law < 4 || a.law > 6)) || !a.tp_hw || !a.tp_hyd || !a.tp_theta || !a.tp_sigma ||
+                !a.tp_temp || !a.tp_pres)))
     return -1;
   constexpr int FPB = FaceGroup<NP>::kFaces;
   const int blocks = (a.face_count + FPB - 1) / FPB;
-  if (a.law == 0)
-    sei_dr_faces<N, B, NP, 0><<<blocks, 128, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (a.law == 0 && a.tp)
+    sei_dr_faces<N, B, NP, 0, true><<<blocks, 128, 0, st>>>(a, v3m, tw, res);
+  else if (a.law == 0)
+    sei_dr_faces<N, B, NP, 0, false><<<blocks, 128, 0, st>>>(a, v3m, tw, res);
+  else if (a.law >= 4 && a.law <= 6 && a.tp)
+    sei_dr_faces<N, B, NP, 1, true><<<blocks, 128, 0, st>>>(a, v3m, tw, res);
   else if (a.law >= 4 && a.law <= 6)
-    sei_dr_faces<N, B, NP, 1><<<blocks, 128, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
+    sei_dr_faces<N, B, NP, 1, false><<<blocks, 128, 0, st>>>(a, v3m, tw, res);
   else if (a.law >= 7)
-    sei_dr_faces<N, B, NP, 3><<<blocks, 128, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
+    sei_dr_faces<N, B, NP, 3, false><<<blocks, 128, 0, st>>>(a, v3m, tw, res);
   else
-    sei_dr_faces<N, B, NP, 2><<<blocks, 128, 0, (cudaStream_t)stream>>>(a, v3m, tw, res);
+    sei_dr_faces<N, B, NP, 2, false><<<blocks, 128, 0, st>>>(a, v3m, tw, res);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -764,6 +834,11 @@ const T* symbolAddress(const T& sym) {
 namespace sei {
 
 int drNumPoints(int order) { return (order + 1) * (order + 1); }
+
+int launchTpTables(void* stream) {
+  sei_tp_tables<<<1, kTpModes, 0, (cudaStream_t)stream>>>();
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
 
 int launchDrAdvanceTime(double* t, double dt, void* stream) {
   sei_dr_advance_time<<<1, 1, 0, (cudaStream_t)stream>>>(t, dt);

@@ -186,7 +186,18 @@ struct DrArgs {
   double* reg;                                            // regularised strength (law 2)
   double healing, v_star, prakash_length, tp_exponent;
   const double *dir1, *dir2, *onset, *taus, *taur;  // imposed slip rates, [nf][npts]
+  // thermal pressurisation of the rate-and-state laws (tp = 1): constants, per-point shear-zone
+  // half width and hydraulic diffusivity, Fourier modes of temperature and pressure [60][nf][npts],
+  // temperature and pressure [nf][npts]
+  int tp;
+  double tp_alpha, tp_rhoc, tp_lambda, tp_t0, tp_p0;
+  const double *tp_hw, *tp_hyd;
+  double *tp_theta, *tp_sigma, *tp_temp, *tp_pres;
 };
+constexpr int kTpModes = 60;
+// Fills the device tables of the thermal-pressurisation modes (wave numbers, inverse-transform
+// weights, heat source); once per device.
+int launchTpTables(void* stream);
 // Adds dt to the device fault time t.
 int launchDrAdvanceTime(double* t, double dt, void* stream);
 int launchDrFaces(int order, const DrArgs& a, void* stream);

@@ -74,6 +74,13 @@ class LSWParams(C.Structure):
         return cls(**d)
 
 
+class TPParams(C.Structure):
+    """sei_tp_params: thermal pressurisation of the rate-and-state laws."""
+    _fields_ = [(n, C.c_double) for n in ("thermal_diffusivity", "heat_capacity", "undrained_tp_response",
+                                          "initial_temperature", "initial_pressure", "half_width_shear_zone",
+                                          "hydraulic_diffusivity")]
+
+
 class ISRParams(C.Structure):
     """sei_isr_params: imposed slip rate, law 7 (regularised Yoffe), 8 (Gaussian) or 9 (delta)."""
     _fields_ = [("law", C.c_int)] + [(n, C.c_double) for n in ("slip_dir1", "slip_dir2", "onset_time", "tau_s", "tau_r",
@@ -84,7 +91,8 @@ DR_FIELDS = {"psi": 0, "slip_rate1": 1, "slip_rate2": 2, "slip1": 3, "slip2": 4,
              "traction2": 8, "a": 9, "sn0": 10, "tau1_0": 11, "tau2_0": 12, "mu_s": 13, "mu_d": 14, "d_c": 15,
              "cohesion": 16, "forced_rupture_time": 17, "peak_slip_rate": 18, "rupture_time": 19,
              "dyn_stress_time": 20, "nuc_sn": 21, "nuc_tau1": 22, "nuc_tau2": 23, "reg_strength": 24,
-             "slip_dir1": 25, "slip_dir2": 26, "onset_time": 27, "tau_s": 28, "tau_r": 29}
+             "slip_dir1": 25, "slip_dir2": 26, "onset_time": 27, "tau_s": 28, "tau_r": 29, "tp_half_width": 30,
+             "tp_hydraulic_diffusivity": 31, "tp_temperature": 32, "tp_pressure": 33}
 
 
 class _Mesh(C.Structure):
@@ -165,6 +173,7 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_dr_setup_lsw", i, [VP, C.POINTER(LSWParams), C.POINTER(i64)])
     _sig(lib, "sei_dr_setup_rate_state", i, [VP, C.POINTER(RSParams), i, C.POINTER(i64)])
     _sig(lib, "sei_dr_setup_imposed", i, [VP, C.POINTER(ISRParams), C.POINTER(i64)])
+    _sig(lib, "sei_dr_set_thermal_pressurization", i, [VP, i, C.POINTER(TPParams)])
     _sig(lib, "sei_set_mesh", i, [VP, C.POINTER(_Mesh), C.POINTER(i64), C.POINTER(i64)])
     _sig(lib, "sei_receivers_setup", i, [VP, i64, VP, C.c_double, C.c_uint, i, VP])
     _sig(lib, "sei_receivers_columns", i, [VP])
@@ -557,6 +566,10 @@ class Context:
         self.nfaces = nf.value
         self.npts = self.lib.sei_dr_num_points(self.order)
         return self.nfaces
+
+    def dr_set_thermal_pressurization(self, on=True, params: "TPParams" = None):
+        self._check(self.lib.sei_dr_set_thermal_pressurization(self.h, int(on), C.byref(params) if params else None),
+                    "sei_dr_set_thermal_pressurization")
 
     def dr_setup_lsw(self, params: "LSWParams"):
         nf = C.c_int64()
