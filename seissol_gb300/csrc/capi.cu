@@ -12,6 +12,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "internal.h"
 #include "output.h"
 #include "mlp.cuh"
@@ -168,6 +170,14 @@ int fail(sei_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
   return code;
 }
+
+// Named NVTX range for timeline tools (Nsight Systems); host-side, a no-op without a tool.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 int cudaFail(sei_ctx* c, cudaError_t e, const char* what) {
   return fail(c, SEI_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
@@ -576,6 +586,7 @@ sei::DrArgs drArgs(sei_ctx* c, double dt) {
 }
 
 int launchDr(sei_ctx* c, double dt) {
+  NvtxRange range("sei fault step");
   if (!c->dr_ready) return fail(c, SEI_ERR_STATE, "dynamic rupture not set up (sei_dr_setup)");
   int rc = profMark(c, 2);
   if (rc) return rc;
@@ -639,6 +650,7 @@ double recvTime(sei_ctx* c, int64_t k) {
 // then the group's receivers h_recv_list[first, first + count) at every sampling time inside the
 // step, in batches of kRecvMaxSamples; each batch is logged for the host-side assembly.
 int recordReceivers(sei_ctx* c, int g, double T, double dt, int64_t first, int64_t count) {
+  NvtxRange range("sei receivers");
   if (c->nrecv == 0 || count == 0) return SEI_OK;
   int64_t& k = c->recv_next[g];
   if (!(recvTime(c, k) < T + dt)) return SEI_OK;
@@ -705,6 +717,7 @@ int runKernel(sei_ctx* c, int kernel, double dt, int steps, const double* given 
   int rc = SEI_OK;
   const bool fullStep = kernel == SEI_KERNEL_ALL || kernel == SEI_KERNEL_ALL_DR;
   for (int s = 0; s < steps && rc == SEI_OK; ++s) {
+    NvtxRange range("sei step");
     if (fullStep && c->nrecv &&
         (rc = recordReceivers(c, (int)c->recv_next.size() - 1, c->sim_time, dt, 0, c->nrecv)))
       return rc;
@@ -1077,6 +1090,7 @@ int sei_evaluate_taylor(sei_ctx* c, const double* coeffs, float* out_device) {
 }
 
 int sei_run(sei_ctx* c, int kernel, double dt, int nsteps) {
+  NvtxRange range("sei_run");
   int rc = checkReady(c);
   if (rc) return rc;
   if (nsteps < 0 || !(dt >= 0) || !std::isfinite(dt)) return fail(c, SEI_ERR_ARG, "invalid dt or step count");
@@ -1166,6 +1180,7 @@ static int runHostPipelined(sei_ctx* c, double dt, int nsteps, const float* in, 
 }
 
 int sei_run_host(sei_ctx* c, int kernel, double dt, int nsteps, const float* dofs_in, float* dofs_out) {
+  NvtxRange range("sei_run_host");
   int rc = checkReady(c);
   if (rc) return rc;
   if (!dofs_in || !dofs_out) return fail(c, SEI_ERR_ARG, "null host buffer");
@@ -2486,6 +2501,7 @@ sei::ViscoArrays viscoRangeView(sei_ctx* c, int64_t s, int64_t e, bool neighbour
 // faces of the cluster, neighbour flux) of the clusters whose step ends at k + 1 (TimeCluster
 // predict / correct, TimeCommon::computeIntegrals).
 int ltsCycle(sei_ctx* c) {
+  NvtxRange range("sei LTS cycle");
   int rc0 = SEI_OK;
   const int blk = c->nq * c->Bp;
   const int64_t steps = (int64_t)1 << (c->ncl - 1);
@@ -2685,6 +2701,7 @@ int sei_kernel_times_by_kind(sei_ctx* c, double* ms, int* counts) {
 }
 
 int sei_autotune(sei_ctx* c, double dt, int steps, sei_tune_result* out) {
+  NvtxRange range("sei_autotune");
   int rc = checkReady(c);
   if (rc) return rc;
   if (c->visco || c->lts) return fail(c, SEI_ERR_UNSUPPORTED, "the autotuner covers global stepping of the elastic kernels");
