@@ -429,8 +429,9 @@ int sei_lts_permutation(sei_ctx* ctx, int64_t* perm /*[n]*/);
  * the start of each of its own steps (the times are the same sequence for all); a sample is
  * returned once every receiver has it, and cycles run without graph replay while receivers are
  * set.  sei_lts_setup locates existing receivers again on the reordered cells and restarts their
- * clocks.  Elastic equations only (SEI_ERR_UNSUPPORTED with the viscoelastic ones).  A new mesh
- * removes the receivers. */
+ * clocks.  With the viscoelastic equations the receivers give the nine elastic quantities (the
+ * quantity mask covers those); set them up after sei_visco_setup.  A new mesh removes the
+ * receivers. */
 #define SEI_RECV_ROTATION 1
 #define SEI_RECV_STRAIN 2
 int sei_receivers_setup(sei_ctx* ctx, int64_t n, const double* xyz /*[n][3]*/, double interval, unsigned quantity_mask,

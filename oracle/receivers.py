@@ -45,13 +45,16 @@ def basis_at(order, xez, cell_coords):
     return phi, grad.T @ dref
 
 
-def sample(order, derivs, phi, dphi, offsets, qmask=0x1FF, rotation=False, strain=False):
-    """Rows (time offset, kept quantities, rot1-3, strain 6) of one receiver for each offset."""
+def sample(order, derivs, phi, dphi, offsets, qmask=0x1FF, rotation=False, strain=False, visco=False):
+    """Rows (time offset, kept quantities, rot1-3, strain 6) of one receiver for each offset.
+    visco: derivatives of the viscoelastic update, [order][27][B] (the nine elastic quantities
+    first, every stage with all basis rows)."""
     blocks, off = [], 0
     for i in range(order):
-        b = dg_setup.nbasis3(order - i)
-        blocks.append(np.asarray(derivs[off: off + 9 * b], float).reshape(9, b))
-        off += 9 * b
+        b = len(phi) if visco else dg_setup.nbasis3(order - i)
+        nq = 27 if visco else 9
+        blocks.append(np.asarray(derivs[off: off + nq * b], float).reshape(nq, b)[:9])
+        off += nq * b
     rows = []
     for t in offsets:
         B = len(phi)

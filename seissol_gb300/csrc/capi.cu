@@ -88,6 +88,7 @@ struct sei_ctx {
   int32_t *d_recv_ucell = nullptr, *d_recv_slot = nullptr;
   float *d_recv_q = nullptr, *d_recv_i = nullptr, *d_recv_star = nullptr, *d_recv_derivs = nullptr;
   float *d_recv_phi = nullptr, *d_recv_dphi = nullptr;
+  float *d_recv_grad = nullptr, *d_recv_theta = nullptr;  // viscoelastic: the cells' gradients and attenuation
   double recv_interval = 0.0;
   unsigned recv_qmask = 0;
   int recv_derived = 0, recv_ncols = 0;
@@ -219,10 +220,11 @@ void freeFault(sei_ctx* c) {
 void freeOutput(sei_ctx* c) {
   for (void* p : {(void*)c->d_recv_ucell, (void*)c->d_recv_slot, (void*)c->d_recv_q, (void*)c->d_recv_i,
                   (void*)c->d_recv_star, (void*)c->d_recv_derivs, (void*)c->d_recv_phi, (void*)c->d_recv_dphi,
-                  (void*)c->d_recv_list})
+                  (void*)c->d_recv_list, (void*)c->d_recv_grad, (void*)c->d_recv_theta})
     cudaFree(p);
   c->d_recv_ucell = c->d_recv_slot = c->d_recv_list = nullptr;
   c->d_recv_q = c->d_recv_i = c->d_recv_star = c->d_recv_derivs = c->d_recv_phi = c->d_recv_dphi = nullptr;
+  c->d_recv_grad = c->d_recv_theta = nullptr;
   c->nrecv = c->nrecv_cells = 0;
   c->recv_cell.clear();
   c->recv_xyz.clear();
@@ -614,6 +616,8 @@ sei::ViscoArrays viscoArrays(sei_ctx* c) {
   return v;
 }
 
+int recordReceivers(sei_ctx* c, int g, double T, double dt, int64_t first, int64_t count);
+
 // Viscoelastic steps: ADER, volume + local flux, neighbour flux (kernel kinds 0, 3, 1).
 int runVisco(sei_ctx* c, int kernel, double dt, int steps, const double* given = nullptr) {
   float coeffs[8];
@@ -628,6 +632,9 @@ int runVisco(sei_ctx* c, int kernel, double dt, int steps, const double* given =
   c->prof_used = 0;
   int rc = SEI_OK;
   for (int s = 0; s < steps && rc == SEI_OK; ++s) {
+    if (kernel == SEI_KERNEL_ALL && c->nrecv &&
+        (rc = recordReceivers(c, (int)c->recv_next.size() - 1, c->sim_time, dt, 0, c->nrecv)))
+      break;
     if (ader && !(rc = profMark(c, 0)) && c->vk.ader(v, coeffs, c->stream)) rc = fail(c, SEI_ERR_CUDA, "viscoelastic ADER launch failed");
     if (!rc && lint && !(rc = profMark(c, 3)) && c->vk.lint(v, c->stream))
       rc = fail(c, SEI_ERR_CUDA, "viscoelastic local-integral launch failed");
@@ -654,19 +661,33 @@ int recordReceivers(sei_ctx* c, int g, double T, double dt, int64_t first, int64
   if (c->nrecv == 0 || count == 0) return SEI_OK;
   int64_t& k = c->recv_next[g];
   if (!(recvTime(c, k) < T + dt)) return SEI_OK;
-  const int blk = 9 * c->Bp;
+  const int blk = c->nq * c->Bp;
   if (sei::launchGatherRows((int)c->nrecv_cells, c->d_recv_ucell, c->Q, c->d_recv_q, blk, c->stream))
     return fail(c, SEI_ERR_CUDA, "receiver gather launch failed");
   float co[8];
   taylorCoeffs(c->cfg.order, dt, co);
-  sei::DeviceArrays d{};
-  d.n = (int)c->nrecv_cells;
-  d.Q = c->d_recv_q;
-  d.I = c->d_recv_i;
-  d.derivs = c->d_recv_derivs;
-  d.dslot = nullptr;
-  d.star_nz = c->d_recv_star;
-  if (c->k.ader(d, co, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "receiver ADER launch failed");
+  if (c->visco) {
+    sei::ViscoArrays v{};
+    v.n = (int)c->nrecv_cells;
+    v.Q = c->d_recv_q;
+    v.I = c->d_recv_i;
+    v.star_nz = c->d_recv_star;
+    v.grad = c->d_recv_grad;
+    v.theta = c->d_recv_theta;
+    for (int i = 0; i < 3; ++i) v.omega[i] = c->omega[i];
+    v.derivs = c->d_recv_derivs;
+    v.dslot = nullptr;
+    if (c->vk.ader(v, co, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "receiver ADER launch failed");
+  } else {
+    sei::DeviceArrays d{};
+    d.n = (int)c->nrecv_cells;
+    d.Q = c->d_recv_q;
+    d.I = c->d_recv_i;
+    d.derivs = c->d_recv_derivs;
+    d.dslot = nullptr;
+    d.star_nz = c->d_recv_star;
+    if (c->k.ader(d, co, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "receiver ADER launch failed");
+  }
   sei::RecvEvalArgs a{};
   a.nrecv = (int)count;
   a.list = c->d_recv_list + first;
@@ -678,6 +699,7 @@ int recordReceivers(sei_ctx* c, int g, double T, double dt, int64_t first, int64
   a.qmask = c->recv_qmask;
   a.derived = c->recv_derived;
   a.ncols = c->recv_ncols;
+  a.visco = c->visco ? 1 : 0;
   while (recvTime(c, k) < T + dt) {
     const int64_t k0 = k;
     a.nsamples = 0;
@@ -1248,7 +1270,6 @@ int sei_receivers_setup(sei_ctx* c, int64_t n, const double* xyz, double interva
   int rc = checkReady(c);
   if (rc) return rc;
   if (!c->has_mesh) return fail(c, SEI_ERR_STATE, "receivers need a mesh built by the context");
-  if (c->visco) return fail(c, SEI_ERR_UNSUPPORTED, "receivers of the viscoelastic equations are not supported");
   if (n < 0 || (n > 0 && !xyz) || !(interval > 0) || !std::isfinite(interval) || qmask > 0x1FFu ||
       (derived & ~(SEI_RECV_ROTATION | SEI_RECV_STRAIN)))
     return fail(c, SEI_ERR_ARG, "receivers: n >= 0, points, interval > 0, quantity mask of 9 bits, derived flags");
@@ -1325,13 +1346,15 @@ int sei_receivers_setup(sei_ctx* c, int64_t n, const double* xyz, double interva
     std::vector<int64_t> fillp(gstart.begin(), gstart.end());
     for (int64_t r = 0; r < n; ++r) list[n + (ncl ? fillp[grp[r]]++ : r)] = (int32_t)r;
   }
-  const size_t blk = (size_t)9 * c->Bp, dsz = (size_t)sei::derivativesSize(order);
+  const size_t blk = (size_t)c->nq * c->Bp;
+  const size_t dsz = c->visco ? (size_t)c->vk.derivSize : (size_t)sei::derivativesSize(order);
   auto dalloc = [&](void** ptr, size_t bytes) { return cudaMalloc(ptr, bytes) == cudaSuccess; };
   bool ok = dalloc((void**)&c->d_recv_ucell, m * 4) && dalloc((void**)&c->d_recv_slot, n * 4) &&
             dalloc((void**)&c->d_recv_q, m * blk * 4) && dalloc((void**)&c->d_recv_i, m * blk * 4) &&
             dalloc((void**)&c->d_recv_star, m * 3 * sei::kStarNnz * 4) && dalloc((void**)&c->d_recv_derivs, m * dsz * 4) &&
             dalloc((void**)&c->d_recv_phi, phi.size() * 4) && dalloc((void**)&c->d_recv_dphi, dphi.size() * 4) &&
-            dalloc((void**)&c->d_recv_list, list.size() * 4);
+            dalloc((void**)&c->d_recv_list, list.size() * 4) &&
+            (!c->visco || (dalloc((void**)&c->d_recv_grad, m * 9 * 4) && dalloc((void**)&c->d_recv_theta, m * 9 * 4)));
   if (!ok) {
     cudaGetLastError();
     return fail(c, SEI_ERR_OOM, "device allocation for the receivers failed");
@@ -1341,7 +1364,9 @@ int sei_receivers_setup(sei_ctx* c, int64_t n, const double* xyz, double interva
   SEI_CUDA(cudaMemcpy(c->d_recv_phi, phi.data(), phi.size() * 4, cudaMemcpyHostToDevice));
   SEI_CUDA(cudaMemcpy(c->d_recv_dphi, dphi.data(), dphi.size() * 4, cudaMemcpyHostToDevice));
   SEI_CUDA(cudaMemcpy(c->d_recv_list, list.data(), list.size() * 4, cudaMemcpyHostToDevice));
-  if (sei::launchGatherRows((int)m, c->d_recv_ucell, c->star_nz, c->d_recv_star, 3 * sei::kStarNnz, c->stream))
+  if (sei::launchGatherRows((int)m, c->d_recv_ucell, c->star_nz, c->d_recv_star, 3 * sei::kStarNnz, c->stream) ||
+      (c->visco && (sei::launchGatherRows((int)m, c->d_recv_ucell, c->d_grad, c->d_recv_grad, 9, c->stream) ||
+                    sei::launchGatherRows((int)m, c->d_recv_ucell, c->d_theta, c->d_recv_theta, 9, c->stream))))
     return fail(c, SEI_ERR_CUDA, "receiver gather launch failed");
   c->recv_qmask = qmask;
   c->recv_derived = derived;

@@ -34,16 +34,16 @@ __global__ void sei_gather_rows(int m, const int32_t* __restrict__ src, const fl
 // One warp per receiver.  Row of sample s: time, the quantities of qmask, then rotation
 // (d8/dy - d7/dz, d6/dz - d8/dx, d7/dx - d6/dy) and strain (eps_xx, eps_xy, eps_xz, eps_yy,
 // eps_yz, eps_zz from the velocity gradient), Receiver.cpp:271-302.
-template <int N>
+template <int N, bool VIS>
 __global__ void __launch_bounds__(128) sei_recv_eval(sei::RecvEvalArgs A) {
   constexpr int B = N * (N + 1) * (N + 2) / 6;
   constexpr int L = (B + 31) / 32;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= A.nrecv) return;
   const int r = A.list[warp];
-  int dsz = 0;
+  int dsz = VIS ? N * 27 * B : 0;
 #pragma unroll
-  for (int i = 0; i < N; ++i) dsz += (N - i) * (N - i + 1) * (N - i + 2) / 6 * 9;
+  for (int i = 0; i < N; ++i) dsz += VIS ? 0 : (N - i) * (N - i + 1) * (N - i + 2) / 6 * 9;
   const float* d = A.derivs + (size_t)A.slot[r] * dsz;
   float phi[L], dphi[L][3];
 #pragma unroll
@@ -78,9 +78,10 @@ __global__ void __launch_bounds__(128) sei_recv_eval(sei::RecvEvalArgs A) {
         int off = 0;
 #pragma unroll
         for (int i = 0; i < N; ++i) {
-          const int bi = (N - i) * (N - i + 1) * (N - i + 2) / 6;
+          // the elastic kernels keep the rows of degree < N - i of stage i; the viscoelastic ones all
+          const int bi = VIS ? B : (N - i) * (N - i + 1) * (N - i + 2) / 6;
           if (l < bi) v = fmaf(co[i], __ldg(d + off + q * bi + l), v);
-          off += 9 * bi;
+          off += (VIS ? 27 : 9) * bi;
         }
         val[q] = fmaf(phi[u], v, val[q]);
         if (q >= 6)
@@ -276,12 +277,15 @@ int launchGatherRows(int m, const int32_t* src, const float* in, float* out, int
 int launchRecvEval(int order, const RecvEvalArgs& a, void* stream) {
   if (a.nrecv <= 0 || a.nsamples <= 0) return 0;
   const int blocks = (a.nrecv + 3) / 4;
-  switch (order) {
-    case 2: sei_recv_eval<2><<<blocks, 128, 0, (cudaStream_t)stream>>>(a); break;
-    case 3: sei_recv_eval<3><<<blocks, 128, 0, (cudaStream_t)stream>>>(a); break;
-    case 4: sei_recv_eval<4><<<blocks, 128, 0, (cudaStream_t)stream>>>(a); break;
-    case 5: sei_recv_eval<5><<<blocks, 128, 0, (cudaStream_t)stream>>>(a); break;
-    case 6: sei_recv_eval<6><<<blocks, 128, 0, (cudaStream_t)stream>>>(a); break;
+  cudaStream_t st = (cudaStream_t)stream;
+  switch (order * 2 + (a.visco ? 1 : 0)) {
+    case 4: sei_recv_eval<2, false><<<blocks, 128, 0, st>>>(a); break;
+    case 6: sei_recv_eval<3, false><<<blocks, 128, 0, st>>>(a); break;
+    case 8: sei_recv_eval<4, false><<<blocks, 128, 0, st>>>(a); break;
+    case 9: sei_recv_eval<4, true><<<blocks, 128, 0, st>>>(a); break;
+    case 10: sei_recv_eval<5, false><<<blocks, 128, 0, st>>>(a); break;
+    case 11: sei_recv_eval<5, true><<<blocks, 128, 0, st>>>(a); break;
+    case 12: sei_recv_eval<6, false><<<blocks, 128, 0, st>>>(a); break;
     default: return -1;
   }
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;

@@ -56,6 +56,7 @@ struct RecvEvalArgs {
   unsigned qmask;                  // quantities written (bit q: quantity q)
   int derived;                     // SEI_RECV_ROTATION | SEI_RECV_STRAIN
   int ncols;
+  int visco;    // derivatives of the viscoelastic kernels: [order][27][B] (every stage all rows)
   double* out;  // [nsamples][nrecv][ncols], receivers in list order
 };
 

@@ -141,14 +141,7 @@ def test_output_errors(built_lib):
     ctx.receivers_setup([], 1e-3)  # removes them
     assert ctx.lib.sei_receivers_columns(ctx.h) == 0
     ctx.close()
-    from seissol_gb300 import Context
-    ctx = Context(4, device=0)
-    ctx.build_periodic_cube(4, 4, 4, seed=13)
-    ctx.visco_setup(50.0, 25.0, 1.0, 100.0)
-    with pytest.raises(SeiError) as e:
-        ctx.receivers_setup([[10.0, 10.0, 10.0]], 1e-3)
-    assert e.value.code == -7
-    ctx.close()
+
 
 
 def test_receivers_under_lts_match_oracle(built_lib):
@@ -226,4 +219,58 @@ def test_receivers_under_lts_match_oracle(built_lib):
     scale = np.abs(want).max(axis=(0, 1))
     err = np.abs(got - want).max(axis=(0, 1)) / np.maximum(scale, 1e-30)
     assert err[1:].max() < 1e-4, err
+    ctx.close()
+
+
+@pytest.mark.parametrize("order", [4, 5])
+def test_viscoelastic_receivers_match_oracle(built_lib, order):
+    """The nine elastic quantities of the viscoelastic equations (3 mechanisms) at 8 receivers, 3
+    samples per step over 3 steps, each step from the GPU's DOFs at its start through the dense
+    FP64 viscoelastic predictor; 2e-5 of each column's largest magnitude, times exact."""
+    from seissol_gb300 import Context
+    from oracle import visco
+    QP, QS, FC, RATIO = 50.0, 25.0, 1.0, 100.0
+    ctx = Context(order, device=0)
+    n = ctx.build_periodic_cube(4, 4, 4, perturb=0.05, seed=2)
+    ctx.visco_setup(QP, QS, FC, RATIO)
+    coords, material, _ = ctx.get_geometry()
+    cells = ctx.get_cells()
+    mats, thetas = [], []
+    for rho, mu, lam in material:
+        mu_u, lam_u, omega, theta = visco.fit_attenuation(rho, mu, lam, QP, QS, FC, RATIO)
+        mats.append([rho, mu_u, lam_u])
+        thetas.append(theta)
+    ops = visco.cell_operators(coords, np.array(mats), omega, np.array(thetas), cells["neighbor"])
+    star = np.concatenate([ops["star"], ops["ET"][:, None]], axis=1)
+    pts = np.random.default_rng(order).uniform(5.0, 395.0, (8, 3))
+    q0 = np.random.default_rng(7).uniform(-1, 1, (n, 27, ctx.B)).astype(np.float32)
+    ctx.set_dofs(q0)
+    dt = ctx.cfl_timestep(0.5)
+    rc = ctx.receivers_setup(pts, dt / 3.0, rotation=True, strain=True)
+    ref_cells, xez = receivers.locate(coords, pts)
+    assert np.array_equal(rc, ref_cells)
+    o = visco.ViscoLts(order)
+    times = _times(0.0, dt / 3.0, dt, 3)
+    want = []
+    for s in range(3):
+        q = ctx.get_dofs()
+        _, d = o.ader(q[rc].astype(np.float64), star[rc], dg_setup.taylor_integrate(order, 0.0, dt), want_derivs=True)
+        T = s * dt
+        rows = []
+        for r in range(len(pts)):
+            phi, dphi = receivers.basis_at(order, xez[r], coords[rc[r]])
+            rr = receivers.sample(order, d[r], phi, dphi, [t - T for t in times[s]], rotation=True, strain=True,
+                                  visco=True)
+            rr[:, 0] += T
+            rows.append(rr)
+        want.append(np.stack(rows, axis=1))
+        ctx.run("all", dt, 1)
+    ctx.sync()
+    want = np.concatenate(want)
+    got = ctx.receivers_read()
+    assert got.shape == want.shape
+    assert np.array_equal(got[:, :, 0], want[:, :, 0])
+    scale = np.abs(want).max(axis=(0, 1))
+    err = np.abs(got - want).max(axis=(0, 1)) / np.maximum(scale, 1e-30)
+    assert err[1:].max() < 2e-5, err
     ctx.close()
