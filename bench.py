@@ -372,6 +372,86 @@ def config1_measurement(local, steps=100):
             "note": "10,000 cells fill a fraction of the GPU: the GPU step time is launch-bound here"}
 
 
+def output_measurement(local, steps, nrecv=1000):
+    """Cost of the receiver output on the headline workload: elastic order 6, 400,000 tets, mixed
+    path, kernel all.  `steps` steps are timed without receivers, then with `nrecv` receivers at
+    seeded random points sampled every dt / 4 (time, nine quantities, rotation and strain: 19 columns),
+    then the drain of the staged samples to host memory.  CUDA events time the GPU side, a wall
+    clock the whole call."""
+    import numpy as np
+
+    from seissol_gb300 import Context
+
+    ctx = Context(ORDER, device=local, precision=PATHS["f16x3"][0])
+    n = ctx.build_periodic_cube(*DIMS, perturb=PERTURB, seed=SEED)
+    dt = ctx.cfl_timestep(0.5)
+    coords, _, _ = ctx.get_geometry()
+    lo, hi = coords.reshape(-1, 3).min(axis=0), coords.reshape(-1, 3).max(axis=0)
+    rng = np.random.default_rng(SEED + 5)
+    pts = lo + (hi - lo) * rng.uniform(0.01, 0.99, (nrecv, 3))
+
+    def timed():
+        ctx.run("all", dt, 3)
+        ctx.sync()
+        t0 = time.perf_counter()
+        ctx.run("all", dt, steps)
+        ctx.sync()
+        return ctx.last_run_ms() / steps, (time.perf_counter() - t0) * 1e3 / steps
+
+    plain_ms, plain_wall = timed()
+    t0 = time.perf_counter()
+    ctx.receivers_setup(pts, dt / 4, rotation=True, strain=True)
+    setup_ms = (time.perf_counter() - t0) * 1e3
+    ctx.receivers_read()  # samples of the setup time
+    recv_ms, recv_wall = timed()
+    t0 = time.perf_counter()
+    samples = ctx.receivers_read()
+    read_ms = (time.perf_counter() - t0) * 1e3
+    ctx.close()
+    return {"workload": f"elastic order {ORDER}, {n:,}-tet periodic cube {DIMS[0]}x{DIMS[1]}x{DIMS[2]} cubes, mixed "
+                        f"path, kernel all, {steps} steps after 3 warm-up steps; {nrecv} receivers at seeded random "
+                        "points, sampled every dt/4, 9 quantities + rotation + strain",
+            "receivers": nrecv, "steps": steps, "ms_per_step_without": plain_ms, "ms_per_step_with": recv_ms,
+            "overhead_ms_per_step": recv_ms - plain_ms, "overhead_frac": recv_ms / plain_ms - 1.0,
+            "wall_ms_per_step_without": plain_wall, "wall_ms_per_step_with": recv_wall,
+            "setup_ms": setup_ms, "samples_read": int(samples.shape[0]), "columns": int(samples.shape[2]),
+            "read_ms": read_ms, "read_bytes": int(samples.nbytes)}
+
+
+def ingest_measurement(local):
+    """sei_set_mesh at benchmark size: the 400,000-tet cube of the headline workload given as PUML
+    arrays (1.6 M geometric vertices, connectivity, identify-vertex topology, material), ingested
+    into a device context (face relations, operators, upload), beside the built-in cube generator
+    on the same device; the two contexts' cell arrays must agree bit for bit."""
+    import numpy as np
+
+    from seissol_gb300 import Context
+
+    host = Context(ORDER, device=-1)
+    n = host.build_periodic_cube(*DIMS, perturb=PERTURB, seed=SEED)
+    coords, material, topo = host.get_geometry()
+    geo = coords.reshape(-1, 3)
+    con = np.arange(4 * n, dtype=np.int64).reshape(n, 4)
+    identify = np.empty(4 * n, np.int64)
+    identify[con.reshape(-1)] = topo.reshape(-1)
+    a = Context(ORDER, device=local)
+    t0 = time.perf_counter()
+    a.build_periodic_cube(*DIMS, perturb=PERTURB, seed=SEED)
+    cube_s = time.perf_counter() - t0
+    b = Context(ORDER, device=local)
+    t0 = time.perf_counter()
+    nb, nf = b.set_mesh(geo, con, material, identify=identify)
+    ingest_s = time.perf_counter() - t0
+    ca, cb = a.get_cells(), b.get_cells()
+    same = nb == n and all(np.array_equal(ca[k], cb[k]) for k in ca)
+    for c in (host, a, b):
+        c.close()
+    return {"workload": f"{n:,}-tet periodic cube {DIMS[0]}x{DIMS[1]}x{DIMS[2]} cubes as PUML arrays "
+                        f"({len(geo):,} vertices + identify), order {ORDER}, device context",
+            "cells": n, "set_mesh_s": ingest_s, "cells_per_s": n / ingest_s, "builtin_cube_s": cube_s,
+            "identical_to_builtin": bool(same)}
+
+
 def lts_accuracy(local, visco, cycles):
     """Accuracy of the local-time-stepping paths on a small case of the same structure: order 5
     viscoelastic (FP32 kernels) or order 6 elastic mixed precision with the fault (FVW, the fault
@@ -970,6 +1050,10 @@ def run_ours(args, world, rank, local):
     cfg1 = None
     if rank == 0 and args.config1_steps > 0:
         cfg1 = config1_measurement(local, args.config1_steps)
+    out = ing = None
+    if rank == 0 and args.output_steps > 0:
+        out = output_measurement(local, args.output_steps)
+        ing = ingest_measurement(local)
 
     base = acc = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -991,7 +1075,7 @@ def run_ours(args, world, rank, local):
                 "gpu_launches": launches, "kernel_ms_per_step": kernels, "paths": paths_out,
                 "mixed_vs_fp32": ratio, "accuracy": acc, "dynamic_rupture": dr, "combined_o6_fault": comb,
                 "combined_o6_fault_lts": comb_lts, "proxy_o4_10k": cfg1,
-                "local_time_stepping": lts, "viscoelastic": vis}
+                "local_time_stepping": lts, "viscoelastic": vis, "receiver_output": out, "mesh_ingestion": ing}
         print(json.dumps(line))
     return 0
 
@@ -1014,6 +1098,8 @@ def main():
                     help="steps of the dynamic-rupture measurement (plain and warm-started); 0 skips it")
     ap.add_argument("--config1-steps", type=int, default=100,
                     help="steps of the order-4, 10,000-tet proxy workload against the FP64 oracle; 0 skips it")
+    ap.add_argument("--output-steps", type=int, default=50,
+                    help="steps of the receiver-output measurement (then the mesh-ingestion timing); 0 skips both")
     ap.add_argument("--combined-steps", type=int, default=10,
                     help="steps of the combined order-6 measurement (1M tets, 50,000-face fault); 0 skips it")
     ap.add_argument("--combined-lts-cycles", type=int, default=3,
