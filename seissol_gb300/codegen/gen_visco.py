@@ -10,12 +10,12 @@ src/Equations/viscoelastic/Model/ViscoelasticSetup.h) have a structure these ker
   diagonal of mechanism l's block;
 * the flux into the memory variables of mechanism l is omega_l W with one 9 x 6 block W per face.
 
-So a CTA holds 32 cells and 15 warps: warps 0..8 run the elastic column q exactly like the elastic
-kernels (premix with the star non-zeros, global matrices as FFMA literals), warps 9..14 run the
-strain column j = q - 9 through the same code with the strain sources (velocities) and
-coefficients, and then update the three memory variables j of their cell elementwise (the ADER
-kernel runs the same 15 column tasks on 16 cells per CTA, half a warp each, so that its larger
-shared memory still fits two CTAs on an SM):
+So a CTA holds 16 cells and 15 column tasks of 16 threads (half a warp each, one thread per cell):
+tasks 0..8 run the elastic column q exactly like the elastic kernels (premix with the star
+non-zeros, global matrices as FFMA literals), tasks 9..14 run the strain column j = q - 9 through
+the same code with the strain sources (velocities) and coefficients, and then update the three
+memory variables j of their cell elementwise.  Two CTAs share an SM (128 registers a thread), so
+one CTA's loads and barriers overlap the other's arithmetic:
 
   ADER    dQ_i(mem l j) = -omega_l (E_i(j) + dQ_{i-1}(mem l j)),  E_i = sum_e kDivMT_e (dQ_{i-1} S_e)
   volume  Q(mem l j) += -omega_l (V(j) + I(mem l j)),             V   = sum_e kDivM_e (I S_e)
@@ -175,6 +175,8 @@ sei_vader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout,
     sei_load_col<kBp>(Q + ((size_t)cl * kNQ + q) * kBp, z);
 #pragma unroll
     for (int k = 0; k < kBp; ++k) I[k] = coeffs.c[0] * z[k];
+#pragma unroll
+    for (int k = 0; k < kB; ++k) Xq[k * 16] = z[k];
     if (dbase) sei_store_col_scalar<kB>(dbase + q * kB, z);
   } else {
 #pragma unroll 1
@@ -193,9 +195,6 @@ sei_vader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout,
     for i in range(1, order):
         a(f"  // ---- stage {i}")
         a("  {")
-        a("    if (el) {")
-        a("#pragma unroll\n      for (int k = 0; k < kB; ++k) Xq[k * 16] = z[k];")
-        a("    }")
         a("    __syncthreads();")
         a("    float zn[kB];")
         a("#pragma unroll\n    for (int k = 0; k < kB; ++k) zn[k] = 0.f;")
@@ -203,7 +202,9 @@ sei_vader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout,
         _theta_from_smem(a, "M", "    ", w=16)
         a("    __syncthreads();")
         a("    if (el) {")
-        a(f"#pragma unroll\n      for (int k = 0; k < kB; ++k) {{ I[k] = fmaf(coeffs.c[{i}], zn[k], I[k]); z[k] = zn[k]; }}")
+        a(f"#pragma unroll\n      for (int k = 0; k < kB; ++k) I[k] = fmaf(coeffs.c[{i}], zn[k], I[k]);")
+        if i < order - 1:  # the next stage's exchange (every thread has read X: the barrier above)
+            a("#pragma unroll\n      for (int k = 0; k < kB; ++k) Xq[k * 16] = zn[k];")
         a(f"      if (dbase) sei_store_col_scalar<kB>(dbase + {i} * kNQ * kB + q * kB, zn);")
         a("    } else {")
         a("#pragma unroll 1")
@@ -242,16 +243,16 @@ sei_vader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout,
     a(f"""
 // Volume + local flux from the time-integrated DOFs (in place on Q).  aplus [n][4][81] (elastic
 // block), wplus [n][4][54] (memory block per unit omega), ftype [n][4].
-extern "C" __global__ void __launch_bounds__(480, 1)
+extern "C" __global__ void __launch_bounds__(240, 2)
 sei_vlint_o{order}(int n, float* __restrict__ Q, const float* __restrict__ Iin, const float* __restrict__ star_nz,
                    const float* __restrict__ grad, const float* __restrict__ theta, SeiOmega omega,
                    const float* __restrict__ aplus, const float* __restrict__ wplus,
-                   const unsigned char* __restrict__ ftype) {{""" + PROLOGUE)
+                   const unsigned char* __restrict__ ftype) {{""" + PROLOGUE_ADER)
     a("""  float I[kBp];
   if (el) sei_load_col<kBp>(Iin + ((size_t)cl * kNQ + q) * kBp, I);
   if (el) {
 #pragma unroll
-    for (int k = 0; k < kB; ++k) Xq[k * 32] = I[k];
+    for (int k = 0; k < kB; ++k) Xq[k * 16] = I[k];
   }
   __syncthreads();
   float acc[kBp];
@@ -262,7 +263,7 @@ sei_vlint_o{order}(int n, float* __restrict__ Q, const float* __restrict__ Iin, 
     for (int k = 0; k < kBp; ++k) acc[k] = 0.f;
   }
   // ---- volume: elastic columns Q += sum_e kDivM_e (I star_e); strain columns V = sum_e kDivM_e (I S_e)""")
-    _premix_matvec(a, G["kDivM"], "acc", B, B, "  ")
+    _premix_matvec(a, G["kDivM"], "acc", B, B, "  ", w=16)
     a("""  if (!el) {  // strain columns accumulate D = flux - V
 #pragma unroll
     for (int k = 0; k < kBp; ++k) acc[k] = -acc[k];
@@ -290,7 +291,7 @@ sei_vlint_o{order}(int n, float* __restrict__ Q, const float* __restrict__ Iin, 
         a("    if (el) {")
         a("      float T[kF];")
         _matvec(L, "      ", G["fMrT"][f], "I", "T", F, B, True)
-        a("#pragma unroll\n      for (int m = 0; m < kF; ++m) Xq[m * 32] = T[m];")
+        a("#pragma unroll\n      for (int m = 0; m < kF; ++m) Xq[m * 16] = T[m];")
         a("    }")
         a("    __syncthreads();")
         a(f"    const bool on = valid && ftype[(size_t)cl * 4 + {f}] != 1;")
@@ -302,7 +303,7 @@ sei_vlint_o{order}(int n, float* __restrict__ Q, const float* __restrict__ Iin, 
             if m not in bycol:
                 continue
             a("    { float g = 0.f;")
-            a(f"#pragma unroll\n      for (int s = 0; s < 9; ++s) g = fmaf(X[(s * kB + {m}) * 32 + lane], av[s], g);")
+            a(f"#pragma unroll\n      for (int s = 0; s < 9; ++s) g = fmaf(X[(s * kB + {m}) * 16 + lane], av[s], g);")
             for k, v in bycol[m]:
                 a(f"      acc[{k}] = fmaf({flit(v)}, g, acc[{k}]);")
             a("    }")
@@ -330,20 +331,20 @@ sei_vlint_o{order}(int n, float* __restrict__ Q, const float* __restrict__ Iin, 
     a(f"""
 // Neighbour flux of the regular faces (in place on Q): elastic columns as in the elastic kernel
 // with A- (elastic block); the memory variables j of mechanism l receive omega_l rDivM_f ((traces) W-).
-extern "C" __global__ void __launch_bounds__(480, 1)
+extern "C" __global__ void __launch_bounds__(240, 2)
 sei_vneighbor_o{order}(int n, float* __restrict__ Q, const float* __restrict__ I, const float* __restrict__ aminus,
                        const float* __restrict__ wminus, const int* __restrict__ nbr,
                        const unsigned char* __restrict__ rel, const unsigned char* __restrict__ ftype,
                        SeiOmega omega) {{
   extern __shared__ float sm[];
-  const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int cell = blockIdx.x * kCPB + lane;
+  const int q = threadIdx.x >> 4, lane = threadIdx.x & 15;
+  const int cell = blockIdx.x * kCPBA + lane;
   const bool valid = cell < n;
   const int cl = valid ? cell : n - 1;
   const bool el = q < 9;
   const int jv = el ? 0 : q - 9;
-  float* X = sm;  // [9][kF][32]
-  float* Xq = X + (el ? q : 0) * kF * 32 + lane;
+  float* X = sm;  // [9][kF][16]
+  float* Xq = X + (el ? q : 0) * kF * 16 + lane;
   float acc[kBp];
   if (el) {{
     sei_load_col<kBp>(Q + ((size_t)cl * kNQ + q) * kBp, acc);
@@ -373,7 +374,7 @@ sei_vneighbor_o{order}(int n, float* __restrict__ Q, const float* __restrict__ I
         _matvec(L, "          ", G["fP"][h], "R", "S", F, F, True)
         a("          break; }")
     a("      }")
-    a("#pragma unroll\n      for (int m = 0; m < kF; ++m) Xq[m * 32] = S[m];")
+    a("#pragma unroll\n      for (int m = 0; m < kF; ++m) Xq[m * 16] = S[m];")
     a("    }")
     a("    const float* am = el ? aminus + ((size_t)cl * 4 + f) * 81 + 9 * q : wminus + ((size_t)cl * 4 + f) * 54 + 9 * jv;")
     a("    float av[9];")
@@ -387,7 +388,7 @@ sei_vneighbor_o{order}(int n, float* __restrict__ Q, const float* __restrict__ I
             if m not in bycol:
                 continue
             a("        { float g = 0.f;")
-            a(f"#pragma unroll\n          for (int s = 0; s < 9; ++s) g = fmaf(X[(s * kF + {m}) * 32 + lane], av[s], g);")
+            a(f"#pragma unroll\n          for (int s = 0; s < 9; ++s) g = fmaf(X[(s * kF + {m}) * 16 + lane], av[s], g);")
             for k, v in bycol[m]:
                 a(f"          acc[{k}] = fmaf({flit(v)}, g, acc[{k}]);")
             a("        }")

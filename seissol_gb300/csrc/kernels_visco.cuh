@@ -12,7 +12,6 @@
 namespace {
 namespace KV = SEI_VCAT(sei_v, SEI_VORDER);
 
-constexpr int kThreads = 480;
 
 SeiOmega toOmega(const sei::ViscoArrays& d) {
   SeiOmega o{};
@@ -37,21 +36,22 @@ int launchVAder(const sei::ViscoArrays& d, const float* coeffs, void* stream) {
 
 int launchVLint(const sei::ViscoArrays& d, void* stream) {
   if (d.n <= 0) return 0;
-  const size_t smem = sizeof(float) * 9 * KV::kB * 32;
+  // 16 cells per CTA, 15 column tasks of 16 threads: the exchange X of 16 cells
+  const size_t smem = sizeof(float) * 9 * KV::kB * KV::kCPBA;
   if (cudaFuncSetAttribute(KV::SEI_VCAT(sei_vlint_o, SEI_VORDER), cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem) != cudaSuccess)
     return -1;
-  const int blocks = (d.n + KV::kCPB - 1) / KV::kCPB;
-  KV::SEI_VCAT(sei_vlint_o, SEI_VORDER)<<<blocks, kThreads, smem, (cudaStream_t)stream>>>(
+  const int blocks = (d.n + KV::kCPBA - 1) / KV::kCPBA;
+  KV::SEI_VCAT(sei_vlint_o, SEI_VORDER)<<<blocks, 15 * KV::kCPBA, smem, (cudaStream_t)stream>>>(
       d.n, d.Q, d.I, d.star_nz, d.grad, d.theta, toOmega(d), d.aplus, d.wplus, d.ftype);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
 int launchVNeighbor(const sei::ViscoArrays& d, void* stream) {
   if (d.n <= 0) return 0;
-  const size_t smem = sizeof(float) * 9 * KV::kF * 32;
-  const int blocks = (d.n + KV::kCPB - 1) / KV::kCPB;
-  KV::SEI_VCAT(sei_vneighbor_o, SEI_VORDER)<<<blocks, kThreads, smem, (cudaStream_t)stream>>>(
+  const size_t smem = sizeof(float) * 9 * KV::kF * KV::kCPBA;
+  const int blocks = (d.n + KV::kCPBA - 1) / KV::kCPBA;
+  KV::SEI_VCAT(sei_vneighbor_o, SEI_VORDER)<<<blocks, 15 * KV::kCPBA, smem, (cudaStream_t)stream>>>(
       d.n, d.Q, d.I, d.aminus, d.wminus, d.nbr, d.rel, d.ftype, toOmega(d));
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }

@@ -6,7 +6,9 @@ app/Proxy/Bindings.cpp:14-60.  Unlike the reference proxy, the data are a real m
 (synthetic periodic cube) with physical operators, and the time step is the CFL step.
 
 CLI:  python -m seissol_gb300.proxy <cells> <timesteps> <kernel>[,kernel...] [--order N] [--format json]
-      [--precision fp32|f16x3]; the *_dr kernels run on a planar fault at orders 4-6.
+      [--precision fp32|f16x3] [--mechanisms 0|3]; the *_dr kernels run on a planar fault at orders
+      4-6; --mechanisms 3 runs the viscoelastic equations (orders 4-5), as the reference's proxy
+      built for them (Qp 100, Qs 50, central frequency 0.5 Hz, frequency ratio 100).
 """
 from __future__ import annotations
 
@@ -33,6 +35,7 @@ class ProxyConfig:
     verbose: bool = True
     device: int = 0
     precision: int = 0  # SEI_PREC_FP32 / SEI_PREC_F16X3
+    mechanisms: int = 0  # 0 elastic, 3 viscoelastic (27 quantities)
 
 
 @dataclasses.dataclass
@@ -117,9 +120,14 @@ def cube_dims(cells: int):
     return nx, ny, nz
 
 
-def bytes_per_cell(order: int) -> float:
-    """Compulsory HBM bytes of one cell update (ADER + local + neighbour), float32."""
+def bytes_per_cell(order: int, mechanisms: int = 0) -> float:
+    """Compulsory HBM bytes of one cell update (ADER + local + neighbour), float32.  With
+    mechanisms: Q read and written, I written and read back, per face the elastic and memory
+    blocks of both flux matrices, the star non-zeros, gradients and theta."""
     b = order * (order + 1) * (order + 2) // 6
+    if mechanisms:
+        nq = 9 + 6 * mechanisms
+        return 4.0 * (4 * b * nq + 4 * 2 * (81 + 9 * 6) + 72 + 9 + 9) + 4 * 4 + 4 + 4
     return 4.0 * (4 * b * 9 + 3 * 24 + 4 * 81 + 4 * 81) + 4 * 4 + 4 + 4
 
 
@@ -136,6 +144,8 @@ def run_proxy(cfg: ProxyConfig) -> ProxyOutput:
         if dr:
             from .lib import RSParams
             ctx.dr_setup(RSParams.fault_config())
+        if cfg.mechanisms:
+            ctx.visco_setup(100.0, 50.0, 0.5, 100.0)
         dt = ctx.cfl_timestep(0.5)
         for k in cfg.kernels:
             ctx.run(k, dt, 1)  # warm-up
@@ -165,7 +175,10 @@ def run_proxy(cfg: ProxyConfig) -> ProxyOutput:
         for part in launched.get(k, ()):
             if perf.get(part):
                 kbytes += perf[part]["bytes"]
-    if ebytes == 0.0:  # fault kernels: the step model of the elastic update
+    if cfg.mechanisms:  # the per-kernel counts above are the elastic kernels'
+        flop = kbytes = 0.0
+        ebytes = bytes_per_cell(cfg.order, cfg.mechanisms) * len(cfg.kernels)
+    elif ebytes == 0.0:  # fault kernels: the step model of the elastic update
         ebytes = bytes_per_cell(cfg.order) * len(cfg.kernels)
     work = n * cfg.timesteps
     secs = total_ms / 1e3 if total_ms > 0 else wall
@@ -228,10 +241,12 @@ def main(argv=None):
     ap.add_argument("--format", choices=("plain", "json"), default="plain")
     ap.add_argument("--precision", choices=("fp32", "f16x3"), default="fp32",
                     help="f16x3: the tensor-core path (split FP16 x3 contractions, FP32 accumulation)")
+    ap.add_argument("--mechanisms", type=int, choices=(0, 3), default=0,
+                    help="3: viscoelastic equations with three relaxation mechanisms (orders 4 and 5)")
     a = ap.parse_args(argv)
     kernels = tuple(Aux.str_to_kernel(a.kernel))
     out = run_proxy(ProxyConfig(cells=a.cells, timesteps=a.timesteps, kernels=kernels, order=a.order,
-                                precision={"fp32": 0, "f16x3": 1}[a.precision]))
+                                precision={"fp32": 0, "f16x3": 1}[a.precision], mechanisms=a.mechanisms))
     write_output(out, a.kernel, a.format)
     return 0
 
