@@ -249,10 +249,28 @@ sei_vlint_o{order}(int n, float* __restrict__ Q, const float* __restrict__ Iin, 
                    const float* __restrict__ aplus, const float* __restrict__ wplus,
                    const unsigned char* __restrict__ ftype) {{""" + PROLOGUE_ADER)
     a("""  float I[kBp];
-  if (el) sei_load_col<kBp>(Iin + ((size_t)cl * kNQ + q) * kBp, I);
+  // TH [9][kB][16]: theta-weighted sums of the time-integrated memory variables, formed by the
+  // strain tasks from the columns they own: slot j < 3 A_j = sum_l theta_l0 I(l, j), slot j in
+  // 3..5 C_j = sum_l theta_l2 I(l, j), slot 6 + j (j < 3) B_j = sum_l theta_l1 I(l, j)
+  float* TH = X + 9 * kB * 16;
   if (el) {
+    sei_load_col<kBp>(Iin + ((size_t)cl * kNQ + q) * kBp, I);
 #pragma unroll
     for (int k = 0; k < kB; ++k) Xq[k * 16] = I[k];
+  } else {
+    float* ta = TH + jv * kB * 16 + lane;
+    float* tb = TH + (6 + (jv < 3 ? jv : 0)) * kB * 16 + lane;
+#pragma unroll 1
+    for (int m = 0; m < 3; ++m) {
+      const float* th = theta + (size_t)cl * 9 + m * 3;
+      const float ca = __ldg(th + (jv < 3 ? 0 : 2)), cb = __ldg(th + 1);
+      sei_load_col<kBp>(Iin + ((size_t)cl * kNQ + 9 + 6 * m + jv) * kBp, I);
+#pragma unroll
+      for (int k = 0; k < kB; ++k) {
+        ta[k * 16] = m ? fmaf(ca, I[k], ta[k * 16]) : ca * I[k];
+        if (jv < 3) tb[k * 16] = m ? fmaf(cb, I[k], tb[k * 16]) : cb * I[k];
+      }
+    }
   }
   __syncthreads();
   float acc[kBp];
@@ -268,21 +286,18 @@ sei_vlint_o{order}(int n, float* __restrict__ Q, const float* __restrict__ Iin, 
 #pragma unroll
     for (int k = 0; k < kBp; ++k) acc[k] = -acc[k];
   }
-  // ---- source term of the stresses: theta-weighted time-integrated memory variables
-  if (el && q < 6) {
-#pragma unroll 1
-    for (int m = 0; m < 3; ++m) {
-      const float* th = theta + (size_t)cl * 9 + m * 3;
-      const int lo = q < 3 ? 0 : q, hi = q < 3 ? 3 : q + 1;
-#pragma unroll 1
-      for (int jj = lo; jj < hi; ++jj) {
-        const float c = q < 3 ? __ldg(th + (jj == q ? 0 : 1)) : __ldg(th + 2);
-        float t[kBp];
-        sei_load_col<kBp>(Iin + ((size_t)cl * kNQ + 9 + 6 * m + jj) * kBp, t);
+  // ---- source term of the stresses: normal stress q < 3 adds A_q + B_j + B_j' (j, j' != q),
+  // shear stress q in 3..5 adds C_q
+  if (el && q < 3) {
+    const float* a0 = TH + q * kB * 16 + lane;
+    const float* b1 = TH + (6 + (q + 1) % 3) * kB * 16 + lane;
+    const float* b2 = TH + (6 + (q + 2) % 3) * kB * 16 + lane;
 #pragma unroll
-        for (int k = 0; k < kB; ++k) acc[k] = fmaf(c, t[k], acc[k]);
-      }
-    }
+    for (int k = 0; k < kB; ++k) acc[k] += a0[k * 16] + b1[k * 16] + b2[k * 16];
+  } else if (el && q < 6) {
+    const float* c0 = TH + q * kB * 16 + lane;
+#pragma unroll
+    for (int k = 0; k < kB; ++k) acc[k] += c0[k * 16];
   }
   __syncthreads();""")
     for f in range(4):

@@ -36,8 +36,8 @@ int launchVAder(const sei::ViscoArrays& d, const float* coeffs, void* stream) {
 
 int launchVLint(const sei::ViscoArrays& d, void* stream) {
   if (d.n <= 0) return 0;
-  // 16 cells per CTA, 15 column tasks of 16 threads: the exchange X of 16 cells
-  const size_t smem = sizeof(float) * 9 * KV::kB * KV::kCPBA;
+  // 16 cells per CTA, 15 column tasks of 16 threads: the exchange X and the theta sums TH of 16 cells
+  const size_t smem = sizeof(float) * 18 * KV::kB * KV::kCPBA;
   if (cudaFuncSetAttribute(KV::SEI_VCAT(sei_vlint_o, SEI_VORDER), cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem) != cudaSuccess)
     return -1;
