@@ -92,14 +92,23 @@ PROLOGUE = """
     }"""
 
 
-# The ADER kernel: 16 cells per CTA, thread (column task q < 15, cell lane < 16), 240 threads, so
-# its exchange X [9][B][16] and memory variables M, IM [18][B][16] take 100.8 KB at order 5 and two
-# CTAs share an SM (their stage barriers and compute overlap).
+# The ADER kernel: CPB_ADER cells per CTA, thread (column task q < 15, cell lane < CPB_ADER); at 16
+# cells (240 threads) its exchange X [9][B][16] and memory variables M, IM [18][B][16] take 100.8 KB
+# at order 5 and two CTAs share an SM (their stage barriers and compute overlap).
 CPBA = 16
-PROLOGUE_ADER = PROLOGUE.replace("const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;",
-                                 "const int q = threadIdx.x >> 4, lane = threadIdx.x & 15;") \
-                        .replace("const int cell = blockIdx.x * kCPB + lane;", "const int cell = blockIdx.x * kCPBA + lane;") \
-                        .replace("[9][kB][32]", "[9][kB][16]").replace("kB * 32 + lane", "kB * 16 + lane")
+CPB_ADER = 16  # cells per CTA of the ADER kernel (column tasks of CPB_ADER threads; 8 measured 3 % slower)
+ADER_CTAS = 2  # its CTAs per SM
+
+
+def _prologue(w, const):
+    """PROLOGUE for w cells per CTA (column tasks of w threads); const names w in the kernel."""
+    return PROLOGUE.replace("const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;",
+                            f"const int q = threadIdx.x / {const}, lane = threadIdx.x % {const};") \
+                   .replace("const int cell = blockIdx.x * kCPB + lane;", f"const int cell = blockIdx.x * {const} + lane;") \
+                   .replace("[9][kB][32]", f"[9][kB][{w}]").replace("kB * 32 + lane", f"kB * {const} + lane")
+
+
+PROLOGUE_ADER = _prologue(16, "kCPBA")
 
 
 def _premix_matvec(a, mats, dst, rows, cols, ind, w=32):
@@ -147,7 +156,8 @@ def gen_visco(order: int) -> str:
     a("// Do not edit.")
     a("#pragma once")
     a(f"namespace sei_v{order} {{")
-    a(f"constexpr int kOrder = {order}, kB = {B}, kBp = {padded(B)}, kF = {F}, kNQ = {NQ}, kCPB = {CPB}, kCPBA = {CPBA};")
+    a(f"constexpr int kOrder = {order}, kB = {B}, kBp = {padded(B)}, kF = {F}, kNQ = {NQ}, kCPB = {CPB}, kCPBA = {CPBA}, "
+      f"kWA = {CPB_ADER};")
     a("// Stored derivatives of one cell: [stage][27][kB] (the source term keeps all basis rows).")
     a(f"constexpr int kDerivSize = {order} * {NQ} * {B};")
     _tables(L)
@@ -156,17 +166,17 @@ def gen_visco(order: int) -> str:
     a(f"""
 // Cauchy-Kovalevskaya predictor with the viscoelastic source term: I = sum_i coeffs[i] dQ(i).
 // Q, I [n][27][Bp]; star_nz [n][3][24] (elastic, unrelaxed moduli); grad [n][3][3]; theta [n][3][3];
-// omega: relaxation frequencies.  16 cells per CTA, 240 threads (column task q = tid / 16: 0..8
-// elastic, 9..14 strain; cell lane = tid % 16); shared memory: X [9][B][16], M and IM [18][B][16]
-// (100.8 KB at order 5: two CTAs per SM).
+// omega: relaxation frequencies.  kWA cells per CTA, 15 kWA threads (column task q = tid / kWA:
+// 0..8 elastic, 9..14 strain; cell lane = tid % kWA); shared memory: X [9][B][kWA], M and IM
+// [18][B][kWA] (100.8 KB at order 5 and 16 cells: two CTAs per SM).
 // derivs (nullable): derivative output [slots][kDerivSize]; the slot of a cell is dslot[cell]
 // (-1: not stored), or the cell itself when dslot is nullptr.
-extern "C" __global__ void __launch_bounds__(240, 2)
+extern "C" __global__ void __launch_bounds__({15 * CPB_ADER}, {ADER_CTAS})
 sei_vader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout, const float* __restrict__ star_nz,
                    const float* __restrict__ grad, const float* __restrict__ theta, SeiOmega omega,
-                   SeiCoeffs coeffs, float* __restrict__ derivs, const int* __restrict__ dslot) {{""" + PROLOGUE_ADER)
-    a("""  float* M = X + 9 * kB * 16;    // memory variables of the current stage [l * 6 + j][kB][16]
-  float* IM = M + 18 * kB * 16;   // their time integral
+                   SeiCoeffs coeffs, float* __restrict__ derivs, const int* __restrict__ dslot) {{""" + _prologue(CPB_ADER, "kWA"))
+    a("""  float* M = X + 9 * kB * kWA;    // memory variables of the current stage [l * 6 + j][kB][kWA]
+  float* IM = M + 18 * kB * kWA;   // their time integral
   float z[kBp];
   float I[kBp];
   const int dsl = derivs ? (dslot ? __ldg(dslot + cl) : cl) : -1;
@@ -176,18 +186,18 @@ sei_vader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout,
 #pragma unroll
     for (int k = 0; k < kBp; ++k) I[k] = coeffs.c[0] * z[k];
 #pragma unroll
-    for (int k = 0; k < kB; ++k) Xq[k * 16] = z[k];
+    for (int k = 0; k < kB; ++k) Xq[k * kWA] = z[k];
     if (dbase) sei_store_col_scalar<kB>(dbase + q * kB, z);
   } else {
 #pragma unroll 1
     for (int m = 0; m < 3; ++m) {
       sei_load_col<kBp>(Q + ((size_t)cl * kNQ + 9 + 6 * m + jv) * kBp, z);
-      float* Mm = M + (m * 6 + jv) * kB * 16 + lane;
-      float* IMm = IM + (m * 6 + jv) * kB * 16 + lane;
+      float* Mm = M + (m * 6 + jv) * kB * kWA + lane;
+      float* IMm = IM + (m * 6 + jv) * kB * kWA + lane;
 #pragma unroll
       for (int k = 0; k < kB; ++k) {
-        Mm[k * 16] = z[k];
-        IMm[k * 16] = coeffs.c[0] * z[k];
+        Mm[k * kWA] = z[k];
+        IMm[k * kWA] = coeffs.c[0] * z[k];
       }
       if (dbase) sei_store_col_scalar<kB>(dbase + (9 + 6 * m + jv) * kB, z);
     }
@@ -198,25 +208,25 @@ sei_vader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout,
         a("    __syncthreads();")
         a("    float zn[kB];")
         a("#pragma unroll\n    for (int k = 0; k < kB; ++k) zn[k] = 0.f;")
-        _premix_matvec(a, G["kDivMT"], "zn", B, B, "    ", w=16)
-        _theta_from_smem(a, "M", "    ", w=16)
+        _premix_matvec(a, G["kDivMT"], "zn", B, B, "    ", w=CPB_ADER)
+        _theta_from_smem(a, "M", "    ", w=CPB_ADER)
         a("    __syncthreads();")
         a("    if (el) {")
         a(f"#pragma unroll\n      for (int k = 0; k < kB; ++k) I[k] = fmaf(coeffs.c[{i}], zn[k], I[k]);")
         if i < order - 1:  # the next stage's exchange (every thread has read X: the barrier above)
-            a("#pragma unroll\n      for (int k = 0; k < kB; ++k) Xq[k * 16] = zn[k];")
+            a("#pragma unroll\n      for (int k = 0; k < kB; ++k) Xq[k * kWA] = zn[k];")
         a(f"      if (dbase) sei_store_col_scalar<kB>(dbase + {i} * kNQ * kB + q * kB, zn);")
         a("    } else {")
         a("#pragma unroll 1")
         a("      for (int m = 0; m < 3; ++m) {")
         a("        const float w = -omega.w[m];")
-        a("        float* Mm = M + (m * 6 + jv) * kB * 16 + lane;")
-        a("        float* IMm = IM + (m * 6 + jv) * kB * 16 + lane;")
+        a("        float* Mm = M + (m * 6 + jv) * kB * kWA + lane;")
+        a("        float* IMm = IM + (m * 6 + jv) * kB * kWA + lane;")
         a("#pragma unroll")
         a("        for (int k = 0; k < kB; ++k) {")
-        a("          const float nw = w * (zn[k] + Mm[k * 16]);")
-        a("          Mm[k * 16] = nw;")
-        a(f"          IMm[k * 16] = fmaf(coeffs.c[{i}], nw, IMm[k * 16]);")
+        a("          const float nw = w * (zn[k] + Mm[k * kWA]);")
+        a("          Mm[k * kWA] = nw;")
+        a(f"          IMm[k * kWA] = fmaf(coeffs.c[{i}], nw, IMm[k * kWA]);")
         a(f"          if (dbase) dbase[{i} * kNQ * kB + (9 + 6 * m + jv) * kB + k] = nw;")
         a("        }")
         a("      }")
@@ -228,9 +238,9 @@ sei_vader_o{order}(int n, const float* __restrict__ Q, float* __restrict__ Iout,
     } else {
 #pragma unroll 1
       for (int m = 0; m < 3; ++m) {
-        const float* IMm = IM + (m * 6 + jv) * kB * 16 + lane;
+        const float* IMm = IM + (m * 6 + jv) * kB * kWA + lane;
 #pragma unroll
-        for (int k = 0; k < kB; ++k) z[k] = IMm[k * 16];
+        for (int k = 0; k < kB; ++k) z[k] = IMm[k * kWA];
 #pragma unroll
         for (int k = kB; k < kBp; ++k) z[k] = 0.f;
         sei_store_col<kBp>(Iout + ((size_t)cell * kNQ + 9 + 6 * m + jv) * kBp, z);

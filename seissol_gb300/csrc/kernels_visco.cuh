@@ -21,15 +21,15 @@ SeiOmega toOmega(const sei::ViscoArrays& d) {
 
 int launchVAder(const sei::ViscoArrays& d, const float* coeffs, void* stream) {
   if (d.n <= 0) return 0;
-  // 16 cells per CTA, 15 column tasks of 16 threads: X, M and IM of 16 cells
-  const size_t smem = sizeof(float) * (9 + 36) * KV::kB * KV::kCPBA;
+  // kWA cells per CTA, 15 column tasks of kWA threads: X, M and IM of kWA cells
+  const size_t smem = sizeof(float) * (9 + 36) * KV::kB * KV::kWA;
   if (cudaFuncSetAttribute(KV::SEI_VCAT(sei_vader_o, SEI_VORDER), cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem) != cudaSuccess)
     return -1;
   SeiCoeffs c{};
   for (int i = 0; i < KV::kOrder; ++i) c.c[i] = coeffs[i];
-  const int blocks = (d.n + KV::kCPBA - 1) / KV::kCPBA;
-  KV::SEI_VCAT(sei_vader_o, SEI_VORDER)<<<blocks, 15 * KV::kCPBA, smem, (cudaStream_t)stream>>>(
+  const int blocks = (d.n + KV::kWA - 1) / KV::kWA;
+  KV::SEI_VCAT(sei_vader_o, SEI_VORDER)<<<blocks, 15 * KV::kWA, smem, (cudaStream_t)stream>>>(
       d.n, d.Q, d.I, d.star_nz, d.grad, d.theta, toOmega(d), c, d.derivs, d.dslot);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
