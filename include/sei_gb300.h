@@ -443,6 +443,32 @@ int sei_receivers_columns(const sei_ctx* ctx);
  * context-free, host only; dphi may be NULL.  Orders 1 to 8. */
 int sei_basis_functions(int order, const double* xez /*[3]*/, double* phi, double* dphi);
 int sei_receivers_read(sei_ctx* ctx, double* out, int64_t max_samples, int64_t* nsamples);
+
+/* Off-fault plasticity (Drucker-Prager, viscoplastic relaxation), applied to every cell after its
+ * neighbour integral in each full step (kernels all and all_dr, sei_run_host, every LTS cluster
+ * step with the cluster's dt), as TimeCluster::computeNeighboringIntegration does
+ * (src/Solver/TimeStepping/TimeCluster.cpp:966-975).  Replaces Plasticity::computePlasticity /
+ * computePlasticityBatched (src/Kernels/Plasticity.cpp:47-238) and the PlasticityData set-up
+ * (src/Model/Plasticity.h:28-59).
+ * nodes: the B nodes [B][3] of the nodal basis on the reference tetrahedron (the vNodes of the
+ * reference's plasticity-nb-matrices-<order>.json); V and its inverse are formed from the basis
+ * functions at them.  NULL: the equispaced lattice of sei_plasticity_nodes (not the reference's
+ * node set: results then differ from the reference's).  tv: relaxation time T_v > 0.
+ * per_node 0: bulk_friction [n], plast_co [n] (cohesion), s0 [n][6] (initial stress xx, yy, zz, xy,
+ * yz, xz) per cell; per_node 1: [n][B], [n][B], [n][B][6] per node.  The material's mu gives
+ * 1 / (2 mu).  Elastic equations, orders 4-6; a new set-up resets the plastic strain.
+ * sei_plasticity_get_strain: [n][7][B] nodal plastic strain (xx, yy, zz, xy, yz, xz) and eta.
+ * sei_plasticity_yield_count: cell updates with yielding since the set-up (the reference's
+ * numberOfTetsWithPlasticYielding summed over steps). */
+int sei_plasticity_setup(sei_ctx* ctx, const double* nodes, double tv, const double* bulk_friction,
+                         const double* plast_co, const double* s0, int per_node);
+int sei_plasticity_disable(sei_ctx* ctx);
+int sei_plasticity_get_strain(sei_ctx* ctx, float* out);
+int sei_plasticity_yield_count(sei_ctx* ctx, int64_t* count);
+/* 1 - exp(-dt / tv), or 1 for tv <= 0 (Plasticity::computeRelaxTime, src/Kernels/Plasticity.h:27-29). */
+double sei_plasticity_relax_factor(double tv, double dt);
+/* The equispaced lattice of degree order - 1: B nodes [B][3] (i, j, k) / (order - 1), i fastest. */
+int sei_plasticity_nodes(int order, double* nodes);
 /* Simulation time: the start of the next full step; advanced by dt per full step (by the cycle
  * length per LTS cycle).  sei_set_time restarts the receivers' sampling at t (unread samples are
  * dropped). */

@@ -389,7 +389,7 @@ def _dr_cluster_step(o, dr, Q, derivs, fsel, dt, time=0.0):
     return dro.nodal_flux(Q, mc, ms, rel, ism, sub["fluxSolverMinus"])
 
 
-def lts_cycles(o, Q, cells, cluster, dt0, ncycles, dr=None, on_predict=None):
+def lts_cycles(o, Q, cells, cluster, dt0, ncycles, dr=None, on_predict=None, on_correct=None):
     """Rate-2 LTS (TimeCluster.cpp:358-440, 695-717; TimeCommon.cpp:40-87) in FP64.
 
     dr (optional): {"faces", "params", "state", "a", "init"[, "aux"]} of a fault whose faces join
@@ -397,7 +397,9 @@ def lts_cycles(o, Q, cells, cluster, dt0, ncycles, dr=None, on_predict=None):
     time step before the neighbour flux (TimeCluster.cpp:804-823); dr["state"] is updated in
     place, and dr["aux"] (fault time at the cycle start, nucleation, outputs, slip-weakening
     fields) too, its time advancing by the cycle length.  on_predict(cluster, step start offset in
-    the run, its time step, Q) is called before each cluster's predictor (receivers).
+    the run, its time step, Q) is called before each cluster's predictor (receivers);
+    on_correct(cells of the cluster, its time step, Q) after each cluster's neighbour flux
+    (plasticity, TimeCluster.cpp:966-975), and may change Q in place.
 
     Every cycle advances all clusters by dt0 2^(C-1).  At sub-step k of the finest cluster the
     clusters whose step starts there predict (ADER with derivatives, integration buffer of cells
@@ -468,6 +470,8 @@ def lts_cycles(o, Q, cells, cluster, dt0, ncycles, dr=None, on_predict=None):
                         t = dr["aux"].get("time", 0.0) + (k + 1 - ln) * dt0 if dr.get("aux") is not None else 0.0
                         Q = _dr_cluster_step(o, dr, Q, derivs, fsel, dt0 * ln, t)
                 Q[idx] = o.neighbor(Q[idx], pool, aminus[idx], pidx, side[idx], orient[idx], ft[idx])
+                if on_correct is not None:
+                    on_correct(idx, ln * dt0, Q)
         if dr is not None and dr.get("aux") is not None:
             dr["aux"]["time"] = dr["aux"].get("time", 0.0) + steps * dt0
     return Q

@@ -9,6 +9,8 @@ from .lib import (  # noqa: F401
     tc_gemm_check,
     mlp_gradient,
     fit_attenuation,
+    plasticity_nodes,
+    plasticity_relax_factor,
     mlp_predict,
     mlp_num_params,
     Context,

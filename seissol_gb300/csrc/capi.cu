@@ -113,6 +113,13 @@ struct sei_ctx {
   int64_t fault_steps = 0;
   std::vector<int> fault_fields;
   sei::Stager fault_stage;
+  // off-fault plasticity (sei_plasticity_setup): per-cell parameters at the nodes, current cell order
+  bool plast = false;
+  double plast_tv = 0.0;
+  float* d_plmats = nullptr;  // V, Vinv [2][B][Bp]
+  float *d_pls0 = nullptr, *d_plccos = nullptr, *d_plssin = nullptr, *d_plmu = nullptr, *d_pstrain = nullptr;
+  unsigned long long* d_plyield = nullptr;
+  std::vector<float> pl_s0, pl_ccos, pl_ssin;  // host copies [n][6][B], [n][B], [n][B]
   int tune_fail_at = -1;     // SEI_OPT_TUNE_FAIL_AT: candidate the autotuner fails on the host (tests)
   float* d_rec = nullptr;  // recorded training samples [rec_cap][6]
   unsigned* d_rec_count = nullptr;
@@ -217,6 +224,21 @@ void freeFault(sei_ctx* c) {
   c->fault_stage.release();
 }
 
+void freePlasticity(sei_ctx* c) {
+  for (void* p : {(void*)c->d_plmats, (void*)c->d_pls0, (void*)c->d_plccos, (void*)c->d_plssin, (void*)c->d_plmu,
+                  (void*)c->d_pstrain, (void*)c->d_plyield})
+    cudaFree(p);
+  c->d_plmats = c->d_pls0 = c->d_plccos = c->d_plssin = c->d_plmu = c->d_pstrain = nullptr;
+  c->d_plyield = nullptr;
+  c->pl_s0.clear();
+  c->pl_ccos.clear();
+  c->pl_ssin.clear();
+  c->plast = false;
+  // a recorded LTS cycle holds the plasticity launches (or lacks them): record it again
+  if (c->lts_exec) cudaGraphExecDestroy(c->lts_exec);
+  c->lts_exec = nullptr;
+}
+
 void freeOutput(sei_ctx* c) {
   for (void* p : {(void*)c->d_recv_ucell, (void*)c->d_recv_slot, (void*)c->d_recv_q, (void*)c->d_recv_i,
                   (void*)c->d_recv_star, (void*)c->d_recv_derivs, (void*)c->d_recv_phi, (void*)c->d_recv_dphi,
@@ -238,6 +260,7 @@ void freeOutput(sei_ctx* c) {
 
 void freeArrays(sei_ctx* c) {
   freeOutput(c);
+  freePlasticity(c);
   cudaFree(c->Q);
   cudaFree(c->I);
   cudaFree(c->derivs);
@@ -728,6 +751,31 @@ int recordFault(sei_ctx* c) {
   return SEI_OK;
 }
 
+// Plasticity of cells [s, e) after their neighbour integral over a step of dt
+// (TimeCluster.cpp:966-975, Plasticity::computeRelaxTime).
+int launchPlast(sei_ctx* c, int64_t s, int64_t e, double dt) {
+  if (!c->plast || e <= s) return SEI_OK;
+  int rc = profMark(c, 4);  // not one of the four reported kinds
+  if (rc) return rc;
+  sei::PlasticityArgs a{};
+  a.Q = c->Q;
+  a.mats = c->d_plmats;
+  a.s0 = c->d_pls0;
+  a.ccos = c->d_plccos;
+  a.ssin = c->d_plssin;
+  a.mufac = c->d_plmu;
+  a.pstrain = c->d_pstrain;
+  a.yield = c->d_plyield;
+  a.begin = s;
+  a.end = e;
+  const double r = sei_plasticity_relax_factor(c->plast_tv, dt);
+  a.relax = (float)r;
+  a.inv_tvr = (float)(1.0 / (c->plast_tv * r));
+  a.dt = (float)dt;
+  if (sei::launchPlasticity(c->cfg.order, a, c->stream) != 0) return fail(c, SEI_ERR_CUDA, "plasticity launch failed");
+  return SEI_OK;
+}
+
 int runKernel(sei_ctx* c, int kernel, double dt, int steps, const double* given = nullptr) {
   if (c->visco) return runVisco(c, kernel, dt, steps, given);
   float coeffs[8];
@@ -747,6 +795,7 @@ int runKernel(sei_ctx* c, int kernel, double dt, int steps, const double* given 
       case SEI_KERNEL_ALL:
         rc = launchLocal(c, d, coeffs, fusedFlux(c));
         if (!rc) rc = launchNeighbor(c, d, fusedFlux(c));
+        if (!rc) rc = launchPlast(c, 0, c->n, dt);
         break;
       case SEI_KERNEL_LOCAL:
         rc = launchLocal(c, d, coeffs);
@@ -768,6 +817,7 @@ int runKernel(sei_ctx* c, int kernel, double dt, int steps, const double* given 
         rc = launchLocal(c, d, coeffs, fusedFlux(c));
         if (!rc) rc = launchDr(c, dt);
         if (!rc) rc = launchNeighbor(c, d, fusedFlux(c));
+        if (!rc) rc = launchPlast(c, 0, c->n, dt);
         break;
       default:
         return fail(c, SEI_ERR_UNSUPPORTED, "kernel not supported by this build");
@@ -1183,12 +1233,13 @@ static int runHostPipelined(sei_ctx* c, double dt, int nsteps, const float* in, 
   c->trace_valid = c->cfg.precision == SEI_PREC_F16X3 && c->d_trace;
   if (nsteps > 1) {
     const sei::DeviceArrays all = arrays(c);
-    if ((rc = launchNeighbor(c, all, fusedFlux(c)))) return rc;
+    if ((rc = launchNeighbor(c, all, fusedFlux(c))) || (rc = launchPlast(c, 0, c->n, dt))) return rc;
     if (nsteps > 2 && (rc = runKernel(c, SEI_KERNEL_ALL, dt, nsteps - 2))) return rc;
     if ((rc = launchLocal(c, all, co, fusedFlux(c)))) return rc;
   }
   for (int k = 0; k < nch && !rc; ++k) {
     rc = launchNeighbor(c, gtsRange(c, b[k], b[k + 1], true), fusedFlux(c));
+    if (!rc) rc = launchPlast(c, b[k], b[k + 1], dt);
     if (rc) return rc;
     SEI_CUDA(cudaEventRecord(ev[kChunks + k], c->stream));
     SEI_CUDA(cudaStreamWaitEvent(c->copy_stream, ev[kChunks + k], 0));
@@ -1387,6 +1438,158 @@ int sei_receivers_setup(sei_ctx* c, int64_t n, const double* xyz, double interva
   c->recv_times.assign(1, c->sim_time);
   c->recv_emit = 0;
   if (cells) std::copy(cell.begin(), cell.end(), cells);
+  return SEI_OK;
+}
+
+double sei_plasticity_relax_factor(double tv, double dt) { return tv > 0.0 ? -std::expm1(-dt / tv) : 1.0; }
+
+int sei_plasticity_nodes(int order, double* nodes) {
+  if (order < 2 || order > 8 || !nodes) return SEI_ERR_ARG;
+  sei::latticeNodes(order, nodes);
+  return SEI_OK;
+}
+
+namespace {
+int uploadF(sei_ctx* c, float** dst, const std::vector<float>& src) {
+  cudaFree(*dst);
+  *dst = nullptr;
+  if (src.empty()) return SEI_OK;
+  if (cudaMalloc(dst, src.size() * sizeof(float)) != cudaSuccess) return fail(c, SEI_ERR_OOM, "plasticity allocation");
+  SEI_CUDA(cudaMemcpy(*dst, src.data(), src.size() * sizeof(float), cudaMemcpyHostToDevice));
+  return SEI_OK;
+}
+
+// Device copies of the plasticity parameters in the current cell order, 1 / (2 mu) from the
+// mesh's materials, and a zero plastic strain when reset.
+int plastUpload(sei_ctx* c, bool resetStrain) {
+  const int64_t n = c->n;
+  const int B = sei::numBasis(c->cfg.order);
+  std::vector<float> mu((size_t)n);
+  for (int64_t i = 0; i < n; ++i) mu[i] = (float)(1.0 / (2.0 * c->mesh.material[(size_t)i * 3 + 1]));
+  int rc;
+  if ((rc = uploadF(c, &c->d_pls0, c->pl_s0)) || (rc = uploadF(c, &c->d_plccos, c->pl_ccos)) ||
+      (rc = uploadF(c, &c->d_plssin, c->pl_ssin)) || (rc = uploadF(c, &c->d_plmu, mu)))
+    return rc;
+  if (resetStrain) {
+    cudaFree(c->d_pstrain);
+    c->d_pstrain = nullptr;
+    if (cudaMalloc(&c->d_pstrain, (size_t)n * 7 * B * sizeof(float)) != cudaSuccess)
+      return fail(c, SEI_ERR_OOM, "plastic strain allocation failed");
+    SEI_CUDA(cudaMemset(c->d_pstrain, 0, (size_t)n * 7 * B * sizeof(float)));
+  }
+  return SEI_OK;
+}
+
+// After sei_lts_setup reordered the cells (new cell i = old cell order[i]).
+int plastPermute(sei_ctx* c, const std::vector<int64_t>& order) {
+  const int64_t n = c->n;
+  const int B = sei::numBasis(c->cfg.order);
+  auto perm = [&](std::vector<float>& a, size_t per) {
+    std::vector<float> b(a.size());
+    for (int64_t i = 0; i < n; ++i)
+      std::copy(a.begin() + order[i] * per, a.begin() + (order[i] + 1) * per, b.begin() + i * per);
+    a.swap(b);
+  };
+  perm(c->pl_s0, (size_t)6 * B);
+  perm(c->pl_ccos, B);
+  perm(c->pl_ssin, B);
+  std::vector<float> ps((size_t)n * 7 * B);
+  SEI_CUDA(cudaStreamSynchronize(c->stream));
+  SEI_CUDA(cudaMemcpy(ps.data(), c->d_pstrain, ps.size() * sizeof(float), cudaMemcpyDeviceToHost));
+  perm(ps, (size_t)7 * B);
+  SEI_CUDA(cudaMemcpy(c->d_pstrain, ps.data(), ps.size() * sizeof(float), cudaMemcpyHostToDevice));
+  return plastUpload(c, false);
+}
+}  // namespace
+
+int sei_plasticity_setup(sei_ctx* c, const double* nodes, double tv, const double* bulk_friction,
+                         const double* plast_co, const double* s0, int per_node) {
+  int rc = checkReady(c);
+  if (rc) return rc;
+  if (c->visco) return fail(c, SEI_ERR_UNSUPPORTED, "plasticity with the viscoelastic equations is not supported");
+  const int order = c->cfg.order;
+  if (order < 4 || order > 6) return fail(c, SEI_ERR_UNSUPPORTED, "plasticity kernels exist for orders 4-6");
+  if (!bulk_friction || !plast_co || !s0) return fail(c, SEI_ERR_ARG, "null plasticity parameters");
+  if (!(tv > 0.0) || !std::isfinite(tv))
+    return fail(c, SEI_ERR_ARG, "relaxation time T_v must be positive (the plastic strain rate divides by it)");
+  if (per_node != 0 && per_node != 1) return fail(c, SEI_ERR_ARG, "per_node must be 0 or 1");
+  const int B = sei::numBasis(order), Bp = c->Bp;
+  std::vector<double> nd((size_t)3 * B);
+  if (nodes)
+    std::copy(nodes, nodes + 3 * B, nd.begin());
+  else
+    sei::latticeNodes(order, nd.data());
+  for (double x : nd)
+    if (!std::isfinite(x)) return fail(c, SEI_ERR_ARG, "non-finite plasticity node");
+  std::vector<double> v, vi;
+  if (!sei::plasticityMatrices(order, nd.data(), v, vi))
+    return fail(c, SEI_ERR_ARG, "the plasticity nodes are not unisolvent for the basis");
+  const int64_t n = c->n;
+  std::vector<float> ps0((size_t)n * 6 * B), pcos((size_t)n * B), psin((size_t)n * B);
+  for (int64_t i = 0; i < n; ++i)
+    for (int j = 0; j < B; ++j) {
+      const size_t p = per_node ? (size_t)i * B + j : (size_t)i;
+      const double phi = std::atan(bulk_friction[p]), co = plast_co[p];
+      if (!std::isfinite(phi) || !std::isfinite(co)) return fail(c, SEI_ERR_ARG, "non-finite plasticity parameter");
+      pcos[(size_t)i * B + j] = (float)(co * std::cos(phi));
+      psin[(size_t)i * B + j] = (float)std::sin(phi);
+      for (int x = 0; x < 6; ++x) {
+        const double sv = s0[p * 6 + x];
+        if (!std::isfinite(sv)) return fail(c, SEI_ERR_ARG, "non-finite initial stress");
+        ps0[((size_t)i * 6 + x) * B + j] = (float)sv;
+      }
+    }
+  std::vector<float> mats((size_t)2 * B * Bp, 0.f);
+  for (int a = 0; a < B; ++a)
+    for (int b = 0; b < B; ++b) {
+      mats[(size_t)a * Bp + b] = (float)v[(size_t)a * B + b];            // V[node][basis]
+      mats[(size_t)(B + a) * Bp + b] = (float)vi[(size_t)a * B + b];     // Vinv[basis][node]
+    }
+  freePlasticity(c);
+  c->pl_s0.swap(ps0);
+  c->pl_ccos.swap(pcos);
+  c->pl_ssin.swap(psin);
+  c->plast_tv = tv;
+  if ((rc = uploadF(c, &c->d_plmats, mats)) || (rc = plastUpload(c, true))) {
+    freePlasticity(c);
+    return rc;
+  }
+  if (cudaMalloc(&c->d_plyield, sizeof(unsigned long long)) != cudaSuccess) {
+    freePlasticity(c);
+    return fail(c, SEI_ERR_OOM, "plasticity counter allocation failed");
+  }
+  SEI_CUDA(cudaMemset(c->d_plyield, 0, sizeof(unsigned long long)));
+  c->plast = true;
+  return SEI_OK;
+}
+
+int sei_plasticity_disable(sei_ctx* c) {
+  if (!c) return SEI_ERR_ARG;
+  if (c->n > 0) cudaStreamSynchronize(c->stream);
+  freePlasticity(c);
+  return SEI_OK;
+}
+
+int sei_plasticity_get_strain(sei_ctx* c, float* out) {
+  int rc = checkReady(c);
+  if (rc) return rc;
+  if (!out) return fail(c, SEI_ERR_ARG, "null output");
+  if (!c->plast) return fail(c, SEI_ERR_STATE, "plasticity not set up (sei_plasticity_setup)");
+  SEI_CUDA(cudaStreamSynchronize(c->stream));
+  SEI_CUDA(cudaMemcpy(out, c->d_pstrain, (size_t)c->n * 7 * sei::numBasis(c->cfg.order) * sizeof(float),
+                      cudaMemcpyDeviceToHost));
+  return SEI_OK;
+}
+
+int sei_plasticity_yield_count(sei_ctx* c, int64_t* count) {
+  int rc = checkReady(c);
+  if (rc) return rc;
+  if (!count) return fail(c, SEI_ERR_ARG, "null output");
+  if (!c->plast) return fail(c, SEI_ERR_STATE, "plasticity not set up (sei_plasticity_setup)");
+  unsigned long long v = 0;
+  SEI_CUDA(cudaStreamSynchronize(c->stream));
+  SEI_CUDA(cudaMemcpy(&v, c->d_plyield, sizeof(v), cudaMemcpyDeviceToHost));
+  *count = (int64_t)v;
   return SEI_OK;
 }
 
@@ -2179,8 +2382,9 @@ int sei_visco_setup(sei_ctx* c, double qp, double qs, double freq_central, doubl
   int rc = host ? SEI_OK : checkReady(c);
   if (rc) return rc;
   if (!c->has_mesh) return fail(c, SEI_ERR_STATE, "the viscoelastic set-up needs a mesh built by the context");
-  if (c->has_fault || c->lts || c->visco)
-    return fail(c, SEI_ERR_UNSUPPORTED, "viscoelastic set-up: not built with a fault or local time stepping, or twice");
+  if (c->has_fault || c->lts || c->visco || c->plast)
+    return fail(c, SEI_ERR_UNSUPPORTED,
+                "viscoelastic set-up: not built with a fault, local time stepping or plasticity, or twice");
   if (c->cfg.precision != SEI_PREC_FP32) return fail(c, SEI_ERR_UNSUPPORTED, "viscoelastic kernels are FP32 only");
   sei::ViscoKernels vk{};
   if (!sei::viscoKernelsForOrder(c->cfg.order, vk))
@@ -2466,6 +2670,7 @@ int sei_lts_setup(sei_ctx* c, double cfl, int max_clusters, int* nclusters) {
   c->g_start = gst;
   c->lts_perm = order;
   if (nclusters) *nclusters = ncl;
+  if (c->plast && (rc = plastPermute(c, order))) return rc;
   if (c->nrecv > 0) {
     // the cells moved: locate the receivers again on the reordered mesh (their clocks restart)
     const std::vector<double> pts = c->recv_xyz;
@@ -2620,6 +2825,7 @@ int ltsCycle(sei_ctx* c) {
         continue;
       }
       int rc = launchNeighbor(c, rangeView(c, s, e, true, parity), fusedFlux(c));
+      if (!rc) rc = launchPlast(c, s, e, c->lts_dt0 * (double)len);
       if (rc) return rc;
     }
   }

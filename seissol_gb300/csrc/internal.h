@@ -293,3 +293,28 @@ int launchMlpGrad(const float* P, const float* norm, const float* X, const float
 int launchMlpAdam(float* P, const float* grads, float* m, float* v, float lr, int step, void* stream);
 int launchMlpPredict(const float* P, const float* norm, const float* X, int n, float* out, void* stream);
 }  // namespace sei
+
+namespace sei {
+// Off-fault plasticity (plasticity.cu): the nodal Drucker-Prager check and viscoplastic return map
+// of Plasticity.cpp:47-214 on cells [begin, end) after their neighbour integral.
+struct PlasticityArgs {
+  float* Q;                   // DOFs [cells][9][Bp] (stresses: quantities 0..5)
+  const float* mats;          // V [B][Bp] (basis values at the nodes) then Vinv [B][Bp]
+  const float* s0;            // initial loading [cells][6][B]
+  const float* ccos;          // cohesion cos(phi) [cells][B]
+  const float* ssin;          // sin(phi) [cells][B]
+  const float* mufac;         // 1 / (2 mu) [cells]
+  float* pstrain;             // plastic strain [cells][7][B] (six components, then eta)
+  unsigned long long* yield;  // cells with yielding, accumulated
+  int64_t begin, end;
+  float relax;     // r = 1 - exp(-dt / T_v)
+  float inv_tvr;   // 1 / (T_v r)
+  float dt;
+};
+int launchPlasticity(int order, const PlasticityArgs& a, void* stream);
+// V [B][B] (phi_k at node n) and its inverse, float64, from reference-element nodes [B][3];
+// false when the nodes are not unisolvent.
+bool plasticityMatrices(int order, const double* nodes, std::vector<double>& v, std::vector<double>& vinv);
+// The equispaced lattice of degree order - 1 on the reference tetrahedron: B nodes [B][3].
+void latticeNodes(int order, double* nodes);
+}  // namespace sei

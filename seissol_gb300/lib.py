@@ -179,6 +179,12 @@ def load_library(path: str | None = None):
     _sig(lib, "sei_receivers_columns", i, [VP])
     _sig(lib, "sei_basis_functions", i, [i, VP, VP, VP])
     _sig(lib, "sei_receivers_read", i, [VP, VP, i64, C.POINTER(i64)])
+    _sig(lib, "sei_plasticity_setup", i, [VP, VP, d, VP, VP, VP, i])
+    _sig(lib, "sei_plasticity_disable", i, [VP])
+    _sig(lib, "sei_plasticity_get_strain", i, [VP, VP])
+    _sig(lib, "sei_plasticity_yield_count", i, [VP, C.POINTER(i64)])
+    _sig(lib, "sei_plasticity_relax_factor", d, [d, d])
+    _sig(lib, "sei_plasticity_nodes", i, [i, VP])
     _sig(lib, "sei_get_time", i, [VP, C.POINTER(C.c_double)])
     _sig(lib, "sei_set_time", i, [VP, C.c_double])
     _sig(lib, "sei_fault_output_setup", i, [VP, i, VP, i])
@@ -288,6 +294,20 @@ def fit_attenuation(mu, lam, qp, qs, freq_central, freq_ratio):
     if rc != SEI_OK:
         raise SeiError(rc, "sei_fit_attenuation")
     return m.value, l.value, om, th.reshape(3, 3)
+
+
+def plasticity_relax_factor(tv, dt):
+    """1 - exp(-dt / tv), 1 for tv <= 0 (sei_plasticity_relax_factor)."""
+    return load_library().sei_plasticity_relax_factor(float(tv), float(dt))
+
+
+def plasticity_nodes(order):
+    """The library's default plasticity nodes [B][3] (equispaced lattice, sei_plasticity_nodes)."""
+    out = np.empty((nbasis(order), 3), np.float64)
+    rc = load_library().sei_plasticity_nodes(int(order), _ptr(out))
+    if rc != SEI_OK:
+        raise SeiError(rc, "sei_plasticity_nodes")
+    return out
 
 
 def mlp_num_params():
@@ -428,6 +448,35 @@ class Context:
 
     def set_time(self, t):
         self._check(self.lib.sei_set_time(self.h, float(t)), "sei_set_time")
+
+    def plasticity_setup(self, bulk_friction, plast_co, s0, tv=0.1, nodes=None, per_node=False):
+        """Off-fault plasticity (sei_plasticity_setup).  Per cell: bulk_friction [n], plast_co [n],
+        s0 [n, 6]; per_node: [n, B], [n, B], [n, B, 6].  nodes [B, 3] (None: the equispaced lattice)."""
+        bf = np.ascontiguousarray(bulk_friction, np.float64)
+        co = np.ascontiguousarray(plast_co, np.float64)
+        s0 = np.ascontiguousarray(s0, np.float64)
+        nd = None if nodes is None else np.ascontiguousarray(nodes, np.float64).reshape(-1, 3)
+        want = (self.n, self.B) if per_node else (self.n,)
+        if bf.shape != want or co.shape != want or s0.shape != want + (6,):
+            raise ValueError(f"plasticity parameters must be {want} and {want + (6,)}")
+        if nd is not None and nd.shape != (self.B, 3):
+            raise ValueError(f"nodes must be [{self.B}, 3]")
+        self._check(self.lib.sei_plasticity_setup(self.h, _ptr(nd) if nd is not None else None, float(tv), _ptr(bf),
+                                                  _ptr(co), _ptr(s0), int(bool(per_node))), "sei_plasticity_setup")
+
+    def plasticity_disable(self):
+        self._check(self.lib.sei_plasticity_disable(self.h), "sei_plasticity_disable")
+
+    def plasticity_strain(self):
+        """Nodal plastic strain [n, 7, B]: xx, yy, zz, xy, yz, xz, then eta."""
+        out = np.empty((self.n, 7, self.B), np.float32)
+        self._check(self.lib.sei_plasticity_get_strain(self.h, _ptr(out)), "sei_plasticity_get_strain")
+        return out
+
+    def plasticity_yield_count(self):
+        v = C.c_int64()
+        self._check(self.lib.sei_plasticity_yield_count(self.h, C.byref(v)), "sei_plasticity_yield_count")
+        return v.value
 
     def fault_output_setup(self, every, fields):
         ids = np.ascontiguousarray([DR_FIELDS[f] if isinstance(f, str) else int(f) for f in fields], np.int32)

@@ -11,6 +11,8 @@ compiled or imported.  Outputs:
 * ``dr_matrices_pin.json`` -- for ``codegen/matrices/dr_stroud_matrices_{4,5,6}.json``: the
   quadrature points and weights in full and the same summary as below for V3mTo2n,
   V3mTo2nTWDivM and resample.
+* ``plasticity_nb_pin.json`` -- for ``codegen/matrices/plasticity-nb-matrices-{4,5,6}.json``:
+  the nodes (vNodes) in full and the same summary as above for v and vInv.
 * ``global_matrices_pin.json`` -- for every matrix of
   ``codegen/matrices/matrices_{20,35,56}.xml``: shape, non-zero count, sum,
   Frobenius norm and a deterministic sample of entries.
@@ -100,6 +102,26 @@ def parse_dr_json(path):
     return res
 
 
+def parse_plasticity_json(path):
+    res = {}
+    for m in json.load(open(path)):
+        if m["name"] not in ("vNodes", "v", "vInv"):
+            continue
+        shape = [int(x) for x in m["shape"]]
+        ent = sorted((int(e[0]) - 1, int(e[1]) - 1, float(e[2])) for e in m["entries"])
+        if m["name"] == "vNodes":
+            full = [[0.0] * shape[1] for _ in range(shape[0])]
+            for r, c, v in ent:
+                full[r][c] = v
+            res["nodes"] = full
+            continue
+        nz = [e for e in ent if e[2] != 0.0]
+        step = max(1, len(nz) // 40)
+        res[m["name"]] = {"shape": shape, "nnz": len(nz), "sum": sum(e[2] for e in nz),
+                          "fro": sum(e[2] ** 2 for e in nz) ** 0.5, "sample": [[r, c, v] for (r, c, v) in nz[::step]]}
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("SEI_REFERENCE_ROOT"),
@@ -118,6 +140,9 @@ def main():
     dr = {str(o): parse_dr_json(os.path.join(a.reference, f"codegen/matrices/dr_stroud_matrices_{o}.json"))
           for o in (4, 5, 6)}
     json.dump(dr, open(os.path.join(HERE, "dr_matrices_pin.json"), "w"))
+    pl = {str(o): parse_plasticity_json(os.path.join(a.reference, f"codegen/matrices/plasticity-nb-matrices-{o}.json"))
+          for o in (4, 5, 6)}
+    json.dump(pl, open(os.path.join(HERE, "plasticity_nb_pin.json"), "w"))
 
 
 if __name__ == "__main__":
