@@ -418,6 +418,53 @@ def output_measurement(local, steps, nrecv=1000):
             "read_ms": read_ms, "read_bytes": int(samples.nbytes)}
 
 
+def plasticity_measurement(local, steps):
+    """Off-fault plasticity on the headline workload (elastic order 6, 400,000 tets, mixed path,
+    kernel all): `steps` steps timed without and with plasticity on every cell (bulk friction
+    0.6, c cos(phi) ~ U[0.7, 1.5] x 87 MPa, initial stress U[-1, 1] MPa, T_v 0.05 s, the default
+    lattice nodes); the difference is the plasticity kernel's time, against its algorithmic bytes
+    (stresses, initial loading, cohesion and friction at the nodes read; for yielding cells the
+    stresses written and the plastic strain read and written)."""
+    import numpy as np
+
+    from seissol_gb300 import Context
+
+    hbm, _ = peaks()
+    ctx = Context(ORDER, device=local, precision=PATHS["f16x3"][0])
+    n = ctx.build_periodic_cube(*DIMS, perturb=PERTURB, seed=SEED)
+    dt = ctx.cfl_timestep(0.5)
+    B = ctx.B
+    q0 = ctx.get_dofs()
+
+    def timed():
+        ctx.set_dofs(q0)
+        ctx.run("all", dt, 3)
+        ctx.sync()
+        ctx.run("all", dt, steps)
+        ctx.sync()
+        return ctx.last_run_ms() / steps
+
+    plain = timed()
+    rng = np.random.default_rng(SEED + 7)
+    ctx.plasticity_setup(np.full(n, 0.6), rng.uniform(0.7, 1.5, n) * 8.7e7 / np.cos(np.arctan(0.6)),
+                         rng.uniform(-1e6, 1e6, (n, 6)), tv=0.05)
+    with_pl = timed()
+    yields = ctx.plasticity_yield_count() / (steps + 3)
+    ctx.close()
+    share = yields / n
+    per_cell = 4 * (6 * 56 + 6 * B + 2 * B + 1) + share * 4 * (6 * 56 + 2 * 7 * B)
+    kern_ms = with_pl - plain
+    return {"workload": f"elastic order {ORDER}, {n:,}-tet periodic cube {DIMS[0]}x{DIMS[1]}x{DIMS[2]} cubes, mixed "
+                        f"path, kernel all, {steps} steps after 3 warm-up steps, with and without plasticity on "
+                        "every cell (bulk friction 0.6, c cos(phi) ~ U[0.7, 1.5] x 87 MPa, T_v 0.05 s, default "
+                        "lattice nodes)",
+            "steps": steps, "ms_per_step_without": plain, "ms_per_step_with": with_pl,
+            "plasticity_ms_per_step": kern_ms, "yielding_cell_share": share,
+            "algorithmic_bytes_per_cell": per_cell,
+            "algorithmic_gbs": per_cell * n / (kern_ms / 1e3) / 1e9 if kern_ms > 0 else None,
+            "frac_of_measured_hbm": per_cell * n / (kern_ms / 1e3) / 1e9 / hbm if kern_ms > 0 else None}
+
+
 def ingest_measurement(local):
     """sei_set_mesh at benchmark size: the 400,000-tet cube of the headline workload given as PUML
     arrays (1.6 M geometric vertices, connectivity, identify-vertex topology, material), ingested
@@ -1050,10 +1097,11 @@ def run_ours(args, world, rank, local):
     cfg1 = None
     if rank == 0 and args.config1_steps > 0:
         cfg1 = config1_measurement(local, args.config1_steps)
-    out = ing = None
+    out = ing = pl = None
     if rank == 0 and args.output_steps > 0:
         out = output_measurement(local, args.output_steps)
         ing = ingest_measurement(local)
+        pl = plasticity_measurement(local, args.output_steps)
 
     base = acc = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -1075,7 +1123,8 @@ def run_ours(args, world, rank, local):
                 "gpu_launches": launches, "kernel_ms_per_step": kernels, "paths": paths_out,
                 "mixed_vs_fp32": ratio, "accuracy": acc, "dynamic_rupture": dr, "combined_o6_fault": comb,
                 "combined_o6_fault_lts": comb_lts, "proxy_o4_10k": cfg1,
-                "local_time_stepping": lts, "viscoelastic": vis, "receiver_output": out, "mesh_ingestion": ing}
+                "local_time_stepping": lts, "viscoelastic": vis, "receiver_output": out, "mesh_ingestion": ing,
+                "plasticity": pl}
         print(json.dumps(line))
     return 0
 
@@ -1099,7 +1148,8 @@ def main():
     ap.add_argument("--config1-steps", type=int, default=100,
                     help="steps of the order-4, 10,000-tet proxy workload against the FP64 oracle; 0 skips it")
     ap.add_argument("--output-steps", type=int, default=50,
-                    help="steps of the receiver-output measurement (then the mesh-ingestion timing); 0 skips both")
+                    help="steps of the receiver-output and plasticity measurements (then the mesh-ingestion "
+                         "timing); 0 skips them")
     ap.add_argument("--combined-steps", type=int, default=10,
                     help="steps of the combined order-6 measurement (1M tets, 50,000-face fault); 0 skips it")
     ap.add_argument("--combined-lts-cycles", type=int, default=3,
