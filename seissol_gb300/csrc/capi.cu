@@ -1459,23 +1459,40 @@ int uploadF(sei_ctx* c, float** dst, const std::vector<float>& src) {
   return SEI_OK;
 }
 
-// Device copies of the plasticity parameters in the current cell order, 1 / (2 mu) from the
-// mesh's materials, and a zero plastic strain when reset.
+// Per-node arrays [n][K][B] <-> the device's tiled layout [n / 32][K][B][32] (cell c in tile
+// c / 32, lane c % 32), in which a warp's 32 cells read one node's values as one 128-byte run.
+std::vector<float> plastTile(const std::vector<float>& a, int64_t n, int K, int B) {
+  const int64_t tiles = (n + 31) / 32;
+  std::vector<float> t((size_t)tiles * K * B * 32, 0.f);
+  for (int64_t i = 0; i < n; ++i)
+    for (int k = 0; k < K * B; ++k) t[((size_t)(i >> 5) * K * B + k) * 32 + (i & 31)] = a[(size_t)i * K * B + k];
+  return t;
+}
+std::vector<float> plastUntile(const std::vector<float>& t, int64_t n, int K, int B) {
+  std::vector<float> a((size_t)n * K * B);
+  for (int64_t i = 0; i < n; ++i)
+    for (int k = 0; k < K * B; ++k) a[(size_t)i * K * B + k] = t[((size_t)(i >> 5) * K * B + k) * 32 + (i & 31)];
+  return a;
+}
+
+// Device copies of the plasticity parameters in the current cell order (tiled), 1 / (2 mu) from
+// the mesh's materials, and a zero plastic strain when reset.
 int plastUpload(sei_ctx* c, bool resetStrain) {
   const int64_t n = c->n;
   const int B = sei::numBasis(c->cfg.order);
   std::vector<float> mu((size_t)n);
   for (int64_t i = 0; i < n; ++i) mu[i] = (float)(1.0 / (2.0 * c->mesh.material[(size_t)i * 3 + 1]));
   int rc;
-  if ((rc = uploadF(c, &c->d_pls0, c->pl_s0)) || (rc = uploadF(c, &c->d_plccos, c->pl_ccos)) ||
-      (rc = uploadF(c, &c->d_plssin, c->pl_ssin)) || (rc = uploadF(c, &c->d_plmu, mu)))
+  if ((rc = uploadF(c, &c->d_pls0, plastTile(c->pl_s0, n, 6, B))) ||
+      (rc = uploadF(c, &c->d_plccos, plastTile(c->pl_ccos, n, 1, B))) ||
+      (rc = uploadF(c, &c->d_plssin, plastTile(c->pl_ssin, n, 1, B))) || (rc = uploadF(c, &c->d_plmu, mu)))
     return rc;
   if (resetStrain) {
+    const size_t bytes = (size_t)((n + 31) / 32) * 32 * 7 * B * sizeof(float);
     cudaFree(c->d_pstrain);
     c->d_pstrain = nullptr;
-    if (cudaMalloc(&c->d_pstrain, (size_t)n * 7 * B * sizeof(float)) != cudaSuccess)
-      return fail(c, SEI_ERR_OOM, "plastic strain allocation failed");
-    SEI_CUDA(cudaMemset(c->d_pstrain, 0, (size_t)n * 7 * B * sizeof(float)));
+    if (cudaMalloc(&c->d_pstrain, bytes) != cudaSuccess) return fail(c, SEI_ERR_OOM, "plastic strain allocation failed");
+    SEI_CUDA(cudaMemset(c->d_pstrain, 0, bytes));
   }
   return SEI_OK;
 }
@@ -1493,11 +1510,13 @@ int plastPermute(sei_ctx* c, const std::vector<int64_t>& order) {
   perm(c->pl_s0, (size_t)6 * B);
   perm(c->pl_ccos, B);
   perm(c->pl_ssin, B);
-  std::vector<float> ps((size_t)n * 7 * B);
+  std::vector<float> pt((size_t)((n + 31) / 32) * 32 * 7 * B);
   SEI_CUDA(cudaStreamSynchronize(c->stream));
-  SEI_CUDA(cudaMemcpy(ps.data(), c->d_pstrain, ps.size() * sizeof(float), cudaMemcpyDeviceToHost));
+  SEI_CUDA(cudaMemcpy(pt.data(), c->d_pstrain, pt.size() * sizeof(float), cudaMemcpyDeviceToHost));
+  std::vector<float> ps = plastUntile(pt, n, 7, B);
   perm(ps, (size_t)7 * B);
-  SEI_CUDA(cudaMemcpy(c->d_pstrain, ps.data(), ps.size() * sizeof(float), cudaMemcpyHostToDevice));
+  pt = plastTile(ps, n, 7, B);
+  SEI_CUDA(cudaMemcpy(c->d_pstrain, pt.data(), pt.size() * sizeof(float), cudaMemcpyHostToDevice));
   return plastUpload(c, false);
 }
 }  // namespace
@@ -1543,7 +1562,7 @@ int sei_plasticity_setup(sei_ctx* c, const double* nodes, double tv, const doubl
   for (int a = 0; a < B; ++a)
     for (int b = 0; b < B; ++b) {
       mats[(size_t)a * Bp + b] = (float)v[(size_t)a * B + b];            // V[node][basis]
-      mats[(size_t)(B + a) * Bp + b] = (float)vi[(size_t)a * B + b];     // Vinv[basis][node]
+      mats[(size_t)(B + a) * Bp + b] = (float)vi[(size_t)b * B + a];     // Vinv transposed: [node][basis]
     }
   freePlasticity(c);
   c->pl_s0.swap(ps0);
@@ -1575,9 +1594,12 @@ int sei_plasticity_get_strain(sei_ctx* c, float* out) {
   if (rc) return rc;
   if (!out) return fail(c, SEI_ERR_ARG, "null output");
   if (!c->plast) return fail(c, SEI_ERR_STATE, "plasticity not set up (sei_plasticity_setup)");
+  const int B = sei::numBasis(c->cfg.order);
+  std::vector<float> pt((size_t)((c->n + 31) / 32) * 32 * 7 * B);
   SEI_CUDA(cudaStreamSynchronize(c->stream));
-  SEI_CUDA(cudaMemcpy(out, c->d_pstrain, (size_t)c->n * 7 * sei::numBasis(c->cfg.order) * sizeof(float),
-                      cudaMemcpyDeviceToHost));
+  SEI_CUDA(cudaMemcpy(pt.data(), c->d_pstrain, pt.size() * sizeof(float), cudaMemcpyDeviceToHost));
+  const std::vector<float> ps = plastUntile(pt, c->n, 7, B);
+  std::copy(ps.begin(), ps.end(), out);
   return SEI_OK;
 }
 

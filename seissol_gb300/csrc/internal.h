@@ -299,12 +299,13 @@ namespace sei {
 // of Plasticity.cpp:47-214 on cells [begin, end) after their neighbour integral.
 struct PlasticityArgs {
   float* Q;                   // DOFs [cells][9][Bp] (stresses: quantities 0..5)
-  const float* mats;          // V [B][Bp] (basis values at the nodes) then Vinv [B][Bp]
-  const float* s0;            // initial loading [cells][6][B]
-  const float* ccos;          // cohesion cos(phi) [cells][B]
-  const float* ssin;          // sin(phi) [cells][B]
+  const float* mats;          // V [B][Bp] (basis values at the nodes) then Vinv transposed [B][Bp]
+  // per-node arrays tiled by 32 cells: [cells / 32][K][B][32] (cell c: tile c / 32, lane c % 32)
+  const float* s0;            // initial loading, K = 6
+  const float* ccos;          // cohesion cos(phi), K = 1
+  const float* ssin;          // sin(phi), K = 1
   const float* mufac;         // 1 / (2 mu) [cells]
-  float* pstrain;             // plastic strain [cells][7][B] (six components, then eta)
+  float* pstrain;             // plastic strain, K = 7 (six components, then eta)
   unsigned long long* yield;  // cells with yielding, accumulated
   int64_t begin, end;
   float relax;     // r = 1 - exp(-dt / T_v)

@@ -6,7 +6,7 @@ app/Proxy/Bindings.cpp:14-60.  Unlike the reference proxy, the data are a real m
 (synthetic periodic cube) with physical operators, and the time step is the CFL step.
 
 CLI:  python -m seissol_gb300.proxy <cells> <timesteps> <kernel>[,kernel...] [--order N] [--format json]
-      [--precision fp32|f16x3] [--mechanisms 0|3]; the *_dr kernels run on a planar fault at orders
+      [--precision fp32|f16x3] [--mechanisms 0|3] [--plasticity]; the *_dr kernels run on a planar fault at orders
       4-6; --mechanisms 3 runs the viscoelastic equations (orders 4-5), as the reference's proxy
       built for them (Qp 100, Qs 50, central frequency 0.5 Hz, frequency ratio 100).
 """
@@ -36,6 +36,7 @@ class ProxyConfig:
     device: int = 0
     precision: int = 0  # SEI_PREC_FP32 / SEI_PREC_F16X3
     mechanisms: int = 0  # 0 elastic, 3 viscoelastic (27 quantities)
+    plasticity: bool = False  # off-fault plasticity on every cell (elastic, orders 4-6)
 
 
 @dataclasses.dataclass
@@ -146,6 +147,13 @@ def run_proxy(cfg: ProxyConfig) -> ProxyOutput:
             ctx.dr_setup(RSParams.fault_config())
         if cfg.mechanisms:
             ctx.visco_setup(100.0, 50.0, 0.5, 100.0)
+        if cfg.plasticity:
+            # bulk friction 0.6, c cos(phi) ~ U[0.7, 1.5] x 87 MPa, initial stress U[-1, 1] MPa,
+            # T_v 0.05 s, the library's default nodes
+            import numpy as np
+            rng = np.random.default_rng(1)
+            ctx.plasticity_setup(np.full(n, 0.6), rng.uniform(0.7, 1.5, n) * 8.7e7 / np.cos(np.arctan(0.6)),
+                                 rng.uniform(-1e6, 1e6, (n, 6)), tv=0.05)
         dt = ctx.cfl_timestep(0.5)
         for k in cfg.kernels:
             ctx.run(k, dt, 1)  # warm-up
@@ -241,12 +249,14 @@ def main(argv=None):
     ap.add_argument("--format", choices=("plain", "json"), default="plain")
     ap.add_argument("--precision", choices=("fp32", "f16x3"), default="fp32",
                     help="f16x3: the tensor-core path (split FP16 x3 contractions, FP32 accumulation)")
+    ap.add_argument("--plasticity", action="store_true", help="off-fault plasticity on every cell (elastic)")
     ap.add_argument("--mechanisms", type=int, choices=(0, 3), default=0,
                     help="3: viscoelastic equations with three relaxation mechanisms (orders 4 and 5)")
     a = ap.parse_args(argv)
     kernels = tuple(Aux.str_to_kernel(a.kernel))
     out = run_proxy(ProxyConfig(cells=a.cells, timesteps=a.timesteps, kernels=kernels, order=a.order,
-                                precision={"fp32": 0, "f16x3": 1}[a.precision], mechanisms=a.mechanisms))
+                                precision={"fp32": 0, "f16x3": 1}[a.precision], mechanisms=a.mechanisms,
+                                plasticity=a.plasticity))
     write_output(out, a.kernel, a.format)
     return 0
 
