@@ -1562,7 +1562,7 @@ int sei_plasticity_setup(sei_ctx* c, const double* nodes, double tv, const doubl
   for (int a = 0; a < B; ++a)
     for (int b = 0; b < B; ++b) {
       mats[(size_t)a * Bp + b] = (float)v[(size_t)a * B + b];            // V[node][basis]
-      mats[(size_t)(B + a) * Bp + b] = (float)vi[(size_t)b * B + a];     // Vinv transposed: [node][basis]
+      mats[(size_t)(B + a) * Bp + b] = (float)vi[(size_t)a * B + b];     // Vinv[basis][node]
     }
   freePlasticity(c);
   c->pl_s0.swap(ps0);

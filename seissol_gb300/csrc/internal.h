@@ -299,7 +299,7 @@ namespace sei {
 // of Plasticity.cpp:47-214 on cells [begin, end) after their neighbour integral.
 struct PlasticityArgs {
   float* Q;                   // DOFs [cells][9][Bp] (stresses: quantities 0..5)
-  const float* mats;          // V [B][Bp] (basis values at the nodes) then Vinv transposed [B][Bp]
+  const float* mats;          // V [B][Bp] (basis values at the nodes) then Vinv [B][Bp]
   // per-node arrays tiled by 32 cells: [cells / 32][K][B][32] (cell c: tile c / 32, lane c % 32)
   const float* s0;            // initial loading, K = 6
   const float* ccos;          // cohesion cos(phi), K = 1

@@ -17,32 +17,22 @@ constexpr int kPlCells = 32;  // cells per CTA; thread (stress component q < 6, 
 
 // A CTA of 192 threads: V and Vinv staged in shared memory (rows padded to Bp floats, read as
 // broadcast float4); the nodal stresses of 32 cells S [6][B][32] exchanged between the column
-// threads (q, lane) and the node threads (nodes q, q + 6, ... of cell lane).  The block's initial
-// loading is copied into S at the start (68 KB of shared memory at order 6: three CTAs per SM).
+// threads (q, lane) and the node threads (nodes q, q + 6, ... of cell lane).
 template <int B>
 __global__ void __launch_bounds__(6 * kPlCells) sei_plasticity(PlasticityArgs a) {
   constexpr int Bp = (B + 3) / 4 * 4;
   extern __shared__ float4 sm4[];
   float* V = reinterpret_cast<float*>(sm4);  // [B][Bp]
-  float* ViT = V + B * Bp;                    // [B][Bp]: ViT[n][k] = Vinv[k][n]
-  float* S = ViT + B * Bp;                    // [6][B][32]
+  float* Vi = V + B * Bp;                     // [B][Bp]
+  float* S = Vi + B * Bp;                     // [6][B][32]
   __shared__ int adjust[kPlCells];
-  __shared__ int ylist[kPlCells];
-  __shared__ int ycount;
   const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t first = a.begin + (int64_t)blockIdx.x * kPlCells;
   {
     const float4* src = reinterpret_cast<const float4*>(a.mats);
     for (int i = threadIdx.x; i < 2 * B * Bp / 4; i += blockDim.x) sm4[i] = src[i];
-    // per-node arrays are tiled [cell / 32][K][B][32]: a block's cells are one run per row when
-    // the block starts on a tile, two runs otherwise
-    for (int i = threadIdx.x; i < 6 * B * kPlCells; i += blockDim.x) {
-      const int64_t c = min(first + (i & 31), a.end - 1);
-      S[i] = __ldg(a.s0 + ((size_t)(c >> 5) * 6 * B + (i >> 5)) * 32 + (c & 31));
-    }
   }
   if (threadIdx.x < kPlCells) adjust[threadIdx.x] = 0;
-  const int64_t cell = first + lane;
+  const int64_t cell = a.begin + (int64_t)blockIdx.x * kPlCells + lane;
   const bool valid = cell < a.end;
   const int64_t cl = valid ? cell : a.end - 1;
   float col[Bp];
@@ -50,13 +40,15 @@ __global__ void __launch_bounds__(6 * kPlCells) sei_plasticity(PlasticityArgs a)
   __syncthreads();
 
   // nodal stresses plus the initial loading: S[q][n] = sum_k V[n][k] Q[q][k] + s0[q][n]
+  // per-node arrays are tiled [cell / 32][K][B][32]: a warp's cells read one node as one run
   const size_t tile = (size_t)(cl >> 5), tl = (size_t)(cl & 31);
+  const float* s0 = a.s0 + (tile * 6 + q) * B * 32 + tl;
   float* Sq = S + q * B * kPlCells + lane;
 #pragma unroll
   for (int n0 = 0; n0 < B; n0 += 4) {
     float acc[4];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[j] = (n0 + j < B) ? Sq[(n0 + j) * kPlCells] : 0.f;
+    for (int j = 0; j < 4; ++j) acc[j] = (n0 + j < B) ? __ldg(s0 + (n0 + j) * 32) : 0.f;
 #pragma unroll
     for (int k = 0; k < Bp; k += 4) {
 #pragma unroll
@@ -114,28 +106,26 @@ __global__ void __launch_bounds__(6 * kPlCells) sei_plasticity(PlasticityArgs a)
   if (any) adjust[lane] = 1;
   __syncthreads();
 
-  // modal update of the yielding cells only, Q[q][k] += sum_n Vinv[k][n] S[q][n]: the block's
-  // threads share the (yielding cell, q, k) items, so a few yielding cells do not hold every warp
-  if (threadIdx.x < kPlCells) {
-    const bool y = adjust[threadIdx.x] != 0;
-    const unsigned m = __ballot_sync(0xffffffffu, y);
-    if (y) ylist[__popc(m & ((1u << threadIdx.x) - 1u))] = threadIdx.x;
-    if (threadIdx.x == 0) {
-      ycount = __popc(m);
-      if (m) atomicAdd(a.yield, (unsigned long long)__popc(m));
+  // modal update of the yielding cells: Q[q][k] += sum_n Vinv[k][n] S[q][n]
+  if (!valid || !adjust[lane]) return;
+  float u[Bp];
+#pragma unroll
+  for (int n = 0; n < Bp; ++n) u[n] = n < B ? Sq[n * kPlCells] : 0.f;
+#pragma unroll
+  for (int k = 0; k < B; ++k) {
+    float acc = col[k];
+#pragma unroll
+    for (int n = 0; n < Bp; n += 4) {
+      const float4 v = *reinterpret_cast<const float4*>(Vi + k * Bp + n);
+      acc = fmaf(v.x, u[n], acc);
+      acc = fmaf(v.y, u[n + 1], acc);
+      acc = fmaf(v.z, u[n + 2], acc);
+      acc = fmaf(v.w, u[n + 3], acc);
     }
+    col[k] = acc;
   }
-  __syncthreads();
-  const int items = ycount * 6 * B;
-  for (int w = threadIdx.x; w < items; w += blockDim.x) {
-    const int ci = w / (6 * B), rem = w - ci * 6 * B, qq = rem / B, k = rem - qq * B;
-    const int l = ylist[ci];
-    const float* Sn = S + qq * B * kPlCells + l;
-    float acc = 0.f;
-#pragma unroll 8
-    for (int n = 0; n < B; ++n) acc = fmaf(ViT[n * Bp + k], Sn[n * kPlCells], acc);
-    a.Q[((size_t)(first + l) * 9 + qq) * Bp + k] += acc;
-  }
+  sei_store_col<Bp>(a.Q + ((size_t)cell * 9 + q) * Bp, col);
+  if (q == 0) atomicAdd(a.yield, 1ull);
 }
 
 template <int B>
@@ -143,10 +133,6 @@ int launchB(const PlasticityArgs& a, cudaStream_t s) {
   constexpr int Bp = (B + 3) / 4 * 4;
   const size_t smem = sizeof(float) * (2 * B * Bp + 6 * B * kPlCells);
   if (cudaFuncSetAttribute(sei_plasticity<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return -1;
-  // the whole unified L1 as shared memory: three 68 KB CTAs per SM at order 6
-  if (cudaFuncSetAttribute(sei_plasticity<B>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                           (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
     return -1;
   const int64_t n = a.end - a.begin;
   const int64_t blocks = (n + kPlCells - 1) / kPlCells;
